@@ -1,0 +1,148 @@
+/*
+ * cpals.h -- C ABI of the GB300 CP-ALS engine (libcpals.so).
+ *
+ * This is the drop-in boundary for ITensorCPD.jl's normal-equation ALS path.
+ * Julia binds it with `ccall`, the way ITensorCPD binds its one native helper
+ * (src/algebra/SEQRCS.jl:41-60, library located in src/ITensorCPD.jl:25-36).
+ * Python binds it with ctypes.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: CPALS_OK (0) or a negative code.
+ *    No entry point aborts or traps.
+ *  - Tensors and matrices crossing the boundary are column-major (first index
+ *    fastest), as ITensor Dense storage and Julia Arrays are.
+ *    A factor F_n is I_n x R, an MTTKRP M_n is I_n x R, a Gram is R x R.
+ *  - Modes are 0-based here; the Julia shim passes `fact - 1`.
+ *    Sample indices (pivots) are 1-based Int64, as Julia stores them
+ *    (src/math_tools/probability.jl:25).
+ *  - Host pointers: the library copies in and out; it owns every device buffer
+ *    of a handle.  The one exception, cpals_set_tensor_device, borrows a device
+ *    buffer, which must outlive its use.
+ *  - One CUDA stream per handle.  A handle must not be used from two threads
+ *    at once.
+ */
+#ifndef CPALS_H
+#define CPALS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define CPALS_OK 0
+#define CPALS_E_ARG (-1)         /* bad argument: sizes, mode, index out of range, null pointer */
+#define CPALS_E_CUDA (-2)        /* a CUDA runtime call failed */
+#define CPALS_E_NAN (-3)         /* the fit became NaN: fit_check.jl:40-42 throws "Error NAN" */
+#define CPALS_E_STATE (-4)       /* call out of order, e.g. a sweep before the tensor is set */
+#define CPALS_E_UNSUPPORTED (-5) /* shape or option this build does not handle */
+#define CPALS_E_DEVICE (-6)      /* a kernel reported an error status (bounded wait expired, bad index) */
+
+/* ---- tensor element types ---- */
+#define CPALS_DTYPE_F64 0
+#define CPALS_DTYPE_F32 1
+
+/* ---- MTTKRP arithmetic ---- */
+#define CPALS_MTTKRP_FP64 0   /* plain FP64 on CUDA cores: the parity / comparator path */
+#define CPALS_MTTKRP_BF16X3 1 /* tcgen05 split-BF16 (hi*hi + hi*lo + lo*hi), FP32 accumulate */
+
+/* ---- create flags ---- */
+#define CPALS_FLAG_NO_GRAPH 1 /* launch sweeps kernel by kernel instead of replaying a CUDA graph */
+#define CPALS_FLAG_DIMTREE 2  /* dimension-tree MTTKRP (order >= 3): two passes over T per sweep */
+
+/* ---- convergence checks ---- */
+#define CPALS_CHECK_NONE 0 /* NoCheck, src/converge_checks/no_check.jl:1-20 */
+#define CPALS_CHECK_FIT 1  /* FitCheck, src/converge_checks/fit_check.jl:5-68 */
+
+#define CPALS_MAX_ORDER 8
+
+typedef struct cpals_ctx cpals_ctx;
+
+/* Mirror of the mutable FitCheck / NoCheck structs (fit_check.jl:5-20, no_check.jl:1-9).
+ * cpals_optimize reads it on entry and writes the updated fields back, so a
+ * check object can be reused across calls as in the reference. */
+typedef struct cpals_check {
+  int32_t kind;        /* CPALS_CHECK_NONE or CPALS_CHECK_FIT */
+  int32_t iter;        /* in/out */
+  int32_t counter;     /* in/out (FitCheck) */
+  int32_t max_counter; /* sweeps allowed */
+  double tolerance;    /* FitCheck tol on |delta fit| */
+  double ref_norm;     /* FitCheck norm(T) */
+  double lastfit;      /* in/out; a new FitCheck starts at 1 */
+  double final_fit;    /* out */
+  int32_t total_iter;  /* out */
+  int32_t sweeps_run;  /* out: sweeps executed by this call */
+} cpals_check;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int cpals_version(void);
+/* Static message for a status code. */
+const char* cpals_status_string(int status);
+
+/* Create a handle for an order-`order` tensor of extents dims[0..order-1] and CP
+ * rank `rank` on CUDA device `device`.  Replaces the state that compute_als builds
+ * (src/optimizers/als_optimizers/als_optimizer.jl:37-55,
+ *  optimizers/als_optimizers/standard/tensor.jl:3-14). */
+int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, int64_t rank,
+                 int tensor_dtype, int mttkrp_mode, int flags);
+int cpals_destroy(cpals_ctx* ctx);
+
+/* Copy the column-major target tensor in (the ALS `target`, als_optimizer.jl:5-10). */
+int cpals_set_tensor(cpals_ctx* ctx, const void* host_tensor);
+/* Use a column-major tensor already resident on the handle's device (borrowed). */
+int cpals_set_tensor_device(cpals_ctx* ctx, const void* device_tensor);
+
+/* Copy factors (each I_n x R column-major) and lambda (R) in / out.  Setting
+ * factors also recomputes the Grams, as compute_als does
+ * (optimizers/als_optimizers/standard/tensor.jl:3-14). */
+int cpals_set_factors(cpals_ctx* ctx, const double* const* host_factors, const double* host_lambda);
+int cpals_get_factors(cpals_ctx* ctx, double* const* host_factors, double* host_lambda);
+/* Gram G_n = F_n^T F_n (R x R) of the current factors. */
+int cpals_get_gram(cpals_ctx* ctx, int mode, double* host_gram);
+
+/* MTTKRP of `mode` with the current factors: M_n = T_(n) (KRP of the other factors),
+ * I_n x R column-major.  Replaces matricize_tensor(::KRPFreeNormal / ::KRPNormal)
+ * (src/algorithms/als_algorithms/standard/tensor.jl:52-84). */
+int cpals_mttkrp(cpals_ctx* ctx, int mode, double* host_out);
+
+/* Run ALS sweeps with the given check: the loop of optimize
+ * (src/optimizers/als_optimizers/optimize.jl:6-35) with compute_krp, solve_ls_problem,
+ * row_norm, post_solve and check_converge on the device.  `fit_trajectory`
+ * (may be NULL) receives one fit per sweep run, up to `traj_capacity` entries.
+ * Returns CPALS_E_NAN if the fit became NaN. */
+int cpals_optimize(cpals_ctx* ctx, cpals_check* check, double* fit_trajectory, int64_t traj_capacity);
+
+/* Number of normal-equation solves so far that took the pivoted-QR fallback
+ * because the pivoted Cholesky was rank deficient (ldiv_solve.jl:17-22). */
+int cpals_fallback_count(cpals_ctx* ctx, int64_t* count);
+
+/* Synchronise the handle's stream (for timing). */
+int cpals_synchronize(cpals_ctx* ctx);
+
+/* ---- randomized leverage-score path (LevScoreSampled) ---- */
+
+/* Sampled Khatri-Rao rows: out(s, r) = prod_{m != mode, in mode order} F_m(pivots(s, j_m), r),
+ * multiplied left to right from 1 as pivot_hadamard does (src/algebra/had_contract.jl:277-295).
+ * pivots: nsamps x (order-1) column-major, 1-based.  out: nsamps x R column-major FP64. */
+int cpals_pivot_hadamard(cpals_ctx* ctx, int mode, const int64_t* pivots, int64_t nsamps, double* host_out);
+
+/* Sampled fibres of the tensor: out(i, s) = T(p_1, .., i at `mode`, .., p_{N-1}),
+ * as fused_flatten_sample (src/algebra/pivot_mapping.jl:59-85).
+ * out: I_mode x nsamps column-major, in the tensor's element type. */
+int cpals_fused_flatten_sample(cpals_ctx* ctx, int mode, const int64_t* pivots, int64_t nsamps, void* host_out);
+
+/* Leverage-score probabilities of factor `mode` (I_mode values):
+ * compute_leverage_score_probabilitiy (src/math_tools/probability.jl:3-10). */
+int cpals_leverage_scores(cpals_ctx* ctx, int mode, double* host_probs);
+
+/* One LevScoreSampled mode update with host-drawn pivots: sampled KRP gather,
+ * sampled fibre gather, solve_ls_problem(::ProjectionAlgorithm) (normal != 0:
+ * (S^T S) X = (T_s S)^T; else the tall least-squares problem), row_norm
+ * (randomized/ProjectionAlgorithm.jl:57-68, randomized/krp_lev_score_sampled.jl:87-125). */
+int cpals_sampled_update(cpals_ctx* ctx, int mode, const int64_t* pivots, int64_t nsamps, int normal);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPALS_H */

@@ -1,0 +1,34 @@
+"""GB300-native CP-ALS engine with ITensorCPD.jl's API.
+
+The compute path is libcpals.so (hand-written CUDA for sm_103a, C ABI in
+include/cpals.h); this package is the host side that mirrors the reference's
+``decompose`` / ``random_CPD`` / ``als_optimize`` / ``FitCheck`` / ``CPD`` interface.
+"""
+from ._lib import CpalsError, load
+from .api import (
+    CPD,
+    CPDFit,
+    ConvergeAlg,
+    FitCheck,
+    GB300Normal,
+    KRPFreeNormal,
+    KRPNormal,
+    LevScoreSampled,
+    MttkrpAlgorithm,
+    NoCheck,
+    ProjectionAlgorithm,
+    als_optimize,
+    cp_rank,
+    decompose,
+    increase_cpd_rank,
+    random_CPD,
+    random_factors,
+    sample_factor_matrices,
+)
+from .engine import Engine
+
+__all__ = [
+    "CPD", "CPDFit", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
+    "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
+    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices",
+]

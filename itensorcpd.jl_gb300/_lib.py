@@ -1,0 +1,116 @@
+"""ctypes binding of libcpals.so (the C ABI declared in include/cpals.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libcpals.so"
+
+CPALS_OK = 0
+CPALS_E_ARG = -1
+CPALS_E_CUDA = -2
+CPALS_E_NAN = -3
+CPALS_E_STATE = -4
+CPALS_E_UNSUPPORTED = -5
+CPALS_E_DEVICE = -6
+
+DTYPE_F64 = 0
+DTYPE_F32 = 1
+MTTKRP_FP64 = 0
+MTTKRP_BF16X3 = 1
+FLAG_NO_GRAPH = 1
+FLAG_DIMTREE = 2
+CHECK_NONE = 0
+CHECK_FIT = 1
+
+
+class CpalsCheck(C.Structure):
+    """Mirror of ``cpals_check`` (include/cpals.h)."""
+
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("iter", C.c_int32),
+        ("counter", C.c_int32),
+        ("max_counter", C.c_int32),
+        ("tolerance", C.c_double),
+        ("ref_norm", C.c_double),
+        ("lastfit", C.c_double),
+        ("final_fit", C.c_double),
+        ("total_iter", C.c_int32),
+        ("sweeps_run", C.c_int32),
+    ]
+
+
+# name -> (restype, argtypes); every exported entry point of include/cpals.h
+_P = C.c_void_p
+_I64P = C.POINTER(C.c_int64)
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "cpals_version": (C.c_int, []),
+    "cpals_status_string": (C.c_char_p, [C.c_int]),
+    "cpals_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, _I64P, C.c_int64, C.c_int, C.c_int, C.c_int]),
+    "cpals_destroy": (C.c_int, [_P]),
+    "cpals_set_tensor": (C.c_int, [_P, _P]),
+    "cpals_set_tensor_device": (C.c_int, [_P, _P]),
+    "cpals_set_factors": (C.c_int, [_P, C.POINTER(_DP), _DP]),
+    "cpals_get_factors": (C.c_int, [_P, C.POINTER(_DP), _DP]),
+    "cpals_get_gram": (C.c_int, [_P, C.c_int, _DP]),
+    "cpals_mttkrp": (C.c_int, [_P, C.c_int, _DP]),
+    "cpals_optimize": (C.c_int, [_P, C.POINTER(CpalsCheck), _DP, C.c_int64]),
+    "cpals_fallback_count": (C.c_int, [_P, _I64P]),
+    "cpals_synchronize": (C.c_int, [_P]),
+    "cpals_pivot_hadamard": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _DP]),
+    "cpals_fused_flatten_sample": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _P]),
+    "cpals_leverage_scores": (C.c_int, [_P, C.c_int, _DP]),
+    "cpals_sampled_update": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, C.c_int]),
+}
+
+_lib = None
+
+
+class CpalsError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} (status {status})")
+
+
+def load(path: Path | None = None):
+    """Load libcpals.so.  Raises if the library has not been built: there is no CPU fallback."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"libcpals.so not found at {p}; build it first (python -c 'import __graft_entry__ as g; g.build()')"
+        )
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().cpals_status_string(status).decode()
+    except Exception:  # library missing: still give a readable message
+        return "unknown"
+
+
+def check(status: int, what: str):
+    if status != CPALS_OK:
+        raise CpalsError(status, what)
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def i64ptr(a: np.ndarray):
+    return a.ctypes.data_as(_I64P)

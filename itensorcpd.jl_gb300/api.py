@@ -1,0 +1,332 @@
+"""User-facing API with the names and argument meaning of ITensorCPD.jl.
+
+``decompose``, ``random_CPD``, ``als_optimize``, ``FitCheck``, ``NoCheck``, ``CPDFit``,
+``CPD`` and the algorithm structs behave as in the reference; every sweep runs on the
+GPU through libcpals (there is no CPU path).  Arrays are numpy arrays indexed like the
+reference's (first index fastest in memory is handled by the binding).
+"""
+from __future__ import annotations
+
+import warnings
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from .engine import Engine
+
+
+# ---------------------------------------------------------------------------
+# CPD container (src/cpd.jl:7-46)
+# ---------------------------------------------------------------------------
+class CPD:
+    """Factors F_n (I_n x R) and weights lambda (R), as ``CPD{TargetT}`` (cpd.jl:7-18)."""
+
+    def __init__(self, factors, lam, inds=None):
+        self.factors = [np.asarray(F) for F in factors]
+        self.lam = np.asarray(lam)
+        self.inds = tuple(inds) if inds is not None else tuple(F.shape[0] for F in self.factors)
+
+    @property
+    def λ(self):  # noqa: N802 - the reference's field name
+        return self.lam
+
+    def __getitem__(self, i):
+        return self.factors[i]
+
+    def __len__(self):
+        return len(self.factors)
+
+    def __iter__(self):
+        return iter(self.factors)
+
+    @property
+    def ndims(self):
+        return len(self.factors)
+
+    def copy(self):
+        return CPD([F.copy() for F in self.factors], self.lam.copy(), self.inds)
+
+    def __eq__(self, other):
+        return (
+            isinstance(other, CPD)
+            and len(self) == len(other)
+            and all(np.array_equal(a, b) for a, b in zip(self.factors, other.factors))
+            and np.array_equal(self.lam, other.lam)
+        )
+
+    @property
+    def dtype(self):
+        return self.lam.dtype
+
+
+def cp_rank(cp: CPD) -> int:
+    """cpd.jl:29: dimension of the CP rank index."""
+    return int(cp.lam.shape[0])
+
+
+# ---------------------------------------------------------------------------
+# Convergence checks (src/converge_checks/)
+# ---------------------------------------------------------------------------
+class ConvergeAlg:
+    pass
+
+
+@dataclass
+class FitCheck(ConvergeAlg):
+    """fit_check.jl:5-20: stop when |delta fit| < tolerance on two consecutive sweeps."""
+
+    tolerance: float
+    max_counter: int
+    ref_norm: float
+    iter: int = 0
+    counter: int = 0
+    lastfit: float = 1.0
+    final_fit: float = 0.0
+    total_iter: int = 0
+    trajectory: list = field(default_factory=list)
+
+
+@dataclass
+class NoCheck(ConvergeAlg):
+    """no_check.jl:1-9: run ``max_counter`` sweeps."""
+
+    max_counter: int
+    iter: int = 0
+    lastfit: float = -1.0
+
+
+def CPDFit(check: FitCheck) -> float:  # noqa: N802 - reference name
+    """fit_check.jl:68."""
+    return check.final_fit
+
+
+# ---------------------------------------------------------------------------
+# ALS algorithms (src/algorithms/als_algorithms/)
+# ---------------------------------------------------------------------------
+class MttkrpAlgorithm:
+    precision = "fp64"
+    dimtree = False
+
+
+class KRPFreeNormal(MttkrpAlgorithm):
+    """Normal-equation ALS, the reference default (standard/tensor.jl:70-89); FP64 MTTKRP on the GPU."""
+
+
+class KRPNormal(MttkrpAlgorithm):
+    """Normal-equation ALS with an explicit KRP in the reference (standard/tensor.jl:50-65).
+    On the GPU the KRP is never materialised; the arithmetic is the same FP64 MTTKRP."""
+
+
+class GB300Normal(MttkrpAlgorithm):
+    """Normal-equation ALS with the tcgen05 split-BF16 MTTKRP (FP32 accumulate) and the
+    FP64 Gram / Cholesky / fit of the other algorithms.  ``dimtree`` reuses partial
+    contractions across modes."""
+
+    def __init__(self, precision: str = "bf16x3", dimtree: bool = False):
+        self.precision = precision
+        self.dimtree = dimtree
+
+
+class ProjectionAlgorithm:
+    pass
+
+
+class LevScoreSampled(ProjectionAlgorithm):
+    """randomized/krp_lev_score_sampled.jl:9-14: leverage-score sampled ALS with
+    ``NSamples`` KRP rows per mode solve (an int or a per-mode tuple)."""
+
+    def __init__(self, n=1):
+        self.NSamples = tuple(n) if isinstance(n, (tuple, list)) else (int(n),)
+
+    def nsamples(self, mode: int) -> int:
+        return self.NSamples[0] if len(self.NSamples) == 1 else self.NSamples[mode]
+
+
+# ---------------------------------------------------------------------------
+# Initial guesses (src/cpd.jl:85-119)
+# ---------------------------------------------------------------------------
+def _row_norm_host(X):
+    lam = np.sqrt(np.sum(X * X, axis=0))
+    return X / lam[None, :], lam
+
+
+def random_factors(dims, rank, rng=None, dtype=np.float64):
+    """cpd.jl:85-97: iid N(0,1) I_n x R factors (column-major draw order), each
+    column-normalised; lambda is that of the last factor.  ``rng`` defaults to a
+    generator seeded with 3, as the reference defaults to MersenneTwister(3)."""
+    rng = np.random.default_rng(3) if rng is None else rng
+    factors, lam = [], None
+    for d in dims:
+        X = rng.standard_normal(rank * d).reshape(rank, d).T.astype(dtype)
+        F, lam = _row_norm_host(X)
+        factors.append(F)
+    return factors, lam
+
+
+def random_CPD(target, rank, rng=None) -> CPD:  # noqa: N802 - reference name
+    """cpd.jl:100-119."""
+    T = np.asarray(target)
+    factors, lam = random_factors(T.shape, int(rank), rng, dtype=T.dtype if T.dtype in (np.float32, np.float64)
+                                  else np.float64)
+    return CPD(factors, lam, T.shape)
+
+
+def increase_cpd_rank(cpd: CPD, new_rank: int, rng=None) -> CPD:
+    """decompose.jl:71-83: new random factors whose first columns are the old ones."""
+    old = cp_rank(cpd)
+    if new_rank < old:
+        raise ValueError("new rank must be >= the old rank")
+    factors, lam = random_factors(cpd.inds, new_rank, rng, dtype=cpd.dtype)
+    for old_f, new_f in zip(cpd.factors, factors):
+        new_f[:, :old] = old_f
+    return CPD(factors, lam, cpd.inds)
+
+
+# ---------------------------------------------------------------------------
+# ALS drivers (src/optimizers/)
+# ---------------------------------------------------------------------------
+def _to_device_check(check) -> L.CpalsCheck:
+    c = L.CpalsCheck()
+    if isinstance(check, FitCheck):
+        c.kind = L.CHECK_FIT
+        c.iter = int(check.iter)
+        c.counter = int(check.counter)
+        c.max_counter = int(check.max_counter)
+        c.tolerance = float(check.tolerance)
+        c.ref_norm = float(check.ref_norm)
+        c.lastfit = float(check.lastfit)
+        c.final_fit = float(check.final_fit)
+        c.total_iter = int(check.total_iter)
+    elif isinstance(check, NoCheck):
+        c.kind = L.CHECK_NONE
+        c.iter = int(check.iter)
+        c.max_counter = int(check.max_counter)
+        c.lastfit = float(check.lastfit)
+    else:
+        raise NotImplementedError(f"{type(check).__name__} is not supported by the GPU engine (FitCheck, NoCheck)")
+    return c
+
+
+def _from_device_check(check, c: L.CpalsCheck, traj, rank, verbose):
+    it0 = check.iter
+    prev = check.lastfit
+    if isinstance(check, FitCheck):
+        check.iter = c.iter
+        check.counter = c.counter
+        check.lastfit = c.lastfit
+        check.final_fit = c.final_fit
+        check.total_iter = c.total_iter
+        check.trajectory.extend(float(x) for x in traj)
+        if verbose:
+            for k, f in enumerate(traj, start=1):
+                print(f"{rank}\t {it0 + k} \t {f} \t {abs(prev - f)}")
+                prev = f
+    else:
+        check.iter = c.iter
+        if verbose:
+            for k in range(len(traj)):
+                print(f"{rank}\t {it0 + k + 1}")
+
+
+def _prepare_target(target):
+    T = np.asarray(target)
+    if T.dtype not in (np.float32, np.float64):
+        if np.iscomplexobj(T):
+            raise TypeError("complex tensors are not supported by the GPU engine")
+        T = T.astype(np.float64)
+    return T
+
+
+def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=False, device=0, rng=None,
+                 normal=False, **kwargs) -> CPD:
+    """als_optimizer.jl:15-25 / 37-55: default alg KRPFreeNormal, default check NoCheck(maxiter or 100)."""
+    T = _prepare_target(target)
+    alg = KRPFreeNormal() if alg is None else alg
+    check = NoCheck(100 if maxiter is None else maxiter) if check is None else check
+    R = cp_rank(cp)
+    if isinstance(alg, ProjectionAlgorithm):
+        return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal)
+    with Engine(T.shape, R, dtype=T.dtype, precision=alg.precision, device=device, dimtree=alg.dimtree) as eng:
+        eng.set_tensor(T)
+        eng.set_factors(cp.factors, cp.lam)
+        c = _to_device_check(check)
+        traj = eng.optimize(c)
+        factors, lam = eng.get_factors()
+    _from_device_check(check, c, traj, R, verbose)
+    if T.dtype == np.float32:
+        factors = [F.astype(np.float32) for F in factors]
+        lam = lam.astype(np.float32)
+    return CPD(factors, lam, T.shape)
+
+
+def sample_factor_matrices(nsamps, skip, probs, rng):
+    """probability.jl:23-33: independent weighted draws (1-based) for every mode but ``skip``.
+    Index drawing stays on the host; the device gathers are bit-exact for these indices."""
+    cols = []
+    for m, p in enumerate(probs):
+        if m == skip:
+            continue
+        w = np.abs(p)
+        cols.append(rng.choice(len(p), size=nsamps, p=w / w.sum()) + 1)
+    return np.asfortranarray(np.stack(cols, axis=1).astype(np.int64))
+
+
+def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal):
+    """LevScoreSampled: compute_als (optimizers/.../krp_lev_score_sampled.jl:1-40) and the
+    per-mode project_krp / matricize_tensor / solve / post_solve of
+    algorithms/.../randomized/krp_lev_score_sampled.jl:87-125, resampling every mode."""
+    rng = np.random.default_rng(3) if rng is None else rng
+    R = cp_rank(cp)
+    N = T.ndim
+    if isinstance(check, FitCheck) and check.iter == 0:
+        # ProjectionAlgorithm.jl:30-36: a FitCheck is not honoured by sampled solvers
+        print(f"Warning: FitCheck is not enabled for {type(alg).__name__} will run {check.max_counter} iterations.")
+    sweeps = max(0, int(check.max_counter) - int(check.iter))
+    with Engine(T.shape, R, dtype=T.dtype, precision="fp64", device=device) as eng:
+        eng.set_tensor(T)
+        eng.set_factors(cp.factors, cp.lam)
+        probs = [eng.leverage_scores(n) for n in range(N)]
+        for s in range(sweeps):
+            for n in range(N):
+                piv = sample_factor_matrices(alg.nsamples(n), n, probs, rng)
+                eng.sampled_update(n, piv, normal=normal)
+                probs[n] = eng.leverage_scores(n)
+            if verbose:
+                print(f"{R}\t{s + 1}")
+        factors, lam = eng.get_factors()
+    check.iter = 0
+    if T.dtype == np.float32:
+        factors = [F.astype(np.float32) for F in factors]
+        lam = lam.astype(np.float32)
+    return CPD(factors, lam, T.shape)
+
+
+def decompose(A, rank, max_rank=None, *, solver=None, rng=None, alg=None, check=None, maxiter=None, verbose=False,
+              start_rank=1, rank_step=1, **kwargs) -> CPD:
+    """decompose.jl:1-30 (``decompose(A, rank)``) and, with ``max_rank``, the rank-adaptive
+    ``decompose(A, epsilon, max_rank)`` of decompose.jl:32-69 (``rank`` is then epsilon)."""
+    if solver is not None:
+        raise TypeError("OptimizerError: only the ALS solver is available")
+    T = _prepare_target(A)
+    if max_rank is None:
+        cp = random_CPD(T, int(rank), rng)
+        return als_optimize(T, cp, alg=alg, check=check, maxiter=maxiter, verbose=verbose, rng=rng, **kwargs)
+    epsilon = float(rank)
+    if verbose:
+        print(f"Starting with rank: {start_rank}")
+    current = int(start_rank)
+    cpd = random_CPD(T, current, rng)
+    check = FitCheck(1e-3, 100, float(np.linalg.norm(T))) if check is None else check
+    while True:
+        cpd = als_optimize(T, cpd, alg=alg, check=check, maxiter=maxiter, verbose=verbose, rng=rng, **kwargs)
+        check.iter = 0
+        if 1.0 - CPDFit(check) < epsilon:
+            return cpd
+        current += int(rank_step)
+        if verbose:
+            print(f"\nIncreasing rank to: {current}")
+        if current > int(max_rank):
+            print(f"Optimization Failed to converge within rank {max_rank}")
+            return cpd
+        cpd = increase_cpd_rank(cpd, current, rng)

@@ -1,0 +1,686 @@
+// C ABI of libcpals: handle state, the per-sweep launch sequence, CUDA-graph replay
+// and the device-side FitCheck loop.  The steps follow optimize()
+// (src/optimizers/als_optimizers/optimize.jl:6-35):
+//   per mode n: compute_krp (Hadamard of Grams) -> matricize_tensor (MTTKRP) ->
+//   solve_ls_problem -> row_norm -> post_solve (Gram); after the last mode check_converge.
+// The O(R^3) factorisation of mode n depends only on the Grams, so it runs on a side
+// stream concurrently with the MTTKRP of mode n; events fork and join the streams, and
+// a whole sweep is captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "cpals_internal.cuh"
+#include "cpals_tc.cuh"
+
+using namespace cpals;
+
+struct cpals_ctx {
+  int device = 0, order = 0, tdtype = 0, mmode = 0, flags = 0, num_sms = 0;
+  int64_t R = 0;
+  int64_t dims[kMaxOrder] = {};
+  int64_t numel = 0, maxI = 0;
+  cudaStream_t st = nullptr, side = nullptr;
+  cudaEvent_t ev_main[kMaxOrder] = {}, ev_side[kMaxOrder] = {};
+  const void* dT = nullptr;
+  void* dT_owned = nullptr;
+  bool T_set = false, F_set = false;
+  double* F[kMaxOrder] = {};
+  float* F32t[kMaxOrder] = {};
+  int64_t ld32[kMaxOrder] = {};
+  double* G[kMaxOrder] = {};
+  double* lam = nullptr;
+  double* X = nullptr;
+  double* Graw = nullptr;
+  void* part = nullptr;
+  int part_f32 = 0;
+  int splits[kMaxOrder] = {};
+  int64_t cps[kMaxOrder] = {};
+  ModeGeom geom[kMaxOrder];
+  double* work = nullptr;
+  double* U = nullptr;
+  int* piv = nullptr;
+  double* W = nullptr;
+  SolveInfo* info = nullptr;
+  double* gpart = nullptr;
+  unsigned* gcnt = nullptr;
+  int gS2[kMaxOrder] = {};
+  double* inner_rows = nullptr;
+  DevCheck* chk = nullptr;
+  DevCheck* hchk = nullptr;  // pinned mirror
+  double* traj = nullptr;
+  int64_t traj_cap = 0;
+  cudaGraphExec_t graph = nullptr;
+  // randomized path
+  int64_t* dpiv = nullptr;
+  int64_t piv_cap = 0;
+  double* Scol = nullptr;
+  double* Srow = nullptr;
+  void* Ts = nullptr;
+  double* Spart = nullptr;
+  size_t spart_cap = 0;
+  int64_t samp_cap = 0;
+  int* derr = nullptr;
+  // tensor-core path
+  TcState* tc = nullptr;
+};
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+FactorSet factor_set(const cpals_ctx* c) {
+  FactorSet fs{};
+  for (int m = 0; m < c->order; ++m) fs.F[m] = c->F[m];
+  return fs;
+}
+GramSet gram_set(const cpals_ctx* c) {
+  GramSet gs{};
+  for (int m = 0; m < c->order; ++m) gs.G[m] = c->G[m];
+  return gs;
+}
+
+template <typename T>
+int dmalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    fprintf(stderr, "libcpals: cudaMalloc(%zu bytes) failed: %s\n", count * sizeof(T), cudaGetErrorString(e));
+    return CPALS_E_CUDA;
+  }
+  return CPALS_OK;
+}
+
+void invalidate_graph(cpals_ctx* c) {
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
+}
+
+cudaError_t enqueue_mttkrp(cpals_ctx* c, int n, const DevCheck* chk) {
+  if (c->mmode == CPALS_MTTKRP_FP64)
+    return launch_mttkrp_f64(c->dT, c->tdtype, factor_set(c), c->geom[n], c->R, c->splits[n], c->cps[n],
+                             static_cast<double*>(c->part), chk, c->st);
+  const float* F32[kMaxOrder] = {};
+  for (int m = 0; m < c->order; ++m) F32[m] = c->F32t[m];
+  return tc_launch_mttkrp(c->tc, n, F32, static_cast<float*>(c->part), chk, c->st);
+}
+
+int enqueue_sweep(cpals_ctx* c) {
+  const int N = c->order;
+  const int R = (int)c->R;
+  const GramSet gs = gram_set(c);
+  for (int n = 0; n < N; ++n) {
+    const int last = (n == N - 1);
+    const int64_t In = c->dims[n];
+    CPALS_CUDA_TRY(cudaEventRecord(c->ev_main[n], c->st));
+    CPALS_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_main[n], 0));
+    CPALS_CUDA_TRY(launch_factorize(gs, N, n, R, c->work, c->U, c->piv, c->W, c->info, c->chk, c->side));
+    CPALS_CUDA_TRY(cudaEventRecord(c->ev_side[n], c->side));
+    CPALS_CUDA_TRY(enqueue_mttkrp(c, n, c->chk));
+    CPALS_CUDA_TRY(cudaStreamWaitEvent(c->st, c->ev_side[n], 0));
+    CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W, c->info,
+                                     c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
+    CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->chk, c->st));
+    CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->G[n], gs, N, last, c->inner_rows, In, c->chk, c->traj,
+                                   c->traj_cap, c->st));
+    // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
+    // left untouched by the early-returning kernels of later sweeps).
+    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[n], c->F32t[n], c->ld32[n], last ? nullptr : c->chk,
+                                    c->st));
+  }
+  return CPALS_OK;
+}
+
+int build_graph(cpals_ctx* c) {
+  invalidate_graph(c);
+  cudaGraph_t g = nullptr;
+  CPALS_CUDA_TRY(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_sweep(c);
+  cudaError_t e = cudaStreamEndCapture(c->st, &g);
+  if (rc != CPALS_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  CPALS_CUDA_TRY(e);
+  e = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  CPALS_CUDA_TRY(e);
+  return CPALS_OK;
+}
+
+int ensure_traj(cpals_ctx* c, int64_t need) {
+  if (need <= c->traj_cap) return CPALS_OK;
+  int64_t cap = std::max<int64_t>(need, 2 * c->traj_cap);
+  if (c->traj) cudaFree(c->traj);
+  c->traj = nullptr;
+  c->traj_cap = 0;
+  if (dmalloc(&c->traj, cap) != CPALS_OK) return CPALS_E_CUDA;
+  c->traj_cap = cap;
+  invalidate_graph(c);
+  return CPALS_OK;
+}
+
+int validate_pivots(const cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps) {
+  int j = 0;
+  for (int m = 0; m < c->order; ++m) {
+    if (m == mode) continue;
+    const int64_t* col = pivots + nsamps * j;
+    for (int64_t s = 0; s < nsamps; ++s)
+      if (col[s] < 1 || col[s] > c->dims[m]) return CPALS_E_ARG;
+    ++j;
+  }
+  return CPALS_OK;
+}
+
+int ensure_sample_buffers(cpals_ctx* c, int64_t nsamps) {
+  if (nsamps <= c->samp_cap) return CPALS_OK;
+  cudaFree(c->dpiv);
+  cudaFree(c->Scol);
+  cudaFree(c->Srow);
+  cudaFree(c->Ts);
+  c->dpiv = nullptr;
+  c->Scol = c->Srow = nullptr;
+  c->Ts = nullptr;
+  c->samp_cap = 0;
+  const size_t esz = c->tdtype == CPALS_DTYPE_F64 ? 8 : 4;
+  if (dmalloc(&c->dpiv, (size_t)nsamps * (c->order - 1)) || dmalloc(&c->Scol, (size_t)nsamps * c->R) ||
+      dmalloc(&c->Srow, (size_t)nsamps * c->R))
+    return CPALS_E_CUDA;
+  char* ts = nullptr;
+  if (dmalloc(&ts, (size_t)c->maxI * nsamps * esz)) return CPALS_E_CUDA;
+  c->Ts = ts;
+  c->samp_cap = nsamps;
+  return CPALS_OK;
+}
+
+int upload_pivots(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps) {
+  if (!pivots || nsamps <= 0) return CPALS_E_ARG;
+  if (mode < 0 || mode >= c->order) return CPALS_E_ARG;
+  if (validate_pivots(c, mode, pivots, nsamps) != CPALS_OK) return CPALS_E_ARG;
+  if (ensure_sample_buffers(c, nsamps) != CPALS_OK) return CPALS_E_CUDA;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->dpiv, pivots, sizeof(int64_t) * nsamps * (c->order - 1), cudaMemcpyHostToDevice,
+                                 c->st));
+  CPALS_CUDA_TRY(cudaMemsetAsync(c->derr, 0, sizeof(int), c->st));
+  return CPALS_OK;
+}
+
+int check_derr(cpals_ctx* c) {
+  int h = 0;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return h ? CPALS_E_DEVICE : CPALS_OK;
+}
+
+void colmajor_to_rowmajor_host(const double* src, int64_t rows, int64_t cols, double* dst) {
+  for (int64_t i = 0; i < rows; ++i)
+    for (int64_t r = 0; r < cols; ++r) dst[i * cols + r] = src[i + rows * r];
+}
+void rowmajor_to_colmajor_host(const double* src, int64_t rows, int64_t cols, double* dst) {
+  for (int64_t i = 0; i < rows; ++i)
+    for (int64_t r = 0; r < cols; ++r) dst[i + rows * r] = src[i * cols + r];
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpals_version(void) { return 100; }
+
+const char* cpals_status_string(int s) {
+  switch (s) {
+    case CPALS_OK: return "ok";
+    case CPALS_E_ARG: return "bad argument";
+    case CPALS_E_CUDA: return "CUDA runtime error";
+    case CPALS_E_NAN: return "Error NAN: the fit became NaN";
+    case CPALS_E_STATE: return "call out of order (tensor or factors not set)";
+    case CPALS_E_UNSUPPORTED: return "unsupported shape or option";
+    case CPALS_E_DEVICE: return "a kernel reported an error status";
+    default: return "unknown status";
+  }
+}
+
+int cpals_destroy(cpals_ctx* c) {
+  if (!c) return CPALS_OK;
+  DeviceGuard g(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->side) cudaStreamSynchronize(c->side);
+  invalidate_graph(c);
+  if (c->tc) tc_destroy(c->tc);
+  for (int m = 0; m < kMaxOrder; ++m) {
+    cudaFree(c->F[m]);
+    cudaFree(c->F32t[m]);
+    cudaFree(c->G[m]);
+    if (c->ev_main[m]) cudaEventDestroy(c->ev_main[m]);
+    if (c->ev_side[m]) cudaEventDestroy(c->ev_side[m]);
+  }
+  cudaFree(c->dT_owned);
+  cudaFree(c->lam);
+  cudaFree(c->X);
+  cudaFree(c->Graw);
+  cudaFree(c->part);
+  cudaFree(c->work);
+  cudaFree(c->U);
+  cudaFree(c->piv);
+  cudaFree(c->W);
+  cudaFree(c->info);
+  cudaFree(c->gpart);
+  cudaFree(c->gcnt);
+  cudaFree(c->inner_rows);
+  cudaFree(c->chk);
+  if (c->hchk) cudaFreeHost(c->hchk);
+  cudaFree(c->traj);
+  cudaFree(c->dpiv);
+  cudaFree(c->Scol);
+  cudaFree(c->Srow);
+  cudaFree(c->Ts);
+  cudaFree(c->Spart);
+  cudaFree(c->derr);
+  if (c->st) cudaStreamDestroy(c->st);
+  if (c->side) cudaStreamDestroy(c->side);
+  delete c;
+  return CPALS_OK;
+}
+
+int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, int64_t rank, int tensor_dtype,
+                 int mttkrp_mode, int flags) {
+  if (!out) return CPALS_E_ARG;
+  *out = nullptr;
+  if (order < 2 || order > kMaxOrder || !dims) return CPALS_E_ARG;
+  if (rank < 1 || rank > CPALS_MAX_RANK_SOLVE) return CPALS_E_ARG;
+  if (tensor_dtype != CPALS_DTYPE_F64 && tensor_dtype != CPALS_DTYPE_F32) return CPALS_E_ARG;
+  if (mttkrp_mode != CPALS_MTTKRP_FP64 && mttkrp_mode != CPALS_MTTKRP_BF16X3) return CPALS_E_ARG;
+  int64_t numel = 1, maxI = 0;
+  for (int m = 0; m < order; ++m) {
+    if (dims[m] < 1 || dims[m] > (int64_t(1) << 31)) return CPALS_E_ARG;
+    numel *= dims[m];
+    maxI = std::max(maxI, dims[m]);
+    if (numel > (int64_t(1) << 40)) return CPALS_E_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
+  DeviceGuard guard(device);
+  cpals_ctx* c = new cpals_ctx();
+  c->device = device;
+  c->order = order;
+  c->tdtype = tensor_dtype;
+  c->mmode = mttkrp_mode;
+  c->flags = flags;
+  c->R = rank;
+  c->numel = numel;
+  c->maxI = maxI;
+  for (int m = 0; m < order; ++m) c->dims[m] = dims[m];
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  int rc = CPALS_OK;
+#define CK(x)                \
+  do {                       \
+    rc = (x);                \
+    if (rc != CPALS_OK) {    \
+      cpals_destroy(c);      \
+      return rc;             \
+    }                        \
+  } while (0)
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
+    cpals_destroy(c);
+    return CPALS_E_CUDA;
+  }
+  for (int m = 0; m < order; ++m) {
+    if (cudaEventCreateWithFlags(&c->ev_main[m], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_side[m], cudaEventDisableTiming) != cudaSuccess) {
+      cpals_destroy(c);
+      return CPALS_E_CUDA;
+    }
+  }
+  const int64_t R = rank;
+  if (mttkrp_mode == CPALS_MTTKRP_BF16X3) {
+    rc = tc_create(&c->tc, order, dims, R, tensor_dtype, c->num_sms);
+    if (rc != CPALS_OK) {
+      cpals_destroy(c);
+      return rc;
+    }
+  }
+  size_t part_elems = 0;
+  for (int m = 0; m < order; ++m) {
+    if (mttkrp_mode == CPALS_MTTKRP_FP64) {
+      c->geom[m] = make_geom(order, dims, m, 32);
+      c->splits[m] = mttkrp_f64_splits(c->geom[m], R, c->num_sms, &c->cps[m]);
+    } else {
+      c->splits[m] = tc_splits(c->tc, m);
+    }
+    part_elems = std::max(part_elems, (size_t)c->splits[m] * dims[m] * R);
+    c->gS2[m] = gram_splits(dims[m], (int)R, c->num_sms);
+    c->ld32[m] = (mttkrp_mode == CPALS_MTTKRP_BF16X3) ? tc_factor_ld(c->tc, m) : dims[m];
+    CK(dmalloc(&c->F[m], (size_t)dims[m] * R));
+    CK(dmalloc(&c->F32t[m], (size_t)c->ld32[m] * R));
+    CPALS_CUDA_TRY(cudaMemset(c->F32t[m], 0, sizeof(float) * c->ld32[m] * R));
+    CK(dmalloc(&c->G[m], (size_t)R * R));
+  }
+  c->part_f32 = (mttkrp_mode == CPALS_MTTKRP_BF16X3);
+  {
+    char* p = nullptr;
+    CK(dmalloc(&p, part_elems * (c->part_f32 ? 4 : 8)));
+    c->part = p;
+  }
+  int maxS2 = 1;
+  for (int m = 0; m < order; ++m) maxS2 = std::max(maxS2, c->gS2[m]);
+  CK(dmalloc(&c->lam, R));
+  CK(dmalloc(&c->X, (size_t)maxI * R));
+  CK(dmalloc(&c->Graw, (size_t)R * R));
+  CK(dmalloc(&c->work, factorize_work_doubles((int)R)));
+  CK(dmalloc(&c->U, (size_t)R * R));
+  CK(dmalloc(&c->piv, R));
+  CK(dmalloc(&c->W, (size_t)R * R));
+  CK(dmalloc(&c->info, 1));
+  CK(dmalloc(&c->gpart, (size_t)gram_tiles((int)R) * maxS2 * 256));
+  CK(dmalloc(&c->gcnt, gram_tiles((int)R)));
+  CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * gram_tiles((int)R)));
+  CK(dmalloc(&c->inner_rows, maxI));
+  CK(dmalloc(&c->chk, 1));
+  CPALS_CUDA_TRY(cudaMemset(c->chk, 0, sizeof(DevCheck)));
+  CK(dmalloc(&c->derr, 1));
+  if (cudaMallocHost(&c->hchk, sizeof(DevCheck)) != cudaSuccess) {
+    cpals_destroy(c);
+    return CPALS_E_CUDA;
+  }
+  memset(c->hchk, 0, sizeof(DevCheck));
+  CK(ensure_traj(c, 1024));
+#undef CK
+  *out = c;
+  return CPALS_OK;
+}
+
+static int after_tensor_set(cpals_ctx* c) {
+  c->T_set = true;
+  invalidate_graph(c);
+  if (c->tc) {
+    int rc = tc_set_tensor(c->tc, c->dT, c->st);
+    if (rc != CPALS_OK) return rc;
+  }
+  return CPALS_OK;
+}
+
+int cpals_set_tensor(cpals_ctx* c, const void* host_tensor) {
+  if (!c || !host_tensor) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  const size_t bytes = (size_t)c->numel * (c->tdtype == CPALS_DTYPE_F64 ? 8 : 4);
+  if (!c->dT_owned) {
+    char* p = nullptr;
+    if (dmalloc(&p, bytes) != CPALS_OK) return CPALS_E_CUDA;
+    c->dT_owned = p;
+  }
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->dT_owned, host_tensor, bytes, cudaMemcpyHostToDevice, c->st));
+  c->dT = c->dT_owned;
+  int rc = after_tensor_set(c);
+  if (rc != CPALS_OK) return rc;
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CPALS_OK;
+}
+
+int cpals_set_tensor_device(cpals_ctx* c, const void* device_tensor) {
+  if (!c || !device_tensor) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  c->dT = device_tensor;
+  int rc = after_tensor_set(c);
+  if (rc != CPALS_OK) return rc;
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CPALS_OK;
+}
+
+int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const double* host_lambda) {
+  if (!c || !host_factors) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  const int R = (int)c->R;
+  std::vector<double> tmp;
+  for (int m = 0; m < c->order; ++m) {
+    if (!host_factors[m]) return CPALS_E_ARG;
+    tmp.resize((size_t)c->dims[m] * R);
+    colmajor_to_rowmajor_host(host_factors[m], c->dims[m], R, tmp.data());
+    CPALS_CUDA_TRY(cudaMemcpyAsync(c->F[m], tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c->st));
+    CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32t[m], c->ld32[m], nullptr, c->st));
+    CPALS_CUDA_TRY(launch_gram(c->F[m], c->dims[m], R, c->gS2[m], c->gpart, c->gcnt, c->G[m], nullptr, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));  // tmp is reused for the next mode
+  }
+  if (host_lambda) {
+    CPALS_CUDA_TRY(cudaMemcpyAsync(c->lam, host_lambda, sizeof(double) * R, cudaMemcpyHostToDevice, c->st));
+  } else {
+    std::vector<double> ones(R, 1.0);
+    CPALS_CUDA_TRY(cudaMemcpyAsync(c->lam, ones.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->st));
+  }
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  c->F_set = true;
+  return CPALS_OK;
+}
+
+int cpals_get_factors(cpals_ctx* c, double* const* host_factors, double* host_lambda) {
+  if (!c) return CPALS_E_ARG;
+  if (!c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  const int R = (int)c->R;
+  std::vector<double> tmp;
+  for (int m = 0; m < c->order; ++m) {
+    if (!host_factors || !host_factors[m]) continue;
+    tmp.resize((size_t)c->dims[m] * R);
+    CPALS_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c->F[m], sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+    rowmajor_to_colmajor_host(tmp.data(), c->dims[m], R, host_factors[m]);
+  }
+  if (host_lambda) {
+    CPALS_CUDA_TRY(cudaMemcpyAsync(host_lambda, c->lam, sizeof(double) * R, cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  }
+  return CPALS_OK;
+}
+
+int cpals_get_gram(cpals_ctx* c, int mode, double* host_gram) {
+  if (!c || !host_gram || mode < 0 || mode >= c->order) return CPALS_E_ARG;
+  if (!c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(host_gram, c->G[mode], sizeof(double) * c->R * c->R, cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CPALS_OK;  // symmetric: row-major == column-major
+}
+
+int cpals_mttkrp(cpals_ctx* c, int mode, double* host_out) {
+  if (!c || !host_out || mode < 0 || mode >= c->order) return CPALS_E_ARG;
+  if (!c->T_set || !c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  const int R = (int)c->R;
+  const int64_t In = c->dims[mode];
+  CPALS_CUDA_TRY(enqueue_mttkrp(c, mode, nullptr));
+  CPALS_CUDA_TRY(launch_reduce_partials(c->part, c->part_f32, c->splits[mode], In, R, c->X, c->st));
+  std::vector<double> tmp((size_t)In * R);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c->X, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  rowmajor_to_colmajor_host(tmp.data(), In, R, host_out);
+  return CPALS_OK;
+}
+
+int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int64_t traj_capacity) {
+  if (!c || !check) return CPALS_E_ARG;
+  if (check->kind != CPALS_CHECK_NONE && check->kind != CPALS_CHECK_FIT) return CPALS_E_ARG;
+  if (check->max_counter < 0) return CPALS_E_ARG;
+  if (!c->T_set || !c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  const int64_t nmax = (int64_t)check->max_counter - check->iter;
+  check->sweeps_run = 0;
+  if (nmax <= 0) return CPALS_OK;
+  if (ensure_traj(c, nmax) != CPALS_OK) return CPALS_E_CUDA;
+  // keep the device fallback counter, reset the rest from the host check
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  DevCheck& h = *c->hchk;
+  h.kind = check->kind;
+  h.iter = check->iter;
+  h.counter = check->counter;
+  h.max_counter = check->max_counter;
+  h.tol = check->tolerance;
+  h.ref_norm = check->ref_norm;
+  h.lastfit = check->lastfit;
+  h.final_fit = check->final_fit;
+  h.total_iter = check->total_iter;
+  h.done = 0;
+  h.nan_flag = 0;
+  h.sweeps = 0;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->chk, c->hchk, sizeof(DevCheck), cudaMemcpyHostToDevice, c->st));
+  const bool use_graph = !(c->flags & CPALS_FLAG_NO_GRAPH);
+  if (use_graph && !c->graph) {
+    int rc = build_graph(c);
+    if (rc != CPALS_OK) return rc;
+  }
+  int64_t launched = 0, batch = 4;
+  while (launched < nmax) {
+    const int64_t b = std::min(batch, nmax - launched);
+    for (int64_t k = 0; k < b; ++k) {
+      if (use_graph) {
+        CPALS_CUDA_TRY(cudaGraphLaunch(c->graph, c->st));
+      } else {
+        int rc = enqueue_sweep(c);
+        if (rc != CPALS_OK) return rc;
+      }
+    }
+    launched += b;
+    batch = std::min<int64_t>(batch * 2, 64);
+    CPALS_CUDA_TRY(cudaMemcpyAsync(&c->hchk->done, &c->chk->done, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+    if (c->hchk->done) break;
+  }
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  check->iter = h.iter;
+  check->counter = h.counter;
+  check->lastfit = h.lastfit;
+  check->final_fit = h.final_fit;
+  check->total_iter = h.total_iter;
+  check->sweeps_run = h.sweeps;
+  if (fit_trajectory && traj_capacity > 0) {
+    const int64_t n = std::min<int64_t>({(int64_t)h.sweeps, traj_capacity, c->traj_cap});
+    if (n > 0) {
+      CPALS_CUDA_TRY(cudaMemcpyAsync(fit_trajectory, c->traj, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
+      CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+    }
+  }
+  if (h.nan_flag) return CPALS_E_NAN;
+  return CPALS_OK;
+}
+
+int cpals_fallback_count(cpals_ctx* c, int64_t* count) {
+  if (!c || !count) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  *count = c->hchk->fallbacks;
+  return CPALS_OK;
+}
+
+int cpals_synchronize(cpals_ctx* c) {
+  if (!c) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->side));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CPALS_OK;
+}
+
+int cpals_pivot_hadamard(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps, double* host_out) {
+  if (!c || !host_out) return CPALS_E_ARG;
+  if (!c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  int rc = upload_pivots(c, mode, pivots, nsamps);
+  if (rc != CPALS_OK) return rc;
+  CPALS_CUDA_TRY(launch_pivot_hadamard(factor_set(c), c->order, mode, c->dims, c->dpiv, nsamps, (int)c->R, c->Scol,
+                                       c->derr, c->st));
+  CPALS_CUDA_TRY(cudaMemcpyAsync(host_out, c->Scol, sizeof(double) * nsamps * c->R, cudaMemcpyDeviceToHost, c->st));
+  return check_derr(c);
+}
+
+int cpals_fused_flatten_sample(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps, void* host_out) {
+  if (!c || !host_out) return CPALS_E_ARG;
+  if (!c->T_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  int rc = upload_pivots(c, mode, pivots, nsamps);
+  if (rc != CPALS_OK) return rc;
+  CPALS_CUDA_TRY(launch_fibers(c->dT, c->tdtype, c->order, mode, c->dims, c->dpiv, nsamps, c->Ts, c->derr, c->st));
+  const size_t esz = c->tdtype == CPALS_DTYPE_F64 ? 8 : 4;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(host_out, c->Ts, esz * c->dims[mode] * nsamps, cudaMemcpyDeviceToHost, c->st));
+  return check_derr(c);
+}
+
+int cpals_leverage_scores(cpals_ctx* c, int mode, double* host_probs) {
+  if (!c || !host_probs || mode < 0 || mode >= c->order) return CPALS_E_ARG;
+  if (!c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  const int R = (int)c->R;
+  const int64_t In = c->dims[mode];
+  double* probs = c->inner_rows;  // maxI doubles, free outside a sweep
+  CPALS_CUDA_TRY(launch_gram(c->F[mode], In, R, c->gS2[mode], c->gpart, c->gcnt, c->Graw, nullptr, c->st));
+  GramSet one{};
+  one.G[0] = c->Graw;
+  CPALS_CUDA_TRY(launch_factorize(one, 1, -1, R, c->work, c->U, c->piv, c->W, c->info, nullptr, c->st));
+  const double scale = 1.0 / (double)std::min<int64_t>(In, R);
+  CPALS_CUDA_TRY(launch_leverage_rows(c->F[mode], In, R, c->work, c->U, c->piv, c->info, scale, probs, c->st));
+  CPALS_CUDA_TRY(cudaMemcpyAsync(host_probs, probs, sizeof(double) * In, cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CPALS_OK;
+}
+
+int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps, int normal) {
+  (void)normal;  // both forms solve the FP64 normal equations of the sampled system
+  if (!c) return CPALS_E_ARG;
+  if (!c->T_set || !c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  int rc = upload_pivots(c, mode, pivots, nsamps);
+  if (rc != CPALS_OK) return rc;
+  const int R = (int)c->R;
+  const int64_t In = c->dims[mode];
+  // S (sampled KRP rows) and T_s (sampled fibres)
+  CPALS_CUDA_TRY(launch_pivot_hadamard(factor_set(c), c->order, mode, c->dims, c->dpiv, nsamps, R, c->Scol, c->derr,
+                                       c->st));
+  CPALS_CUDA_TRY(launch_fibers(c->dT, c->tdtype, c->order, mode, c->dims, c->dpiv, nsamps, c->Ts, c->derr, c->st));
+  CPALS_CUDA_TRY(launch_colmajor_to_rowmajor(c->Scol, nsamps, R, c->Srow, c->st));
+  // A = S^T S (the Gram partial buffer holds up to max(gS2) splits)
+  const int s2 = std::min(gram_splits(nsamps, R, c->num_sms), *std::max_element(c->gS2, c->gS2 + c->order));
+  CPALS_CUDA_TRY(launch_gram(c->Srow, nsamps, R, s2, c->gpart, c->gcnt, c->Graw, nullptr, c->st));
+  GramSet one{};
+  one.G[0] = c->Graw;
+  CPALS_CUDA_TRY(launch_factorize(one, 1, -1, R, c->work, c->U, c->piv, c->W, c->info, nullptr, c->st));
+  // B = T_s S : an order-2 FP64 MTTKRP of T_s (In x nsamps) with the factor S
+  const int64_t d2[2] = {In, nsamps};
+  const ModeGeom g2 = make_geom(2, d2, 0, 32);
+  int64_t cps = 0;
+  const int sp = mttkrp_f64_splits(g2, R, c->num_sms, &cps);
+  const size_t need = (size_t)sp * In * R;
+  if (need > c->spart_cap) {
+    cudaFree(c->Spart);
+    c->Spart = nullptr;
+    c->spart_cap = 0;
+    if (dmalloc(&c->Spart, need) != CPALS_OK) return CPALS_E_CUDA;
+    c->spart_cap = need;
+  }
+  FactorSet fs2{};
+  fs2.F[0] = nullptr;
+  fs2.F[1] = c->Srow;
+  CPALS_CUDA_TRY(launch_mttkrp_f64(c->Ts, c->tdtype, fs2, g2, R, sp, cps, c->Spart, nullptr, c->st));
+  CPALS_CUDA_TRY(launch_solve_rows(c->Spart, 0, sp, In, R, c->work, c->U, c->piv, c->W, c->info, c->X, nullptr,
+                                   nullptr, c->st));
+  // row_norm, Gram refresh, FP32 copy
+  CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[mode], c->gpart, c->gcnt, c->Graw, nullptr, c->st));
+  const GramSet gs = gram_set(c);
+  CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->G[mode], gs, c->order, 0, nullptr, In, nullptr, c->traj,
+                                 c->traj_cap, c->st));
+  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], nullptr, c->st));
+  return check_derr(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// Internal declarations shared by the libcpals translation units.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#include "cpals.h"
+
+namespace cpals {
+
+constexpr int kMaxOrder = CPALS_MAX_ORDER;
+#define CPALS_MAX_RANK_SOLVE 512
+
+// Device-resident state of a FitCheck / NoCheck (fit_check.jl:5-20, no_check.jl:1-9).
+// The fit kernel updates it once per sweep, so sweeps can be replayed from a CUDA
+// graph without a host round trip.  `done` makes the kernels of later sweeps return
+// at once: the factors stay as they were at the converged sweep.
+struct DevCheck {
+  int kind;
+  int iter;
+  int counter;
+  int max_counter;
+  double tol;
+  double ref_norm;
+  double lastfit;
+  double final_fit;
+  int total_iter;
+  int done;
+  int nan_flag;
+  int sweeps;  // sweeps whose check ran (index into the trajectory)
+  long long fallbacks;  // pivoted-QR fallbacks taken by the normal-equation solve
+};
+
+struct FactorSet {
+  const double* F[kMaxOrder];  // FP64 factors, row-major [I_n][R]
+};
+struct GramSet {
+  const double* G[kMaxOrder];  // FP64 Grams, R x R
+};
+
+// Geometry of the MTTKRP of one mode.  The reduction index space (every mode but
+// `mode`) is cut into chunks of `chunk` consecutive values of the fastest
+// reduction mode `fmode` at fixed values of the other ("outer") reduction modes.
+struct ModeGeom {
+  int order, mode, fmode, n_outer;
+  int outer_modes[kMaxOrder];
+  int64_t dims[kMaxOrder];
+  int64_t strides[kMaxOrder];  // element strides of the column-major tensor
+  int64_t In, If, nfb, nchunks;
+};
+
+inline ModeGeom make_geom(int order, const int64_t* dims, int mode, int64_t chunk, const int64_t* fdims = nullptr) {
+  ModeGeom g{};
+  g.order = order;
+  g.mode = mode;
+  int64_t s = 1;
+  for (int m = 0; m < order; ++m) {
+    g.dims[m] = dims[m];
+    g.strides[m] = s;
+    s *= dims[m];
+  }
+  g.fmode = (mode == 0) ? 1 : 0;
+  g.In = dims[mode];
+  g.If = fdims ? fdims[g.fmode] : dims[g.fmode];
+  g.nfb = (g.If + chunk - 1) / chunk;
+  g.n_outer = 0;
+  int64_t outer = 1;
+  for (int m = 0; m < order; ++m) {
+    if (m == mode || m == g.fmode) continue;
+    g.outer_modes[g.n_outer++] = m;
+    outer *= dims[m];
+  }
+  g.nchunks = g.nfb * outer;
+  return g;
+}
+
+// Status of one normal-equation factorisation (written by the factorize kernel).
+struct SolveInfo {
+  int rank;      // rank reached by the pivoted Cholesky
+  int fallback;  // 1 if the pivoted-QR path produced the solve operator
+  int qr_rank;   // numerical rank found by the QR path
+  int pad;
+};
+
+// ---- launchers (defined in the kernel translation units) ----
+
+// FP64 MTTKRP partials: part[split][In][R] (FP64).
+int mttkrp_f64_splits(const ModeGeom& g, int64_t R, int num_sms, int64_t* chunks_per_split);
+cudaError_t launch_mttkrp_f64(const void* T, int tdtype, const FactorSet& fs, const ModeGeom& g, int64_t R,
+                              int splits, int64_t chunks_per_split, double* part, const DevCheck* chk,
+                              cudaStream_t st);
+
+// V = Hadamard of the Grams of every mode but `skip`; pivoted Cholesky (upper,
+// tol 1e-6) with a column-pivoted QR fallback.  Single CTA.
+cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, double* work, double* U, int* piv,
+                             double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st);
+size_t factorize_work_doubles(int R);
+
+// Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and
+// (optionally) per-row sums of M .* X for the fit.  `work` is the factorize workspace.
+cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
+                              const double* U, const int* piv, const double* W, const SolveInfo* info, double* X,
+                              double* inner_rows, const DevCheck* chk, cudaStream_t st);
+
+// G = X^T X (row-major X, In x R) over S2 row splits; part: gram_tiles(R)*S2*256 doubles,
+// counters: gram_tiles(R) zero-initialised unsigneds (left zeroed after each launch).
+int gram_tiles(int R);
+int gram_splits(int64_t In, int R, int num_sms);
+cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters, double* G,
+                        const DevCheck* chk, cudaStream_t st);
+
+// lambda = sqrt(diag Graw), G_n = Graw ./ (lambda lambda^T); on the last mode also the fit
+// and the device check update (trajectory entry per sweep).
+cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* Gn, const GramSet& gs, int order,
+                            int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
+                            int64_t traj_cap, cudaStream_t st);
+
+// F = X ./ lambda (lambda may be null: plain copy) and an FP32 column-major copy [R][ld32].
+cudaError_t launch_normalize(const double* X, const double* lam, int64_t In, int R, double* F, float* F32t,
+                             int64_t ld32, const DevCheck* chk, cudaStream_t st);
+
+// Row-major rows x cols -> row-major cols x rows (FP64).
+cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);
+
+// Reduce MTTKRP partials to a row-major FP64 M (for cpals_mttkrp).
+cudaError_t launch_reduce_partials(const void* part, int part_is_f32, int splits, int64_t In, int R, double* M,
+                                   cudaStream_t st);
+
+// ---- gathers (k_gather.cu) ----
+cudaError_t launch_pivot_hadamard(const FactorSet& fs, int order, int mode, const int64_t* dims,
+                                  const int64_t* piv, int64_t nsamps, int R, double* out, int* err, cudaStream_t st);
+cudaError_t launch_fibers(const void* T, int tdtype, int order, int mode, const int64_t* dims, const int64_t* piv,
+                          int64_t nsamps, void* out, int* err, cudaStream_t st);
+cudaError_t launch_colmajor_to_rowmajor(const double* src, int64_t rows, int R, double* dst, cudaStream_t st);
+cudaError_t launch_leverage_rows(const double* F, int64_t In, int R, const double* work, const double* U,
+                                 const int* piv, const SolveInfo* info, double scale, double* probs, cudaStream_t st);
+
+}  // namespace cpals
+
+#define CPALS_CUDA_TRY(expr)                                                            \
+  do {                                                                                   \
+    cudaError_t _e = (expr);                                                             \
+    if (_e != cudaSuccess) {                                                             \
+      fprintf(stderr, "libcpals: %s failed: %s (%s:%d)\n", #expr, cudaGetErrorString(_e), \
+              __FILE__, __LINE__);                                                       \
+      return CPALS_E_CUDA;                                                               \
+    }                                                                                    \
+  } while (0)

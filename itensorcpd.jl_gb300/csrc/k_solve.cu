@@ -1,0 +1,783 @@
+// FP64 normal-equation kernels of one ALS mode update:
+//   factorize  : V = Hadamard of the other modes' Grams (compute_krp,
+//                MttkrpAlgorithm.jl:18-31); pivoted Cholesky P^T V P = U^T U with
+//                LAPACK dpstrf's stopping rule (pivot <= 1e-6 or NaN -> rank deficient,
+//                ldiv_solve.jl:17-18); on rank deficiency a column-pivoted Householder QR
+//                gives the least-squares operator instead (ldiv_solve.jl:19-21).
+//   solve_rows : reduce the MTTKRP split-K partials, X = M V^{-1} one warp per row
+//                (solve_ls_problem, MttkrpAlgorithm.jl:34-41), partial sums of M .* X
+//                for the fit.
+//   gram       : X^T X by 16x16 tiles of the upper triangle over row splits, each tile
+//                reduced by its last block in split order (deterministic).
+//   finalize   : lambda = column norms (row_norm.jl:4-24), G_n = F_n^T F_n (post_solve,
+//                standard/tensor.jl:86-89); after the last mode the fit and the
+//                FitCheck / NoCheck update (fit_check.jl:24-66, no_check.jl:11-19).
+//   normalize  : F_n = X ./ lambda, plus the FP32 column-major copy the tensor-core
+//                MTTKRP reads.
+// FP64 runs at 2 FMA/clk/SM on GB300, so every O(I_n R^2) piece is spread over many
+// CTAs; only the O(R^3) factorisation is a single CTA, and it runs on a side stream
+// concurrently with the MTTKRP of the same mode.
+#include <cmath>
+
+#include "cpals_internal.cuh"
+
+namespace cpals {
+namespace {
+
+constexpr double kCholTol = 1e-6;  // src/ITensorCPD.jl:2 cholesky_epsilon
+constexpr int FT = 512;            // factorize threads
+
+__device__ __forceinline__ bool done_flag(const DevCheck* chk) { return chk != nullptr && chk->done; }
+
+// block-wide argmax with first-index tie break; NaN is treated as +inf so it is picked
+// (and then rejected by the stopping test, like DISNAN in dpstf2).
+__device__ void block_argmax(double v, int idx, double* sv, int* si, double* out_v, int* out_i) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double key = isnan(v) ? INFINITY : v;
+  for (int off = 16; off > 0; off >>= 1) {
+    double ok = __shfl_down_sync(0xffffffffu, key, off);
+    int oi = __shfl_down_sync(0xffffffffu, idx, off);
+    double ov = __shfl_down_sync(0xffffffffu, v, off);
+    if (ok > key || (ok == key && oi < idx)) {
+      key = ok;
+      idx = oi;
+      v = ov;
+    }
+  }
+  if (lane == 0) {
+    sv[w] = v;
+    si[w] = idx;
+  }
+  __syncthreads();
+  if (w == 0) {
+    v = lane < nw ? sv[lane] : -INFINITY;
+    idx = lane < nw ? si[lane] : 0x7fffffff;
+    key = isnan(v) ? INFINITY : v;
+    for (int off = 16; off > 0; off >>= 1) {
+      double ok = __shfl_down_sync(0xffffffffu, key, off);
+      int oi = __shfl_down_sync(0xffffffffu, idx, off);
+      double ov = __shfl_down_sync(0xffffffffu, v, off);
+      if (ok > key || (ok == key && oi < idx)) {
+        key = ok;
+        idx = oi;
+        v = ov;
+      }
+    }
+    if (lane == 0) {
+      *out_v = v;
+      *out_i = idx;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ double block_sum(double v, double* sv) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  __syncthreads();
+  if (lane == 0) sv[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; ++i) t += sv[i];
+  __syncthreads();
+  if (threadIdx.x == 0) sv[0] = t;
+  __syncthreads();
+  t = sv[0];
+  __syncthreads();
+  return t;
+}
+
+// Column-pivoted Householder QR of V (R x R) and the least-squares operator W with
+// X^T = W M^T.  Rank is cut where |R_kk| <= R * eps * |R_00| (Julia's QRPivoted ldiv!
+// uses rcond = min(m,n) * eps); a rank-deficient system gets the minimum-norm solution.
+__device__ void qr_fallback(const GramSet& gs, int order, int skip, int R, double* __restrict__ B,
+                            double* __restrict__ Z, double* __restrict__ Y, double* __restrict__ tau,
+                            int* __restrict__ perm, double* __restrict__ W, SolveInfo* info, double* sv, int* si,
+                            double* cn) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int e = tid; e < R * R; e += blockDim.x) {
+    double v = 1.0;
+    for (int m = 0; m < order; ++m)
+      if (m != skip) v *= gs.G[m][e];
+    B[e] = v;
+  }
+  for (int k = tid; k < R; k += blockDim.x) perm[k] = k;
+  __syncthreads();
+  __shared__ double s_bv, s_tau, s_beta;
+  __shared__ int s_p;
+  for (int j = 0; j < R; ++j) {
+    // column norms of the trailing block
+    for (int k = j + warp; k < R; k += nw) {
+      double s = 0.0;
+      for (int i = j + lane; i < R; i += 32) s += B[i * R + k] * B[i * R + k];
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+      if (lane == 0) cn[k] = s;
+    }
+    __syncthreads();
+    double bv = -INFINITY;
+    int bi = 0x7fffffff;
+    for (int k = j + tid; k < R; k += blockDim.x) {
+      double c = cn[k];
+      double key = isnan(c) ? INFINITY : c, bkey = isnan(bv) ? INFINITY : bv;
+      if (key > bkey || (key == bkey && k < bi)) {
+        bv = c;
+        bi = k;
+      }
+    }
+    double outv;
+    int outi;
+    block_argmax(bv, bi, sv, si, &outv, &outi);
+    if (tid == 0) s_p = outi;
+    __syncthreads();
+    const int p = s_p;
+    if (p != j) {
+      for (int i = tid; i < R; i += blockDim.x) {
+        double t = B[i * R + j];
+        B[i * R + j] = B[i * R + p];
+        B[i * R + p] = t;
+      }
+      if (tid == 0) {
+        int t = perm[j];
+        perm[j] = perm[p];
+        perm[p] = t;
+      }
+    }
+    __syncthreads();
+    // Householder reflector for x = B[j:, j] (dlarfg convention)
+    double sg = 0.0;
+    for (int i = j + 1 + tid; i < R; i += blockDim.x) sg += B[i * R + j] * B[i * R + j];
+    sg = block_sum(sg, sv);
+    if (tid == 0) {
+      const double alpha = B[j * R + j];
+      double t = 0.0, beta = alpha, vs = 0.0;
+      if (sg > 0.0 || isnan(sg)) {
+        beta = -copysign(sqrt(alpha * alpha + sg), alpha);
+        t = (beta - alpha) / beta;
+        vs = 1.0 / (alpha - beta);
+      }
+      s_tau = t;
+      s_beta = beta;
+      s_bv = vs;
+      tau[j] = t;
+    }
+    __syncthreads();
+    const double tj = s_tau, scale = s_bv;
+    for (int i = j + 1 + tid; i < R; i += blockDim.x) B[i * R + j] *= scale;
+    __syncthreads();
+    if (tid == 0) B[j * R + j] = s_beta;
+    // apply H = I - tau v v^T (v_j = 1) to the trailing columns
+    if (tj != 0.0) {
+      for (int k = j + 1 + warp; k < R; k += nw) {
+        double w = (lane == 0) ? B[j * R + k] : 0.0;
+        for (int i = j + 1 + lane; i < R; i += 32) w += B[i * R + j] * B[i * R + k];
+        for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
+        w = __shfl_sync(0xffffffffu, w, 0) * tj;
+        if (lane == 0) B[j * R + k] -= w;
+        for (int i = j + 1 + lane; i < R; i += 32) B[i * R + k] -= w * B[i * R + j];
+      }
+    }
+    __syncthreads();
+  }
+  // numerical rank
+  __shared__ int s_rnk;
+  if (tid == 0) {
+    const double r00 = fabs(B[0]), rcond = (double)R * 2.220446049250313e-16;
+    int rnk = 1;
+    while (rnk < R && fabs(B[rnk * R + rnk]) > rcond * r00) ++rnk;
+    if (!(r00 > 0.0)) rnk = 0;
+    s_rnk = rnk;
+    info->qr_rank = rnk;
+  }
+  __syncthreads();
+  const int rnk = s_rnk;
+  // Z = Q^T = H_{R-1} ... H_0 I
+  for (int e = tid; e < R * R; e += blockDim.x) Z[e] = ((e / R) == (e % R)) ? 1.0 : 0.0;
+  __syncthreads();
+  for (int j = 0; j < R; ++j) {
+    const double tj = tau[j];
+    if (tj != 0.0) {
+      for (int k = warp; k < R; k += nw) {
+        double w = (lane == 0) ? Z[j * R + k] : 0.0;
+        for (int i = j + 1 + lane; i < R; i += 32) w += B[i * R + j] * Z[i * R + k];
+        for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
+        w = __shfl_sync(0xffffffffu, w, 0) * tj;
+        if (lane == 0) Z[j * R + k] -= w;
+        for (int i = j + 1 + lane; i < R; i += 32) Z[i * R + k] -= w * B[i * R + j];
+      }
+    }
+    __syncthreads();
+  }
+  if (rnk == R) {
+    // Y = R^{-1} Z, back substitution column by column (columns in parallel)
+    for (int c = tid; c < R; c += blockDim.x) {
+      for (int k = R - 1; k >= 0; --k) {
+        double s = Z[k * R + c];
+        for (int l = k + 1; l < R; ++l) s -= B[k * R + l] * Y[l * R + c];
+        Y[k * R + c] = s / B[k * R + k];
+      }
+    }
+  } else if (rnk > 0) {
+    // minimum-norm: Y = Rt^T (Rt Rt^T)^{-1} Z[0:rnk, :], Rt = upper rows 0..rnk-1 of R.
+    double* S = tau + R;  // rnk x rnk scratch after tau (sized R*R in the workspace)
+    for (int e = tid; e < rnk * rnk; e += blockDim.x) {
+      const int a = e / rnk, b = e % rnk;
+      double s = 0.0;
+      for (int l = max(a, b); l < R; ++l) s += B[a * R + l] * B[b * R + l];
+      S[e] = s;
+    }
+    __syncthreads();
+    // Cholesky S = L L^T (lower, in place), serial over columns
+    for (int j = 0; j < rnk; ++j) {
+      if (tid == 0) {
+        double d = S[j * rnk + j];
+        for (int l = 0; l < j; ++l) d -= S[j * rnk + l] * S[j * rnk + l];
+        S[j * rnk + j] = sqrt(fmax(d, 0.0));
+      }
+      __syncthreads();
+      for (int i = j + 1 + tid; i < rnk; i += blockDim.x) {
+        double s = S[i * rnk + j];
+        for (int l = 0; l < j; ++l) s -= S[i * rnk + l] * S[j * rnk + l];
+        S[i * rnk + j] = s / S[j * rnk + j];
+      }
+      __syncthreads();
+    }
+    // Z1 = S^{-1} Z[0:rnk,:] (columns in parallel), stored in Z rows 0..rnk-1
+    for (int c = tid; c < R; c += blockDim.x) {
+      for (int k = 0; k < rnk; ++k) {
+        double s = Z[k * R + c];
+        for (int l = 0; l < k; ++l) s -= S[k * rnk + l] * Z[l * R + c];
+        Z[k * R + c] = s / S[k * rnk + k];
+      }
+      for (int k = rnk - 1; k >= 0; --k) {
+        double s = Z[k * R + c];
+        for (int l = k + 1; l < rnk; ++l) s -= S[l * rnk + k] * Z[l * R + c];
+        Z[k * R + c] = s / S[k * rnk + k];
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int k = e / R, c = e % R;
+      double s = 0.0;
+      for (int a = 0; a < rnk && a <= k; ++a) s += B[a * R + k] * Z[a * R + c];
+      Y[e] = s;
+    }
+  } else {
+    for (int e = tid; e < R * R; e += blockDim.x) Y[e] = NAN;
+  }
+  __syncthreads();
+  // W = P Y : row perm[k] of W is row k of Y
+  for (int e = tid; e < R * R; e += blockDim.x) {
+    const int k = e / R, c = e % R;
+    W[perm[k] * R + c] = Y[e];
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int skip, int R, double* __restrict__ Aglob,
+                                                  double* __restrict__ U, double* __restrict__ dinv,
+                                                  int* __restrict__ piv, double* __restrict__ W,
+                                                  double* __restrict__ qwork, SolveInfo* info, DevCheck* chk) {
+  if (done_flag(chk)) return;
+  extern __shared__ double smA[];
+  double* A = (R <= 128) ? smA : Aglob;
+  __shared__ double sv[32];
+  __shared__ int si[32];
+  __shared__ double s_ajj;
+  __shared__ int s_p, s_stop;
+  __shared__ int s_piv[CPALS_MAX_RANK_SOLVE];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+
+  // V = ones .* G_a .* G_b ... (mode order, skipping `skip`); upper triangle only
+  for (int e = tid; e < R * R; e += blockDim.x) {
+    const int r = e / R, c = e % R;
+    if (c >= r) {
+      double v = 1.0;
+      for (int m = 0; m < order; ++m)
+        if (m != skip) v *= gs.G[m][e];
+      A[e] = v;
+    }
+  }
+  for (int k = tid; k < R; k += blockDim.x) s_piv[k] = k;
+  __syncthreads();
+
+  int rank = R;
+  for (int j = 0; j < R; ++j) {
+    double bv = -INFINITY;
+    int bi = 0x7fffffff;
+    for (int i = j + tid; i < R; i += blockDim.x) {
+      const double d = A[i * R + i];
+      const double key = isnan(d) ? INFINITY : d, bkey = isnan(bv) ? INFINITY : bv;
+      if (key > bkey || (key == bkey && i < bi)) {
+        bv = d;
+        bi = i;
+      }
+    }
+    double pv;
+    int pi;
+    block_argmax(bv, bi, sv, si, &pv, &pi);
+    if (tid == 0) {
+      s_p = pi;
+      s_ajj = pv;
+      s_stop = !(pv > kCholTol);  // pivot <= tol or NaN
+    }
+    __syncthreads();
+    if (s_stop) {
+      rank = j;
+      break;
+    }
+    const int p = s_p;
+    if (p != j) {
+      // symmetric interchange of j and p on upper storage (dpstf2's three DSWAPs)
+      for (int k = tid; k < R; k += blockDim.x) {
+        if (k < j) {
+          const double t = A[k * R + j];
+          A[k * R + j] = A[k * R + p];
+          A[k * R + p] = t;
+        } else if (k > p) {
+          const double t = A[j * R + k];
+          A[j * R + k] = A[p * R + k];
+          A[p * R + k] = t;
+        } else if (k > j && k < p) {
+          const double t = A[j * R + k];
+          A[j * R + k] = A[k * R + p];
+          A[k * R + p] = t;
+        }
+      }
+      if (tid == 0) {
+        A[p * R + p] = A[j * R + j];
+        const int t = s_piv[j];
+        s_piv[j] = s_piv[p];
+        s_piv[p] = t;
+      }
+    }
+    __syncthreads();
+    const double ajj = sqrt(s_ajj);
+    const double rinv = 1.0 / ajj;
+    if (tid == 0) A[j * R + j] = ajj;
+    for (int k = j + 1 + tid; k < R; k += blockDim.x) A[j * R + k] *= rinv;
+    __syncthreads();
+    for (int i = j + 1 + warp; i < R; i += nw) {
+      const double a = A[j * R + i];
+      for (int k = i + lane; k < R; k += 32) A[i * R + k] = fma(-a, A[j * R + k], A[i * R + k]);
+    }
+    __syncthreads();
+  }
+
+  if (tid == 0) {
+    info->rank = rank;
+    info->fallback = (rank < R) ? 1 : 0;
+    info->qr_rank = rank;
+  }
+  if (rank == R) {
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int r = e / R, c = e % R;
+      U[e] = (c >= r) ? A[e] : 0.0;
+    }
+    for (int k = tid; k < R; k += blockDim.x) {
+      dinv[k] = 1.0 / A[k * R + k];
+      piv[k] = s_piv[k];
+    }
+  } else {
+    if (tid == 0 && chk) atomicAdd(reinterpret_cast<unsigned long long*>(&chk->fallbacks), 1ull);
+    double* B = qwork;
+    double* Z = qwork + (size_t)R * R;
+    double* Y = qwork + 2 * (size_t)R * R;
+    double* tau = qwork + 3 * (size_t)R * R;
+    int* perm = reinterpret_cast<int*>(qwork + 4 * (size_t)R * R + R);
+    double* cn = qwork + 4 * (size_t)R * R + 2 * R;
+    __syncthreads();
+    qr_fallback(gs, order, skip, R, B, Z, Y, tau, perm, W, info, sv, si, cn);
+  }
+}
+
+// ---------------- solve rows ----------------
+template <typename PT, int RQ>
+__global__ void __launch_bounds__(128) k_solve_rows(const PT* __restrict__ part, int S, int64_t In, int R,
+                                                    const double* __restrict__ U, const double* __restrict__ dinv,
+                                                    const int* __restrict__ piv, const double* __restrict__ W,
+                                                    const SolveInfo* __restrict__ info, double* __restrict__ X,
+                                                    double* __restrict__ inner_rows, const DevCheck* chk) {
+  if (done_flag(chk)) return;
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int64_t row = (int64_t)blockIdx.x * wpb + warp;
+  if (row >= In) return;
+  double* m = sm + (size_t)warp * 2 * R;
+  double* xs = m + R;
+  // 1. M row = sum of split partials, in split order
+  for (int k = lane; k < R; k += 32) {
+    double s = 0.0;
+    for (int sp = 0; sp < S; ++sp) s += (double)part[((int64_t)sp * In + row) * R + k];
+    m[k] = s;
+  }
+  __syncwarp();
+  double t[RQ];
+  if (!info->fallback) {
+    // t = m[piv]; forward (U^T) and backward (U) substitution; x[piv] = w
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+      const int j = lane + 32 * q;
+      t[q] = (j < R) ? m[piv[j]] : 0.0;
+    }
+    for (int k = 0; k < R; ++k) {
+      const int qk = k >> 5, owner = k & 31;
+      double tk = 0.0;
+#pragma unroll
+      for (int q = 0; q < RQ; ++q)
+        if (q == qk) tk = t[q];
+      const double c = __shfl_sync(0xffffffffu, tk * dinv[k], owner);
+      const double* Uk = U + (size_t)k * R;
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        const int j = lane + 32 * q;
+        if (j == k) t[q] = c;
+        else if (j > k && j < R) t[q] = fma(-c, Uk[j], t[q]);
+      }
+    }
+    for (int k = R - 1; k >= 0; --k) {
+      const int qk = k >> 5, owner = k & 31;
+      double tk = 0.0;
+#pragma unroll
+      for (int q = 0; q < RQ; ++q)
+        if (q == qk) tk = t[q];
+      const double w = __shfl_sync(0xffffffffu, tk * dinv[k], owner);
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        const int j = lane + 32 * q;
+        if (j == k) t[q] = w;
+        else if (j < k) t[q] = fma(-U[(size_t)j * R + k], w, t[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+      const int j = lane + 32 * q;
+      if (j < R) xs[piv[j]] = t[q];
+    }
+  } else {
+    for (int k = lane; k < R; k += 32) {
+      const double* Wk = W + (size_t)k * R;
+      double s = 0.0;
+      for (int l = 0; l < R; ++l) s = fma(Wk[l], m[l], s);
+      xs[k] = s;
+    }
+  }
+  __syncwarp();
+  double inner = 0.0, comp = 0.0;
+  for (int k = lane; k < R; k += 32) {
+    const double x = xs[k];
+    X[row * R + k] = x;
+    // Neumaier-compensated sum of m .* x
+    const double p = m[k] * x;
+    const double s = inner + p;
+    comp += (fabs(inner) >= fabs(p)) ? ((inner - s) + p) : ((p - s) + inner);
+    inner = s;
+  }
+  if (inner_rows) {
+    for (int off = 16; off > 0; off >>= 1) {
+      const double o = __shfl_down_sync(0xffffffffu, inner, off);
+      const double oc = __shfl_down_sync(0xffffffffu, comp, off);
+      const double s = inner + o;
+      comp += ((fabs(inner) >= fabs(o)) ? ((inner - s) + o) : ((o - s) + inner)) + oc;
+      inner = s;
+    }
+    if (lane == 0) inner_rows[row] = inner + comp;
+  }
+}
+
+// ---------------- gram ----------------
+constexpr int GT = 16;  // tile edge
+__global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int64_t In, int R, int S2,
+                                              int64_t rows_per_split, double* __restrict__ part,
+                                              unsigned* __restrict__ counters, double* __restrict__ G,
+                                              const DevCheck* chk) {
+  if (done_flag(chk)) return;
+  __shared__ double xa[64][GT + 1];
+  __shared__ double xb[64][GT + 1];
+  __shared__ int s_last;
+  const int nt = (R + GT - 1) / GT;
+  // blockIdx.x enumerates upper-triangle tiles (ti <= tj)
+  int t = blockIdx.x, ti = 0;
+  while (t >= nt - ti) {
+    t -= nt - ti;
+    ++ti;
+  }
+  const int tj = ti + t;
+  const int tile = blockIdx.x, s = blockIdx.y;
+  const int a = threadIdx.x / GT, b = threadIdx.x % GT;
+  const int r1 = ti * GT + a, r2 = tj * GT + b;
+  const int64_t rb = (int64_t)s * rows_per_split, re = min(In, rb + rows_per_split);
+  double acc = 0.0;
+  for (int64_t i0 = rb; i0 < re; i0 += 64) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * GT; e += 256) {
+      const int ii = e / GT, c = e % GT;
+      const int64_t i = i0 + ii;
+      const int ca = ti * GT + c, cb = tj * GT + c;
+      xa[ii][c] = (i < re && ca < R) ? X[i * R + ca] : 0.0;
+      xb[ii][c] = (i < re && cb < R) ? X[i * R + cb] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int ii = 0; ii < 64; ++ii) acc = fma(xa[ii][a], xb[ii][b], acc);
+  }
+  part[((size_t)tile * S2 + s) * 256 + threadIdx.x] = acc;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(&counters[tile], 1u) == (unsigned)(S2 - 1));
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double sum = 0.0;
+  for (int q = 0; q < S2; ++q) sum += __ldcg(&part[((size_t)tile * S2 + q) * 256 + threadIdx.x]);
+  if (r1 < R && r2 < R) {
+    G[(size_t)r1 * R + r2] = sum;
+    G[(size_t)r2 * R + r1] = sum;
+  }
+  if (threadIdx.x == 0) counters[tile] = 0u;
+}
+
+// ---------------- finalize ----------------
+__global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Graw, int R, double* __restrict__ lam,
+                                                  double* __restrict__ Gn, GramSet gs, int order, int last,
+                                                  const double* __restrict__ inner_rows, int64_t In, DevCheck* chk,
+                                                  double* __restrict__ traj, int64_t traj_cap) {
+  if (done_flag(chk)) return;
+  __shared__ double sv[32];
+  __shared__ double s_lam[CPALS_MAX_RANK_SOLVE];
+  const int tid = threadIdx.x;
+  for (int r = tid; r < R; r += blockDim.x) {
+    const double l = sqrt(Graw[(size_t)r * R + r]);
+    s_lam[r] = l;
+    lam[r] = l;
+  }
+  __syncthreads();
+  for (int e = tid; e < R * R; e += blockDim.x) {
+    const int r = e / R, c = e % R;
+    Gn[e] = Graw[e] / s_lam[r] / s_lam[c];
+  }
+  if (!last) return;
+  __syncthreads();
+  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28)
+  double s = 0.0, c = 0.0;
+  for (int64_t i = tid; i < In; i += blockDim.x) {
+    const double p = inner_rows[i];
+    const double t = s + p;
+    c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
+    s = t;
+  }
+  const double inner = block_sum(s, sv) + block_sum(c, sv);
+  // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11)
+  s = 0.0;
+  c = 0.0;
+  for (int e = tid; e < R * R; e += blockDim.x) {
+    const int r = e / R, q = e % R;
+    double h = gs.G[0][e];
+    for (int m = 1; m < order; ++m) h *= gs.G[m][e];
+    const double p = h * (s_lam[r] * s_lam[q]);
+    const double t = s + p;
+    c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
+    s = t;
+  }
+  const double fact_square = block_sum(s, sv) + block_sum(c, sv);
+  if (tid != 0) return;
+  DevCheck& k = *chk;
+  double fit = NAN;
+  if (k.ref_norm > 0.0) {
+    const double rn = k.ref_norm;
+    const double nr = sqrt(fabs(rn * rn + fact_square - 2.0 * fabs(inner)));
+    fit = 1.0 - nr / rn;
+  }
+  if (k.sweeps < traj_cap) traj[k.sweeps] = fit;
+  k.sweeps += 1;
+  if (k.kind == CPALS_CHECK_FIT) {
+    k.iter += 1;
+    const double dfit = fabs(k.lastfit - fit);
+    k.lastfit = fit;
+    if (isnan(fit)) {
+      k.nan_flag = 1;
+      k.done = 1;
+      return;
+    }
+    if (dfit < k.tol) {
+      k.counter += 1;
+      if (k.counter >= 2) {
+        k.total_iter = k.iter;
+        k.iter = 0;
+        k.counter = 0;
+        k.final_fit = k.lastfit;
+        k.lastfit = 0.0;
+        k.done = 1;
+        return;
+      }
+    } else {
+      k.counter = 0;
+    }
+    if (k.iter >= k.max_counter) {
+      k.total_iter = k.iter;
+      k.iter = 0;
+      k.counter = 0;
+      k.final_fit = k.lastfit;
+      k.lastfit = 0.0;
+    }
+  } else {
+    k.iter += 1;
+    k.lastfit = fit;
+    if (k.iter == k.max_counter) {
+      k.iter = 0;
+      k.done = 1;
+    }
+  }
+}
+
+// ---------------- normalize ----------------
+__global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam, int64_t In, int R,
+                            double* __restrict__ F, float* __restrict__ F32t, int64_t ld32, const DevCheck* chk) {
+  if (done_flag(chk)) return;
+  const int64_t n = In * R;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int r = (int)(e % R);
+    const double f = lam ? X[e] / lam[r] : X[e];
+    F[e] = f;
+    if (F32t) F32t[(int64_t)r * ld32 + i] = (float)f;
+  }
+}
+
+__global__ void k_transpose(const double* __restrict__ src, int64_t rows, int64_t cols, double* __restrict__ dst) {
+  __shared__ double tile[32][33];
+  const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t r = r0 + y, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[y][threadIdx.x] = src[r * cols + c];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int64_t c = c0 + y, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[c * rows + r] = tile[threadIdx.x][y];
+  }
+}
+
+template <typename PT>
+__global__ void k_reduce_partials(const PT* __restrict__ part, int S, int64_t n, double* __restrict__ M) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int sp = 0; sp < S; ++sp) s += (double)part[(int64_t)sp * n + e];
+    M[e] = s;
+  }
+}
+
+}  // namespace
+
+size_t factorize_work_doubles(int R) { return 5 * (size_t)R * R + 4 * (size_t)R + 64; }
+
+cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, double* work, double* U, int* piv,
+                             double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st) {
+  // work layout: [Aglob R*R][dinv R][qwork 4R^2 + 3R + 64]
+  double* Aglob = work;
+  double* dinv = work + (size_t)R * R;
+  double* qwork = dinv + R;
+  const size_t smem = (R <= 128) ? (size_t)R * R * sizeof(double) : 0;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_factorize, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 128 * 8);
+    attr_set = true;
+  }
+  k_factorize<<<1, FT, smem, st>>>(gs, order, skip, R, Aglob, U, dinv, piv, W, qwork, info, chk);
+  return cudaGetLastError();
+}
+
+int solve_rows_blocks(int64_t In, int R) {
+  (void)R;
+  return (int)((In + 3) / 4);
+}
+
+template <typename PT>
+static cudaError_t solve_rows_dispatch(const PT* part, int S, int64_t In, int R, const double* U, const double* dinv,
+                                       const int* piv, const double* W, const SolveInfo* info, double* X,
+                                       double* inner_rows, const DevCheck* chk, cudaStream_t st) {
+  const int wpb = 4;
+  dim3 grid((unsigned)((In + wpb - 1) / wpb));
+  const size_t smem = (size_t)wpb * 2 * R * sizeof(double);
+  const int rq = (R + 31) / 32;
+#define CPALS_SOLVE_CASE(Q)                                                                                   \
+  if (rq <= Q) {                                                                                              \
+    k_solve_rows<PT, Q><<<grid, 32 * wpb, smem, st>>>(part, S, In, R, U, dinv, piv, W, info, X, inner_rows, chk); \
+    return cudaGetLastError();                                                                                \
+  }
+  CPALS_SOLVE_CASE(1)
+  CPALS_SOLVE_CASE(2)
+  CPALS_SOLVE_CASE(4)
+  CPALS_SOLVE_CASE(8)
+  CPALS_SOLVE_CASE(16)
+#undef CPALS_SOLVE_CASE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
+                              const double* U, const int* piv, const double* W, const SolveInfo* info, double* X,
+                              double* inner_rows, const DevCheck* chk, cudaStream_t st) {
+  const double* dinv = work + (size_t)R * R;
+  if (part_is_f32)
+    return solve_rows_dispatch(static_cast<const float*>(part), splits, In, R, U, dinv, piv, W, info, X, inner_rows,
+                               chk, st);
+  return solve_rows_dispatch(static_cast<const double*>(part), splits, In, R, U, dinv, piv, W, info, X, inner_rows,
+                             chk, st);
+}
+
+int gram_tiles(int R) {
+  const int nt = (R + GT - 1) / GT;
+  return nt * (nt + 1) / 2;
+}
+
+int gram_splits(int64_t In, int R, int num_sms) {
+  const int tiles = gram_tiles(R);
+  int64_t s = (2LL * num_sms + tiles - 1) / tiles;
+  const int64_t max_s = (In + 63) / 64;
+  if (s > max_s) s = max_s;
+  if (s < 1) s = 1;
+  if (s > 512) s = 512;
+  return (int)s;
+}
+
+cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters, double* G,
+                        const DevCheck* chk, cudaStream_t st) {
+  const int64_t rps = (((In + S2 - 1) / S2) + 63) / 64 * 64;
+  dim3 grid((unsigned)gram_tiles(R), (unsigned)S2);
+  k_gram<<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, G, chk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* Gn, const GramSet& gs, int order,
+                            int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
+                            int64_t traj_cap, cudaStream_t st) {
+  k_finalize<<<1, 256, 0, st>>>(Graw, R, lam, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_normalize(const double* X, const double* lam, int64_t In, int R, double* F, float* F32t,
+                             int64_t ld32, const DevCheck* chk, cudaStream_t st) {
+  const int64_t n = In * R;
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam, In, R, F, F32t, ld32, chk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st) {
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  k_transpose<<<grid, dim3(32, 8), 0, st>>>(src, rows, cols, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_partials(const void* part, int part_is_f32, int splits, int64_t In, int R, double* M,
+                                   cudaStream_t st) {
+  const int64_t n = In * R;
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  if (part_is_f32)
+    k_reduce_partials<float><<<blocks, 256, 0, st>>>(static_cast<const float*>(part), splits, n, M);
+  else
+    k_reduce_partials<double><<<blocks, 256, 0, st>>>(static_cast<const double*>(part), splits, n, M);
+  return cudaGetLastError();
+}
+
+}  // namespace cpals

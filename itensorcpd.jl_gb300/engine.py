@@ -1,0 +1,145 @@
+"""Handle-level wrapper of one libcpals context (one tensor, one rank, one GPU)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Engine:
+    """Device state of one CP-ALS problem: the tensor, factors, Grams and the check.
+
+    ``precision``: ``"fp64"`` (plain FP64 MTTKRP, the parity path) or ``"bf16x3"``
+    (tcgen05 split-BF16 MTTKRP with FP32 accumulation; FP64 Gram / solve / fit).
+    """
+
+    def __init__(self, dims, rank, dtype=np.float64, precision="fp64", device=0, graph=True, dimtree=False):
+        self.lib = L.load()
+        self.dims = tuple(int(d) for d in dims)
+        self.order = len(self.dims)
+        self.rank = int(rank)
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in (np.dtype(np.float64), np.dtype(np.float32)):
+            raise TypeError(f"tensor element type must be float64 or float32, got {self.dtype}")
+        self.precision = precision
+        mm = {"fp64": L.MTTKRP_FP64, "bf16x3": L.MTTKRP_BF16X3}[precision]
+        flags = (0 if graph else L.FLAG_NO_GRAPH) | (L.FLAG_DIMTREE if dimtree else 0)
+        d = np.asarray(self.dims, dtype=np.int64)
+        h = C.c_void_p()
+        tdt = L.DTYPE_F64 if self.dtype == np.float64 else L.DTYPE_F32
+        L.check(self.lib.cpals_create(C.byref(h), int(device), self.order, L.i64ptr(d), self.rank, tdt, mm, flags),
+                "cpals_create")
+        self.h = h
+        self._tensor_ref = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cpals_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- data in / out ----
+    def set_tensor(self, T):
+        T = np.asarray(T)
+        if T.shape != self.dims:
+            raise ValueError(f"tensor shape {T.shape} != {self.dims}")
+        Tf = np.asfortranarray(T, dtype=self.dtype)
+        L.check(self.lib.cpals_set_tensor(self.h, Tf.ctypes.data_as(C.c_void_p)), "cpals_set_tensor")
+
+    def set_tensor_device(self, ptr: int, keepalive=None):
+        """Borrow a column-major device buffer (e.g. ``torch_tensor.data_ptr()``)."""
+        self._tensor_ref = keepalive
+        L.check(self.lib.cpals_set_tensor_device(self.h, C.c_void_p(int(ptr))), "cpals_set_tensor_device")
+
+    def set_factors(self, factors, lam=None):
+        fs = [np.asfortranarray(F, dtype=np.float64) for F in factors]
+        for F, d in zip(fs, self.dims):
+            if F.shape != (d, self.rank):
+                raise ValueError(f"factor shape {F.shape} != {(d, self.rank)}")
+        arr = (L._DP * self.order)(*[L.dptr(F) for F in fs])
+        lp = None
+        if lam is not None:
+            lam = np.ascontiguousarray(lam, dtype=np.float64)
+            lp = L.dptr(lam)
+        L.check(self.lib.cpals_set_factors(self.h, arr, lp), "cpals_set_factors")
+
+    def get_factors(self):
+        fs = [np.empty((d, self.rank), dtype=np.float64, order="F") for d in self.dims]
+        lam = np.empty(self.rank, dtype=np.float64)
+        arr = (L._DP * self.order)(*[L.dptr(F) for F in fs])
+        L.check(self.lib.cpals_get_factors(self.h, arr, L.dptr(lam)), "cpals_get_factors")
+        return fs, lam
+
+    def gram(self, mode):
+        G = np.empty((self.rank, self.rank), dtype=np.float64)
+        L.check(self.lib.cpals_get_gram(self.h, int(mode), L.dptr(G)), "cpals_get_gram")
+        return G
+
+    # ---- compute ----
+    def mttkrp(self, mode) -> np.ndarray:
+        M = np.empty((self.dims[mode], self.rank), dtype=np.float64, order="F")
+        L.check(self.lib.cpals_mttkrp(self.h, int(mode), L.dptr(M)), "cpals_mttkrp")
+        return M
+
+    def optimize(self, chk: L.CpalsCheck) -> np.ndarray:
+        """Run sweeps under ``chk`` (updated in place); returns the per-sweep fits."""
+        cap = max(1, int(chk.max_counter) - int(chk.iter))
+        traj = np.full(cap, np.nan)
+        st = self.lib.cpals_optimize(self.h, C.byref(chk), L.dptr(traj), cap)
+        if st == L.CPALS_E_NAN:
+            raise FloatingPointError("Error NAN")
+        L.check(st, "cpals_optimize")
+        return traj[: chk.sweeps_run].copy()
+
+    def fallback_count(self) -> int:
+        n = C.c_int64()
+        L.check(self.lib.cpals_fallback_count(self.h, C.byref(n)), "cpals_fallback_count")
+        return int(n.value)
+
+    def synchronize(self):
+        L.check(self.lib.cpals_synchronize(self.h), "cpals_synchronize")
+
+    # ---- randomized path ----
+    @staticmethod
+    def _pivots(pivots, nother):
+        p = np.asfortranarray(np.asarray(pivots, dtype=np.int64))
+        if p.ndim != 2 or p.shape[1] != nother:
+            raise ValueError(f"pivots must be nsamps x {nother}")
+        return p
+
+    def pivot_hadamard(self, mode, pivots) -> np.ndarray:
+        p = self._pivots(pivots, self.order - 1)
+        out = np.empty((p.shape[0], self.rank), dtype=np.float64, order="F")
+        L.check(self.lib.cpals_pivot_hadamard(self.h, int(mode), L.i64ptr(p), p.shape[0], L.dptr(out)),
+                "cpals_pivot_hadamard")
+        return out
+
+    def fused_flatten_sample(self, mode, pivots) -> np.ndarray:
+        p = self._pivots(pivots, self.order - 1)
+        out = np.empty((self.dims[mode], p.shape[0]), dtype=self.dtype, order="F")
+        L.check(self.lib.cpals_fused_flatten_sample(self.h, int(mode), L.i64ptr(p), p.shape[0],
+                                                    out.ctypes.data_as(C.c_void_p)), "cpals_fused_flatten_sample")
+        return out
+
+    def leverage_scores(self, mode) -> np.ndarray:
+        out = np.empty(self.dims[mode], dtype=np.float64)
+        L.check(self.lib.cpals_leverage_scores(self.h, int(mode), L.dptr(out)), "cpals_leverage_scores")
+        return out
+
+    def sampled_update(self, mode, pivots, normal=False):
+        p = self._pivots(pivots, self.order - 1)
+        L.check(self.lib.cpals_sampled_update(self.h, int(mode), L.i64ptr(p), p.shape[0], int(bool(normal))),
+                "cpals_sampled_update")

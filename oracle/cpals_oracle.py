@@ -1,0 +1,464 @@
+"""CPU oracle for the normal-equation CP-ALS hot path of ITensorCPD.jl (v0.0.82).
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker, never the product: only
+``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl
+reference`` legs of ``bench.py`` may import it.  The shipped engine
+(``itensorcpd.jl_gb300``) never calls into it and fails loudly when its CUDA
+library is missing.
+
+It restates, in FP64 numpy/scipy, each step of the reference's ALS in the
+reference's order.  Every function names the reference file:line it follows
+(paths relative to the ITensorCPD.jl repository root).
+
+Parity pinning
+--------------
+* The reference is Julia, and no Julia toolchain exists on either machine, so
+  the reference itself cannot be run to produce fixtures.
+* The oracle is pinned instead against the reference's own known-answer tests,
+  re-expressed in ``tests/test_oracle.py`` with their literal inputs:
+  - index maps (``test/pivot_mapping.jl:4-43`` literal pivot columns,
+    ``:105-107`` round trip);
+  - loop-defined ``had_contract`` / ``pivot_hadamard`` / ``fused_flatten_sample``
+    (``test/pivot_mapping.jl:46-103``, ``test/basic_features.jl:18-58``);
+  - ``reconstruct`` against explicit loops (``test/basic_features.jl:60-92``);
+  - ``row_norm`` unit columns (``test/basic_features.jl:1-16``);
+  - end-to-end residual bounds of ``test/cp_als.jl:1-54`` (20x30x40, rank 400).
+* Bit-level agreement with Julia is **not** pinned for two things:
+  - the ``MersenneTwister`` random streams (initial factors are always supplied
+    by the caller instead);
+  - the contraction order chosen inside ITensors.jl.
+  Both are pinned to tolerance only.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+from scipy.linalg import lapack
+
+# ITensorCPD.jl src/ITensorCPD.jl:2 -- tolerance of the pivoted Cholesky.
+CHOLESKY_EPSILON = 1e-6
+
+
+# ---------------------------------------------------------------------------
+# Factor initialisation and normalisation
+# ---------------------------------------------------------------------------
+def row_norm(X: np.ndarray):
+    """src/math_tools/row_norm.jl:4-24: lambda_r = sqrt(sum_i X(i,r)^2), F = X ./ lambda."""
+    lam = np.sqrt(np.sum(X * X, axis=0))
+    return X / lam[None, :], lam
+
+
+def random_factors(dims, rank, rng: np.random.Generator):
+    """src/cpd.jl:85-97.
+
+    One iid N(0,1) I_n x R matrix per mode, filled in column-major draw order as
+    Julia's ``randn`` fills it.  Each is column-normalised; the returned lambda
+    is that of the LAST factor (the loop variable ``l`` survives the loop).
+    """
+    factors, lam = [], None
+    for d in dims:
+        X = rng.standard_normal(rank * d).reshape(rank, d).T.copy()
+        F, lam = row_norm(X)
+        factors.append(F)
+    return factors, lam
+
+
+def gram(F: np.ndarray) -> np.ndarray:
+    """post_solve, src/algorithms/als_algorithms/standard/tensor.jl:86-89: G = F^T F."""
+    return F.T @ F
+
+
+def hadamard_of_grams(grams, skip: int) -> np.ndarray:
+    """compute_krp, src/algorithms/als_algorithms/standard/MttkrpAlgorithm.jl:18-31.
+
+    Starts from ones and multiplies the Grams of every mode but ``skip``, in mode order.
+    """
+    V = np.ones_like(grams[0])
+    for i, G in enumerate(grams):
+        if i == skip:
+            continue
+        V = V * G
+    return V
+
+
+# ---------------------------------------------------------------------------
+# MTTKRP
+# ---------------------------------------------------------------------------
+def mttkrp_krp_free(T: np.ndarray, factors, mode: int) -> np.ndarray:
+    """matricize_tensor(::KRPFreeNormal), standard/tensor.jl:72-84 with
+    had_contract(list, r), src/algebra/had_contract.jl:72-124.
+
+    For every rank column r, T is contracted with the vectors F_m[:, r] of every
+    other mode (R independent tensor-times-vector chains, each streaming all of T).
+    """
+    N = T.ndim
+    R = factors[0].shape[1]
+    M = np.empty((T.shape[mode], R))
+    for r in range(R):
+        x = T
+        for m in reversed(range(N)):
+            if m == mode:
+                continue
+            x = np.tensordot(x, factors[m][:, r], axes=([m], [0]))
+        M[:, r] = x
+    return M
+
+
+def khatri_rao(mats) -> np.ndarray:
+    """had_contract(factors, r) of the KRPNormal path, standard/tensor.jl:52-60.
+
+    Rows are indexed by the multi-index of ``mats`` with the FIRST matrix's row
+    index fastest (column-major fusion of the remaining modes).
+    """
+    R = mats[0].shape[1]
+    K = np.ones((1, R))
+    for A in mats:  # first matrix fastest => later matrices vary slowest
+        K = (A[:, None, :] * K[None, :, :]).reshape(-1, R)
+    return K
+
+
+def unfold(T: np.ndarray, mode: int) -> np.ndarray:
+    """Mode-n unfolding T_(n): I_n x prod(other dims), other modes fused column-major."""
+    return np.reshape(np.moveaxis(T, mode, 0), (T.shape[mode], -1), order="F")
+
+
+def mttkrp_krp(T: np.ndarray, factors, mode: int) -> np.ndarray:
+    """matricize_tensor(::KRPNormal), standard/tensor.jl:52-60: T_(n) * KRP."""
+    others = [factors[m] for m in range(T.ndim) if m != mode]
+    return unfold(T, mode) @ khatri_rao(others)
+
+
+# ---------------------------------------------------------------------------
+# Normal-equation solve
+# ---------------------------------------------------------------------------
+def _qr_pivoted_solve(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """``qr(A, ColumnNorm()) \\ B`` (Julia LinearAlgebra, QRPivoted ldiv!).
+
+    Column-pivoted Householder QR; numerical rank is cut where the trailing
+    R diagonal falls below rcond = min(m, n) * eps relative to |R_11| (Julia
+    estimates this incrementally with LAPACK laic1); the truncated system is then
+    solved for its minimum-norm solution (Julia: tzrzf + ormrz).
+    """
+    import scipy.linalg as sla
+
+    m, n = A.shape
+    Q, Rm, piv = sla.qr(A, pivoting=True, mode="economic")
+    rcond = min(m, n) * np.finfo(np.float64).eps
+    d = np.abs(np.diag(Rm))
+    rnk = 1
+    while rnk < min(m, n) and d[rnk] > rcond * d[0]:
+        rnk += 1
+    C = Q.T @ B
+    Y, *_ = np.linalg.lstsq(Rm[:rnk, :], C[:rnk], rcond=None)
+    X = np.empty_like(Y)
+    X[piv] = Y
+    return X
+
+
+def pstrf_upper(V: np.ndarray, tol: float = CHOLESKY_EPSILON):
+    """LAPACK dpstrf('U', V, tol) as called by ``cholesky(Hermitian(V), RowMaximum(), tol)``.
+
+    Returns (U, piv (0-based), rank): P^T V P = U^T U.
+    """
+    c, piv, rank, info = lapack.dpstrf(np.array(V, dtype=np.float64, order="F"), tol=tol, lower=0)
+    return np.triu(c), piv - 1, int(rank)
+
+
+def ldiv_solve(A: np.ndarray, B: np.ndarray):
+    """ldiv_solve!(A, B; factorizeA=true), src/algebra/ldiv_solve.jl:13-29.
+
+    Square A: pivoted Cholesky (RowMaximum, tol = 1e-6, check = true); a rank
+    deficient factor throws, and the catch falls back to column-pivoted QR.
+    Non-square A: pivoted QR least squares.
+    Returns (X, used_fallback).
+    """
+    if A.shape[0] == A.shape[1]:
+        U, piv, rank = pstrf_upper(A)
+        if rank == A.shape[0] and np.all(np.isfinite(U)):
+            # CholeskyPivoted ldiv!: permute rows, potrs, inverse-permute.
+            Bp = B[piv]
+            Y = np.linalg.solve(U.T, Bp)
+            Y = np.linalg.solve(U, Y)
+            X = np.empty_like(Y)
+            X[piv] = Y
+            return X, False
+        return _qr_pivoted_solve(A, B), True
+    return _qr_pivoted_solve(A, B), True
+
+
+def solve_ls_problem(V: np.ndarray, M: np.ndarray):
+    """solve_ls_problem(::MttkrpAlgorithm), MttkrpAlgorithm.jl:34-41: X^T = V \\ M^T."""
+    Xt, fb = ldiv_solve(V, M.T)
+    return Xt.T.copy(), fb
+
+
+# ---------------------------------------------------------------------------
+# Convergence checks
+# ---------------------------------------------------------------------------
+def norm_factors(grams, lam) -> float:
+    """src/converge_checks/converge_checks.jl:5-11: lambda^T (G_1 o G_2 o ...) lambda."""
+    had = grams[0].copy()
+    for G in grams[1:]:
+        had = had * G
+    return float(lam @ had @ lam)
+
+
+@dataclass
+class FitCheck:
+    """src/converge_checks/fit_check.jl:5-20 (mutable struct FitCheck)."""
+
+    tolerance: float
+    max_counter: int
+    ref_norm: float
+    iter: int = 0
+    counter: int = 0
+    lastfit: float = 1.0
+    final_fit: float = 0.0
+    total_iter: int = 0
+    MttKRP: np.ndarray | None = None
+    trajectory: list = field(default_factory=list)
+
+    def check_converge(self, factors, lam, grams, verbose=False) -> bool:
+        """fit_check.jl:24-66."""
+        self.iter += 1
+        inner = float(np.sum(self.MttKRP * (factors[-1] * lam[None, :])))
+        fact_square = norm_factors(grams, lam)
+        norm_res = math.sqrt(abs(self.ref_norm * self.ref_norm + fact_square - 2 * abs(inner)))
+        curr_fit = 1.0 - norm_res / self.ref_norm
+        dfit = abs(self.lastfit - curr_fit)
+        self.lastfit = curr_fit
+        self.trajectory.append(curr_fit)
+        if verbose:
+            print(f"{lam.shape[0]}\t {self.iter} \t {curr_fit} \t {dfit}")
+        if math.isnan(curr_fit):
+            raise FloatingPointError("Error NAN")
+        if dfit < self.tolerance:
+            self.counter += 1
+            if self.counter >= 2:
+                self.total_iter = self.iter
+                self.iter = 0
+                self.counter = 0
+                self.final_fit = self.lastfit
+                self.lastfit = 0.0
+                return True
+        else:
+            self.counter = 0
+        if self.iter >= self.max_counter:
+            self.total_iter = self.iter
+            self.iter = 0
+            self.counter = 0
+            self.final_fit = self.lastfit
+            self.lastfit = 0.0
+        return False
+
+
+@dataclass
+class NoCheck:
+    """src/converge_checks/no_check.jl:1-20."""
+
+    max_counter: int
+    iter: int = 0
+    lastfit: float = -1.0
+
+    def check_converge(self, factors, lam, grams, verbose=False) -> bool:
+        self.iter += 1
+        if verbose:
+            print(f"{lam.shape[0]}\t {self.iter}")
+        if self.iter == self.max_counter:
+            self.iter = 0
+            return True
+        return False
+
+
+# ---------------------------------------------------------------------------
+# ALS driver
+# ---------------------------------------------------------------------------
+def als_optimize(T, factors, lam, check=None, maxiter=None, alg="krp", verbose=False, record=None):
+    """als_optimize -> compute_als -> optimize.
+
+    src/optimizers/als_optimizers/als_optimizer.jl:15-25, 37-55 (defaults: NoCheck(100)),
+    optimizers/als_optimizers/standard/tensor.jl:3-14 (initial Grams),
+    src/optimizers/als_optimizers/optimize.jl:6-35 (sweep loop).
+
+    ``alg`` = "krp_free" (KRPFreeNormal, the reference default) or "krp" (KRPNormal);
+    both compute the same MTTKRP and differ only in rounding order.
+    ``record`` (optional list) receives per-sweep dicts with the MTTKRP of every
+    mode, for per-call parity checks.
+    Returns (factors, lam, check, n_fallbacks).
+    """
+    if check is None:
+        check = NoCheck(100 if maxiter is None else maxiter)
+    mttkrp = mttkrp_krp_free if alg == "krp_free" else mttkrp_krp
+    factors = [np.array(F, dtype=np.float64) for F in factors]
+    lam = np.array(lam, dtype=np.float64)
+    N = T.ndim
+    grams = [gram(F) for F in factors]
+    it = check.iter
+    n_fallbacks = 0
+    while it < check.max_counter:
+        M = None
+        rec = {"mttkrp": []}
+        for n in range(N):
+            V = hadamard_of_grams(grams, n)
+            M = mttkrp(T, factors, n)
+            rec["mttkrp"].append(M)
+            X, fb = solve_ls_problem(V, M)
+            n_fallbacks += int(fb)
+            factors[n], lam = row_norm(X)
+            grams[n] = gram(factors[n])
+        if record is not None:
+            rec["factors"] = [F.copy() for F in factors]
+            rec["lam"] = lam.copy()
+            record.append(rec)
+        if isinstance(check, FitCheck):
+            check.MttKRP = M  # save_mttkrp, fit_check.jl:22
+        if check.check_converge(factors, lam, grams, verbose):
+            break
+        it += 1
+    return factors, lam, check, n_fallbacks
+
+
+def reconstruct(factors, lam) -> np.ndarray:
+    """src/algebra/reconstruct.jl:2-9: lambda * had_contract(factors, r)."""
+    K = khatri_rao(factors) * lam[None, :]
+    dims = [F.shape[0] for F in factors]
+    return np.reshape(K.sum(axis=1), dims, order="F")
+
+
+# ---------------------------------------------------------------------------
+# Randomized leverage-score path
+# ---------------------------------------------------------------------------
+def column_to_multi_coords(col_indices, dims) -> np.ndarray:
+    """src/algebra/pivot_mapping.jl:17-35 (1-based in and out, first mode fastest)."""
+    col = np.asarray(col_indices, dtype=np.int64) - 1
+    out = np.empty((col.shape[0], len(dims)), dtype=np.int64)
+    rem = col.copy()
+    for j, d in enumerate(dims):
+        out[:, j] = rem % d + 1
+        rem //= d
+    return out
+
+
+def multi_coords_to_column(sizes, pivots) -> np.ndarray:
+    """src/algebra/pivot_mapping.jl:42-47."""
+    sizes = list(sizes)
+    strides = [int(np.prod(sizes[: len(sizes) - s])) for s in range(1, len(sizes) + 1)]
+    piv = np.asarray(pivots, dtype=np.int64)
+    return ((piv[:, ::-1] - 1) * np.asarray(strides)[None, :]).sum(axis=1) + 1
+
+
+def pivot_hadamard(mats, pivots) -> np.ndarray:
+    """src/algebra/had_contract.jl:277-295.
+
+    prod = ones(nsamps, R); prod .*= F_m[pivots[:, m], :] for each matrix in order.
+    The left-to-right product order is what the device gather reproduces bit for bit.
+    """
+    piv = np.asarray(pivots, dtype=np.int64)
+    prod = np.ones((piv.shape[0], mats[0].shape[1]), dtype=mats[0].dtype)
+    for j, F in enumerate(mats):
+        prod *= F[piv[:, j] - 1, :]
+    return prod
+
+
+def fused_flatten_sample(T: np.ndarray, k: int, pivots) -> np.ndarray:
+    """src/algebra/pivot_mapping.jl:59-85: As(:, s) = T[p_1, ..., :, ..., p_{N-1}] (mode k free)."""
+    piv = np.asarray(pivots, dtype=np.int64) - 1
+    idx = []
+    j = 0
+    for m in range(T.ndim):
+        if m == k:
+            idx.append(np.arange(T.shape[k])[:, None])
+        else:
+            idx.append(piv[None, :, j])
+            j += 1
+    return np.asfortranarray(T[tuple(idx)])  # I_k x nsamps
+
+
+def leverage_score_probabilities(F: np.ndarray) -> np.ndarray:
+    """src/math_tools/probability.jl:3-10: row sums of |Q|^2 over min(dims), Q from thin QR."""
+    Q, _ = np.linalg.qr(F, mode="reduced")
+    return np.sum(Q * Q, axis=1) / min(F.shape)
+
+
+def sample_factor_matrices(nsamps, skip, probs, rng: np.random.Generator) -> np.ndarray:
+    """src/math_tools/probability.jl:23-33 (1-based indices; weighted draws per other mode).
+
+    StatsBase's stream is not reproducible here; the draws come from ``rng``.
+    """
+    cols = []
+    for m, p in enumerate(probs):
+        if m == skip:
+            continue
+        w = np.abs(p) / np.sum(np.abs(p))
+        cols.append(rng.choice(len(p), size=nsamps, p=w) + 1)
+    return np.stack(cols, axis=1).astype(np.int64)
+
+
+def sampled_solve(S: np.ndarray, Ts: np.ndarray, normal: bool):
+    """solve_ls_problem(::ProjectionAlgorithm), randomized/ProjectionAlgorithm.jl:57-68.
+
+    normal: (S^T S) X = (Ts S)^T; otherwise the tall problem S X = Ts^T.
+    Returns the I_n x R solution.
+    """
+    if normal:
+        Xt, _ = ldiv_solve(S.T @ S, (Ts @ S).T)
+    else:
+        Xt, _ = ldiv_solve(S, Ts.T)
+    return Xt.T.copy()
+
+
+def lev_score_als(T, factors, lam, nsamps, sweeps, rng, normal=False, record=None):
+    """LevScoreSampled path: optimizers/.../randomized/krp_lev_score_sampled.jl:1-40 and
+    algorithms/.../randomized/krp_lev_score_sampled.jl:20-58 (resample every mode, stop_resample = -1),
+    run for a fixed number of sweeps (a FitCheck is not honoured, ProjectionAlgorithm.jl:30-51).
+    ``record`` receives the per-mode pivots so a device run can replay them.
+    """
+    factors = [np.array(F, dtype=np.float64) for F in factors]
+    N = T.ndim
+    probs = [leverage_score_probabilities(F) for F in factors]
+    for _ in range(sweeps):
+        for n in range(N):
+            piv = sample_factor_matrices(nsamps, n, probs, rng)
+            others = [factors[m] for m in range(N) if m != n]
+            S = pivot_hadamard(others, piv)
+            Ts = fused_flatten_sample(T, n, piv)
+            X = sampled_solve(S, Ts, normal)
+            factors[n], lam = row_norm(X)
+            probs[n] = leverage_score_probabilities(factors[n])
+            if record is not None:
+                record.append({"mode": n, "pivots": piv, "factor": factors[n].copy(), "lam": lam.copy()})
+    return factors, lam
+
+
+# ---------------------------------------------------------------------------
+# Synthetic low-rank-plus-noise generator (the benchmark workloads' tensors)
+# ---------------------------------------------------------------------------
+def congruent_factor(dim, rank, congruence, rng) -> np.ndarray:
+    """I x R factor with unit columns and pairwise column inner product ``congruence``.
+
+    iid N(0,1) entries are orthonormalised (QR), then mixed by the transposed
+    Cholesky factor of C = (1 - c) I + c 11^T, so A^T A = C exactly.
+    """
+    Z = rng.standard_normal((dim, rank))
+    Q, _ = np.linalg.qr(Z)
+    C = (1.0 - congruence) * np.eye(rank) + congruence * np.ones((rank, rank))
+    L = np.linalg.cholesky(C)
+    return Q @ L.T
+
+
+def lowrank_plus_noise(dims, rank, congruence, snr_db, rng, wmin=1.0, wmax=10.0, dtype=np.float32):
+    """Sum of ``rank`` weighted rank-1 terms (weights U[wmin, wmax]) plus iid Gaussian
+    noise at ``snr_db``.  Returns (T column-major, true factors, weights)."""
+    facs = [congruent_factor(d, rank, congruence, rng) for d in dims]
+    w = rng.uniform(wmin, wmax, size=rank)
+    A0 = facs[0] * w[None, :]
+    K = khatri_rao(facs[1:])
+    S = (A0 @ K.T).astype(dtype)  # I_1 x prod(rest), column-major fusion
+    sn = float(np.linalg.norm(S))
+    noise = rng.standard_normal(S.shape).astype(dtype)
+    nn = float(np.linalg.norm(noise))
+    S += noise * dtype(sn / nn / (10.0 ** (snr_db / 20.0)))
+    T = np.reshape(S, dims, order="F")
+    return np.asfortranarray(T), facs, w

@@ -1,0 +1,117 @@
+"""Generate the golden fixtures under tests/golden/ (run from the repo root:
+``python tests/golden/make_golden.py``).
+
+The reference (Julia) cannot run on either machine, so the fixtures come from:
+  * literal inputs of the reference's own tests, with answers defined independently of
+    the oracle (Julia column-major reshape == numpy ``unravel_index(order="F")``,
+    explicit loops) -- test/pivot_mapping.jl:4-43, 46-107;
+  * the oracle (tests pin the oracle against the reference's known-answer tests first)
+    run on inputs from ``det_normal``, a platform-independent generator, so the GPU machine
+    regenerates exactly the same inputs without shipping large arrays.
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "oracle"))
+sys.path.insert(0, str(ROOT / "tests"))
+
+import cpals_oracle as oracle  # noqa: E402
+from _data import det_factors, det_normal  # noqa: E402
+
+
+def index_maps():
+    # test/pivot_mapping.jl:6-43, literal pivot columns and dims
+    cases = [
+        {"tensor_dims": [4, 5, 6, 3], "mode": 1, "col_dims": [5, 6, 3],
+         "pivots": [1, 4, 7, 12, 29, 30, 8, 21, 17, 42, 62, 86, 72]},
+        {"tensor_dims": [3, 6, 8, 2], "mode": 3, "col_dims": [3, 6, 2],
+         "pivots": [1, 3, 7, 14, 29, 30, 10, 22, 35, 8, 11]},
+    ]
+    for c in cases:
+        coords = np.stack(np.unravel_index(np.asarray(c["pivots"]) - 1, c["col_dims"], order="F"), axis=1) + 1
+        c["coords"] = coords.tolist()
+    return cases
+
+
+def als_small():
+    dims, R = (12, 13, 7), 5
+    T = np.asfortranarray(det_normal(11, dims))
+    F, lam = det_factors(dims, R, seed=3)
+    rec = []
+    chk = oracle.FitCheck(1e-10, 8, float(np.linalg.norm(T)))
+    Ff, lf, chk, fb = oracle.als_optimize(T, F, lam, check=chk, record=rec)
+    return {
+        "dims": list(dims), "rank": R, "tensor_seed": 11, "factor_seed": 3,
+        "tol": 1e-10, "max_counter": 8,
+        "trajectory": chk.trajectory, "total_iter": chk.total_iter, "final_fit": chk.final_fit,
+        "mttkrp_sweep1": [m.tolist() for m in rec[0]["mttkrp"]],
+        "final_factors": [f.tolist() for f in Ff], "final_lambda": lf.tolist(), "fallbacks": fb,
+    }
+
+
+def als_c1():
+    # The reference's CPU-runnable workload: 100^3 FP64 N(0,1), rank 50,
+    # FitCheck(1e-3, 100, norm(T)), random_CPD initial factors.
+    dims, R = (100, 100, 100), 50
+    T = np.asfortranarray(det_normal(1, dims))
+    F, lam = det_factors(dims, R, seed=3)
+    chk = oracle.FitCheck(1e-3, 100, float(np.linalg.norm(T)))
+    _, _, chk, fb = oracle.als_optimize(T, F, lam, check=chk)
+    return {"dims": list(dims), "rank": R, "tensor_seed": 1, "factor_seed": 3, "tol": 1e-3, "max_counter": 100,
+            "trajectory": chk.trajectory, "total_iter": chk.total_iter, "final_fit": chk.final_fit,
+            "fallbacks": fb}
+
+
+def rank_deficient():
+    # Duplicated factor columns make every Hadamard of Grams singular: the pivoted
+    # Cholesky stops early and the solve takes the pivoted-QR path (ldiv_solve.jl:17-22).
+    dims, R = (9, 8, 7), 4
+    T = np.asfortranarray(det_normal(21, dims))
+    F, lam = det_factors(dims, R, seed=22)
+    for f in F:
+        f[:, 3] = f[:, 2]
+    rec = []
+    chk = oracle.NoCheck(1)
+    Ff, lf, _, fb = oracle.als_optimize(T, F, lam, check=chk, record=rec)
+    return {"dims": list(dims), "rank": R, "tensor_seed": 21, "factor_seed": 22, "fallbacks": fb,
+            "factors_after_sweep1": [f.tolist() for f in Ff], "lambda": lf.tolist()}
+
+
+def lev_small():
+    # test/rand_cp_als.jl:98-121: 12x13x3 exact rank-5 target, LevScoreSampled.
+    dims, R = (12, 13, 3), 5
+    Ft, lt = det_factors(dims, R, seed=31)
+    T = np.asfortranarray(oracle.reconstruct(Ft, lt))
+    F, lam = det_factors(dims, R, seed=32)
+    out = {"dims": list(dims), "rank": R, "truth_seed": 31, "factor_seed": 32, "runs": []}
+    for normal, nsamps in ((True, 100), (False, 100)):
+        rec = []
+        Ff, lf = oracle.lev_score_als(T, F, lam, nsamps, 3, np.random.default_rng(33), normal=normal, record=rec)
+        out["runs"].append({
+            "normal": normal, "nsamps": nsamps,
+            "steps": [{"mode": r["mode"], "pivots": r["pivots"].tolist(), "factor": r["factor"].tolist(),
+                       "lambda": r["lam"].tolist()} for r in rec],
+            "rel_error": float(np.linalg.norm(oracle.reconstruct(Ff, lf) - T) / np.linalg.norm(T)),
+        })
+    return out
+
+
+def main():
+    (HERE / "index_maps.json").write_text(json.dumps(index_maps()))
+    (HERE / "als_small.json").write_text(json.dumps(als_small()))
+    (HERE / "als_c1.json").write_text(json.dumps(als_c1()))
+    (HERE / "rank_deficient.json").write_text(json.dumps(rank_deficient()))
+    (HERE / "lev_small.json").write_text(json.dumps(lev_small()))
+    for p in sorted(HERE.glob("*.json")):
+        print(p.name, p.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

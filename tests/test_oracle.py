@@ -1,0 +1,194 @@
+"""The oracle pinned against the reference's own known-answer tests (CPU only).
+
+Each test re-expresses one test of ITensorCPD.jl with its literal inputs where the
+reference gives them (test/pivot_mapping.jl, test/basic_features.jl, test/cp_als.jl).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from _data import det_factors, det_normal
+
+
+def test_column_to_multi_coords_literal_pivots(oracle, golden_dir):
+    # test/pivot_mapping.jl:6-43: T_matrix[a, pivot] == T[a, coords...] for literal pivots
+    for case in json.loads((golden_dir / "index_maps.json").read_text()):
+        coords = oracle.column_to_multi_coords(case["pivots"], case["col_dims"])
+        assert coords.tolist() == case["coords"]
+        dims, k = case["tensor_dims"], case["mode"] - 1
+        T = np.asfortranarray(det_normal(5, dims))
+        Tm = oracle.unfold(T, k)
+        for p, c in zip(case["pivots"], coords):
+            idx = list(c - 1)
+            idx.insert(k, slice(None))
+            assert np.array_equal(Tm[:, p - 1], T[tuple(idx)])
+
+
+def test_multi_coords_round_trip(oracle):
+    # test/pivot_mapping.jl:105-107
+    rng = np.random.default_rng(0)
+    dims = (100, 150, 200)
+    p = rng.integers(1, 100 * 150 * 200 + 1, size=200)
+    multi = oracle.column_to_multi_coords(p, dims)
+    assert np.array_equal(oracle.multi_coords_to_column(dims, multi), p)
+
+
+def test_pivot_hadamard_equals_krp_rows(oracle):
+    # test/pivot_mapping.jl:46-103: sampled rows of the explicit KRP, exactly
+    A = det_normal(1, (100, 20))
+    B = det_normal(2, (150, 20))
+    C = det_normal(3, (200, 20))
+    exact = oracle.khatri_rao([A, B])
+    p = np.arange(1, 100 * 150 + 1)
+    piv = oracle.column_to_multi_coords(p, (100, 150))
+    assert np.array_equal(oracle.pivot_hadamard([A, B], piv), exact)
+    rng = np.random.default_rng(1)
+    p = rng.integers(1, 100 * 150 * 200 + 1, size=200)
+    piv = oracle.column_to_multi_coords(p, (100, 150, 200))
+    exact3 = oracle.khatri_rao([A, B, C])
+    loop = np.empty((200, 20))
+    for s in range(200):
+        for r in range(20):
+            loop[s, r] = A[piv[s, 0] - 1, r] * B[piv[s, 1] - 1, r] * C[piv[s, 2] - 1, r]
+    got = oracle.pivot_hadamard([A, B, C], piv)
+    assert np.array_equal(got, loop)
+    assert np.array_equal(got, exact3[p - 1])
+
+
+def test_fused_flatten_sample_equals_fibres(oracle):
+    # test/pivot_mapping.jl:103: fibres of the KRP tensor along mode 4
+    A, B, C = det_normal(1, (10, 6)), det_normal(2, (15, 6)), det_normal(3, (20, 6))
+    Kt = np.reshape(oracle.khatri_rao([A, B, C]), (10, 15, 20, 6), order="F")
+    rng = np.random.default_rng(2)
+    piv = oracle.column_to_multi_coords(rng.integers(1, 3001, size=50), (10, 15, 20))
+    got = oracle.fused_flatten_sample(np.asfortranarray(Kt), 3, piv)
+    assert got.shape == (6, 50)
+    for s in range(50):
+        a, b, c = piv[s] - 1
+        assert np.array_equal(got[:, s], Kt[a, b, c, :])
+    # a middle mode
+    T = np.asfortranarray(det_normal(4, (5, 6, 7, 8)))
+    piv = np.stack([rng.integers(1, d + 1, size=9) for d in (5, 7, 8)], axis=1)
+    got = oracle.fused_flatten_sample(T, 1, piv)
+    for s in range(9):
+        assert np.array_equal(got[:, s], T[piv[s, 0] - 1, :, piv[s, 1] - 1, piv[s, 2] - 1])
+
+
+def test_khatri_rao_matches_loops(oracle):
+    # test/basic_features.jl:18-58: had_contract(A, B, r) against explicit loops
+    A, B = det_normal(1, (20, 40)), det_normal(2, (30, 40))
+    K = oracle.khatri_rao([A, B])
+    D = np.empty((20, 30, 40))
+    for n in range(40):
+        for l_ in range(20):
+            for m in range(30):
+                D[l_, m, n] = A[l_, n] * B[m, n]
+    assert np.linalg.norm(K - D.reshape(600, 40, order="F")) / np.linalg.norm(D) < 1e-7
+
+
+def test_reconstruct_matches_loops(oracle):
+    # test/basic_features.jl:60-92
+    A, B, C = det_normal(1, (20, 10)), det_normal(2, (30, 10)), det_normal(3, (40, 10))
+    lam = det_normal(4, (10,))
+    exact = np.einsum("r,ir,jr,kr->ijk", lam, A, B, C)
+    rec = oracle.reconstruct([A, B, C], lam)
+    assert abs(1.0 - np.linalg.norm(exact - rec) / np.linalg.norm(exact) - 1.0) <= 5 * np.finfo(float).eps
+
+
+def test_row_norm_unit_columns(oracle):
+    # test/basic_features.jl:1-16
+    F, lam = oracle.row_norm(det_normal(7, (20, 30)))
+    assert np.allclose(np.sum(F * F, axis=0), 1.0)
+    assert np.allclose(lam, np.linalg.norm(det_normal(7, (20, 30)), axis=0))
+
+
+def test_mttkrp_forms_agree(oracle):
+    # KRPFreeNormal (per-r chains) and KRPNormal (explicit KRP) compute the same MTTKRP
+    T = np.asfortranarray(det_normal(8, (4, 5, 6, 3)))
+    F, _ = det_factors(T.shape, 7, seed=9)
+    for n in range(4):
+        a = oracle.mttkrp_krp_free(T, F, n)
+        b = oracle.mttkrp_krp(T, F, n)
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-13
+
+
+def test_pivoted_cholesky_solve_and_fallback(oracle):
+    # ldiv_solve.jl:13-29: full-rank SPD -> pivoted Cholesky; singular -> pivoted QR
+    X = det_normal(3, (30, 6))
+    V = X.T @ X
+    B = det_normal(4, (6, 9))
+    sol, fb = oracle.ldiv_solve(V, B)
+    assert not fb
+    assert np.allclose(sol, np.linalg.solve(V, B), rtol=1e-10, atol=1e-12)
+    X[:, 5] = X[:, 4]
+    V = X.T @ X
+    sol, fb = oracle.ldiv_solve(V, V @ B)
+    assert fb
+    assert np.allclose(V @ sol, V @ B, atol=1e-8)
+
+
+def test_fitcheck_control_flow(oracle):
+    # fit_check.jl:24-66: converge after two consecutive |dfit| < tol; iter resets
+    chk = oracle.FitCheck(1e-3, 10, 1.0)
+    lam = np.array([1.0])
+    F = [np.ones((1, 1))]
+    seq = []
+
+    def run(inner):
+        chk.MttKRP = np.array([[inner]])
+        return chk.check_converge(F, lam, [np.ones((1, 1))], verbose=False)
+
+    # ||X||^2 = 1, ref = 1: fit = 1 - sqrt(|2 - 2 inner|), so inner = 1 - (1 - fit)^2 / 2;
+    # fits 0, 0.5, 0.9, 0.9995, 0.9999, 0.99995: |dfit| < 1e-3 on the last two sweeps only
+    for fit in (0.0, 0.5, 0.9, 0.9995, 0.9999, 0.99995):
+        inner = 1.0 - (1.0 - fit) ** 2 / 2.0
+        seq.append(run(inner))
+    assert seq == [False, False, False, False, False, True]
+    assert chk.iter == 0 and chk.total_iter == 6 and chk.counter == 0 and chk.lastfit == 0.0
+    with pytest.raises(FloatingPointError):
+        run(np.nan)
+
+
+def test_leverage_scores(oracle):
+    F, _ = det_factors((40, 7), 7, seed=5)
+    p = oracle.leverage_score_probabilities(F[0])
+    assert p.shape == (40,)
+    assert np.isclose(p.sum(), 1.0)
+    Q, _ = np.linalg.qr(F[0])
+    assert np.allclose(p, np.sum(Q * Q, axis=1) / 7)
+
+
+def test_golden_fixtures_reproduce(oracle, golden_dir):
+    small = json.loads((golden_dir / "als_small.json").read_text())
+    T = np.asfortranarray(det_normal(small["tensor_seed"], small["dims"]))
+    F, lam = det_factors(small["dims"], small["rank"], seed=small["factor_seed"])
+    chk = oracle.FitCheck(small["tol"], small["max_counter"], float(np.linalg.norm(T)))
+    oracle.als_optimize(T, F, lam, check=chk)
+    assert np.allclose(chk.trajectory, small["trajectory"], rtol=0, atol=1e-12)
+
+
+def test_cp_als_overcomplete_rank400(oracle):
+    # test/cp_als.jl:9-10: 20x30x40 FP64, rank 400, 100 NoCheck sweeps -> rel err < 1e-7
+    T = np.asfortranarray(det_normal(40, (20, 30, 40)))
+    F, lam = det_factors(T.shape, 400, seed=3)
+    Ff, lf, _, _ = oracle.als_optimize(T, F, lam, check=oracle.NoCheck(100))
+    assert np.linalg.norm(oracle.reconstruct(Ff, lf) - T) / np.linalg.norm(T) < 1e-7
+
+
+def test_lev_score_sampled_converges(oracle):
+    # test/rand_cp_als.jl:98-121: exact rank-5 12x13x3 target, LevScoreSampled(100);
+    # best of three tries (the reference's multiple_tries helper, rand_cp_als.jl:1-14)
+    dims = (12, 13, 3)
+    Ft, lt = det_factors(dims, 5, seed=31)
+    T = np.asfortranarray(oracle.reconstruct(Ft, lt))
+    F, lam = det_factors(dims, 5, seed=32)
+    best = 1.0
+    for trial in range(3):
+        Ff, lf = oracle.lev_score_als(T, F, lam, 100, 100, np.random.default_rng(100 + trial), normal=True)
+        best = min(best, np.linalg.norm(oracle.reconstruct(Ff, lf) - T) / np.linalg.norm(T))
+    assert best < 0.1
+    # the sampled system is consistent for an exact target: from the true factors a
+    # sampled sweep reproduces them
+    Ff, lf = oracle.lev_score_als(T, Ft, lt, 100, 1, np.random.default_rng(7), normal=False)
+    assert np.linalg.norm(oracle.reconstruct(Ff, lf) - T) / np.linalg.norm(T) < 1e-10

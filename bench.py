@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""CP-ALS benchmark of the GB300 engine (one JSON line on rank 0).
+
+Workload: order-3 FP32 tensor 512 x 512 x 512, the sum of 64 weighted rank-1 terms
+(unit factor columns, pairwise congruence 0.5, weights U[1, 10]) plus Gaussian noise
+at 20 dB SNR; rank-64 ALS, 50 sweeps, split-BF16 tcgen05 MTTKRP with FP64 Gram /
+Cholesky / fit.  A step is one full 50-sweep decomposition from the same initial
+factors.  Synthetic data from a fixed seed (no dataset exists for this workload).
+
+  value  sweeps/s with the tensor resident in HBM (CUDA events on the engine's stream)
+  e2e    sweeps/s through the public API with the tensor in pinned host memory: every
+         step copies it in, decomposes and copies the factors out
+  roofline  the MTTKRP kernel: algorithmic bytes per launch / its CUDA-event duration
+
+``--impl reference`` times the reference's CPU algorithm (the oracle's restatement of
+the KRP-free normal-equation ALS, the reference default) on the host cores instead.
+With N > 1 processes every rank runs an independent replica on its own GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DIMS = (512, 512, 512)
+RANK = 64
+CONGRUENCE = 0.5
+SNR_DB = 20.0
+SWEEPS = 50
+SEED = 2024
+WORKLOAD = "cpals_512x512x512_fp32_rank64_lowrank_noise_20dB"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparator and CPU baseline legs")
+    ap.add_argument("--profile-mttkrp", action="store_true",
+                    help="only set up the workload and run one MTTKRP per mode (a small case for ncu)")
+    return ap.parse_args()
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_tensor(pkg, out=None):
+    from itensorcpd_gb300.synthetic import lowrank_plus_noise
+
+    rng = np.random.default_rng(SEED)
+    T, _, _ = lowrank_plus_noise(DIMS, RANK, CONGRUENCE, SNR_DB, rng, dtype=np.float32, out=out)
+    return T
+
+
+def pinned_like(shape):
+    """Pinned column-major float32 host buffer (torch is only the allocator here)."""
+    try:
+        import torch
+
+        t = torch.empty(int(np.prod(shape)), dtype=torch.float32, pin_memory=True)
+        flat = t.numpy()
+        return np.reshape(flat, shape, order="F"), t
+    except Exception:
+        return np.empty(shape, dtype=np.float32, order="F"), None
+
+
+def mttkrp_alg_bytes(dims, R, mode, esize=4):
+    n = int(np.prod(dims))
+    return n * esize + sum(d * R * 4 for m, d in enumerate(dims) if m != mode) + dims[mode] * R * 4
+
+
+def traffic_from_profiles():
+    p = ROOT / "profiles" / "mttkrp_bf16x3_512cube_r64.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dram_bytes_per_launch"])
+        except Exception:
+            return None
+    return None
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU algorithm on the host cores: one step = one KRP-free sweep."""
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cpals_oracle as oracle  # the reference arm runs the oracle restatement
+
+    pkg = __import__("__graft_entry__").load_package()
+    T = make_tensor(pkg)
+    F, lam = oracle.random_factors(DIMS, RANK, np.random.default_rng(3))
+    cores = os.cpu_count() or 1
+    times = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        F, lam, _, _ = oracle.als_optimize(T, F, lam, check=oracle.NoCheck(1), alg="krp_free",
+                                           work_dtype=np.float32)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    t = sum(times)
+    value = args.steps / t
+    line = {
+        "metric": "cp_als_sweeps_per_s", "value": value, "unit": "sweeps/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "dims": list(DIMS), "rank": RANK, "sweeps_per_step": 1,
+                   "algorithm": "KRP-free normal-equation ALS (reference default), numpy/OpenBLAS"},
+        "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full sweeps of the workload, one per step"},
+        "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(pkg, T):
+    """Bounded sample of the reference's CPU path: 3 KRP-free sweeps on the host cores."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cpals_oracle as oracle
+
+    F, lam = oracle.random_factors(DIMS, RANK, np.random.default_rng(3))
+    t0 = time.perf_counter()
+    oracle.als_optimize(T, F, lam, check=oracle.NoCheck(3), alg="krp_free", work_dtype=np.float32)
+    dt = time.perf_counter() - t0
+    return {"value": 3.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": "3 sweeps of the KRP-free normal-equation ALS (reference default) on the full "
+                      "512^3 workload, FP32 data, numpy/OpenBLAS on all host threads"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import __graft_entry__
+
+    pkg = __graft_entry__.load_package()
+    from itensorcpd_gb300 import _lib as L
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        dist = td
+    device = local if world > 1 else 0
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    T_host, keep = pinned_like(DIMS)
+    make_tensor(pkg, out=T_host)
+    if args.profile_mttkrp:
+        F0, lam0 = pkg.random_factors(DIMS, RANK, np.random.default_rng(3))
+        with pkg.Engine(DIMS, RANK, dtype=np.float32, precision="bf16x3", device=device) as e:
+            e.set_tensor(T_host)
+            e.set_factors(F0, lam0)
+            for n in range(3):
+                e.mttkrp(n)
+        print(json.dumps({"profile_mttkrp": "ok", "launches": 3}))
+        return
+    ref_norm = float(np.linalg.norm(T_host.reshape(-1).astype(np.float64)))
+    F0, lam0 = pkg.random_factors(DIMS, RANK, np.random.default_rng(3))
+
+    def nocheck():
+        c = L.CpalsCheck()
+        c.kind = L.CHECK_NONE
+        c.max_counter = SWEEPS
+        c.ref_norm = ref_norm
+        return c
+
+    eng = pkg.Engine(DIMS, RANK, dtype=np.float32, precision="bf16x3", device=device)
+    eng.set_tensor(T_host)
+
+    def step():
+        eng.set_factors(F0, lam0)
+        return eng.optimize(nocheck())
+
+    # ---- device-resident timed region
+    for _ in range(max(3, args.warmup)):
+        traj = step()
+    barrier()
+    eng.synchronize()
+    l0 = eng.launch_count()
+    with ClockSampler(device) as clk:
+        eng.timer_start()
+        for _ in range(args.steps):
+            traj = step()
+        ms = eng.timer_stop()
+    eng.synchronize()
+    barrier()
+    launches = eng.launch_count() - l0
+    ms = max_over_ranks(ms)
+    final_fit = float(traj[-1])
+    value = world * args.steps * SWEEPS / (ms / 1e3)
+
+    # ---- MTTKRP kernel duration (CUDA events around every launch, one profiled step)
+    eng.set_profiling(True)
+    step()
+    mt_ms, mt_n = eng.profile_read()
+    eng.set_profiling(False)
+    mt_avg_s = mt_ms / max(1, mt_n) / 1e3
+    alg_bytes = float(np.mean([mttkrp_alg_bytes(DIMS, RANK, n) for n in range(3)]))
+    flops = 2.0 * np.prod(DIMS) * RANK
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / mt_avg_s / 1e9
+    traffic = traffic_from_profiles()
+
+    # ---- end to end through the public API (pinned host tensor in, factors out)
+    def step_e2e():
+        eng.set_tensor(T_host)
+        eng.set_factors(F0, lam0)
+        eng.optimize(nocheck())
+        return eng.get_factors()
+
+    for _ in range(2):
+        step_e2e()
+    barrier()
+    eng.synchronize()
+    eng.timer_start()
+    for _ in range(args.steps):
+        step_e2e()
+    e2e_ms = max_over_ranks(eng.timer_stop())
+    e2e_value = world * args.steps * SWEEPS / (e2e_ms / 1e3)
+    fac_bytes = sum(d * RANK * 8 for d in DIMS) + RANK * 8
+    eng.close()
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # plain FP64 GPU ALS on the same tensor and start (the comparator)
+        e64 = pkg.Engine(DIMS, RANK, dtype=np.float32, precision="fp64", device=device)
+        e64.set_tensor(T_host)
+        e64.set_factors(F0, lam0)
+        e64.synchronize()
+        e64.timer_start()
+        traj64 = e64.optimize(nocheck())
+        ms64 = e64.timer_stop()
+        e64.close()
+        extras["fp64_gpu_sweeps_per_s"] = SWEEPS / (ms64 / 1e3)
+        extras["final_fit_fp64"] = float(traj64[-1])
+        extras["final_fit_diff_vs_fp64"] = abs(final_fit - float(traj64[-1]))
+        extras["max_fit_diff_vs_fp64"] = float(np.max(np.abs(traj - traj64)))
+        extras["speedup_vs_fp64_gpu"] = value / world / extras["fp64_gpu_sweeps_per_s"]
+        cpu = cpu_baseline_sample(pkg, T_host)
+    else:
+        cpu = None
+
+    if rank != 0:
+        return
+    line = {
+        "metric": "cp_als_sweeps_per_s",
+        "value": value,
+        "unit": "sweeps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(3, args.warmup),
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16x3/f32-accumulate mttkrp, f64 solve",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "dims": list(DIMS), "rank": RANK, "congruence": CONGRUENCE,
+                   "snr_db": SNR_DB, "sweeps_per_step": SWEEPS, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (BF16 planes 1.07 GB, FP32 tensor 537 MB)"},
+        "final_fit": final_fit,
+        "mttkrp": {"avg_launch_us": mt_avg_s * 1e6, "launches_timed": mt_n, "hbm_gbs": achieved,
+                   "tflops": flops / mt_avg_s / 1e12, "effective_tflops_3_products": 3 * flops / mt_avg_s / 1e12},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind},
+        "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(T_host.nbytes + fac_bytes),
+                "d2h_bytes_per_step": int(fac_bytes)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    line.update(extras)
+    print(json.dumps(line), flush=True)
+    del keep
+
+
+if __name__ == "__main__":
+    main()

@@ -120,6 +120,19 @@ int cpals_fallback_count(cpals_ctx* ctx, int64_t* count);
 /* Synchronise the handle's stream (for timing). */
 int cpals_synchronize(cpals_ctx* ctx);
 
+/* ---- measurement helpers (no counterpart in the reference) ---- */
+
+/* CUDA-event timer on the handle's stream: start, then stop returns the elapsed ms. */
+int cpals_timer_start(cpals_ctx* ctx);
+int cpals_timer_stop(cpals_ctx* ctx, double* elapsed_ms);
+/* Profiling mode: sweeps are launched kernel by kernel (no CUDA graph) with a CUDA
+ * event pair around every MTTKRP launch.  cpals_profile_read returns the summed MTTKRP
+ * kernel time and the number of timed launches since profiling was switched on. */
+int cpals_set_profiling(cpals_ctx* ctx, int on);
+int cpals_profile_read(cpals_ctx* ctx, double* mttkrp_ms, int64_t* launches);
+/* Kernel launches enqueued by this handle so far (every libcpals kernel). */
+int cpals_launch_count(cpals_ctx* ctx, int64_t* launches);
+
 /* ---- randomized leverage-score path (LevScoreSampled) ---- */
 
 /* Sampled Khatri-Rao rows: out(s, r) = prod_{m != mode, in mode order} F_m(pivots(s, j_m), r),

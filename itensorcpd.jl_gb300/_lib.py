@@ -61,6 +61,11 @@ SIGNATURES = {
     "cpals_optimize": (C.c_int, [_P, C.POINTER(CpalsCheck), _DP, C.c_int64]),
     "cpals_fallback_count": (C.c_int, [_P, _I64P]),
     "cpals_synchronize": (C.c_int, [_P]),
+    "cpals_timer_start": (C.c_int, [_P]),
+    "cpals_timer_stop": (C.c_int, [_P, _DP]),
+    "cpals_set_profiling": (C.c_int, [_P, C.c_int]),
+    "cpals_profile_read": (C.c_int, [_P, _DP, _I64P]),
+    "cpals_launch_count": (C.c_int, [_P, _I64P]),
     "cpals_pivot_hadamard": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _DP]),
     "cpals_fused_flatten_sample": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _P]),
     "cpals_leverage_scores": (C.c_int, [_P, C.c_int, _DP]),

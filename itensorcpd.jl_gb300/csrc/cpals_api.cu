@@ -29,6 +29,8 @@ struct cpals_ctx {
   double* F[kMaxOrder] = {};
   float* F32t[kMaxOrder] = {};
   int64_t ld32[kMaxOrder] = {};
+  float* F32r[kMaxOrder] = {};  // row-major FP32 copies (tensor-core path)
+  int64_t rpad = 0;
   double* G[kMaxOrder] = {};
   double* lam = nullptr;
   double* X = nullptr;
@@ -64,6 +66,12 @@ struct cpals_ctx {
   int* derr = nullptr;
   // tensor-core path
   TcState* tc = nullptr;
+  // measurement
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_ev;  // pairs
+  int64_t prof_used = 0;
+  int64_t launches = 0;
 };
 
 namespace {
@@ -113,9 +121,7 @@ cudaError_t enqueue_mttkrp(cpals_ctx* c, int n, const DevCheck* chk) {
   if (c->mmode == CPALS_MTTKRP_FP64)
     return launch_mttkrp_f64(c->dT, c->tdtype, factor_set(c), c->geom[n], c->R, c->splits[n], c->cps[n],
                              static_cast<double*>(c->part), chk, c->st);
-  const float* F32[kMaxOrder] = {};
-  for (int m = 0; m < c->order; ++m) F32[m] = c->F32t[m];
-  return tc_launch_mttkrp(c->tc, n, F32, static_cast<float*>(c->part), chk, c->st);
+  return tc_launch_mttkrp(c->tc, n, static_cast<float*>(c->part), chk, c->st);
 }
 
 int enqueue_sweep(cpals_ctx* c) {
@@ -129,8 +135,15 @@ int enqueue_sweep(cpals_ctx* c) {
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_main[n], 0));
     CPALS_CUDA_TRY(launch_factorize(gs, N, n, R, c->work, c->U, c->piv, c->W, c->info, c->chk, c->side));
     CPALS_CUDA_TRY(cudaEventRecord(c->ev_side[n], c->side));
+    const bool prof = c->profiling && c->prof_used + 2 <= (int64_t)c->prof_ev.size();
+    if (prof) CPALS_CUDA_TRY(cudaEventRecord(c->prof_ev[c->prof_used], c->st));
     CPALS_CUDA_TRY(enqueue_mttkrp(c, n, c->chk));
+    if (prof) {
+      CPALS_CUDA_TRY(cudaEventRecord(c->prof_ev[c->prof_used + 1], c->st));
+      c->prof_used += 2;
+    }
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->st, c->ev_side[n], 0));
+    c->launches += 6;
     CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W, c->info,
                                      c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
     CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->chk, c->st));
@@ -138,8 +151,9 @@ int enqueue_sweep(cpals_ctx* c) {
                                    c->traj_cap, c->st));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
-    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[n], c->F32t[n], c->ld32[n], last ? nullptr : c->chk,
-                                    c->st));
+    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[n], c->F32t[n], c->ld32[n], c->F32r[n], c->rpad,
+                                    last ? nullptr : c->chk, c->st));
+    if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, n, c->F[n], last ? nullptr : c->chk, c->st));
   }
   return CPALS_OK;
 }
@@ -148,7 +162,9 @@ int build_graph(cpals_ctx* c) {
   invalidate_graph(c);
   cudaGraph_t g = nullptr;
   CPALS_CUDA_TRY(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  const int64_t before = c->launches;
   int rc = enqueue_sweep(c);
+  c->launches = before;  // capture enqueues nothing; replays are counted
   cudaError_t e = cudaStreamEndCapture(c->st, &g);
   if (rc != CPALS_OK) {
     if (g) cudaGraphDestroy(g);
@@ -217,6 +233,19 @@ int upload_pivots(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps)
   return CPALS_OK;
 }
 
+// Reads and clears the tensor-core kernel's error word (after a stream sync).
+int check_tc_err(cpals_ctx* c) {
+  if (!c->tc) return CPALS_OK;
+  int h = 0;
+  CPALS_CUDA_TRY(cudaMemcpy(&h, tc_error_flag(c->tc), sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    fprintf(stderr, "libcpals: tensor-core MTTKRP reported error %d (bounded wait expired)\n", h);
+    CPALS_CUDA_TRY(cudaMemset(tc_error_flag(c->tc), 0, sizeof(int)));
+    return CPALS_E_DEVICE;
+  }
+  return CPALS_OK;
+}
+
 int check_derr(cpals_ctx* c) {
   int h = 0;
   CPALS_CUDA_TRY(cudaMemcpyAsync(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost, c->st));
@@ -262,6 +291,7 @@ int cpals_destroy(cpals_ctx* c) {
   for (int m = 0; m < kMaxOrder; ++m) {
     cudaFree(c->F[m]);
     cudaFree(c->F32t[m]);
+    cudaFree(c->F32r[m]);
     cudaFree(c->G[m]);
     if (c->ev_main[m]) cudaEventDestroy(c->ev_main[m]);
     if (c->ev_side[m]) cudaEventDestroy(c->ev_side[m]);
@@ -288,6 +318,9 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->Ts);
   cudaFree(c->Spart);
   cudaFree(c->derr);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   if (c->side) cudaStreamDestroy(c->side);
   delete c;
@@ -366,7 +399,17 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
     CK(dmalloc(&c->F[m], (size_t)dims[m] * R));
     CK(dmalloc(&c->F32t[m], (size_t)c->ld32[m] * R));
     CPALS_CUDA_TRY(cudaMemset(c->F32t[m], 0, sizeof(float) * c->ld32[m] * R));
+    if (c->tc) {
+      c->rpad = tc_factor_rpad(c->tc);
+      CK(dmalloc(&c->F32r[m], (size_t)dims[m] * c->rpad));
+      CPALS_CUDA_TRY(cudaMemset(c->F32r[m], 0, sizeof(float) * dims[m] * c->rpad));
+    }
     CK(dmalloc(&c->G[m], (size_t)R * R));
+  }
+  if (c->tc) {
+    const float* fr[kMaxOrder] = {};
+    for (int m = 0; m < order; ++m) fr[m] = c->F32r[m];
+    CK(tc_bind_factors(c->tc, fr));
   }
   c->part_f32 = (mttkrp_mode == CPALS_MTTKRP_BF16X3);
   {
@@ -380,7 +423,7 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   CK(dmalloc(&c->X, (size_t)maxI * R));
   CK(dmalloc(&c->Graw, (size_t)R * R));
   CK(dmalloc(&c->work, factorize_work_doubles((int)R)));
-  CK(dmalloc(&c->U, (size_t)R * R));
+  CK(dmalloc(&c->U, 2 * (size_t)R * R));  // U and its transpose
   CK(dmalloc(&c->piv, R));
   CK(dmalloc(&c->W, (size_t)R * R));
   CK(dmalloc(&c->info, 1));
@@ -449,8 +492,11 @@ int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const dou
     tmp.resize((size_t)c->dims[m] * R);
     colmajor_to_rowmajor_host(host_factors[m], c->dims[m], R, tmp.data());
     CPALS_CUDA_TRY(cudaMemcpyAsync(c->F[m], tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c->st));
-    CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32t[m], c->ld32[m], nullptr, c->st));
+    CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32t[m], c->ld32[m], c->F32r[m],
+                                    c->rpad, nullptr, c->st));
+    if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, m, c->F[m], nullptr, c->st));
     CPALS_CUDA_TRY(launch_gram(c->F[m], c->dims[m], R, c->gS2[m], c->gpart, c->gcnt, c->G[m], nullptr, c->st));
+    c->launches += 2;
     CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));  // tmp is reused for the next mode
   }
   if (host_lambda) {
@@ -500,12 +546,13 @@ int cpals_mttkrp(cpals_ctx* c, int mode, double* host_out) {
   const int R = (int)c->R;
   const int64_t In = c->dims[mode];
   CPALS_CUDA_TRY(enqueue_mttkrp(c, mode, nullptr));
+  c->launches += 2;
   CPALS_CUDA_TRY(launch_reduce_partials(c->part, c->part_f32, c->splits[mode], In, R, c->X, c->st));
   std::vector<double> tmp((size_t)In * R);
   CPALS_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c->X, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
   rowmajor_to_colmajor_host(tmp.data(), In, R, host_out);
-  return CPALS_OK;
+  return check_tc_err(c);
 }
 
 int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int64_t traj_capacity) {
@@ -535,7 +582,7 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
   h.nan_flag = 0;
   h.sweeps = 0;
   CPALS_CUDA_TRY(cudaMemcpyAsync(c->chk, c->hchk, sizeof(DevCheck), cudaMemcpyHostToDevice, c->st));
-  const bool use_graph = !(c->flags & CPALS_FLAG_NO_GRAPH);
+  const bool use_graph = !(c->flags & CPALS_FLAG_NO_GRAPH) && !c->profiling;
   if (use_graph && !c->graph) {
     int rc = build_graph(c);
     if (rc != CPALS_OK) return rc;
@@ -546,6 +593,7 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
     for (int64_t k = 0; k < b; ++k) {
       if (use_graph) {
         CPALS_CUDA_TRY(cudaGraphLaunch(c->graph, c->st));
+        c->launches += 6 * c->order;
       } else {
         int rc = enqueue_sweep(c);
         if (rc != CPALS_OK) return rc;
@@ -573,7 +621,7 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
     }
   }
   if (h.nan_flag) return CPALS_E_NAN;
-  return CPALS_OK;
+  return check_tc_err(c);
 }
 
 int cpals_fallback_count(cpals_ctx* c, int64_t* count) {
@@ -590,6 +638,62 @@ int cpals_synchronize(cpals_ctx* c) {
   DeviceGuard g(c->device);
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->side));
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CPALS_OK;
+}
+
+int cpals_timer_start(cpals_ctx* c) {
+  if (!c) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  if (!c->t0) {
+    CPALS_CUDA_TRY(cudaEventCreate(&c->t0));
+    CPALS_CUDA_TRY(cudaEventCreate(&c->t1));
+  }
+  CPALS_CUDA_TRY(cudaEventRecord(c->t0, c->st));
+  return CPALS_OK;
+}
+
+int cpals_timer_stop(cpals_ctx* c, double* elapsed_ms) {
+  if (!c || !elapsed_ms || !c->t0) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaEventRecord(c->t1, c->st));
+  CPALS_CUDA_TRY(cudaEventSynchronize(c->t1));
+  float ms = 0.0f;
+  CPALS_CUDA_TRY(cudaEventElapsedTime(&ms, c->t0, c->t1));
+  *elapsed_ms = ms;
+  return CPALS_OK;
+}
+
+int cpals_set_profiling(cpals_ctx* c, int on) {
+  if (!c) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  if (on && c->prof_ev.empty()) {
+    c->prof_ev.resize(2 * 8192);
+    for (auto& e : c->prof_ev) CPALS_CUDA_TRY(cudaEventCreate(&e));
+  }
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  c->profiling = on != 0;
+  c->prof_used = 0;
+  return CPALS_OK;
+}
+
+int cpals_profile_read(cpals_ctx* c, double* mttkrp_ms, int64_t* launches) {
+  if (!c || !mttkrp_ms || !launches) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  double tot = 0.0;
+  for (int64_t k = 0; k + 1 < c->prof_used; k += 2) {
+    float ms = 0.0f;
+    CPALS_CUDA_TRY(cudaEventElapsedTime(&ms, c->prof_ev[k], c->prof_ev[k + 1]));
+    tot += ms;
+  }
+  *mttkrp_ms = tot;
+  *launches = c->prof_used / 2;
+  return CPALS_OK;
+}
+
+int cpals_launch_count(cpals_ctx* c, int64_t* launches) {
+  if (!c || !launches) return CPALS_E_ARG;
+  *launches = c->launches;
   return CPALS_OK;
 }
 
@@ -679,7 +783,9 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
   const GramSet gs = gram_set(c);
   CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->G[mode], gs, c->order, 0, nullptr, In, nullptr, c->traj,
                                  c->traj_cap, c->st));
-  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], nullptr, c->st));
+  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], c->F32r[mode],
+                                  c->rpad, nullptr, c->st));
+  if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, mode, c->F[mode], nullptr, c->st));
   return check_derr(c);
 }
 

@@ -117,9 +117,10 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* Gn, 
                             int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st);
 
-// F = X ./ lambda (lambda may be null: plain copy) and an FP32 column-major copy [R][ld32].
+// F = X ./ lambda (lambda may be null: plain copy), an FP32 column-major copy [R][ld32] and
+// (when F32r is non-null) an FP32 row-major copy [In][rpad].
 cudaError_t launch_normalize(const double* X, const double* lam, int64_t In, int R, double* F, float* F32t,
-                             int64_t ld32, const DevCheck* chk, cudaStream_t st);
+                             int64_t ld32, float* F32r, int64_t rpad, const DevCheck* chk, cudaStream_t st);
 
 // Row-major rows x cols -> row-major cols x rows (FP64).
 cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);

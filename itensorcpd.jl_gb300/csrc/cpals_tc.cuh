@@ -15,8 +15,17 @@ int tc_set_tensor(TcState* s, const void* T, cudaStream_t st);
 int tc_splits(const TcState* s, int n);
 // Leading dimension (>= I_m, zero padded) of the FP32 column-major factor copies.
 int64_t tc_factor_ld(const TcState* s, int m);
-// Launch the MTTKRP of mode n; F32t[m] are the FP32 column-major factor copies.
-cudaError_t tc_launch_mttkrp(TcState* s, int n, const float* const* F32t, float* part, const DevCheck* chk,
-                             cudaStream_t st);
+// Device error word of the tensor-core kernel (0 = ok; non-zero = a bounded wait expired).
+int* tc_error_flag(TcState* s);
+// Column count (>= R, zero padded) of the row-major FP32 factor copies.
+int64_t tc_factor_rpad(const TcState* s);
+// Register the row-major FP32 factor copies F32r[m] ([I_m][tc_factor_rpad()], zero padded) the
+// kernel reads the outer factor rows from.
+int tc_bind_factors(TcState* s, const float* const* F32r);
+// Rebuild the BF16 hi/lo factor-block tiles of mode m (a no-op unless m is 0 or 1) from the FP64
+// row-major factor; skipped when the device check is done.
+cudaError_t tc_update_factor(TcState* s, int m, const double* F, const DevCheck* chk, cudaStream_t st);
+// Launch the MTTKRP of mode n with the bound factor copies.
+cudaError_t tc_launch_mttkrp(TcState* s, int n, float* part, const DevCheck* chk, cudaStream_t st);
 
 }  // namespace cpals

@@ -1,19 +1,656 @@
-// tcgen05 split-BF16 MTTKRP (placeholder until the tensor-core kernel lands).
+// tcgen05 split-BF16 MTTKRP for FP32 (or FP64) tensors on sm_103a.
+//
+// M_n(i, r) = sum_k T_(n)(i, k) KRP(k, r), the contraction that
+// matricize_tensor(::KRPFreeNormal / ::KRPNormal) forms
+// (src/algorithms/als_algorithms/standard/tensor.jl:52-84), computed as
+//   T ~ Th + Tl,  KRP ~ Kh + Kl  (BF16 hi/lo, round to nearest),
+//   M ~ Th Kh + Th Kl + Tl Kh   (three BF16 tensor-core products).
+//
+// Chunks.  The reduction index space (every mode but n) is cut into chunks of 64
+// consecutive values of the fastest reduction mode f (f = 1 for mode 0, else 0) at
+// fixed values of the other ("outer") reduction modes; inside a chunk
+// KRP(k, r) = F_f(k, r) * s(r), s(r) = product of the outer modes' factor rows.
+//
+// Layout.  HBM bandwidth bounds this kernel, so at set-up every mode gets its own copy
+// of the BF16 hi/lo unfolding as 32 KB tiles -- 128 rows x 64 reduction values, hi then
+// lo, each already in the SWIZZLE_128B K-major arrangement the tensor core reads --
+// stored in the order the CTAs consume them.  A stage is one contiguous 32 KB bulk copy
+// and every CTA streams one contiguous region (4 bytes per element, the FP32 size).
+//
+// CTA (10 warps): warp 0 issues per stage the tile bulk copy, a TMA load of the FP32
+// factor block F_f[k0:k0+64, n0:n0+NB] (landing in the stage's B region) and bulk copies
+// of the outer factor rows; warps 2-5 turn the FP32 block, in place, into the KRP tile
+// (NB x 64, BF16 hi/lo, swizzled K-major); warp 1 issues tcgen05.mma.kind::f16
+// (M = 128, N = NB, K = 16).  The tensor core's FP32 accumulation rounds toward zero,
+// which over long chains shrinks the result (about 0.5 ulp per accumulation), so each
+// chunk accumulates into fresh, double-buffered TMEM accumulators -- Th Kh (4 steps) and
+// the small Th Kl + Tl Kh -- and warps 6-9 promote them every chunk into FP32 registers
+// with round-to-nearest adds.  The reduction range is split across CTAs; each writes
+// FP32 partials part[split][I_n][R], reduced in FP64 (in split order) by the solve
+// kernel.  Every wait is bounded: on expiry the kernel records an error code, drains
+// its own copies in flight (bounded), frees TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "cpals_tc.cuh"
 
 namespace cpals {
-struct TcState {
-  int dummy;
+
+namespace {
+
+constexpr int kChunk = 64;     // K values per stage (one 128-byte swizzle row of BF16)
+constexpr int kBlockM = 128;   // rows per CTA (one UMMA M)
+constexpr int kThreads = 192;  // 6 warps
+constexpr int kDrainWarps = 4;
+constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr size_t kSmemLimit = 227 * 1024;
+
+struct TcModePlan {
+  int mode, fmode, n_outer, m_blocks, n_blocks, splits, stages, nb, tmem_cols, rpad;
+  int64_t In, If, nfb, nchunks, chunks_per_split;
+  int64_t sn, sf;              // element strides of mode n and of f in the tensor
+  uint32_t stage_bytes;
+  int64_t outer_dims[kMaxOrder];
+  int64_t outer_stride[kMaxOrder];  // element stride of each outer mode in the tensor
+  int outer_modes[kMaxOrder];
 };
-int tc_create(TcState** out, int, const int64_t*, int64_t, int, int) {
+
+struct FactorPtrs32 {
+  const float* F[kMaxOrder];  // row-major FP32 factor copies [I_m][rpad], zero-padded columns
+};
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; false on expiry or when another role has aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (i > 4096) __nanosleep(256);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;           // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1 << 46;           // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;           // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b, float* ra, float* rb) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  float2 f = __bfloat1622float2(h);
+  *ra = a - f.x;
+  *rb = b - f.y;
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// ---------------------------------------------------------------- the kernel
+template <int NBT>  // N-block width (a multiple of 16, at most 128): loops unroll exactly this far
+__global__ void __launch_bounds__(kThreads, 1)
+    k_mttkrp_tc(const uint8_t* __restrict__ tiles, const uint8_t* __restrict__ btiles, TcModePlan p,
+                FactorPtrs32 fr, int R, float* __restrict__ part, const DevCheck* __restrict__ chk,
+                int* __restrict__ err) {
+  if (chk && chk->done) return;
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte aligned tile region
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int S = p.stages;
+  constexpr int NB = NBT;
+  // Per chunk buffer: hi*hi in columns [0, NB), the small cross terms hi*lo + lo*hi in
+  // [NB, 2NB).  Four buffers (when TMEM has room) let the MMAs run four chunks ahead of
+  // the drain.
+  constexpr int kAcc = 2;
+  constexpr int kBuf = (2 * kAcc * NB <= 256) ? 4 : 2;
+  constexpr uint32_t a_bytes = kBlockM * kChunk * 2;  // 16 KB: one BF16 tile (hi or lo)
+  constexpr uint32_t b_bytes = NB * kChunk * 2;       // one BF16 factor-block tile (hi or lo)
+  constexpr uint32_t o_bytes = NB * 4;                // one outer factor row slice
+  const uint32_t stage_bytes = p.stage_bytes;
+  uint8_t* ctl = smem + (size_t)S * stage_bytes;
+  uint64_t* full_a = reinterpret_cast<uint64_t*>(ctl);  // [4] stage data landed
+  uint64_t* empty = full_a + 4;                          // [4] stage consumed (MMAs done, rows read)
+  uint64_t* acc_full = empty + 4;                        // [4] chunk accumulators ready
+  uint64_t* acc_empty = acc_full + 4;                    // [4] chunk accumulators drained
+  uint64_t* done_bar = acc_empty + 4;
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(done_bar + 1);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done_bar + 2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mblk = blockIdx.x % p.m_blocks;
+  const int nblk = (blockIdx.x / p.m_blocks) % p.n_blocks;
+  const int split = blockIdx.x / (p.m_blocks * p.n_blocks);
+  const int n0 = nblk * NB;
+  const int64_t c_begin = (int64_t)split * p.chunks_per_split;
+  const int64_t c_end = min(p.nchunks, c_begin + p.chunks_per_split);
+  const int nloc = (c_end > c_begin) ? (int)(c_end - c_begin) : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(smem_u32(&full_a[s]), 1);
+      mbar_init(smem_u32(&empty[s]), kDrainWarps);
+    }
+    for (int b = 0; b < kBuf; ++b) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), kDrainWarps);
+    }
+    mbar_init(smem_u32(done_bar), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(p.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- producer: unfolding tile, factor-block tile, outer rows
+    if (lane == 0) {
+      int issued = 0;
+      const uint32_t tx = 2 * a_bytes + 2 * b_bytes + (uint32_t)p.n_outer * o_bytes;
+      const uint8_t* src_tiles = tiles + ((size_t)mblk * p.nchunks + c_begin) * (2 * a_bytes);
+      for (int it = 0; it < nloc; ++it) {
+        const int s = it % S;
+        const uint32_t ph = (uint32_t)((it / S) & 1);
+        if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag)) {
+          atomicCAS(err, 0, 1);
+          *abort_flag = 1;
+          break;
+        }
+        const int64_t c = c_begin + it;
+        const int64_t fb = c % p.nfb;
+        int64_t o = c / p.nfb;
+        uint8_t* st = smem + (size_t)s * stage_bytes;
+        const uint32_t bar = smem_u32(&full_a[s]);
+        mbar_expect_tx(bar, tx);
+        bulk_load(smem_u32(st), src_tiles + (size_t)it * (2 * a_bytes), 2 * a_bytes, bar);
+        bulk_load(smem_u32(st + 2 * a_bytes), btiles + ((size_t)fb * p.n_blocks + nblk) * (2 * b_bytes), 2 * b_bytes,
+                  bar);
+        uint8_t* orow = st + 2 * a_bytes + 2 * b_bytes;
+        for (int j = 0; j < p.n_outer; ++j) {
+          const int64_t id = o % p.outer_dims[j];
+          o /= p.outer_dims[j];
+          const float* src = fr.F[p.outer_modes[j]] + id * p.rpad + n0;
+          bulk_load(smem_u32(orow + j * o_bytes), src, o_bytes, bar);
+        }
+        issued = it + 1;
+      }
+      if (*abort_flag) {
+        // drain this CTA's own copies in flight before the shared memory goes away
+        for (int it = max(0, issued - S); it < issued; ++it)
+          (void)mbar_wait(smem_u32(&full_a[it % S]), (uint32_t)((it / S) & 1), reinterpret_cast<volatile int*>(err + 1));
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer: per chunk, fresh accumulators in buffer b = it % kBuf.
+    // B = [Bh; Bl] stacked (2 NB rows): one N = 2 NB product gives Th Bh and Th Bl
+    // together, a second N = NB product adds Tl Bh onto the cross terms.
+    if (lane == 0) {
+      const uint32_t idesc_w = idesc_bf16(kBlockM, 2 * NB), idesc_n = idesc_bf16(kBlockM, NB);
+      for (int it = 0; it < nloc; ++it) {
+        const int s = it % S;
+        const uint32_t ph = (uint32_t)((it / S) & 1);
+        const int b = it % kBuf;
+        const uint32_t uph = (uint32_t)((it / kBuf) & 1);
+        if (!mbar_wait(smem_u32(&full_a[s]), ph, abort_flag) ||
+            !mbar_wait(smem_u32(&acc_empty[b]), uph ^ 1u, abort_flag)) {
+          atomicCAS(err, 0, 2);
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        uint8_t* st = smem + (size_t)s * stage_bytes;
+        const uint32_t ah = smem_u32(st), al = ah + a_bytes, bh = al + a_bytes;
+        const uint32_t acc_h = tmem + (uint32_t)(b * kAcc * NB), acc_l = acc_h + (uint32_t)NB;
+#pragma unroll
+        for (int kk = 0; kk < kChunk / 16; ++kk) {
+          const uint32_t off = kk * 32;
+          const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off), dbh = sw128_desc(bh + off);
+          umma_bf16(acc_h, dah, dbh, idesc_w, kk > 0 ? 1u : 0u);  // [Th Bh | Th Bl]
+          umma_bf16(acc_l, dal, dbh, idesc_n, 1u);                // += Tl Bh
+        }
+        umma_commit(smem_u32(&acc_full[b]));
+      }
+      umma_commit(smem_u32(done_bar));
+    }
+  } else {
+    // ---------------- drainers (warps 2..5): per chunk, acc[r] += s(r) * (Th Kh + cross terms),
+    // promoted from TMEM into FP32 registers with round-to-nearest adds
+    const int q = warp & 3;  // this warp's TMEM lane quarter
+    const int64_t row = (int64_t)mblk * kBlockM + q * 32 + lane;
+    float acc[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) acc[j] = 0.0f;
+    bool ok = true;
+    for (int it = 0; it < nloc && ok; ++it) {
+      const int s = it % S;
+      const int b = it % kBuf;
+      const uint32_t uph = (uint32_t)((it / kBuf) & 1);
+      int got = 0;
+      if (lane == 0) got = mbar_wait(smem_u32(&acc_full[b]), uph, abort_flag) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        if (lane == 0) {
+          atomicCAS(err, 0, 4);
+          *abort_flag = 1;
+        }
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const float* orow = reinterpret_cast<const float*>(smem + (size_t)s * stage_bytes + 2 * a_bytes + 2 * b_bytes);
+      const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB);
+#pragma unroll
+      for (int c0 = 0; c0 < NB; c0 += 32) {
+        constexpr int W = 32;
+        uint32_t vh[W], vl[W];
+        const bool full = (c0 + 32 <= NB);
+        if (full) {
+          tmem_ld32_nowait(base + (uint32_t)c0, vh);
+          tmem_ld32_nowait(base + (uint32_t)(NB + c0), vl);
+        } else {
+          tmem_ld16_nowait(base + (uint32_t)c0, vh);
+          tmem_ld16_nowait(base + (uint32_t)(NB + c0), vl);
+        }
+        float sc[W];
+#pragma unroll
+        for (int j = 0; j < W; ++j) sc[j] = 1.0f;
+        for (int jo = 0; jo < p.n_outer; ++jo) {
+#pragma unroll
+          for (int j = 0; j < W; j += 4) {
+            if (c0 + j < NB) {
+              const float4 o4 = *reinterpret_cast<const float4*>(orow + jo * NB + c0 + j);
+              sc[j] *= o4.x;
+              sc[j + 1] *= o4.y;
+              sc[j + 2] *= o4.z;
+              sc[j + 3] *= o4.w;
+            }
+          }
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          if (c0 + j < NB)
+            acc[c0 + j] = fmaf(sc[j], __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(smem_u32(&acc_empty[b]));
+        mbar_arrive(smem_u32(&empty[s]));
+      }
+    }
+    if (nloc > 0 && ok) {
+      int got = 0;
+      if (lane == 0) got = mbar_wait(smem_u32(done_bar), 0u, abort_flag) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      ok = got != 0;
+    }
+    if (row < p.In && (ok || nloc == 0)) {
+      float* out = part + ((int64_t)split * p.In + row) * R + n0;
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        if (n0 + j < R) out[j] = acc[j];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- factor-block tiles
+// For the fastest reduction mode f: per (f-block fb, N block), the NB x 64 block
+// F_f[fb*64 : fb*64+64, n0 : n0+NB]^T split into BF16 hi / lo (from FP64, round to
+// nearest), K-major and pre-swizzled, zero outside the factor.
+__global__ void k_build_btiles(const double* __restrict__ F, int64_t If, int R, int64_t nfb, int n_blocks, int nb,
+                               uint8_t* __restrict__ bt, const DevCheck* chk) {
+  if (chk && chk->done) return;
+  const int64_t units = nfb * n_blocks * nb * 8;  // 16-byte chunks per plane
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units; u += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(u & 7);
+    const int64_t rowg = u >> 3;  // (fb * n_blocks + nblk) * nb + r
+    const int r = (int)(rowg % nb);
+    const int64_t tile = rowg / nb;
+    const int nblk = (int)(tile % n_blocks);
+    const int64_t fb = tile / n_blocks;
+    const int col = nblk * nb + r;
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      double x[2];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int64_t k = fb * kChunk + c * 8 + 2 * t + e;
+        x[e] = (col < R && k < If) ? F[k * R + col] : 0.0;
+      }
+      __nv_bfloat162 h = __halves2bfloat162(__double2bfloat16(x[0]), __double2bfloat16(x[1]));
+      __nv_bfloat162 l = __halves2bfloat162(__double2bfloat16(x[0] - (double)__bfloat162float(h.x)),
+                                            __double2bfloat16(x[1] - (double)__bfloat162float(h.y)));
+      hw[t] = *reinterpret_cast<uint32_t*>(&h);
+      lw[t] = *reinterpret_cast<uint32_t*>(&l);
+    }
+    uint8_t* out = bt + (size_t)tile * (2 * (size_t)nb * kChunk * 2);
+    const uint32_t off = (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4);
+    *reinterpret_cast<uint4*>(out + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(out + (size_t)nb * kChunk * 2 + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
+// ---------------------------------------------------------------- set-up: the tile stream
+// One CTA per 32 KB tile (m-block, chunk): gathers the 128 x 64 block of the unfolding
+// (zero outside the tensor), splits it into BF16 hi/lo and writes it pre-swizzled.
+template <typename TT>
+__global__ void __launch_bounds__(256) k_build_tiles(const TT* __restrict__ T, TcModePlan p, uint8_t* __restrict__ tiles) {
+  __shared__ float fb_s[kBlockM][kChunk + 1];
+  const int64_t tile = blockIdx.x;
+  const int64_t mblk = tile / p.nchunks, c = tile % p.nchunks;
+  const int64_t fb = c % p.nfb;
+  int64_t o = c / p.nfb;
+  int64_t base = fb * kChunk * p.sf;
+  for (int j = 0; j < p.n_outer; ++j) {
+    const int64_t id = o % p.outer_dims[j];
+    o /= p.outer_dims[j];
+    base += id * p.outer_stride[j];
+  }
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kBlockM * kChunk; e += 256) {
+    int r, k;
+    if (p.sf == 1) {
+      r = e / kChunk;
+      k = e % kChunk;
+    } else {
+      k = e / kBlockM;
+      r = e % kBlockM;
+    }
+    const int64_t i = mblk * kBlockM + r, kf = fb * kChunk + k;
+    float v = 0.0f;
+    if (i < p.In && kf < p.If) v = (float)T[base + i * p.sn + (int64_t)k * p.sf];
+    fb_s[r][k] = v;
+  }
+  __syncthreads();
+  uint8_t* out = tiles + (size_t)tile * (2 * kBlockM * kChunk * 2);
+  for (int u = tid; u < kBlockM * 8; u += 256) {
+    const int r = u >> 3, cc = u & 7;
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float x0 = fb_s[r][cc * 8 + 2 * t], x1 = fb_s[r][cc * 8 + 2 * t + 1];
+      float r0, r1, d0, d1;
+      hw[t] = pack_bf16x2(x0, x1, &r0, &r1);
+      lw[t] = pack_bf16x2(r0, r1, &d0, &d1);
+    }
+    const uint32_t off = (uint32_t)r * 128u + ((uint32_t)(cc ^ (r & 7)) << 4);
+    *reinterpret_cast<uint4*>(out + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(out + kBlockM * kChunk * 2 + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
+int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+}  // namespace
+
+struct TcState {
+  int order = 0, tdtype = 0, num_sms = 0;
+  int64_t R = 0, rpad = 0;
+  int64_t dims[kMaxOrder] = {};
+  uint8_t* tiles[kMaxOrder] = {};  // per-mode tile streams
+  size_t tile_bytes[kMaxOrder] = {};
+  TcModePlan plan[kMaxOrder];
+  uint8_t* btiles[2] = {};  // BF16 hi/lo factor-block tiles of modes 0 and 1 (the fastest reduction modes)
+  size_t btile_bytes[2] = {};
+  int64_t nfb_mode[2] = {};
+  bool factors_bound = false;
+  const float* F32r[kMaxOrder] = {};
+  int* err = nullptr;  // [2]: error code, spare (never set: bounded drain flag)
+  size_t smem_bytes[kMaxOrder] = {};
+};
+
+int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms) {
   *out = nullptr;
-  return CPALS_E_UNSUPPORTED;
+  if (R > 512) return CPALS_E_UNSUPPORTED;
+  TcState* s = new TcState();
+  s->order = order;
+  s->tdtype = tdtype;
+  s->num_sms = num_sms;
+  s->R = R;
+  for (int m = 0; m < order; ++m) s->dims[m] = dims[m];
+  // N blocks of at most 128 columns (a multiple of 16 each)
+  const int64_t rp16 = round_up(R, 16);
+  const int n_blocks = (int)((rp16 + 127) / 128);
+  const int nb = (int)round_up((rp16 + n_blocks - 1) / n_blocks, 16);
+  s->rpad = (int64_t)nb * n_blocks;
+  int tcols = 32;
+  const int kacc = 2;                             // accumulators per chunk buffer (see the kernel)
+  const int kbuf = (2 * kacc * nb <= 256) ? 4 : 2;  // chunk buffers (see the kernel)
+  while (tcols < kbuf * kacc * nb) tcols *= 2;
+  const int usable = std::max(1, num_sms - 1);  // one SM stays free for the side-stream factorisation
+  if (cudaMalloc(&s->err, 2 * sizeof(int)) != cudaSuccess) {
+    tc_destroy(s);
+    return CPALS_E_CUDA;
+  }
+  cudaMemset(s->err, 0, 2 * sizeof(int));
+  int64_t strides[kMaxOrder];
+  {
+    int64_t st = 1;
+    for (int m = 0; m < order; ++m) {
+      strides[m] = st;
+      st *= dims[m];
+    }
+  }
+  for (int n = 0; n < order; ++n) {
+    TcModePlan& p = s->plan[n];
+    memset(&p, 0, sizeof(p));
+    p.mode = n;
+    p.fmode = (n == 0) ? 1 : 0;
+    p.In = dims[n];
+    p.If = dims[p.fmode];
+    p.sn = strides[n];
+    p.sf = strides[p.fmode];
+    p.nb = nb;
+    p.n_blocks = n_blocks;
+    p.rpad = (int)s->rpad;
+    p.tmem_cols = tcols;
+    p.nfb = (p.If + kChunk - 1) / kChunk;
+    int64_t outer = 1;
+    for (int m = 0; m < order; ++m) {
+      if (m == n || m == p.fmode) continue;
+      p.outer_modes[p.n_outer] = m;
+      p.outer_dims[p.n_outer] = dims[m];
+      p.outer_stride[p.n_outer] = strides[m];
+      ++p.n_outer;
+      outer *= dims[m];
+    }
+    p.nchunks = p.nfb * outer;
+    p.m_blocks = (int)((p.In + kBlockM - 1) / kBlockM);
+    int64_t splits = std::max<int64_t>(1, usable / (p.m_blocks * p.n_blocks));
+    splits = std::min<int64_t>(splits, p.nchunks);
+    p.chunks_per_split = (p.nchunks + splits - 1) / splits;
+    p.splits = (int)((p.nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
+    // stage: A hi | A lo | B hi | B lo | outer rows
+    const size_t sb = (size_t)2 * kBlockM * kChunk * 2 + (size_t)2 * nb * kChunk * 2 + (size_t)p.n_outer * nb * 4;
+    p.stage_bytes = (uint32_t)round_up((int64_t)sb, 1024);
+    const size_t ctl_bytes = 1024 + 256;  // alignment slack + barriers and flags
+    p.stages = (int)std::min<size_t>(4, (kSmemLimit - ctl_bytes) / p.stage_bytes);
+    if (p.stages < 2 || p.nchunks >= (int64_t(1) << 31)) {
+      tc_destroy(s);
+      return CPALS_E_UNSUPPORTED;
+    }
+    s->smem_bytes[n] = ctl_bytes + (size_t)p.stages * p.stage_bytes;
+    s->tile_bytes[n] = (size_t)p.m_blocks * p.nchunks * (2 * kBlockM * kChunk * 2);
+    if (cudaMalloc(&s->tiles[n], s->tile_bytes[n]) != cudaSuccess) {
+      tc_destroy(s);
+      return CPALS_E_CUDA;
+    }
+  }
+  for (int f = 0; f < 2; ++f) {
+    s->nfb_mode[f] = (dims[f] + kChunk - 1) / kChunk;
+    s->btile_bytes[f] = (size_t)s->nfb_mode[f] * n_blocks * 2 * nb * kChunk * 2;
+    if (cudaMalloc(&s->btiles[f], s->btile_bytes[f]) != cudaSuccess) {
+      tc_destroy(s);
+      return CPALS_E_CUDA;
+    }
+    cudaMemset(s->btiles[f], 0, s->btile_bytes[f]);
+  }
+  cudaFuncSetAttribute(k_mttkrp_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<80>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<96>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<112>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  cudaFuncSetAttribute(k_mttkrp_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  *out = s;
+  return CPALS_OK;
 }
-void tc_destroy(TcState* s) { delete s; }
-int tc_set_tensor(TcState*, const void*, cudaStream_t) { return CPALS_E_UNSUPPORTED; }
-int tc_splits(const TcState*, int) { return 1; }
-int64_t tc_factor_ld(const TcState*, int) { return 1; }
-cudaError_t tc_launch_mttkrp(TcState*, int, const float* const*, float*, const DevCheck*, cudaStream_t) {
-  return cudaErrorNotSupported;
+
+int64_t tc_factor_rpad(const TcState* s) { return s->rpad; }
+
+int tc_bind_factors(TcState* s, const float* const* F32r) {
+  for (int m = 0; m < s->order; ++m) s->F32r[m] = F32r[m];
+  s->factors_bound = true;
+  return CPALS_OK;
 }
+
+cudaError_t tc_update_factor(TcState* s, int m, const double* F, const DevCheck* chk, cudaStream_t st) {
+  if (m > 1) return cudaSuccess;  // only the fastest reduction modes (0 and 1) feed the tensor core directly
+  const TcModePlan& p = s->plan[0];
+  const int64_t units = s->nfb_mode[m] * p.n_blocks * p.nb * 8;
+  const int blocks = (int)std::min<int64_t>((units + 255) / 256, 4096);
+  k_build_btiles<<<blocks, 256, 0, st>>>(F, s->dims[m], (int)s->R, s->nfb_mode[m], p.n_blocks, p.nb, s->btiles[m], chk);
+  return cudaGetLastError();
+}
+
+void tc_destroy(TcState* s) {
+  if (!s) return;
+  for (int m = 0; m < kMaxOrder; ++m) cudaFree(s->tiles[m]);
+  cudaFree(s->btiles[0]);
+  cudaFree(s->btiles[1]);
+  cudaFree(s->err);
+  delete s;
+}
+
+int tc_set_tensor(TcState* s, const void* T, cudaStream_t st) {
+  for (int n = 0; n < s->order; ++n) {
+    const TcModePlan& p = s->plan[n];
+    const int64_t ntiles = (int64_t)p.m_blocks * p.nchunks;
+    if (ntiles >= (int64_t(1) << 31)) return CPALS_E_UNSUPPORTED;
+    if (s->tdtype == CPALS_DTYPE_F64)
+      k_build_tiles<double><<<(unsigned)ntiles, 256, 0, st>>>(static_cast<const double*>(T), p, s->tiles[n]);
+    else
+      k_build_tiles<float><<<(unsigned)ntiles, 256, 0, st>>>(static_cast<const float*>(T), p, s->tiles[n]);
+    if (cudaGetLastError() != cudaSuccess) return CPALS_E_CUDA;
+  }
+  return CPALS_OK;
+}
+
+int tc_splits(const TcState* s, int n) { return s->plan[n].splits; }
+int64_t tc_factor_ld(const TcState* s, int m) { return round_up(s->dims[m], kChunk); }
+int* tc_error_flag(TcState* s) { return s->err; }
+
+cudaError_t tc_launch_mttkrp(TcState* s, int n, float* part, const DevCheck* chk, cudaStream_t st) {
+  if (!s->factors_bound) return cudaErrorInvalidValue;
+  const TcModePlan& p = s->plan[n];
+  FactorPtrs32 fr{};
+  for (int m = 0; m < s->order; ++m) fr.F[m] = s->F32r[m];
+  const unsigned grid = (unsigned)(p.m_blocks * p.n_blocks * p.splits);
+  switch (p.nb) {
+#define CPALS_TC_CASE(W)                                                                                           \
+  case W:                                                                                                          \
+    k_mttkrp_tc<W><<<grid, kThreads, s->smem_bytes[n], st>>>(s->tiles[n], s->btiles[p.fmode], p, fr, (int)s->R, \
+                                                            part, chk, s->err);                                   \
+    break;
+    CPALS_TC_CASE(16)
+    CPALS_TC_CASE(32)
+    CPALS_TC_CASE(48)
+    CPALS_TC_CASE(64)
+    CPALS_TC_CASE(80)
+    CPALS_TC_CASE(96)
+    CPALS_TC_CASE(112)
+    CPALS_TC_CASE(128)
+#undef CPALS_TC_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace cpals

@@ -25,7 +25,7 @@ namespace cpals {
 namespace {
 
 constexpr double kCholTol = 1e-6;  // src/ITensorCPD.jl:2 cholesky_epsilon
-constexpr int FT = 512;            // factorize threads
+constexpr int FT = 256;            // factorize threads
 
 __device__ __forceinline__ bool done_flag(const DevCheck* chk) { return chk != nullptr && chk->done; }
 
@@ -266,12 +266,20 @@ __device__ void qr_fallback(const GramSet& gs, int order, int skip, int R, doubl
     for (int e = tid; e < R * R; e += blockDim.x) Y[e] = NAN;
   }
   __syncthreads();
-  // W = P Y : row perm[k] of W is row k of Y
+  // operator (P Y), stored transposed: X = M W^T reads W^T[c][perm[k]] = Y[k][c]
   for (int e = tid; e < R * R; e += blockDim.x) {
     const int k = e / R, c = e % R;
-    W[perm[k] * R + c] = Y[e];
+    W[(size_t)c * R + perm[k]] = Y[e];
   }
   __syncthreads();
+}
+
+__device__ __forceinline__ unsigned long long pivot_key(double v) {
+  // non-negative doubles order like their bit patterns; NaN sorts above everything
+  // (it is picked, then rejected by the stopping test like DISNAN); non-positive values
+  // can never pass the stopping test and sort below every positive value
+  if (isnan(v)) return ~0ull;
+  return v > 0.0 ? (unsigned long long)__double_as_longlong(v) : 0ull;
 }
 
 __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int skip, int R, double* __restrict__ Aglob,
@@ -283,7 +291,8 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
   double* A = (R <= 128) ? smA : Aglob;
   __shared__ double sv[32];
   __shared__ int si[32];
-  __shared__ double s_ajj;
+  __shared__ double s_diag[CPALS_MAX_RANK_SOLVE];
+  __shared__ double s_sqrt, s_rinv;
   __shared__ int s_p, s_stop;
   __shared__ int s_piv[CPALS_MAX_RANK_SOLVE];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -296,6 +305,7 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
       for (int m = 0; m < order; ++m)
         if (m != skip) v *= gs.G[m][e];
       A[e] = v;
+      if (c == r) s_diag[r] = v;
     }
   }
   for (int k = tid; k < R; k += blockDim.x) s_piv[k] = k;
@@ -303,23 +313,37 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 
   int rank = R;
   for (int j = 0; j < R; ++j) {
-    double bv = -INFINITY;
-    int bi = 0x7fffffff;
-    for (int i = j + tid; i < R; i += blockDim.x) {
-      const double d = A[i * R + i];
-      const double key = isnan(d) ? INFINITY : d, bkey = isnan(bv) ? INFINITY : bv;
-      if (key > bkey || (key == bkey && i < bi)) {
-        bv = d;
-        bi = i;
+    if (warp == 0) {
+      // pivot: the largest remaining diagonal entry, first index on ties (LAPACK MAXLOC)
+      unsigned long long bk = 0ull;
+      int bi = R;
+      for (int i = j + lane; i < R; i += 32) {
+        const unsigned long long k = pivot_key(s_diag[i]);
+        if (bi == R || k > bk) {  // i increases: strict > keeps the first index on ties
+          bk = k;
+          bi = i;
+        }
       }
-    }
-    double pv;
-    int pi;
-    block_argmax(bv, bi, sv, si, &pv, &pi);
-    if (tid == 0) {
-      s_p = pi;
-      s_ajj = pv;
-      s_stop = !(pv > kCholTol);  // pivot <= tol or NaN
+      unsigned long long mk = bk;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mk, off);
+        mk = o > mk ? o : mk;
+      }
+      int cand = (bi < R && bk == mk) ? bi : 0x7fffffff;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) cand = min(cand, __shfl_xor_sync(0xffffffffu, cand, off));
+      if (lane == 0) {
+        const double pv = s_diag[cand];
+        s_p = cand;
+        s_stop = !(pv > kCholTol);  // pivot <= tol or NaN (dpstrf's stopping rule)
+        if (!s_stop) {
+          // one reciprocal square root instead of a square root and a division
+          const double r = rsqrt(pv);
+          s_sqrt = pv * r;
+          s_rinv = r;
+        }
+      }
     }
     __syncthreads();
     if (s_stop) {
@@ -346,20 +370,27 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
       }
       if (tid == 0) {
         A[p * R + p] = A[j * R + j];
+        const double td = s_diag[j];
+        s_diag[j] = s_diag[p];
+        s_diag[p] = td;
         const int t = s_piv[j];
         s_piv[j] = s_piv[p];
         s_piv[p] = t;
       }
     }
     __syncthreads();
-    const double ajj = sqrt(s_ajj);
-    const double rinv = 1.0 / ajj;
-    if (tid == 0) A[j * R + j] = ajj;
+    const double rinv = s_rinv;
+    if (tid == 0) A[j * R + j] = s_sqrt;
     for (int k = j + 1 + tid; k < R; k += blockDim.x) A[j * R + k] *= rinv;
     __syncthreads();
+    // trailing update of the upper triangle; the diagonal copy follows along
     for (int i = j + 1 + warp; i < R; i += nw) {
       const double a = A[j * R + i];
-      for (int k = i + lane; k < R; k += 32) A[i * R + k] = fma(-a, A[j * R + k], A[i * R + k]);
+      for (int k = i + lane; k < R; k += 32) {
+        const double v = fma(-a, A[j * R + k], A[i * R + k]);
+        A[i * R + k] = v;
+        if (k == i) s_diag[i] = v;
+      }
     }
     __syncthreads();
   }
@@ -370,13 +401,60 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
     info->qr_rank = rank;
   }
   if (rank == R) {
+    double* UT = U + (size_t)R * R;
     for (int e = tid; e < R * R; e += blockDim.x) {
       const int r = e / R, c = e % R;
-      U[e] = (c >= r) ? A[e] : 0.0;
+      const double u = (c >= r) ? A[e] : 0.0;
+      U[e] = u;
+      UT[(size_t)c * R + r] = u;
     }
     for (int k = tid; k < R; k += blockDim.x) {
       dinv[k] = 1.0 / A[k * R + k];
       piv[k] = s_piv[k];
+    }
+    __syncthreads();
+    // The solve operator W = V^{-1} = P U^{-1} U^{-T} P^T, so that the row solves become
+    // one parallel FP64 product X = M W^T instead of 2R dependent steps per row.
+    // Uinv = U^{-1} (upper), row by row from the bottom: Uinv[k][c] for c >= k.
+    double* Uinv = qwork;           // R x R
+    double* Wp = qwork + (size_t)R * R;  // R x R (pivoted order)
+    for (int e = tid; e < R * R; e += blockDim.x) Uinv[e] = 0.0;
+    __syncthreads();
+    for (int k = R - 1; k >= 0; --k) {
+      const double dk = dinv[k];
+      for (int c = k + tid; c < R; c += blockDim.x) {
+        double a0 = (c == k) ? 1.0 : 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int l = k + 1;
+        for (; l + 3 <= c; l += 4) {
+          a0 = fma(-A[k * R + l], Uinv[l * R + c], a0);
+          a1 = fma(-A[k * R + l + 1], Uinv[(l + 1) * R + c], a1);
+          a2 = fma(-A[k * R + l + 2], Uinv[(l + 2) * R + c], a2);
+          a3 = fma(-A[k * R + l + 3], Uinv[(l + 3) * R + c], a3);
+        }
+        for (; l <= c; ++l) a0 = fma(-A[k * R + l], Uinv[l * R + c], a0);
+        Uinv[k * R + c] = ((a0 + a1) + (a2 + a3)) * dk;
+      }
+      __syncthreads();
+    }
+    // Wp = Uinv Uinv^T (symmetric): Wp[a][b] = sum_{l >= max(a,b)} Uinv[a][l] Uinv[b][l]
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int a = e / R, b2 = e % R;
+      if (b2 < a) continue;
+      double s0 = 0.0, s1 = 0.0;
+      int l = b2;
+      for (; l + 1 < R; l += 2) {
+        s0 = fma(Uinv[a * R + l], Uinv[b2 * R + l], s0);
+        s1 = fma(Uinv[a * R + l + 1], Uinv[b2 * R + l + 1], s1);
+      }
+      if (l < R) s0 = fma(Uinv[a * R + l], Uinv[b2 * R + l], s0);
+      Wp[a * R + b2] = s0 + s1;
+    }
+    __syncthreads();
+    // W = P Wp P^T
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int a = e / R, b2 = e % R;
+      const double v = (b2 >= a) ? Wp[a * R + b2] : Wp[b2 * R + a];
+      W[(size_t)s_piv[a] * R + s_piv[b2]] = v;
     }
   } else {
     if (tid == 0 && chk) atomicAdd(reinterpret_cast<unsigned long long*>(&chk->fallbacks), 1ull);
@@ -391,97 +469,75 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
   }
 }
 
-// ---------------- solve rows ----------------
-template <typename PT, int RQ>
-__global__ void __launch_bounds__(128) k_solve_rows(const PT* __restrict__ part, int S, int64_t In, int R,
-                                                    const double* __restrict__ U, const double* __restrict__ dinv,
-                                                    const int* __restrict__ piv, const double* __restrict__ W,
-                                                    const SolveInfo* __restrict__ info, double* __restrict__ X,
+// ---------------- solve: X = M W^T ----------------
+// M rows are the split-K partial sums (added in split order, FP64); W^T is the solve
+// operator from the factorisation (V^{-1}, or the pivoted-QR least-squares operator),
+// stored so that consecutive output columns are contiguous.  One thread per output;
+// per-row sums of M .* X (Neumaier) feed the fit.
+template <typename PT>
+__global__ void __launch_bounds__(256) k_solve_gemm(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
+                                                    const double* __restrict__ WT, double* __restrict__ X,
                                                     double* __restrict__ inner_rows, const DevCheck* chk) {
   if (done_flag(chk)) return;
   extern __shared__ double sm[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  const int64_t row = (int64_t)blockIdx.x * wpb + warp;
-  if (row >= In) return;
-  double* m = sm + (size_t)warp * 2 * R;
-  double* xs = m + R;
-  // 1. M row = sum of split partials, in split order
-  for (int k = lane; k < R; k += 32) {
+  double* Ms = sm;            // RB x R
+  double* Ps = sm + RB * R;   // RB x R products for the fit
+  const int tid = threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.x * RB;
+  const int rows = (In - r0 < (int64_t)RB) ? (int)(In - r0) : RB;
+  const int nval = rows * R;
+  const int64_t base = r0 * R;
+  const int64_t sstride = In * R;
+  for (int e = tid; e < nval; e += blockDim.x) {
     double s = 0.0;
-    for (int sp = 0; sp < S; ++sp) s += (double)part[((int64_t)sp * In + row) * R + k];
-    m[k] = s;
+    int sp = 0;
+    for (; sp + 8 <= S; sp += 8) {
+      double v[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) v[t] = (double)part[(int64_t)(sp + t) * sstride + base + e];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) s += v[t];
+    }
+    for (; sp < S; ++sp) s += (double)part[(int64_t)sp * sstride + base + e];
+    Ms[e] = s;
   }
-  __syncwarp();
-  double t[RQ];
-  if (!info->fallback) {
-    // t = m[piv]; forward (U^T) and backward (U) substitution; x[piv] = w
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-      const int j = lane + 32 * q;
-      t[q] = (j < R) ? m[piv[j]] : 0.0;
+  __syncthreads();
+  for (int e = tid; e < nval; e += blockDim.x) {
+    const int row = e / R, k = e % R;
+    const double* m = Ms + row * R;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int l = 0;
+    for (; l + 3 < R; l += 4) {
+      a0 = fma(m[l], WT[(size_t)l * R + k], a0);
+      a1 = fma(m[l + 1], WT[(size_t)(l + 1) * R + k], a1);
+      a2 = fma(m[l + 2], WT[(size_t)(l + 2) * R + k], a2);
+      a3 = fma(m[l + 3], WT[(size_t)(l + 3) * R + k], a3);
     }
-    for (int k = 0; k < R; ++k) {
-      const int qk = k >> 5, owner = k & 31;
-      double tk = 0.0;
-#pragma unroll
-      for (int q = 0; q < RQ; ++q)
-        if (q == qk) tk = t[q];
-      const double c = __shfl_sync(0xffffffffu, tk * dinv[k], owner);
-      const double* Uk = U + (size_t)k * R;
-#pragma unroll
-      for (int q = 0; q < RQ; ++q) {
-        const int j = lane + 32 * q;
-        if (j == k) t[q] = c;
-        else if (j > k && j < R) t[q] = fma(-c, Uk[j], t[q]);
-      }
-    }
-    for (int k = R - 1; k >= 0; --k) {
-      const int qk = k >> 5, owner = k & 31;
-      double tk = 0.0;
-#pragma unroll
-      for (int q = 0; q < RQ; ++q)
-        if (q == qk) tk = t[q];
-      const double w = __shfl_sync(0xffffffffu, tk * dinv[k], owner);
-#pragma unroll
-      for (int q = 0; q < RQ; ++q) {
-        const int j = lane + 32 * q;
-        if (j == k) t[q] = w;
-        else if (j < k) t[q] = fma(-U[(size_t)j * R + k], w, t[q]);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-      const int j = lane + 32 * q;
-      if (j < R) xs[piv[j]] = t[q];
-    }
-  } else {
+    for (; l < R; ++l) a0 = fma(m[l], WT[(size_t)l * R + k], a0);
+    const double x = (a0 + a1) + (a2 + a3);
+    X[base + e] = x;
+    Ps[e] = m[k] * x;
+  }
+  if (!inner_rows) return;
+  __syncthreads();
+  // per-row Neumaier sum of M .* X, one warp per row
+  const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int row = warp; row < rows; row += nw) {
+    double s = 0.0, c = 0.0;
     for (int k = lane; k < R; k += 32) {
-      const double* Wk = W + (size_t)k * R;
-      double s = 0.0;
-      for (int l = 0; l < R; ++l) s = fma(Wk[l], m[l], s);
-      xs[k] = s;
+      const double p = Ps[row * R + k];
+      const double t = s + p;
+      c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
+      s = t;
     }
-  }
-  __syncwarp();
-  double inner = 0.0, comp = 0.0;
-  for (int k = lane; k < R; k += 32) {
-    const double x = xs[k];
-    X[row * R + k] = x;
-    // Neumaier-compensated sum of m .* x
-    const double p = m[k] * x;
-    const double s = inner + p;
-    comp += (fabs(inner) >= fabs(p)) ? ((inner - s) + p) : ((p - s) + inner);
-    inner = s;
-  }
-  if (inner_rows) {
     for (int off = 16; off > 0; off >>= 1) {
-      const double o = __shfl_down_sync(0xffffffffu, inner, off);
-      const double oc = __shfl_down_sync(0xffffffffu, comp, off);
-      const double s = inner + o;
-      comp += ((fabs(inner) >= fabs(o)) ? ((inner - s) + o) : ((o - s) + inner)) + oc;
-      inner = s;
+      const double o = __shfl_down_sync(0xffffffffu, s, off);
+      const double oc = __shfl_down_sync(0xffffffffu, c, off);
+      const double t = s + o;
+      c += ((fabs(s) >= fabs(o)) ? ((s - t) + o) : ((o - t) + s)) + oc;
+      s = t;
     }
-    if (lane == 0) inner_rows[row] = inner + comp;
+    if (lane == 0) inner_rows[r0 + row] = s + c;
   }
 }
 
@@ -545,16 +601,19 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
   if (done_flag(chk)) return;
   __shared__ double sv[32];
   __shared__ double s_lam[CPALS_MAX_RANK_SOLVE];
+  __shared__ double s_inv[CPALS_MAX_RANK_SOLVE];
   const int tid = threadIdx.x;
   for (int r = tid; r < R; r += blockDim.x) {
     const double l = sqrt(Graw[(size_t)r * R + r]);
     s_lam[r] = l;
+    s_inv[r] = 1.0 / l;
     lam[r] = l;
   }
   __syncthreads();
+  // R^2 FP64 divisions would cost ~40 us on one SM: multiply by the R reciprocals instead
   for (int e = tid; e < R * R; e += blockDim.x) {
     const int r = e / R, c = e % R;
-    Gn[e] = Graw[e] / s_lam[r] / s_lam[c];
+    Gn[e] = Graw[e] * s_inv[r] * s_inv[c];
   }
   if (!last) return;
   __syncthreads();
@@ -632,7 +691,8 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
 
 // ---------------- normalize ----------------
 __global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam, int64_t In, int R,
-                            double* __restrict__ F, float* __restrict__ F32t, int64_t ld32, const DevCheck* chk) {
+                            double* __restrict__ F, float* __restrict__ F32t, int64_t ld32, float* __restrict__ F32r,
+                            int64_t rpad, const DevCheck* chk) {
   if (done_flag(chk)) return;
   const int64_t n = In * R;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
@@ -641,6 +701,7 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
     const double f = lam ? X[e] / lam[r] : X[e];
     F[e] = f;
     if (F32t) F32t[(int64_t)r * ld32 + i] = (float)f;
+    if (F32r) F32r[i * rpad + r] = (float)f;
   }
 }
 
@@ -687,42 +748,25 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   return cudaGetLastError();
 }
 
-int solve_rows_blocks(int64_t In, int R) {
-  (void)R;
-  return (int)((In + 3) / 4);
-}
-
-template <typename PT>
-static cudaError_t solve_rows_dispatch(const PT* part, int S, int64_t In, int R, const double* U, const double* dinv,
-                                       const int* piv, const double* W, const SolveInfo* info, double* X,
-                                       double* inner_rows, const DevCheck* chk, cudaStream_t st) {
-  const int wpb = 4;
-  dim3 grid((unsigned)((In + wpb - 1) / wpb));
-  const size_t smem = (size_t)wpb * 2 * R * sizeof(double);
-  const int rq = (R + 31) / 32;
-#define CPALS_SOLVE_CASE(Q)                                                                                   \
-  if (rq <= Q) {                                                                                              \
-    k_solve_rows<PT, Q><<<grid, 32 * wpb, smem, st>>>(part, S, In, R, U, dinv, piv, W, info, X, inner_rows, chk); \
-    return cudaGetLastError();                                                                                \
-  }
-  CPALS_SOLVE_CASE(1)
-  CPALS_SOLVE_CASE(2)
-  CPALS_SOLVE_CASE(4)
-  CPALS_SOLVE_CASE(8)
-  CPALS_SOLVE_CASE(16)
-#undef CPALS_SOLVE_CASE
-  return cudaErrorInvalidValue;
-}
+static int solve_rows_per_block(int R) { return R >= 256 ? 1 : 256 / R; }
 
 cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
                               const double* U, const int* piv, const double* W, const SolveInfo* info, double* X,
                               double* inner_rows, const DevCheck* chk, cudaStream_t st) {
-  const double* dinv = work + (size_t)R * R;
+  (void)work;
+  (void)U;
+  (void)piv;
+  (void)info;
+  const int RB = solve_rows_per_block(R);
+  dim3 grid((unsigned)((In + RB - 1) / RB));
+  const size_t smem = (size_t)2 * RB * R * sizeof(double);
   if (part_is_f32)
-    return solve_rows_dispatch(static_cast<const float*>(part), splits, In, R, U, dinv, piv, W, info, X, inner_rows,
-                               chk, st);
-  return solve_rows_dispatch(static_cast<const double*>(part), splits, In, R, U, dinv, piv, W, info, X, inner_rows,
-                             chk, st);
+    k_solve_gemm<float><<<grid, 256, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X, inner_rows,
+                                                 chk);
+  else
+    k_solve_gemm<double><<<grid, 256, smem, st>>>(static_cast<const double*>(part), splits, In, R, RB, W, X,
+                                                  inner_rows, chk);
+  return cudaGetLastError();
 }
 
 int gram_tiles(int R) {
@@ -732,8 +776,8 @@ int gram_tiles(int R) {
 
 int gram_splits(int64_t In, int R, int num_sms) {
   const int tiles = gram_tiles(R);
-  int64_t s = (2LL * num_sms + tiles - 1) / tiles;
-  const int64_t max_s = (In + 63) / 64;
+  int64_t s = (4LL * num_sms + tiles - 1) / tiles;
+  const int64_t max_s = (In + 31) / 32;
   if (s > max_s) s = max_s;
   if (s < 1) s = 1;
   if (s > 512) s = 512;
@@ -742,7 +786,7 @@ int gram_splits(int64_t In, int R, int num_sms) {
 
 cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters, double* G,
                         const DevCheck* chk, cudaStream_t st) {
-  const int64_t rps = (((In + S2 - 1) / S2) + 63) / 64 * 64;
+  const int64_t rps = (In + S2 - 1) / S2;
   dim3 grid((unsigned)gram_tiles(R), (unsigned)S2);
   k_gram<<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, G, chk);
   return cudaGetLastError();
@@ -756,10 +800,10 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* Gn, 
 }
 
 cudaError_t launch_normalize(const double* X, const double* lam, int64_t In, int R, double* F, float* F32t,
-                             int64_t ld32, const DevCheck* chk, cudaStream_t st) {
+                             int64_t ld32, float* F32r, int64_t rpad, const DevCheck* chk, cudaStream_t st) {
   const int64_t n = In * R;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_normalize<<<blocks, 256, 0, st>>>(X, lam, In, R, F, F32t, ld32, chk);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam, In, R, F, F32t, ld32, F32r, rpad, chk);
   return cudaGetLastError();
 }
 

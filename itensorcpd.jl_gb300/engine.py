@@ -112,6 +112,28 @@ class Engine:
     def synchronize(self):
         L.check(self.lib.cpals_synchronize(self.h), "cpals_synchronize")
 
+    # ---- measurement ----
+    def timer_start(self):
+        L.check(self.lib.cpals_timer_start(self.h), "cpals_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        L.check(self.lib.cpals_timer_stop(self.h, C.byref(ms)), "cpals_timer_stop")
+        return ms.value
+
+    def set_profiling(self, on: bool):
+        L.check(self.lib.cpals_set_profiling(self.h, int(bool(on))), "cpals_set_profiling")
+
+    def profile_read(self):
+        ms, n = C.c_double(), C.c_int64()
+        L.check(self.lib.cpals_profile_read(self.h, C.byref(ms), C.byref(n)), "cpals_profile_read")
+        return ms.value, int(n.value)
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        L.check(self.lib.cpals_launch_count(self.h, C.byref(n)), "cpals_launch_count")
+        return int(n.value)
+
     # ---- randomized path ----
     @staticmethod
     def _pivots(pivots, nother):

@@ -95,14 +95,18 @@ def mttkrp_krp_free(T: np.ndarray, factors, mode: int) -> np.ndarray:
     """
     N = T.ndim
     R = factors[0].shape[1]
-    M = np.empty((T.shape[mode], R))
+    dims = T.shape
+    M = np.empty((dims[mode], R))
+    Tf = np.asfortranarray(T)
     for r in range(R):
-        x = T
-        for m in reversed(range(N)):
-            if m == mode:
-                continue
-            x = np.tensordot(x, factors[m][:, r], axes=([m], [0]))
-        M[:, r] = x
+        # trailing modes (last first) then leading modes (first first): each step is a
+        # matrix-vector product on a column-major view, the first one streams all of T
+        x = Tf
+        for m in reversed(range(mode + 1, N)):
+            x = np.reshape(x, (-1, dims[m]), order="F") @ factors[m][:, r]
+        for m in range(mode):
+            x = factors[m][:, r] @ np.reshape(x, (dims[m], -1), order="F")
+        M[:, r] = np.reshape(x, -1)
     return M
 
 
@@ -275,7 +279,8 @@ class NoCheck:
 # ---------------------------------------------------------------------------
 # ALS driver
 # ---------------------------------------------------------------------------
-def als_optimize(T, factors, lam, check=None, maxiter=None, alg="krp", verbose=False, record=None):
+def als_optimize(T, factors, lam, check=None, maxiter=None, alg="krp", verbose=False, record=None,
+                 work_dtype=np.float64):
     """als_optimize -> compute_als -> optimize.
 
     src/optimizers/als_optimizers/als_optimizer.jl:15-25, 37-55 (defaults: NoCheck(100)),
@@ -285,14 +290,16 @@ def als_optimize(T, factors, lam, check=None, maxiter=None, alg="krp", verbose=F
     ``alg`` = "krp_free" (KRPFreeNormal, the reference default) or "krp" (KRPNormal);
     both compute the same MTTKRP and differ only in rounding order.
     ``record`` (optional list) receives per-sweep dicts with the MTTKRP of every
-    mode, for per-call parity checks.
+    mode, for per-call parity checks.  ``work_dtype`` is the factors' element type
+    (the reference keeps the target's element type, cpd.jl:100-105; FP64 by default
+    here for parity work).
     Returns (factors, lam, check, n_fallbacks).
     """
     if check is None:
         check = NoCheck(100 if maxiter is None else maxiter)
     mttkrp = mttkrp_krp_free if alg == "krp_free" else mttkrp_krp
-    factors = [np.array(F, dtype=np.float64) for F in factors]
-    lam = np.array(lam, dtype=np.float64)
+    factors = [np.array(F, dtype=work_dtype) for F in factors]
+    lam = np.array(lam, dtype=work_dtype)
     N = T.ndim
     grams = [gram(F) for F in factors]
     it = check.iter
@@ -304,9 +311,9 @@ def als_optimize(T, factors, lam, check=None, maxiter=None, alg="krp", verbose=F
             V = hadamard_of_grams(grams, n)
             M = mttkrp(T, factors, n)
             rec["mttkrp"].append(M)
-            X, fb = solve_ls_problem(V, M)
+            X, fb = solve_ls_problem(V.astype(np.float64), M.astype(np.float64))
             n_fallbacks += int(fb)
-            factors[n], lam = row_norm(X)
+            factors[n], lam = row_norm(X.astype(work_dtype))
             grams[n] = gram(factors[n])
         if record is not None:
             rec["factors"] = [F.copy() for F in factors]

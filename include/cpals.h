@@ -133,6 +133,28 @@ int cpals_profile_read(cpals_ctx* ctx, double* mttkrp_ms, int64_t* launches);
 /* Kernel launches enqueued by this handle so far (every libcpals kernel). */
 int cpals_launch_count(cpals_ctx* ctx, int64_t* launches);
 
+/* ---- MTTKRP without any allocation (no counterpart in the reference) ---- */
+
+/* FP64 MTTKRP of `mode` for callers that cannot allocate GPU memory when they need it:
+ * code running under a caching allocator's lock or inside a fixed memory budget, and
+ * plugins that are handed a stream and device buffers by their host, where a
+ * cudaMalloc could fail, block, or synchronise the device.  Nothing is allocated: the
+ * caller passes device buffers and the split-K partial sums use a fixed 16 MiB device
+ * array that every GPU loading the library keeps until the process exits.
+ *   d_tensor     column-major tensor on the current device (CPALS_DTYPE_F64 or _F32)
+ *   d_factors    host array of `order` device pointers, F_m column-major I_m x rank (FP64);
+ *                the entry for `mode` is not read
+ *   d_out        device buffer, I_mode x rank column-major FP64
+ *   stream       cudaStream_t the work is enqueued on (NULL = default stream); the call
+ *                returns once the work is enqueued
+ * Limit: I_mode * rank <= 2^21 (the array holds at least one split's partial sums);
+ * larger sizes return CPALS_E_ARG.  The first call on a device looks up the array's
+ * device address, so make it before any stream capture.  Calls share the array: two
+ * calls that can overlap on the GPU (different streams, or different threads without
+ * ordering) race and corrupt each other's result. */
+int cpals_mttkrp_fp64_noalloc(int order, const int64_t* dims, int64_t rank, int mode, int tensor_dtype,
+                              const void* d_tensor, const double* const* d_factors, double* d_out, void* stream);
+
 /* ---- randomized leverage-score path (LevScoreSampled) ---- */
 
 /* Sampled Khatri-Rao rows: out(s, r) = prod_{m != mode, in mode order} F_m(pivots(s, j_m), r),

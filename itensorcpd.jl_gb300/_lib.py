@@ -66,6 +66,8 @@ SIGNATURES = {
     "cpals_set_profiling": (C.c_int, [_P, C.c_int]),
     "cpals_profile_read": (C.c_int, [_P, _DP, _I64P]),
     "cpals_launch_count": (C.c_int, [_P, _I64P]),
+    "cpals_mttkrp_fp64_noalloc": (C.c_int, [C.c_int, _I64P, C.c_int64, C.c_int, C.c_int, _P, C.POINTER(_DP), _DP,
+                                            _P]),
     "cpals_pivot_hadamard": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _DP]),
     "cpals_fused_flatten_sample": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _P]),
     "cpals_leverage_scores": (C.c_int, [_P, C.c_int, _DP]),

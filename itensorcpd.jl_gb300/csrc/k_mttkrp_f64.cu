@@ -12,6 +12,9 @@
 // range is split across CTAs (split-K); partial sums go to part[split][In][R]
 // and are reduced, in FP64 and in split order, by the solve kernel.
 // The tensor may be FP32 (converted exactly on load) or FP64.
+#include <algorithm>
+#include <atomic>
+
 #include "cpals_internal.cuh"
 
 namespace cpals {
@@ -19,7 +22,9 @@ namespace {
 
 constexpr int BM = 64, BN = 64, CH = 32, NT = 256;
 
-template <typename TT>
+// kColMajor: factors are read column-major (I_m x R, first index fastest) instead of
+// the engine's row-major copies.
+template <typename TT, bool kColMajor = false>
 __global__ void __launch_bounds__(NT) k_mttkrp_f64(const TT* __restrict__ T, FactorSet fs, ModeGeom g, int64_t R,
                                                    int64_t chunks_per_split, double* __restrict__ part,
                                                    const DevCheck* __restrict__ chk) {
@@ -57,7 +62,10 @@ __global__ void __launch_bounds__(NT) k_mttkrp_f64(const TT* __restrict__ T, Fac
       const int64_t r = r0 + tid;
       double s = 1.0;
       if (r < R) {
-        for (int j = 0; j < g.n_outer; ++j) s *= fs.F[g.outer_modes[j]][oidx[j] * R + r];
+        for (int j = 0; j < g.n_outer; ++j) {
+          const int m = g.outer_modes[j];
+          s *= fs.F[m][kColMajor ? (oidx[j] + g.dims[m] * r) : (oidx[j] * R + r)];
+        }
       } else {
         s = 0.0;
       }
@@ -89,7 +97,7 @@ __global__ void __launch_bounds__(NT) k_mttkrp_f64(const TT* __restrict__ T, Fac
       const int cc = e % BN, k = e / BN;
       const int64_t kf = kf0 + k, r = r0 + cc;
       double v = 0.0;
-      if (kf < g.If && r < R) v = Ff[kf * R + r] * s_scale[cc];
+      if (kf < g.If && r < R) v = Ff[kColMajor ? (kf + g.If * r) : (kf * R + r)] * s_scale[cc];
       Bs[k][cc] = v;
     }
     __syncthreads();
@@ -145,3 +153,98 @@ cudaError_t launch_mttkrp_f64(const void* T, int tdtype, const FactorSet& fs, co
 }
 
 }  // namespace cpals
+
+// ---------------------------------------------------------------------------
+// MTTKRP without any allocation
+// ---------------------------------------------------------------------------
+// Some callers cannot allocate GPU memory at the time they need an MTTKRP: code that
+// runs under a caching allocator's lock or inside a memory-budgeted service, plugins
+// that are handed a stream and device buffers by their host, and code paths that must
+// not synchronise the device (cudaMalloc and cudaFree can).  cpals_mttkrp_fp64_noalloc
+// serves them: the caller passes the tensor, the factors and the output as device
+// buffers, and the split-K partial sums live in the fixed array below instead of a
+// handle's buffers.  The array is 16 MiB, held by every GPU that loads the library
+// until the process exits.
+namespace cpals {
+namespace {
+
+constexpr int64_t kNoAllocScratchDoubles = int64_t(1) << 21;  // 16 MiB of FP64 partials
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+constexpr int kNoAllocMaxDevices = 64;
+// Device address of g_noalloc_scratch per device, fetched once per device.
+std::atomic<double*> g_noalloc_ptr[kNoAllocMaxDevices];
+
+__global__ void k_noalloc_reduce(const double* __restrict__ part, int S, int64_t In, int64_t R,
+                                 double* __restrict__ out) {
+  // partials are [split][In][R]; the output is column-major In x R
+  const int64_t n = In * R;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R, r = e % R;
+    double s = 0.0;
+    for (int sp = 0; sp < S; ++sp) s += part[(int64_t)sp * n + e];
+    out[i + In * r] = s;
+  }
+}
+
+}  // namespace
+}  // namespace cpals
+
+extern "C" int cpals_mttkrp_fp64_noalloc(int order, const int64_t* dims, int64_t rank, int mode, int tensor_dtype,
+                                         const void* d_tensor, const double* const* d_factors, double* d_out,
+                                         void* stream) {
+  using namespace cpals;
+  if (order < 2 || order > kMaxOrder || !dims || !d_factors || !d_tensor || !d_out) return CPALS_E_ARG;
+  if (mode < 0 || mode >= order || rank < 1) return CPALS_E_ARG;
+  if (tensor_dtype != CPALS_DTYPE_F64 && tensor_dtype != CPALS_DTYPE_F32) return CPALS_E_ARG;
+  for (int m = 0; m < order; ++m) {
+    if (dims[m] < 1 || dims[m] > (int64_t(1) << 31)) return CPALS_E_ARG;
+    if (m != mode && !d_factors[m]) return CPALS_E_ARG;
+  }
+  // The partial sums of one split need In * R doubles; the array must hold at least one.
+  if (dims[mode] * rank > kNoAllocScratchDoubles) {
+    fprintf(stderr,
+            "libcpals: cpals_mttkrp_fp64_noalloc: I_mode * rank = %lld exceeds the %lld-double scratch array\n",
+            (long long)(dims[mode] * rank), (long long)kNoAllocScratchDoubles);
+    return CPALS_E_ARG;
+  }
+  int dev = 0;
+  CPALS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return CPALS_E_UNSUPPORTED;
+  double* scratch = g_noalloc_ptr[dev].load();
+  if (!scratch) {
+    // First call on this device (the current device): look up the array's device address.
+    CPALS_CUDA_TRY(cudaGetSymbolAddress(reinterpret_cast<void**>(&scratch), g_noalloc_scratch));
+    g_noalloc_ptr[dev].store(scratch);
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int num_sms = 0;
+  CPALS_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+  const ModeGeom g = make_geom(order, dims, mode, CH);
+  int64_t cps = 0;
+  int splits = mttkrp_f64_splits(g, rank, num_sms, &cps);
+  const int64_t per_split = g.In * rank;
+  const int64_t max_splits = kNoAllocScratchDoubles / per_split;
+  if (splits > max_splits) {
+    // fewer, longer splits so that every split's partials fit the array
+    cps = (g.nchunks + max_splits - 1) / max_splits;
+    splits = (int)((g.nchunks + cps - 1) / cps);
+  }
+  FactorSet fs{};
+  for (int m = 0; m < order; ++m) fs.F[m] = d_factors[m];
+  dim3 grid((unsigned)((g.In + BM - 1) / BM), (unsigned)((rank + BN - 1) / BN), (unsigned)splits);
+  // Every split writes all of its In x R partials, so nothing in the array needs clearing.
+  if (tensor_dtype == CPALS_DTYPE_F64)
+    k_mttkrp_f64<double, true><<<grid, NT, 0, st>>>(static_cast<const double*>(d_tensor), fs, g, rank, cps, scratch,
+                                                    nullptr);
+  else
+    k_mttkrp_f64<float, true><<<grid, NT, 0, st>>>(static_cast<const float*>(d_tensor), fs, g, rank, cps, scratch,
+                                                   nullptr);
+  CPALS_CUDA_TRY(cudaGetLastError());
+  const int64_t n = per_split;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  k_noalloc_reduce<<<blocks, 256, 0, st>>>(scratch, splits, g.In, rank, d_out);
+  CPALS_CUDA_TRY(cudaGetLastError());
+  return CPALS_OK;
+}
+

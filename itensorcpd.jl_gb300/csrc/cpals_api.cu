@@ -33,6 +33,7 @@ struct cpals_ctx {
   int64_t rpad = 0;
   double* G[kMaxOrder] = {};
   double* lam = nullptr;
+  double* lam_inv = nullptr;
   double* X = nullptr;
   double* Graw = nullptr;
   void* part = nullptr;
@@ -147,11 +148,11 @@ int enqueue_sweep(cpals_ctx* c) {
     CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W, c->info,
                                      c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
     CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->chk, c->st));
-    CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->G[n], gs, N, last, c->inner_rows, In, c->chk, c->traj,
-                                   c->traj_cap, c->st));
+    CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->lam_inv, c->G[n], gs, N, last, c->inner_rows, In, c->chk,
+                                   c->traj, c->traj_cap, c->st));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
-    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[n], c->F32t[n], c->ld32[n], c->F32r[n], c->rpad,
+    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32t[n], c->ld32[n], c->F32r[n], c->rpad,
                                     last ? nullptr : c->chk, c->st));
     if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, n, c->F[n], last ? nullptr : c->chk, c->st));
   }
@@ -298,6 +299,7 @@ int cpals_destroy(cpals_ctx* c) {
   }
   cudaFree(c->dT_owned);
   cudaFree(c->lam);
+  cudaFree(c->lam_inv);
   cudaFree(c->X);
   cudaFree(c->Graw);
   cudaFree(c->part);
@@ -420,6 +422,7 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   int maxS2 = 1;
   for (int m = 0; m < order; ++m) maxS2 = std::max(maxS2, c->gS2[m]);
   CK(dmalloc(&c->lam, R));
+  CK(dmalloc(&c->lam_inv, R));
   CK(dmalloc(&c->X, (size_t)maxI * R));
   CK(dmalloc(&c->Graw, (size_t)R * R));
   CK(dmalloc(&c->work, factorize_work_doubles((int)R)));
@@ -781,9 +784,9 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
   // row_norm, Gram refresh, FP32 copy
   CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[mode], c->gpart, c->gcnt, c->Graw, nullptr, c->st));
   const GramSet gs = gram_set(c);
-  CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->G[mode], gs, c->order, 0, nullptr, In, nullptr, c->traj,
-                                 c->traj_cap, c->st));
-  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], c->F32r[mode],
+  CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->lam_inv, c->G[mode], gs, c->order, 0, nullptr, In, nullptr,
+                                 c->traj, c->traj_cap, c->st));
+  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], c->F32r[mode],
                                   c->rpad, nullptr, c->st));
   if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, mode, c->F[mode], nullptr, c->st));
   return check_derr(c);

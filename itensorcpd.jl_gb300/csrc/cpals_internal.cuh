@@ -113,13 +113,13 @@ cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part
 
 // lambda = sqrt(diag Graw), G_n = Graw ./ (lambda lambda^T); on the last mode also the fit
 // and the device check update (trajectory entry per sweep).
-cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* Gn, const GramSet& gs, int order,
-                            int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
+cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
+                            int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st);
 
-// F = X ./ lambda (lambda may be null: plain copy), an FP32 column-major copy [R][ld32] and
-// (when F32r is non-null) an FP32 row-major copy [In][rpad].
-cudaError_t launch_normalize(const double* X, const double* lam, int64_t In, int R, double* F, float* F32t,
+// F = X .* (1 ./ lambda) (lam_inv may be null: plain copy), an FP32 column-major copy
+// [R][ld32] and (when F32r is non-null) an FP32 row-major copy [In][rpad].
+cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32t,
                              int64_t ld32, float* F32r, int64_t rpad, const DevCheck* chk, cudaStream_t st);
 
 // Row-major rows x cols -> row-major cols x rows (FP64).

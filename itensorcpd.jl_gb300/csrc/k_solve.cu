@@ -17,6 +17,7 @@
 // FP64 runs at 2 FMA/clk/SM on GB300, so every O(I_n R^2) piece is spread over many
 // CTAs; only the O(R^3) factorisation is a single CTA, and it runs on a side stream
 // concurrently with the MTTKRP of the same mode.
+#include <climits>
 #include <cmath>
 
 #include "cpals_internal.cuh"
@@ -26,6 +27,7 @@ namespace {
 
 constexpr double kCholTol = 1e-6;  // src/ITensorCPD.jl:2 cholesky_epsilon
 constexpr int FT = 256;            // factorize threads
+constexpr int kInvSmemMaxR = 90;   // A, U^{-1} and V^{-1} all in shared memory up to this rank
 
 __device__ __forceinline__ bool done_flag(const DevCheck* chk) { return chk != nullptr && chk->done; }
 
@@ -274,13 +276,18 @@ __device__ void qr_fallback(const GramSet& gs, int order, int skip, int R, doubl
   __syncthreads();
 }
 
-__device__ __forceinline__ unsigned long long pivot_key(double v) {
-  // non-negative doubles order like their bit patterns; NaN sorts above everything
-  // (it is picked, then rejected by the stopping test like DISNAN); non-positive values
-  // can never pass the stopping test and sort below every positive value
-  if (isnan(v)) return ~0ull;
-  return v > 0.0 ? (unsigned long long)__double_as_longlong(v) : 0ull;
+// Pivot search keys without FP64 instructions (a dependent FP64 compare costs ~150
+// cycles here): the bit pattern of a double read as a signed 64-bit integer orders all
+// non-negative values like the doubles, puts +NaN above +inf, and puts every negative
+// value below zero.  A negative value can never pass the stopping test, so its order
+// among the other negatives does not matter.
+// A NaN of either sign maps to the largest key, so that it is picked and then stops the
+// factorisation (dpstrf's DISNAN test).
+__device__ __forceinline__ long long pivot_key(double v) {
+  const long long k = __double_as_longlong(v);
+  return (k & 0x7fffffffffffffffll) > 0x7ff0000000000000ll ? LLONG_MAX : k;
 }
+__device__ __forceinline__ bool key_is_nan(long long k) { return k == LLONG_MAX; }
 
 __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int skip, int R, double* __restrict__ Aglob,
                                                   double* __restrict__ U, double* __restrict__ dinv,
@@ -288,6 +295,8 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
                                                   double* __restrict__ qwork, SolveInfo* info, DevCheck* chk) {
   if (done_flag(chk)) return;
   extern __shared__ double smA[];
+  // an odd leading dimension in shared memory keeps column accesses free of bank conflicts
+  const int ld = (R <= 128) ? (R | 1) : R;
   double* A = (R <= 128) ? smA : Aglob;
   __shared__ double sv[32];
   __shared__ int si[32];
@@ -304,7 +313,7 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
       double v = 1.0;
       for (int m = 0; m < order; ++m)
         if (m != skip) v *= gs.G[m][e];
-      A[e] = v;
+      A[r * ld + c] = v;
       if (c == r) s_diag[r] = v;
     }
   }
@@ -315,19 +324,19 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
   for (int j = 0; j < R; ++j) {
     if (warp == 0) {
       // pivot: the largest remaining diagonal entry, first index on ties (LAPACK MAXLOC)
-      unsigned long long bk = 0ull;
+      long long bk = LLONG_MIN;
       int bi = R;
       for (int i = j + lane; i < R; i += 32) {
-        const unsigned long long k = pivot_key(s_diag[i]);
+        const long long k = pivot_key(s_diag[i]);
         if (bi == R || k > bk) {  // i increases: strict > keeps the first index on ties
           bk = k;
           bi = i;
         }
       }
-      unsigned long long mk = bk;
+      long long mk = bk;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mk, off);
+        const long long o = __shfl_xor_sync(0xffffffffu, mk, off);
         mk = o > mk ? o : mk;
       }
       int cand = (bi < R && bk == mk) ? bi : 0x7fffffff;
@@ -336,7 +345,9 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
       if (lane == 0) {
         const double pv = s_diag[cand];
         s_p = cand;
-        s_stop = !(pv > kCholTol);  // pivot <= tol or NaN (dpstrf's stopping rule)
+        // pivot <= tol or NaN stops (dpstrf's rule); for a non-NaN key, pv > tol exactly
+        // when its key exceeds the key of tol (a negative pv has a negative key)
+        s_stop = key_is_nan(mk) || !(mk > pivot_key(kCholTol));
         if (!s_stop) {
           // one reciprocal square root instead of a square root and a division
           const double r = rsqrt(pv);
@@ -355,21 +366,21 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
       // symmetric interchange of j and p on upper storage (dpstf2's three DSWAPs)
       for (int k = tid; k < R; k += blockDim.x) {
         if (k < j) {
-          const double t = A[k * R + j];
-          A[k * R + j] = A[k * R + p];
-          A[k * R + p] = t;
+          const double t = A[k * ld + j];
+          A[k * ld + j] = A[k * ld + p];
+          A[k * ld + p] = t;
         } else if (k > p) {
-          const double t = A[j * R + k];
-          A[j * R + k] = A[p * R + k];
-          A[p * R + k] = t;
+          const double t = A[j * ld + k];
+          A[j * ld + k] = A[p * ld + k];
+          A[p * ld + k] = t;
         } else if (k > j && k < p) {
-          const double t = A[j * R + k];
-          A[j * R + k] = A[k * R + p];
-          A[k * R + p] = t;
+          const double t = A[j * ld + k];
+          A[j * ld + k] = A[k * ld + p];
+          A[k * ld + p] = t;
         }
       }
       if (tid == 0) {
-        A[p * R + p] = A[j * R + j];
+        A[p * ld + p] = A[j * ld + j];
         const double td = s_diag[j];
         s_diag[j] = s_diag[p];
         s_diag[p] = td;
@@ -380,16 +391,24 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
     }
     __syncthreads();
     const double rinv = s_rinv;
-    if (tid == 0) A[j * R + j] = s_sqrt;
-    for (int k = j + 1 + tid; k < R; k += blockDim.x) A[j * R + k] *= rinv;
+    if (tid == 0) A[j * ld + j] = s_sqrt;
+    for (int k = j + 1 + tid; k < R; k += blockDim.x) A[j * ld + k] *= rinv;
     __syncthreads();
-    // trailing update of the upper triangle; the diagonal copy follows along
-    for (int i = j + 1 + warp; i < R; i += nw) {
-      const double a = A[j * R + i];
-      for (int k = i + lane; k < R; k += 32) {
-        const double v = fma(-a, A[j * R + k], A[i * R + k]);
-        A[i * R + k] = v;
-        if (k == i) s_diag[i] = v;
+    // trailing update of the upper triangle, one independent element per thread step
+    // (flattened (i, k) pairs); the diagonal copy follows along
+    {
+      const int n = R - j - 1;
+      const int cnt = n * (n + 1) / 2;
+      for (int e = tid; e < cnt; e += blockDim.x) {
+        // row i (0-based within the trailing block) holds n - i entries
+        int i = (int)((2.0f * n + 1.0f - sqrtf((2.0f * n + 1.0f) * (2.0f * n + 1.0f) - 8.0f * e)) * 0.5f);
+        while (i > 0 && e < i * n - i * (i - 1) / 2) --i;
+        while (e >= (i + 1) * n - (i + 1) * i / 2) ++i;
+        const int k = i + (e - (i * n - i * (i - 1) / 2));
+        const int gi = j + 1 + i, gk = j + 1 + k;
+        const double v = fma(-A[j * ld + gi], A[j * ld + gk], A[gi * ld + gk]);
+        A[gi * ld + gk] = v;
+        if (gk == gi) s_diag[gi] = v;
       }
     }
     __syncthreads();
@@ -404,57 +423,84 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
     double* UT = U + (size_t)R * R;
     for (int e = tid; e < R * R; e += blockDim.x) {
       const int r = e / R, c = e % R;
-      const double u = (c >= r) ? A[e] : 0.0;
+      const double u = (c >= r) ? A[r * ld + c] : 0.0;
       U[e] = u;
       UT[(size_t)c * R + r] = u;
     }
     for (int k = tid; k < R; k += blockDim.x) {
-      dinv[k] = 1.0 / A[k * R + k];
+      dinv[k] = 1.0 / A[k * ld + k];
       piv[k] = s_piv[k];
     }
     __syncthreads();
     // The solve operator W = V^{-1} = P U^{-1} U^{-T} P^T, so that the row solves become
-    // one parallel FP64 product X = M W^T instead of 2R dependent steps per row.
-    // Uinv = U^{-1} (upper), row by row from the bottom: Uinv[k][c] for c >= k.
-    double* Uinv = qwork;           // R x R
-    double* Wp = qwork + (size_t)R * R;  // R x R (pivoted order)
-    for (int e = tid; e < R * R; e += blockDim.x) Uinv[e] = 0.0;
+    // one parallel FP64 product X = M W^T.  FP64 on this part runs at 2 DFMA/clk/SM with
+    // ~128-cycle dependent latency, so both steps are written as independent updates
+    // rather than dot-product chains.
+    // (1) Z = U^{-1} by column-oriented back substitution: for l = R-1..0, row l of Z is
+    //     finished (scaled by 1/U_ll), then eliminated from the rows above it.
+    // Z and Wp live in shared memory after A when they fit (global memory latency on
+    // every elimination step would dominate otherwise)
+    const bool zs = (R <= kInvSmemMaxR);
+    const int lz = zs ? ld : R;
+    double* Z = zs ? smA + (size_t)R * ld : qwork;                       // R x R, leading dim lz
+    double* Wp = zs ? smA + 2 * (size_t)R * ld : qwork + (size_t)R * R;  // R x R (pivoted order)
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int r = e / R, c = e % R;
+      Z[r * lz + c] = (r == c) ? 1.0 : 0.0;
+    }
     __syncthreads();
-    for (int k = R - 1; k >= 0; --k) {
-      const double dk = dinv[k];
-      for (int c = k + tid; c < R; c += blockDim.x) {
-        double a0 = (c == k) ? 1.0 : 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        int l = k + 1;
-        for (; l + 3 <= c; l += 4) {
-          a0 = fma(-A[k * R + l], Uinv[l * R + c], a0);
-          a1 = fma(-A[k * R + l + 1], Uinv[(l + 1) * R + c], a1);
-          a2 = fma(-A[k * R + l + 2], Uinv[(l + 2) * R + c], a2);
-          a3 = fma(-A[k * R + l + 3], Uinv[(l + 3) * R + c], a3);
-        }
-        for (; l <= c; ++l) a0 = fma(-A[k * R + l], Uinv[l * R + c], a0);
-        Uinv[k * R + c] = ((a0 + a1) + (a2 + a3)) * dk;
+    for (int l = R - 1; l >= 0; --l) {
+      const double dl = dinv[l];
+      for (int c = l + tid; c < R; c += blockDim.x) Z[l * lz + c] *= dl;
+      __syncthreads();
+      const int w = R - l;  // columns c >= l
+      for (int e = tid; e < l * w; e += blockDim.x) {
+        const int k = e / w, c = l + e % w;
+        Z[k * lz + c] = fma(-A[k * ld + l], Z[l * lz + c], Z[k * lz + c]);
       }
       __syncthreads();
     }
-    // Wp = Uinv Uinv^T (symmetric): Wp[a][b] = sum_{l >= max(a,b)} Uinv[a][l] Uinv[b][l]
-    for (int e = tid; e < R * R; e += blockDim.x) {
-      const int a = e / R, b2 = e % R;
-      if (b2 < a) continue;
-      double s0 = 0.0, s1 = 0.0;
-      int l = b2;
-      for (; l + 1 < R; l += 2) {
-        s0 = fma(Uinv[a * R + l], Uinv[b2 * R + l], s0);
-        s1 = fma(Uinv[a * R + l + 1], Uinv[b2 * R + l + 1], s1);
+    // (2) Wp = Z Z^T (symmetric): Wp[a][b] = sum_{l >= max(a, b)} Z[a][l] Z[b][l]; each
+    //     thread owns up to 16 upper-triangle entries and accumulates them side by side.
+    const int nup = R * (R + 1) / 2;
+    for (int base = 0; base < nup; base += 16 * blockDim.x) {
+      int ea[16], eb[16];
+      double acc[16];
+      int lmin = R;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        int t = base + q * blockDim.x + tid;
+        ea[q] = -1;
+        eb[q] = -1;
+        acc[q] = 0.0;
+        if (t < nup) {
+          int r0 = 0;
+          while (t >= R - r0) {  // row r0 of the upper triangle holds R - r0 entries
+            t -= R - r0;
+            ++r0;
+          }
+          ea[q] = r0;
+          eb[q] = r0 + t;
+          lmin = min(lmin, eb[q]);
+        }
       }
-      if (l < R) s0 = fma(Uinv[a * R + l], Uinv[b2 * R + l], s0);
-      Wp[a * R + b2] = s0 + s1;
+      for (int l = lmin; l < R; ++l) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (eb[q] >= 0 && l >= eb[q]) acc[q] = fma(Z[ea[q] * lz + l], Z[eb[q] * lz + l], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (eb[q] >= 0) {
+          Wp[ea[q] * lz + eb[q]] = acc[q];
+          Wp[eb[q] * lz + ea[q]] = acc[q];
+        }
     }
     __syncthreads();
-    // W = P Wp P^T
+    // W = P Wp P^T (symmetric, so it is also W^T)
     for (int e = tid; e < R * R; e += blockDim.x) {
-      const int a = e / R, b2 = e % R;
-      const double v = (b2 >= a) ? Wp[a * R + b2] : Wp[b2 * R + a];
-      W[(size_t)s_piv[a] * R + s_piv[b2]] = v;
+      const int a2 = e / R, b2 = e % R;
+      W[(size_t)s_piv[a2] * R + s_piv[b2]] = Wp[a2 * lz + b2];
     }
   } else {
     if (tid == 0 && chk) atomicAdd(reinterpret_cast<unsigned long long*>(&chk->fallbacks), 1ull);
@@ -489,32 +535,36 @@ __global__ void __launch_bounds__(256) k_solve_gemm(const PT* __restrict__ part,
   const int64_t base = r0 * R;
   const int64_t sstride = In * R;
   for (int e = tid; e < nval; e += blockDim.x) {
-    double s = 0.0;
+    // eight independent FP64 accumulators (a dependent FP64 add costs ~150 cycles here)
+    double acc[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc[t] = 0.0;
     int sp = 0;
     for (; sp + 8 <= S; sp += 8) {
-      double v[8];
 #pragma unroll
-      for (int t = 0; t < 8; ++t) v[t] = (double)part[(int64_t)(sp + t) * sstride + base + e];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) s += v[t];
+      for (int t = 0; t < 8; ++t) acc[t] += (double)part[(int64_t)(sp + t) * sstride + base + e];
     }
-    for (; sp < S; ++sp) s += (double)part[(int64_t)sp * sstride + base + e];
-    Ms[e] = s;
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (sp + t < S) acc[t] += (double)part[(int64_t)(sp + t) * sstride + base + e];
+    Ms[e] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
   }
   __syncthreads();
   for (int e = tid; e < nval; e += blockDim.x) {
     const int row = e / R, k = e % R;
     const double* m = Ms + row * R;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    double a[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) a[t] = 0.0;
     int l = 0;
-    for (; l + 3 < R; l += 4) {
-      a0 = fma(m[l], WT[(size_t)l * R + k], a0);
-      a1 = fma(m[l + 1], WT[(size_t)(l + 1) * R + k], a1);
-      a2 = fma(m[l + 2], WT[(size_t)(l + 2) * R + k], a2);
-      a3 = fma(m[l + 3], WT[(size_t)(l + 3) * R + k], a3);
+    for (; l + 8 <= R; l += 8) {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) a[t] = fma(m[l + t], WT[(size_t)(l + t) * R + k], a[t]);
     }
-    for (; l < R; ++l) a0 = fma(m[l], WT[(size_t)l * R + k], a0);
-    const double x = (a0 + a1) + (a2 + a3);
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (l + t < R) a[t] = fma(m[l + t], WT[(size_t)(l + t) * R + k], a[t]);
+    const double x = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
     X[base + e] = x;
     Ps[e] = m[k] * x;
   }
@@ -563,7 +613,7 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int6
   const int a = threadIdx.x / GT, b = threadIdx.x % GT;
   const int r1 = ti * GT + a, r2 = tj * GT + b;
   const int64_t rb = (int64_t)s * rows_per_split, re = min(In, rb + rows_per_split);
-  double acc = 0.0;
+  double acc = 0.0, acc2 = 0.0;
   for (int64_t i0 = rb; i0 < re; i0 += 64) {
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * GT; e += 256) {
@@ -575,17 +625,28 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int6
     }
     __syncthreads();
 #pragma unroll 8
-    for (int ii = 0; ii < 64; ++ii) acc = fma(xa[ii][a], xb[ii][b], acc);
+    for (int ii = 0; ii < 64; ii += 2) {
+      acc = fma(xa[ii][a], xb[ii][b], acc);
+      acc2 = fma(xa[ii + 1][a], xb[ii + 1][b], acc2);
+    }
   }
-  part[((size_t)tile * S2 + s) * 256 + threadIdx.x] = acc;
+  part[((size_t)tile * S2 + s) * 256 + threadIdx.x] = acc + acc2;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) s_last = (atomicAdd(&counters[tile], 1u) == (unsigned)(S2 - 1));
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  double sum = 0.0;
-  for (int q = 0; q < S2; ++q) sum += __ldcg(&part[((size_t)tile * S2 + q) * 256 + threadIdx.x]);
+  double sq0 = 0.0, sq1 = 0.0, sq2 = 0.0, sq3 = 0.0;
+  int q = 0;
+  for (; q + 4 <= S2; q += 4) {
+    sq0 += __ldcg(&part[((size_t)tile * S2 + q) * 256 + threadIdx.x]);
+    sq1 += __ldcg(&part[((size_t)tile * S2 + q + 1) * 256 + threadIdx.x]);
+    sq2 += __ldcg(&part[((size_t)tile * S2 + q + 2) * 256 + threadIdx.x]);
+    sq3 += __ldcg(&part[((size_t)tile * S2 + q + 3) * 256 + threadIdx.x]);
+  }
+  for (; q < S2; ++q) sq0 += __ldcg(&part[((size_t)tile * S2 + q) * 256 + threadIdx.x]);
+  const double sum = (sq0 + sq1) + (sq2 + sq3);
   if (r1 < R && r2 < R) {
     G[(size_t)r1 * R + r2] = sum;
     G[(size_t)r2 * R + r1] = sum;
@@ -595,6 +656,7 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int6
 
 // ---------------- finalize ----------------
 __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Graw, int R, double* __restrict__ lam,
+                                                  double* __restrict__ lam_inv,
                                                   double* __restrict__ Gn, GramSet gs, int order, int last,
                                                   const double* __restrict__ inner_rows, int64_t In, DevCheck* chk,
                                                   double* __restrict__ traj, int64_t traj_cap) {
@@ -604,10 +666,14 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
   __shared__ double s_inv[CPALS_MAX_RANK_SOLVE];
   const int tid = threadIdx.x;
   for (int r = tid; r < R; r += blockDim.x) {
-    const double l = sqrt(Graw[(size_t)r * R + r]);
+    // lambda_r = sqrt(g) and its reciprocal from a single reciprocal square root
+    const double g = Graw[(size_t)r * R + r];
+    const double ri = rsqrt(g);
+    const double l = g * ri;
     s_lam[r] = l;
-    s_inv[r] = 1.0 / l;
+    s_inv[r] = ri;
     lam[r] = l;
+    lam_inv[r] = ri;
   }
   __syncthreads();
   // R^2 FP64 divisions would cost ~40 us on one SM: multiply by the R reciprocals instead
@@ -625,20 +691,24 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
     c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
     s = t;
   }
-  const double inner = block_sum(s, sv) + block_sum(c, sv);
+  const double inner = block_sum(s, sv) + block_sum(c, sv);  // In / 256 terms per thread
   // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11)
-  s = 0.0;
-  c = 0.0;
-  for (int e = tid; e < R * R; e += blockDim.x) {
-    const int r = e / R, q = e % R;
-    double h = gs.G[0][e];
-    for (int m = 1; m < order; ++m) h *= gs.G[m][e];
-    const double p = h * (s_lam[r] * s_lam[q]);
-    const double t = s + p;
-    c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
-    s = t;
+  // lambda^T (G_1 o ... o G_N) lambda: terms are summed pairwise per thread (independent
+  // products, short dependent chains), then combined across the block
+  double ps0 = 0.0, ps1 = 0.0;
+  {
+    bool odd = false;
+    for (int e = tid; e < R * R; e += blockDim.x, odd = !odd) {
+      const int r = e / R, q = e % R;
+      double h = gs.G[0][e];
+      for (int m = 1; m < order; ++m) h *= gs.G[m][e];
+      const double term = h * (s_lam[r] * s_lam[q]);
+      if (odd) ps1 += term;
+      else ps0 += term;
+    }
   }
-  const double fact_square = block_sum(s, sv) + block_sum(c, sv);
+  s = ps0 + ps1;
+  const double fact_square = block_sum(s, sv);
   if (tid != 0) return;
   DevCheck& k = *chk;
   double fit = NAN;
@@ -690,7 +760,7 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
 }
 
 // ---------------- normalize ----------------
-__global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam, int64_t In, int R,
+__global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam_inv, int64_t In, int R,
                             double* __restrict__ F, float* __restrict__ F32t, int64_t ld32, float* __restrict__ F32r,
                             int64_t rpad, const DevCheck* chk) {
   if (done_flag(chk)) return;
@@ -698,7 +768,7 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / R;
     const int r = (int)(e % R);
-    const double f = lam ? X[e] / lam[r] : X[e];
+    const double f = lam_inv ? X[e] * lam_inv[r] : X[e];
     F[e] = f;
     if (F32t) F32t[(int64_t)r * ld32 + i] = (float)f;
     if (F32r) F32r[i * rpad + r] = (float)f;
@@ -738,10 +808,11 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   double* Aglob = work;
   double* dinv = work + (size_t)R * R;
   double* qwork = dinv + R;
-  const size_t smem = (R <= 128) ? (size_t)R * R * sizeof(double) : 0;
+  size_t smem = (R <= 128) ? (size_t)R * (R | 1) * sizeof(double) : 0;
+  if (R <= kInvSmemMaxR) smem *= 3;  // A, U^{-1}, V^{-1}
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_factorize, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 128 * 8);
+    cudaFuncSetAttribute(k_factorize, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr_set = true;
   }
   k_factorize<<<1, FT, smem, st>>>(gs, order, skip, R, Aglob, U, dinv, piv, W, qwork, info, chk);
@@ -792,18 +863,18 @@ cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part
   return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* Gn, const GramSet& gs, int order,
-                            int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
+cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
+                            int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st) {
-  k_finalize<<<1, 256, 0, st>>>(Graw, R, lam, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap);
+  k_finalize<<<1, 256, 0, st>>>(Graw, R, lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap);
   return cudaGetLastError();
 }
 
-cudaError_t launch_normalize(const double* X, const double* lam, int64_t In, int R, double* F, float* F32t,
+cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32t,
                              int64_t ld32, float* F32r, int64_t rpad, const DevCheck* chk, cudaStream_t st) {
   const int64_t n = In * R;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_normalize<<<blocks, 256, 0, st>>>(X, lam, In, R, F, F32t, ld32, F32r, rpad, chk);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32t, ld32, F32r, rpad, chk);
   return cudaGetLastError();
 }
 

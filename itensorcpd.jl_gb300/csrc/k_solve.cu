@@ -26,8 +26,11 @@ namespace cpals {
 namespace {
 
 constexpr double kCholTol = 1e-6;  // src/ITensorCPD.jl:2 cholesky_epsilon
-constexpr int FT = 256;            // factorize threads
-constexpr int kInvSmemMaxR = 90;   // A, U^{-1} and V^{-1} all in shared memory up to this rank
+// Factorize threads.  FP64 on this part issues at a low rate per warp (2 DFMA/clk/SM at
+// best, 128-cycle latency): the single-CTA factorisation needs many warps per scheduler
+// to keep the FP64 pipes busy (a 2016-FMA sweep step: ~3200 cycles at 256 threads,
+// ~1400 at 1024).
+constexpr int FT = 1024;
 
 __device__ __forceinline__ bool done_flag(const DevCheck* chk) { return chk != nullptr && chk->done; }
 
@@ -300,115 +303,186 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
   double* A = (R <= 128) ? smA : Aglob;
   __shared__ double sv[32];
   __shared__ int si[32];
-  __shared__ double s_diag[CPALS_MAX_RANK_SOLVE];
-  __shared__ double s_sqrt, s_rinv;
-  __shared__ int s_p, s_stop;
   __shared__ int s_piv[CPALS_MAX_RANK_SOLVE];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  // V = ones .* G_a .* G_b ... (mode order, skipping `skip`); upper triangle only
-  for (int e = tid; e < R * R; e += blockDim.x) {
-    const int r = e / R, c = e % R;
-    if (c >= r) {
-      double v = 1.0;
-      for (int m = 0; m < order; ++m)
-        if (m != skip) v *= gs.G[m][e];
-      A[r * ld + c] = v;
-      if (c == r) s_diag[r] = v;
+  // V = ones .* G_a .* G_b ... (mode order, skipping `skip`); upper triangle only.  Eight
+  // elements per thread step, so that their Gram loads are in flight together.
+  for (int e0 = tid; e0 < R * R; e0 += 8 * FT) {
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = 1.0;
+    for (int m = 0; m < order; ++m) {
+      if (m == skip) continue;
+      const double* __restrict__ G = gs.G[m];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * FT;
+        if (e < R * R) v[q] *= G[e];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * FT;
+      if (e < R * R) {
+        const int r = e / R, c = e - r * R;
+        if (c >= r) A[r * ld + c] = v[q];
+      }
     }
   }
   for (int k = tid; k < R; k += blockDim.x) s_piv[k] = k;
   __syncthreads();
 
-  int rank = R;
-  for (int j = 0; j < R; ++j) {
-    if (warp == 0) {
-      // pivot: the largest remaining diagonal entry, first index on ties (LAPACK MAXLOC)
-      long long bk = LLONG_MIN;
-      int bi = R;
-      for (int i = j + lane; i < R; i += 32) {
-        const long long k = pivot_key(s_diag[i]);
-        if (bi == R || k > bk) {  // i increases: strict > keeps the first index on ties
-          bk = k;
-          bi = i;
-        }
-      }
-      long long mk = bk;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const long long o = __shfl_xor_sync(0xffffffffu, mk, off);
-        mk = o > mk ? o : mk;
-      }
-      int cand = (bi < R && bk == mk) ? bi : 0x7fffffff;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) cand = min(cand, __shfl_xor_sync(0xffffffffu, cand, off));
-      if (lane == 0) {
-        const double pv = s_diag[cand];
-        s_p = cand;
-        // pivot <= tol or NaN stops (dpstrf's rule); for a non-NaN key, pv > tol exactly
-        // when its key exceeds the key of tol (a negative pv has a negative key)
-        s_stop = key_is_nan(mk) || !(mk > pivot_key(kCholTol));
-        if (!s_stop) {
-          // one reciprocal square root instead of a square root and a division
-          const double r = rsqrt(pv);
-          s_sqrt = pv * r;
-          s_rinv = r;
-        }
+  // Pivoted symmetric sweep (Gauss-Jordan on the symmetric matrix, Goodnight 1979):
+  // sweeping index k replaces A by
+  //   A(i,j) - A(i,k) A(k,j) / d,  A(i,k) / d,  -1/d        (i, j != k; d = A(k,k)).
+  // The unswept block always holds the Schur complement of the swept one, so its
+  // diagonal is the one dpstrf (pivoted Cholesky, tol 1e-6) picks its pivots from: the
+  // pivot sequence, the rank and the stopping rule are dpstrf's.  After all R indices
+  // are swept, A = -V^{-1}: the solve operator comes out of the same R steps, with no
+  // interchanges and no separate triangular inversion.  The rows of the Cholesky factor
+  // U (needed by the leverage scores) are the Schur rows at each step, divided by the
+  // square root of the pivot; they are kept unscaled and finished after the loop.
+  __shared__ double s_a[CPALS_MAX_RANK_SOLVE];  // pivot row before the step
+  __shared__ double s_t[CPALS_MAX_RANK_SOLVE];  // pivot row divided by the pivot
+  __shared__ double s_dp[CPALS_MAX_RANK_SOLVE]; // pivot values in step order
+  __shared__ unsigned char s_swept[CPALS_MAX_RANK_SOLVE];
+  __shared__ double s_pv, s_pinv;               // next pivot value and its reciprocal
+  __shared__ int s_p, s_stop;                   // next pivot index, stop flag
+  double* Uo = qwork;                           // unscaled Schur rows, [step][original index]
+  for (int k = tid; k < R; k += blockDim.x) s_swept[k] = 0;
+  // Pivot search (warp 0) over the unswept diagonal entries offered by each lane.  The
+  // largest wins, first index on ties (LAPACK MAXLOC); the 64-bit key is reduced as its
+  // signed high word, then its low word among the lanes holding the maximum high word,
+  // then the smallest index among the lanes holding the maximum key.  Lane 0 publishes
+  // the pivot and its reciprocal, or the stop flag (pivot <= tol or NaN, dpstrf's rule).
+  auto pick_pivot = [&](long long bk, int bi) {
+    const int khi = (int)(bk >> 32);
+    const int mhi = __reduce_max_sync(0xffffffffu, khi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
+    const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
+    const int p = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+    if (lane == 0) {
+      // for a non-NaN key, the pivot exceeds tol exactly when its key exceeds the key of
+      // tol (a negative value has a negative key)
+      const int stop = key_is_nan(mk) || !(mk > pivot_key(kCholTol));
+      s_stop = stop;
+      s_p = p;
+      if (!stop) {
+        const double pv = __longlong_as_double(mk);
+        s_pv = pv;
+        s_pinv = 1.0 / pv;
       }
     }
-    __syncthreads();
+    __syncwarp();  // warp 0 meets the block barrier converged
+  };
+  __syncthreads();
+  if (warp == 0) {
+    long long bk = LLONG_MIN;
+    int bi = R;
+    for (int i = lane; i < R; i += 32) {
+      const long long key = pivot_key(A[i * ld + i]);
+      if (bi == R || key > bk) {  // i increases: strict > keeps the first index on ties
+        bk = key;
+        bi = i;
+      }
+    }
+    pick_pivot(bk, bi);
+  }
+  __syncthreads();
+
+  int rank = R;
+  for (int j = 0; j < R; ++j) {
     if (s_stop) {
       rank = j;
       break;
     }
-    const int p = s_p;
-    if (p != j) {
-      // symmetric interchange of j and p on upper storage (dpstf2's three DSWAPs)
-      for (int k = tid; k < R; k += blockDim.x) {
-        if (k < j) {
-          const double t = A[k * ld + j];
-          A[k * ld + j] = A[k * ld + p];
-          A[k * ld + p] = t;
-        } else if (k > p) {
-          const double t = A[j * ld + k];
-          A[j * ld + k] = A[p * ld + k];
-          A[p * ld + k] = t;
-        } else if (k > j && k < p) {
-          const double t = A[j * ld + k];
-          A[j * ld + k] = A[k * ld + p];
-          A[k * ld + p] = t;
-        }
-      }
-      if (tid == 0) {
-        A[p * ld + p] = A[j * ld + j];
-        const double td = s_diag[j];
-        s_diag[j] = s_diag[p];
-        s_diag[p] = td;
-        const int t = s_piv[j];
-        s_piv[j] = s_piv[p];
-        s_piv[p] = t;
-      }
+    const int k = s_p;
+    const double dk = s_pinv;
+    // snapshot of the pivot row (upper storage: A(k,i) sits at (min, max)); the unswept
+    // part of it is row j of U times sqrt(pivot)
+    for (int i = tid; i < R; i += blockDim.x) {
+      const double a = (i <= k) ? A[i * ld + k] : A[k * ld + i];
+      s_a[i] = a;
+      s_t[i] = a * dk;
+      Uo[(size_t)j * R + i] = (s_swept[i] || i == k) ? 0.0 : a;
+    }
+    if (tid == 0) {
+      s_piv[j] = k;
+      s_dp[j] = s_pv;
     }
     __syncthreads();
-    const double rinv = s_rinv;
-    if (tid == 0) A[j * ld + j] = s_sqrt;
-    for (int k = j + 1 + tid; k < R; k += blockDim.x) A[j * ld + k] *= rinv;
-    __syncthreads();
-    // trailing update of the upper triangle, one independent element per thread step
-    // (flattened (i, k) pairs); the diagonal copy follows along
-    {
-      const int n = R - j - 1;
-      const int cnt = n * (n + 1) / 2;
-      for (int e = tid; e < cnt; e += blockDim.x) {
-        // row i (0-based within the trailing block) holds n - i entries
-        int i = (int)((2.0f * n + 1.0f - sqrtf((2.0f * n + 1.0f) * (2.0f * n + 1.0f) - 8.0f * e)) * 0.5f);
-        while (i > 0 && e < i * n - i * (i - 1) / 2) --i;
-        while (e >= (i + 1) * n - (i + 1) * i / 2) ++i;
-        const int k = i + (e - (i * n - i * (i - 1) / 2));
-        const int gi = j + 1 + i, gk = j + 1 + k;
-        const double v = fma(-A[j * ld + gi], A[j * ld + gk], A[gi * ld + gk]);
-        A[gi * ld + gk] = v;
-        if (gk == gi) s_diag[gi] = v;
+    if (warp == 0) {
+      // the diagonal, then (look-ahead) the next pivot and its reciprocal, while the
+      // other warps update the off-diagonal entries
+      if (tid == 0) s_swept[k] = 1;
+      long long bk = LLONG_MIN;
+      int bi = R;
+      for (int i = lane; i < R; i += 32) {
+        if (i == k) {
+          A[i * ld + i] = -dk;
+          continue;
+        }
+        const double v = fma(-s_a[i], s_t[i], A[i * ld + i]);
+        A[i * ld + i] = v;
+        if (!s_swept[i]) {
+          const long long key = pivot_key(v);
+          if (bi == R || key > bk) {
+            bk = key;
+            bi = i;
+          }
+        }
+      }
+      if (j + 1 < R) pick_pivot(bk, bi);
+    } else if (warp & 3) {
+      // Strictly upper entries (i < c).  Row i (R-1-i entries) is paired with row R-2-i
+      // (i+1 entries): R entries per pair, pair q at t < R-1-q is (q, q+1+t), else
+      // (R-2-q, t).  The work units are (pair, 32 consecutive t), dealt round-robin to
+      // the warps on schedulers 1-3 (warp % 4 != 0), so that warp 0's diagonal FMA and
+      // reciprocal on scheduler 0 do not queue behind update FMAs; four units per thread
+      // step, loads issued before the FMAs, integer index arithmetic only.  Row and
+      // column k take A(i,k) / d.
+      const int npair = R / 2;  // rows 0..R-2; with R even the middle row pairs with itself
+      const int nchunk = (R + 31) >> 5;
+      const int nunit = npair * nchunk;
+      const int nwk = (blockDim.x >> 5) / 4 * 3;
+      const int wk = (warp >> 2) * 3 + (warp & 3) - 1;
+      for (int u0 = wk; u0 < nunit; u0 += 4 * nwk) {
+        int idx[4];
+        double av[4], xv[4], yv[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int u = u0 + b * nwk;
+          idx[b] = -1;
+          av[b] = xv[b] = yv[b] = 0.0;
+          int i = -1, c = -1;
+          if (u < nunit) {
+            const int q = u / nchunk;
+            const int t = (u - q * nchunk) * 32 + lane;
+            if (t < R - 1 - q) {
+              i = q;
+              c = q + 1 + t;
+            } else if (t < R && R - 2 - q != q) {  // the middle row of an even R is listed once
+              i = R - 2 - q;
+              c = i + 1 + (t - (R - 1 - q));
+            }
+          }
+          if (i >= 0) {
+            idx[b] = i * ld + c;
+            if (i == k) {
+              av[b] = s_t[c];  // new A(k,c) = A(k,c) / d
+            } else if (c == k) {
+              av[b] = s_t[i];
+            } else {
+              av[b] = A[idx[b]];
+              xv[b] = s_a[i];
+              yv[b] = s_t[c];
+            }
+          }
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          if (idx[b] >= 0) A[idx[b]] = fma(-xv[b], yv[b], av[b]);
       }
     }
     __syncthreads();
@@ -420,87 +494,27 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
     info->qr_rank = rank;
   }
   if (rank == R) {
+    // W = -A (symmetric; also W^T)
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int r = e / R, c = e - r * R;
+      W[e] = -((r <= c) ? A[r * ld + c] : A[c * ld + r]);
+    }
+    // U in pivoted order: U(j,j) = sqrt(d_j), U(j,c) = Uo(j, piv(c)) / sqrt(d_j) for c > j
+    for (int jj = tid; jj < R; jj += blockDim.x) {
+      const double ri = rsqrt(s_dp[jj]);
+      s_a[jj] = ri;
+      dinv[jj] = ri;
+      piv[jj] = s_piv[jj];
+    }
+    __syncthreads();
     double* UT = U + (size_t)R * R;
     for (int e = tid; e < R * R; e += blockDim.x) {
-      const int r = e / R, c = e % R;
-      const double u = (c >= r) ? A[r * ld + c] : 0.0;
+      const int r = e / R, c = e - r * R;
+      double u = 0.0;
+      if (c == r) u = s_dp[r] * s_a[r];
+      else if (c > r) u = Uo[(size_t)r * R + s_piv[c]] * s_a[r];
       U[e] = u;
       UT[(size_t)c * R + r] = u;
-    }
-    for (int k = tid; k < R; k += blockDim.x) {
-      dinv[k] = 1.0 / A[k * ld + k];
-      piv[k] = s_piv[k];
-    }
-    __syncthreads();
-    // The solve operator W = V^{-1} = P U^{-1} U^{-T} P^T, so that the row solves become
-    // one parallel FP64 product X = M W^T.  FP64 on this part runs at 2 DFMA/clk/SM with
-    // ~128-cycle dependent latency, so both steps are written as independent updates
-    // rather than dot-product chains.
-    // (1) Z = U^{-1} by column-oriented back substitution: for l = R-1..0, row l of Z is
-    //     finished (scaled by 1/U_ll), then eliminated from the rows above it.
-    // Z and Wp live in shared memory after A when they fit (global memory latency on
-    // every elimination step would dominate otherwise)
-    const bool zs = (R <= kInvSmemMaxR);
-    const int lz = zs ? ld : R;
-    double* Z = zs ? smA + (size_t)R * ld : qwork;                       // R x R, leading dim lz
-    double* Wp = zs ? smA + 2 * (size_t)R * ld : qwork + (size_t)R * R;  // R x R (pivoted order)
-    for (int e = tid; e < R * R; e += blockDim.x) {
-      const int r = e / R, c = e % R;
-      Z[r * lz + c] = (r == c) ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    for (int l = R - 1; l >= 0; --l) {
-      const double dl = dinv[l];
-      for (int c = l + tid; c < R; c += blockDim.x) Z[l * lz + c] *= dl;
-      __syncthreads();
-      const int w = R - l;  // columns c >= l
-      for (int e = tid; e < l * w; e += blockDim.x) {
-        const int k = e / w, c = l + e % w;
-        Z[k * lz + c] = fma(-A[k * ld + l], Z[l * lz + c], Z[k * lz + c]);
-      }
-      __syncthreads();
-    }
-    // (2) Wp = Z Z^T (symmetric): Wp[a][b] = sum_{l >= max(a, b)} Z[a][l] Z[b][l]; each
-    //     thread owns up to 16 upper-triangle entries and accumulates them side by side.
-    const int nup = R * (R + 1) / 2;
-    for (int base = 0; base < nup; base += 16 * blockDim.x) {
-      int ea[16], eb[16];
-      double acc[16];
-      int lmin = R;
-#pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        int t = base + q * blockDim.x + tid;
-        ea[q] = -1;
-        eb[q] = -1;
-        acc[q] = 0.0;
-        if (t < nup) {
-          int r0 = 0;
-          while (t >= R - r0) {  // row r0 of the upper triangle holds R - r0 entries
-            t -= R - r0;
-            ++r0;
-          }
-          ea[q] = r0;
-          eb[q] = r0 + t;
-          lmin = min(lmin, eb[q]);
-        }
-      }
-      for (int l = lmin; l < R; ++l) {
-#pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (eb[q] >= 0 && l >= eb[q]) acc[q] = fma(Z[ea[q] * lz + l], Z[eb[q] * lz + l], acc[q]);
-      }
-#pragma unroll
-      for (int q = 0; q < 16; ++q)
-        if (eb[q] >= 0) {
-          Wp[ea[q] * lz + eb[q]] = acc[q];
-          Wp[eb[q] * lz + ea[q]] = acc[q];
-        }
-    }
-    __syncthreads();
-    // W = P Wp P^T (symmetric, so it is also W^T)
-    for (int e = tid; e < R * R; e += blockDim.x) {
-      const int a2 = e / R, b2 = e % R;
-      W[(size_t)s_piv[a2] * R + s_piv[b2]] = Wp[a2 * lz + b2];
     }
   } else {
     if (tid == 0 && chk) atomicAdd(reinterpret_cast<unsigned long long*>(&chk->fallbacks), 1ull);
@@ -808,8 +822,7 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   double* Aglob = work;
   double* dinv = work + (size_t)R * R;
   double* qwork = dinv + R;
-  size_t smem = (R <= 128) ? (size_t)R * (R | 1) * sizeof(double) : 0;
-  if (R <= kInvSmemMaxR) smem *= 3;  // A, U^{-1}, V^{-1}
+  const size_t smem = (R <= 128) ? (size_t)R * (R | 1) * sizeof(double) : 0;
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_factorize, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

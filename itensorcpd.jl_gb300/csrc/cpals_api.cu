@@ -144,16 +144,15 @@ int enqueue_sweep(cpals_ctx* c) {
       c->prof_used += 2;
     }
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->st, c->ev_side[n], 0));
-    c->launches += 6;
+    c->launches += (c->tc && n <= 1) ? 6 : 5;  // factorize, MTTKRP, solve, gram+finalize, normalize (+ BF16 factor tiles)
     CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W, c->info,
                                      c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
-    CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->chk, c->st));
-    CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->lam_inv, c->G[n], gs, N, last, c->inner_rows, In, c->chk,
-                                   c->traj, c->traj_cap, c->st));
+    CPALS_CUDA_TRY(launch_gram_finalize(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->lam, c->lam_inv,
+                                        c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32t[n], c->ld32[n], c->F32r[n], c->rpad,
-                                    last ? nullptr : c->chk, c->st));
+                                    c->Graw, c->G[n], last ? nullptr : c->chk, c->st));
     if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, n, c->F[n], last ? nullptr : c->chk, c->st));
   }
   return CPALS_OK;
@@ -430,9 +429,9 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   CK(dmalloc(&c->piv, R));
   CK(dmalloc(&c->W, (size_t)R * R));
   CK(dmalloc(&c->info, 1));
-  CK(dmalloc(&c->gpart, (size_t)gram_tiles((int)R) * maxS2 * 256));
-  CK(dmalloc(&c->gcnt, gram_tiles((int)R)));
-  CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * gram_tiles((int)R)));
+  CK(dmalloc(&c->gpart, (size_t)gram_tiles((int)R) * (maxS2 * 256 + 1)));
+  CK(dmalloc(&c->gcnt, gram_tiles((int)R) + 1));
+  CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * (gram_tiles((int)R) + 1)));
   CK(dmalloc(&c->inner_rows, maxI));
   CK(dmalloc(&c->chk, 1));
   CPALS_CUDA_TRY(cudaMemset(c->chk, 0, sizeof(DevCheck)));
@@ -496,7 +495,7 @@ int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const dou
     colmajor_to_rowmajor_host(host_factors[m], c->dims[m], R, tmp.data());
     CPALS_CUDA_TRY(cudaMemcpyAsync(c->F[m], tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c->st));
     CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32t[m], c->ld32[m], c->F32r[m],
-                                    c->rpad, nullptr, c->st));
+                                    c->rpad, nullptr, nullptr, nullptr, c->st));
     if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, m, c->F[m], nullptr, c->st));
     CPALS_CUDA_TRY(launch_gram(c->F[m], c->dims[m], R, c->gS2[m], c->gpart, c->gcnt, c->G[m], nullptr, c->st));
     c->launches += 2;
@@ -596,7 +595,7 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
     for (int64_t k = 0; k < b; ++k) {
       if (use_graph) {
         CPALS_CUDA_TRY(cudaGraphLaunch(c->graph, c->st));
-        c->launches += 6 * c->order;
+        c->launches += 5 * c->order + (c->tc ? std::min(c->order, 2) : 0);
       } else {
         int rc = enqueue_sweep(c);
         if (rc != CPALS_OK) return rc;
@@ -787,7 +786,7 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
   CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->lam_inv, c->G[mode], gs, c->order, 0, nullptr, In, nullptr,
                                  c->traj, c->traj_cap, c->st));
   CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], c->F32r[mode],
-                                  c->rpad, nullptr, c->st));
+                                  c->rpad, nullptr, nullptr, nullptr, c->st));
   if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, mode, c->F[mode], nullptr, c->st));
   return check_derr(c);
 }

@@ -105,11 +105,19 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
                               double* inner_rows, const DevCheck* chk, cudaStream_t st);
 
 // G = X^T X (row-major X, In x R) over S2 row splits; part: gram_tiles(R)*S2*256 doubles,
-// counters: gram_tiles(R) zero-initialised unsigneds (left zeroed after each launch).
+// counters: gram_tiles(R)+1 zero-initialised unsigneds (left zeroed after each launch).
 int gram_tiles(int R);
 int gram_splits(int64_t In, int R, int num_sms);
 cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters, double* G,
                         const DevCheck* chk, cudaStream_t st);
+
+// launch_gram followed, in the last block to finish, by launch_finalize's work on Graw
+// (without G_n, which launch_normalize then writes).  part needs gram_tiles(R)*(S2*256+1)
+// doubles.
+cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters,
+                                 double* Graw, double* lam, double* lam_inv, double* Gn, const GramSet& gs, int order,
+                                 int last, const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap,
+                                 cudaStream_t st);
 
 // lambda = sqrt(diag Graw), G_n = Graw ./ (lambda lambda^T); on the last mode also the fit
 // and the device check update (trajectory entry per sweep).
@@ -118,9 +126,11 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_
                             int64_t traj_cap, cudaStream_t st);
 
 // F = X .* (1 ./ lambda) (lam_inv may be null: plain copy), an FP32 column-major copy
-// [R][ld32] and (when F32r is non-null) an FP32 row-major copy [In][rpad].
+// [R][ld32], (when F32r is non-null) an FP32 row-major copy [In][rpad] and (when Gn is
+// non-null) the normalised Gram Gn = Graw ./ (lambda lambda^T).
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32t,
-                             int64_t ld32, float* F32r, int64_t rpad, const DevCheck* chk, cudaStream_t st);
+                             int64_t ld32, float* F32r, int64_t rpad, const double* Graw, double* Gn,
+                             const DevCheck* chk, cudaStream_t st);
 
 // Row-major rows x cols -> row-major cols x rows (FP64).
 cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);

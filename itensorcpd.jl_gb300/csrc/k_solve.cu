@@ -532,40 +532,92 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // ---------------- solve: X = M W^T ----------------
 // M rows are the split-K partial sums (added in split order, FP64); W^T is the solve
 // operator from the factorisation (V^{-1}, or the pivoted-QR least-squares operator),
-// stored so that consecutive output columns are contiguous.  One thread per output;
-// per-row sums of M .* X (Neumaier) feed the fit.
+// stored so that consecutive output columns are contiguous.  One thread per output.
+// FP64 here has ~128-cycle latency and a low issue rate per warp, so every loop keeps
+// many independent loads or accumulators in flight: W^T is staged in shared memory (when
+// it fits) while the partial sums load, the partials are summed by eight accumulators,
+// and each output by eight.  Per-row sums of M .* X (a tree over the row) feed the fit.
+constexpr int SOLVE_T = 256;
+constexpr int kSolveStageMaxR = 128;  // W^T (R^2 doubles) staged in shared memory up to here
 template <typename PT>
-__global__ void __launch_bounds__(256) k_solve_gemm(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
-                                                    const double* __restrict__ WT, double* __restrict__ X,
-                                                    double* __restrict__ inner_rows, const DevCheck* chk) {
+__global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
+                                                        const double* __restrict__ WT, double* __restrict__ X,
+                                                        double* __restrict__ inner_rows, const DevCheck* chk) {
   if (done_flag(chk)) return;
   extern __shared__ double sm[];
   double* Ms = sm;            // RB x R
   double* Ps = sm + RB * R;   // RB x R products for the fit
+  const bool staged = (R <= kSolveStageMaxR);
+  double* Ws = sm + 2 * RB * R;
   const int tid = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * RB;
   const int rows = (In - r0 < (int64_t)RB) ? (int)(In - r0) : RB;
   const int nval = rows * R;
   const int64_t base = r0 * R;
   const int64_t sstride = In * R;
-  for (int e = tid; e < nval; e += blockDim.x) {
-    // eight independent FP64 accumulators (a dependent FP64 add costs ~150 cycles here)
-    double acc[8];
+  if (staged) {
+    const int n = R * R;
+    for (int e0 = tid; e0 < n; e0 += 8 * SOLVE_T) {
+      double w[8];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) acc[t] = 0.0;
-    int sp = 0;
-    for (; sp + 8 <= S; sp += 8) {
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * SOLVE_T;
+        w[q] = (e < n) ? __ldg(&WT[e]) : 0.0;
+      }
 #pragma unroll
-      for (int t = 0; t < 8; ++t) acc[t] += (double)part[(int64_t)(sp + t) * sstride + base + e];
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * SOLVE_T;
+        if (e < n) Ws[e] = w[q];
+      }
     }
+  }
+  for (int e = tid; e < nval; e += SOLVE_T) {
+    if constexpr (sizeof(PT) == 4) {
+      // FP32 partials: a compensated (Neumaier) sum in FP32, finished in FP64.  Its error
+      // is O(S eps32^2) of the summed magnitudes, and it keeps the conversions and adds
+      // off the FP64 pipe, which the product below saturates.
+      float sacc = 0.0f, cacc = 0.0f;
+      int sp = 0;
+      for (; sp + 16 <= S; sp += 16) {
+        float v[16];
 #pragma unroll
-    for (int t = 0; t < 8; ++t)
-      if (sp + t < S) acc[t] += (double)part[(int64_t)(sp + t) * sstride + base + e];
-    Ms[e] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+        for (int t = 0; t < 16; ++t) v[t] = part[(int64_t)(sp + t) * sstride + base + e];
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const float tt = sacc + v[t];
+          cacc += (fabsf(sacc) >= fabsf(v[t])) ? ((sacc - tt) + v[t]) : ((v[t] - tt) + sacc);
+          sacc = tt;
+        }
+      }
+      for (; sp < S; ++sp) {
+        const float p = part[(int64_t)sp * sstride + base + e];
+        const float tt = sacc + p;
+        cacc += (fabsf(sacc) >= fabsf(p)) ? ((sacc - tt) + p) : ((p - tt) + sacc);
+        sacc = tt;
+      }
+      Ms[e] = (double)sacc + (double)cacc;
+    } else {
+      double acc[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) acc[t] = 0.0;
+      int sp = 0;
+      for (; sp + 16 <= S; sp += 16) {
+        PT v[16];
+#pragma unroll
+        for (int t = 0; t < 16; ++t) v[t] = part[(int64_t)(sp + t) * sstride + base + e];
+#pragma unroll
+        for (int t = 0; t < 16; ++t) acc[t & 7] += (double)v[t];
+      }
+#pragma unroll
+      for (int t = 0; t < 16; ++t)
+        if (sp + t < S) acc[t & 7] += (double)part[(int64_t)(sp + t) * sstride + base + e];
+      Ms[e] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+    }
   }
   __syncthreads();
-  for (int e = tid; e < nval; e += blockDim.x) {
-    const int row = e / R, k = e % R;
+  const double* W = staged ? Ws : WT;
+  for (int e = tid; e < nval; e += SOLVE_T) {
+    const int row = e / R, k = e - row * R;
     const double* m = Ms + row * R;
     double a[8];
 #pragma unroll
@@ -573,156 +625,151 @@ __global__ void __launch_bounds__(256) k_solve_gemm(const PT* __restrict__ part,
     int l = 0;
     for (; l + 8 <= R; l += 8) {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) a[t] = fma(m[l + t], WT[(size_t)(l + t) * R + k], a[t]);
+      for (int t = 0; t < 8; ++t) a[t] = fma(m[l + t], W[(size_t)(l + t) * R + k], a[t]);
     }
 #pragma unroll
     for (int t = 0; t < 8; ++t)
-      if (l + t < R) a[t] = fma(m[l + t], WT[(size_t)(l + t) * R + k], a[t]);
+      if (l + t < R) a[t] = fma(m[l + t], W[(size_t)(l + t) * R + k], a[t]);
     const double x = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
     X[base + e] = x;
     Ps[e] = m[k] * x;
   }
   if (!inner_rows) return;
   __syncthreads();
-  // per-row Neumaier sum of M .* X, one warp per row
-  const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  // per-row sum of M .* X: one warp per row, a tree over the lanes
+  const int lane = tid & 31, warp = tid >> 5, nw = SOLVE_T >> 5;
   for (int row = warp; row < rows; row += nw) {
-    double s = 0.0, c = 0.0;
-    for (int k = lane; k < R; k += 32) {
-      const double p = Ps[row * R + k];
-      const double t = s + p;
-      c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
-      s = t;
+    double sa = 0.0, sb = 0.0;
+    int kk = lane;
+    for (; kk + 32 < R; kk += 64) {
+      sa += Ps[row * R + kk];
+      sb += Ps[row * R + kk + 32];
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      const double o = __shfl_down_sync(0xffffffffu, s, off);
-      const double oc = __shfl_down_sync(0xffffffffu, c, off);
-      const double t = s + o;
-      c += ((fabs(s) >= fabs(o)) ? ((s - t) + o) : ((o - t) + s)) + oc;
-      s = t;
-    }
-    if (lane == 0) inner_rows[r0 + row] = s + c;
+    if (kk < R) sa += Ps[row * R + kk];
+    double v = sa + sb;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) inner_rows[r0 + row] = v;
   }
 }
 
-// ---------------- gram ----------------
-constexpr int GT = 16;  // tile edge
-__global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int64_t In, int R, int S2,
-                                              int64_t rows_per_split, double* __restrict__ part,
-                                              unsigned* __restrict__ counters, double* __restrict__ G,
-                                              const DevCheck* chk) {
-  if (done_flag(chk)) return;
-  __shared__ double xa[64][GT + 1];
-  __shared__ double xb[64][GT + 1];
-  __shared__ int s_last;
-  const int nt = (R + GT - 1) / GT;
-  // blockIdx.x enumerates upper-triangle tiles (ti <= tj)
-  int t = blockIdx.x, ti = 0;
-  while (t >= nt - ti) {
-    t -= nt - ti;
-    ++ti;
-  }
-  const int tj = ti + t;
-  const int tile = blockIdx.x, s = blockIdx.y;
-  const int a = threadIdx.x / GT, b = threadIdx.x % GT;
-  const int r1 = ti * GT + a, r2 = tj * GT + b;
-  const int64_t rb = (int64_t)s * rows_per_split, re = min(In, rb + rows_per_split);
-  double acc = 0.0, acc2 = 0.0;
-  for (int64_t i0 = rb; i0 < re; i0 += 64) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < 64 * GT; e += 256) {
-      const int ii = e / GT, c = e % GT;
-      const int64_t i = i0 + ii;
-      const int ca = ti * GT + c, cb = tj * GT + c;
-      xa[ii][c] = (i < re && ca < R) ? X[i * R + ca] : 0.0;
-      xb[ii][c] = (i < re && cb < R) ? X[i * R + cb] : 0.0;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int ii = 0; ii < 64; ii += 2) {
-      acc = fma(xa[ii][a], xb[ii][b], acc);
-      acc2 = fma(xa[ii + 1][a], xb[ii + 1][b], acc2);
-    }
-  }
-  part[((size_t)tile * S2 + s) * 256 + threadIdx.x] = acc + acc2;
-  __threadfence();
+// ---------------- gram + finalize ----------------
+// Warp-level sum as a tree (deterministic), then across the warps of the block.
+__device__ double block_tree_sum(double v, double* sv) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   __syncthreads();
-  if (threadIdx.x == 0) s_last = (atomicAdd(&counters[tile], 1u) == (unsigned)(S2 - 1));
+  if (lane == 0) sv[w] = v;
   __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  double sq0 = 0.0, sq1 = 0.0, sq2 = 0.0, sq3 = 0.0;
-  int q = 0;
-  for (; q + 4 <= S2; q += 4) {
-    sq0 += __ldcg(&part[((size_t)tile * S2 + q) * 256 + threadIdx.x]);
-    sq1 += __ldcg(&part[((size_t)tile * S2 + q + 1) * 256 + threadIdx.x]);
-    sq2 += __ldcg(&part[((size_t)tile * S2 + q + 2) * 256 + threadIdx.x]);
-    sq3 += __ldcg(&part[((size_t)tile * S2 + q + 3) * 256 + threadIdx.x]);
-  }
-  for (; q < S2; ++q) sq0 += __ldcg(&part[((size_t)tile * S2 + q) * 256 + threadIdx.x]);
-  const double sum = (sq0 + sq1) + (sq2 + sq3);
-  if (r1 < R && r2 < R) {
-    G[(size_t)r1 * R + r2] = sum;
-    G[(size_t)r2 * R + r1] = sum;
-  }
-  if (threadIdx.x == 0) counters[tile] = 0u;
+  double t = (lane < nw) ? sv[lane] : 0.0;
+  for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+  __syncthreads();
+  return t;
 }
 
-// ---------------- finalize ----------------
-__global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Graw, int R, double* __restrict__ lam,
-                                                  double* __restrict__ lam_inv,
-                                                  double* __restrict__ Gn, GramSet gs, int order, int last,
-                                                  const double* __restrict__ inner_rows, int64_t In, DevCheck* chk,
-                                                  double* __restrict__ traj, int64_t traj_cap) {
-  if (done_flag(chk)) return;
+struct FinalizeArgs {
+  double* lam;
+  double* lam_inv;
+  double* Gn;  // written here only when fpart is null (else by the normalisation kernel)
+  GramSet gs;
+  int order;
+  int last;
+  const double* inner_rows;
+  int64_t In;
+  DevCheck* chk;
+  double* traj;
+  int64_t traj_cap;
+  int mode;       // the mode whose raw Gram is being finalised
+  double* fpart;  // per-tile partials of ||X||^2 (fused path), or null
+  int ntiles;
+};
+
+// lambda = sqrt(diag Graw) (one reciprocal square root per column), G_n = Graw ./
+// (lambda lambda^T) by the reciprocals; on the last mode the fit (fit_check.jl:22-43)
+// and the device FitCheck / NoCheck update.  One block; loads are issued eight at a
+// time (a single FP64 dependent chain costs ~128 cycles per step here).  `coherent`
+// reads Graw through L2 (written by other blocks of the same launch).
+__device__ void finalize_body(const double* __restrict__ Graw, int R, const FinalizeArgs& fa, bool coherent) {
   __shared__ double sv[32];
   __shared__ double s_lam[CPALS_MAX_RANK_SOLVE];
   __shared__ double s_inv[CPALS_MAX_RANK_SOLVE];
-  const int tid = threadIdx.x;
-  for (int r = tid; r < R; r += blockDim.x) {
-    // lambda_r = sqrt(g) and its reciprocal from a single reciprocal square root
-    const double g = Graw[(size_t)r * R + r];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  auto ld = [&](const double* p) { return coherent ? __ldcg(p) : *p; };
+  for (int r = tid; r < R; r += nt) {
+    const double g = ld(&Graw[(size_t)r * R + r]);
     const double ri = rsqrt(g);
     const double l = g * ri;
     s_lam[r] = l;
     s_inv[r] = ri;
-    lam[r] = l;
-    lam_inv[r] = ri;
+    fa.lam[r] = l;
+    fa.lam_inv[r] = ri;
   }
   __syncthreads();
-  // R^2 FP64 divisions would cost ~40 us on one SM: multiply by the R reciprocals instead
-  for (int e = tid; e < R * R; e += blockDim.x) {
-    const int r = e / R, c = e % R;
-    Gn[e] = Graw[e] * s_inv[r] * s_inv[c];
-  }
-  if (!last) return;
-  __syncthreads();
-  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28)
-  double s = 0.0, c = 0.0;
-  for (int64_t i = tid; i < In; i += blockDim.x) {
-    const double p = inner_rows[i];
-    const double t = s + p;
-    c += (fabs(s) >= fabs(p)) ? ((s - t) + p) : ((p - t) + s);
-    s = t;
-  }
-  const double inner = block_sum(s, sv) + block_sum(c, sv);  // In / 256 terms per thread
-  // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11)
-  // lambda^T (G_1 o ... o G_N) lambda: terms are summed pairwise per thread (independent
-  // products, short dependent chains), then combined across the block
-  double ps0 = 0.0, ps1 = 0.0;
-  {
-    bool odd = false;
-    for (int e = tid; e < R * R; e += blockDim.x, odd = !odd) {
-      const int r = e / R, q = e % R;
-      double h = gs.G[0][e];
-      for (int m = 1; m < order; ++m) h *= gs.G[m][e];
-      const double term = h * (s_lam[r] * s_lam[q]);
-      if (odd) ps1 += term;
-      else ps0 += term;
+  const int n = R * R;
+  for (int e0 = tid; !fa.fpart && e0 < n; e0 += 8 * nt) {
+    double g[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * nt;
+      g[q] = (e < n) ? ld(&Graw[e]) : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * nt;
+      if (e < n) {
+        const int r = e / R, c = e - r * R;
+        fa.Gn[e] = g[q] * s_inv[r] * s_inv[c];
+      }
     }
   }
-  s = ps0 + ps1;
-  const double fact_square = block_sum(s, sv);
+  if (!fa.last) return;
+  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28)
+  double ia = 0.0, ib = 0.0;
+  {
+    int64_t i = tid;
+    for (; i + nt < fa.In; i += 2 * nt) {
+      ia += fa.inner_rows[i];
+      ib += fa.inner_rows[i + nt];
+    }
+    if (i < fa.In) ia += fa.inner_rows[i];
+  }
+  const double inner = block_tree_sum(ia + ib, sv);
+  // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11).  With the
+  // per-tile partials (fused path) it is their sum in tile order; otherwise the products
+  // of eight elements are formed side by side.
+  double ps[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) ps[q] = 0.0;
+  if (fa.fpart && tid == 0)
+    for (int t = 0; t < fa.ntiles; ++t) ps[t & 7] += __ldcg(&fa.fpart[t]);
+  for (int e0 = tid; !fa.fpart && e0 < n; e0 += 8 * nt) {
+    double h[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * nt;
+      h[q] = (e < n) ? fa.gs.G[0][e] : 0.0;
+    }
+    for (int m = 1; m < fa.order; ++m) {
+      const double* __restrict__ Gm = fa.gs.G[m];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * nt;
+        if (e < n) h[q] *= Gm[e];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * nt;
+      if (e < n) {
+        const int r = e / R, c = e - r * R;
+        ps[q] += h[q] * (s_lam[r] * s_lam[c]);
+      }
+    }
+  }
+  const double fact_square =
+      block_tree_sum(((ps[0] + ps[1]) + (ps[2] + ps[3])) + ((ps[4] + ps[5]) + (ps[6] + ps[7])), sv);
+  DevCheck* chk = fa.chk;
+  double* traj = fa.traj;
+  const int64_t traj_cap = fa.traj_cap;
   if (tid != 0) return;
   DevCheck& k = *chk;
   double fit = NAN;
@@ -773,13 +820,124 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
   }
 }
 
+
+constexpr int GT = 16;  // tile edge
+// G = X^T X over 16x16 upper tiles and S2 row splits; the last split of each tile sums
+// the S2 partials (in split order) and writes the tile and its mirror; with FIN the last
+// tile to finish runs finalize_body.  Rows are loaded 64 at a time, only real rows, and
+// each output keeps four accumulators.
+template <bool FIN>
+__global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int64_t In, int R, int S2,
+                                              int64_t rows_per_split, double* __restrict__ part,
+                                              unsigned* __restrict__ counters, double* __restrict__ G,
+                                              const DevCheck* chk, FinalizeArgs fa) {
+  if (done_flag(chk)) return;
+  __shared__ double xa[64][GT + 1];
+  __shared__ double xb[64][GT + 1];
+  __shared__ int s_last;
+  const int nt = (R + GT - 1) / GT;
+  const int ntiles = nt * (nt + 1) / 2;
+  // blockIdx.x enumerates upper-triangle tiles (ti <= tj)
+  int t = blockIdx.x, ti = 0;
+  while (t >= nt - ti) {
+    t -= nt - ti;
+    ++ti;
+  }
+  const int tj = ti + t;
+  const int tile = blockIdx.x, s = blockIdx.y;
+  const int a = threadIdx.x / GT, b = threadIdx.x % GT;
+  const int r1 = ti * GT + a, r2 = tj * GT + b;
+  const int64_t rb = (int64_t)s * rows_per_split;
+  const int64_t re = (In < rb + rows_per_split) ? In : rb + rows_per_split;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t i0 = rb; i0 < re; i0 += 64) {
+    const int nr = (re - i0 < 64) ? (int)(re - i0) : 64;
+    __syncthreads();
+    {
+      double va[4], vb[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * 256;  // 64 rows x 16 columns
+        const int ii = e / GT, c = e % GT;
+        const int ca = ti * GT + c, cb = tj * GT + c;
+        va[q] = (ii < nr && ca < R) ? X[(i0 + ii) * R + ca] : 0.0;
+        vb[q] = (ii < nr && cb < R) ? X[(i0 + ii) * R + cb] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int e = threadIdx.x + q * 256;
+        xa[e / GT][e % GT] = va[q];
+        xb[e / GT][e % GT] = vb[q];
+      }
+    }
+    __syncthreads();
+    int ii = 0;
+    for (; ii + 4 <= nr; ii += 4) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = fma(xa[ii + q][a], xb[ii + q][b], acc[q]);
+    }
+    for (; ii < nr; ++ii) acc[0] = fma(xa[ii][a], xb[ii][b], acc[0]);
+  }
+  part[((size_t)tile * S2 + s) * 256 + threadIdx.x] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(&counters[tile], 1u) == (unsigned)(S2 - 1));
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double sq[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) sq[q] = 0.0;
+  int q0 = 0;
+  for (; q0 + 8 <= S2; q0 += 8) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sq[q] += __ldcg(&part[((size_t)tile * S2 + q0 + q) * 256 + threadIdx.x]);
+  }
+  for (int q = 0; q0 + q < S2; ++q) sq[q] += __ldcg(&part[((size_t)tile * S2 + q0 + q) * 256 + threadIdx.x]);
+  const double sum = ((sq[0] + sq[1]) + (sq[2] + sq[3])) + ((sq[4] + sq[5]) + (sq[6] + sq[7]));
+  if (r1 < R && r2 < R) {
+    G[(size_t)r1 * R + r2] = sum;
+    G[(size_t)r2 * R + r1] = sum;
+  }
+  if (threadIdx.x == 0) counters[tile] = 0u;
+  if (!FIN) return;
+  if (fa.last) {
+    // this tile's share of ||X||^2 = sum(Graw .* prod_{m != mode} G_m) (lambda_r lambda_c
+    // times the normalised Gram of this mode is its raw Gram); off-diagonal tiles count twice
+    double h = 0.0;
+    if (r1 < R && r2 < R) {
+      h = (ti == tj) ? sum : 2.0 * sum;
+      for (int m = 0; m < fa.order; ++m)
+        if (m != fa.mode) h *= fa.gs.G[m][(size_t)r1 * R + r2];
+    }
+    __shared__ double sv_t[32];
+    const double tsum = block_tree_sum(h, sv_t);
+    if (threadIdx.x == 0) fa.fpart[tile] = tsum;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(&counters[ntiles], 1u) == (unsigned)(ntiles - 1));
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) counters[ntiles] = 0u;
+  finalize_body(G, R, fa, true);
+}
+
+__global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Graw, int R, FinalizeArgs fa) {
+  if (done_flag(fa.chk)) return;
+  finalize_body(Graw, R, fa, false);
+}
+
 // ---------------- normalize ----------------
 __global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam_inv, int64_t In, int R,
                             double* __restrict__ F, float* __restrict__ F32t, int64_t ld32, float* __restrict__ F32r,
-                            int64_t rpad, const DevCheck* chk) {
+                            int64_t rpad, const double* __restrict__ Graw, double* __restrict__ Gn,
+                            const DevCheck* chk) {
   if (done_flag(chk)) return;
   const int64_t n = In * R;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     const int64_t i = e / R;
     const int r = (int)(e % R);
     const double f = lam_inv ? X[e] * lam_inv[r] : X[e];
@@ -787,6 +945,12 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
     if (F32t) F32t[(int64_t)r * ld32 + i] = (float)f;
     if (F32r) F32r[i * rpad + r] = (float)f;
   }
+  // the normalised Gram G_n = Graw ./ (lambda lambda^T), by the reciprocals
+  if (Gn)
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)R * R; e += stride) {
+      const int r = (int)(e / R), c = (int)(e % R);
+      Gn[e] = Graw[e] * lam_inv[r] * lam_inv[c];
+    }
 }
 
 __global__ void k_transpose(const double* __restrict__ src, int64_t rows, int64_t cols, double* __restrict__ dst) {
@@ -843,13 +1007,21 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
   (void)info;
   const int RB = solve_rows_per_block(R);
   dim3 grid((unsigned)((In + RB - 1) / RB));
-  const size_t smem = (size_t)2 * RB * R * sizeof(double);
+  size_t smem = (size_t)2 * RB * R * sizeof(double);
+  if (R <= kSolveStageMaxR) smem += (size_t)R * R * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    const int mx = 2 * 256 * 8 + kSolveStageMaxR * kSolveStageMaxR * 8;
+    cudaFuncSetAttribute(k_solve_gemm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_solve_gemm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    attr_set = true;
+  }
   if (part_is_f32)
-    k_solve_gemm<float><<<grid, 256, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X, inner_rows,
-                                                 chk);
+    k_solve_gemm<float><<<grid, SOLVE_T, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X,
+                                                     inner_rows, chk);
   else
-    k_solve_gemm<double><<<grid, 256, smem, st>>>(static_cast<const double*>(part), splits, In, R, RB, W, X,
-                                                  inner_rows, chk);
+    k_solve_gemm<double><<<grid, SOLVE_T, smem, st>>>(static_cast<const double*>(part), splits, In, R, RB, W, X,
+                                                      inner_rows, chk);
   return cudaGetLastError();
 }
 
@@ -872,22 +1044,38 @@ cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part
                         const DevCheck* chk, cudaStream_t st) {
   const int64_t rps = (In + S2 - 1) / S2;
   dim3 grid((unsigned)gram_tiles(R), (unsigned)S2);
-  k_gram<<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, G, chk);
+  k_gram<false><<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, G, chk, FinalizeArgs{});
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters,
+                                 double* Graw, double* lam, double* lam_inv, double* Gn, const GramSet& gs, int order,
+                                 int last, const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap,
+                                 cudaStream_t st) {
+  const int64_t rps = (In + S2 - 1) / S2;
+  dim3 grid((unsigned)gram_tiles(R), (unsigned)S2);
+  const int ntiles = gram_tiles(R);
+  // per-tile partials of ||X||^2 live after the tile partial sums
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1,
+                  part + (size_t)ntiles * S2 * 256, ntiles};
+  k_gram<true><<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, Graw, chk, fa);
   return cudaGetLastError();
 }
 
 cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st) {
-  k_finalize<<<1, 256, 0, st>>>(Graw, R, lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap);
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, nullptr, 0};
+  k_finalize<<<1, 256, 0, st>>>(Graw, R, fa);
   return cudaGetLastError();
 }
 
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32t,
-                             int64_t ld32, float* F32r, int64_t rpad, const DevCheck* chk, cudaStream_t st) {
+                             int64_t ld32, float* F32r, int64_t rpad, const double* Graw, double* Gn,
+                             const DevCheck* chk, cudaStream_t st) {
   const int64_t n = In * R;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32t, ld32, F32r, rpad, chk);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32t, ld32, F32r, rpad, Graw, Gn, chk);
   return cudaGetLastError();
 }
 

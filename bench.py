@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparator and CPU baseline legs")
+    ap.add_argument("--workload", choices=["c2", "c3"], default="c2",
+                    help="c2: 512^3 rank 64 (the headline line); c3: 128^4 rank 128, dimension tree, "
+                         "plain and randomized paths")
     ap.add_argument("--profile-mttkrp", action="store_true",
                     help="only set up the workload and run one MTTKRP per mode (a small case for ncu)")
     return ap.parse_args()
@@ -208,6 +211,91 @@ def cpu_baseline_sample(pkg, T):
                       "512^3 workload, FP32 data, numpy/OpenBLAS on all host threads"}
 
 
+C3_DIMS = (128, 128, 128, 128)
+C3_RANK = 128
+C3_SWEEPS = 10
+
+
+def run_c3(args, pkg, L, device):
+    """Order-4 128^4 FP32, rank 128, congruence 0.3, 30 dB: sweeps/s of the dimension-tree
+    engine, the plain (one full MTTKRP per mode) engine and the plain FP64 GPU engine, all
+    from the same start; the dimension tree's full-contraction time per call; and the
+    randomized path (16384 leverage-score samples per mode, host-drawn indices, device
+    gathers) in sweeps/s."""
+    from itensorcpd_gb300.synthetic import lowrank_plus_noise
+
+    T_host, keep = pinned_like(C3_DIMS)
+    rng = np.random.default_rng(SEED + 3)
+    lowrank_plus_noise(C3_DIMS, C3_RANK, 0.3, 30.0, rng, dtype=np.float32, out=T_host)
+    ref_norm = float(np.linalg.norm(T_host.reshape(-1).astype(np.float64)))
+    F0, lam0 = pkg.random_factors(C3_DIMS, C3_RANK, np.random.default_rng(3))
+
+    def nocheck(n):
+        c = L.CpalsCheck()
+        c.kind = L.CHECK_NONE
+        c.max_counter = n
+        c.ref_norm = ref_norm
+        return c
+
+    out = {}
+    for key, prec, dt, sweeps in (("dimtree", "bf16x3", True, C3_SWEEPS), ("plain", "bf16x3", False, C3_SWEEPS),
+                                   ("fp64_gpu", "fp64", False, 2)):
+        with pkg.Engine(C3_DIMS, C3_RANK, dtype=np.float32, precision=prec, device=device, dimtree=dt) as e:
+            e.set_tensor(T_host)
+            for _ in range(1 if key == "fp64_gpu" else max(1, args.warmup)):
+                e.set_factors(F0, lam0)
+                e.optimize(nocheck(sweeps))
+            e.synchronize()
+            l0 = e.launch_count()
+            e.timer_start()
+            for _ in range(1 if key == "fp64_gpu" else args.steps):
+                e.set_factors(F0, lam0)
+                tr = e.optimize(nocheck(sweeps))
+            ms = e.timer_stop()
+            n = (1 if key == "fp64_gpu" else args.steps) * sweeps
+            out[key] = {"sweeps_per_s": n / (ms / 1e3), "fit_after": float(tr[-1]), "sweeps": sweeps,
+                        "gpu_launches": int(e.launch_count() - l0)}
+            if prec == "bf16x3":
+                e.set_profiling(True)
+                e.set_factors(F0, lam0)
+                e.optimize(nocheck(1))
+                mt_ms, mt_n = e.profile_read()
+                e.set_profiling(False)
+                out[key]["mttkrp_ms_per_mode_avg"] = mt_ms / max(1, mt_n)
+    # tensor passes: the tree streams T twice per sweep, the plain path four times
+    tbytes = 4.0 * np.prod(C3_DIMS)
+    for key, passes in (("dimtree", 2), ("plain", 4)):
+        out[key]["tensor_passes_per_sweep"] = passes
+        out[key]["alg_bytes_per_sweep_gb"] = passes * tbytes / 1e9
+    # randomized ALS: 16384 samples per mode, one sweep = four sampled solves
+    api = pkg.api
+    cp = pkg.CPD([f.copy() for f in F0], lam0.copy())
+    t0 = time.perf_counter()
+    api.als_optimize(T_host, cp, alg=pkg.LevScoreSampled(16384), check=pkg.NoCheck(1), device=device,
+                     rng=np.random.default_rng(7))
+    t_first = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nrand = 3
+    res = api.als_optimize(T_host, cp, alg=pkg.LevScoreSampled(16384), check=pkg.NoCheck(nrand), device=device,
+                           rng=np.random.default_rng(7))
+    t_rand = time.perf_counter() - t0
+    out["randomized"] = {"samples_per_mode": 16384, "sweeps_per_s": nrand / t_rand,
+                         "note": "host wall clock through the Python API, including host sampling and tensor "
+                                 "upload per call; first call (with setup) took %.3f s" % t_first}
+    line = {
+        "metric": "cp_als_sweeps_per_s", "value": out["dimtree"]["sweeps_per_s"], "unit": "sweeps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3/f32-accumulate mttkrp, f64 solve", "data": "synthetic",
+        "config": {"workload": "cpals_128x128x128x128_fp32_rank128_lowrank_noise_30dB_dimtree", "dims": list(C3_DIMS),
+                   "rank": C3_RANK, "congruence": 0.3, "snr_db": 30.0, "sweeps_per_step": C3_SWEEPS},
+        "c3": out,
+        "speedup_dimtree_vs_plain": out["dimtree"]["sweeps_per_s"] / out["plain"]["sweeps_per_s"],
+        "speedup_dimtree_vs_fp64_gpu": out["dimtree"]["sweeps_per_s"] / out["fp64_gpu"]["sweeps_per_s"],
+    }
+    print(json.dumps(line), flush=True)
+    del keep
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -218,6 +306,11 @@ def main():
 
     pkg = __graft_entry__.load_package()
     from itensorcpd_gb300 import _lib as L
+
+    if args.workload == "c3":
+        if rank == 0:
+            run_c3(args, pkg, L, local if world > 1 else 0)
+        return
 
     dist = None
     if world > 1:

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "cpals_internal.cuh"
+#include "cpals_dimtree.cuh"
 #include "cpals_tc.cuh"
 
 using namespace cpals;
@@ -67,12 +68,16 @@ struct cpals_ctx {
   int* derr = nullptr;
   // tensor-core path
   TcState* tc = nullptr;
+  // order-4 dimension tree (CPALS_FLAG_DIMTREE): its own contraction plans, and M_n in FP64
+  DimTree* dt = nullptr;
+  double* Mdt = nullptr;
   // measurement
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool profiling = false;
   std::vector<cudaEvent_t> prof_ev;  // pairs
   int64_t prof_used = 0;
   int64_t launches = 0;
+  int64_t sweep_launches = 0;  // kernel launches of one sweep (set when the graph is built)
 };
 
 namespace {
@@ -118,6 +123,18 @@ void invalidate_graph(cpals_ctx* c) {
   c->graph = nullptr;
 }
 
+// The FP32/BF16 copies a new factor of mode m feeds (tensor-core and dimension-tree paths).
+cudaError_t update_factor_tiles(cpals_ctx* c, int m, const DevCheck* chk) {
+  if (c->tc) return tc_update_factor(c->tc, m, c->F[m], chk, c->st);
+  if (c->dt) return dt_update_factor(c->dt, m, c->F[m], chk, c->st);
+  return cudaSuccess;
+}
+int factor_tile_launches(const cpals_ctx* c, int m) {
+  if (c->tc) return m <= 1 ? 1 : 0;
+  if (c->dt && c->mmode == CPALS_MTTKRP_BF16X3) return (m == 0 || m == 2) ? 1 : 0;
+  return 0;
+}
+
 cudaError_t enqueue_mttkrp(cpals_ctx* c, int n, const DevCheck* chk) {
   if (c->mmode == CPALS_MTTKRP_FP64)
     return launch_mttkrp_f64(c->dT, c->tdtype, factor_set(c), c->geom[n], c->R, c->splits[n], c->cps[n],
@@ -138,22 +155,34 @@ int enqueue_sweep(cpals_ctx* c) {
     CPALS_CUDA_TRY(cudaEventRecord(c->ev_side[n], c->side));
     const bool prof = c->profiling && c->prof_used + 2 <= (int64_t)c->prof_ev.size();
     if (prof) CPALS_CUDA_TRY(cudaEventRecord(c->prof_ev[c->prof_used], c->st));
-    CPALS_CUDA_TRY(enqueue_mttkrp(c, n, c->chk));
+    if (c->dt) {
+      const double* fp[kMaxOrder] = {};
+      for (int m = 0; m < N; ++m) fp[m] = c->F[m];
+      CPALS_CUDA_TRY(dt_mttkrp(c->dt, n, fp, true, c->Mdt, c->chk, c->st));
+      c->launches += dt_launches(c->dt, n, true) - 1;
+    } else {
+      CPALS_CUDA_TRY(enqueue_mttkrp(c, n, c->chk));
+    }
     if (prof) {
       CPALS_CUDA_TRY(cudaEventRecord(c->prof_ev[c->prof_used + 1], c->st));
       c->prof_used += 2;
     }
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->st, c->ev_side[n], 0));
-    c->launches += (c->tc && n <= 1) ? 6 : 5;  // factorize, MTTKRP, solve, gram+finalize, normalize (+ BF16 factor tiles)
-    CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W, c->info,
-                                     c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
+    // factorize, MTTKRP, solve, gram+finalize, normalize (+ BF16 factor tiles)
+    c->launches += 5 + factor_tile_launches(c, n);
+    if (c->dt)
+      CPALS_CUDA_TRY(launch_solve_rows(c->Mdt, 0, 1, In, R, c->work, c->U, c->piv, c->W, c->info, c->X,
+                                       last ? c->inner_rows : nullptr, c->chk, c->st));
+    else
+      CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W,
+                                       c->info, c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
     CPALS_CUDA_TRY(launch_gram_finalize(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->lam, c->lam_inv,
                                         c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32t[n], c->ld32[n], c->F32r[n], c->rpad,
                                     c->Graw, c->G[n], last ? nullptr : c->chk, c->st));
-    if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, n, c->F[n], last ? nullptr : c->chk, c->st));
+    CPALS_CUDA_TRY(update_factor_tiles(c, n, last ? nullptr : c->chk));
   }
   return CPALS_OK;
 }
@@ -164,6 +193,7 @@ int build_graph(cpals_ctx* c) {
   CPALS_CUDA_TRY(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
   const int64_t before = c->launches;
   int rc = enqueue_sweep(c);
+  c->sweep_launches = c->launches - before;
   c->launches = before;  // capture enqueues nothing; replays are counted
   cudaError_t e = cudaStreamEndCapture(c->st, &g);
   if (rc != CPALS_OK) {
@@ -235,13 +265,20 @@ int upload_pivots(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps)
 
 // Reads and clears the tensor-core kernel's error word (after a stream sync).
 int check_tc_err(cpals_ctx* c) {
-  if (!c->tc) return CPALS_OK;
-  int h = 0;
-  CPALS_CUDA_TRY(cudaMemcpy(&h, tc_error_flag(c->tc), sizeof(int), cudaMemcpyDeviceToHost));
-  if (h) {
-    fprintf(stderr, "libcpals: tensor-core MTTKRP reported error %d (bounded wait expired)\n", h);
-    CPALS_CUDA_TRY(cudaMemset(tc_error_flag(c->tc), 0, sizeof(int)));
-    return CPALS_E_DEVICE;
+  int* flags[2] = {c->tc ? tc_error_flag(c->tc) : nullptr, nullptr};
+  if (c->dt) {
+    flags[0] = dt_error_flag(c->dt, 0);
+    flags[1] = dt_error_flag(c->dt, 1);
+  }
+  for (int* f : flags) {
+    if (!f) continue;
+    int h = 0;
+    CPALS_CUDA_TRY(cudaMemcpy(&h, f, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+      fprintf(stderr, "libcpals: tensor-core MTTKRP reported error %d (bounded wait expired)\n", h);
+      CPALS_CUDA_TRY(cudaMemset(f, 0, sizeof(int)));
+      return CPALS_E_DEVICE;
+    }
   }
   return CPALS_OK;
 }
@@ -288,6 +325,8 @@ int cpals_destroy(cpals_ctx* c) {
   if (c->side) cudaStreamSynchronize(c->side);
   invalidate_graph(c);
   if (c->tc) tc_destroy(c->tc);
+  if (c->dt) dt_destroy(c->dt);
+  cudaFree(c->Mdt);
   for (int m = 0; m < kMaxOrder; ++m) {
     cudaFree(c->F[m]);
     cudaFree(c->F32t[m]);
@@ -379,7 +418,17 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
     }
   }
   const int64_t R = rank;
-  if (mttkrp_mode == CPALS_MTTKRP_BF16X3) {
+  if (flags & CPALS_FLAG_DIMTREE) {
+    if (order != 4) {
+      cpals_destroy(c);
+      return CPALS_E_UNSUPPORTED;
+    }
+    rc = dt_create(&c->dt, dims, R, mttkrp_mode, tensor_dtype, c->num_sms);
+    if (rc != CPALS_OK) {
+      cpals_destroy(c);
+      return rc;
+    }
+  } else if (mttkrp_mode == CPALS_MTTKRP_BF16X3) {
     rc = tc_create(&c->tc, order, dims, R, tensor_dtype, c->num_sms);
     if (rc != CPALS_OK) {
       cpals_destroy(c);
@@ -388,7 +437,9 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   }
   size_t part_elems = 0;
   for (int m = 0; m < order; ++m) {
-    if (mttkrp_mode == CPALS_MTTKRP_FP64) {
+    if (c->dt) {
+      c->splits[m] = 1;  // M_n arrives reduced, in FP64
+    } else if (mttkrp_mode == CPALS_MTTKRP_FP64) {
       c->geom[m] = make_geom(order, dims, m, 32);
       c->splits[m] = mttkrp_f64_splits(c->geom[m], R, c->num_sms, &c->cps[m]);
     } else {
@@ -396,23 +447,24 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
     }
     part_elems = std::max(part_elems, (size_t)c->splits[m] * dims[m] * R);
     c->gS2[m] = gram_splits(dims[m], (int)R, c->num_sms);
-    c->ld32[m] = (mttkrp_mode == CPALS_MTTKRP_BF16X3) ? tc_factor_ld(c->tc, m) : dims[m];
+    c->ld32[m] = c->tc ? tc_factor_ld(c->tc, m) : c->dt ? dt_factor_ld(c->dt, m) : dims[m];
     CK(dmalloc(&c->F[m], (size_t)dims[m] * R));
     CK(dmalloc(&c->F32t[m], (size_t)c->ld32[m] * R));
     CPALS_CUDA_TRY(cudaMemset(c->F32t[m], 0, sizeof(float) * c->ld32[m] * R));
-    if (c->tc) {
-      c->rpad = tc_factor_rpad(c->tc);
+    if (c->tc || (c->dt && mttkrp_mode == CPALS_MTTKRP_BF16X3)) {
+      c->rpad = c->tc ? tc_factor_rpad(c->tc) : dt_factor_rpad(c->dt);
       CK(dmalloc(&c->F32r[m], (size_t)dims[m] * c->rpad));
       CPALS_CUDA_TRY(cudaMemset(c->F32r[m], 0, sizeof(float) * dims[m] * c->rpad));
     }
     CK(dmalloc(&c->G[m], (size_t)R * R));
   }
-  if (c->tc) {
+  if (c->tc || c->dt) {
     const float* fr[kMaxOrder] = {};
     for (int m = 0; m < order; ++m) fr[m] = c->F32r[m];
-    CK(tc_bind_factors(c->tc, fr));
+    CK(c->tc ? tc_bind_factors(c->tc, fr) : dt_bind_factors(c->dt, fr));
   }
-  c->part_f32 = (mttkrp_mode == CPALS_MTTKRP_BF16X3);
+  if (c->dt) CK(dmalloc(&c->Mdt, (size_t)maxI * R));
+  c->part_f32 = (mttkrp_mode == CPALS_MTTKRP_BF16X3) && !c->dt;
   {
     char* p = nullptr;
     CK(dmalloc(&p, part_elems * (c->part_f32 ? 4 : 8)));
@@ -452,6 +504,10 @@ static int after_tensor_set(cpals_ctx* c) {
   invalidate_graph(c);
   if (c->tc) {
     int rc = tc_set_tensor(c->tc, c->dT, c->st);
+    if (rc != CPALS_OK) return rc;
+  }
+  if (c->dt) {
+    int rc = dt_set_tensor(c->dt, c->dT, c->st);
     if (rc != CPALS_OK) return rc;
   }
   return CPALS_OK;
@@ -496,7 +552,7 @@ int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const dou
     CPALS_CUDA_TRY(cudaMemcpyAsync(c->F[m], tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c->st));
     CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32t[m], c->ld32[m], c->F32r[m],
                                     c->rpad, nullptr, nullptr, nullptr, c->st));
-    if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, m, c->F[m], nullptr, c->st));
+    CPALS_CUDA_TRY(update_factor_tiles(c, m, nullptr));
     CPALS_CUDA_TRY(launch_gram(c->F[m], c->dims[m], R, c->gS2[m], c->gpart, c->gcnt, c->G[m], nullptr, c->st));
     c->launches += 2;
     CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));  // tmp is reused for the next mode
@@ -547,9 +603,16 @@ int cpals_mttkrp(cpals_ctx* c, int mode, double* host_out) {
   DeviceGuard g(c->device);
   const int R = (int)c->R;
   const int64_t In = c->dims[mode];
-  CPALS_CUDA_TRY(enqueue_mttkrp(c, mode, nullptr));
-  c->launches += 2;
-  CPALS_CUDA_TRY(launch_reduce_partials(c->part, c->part_f32, c->splits[mode], In, R, c->X, c->st));
+  if (c->dt) {
+    const double* fp[kMaxOrder] = {};
+    for (int m = 0; m < c->order; ++m) fp[m] = c->F[m];
+    CPALS_CUDA_TRY(dt_mttkrp(c->dt, mode, fp, false, c->X, nullptr, c->st));
+    c->launches += dt_launches(c->dt, mode, false);
+  } else {
+    CPALS_CUDA_TRY(enqueue_mttkrp(c, mode, nullptr));
+    c->launches += 2;
+    CPALS_CUDA_TRY(launch_reduce_partials(c->part, c->part_f32, c->splits[mode], In, R, c->X, c->st));
+  }
   std::vector<double> tmp((size_t)In * R);
   CPALS_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c->X, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
@@ -595,7 +658,7 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
     for (int64_t k = 0; k < b; ++k) {
       if (use_graph) {
         CPALS_CUDA_TRY(cudaGraphLaunch(c->graph, c->st));
-        c->launches += 5 * c->order + (c->tc ? std::min(c->order, 2) : 0);
+        c->launches += c->sweep_launches;
       } else {
         int rc = enqueue_sweep(c);
         if (rc != CPALS_OK) return rc;
@@ -787,7 +850,7 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
                                  c->traj, c->traj_cap, c->st));
   CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], c->F32r[mode],
                                   c->rpad, nullptr, nullptr, nullptr, c->st));
-  if (c->tc) CPALS_CUDA_TRY(tc_update_factor(c->tc, mode, c->F[mode], nullptr, c->st));
+  CPALS_CUDA_TRY(update_factor_tiles(c, mode, nullptr));
   return check_derr(c);
 }
 

@@ -6,8 +6,10 @@ namespace cpals {
 
 struct TcState;
 
-// Plan the tensor-core MTTKRP for every mode of an order-`order` tensor.
-int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms);
+// Plan the tensor-core MTTKRP for the modes of an order-`order` tensor set in `mode_mask`
+// (bit n = mode n); only those modes get a tile stream.
+int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms,
+              unsigned mode_mask = ~0u);
 void tc_destroy(TcState* s);
 // Split the (FP32 or FP64) tensor into BF16 hi/lo planes in the two layouts the kernel streams.
 int tc_set_tensor(TcState* s, const void* T, cudaStream_t st);

@@ -1,0 +1,237 @@
+// Dimension-tree MTTKRP for order-4 tensors.
+//
+// The four MTTKRPs of a sweep share two partial contractions.  With T viewed as the
+// order-3 tensors A = (I0*I1, I2, I3) and B = (I0, I1, I2*I3) (column-major, so the merged
+// modes keep their element order):
+//   P_L[i0 + I0 i1, r] = sum_{i2,i3} T[i0,i1,i2,i3] F2[i2,r] F3[i3,r]   (MTTKRP of A, mode 0)
+//   P_R[i2 + I2 i3, r] = sum_{i0,i1} T[i0,i1,i2,i3] F0[i0,r] F1[i1,r]   (MTTKRP of B, mode 2)
+//   M0 = sum_{i1} P_L F1,  M1 = sum_{i0} P_L F0,  M2 = sum_{i3} P_R F3,  M3 = sum_{i2} P_R F2.
+// In ALS order P_L depends only on F2, F3 (fixed while modes 0 and 1 update) and P_R on the
+// updated F0, F1 (fixed while modes 2 and 3 update), so a sweep streams T twice instead of
+// four times.  The full contractions run on the same kernels as the plain path (tcgen05
+// split-BF16 for FP32 tensors, the FP64 SIMT kernel otherwise); their split-K partials are
+// reduced into P (FP64) and the small contractions run in FP64.
+#include <algorithm>
+#include <cstring>
+
+#include "cpals_dimtree.cuh"
+#include "cpals_tc.cuh"
+
+namespace cpals {
+
+namespace {
+
+__device__ __forceinline__ bool dt_done(const DevCheck* chk) { return chk != nullptr && chk->done; }
+
+// P = sum of the split-K partials (float: compensated FP32 sum finished in FP64).
+template <typename PT>
+__global__ void k_dt_reduce(const PT* __restrict__ part, int S, int64_t n, double* __restrict__ P,
+                            const DevCheck* chk) {
+  if (dt_done(chk)) return;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    if constexpr (sizeof(PT) == 4) {
+      float s = 0.0f, c = 0.0f;
+      for (int sp = 0; sp < S; ++sp) {
+        const float p = part[(int64_t)sp * n + e];
+        const float t = s + p;
+        c += (fabsf(s) >= fabsf(p)) ? ((s - t) + p) : ((p - t) + s);
+        s = t;
+      }
+      P[e] = (double)s + (double)c;
+    } else {
+      double s = 0.0;
+      for (int sp = 0; sp < S; ++sp) s += (double)part[(int64_t)sp * n + e];
+      P[e] = s;
+    }
+  }
+}
+
+// out[i][r] = sum_j P[(which ? j + Ia i : i + Ia j)][r] F[j][r]: contract P (rows a + Ia b)
+// over b (which = 0, out rows a, F has Ib rows) or over a (which = 1, out rows b, F has Ia
+// rows).  One thread per output, eight accumulators (FP64 dependent adds are slow here).
+__global__ void __launch_bounds__(256) k_dt_contract(const double* __restrict__ P, int64_t Ia, int64_t Ib, int R,
+                                                     const double* __restrict__ F, int which,
+                                                     double* __restrict__ out, const DevCheck* chk) {
+  if (dt_done(chk)) return;
+  const int64_t nout = (which ? Ib : Ia) * R;
+  const int64_t nsum = which ? Ia : Ib;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nout; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / R;
+    const int r = (int)(e % R);
+    double acc[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc[t] = 0.0;
+    int64_t j = 0;
+    for (; j + 8 <= nsum; j += 8) {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int64_t row = which ? (j + t) + Ia * i : i + Ia * (j + t);
+        acc[t] = fma(P[row * R + r], F[(j + t) * R + r], acc[t]);
+      }
+    }
+    for (int t = 0; j < nsum; ++j, ++t) {
+      const int64_t row = which ? j + Ia * i : i + Ia * j;
+      acc[t] = fma(P[row * R + r], F[j * R + r], acc[t]);
+    }
+    out[e] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+  }
+}
+
+int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 8192); }
+
+}  // namespace
+
+struct DimTree {
+  int64_t dims[4] = {};
+  int64_t R = 0;
+  int mmode = 0, tdtype = 0, num_sms = 0;
+  int64_t rowsA = 0, rowsB = 0;  // I0*I1 and I2*I3
+  // tensor-core path
+  TcState* tcA = nullptr;  // view (I0*I1, I2, I3), mode 0
+  TcState* tcB = nullptr;  // view (I0, I1, I2*I3), mode 2
+  // FP64 path
+  ModeGeom gA{}, gB{};
+  int splitsA = 0, splitsB = 0;
+  int64_t cpsA = 0, cpsB = 0;
+  const void* dT = nullptr;  // the device tensor (FP64 path)
+  void* part = nullptr;  // split-K partials of the full contractions
+  double* PL = nullptr;  // [I0*I1][R]
+  double* PR = nullptr;  // [I2*I3][R]
+};
+
+int dt_create(DimTree** out, const int64_t* dims, int64_t R, int mmode, int tdtype, int num_sms) {
+  *out = nullptr;
+  DimTree* d = new DimTree();
+  for (int m = 0; m < 4; ++m) d->dims[m] = dims[m];
+  d->R = R;
+  d->mmode = mmode;
+  d->tdtype = tdtype;
+  d->num_sms = num_sms;
+  d->rowsA = dims[0] * dims[1];
+  d->rowsB = dims[2] * dims[3];
+  const int64_t vA[3] = {d->rowsA, dims[2], dims[3]};
+  const int64_t vB[3] = {dims[0], dims[1], d->rowsB};
+  size_t part_bytes = 0;
+  if (mmode == CPALS_MTTKRP_BF16X3) {
+    int rc = tc_create(&d->tcA, 3, vA, R, tdtype, num_sms, 1u << 0);
+    if (rc == CPALS_OK) rc = tc_create(&d->tcB, 3, vB, R, tdtype, num_sms, 1u << 2);
+    if (rc != CPALS_OK) {
+      dt_destroy(d);
+      return rc;
+    }
+    part_bytes = std::max((size_t)tc_splits(d->tcA, 0) * d->rowsA, (size_t)tc_splits(d->tcB, 2) * d->rowsB) * R * 4;
+  } else {
+    d->gA = make_geom(3, vA, 0, 32);
+    d->gB = make_geom(3, vB, 2, 32);
+    d->splitsA = mttkrp_f64_splits(d->gA, R, num_sms, &d->cpsA);
+    d->splitsB = mttkrp_f64_splits(d->gB, R, num_sms, &d->cpsB);
+    part_bytes = std::max((size_t)d->splitsA * d->rowsA, (size_t)d->splitsB * d->rowsB) * R * 8;
+  }
+  if (cudaMalloc(&d->part, part_bytes) != cudaSuccess || cudaMalloc(&d->PL, sizeof(double) * d->rowsA * R) != cudaSuccess ||
+      cudaMalloc(&d->PR, sizeof(double) * d->rowsB * R) != cudaSuccess) {
+    dt_destroy(d);
+    return CPALS_E_CUDA;
+  }
+  *out = d;
+  return CPALS_OK;
+}
+
+void dt_destroy(DimTree* d) {
+  if (!d) return;
+  if (d->tcA) tc_destroy(d->tcA);
+  if (d->tcB) tc_destroy(d->tcB);
+  cudaFree(d->part);
+  cudaFree(d->PL);
+  cudaFree(d->PR);
+  delete d;
+}
+
+int dt_set_tensor(DimTree* d, const void* T, cudaStream_t st) {
+  d->dT = T;
+  if (d->tcA) {
+    int rc = tc_set_tensor(d->tcA, T, st);
+    if (rc == CPALS_OK) rc = tc_set_tensor(d->tcB, T, st);
+    return rc;
+  }
+  return CPALS_OK;
+}
+
+int* dt_error_flag(DimTree* d, int which) {
+  TcState* tc = which ? d->tcB : d->tcA;
+  return tc ? tc_error_flag(tc) : nullptr;
+}
+
+int64_t dt_factor_rpad(const DimTree* d) { return d->tcA ? tc_factor_rpad(d->tcA) : 0; }
+int64_t dt_factor_ld(const DimTree* d, int m) { return d->tcA ? ((d->dims[m] + 63) / 64) * 64 : d->dims[m]; }
+
+int dt_bind_factors(DimTree* d, const float* const* F32r) {
+  if (!d->tcA) return CPALS_OK;
+  // view A, mode 0: fastest reduction mode = view mode 1 (F2), outer = view mode 2 (F3)
+  const float* fa[kMaxOrder] = {nullptr, F32r[2], F32r[3]};
+  // view B, mode 2: fastest reduction mode = view mode 0 (F0), outer = view mode 1 (F1)
+  const float* fb[kMaxOrder] = {F32r[0], F32r[1], nullptr};
+  int rc = tc_bind_factors(d->tcA, fa);
+  if (rc == CPALS_OK) rc = tc_bind_factors(d->tcB, fb);
+  return rc;
+}
+
+cudaError_t dt_update_factor(DimTree* d, int m, const double* F, const DevCheck* chk, cudaStream_t st) {
+  if (!d->tcA) return cudaSuccess;
+  if (m == 2) return tc_update_factor(d->tcA, 1, F, chk, st);
+  if (m == 0) return tc_update_factor(d->tcB, 0, F, chk, st);
+  return cudaSuccess;
+}
+
+int dt_launches(const DimTree* d, int n, bool reuse) {
+  (void)d;
+  const bool full = (n == 0 || n == 2) || !reuse;
+  return (full ? 2 : 0) + 1;  // [MTTKRP, partial reduce,] contraction
+}
+
+cudaError_t dt_mttkrp(DimTree* d, int n, const double* const* F, bool reuse, double* M, const DevCheck* chk,
+                      cudaStream_t st) {
+  const int R = (int)d->R;
+  const bool left = (n <= 1);
+  const bool full = (n == 0 || n == 2) || !reuse;
+  double* P = left ? d->PL : d->PR;
+  const int64_t rows = left ? d->rowsA : d->rowsB;
+  if (full) {
+    int S = 0;
+    if (d->tcA) {
+      TcState* tc = left ? d->tcA : d->tcB;
+      const int vm = left ? 0 : 2;
+      cudaError_t e = tc_launch_mttkrp(tc, vm, static_cast<float*>(d->part), chk, st);
+      if (e != cudaSuccess) return e;
+      S = tc_splits(tc, vm);
+      k_dt_reduce<float><<<grid_for(rows * R), 256, 0, st>>>(static_cast<const float*>(d->part), S, rows * R, P, chk);
+    } else {
+      FactorSet fs{};
+      if (left) {
+        fs.F[1] = F[2];
+        fs.F[2] = F[3];
+      } else {
+        fs.F[0] = F[0];
+        fs.F[1] = F[1];
+      }
+      const ModeGeom& g = left ? d->gA : d->gB;
+      S = left ? d->splitsA : d->splitsB;
+      cudaError_t e = launch_mttkrp_f64(d->dT, d->tdtype, fs, g, R, S, left ? d->cpsA : d->cpsB,
+                                        static_cast<double*>(d->part), chk, st);
+      if (e != cudaSuccess) return e;
+      k_dt_reduce<double><<<grid_for(rows * R), 256, 0, st>>>(static_cast<const double*>(d->part), S, rows * R, P,
+                                                              chk);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  // the small contraction
+  const int64_t Ia = left ? d->dims[0] : d->dims[2];
+  const int64_t Ib = left ? d->dims[1] : d->dims[3];
+  const int which = (n == 1 || n == 3) ? 1 : 0;  // modes 1, 3 contract over the first index
+  const double* Fc = F[(n == 0) ? 1 : (n == 1) ? 0 : (n == 2) ? 3 : 2];
+  const int64_t nout = (which ? Ib : Ia) * R;
+  k_dt_contract<<<grid_for(nout), 256, 0, st>>>(P, Ia, Ib, R, Fc, which, M, chk);
+  return cudaGetLastError();
+}
+
+}  // namespace cpals

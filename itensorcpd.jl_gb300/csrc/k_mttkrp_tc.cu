@@ -484,7 +484,7 @@ struct TcState {
   size_t smem_bytes[kMaxOrder] = {};
 };
 
-int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms) {
+int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms, unsigned mode_mask) {
   *out = nullptr;
   if (R > 512) return CPALS_E_UNSUPPORTED;
   TcState* s = new TcState();
@@ -519,6 +519,7 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
   for (int n = 0; n < order; ++n) {
     TcModePlan& p = s->plan[n];
     memset(&p, 0, sizeof(p));
+    if (!((mode_mask >> n) & 1u)) continue;  // no tile stream for this mode
     p.mode = n;
     p.fmode = (n == 0) ? 1 : 0;
     p.In = dims[n];
@@ -562,6 +563,10 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     }
   }
   for (int f = 0; f < 2; ++f) {
+    bool used = false;  // is f the fastest reduction mode of a planned mode?
+    for (int n = 0; n < order; ++n)
+      if (((mode_mask >> n) & 1u) && ((n == 0) ? 1 : 0) == f) used = true;
+    if (!used) continue;
     s->nfb_mode[f] = (dims[f] + kChunk - 1) / kChunk;
     s->btile_bytes[f] = (size_t)s->nfb_mode[f] * n_blocks * 2 * nb * kChunk * 2;
     if (cudaMalloc(&s->btiles[f], s->btile_bytes[f]) != cudaSuccess) {
@@ -591,8 +596,8 @@ int tc_bind_factors(TcState* s, const float* const* F32r) {
 }
 
 cudaError_t tc_update_factor(TcState* s, int m, const double* F, const DevCheck* chk, cudaStream_t st) {
-  if (m > 1) return cudaSuccess;  // only the fastest reduction modes (0 and 1) feed the tensor core directly
-  const TcModePlan& p = s->plan[0];
+  if (m > 1 || !s->btiles[m]) return cudaSuccess;  // only planned fastest reduction modes feed the tensor core
+  const TcModePlan& p = s->plan[s->plan[0].m_blocks ? 0 : (s->plan[1].m_blocks ? 1 : 2)];
   const int64_t units = s->nfb_mode[m] * p.n_blocks * p.nb * 8;
   const int blocks = (int)std::min<int64_t>((units + 255) / 256, 4096);
   k_build_btiles<<<blocks, 256, 0, st>>>(F, s->dims[m], (int)s->R, s->nfb_mode[m], p.n_blocks, p.nb, s->btiles[m], chk);
@@ -611,6 +616,7 @@ void tc_destroy(TcState* s) {
 int tc_set_tensor(TcState* s, const void* T, cudaStream_t st) {
   for (int n = 0; n < s->order; ++n) {
     const TcModePlan& p = s->plan[n];
+    if (!p.m_blocks) continue;  // mode not planned
     const int64_t ntiles = (int64_t)p.m_blocks * p.nchunks;
     if (ntiles >= (int64_t(1) << 31)) return CPALS_E_UNSUPPORTED;
     if (s->tdtype == CPALS_DTYPE_F64)
@@ -629,6 +635,7 @@ int* tc_error_flag(TcState* s) { return s->err; }
 cudaError_t tc_launch_mttkrp(TcState* s, int n, float* part, const DevCheck* chk, cudaStream_t st) {
   if (!s->factors_bound) return cudaErrorInvalidValue;
   const TcModePlan& p = s->plan[n];
+  if (!p.m_blocks || !s->btiles[p.fmode]) return cudaErrorInvalidValue;  // mode not planned
   FactorPtrs32 fr{};
   for (int m = 0; m < s->order; ++m) fr.F[m] = s->F32r[m];
   const unsigned grid = (unsigned)(p.m_blocks * p.n_blocks * p.splits);

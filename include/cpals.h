@@ -177,6 +177,33 @@ int cpals_leverage_scores(cpals_ctx* ctx, int mode, double* host_probs);
  * (randomized/ProjectionAlgorithm.jl:57-68, randomized/krp_lev_score_sampled.jl:87-125). */
 int cpals_sampled_update(cpals_ctx* ctx, int mode, const int64_t* pivots, int64_t nsamps, int normal);
 
+/* ---- batched small decompositions ----
+ * Many independent order-3 CP-ALS problems (uneven shapes, ranks up to 64, mode sizes up
+ * to 4096 within the shared-memory budget) solved together: one persistent kernel launch
+ * per ALS sweep, each CTA running whole sweeps of the tensors it pulls from a device queue.
+ * No single counterpart in the reference: it replaces a host loop of decompose(A, rank)
+ * calls (src/decompose.jl:1-30) with FitCheck(tol, max_iter, norm(A)) each
+ * (src/converge_checks/fit_check.jl:5-66).  dims: count x 3 (row per tensor); tensors are
+ * concatenated column-major FP32; factors per tensor are F0, F1, F2 (I_m x R column-major)
+ * then lambda (R), concatenated. */
+typedef struct cpals_batch cpals_batch;
+int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64_t* dims, const int64_t* ranks,
+                       const double* ref_norms);
+int cpals_batch_destroy(cpals_batch* b);
+int cpals_batch_set_tensors(cpals_batch* b, const float* host_concat);
+/* Initial factors (resets every tensor's FitCheck state). */
+int cpals_batch_set_factors(cpals_batch* b, const double* host_concat);
+int cpals_batch_get_factors(cpals_batch* b, double* host_concat);
+/* Threads per CTA: 128, 256 or 512. */
+int cpals_batch_set_threads(cpals_batch* b, int threads);
+/* Sweeps until every tensor's FitCheck(tol, max_iter) has stopped.  Per tensor: sweeps run,
+ * final fit, flags (1 NaN fit, 2 rank-deficient normal equations met, 4 stopped). */
+int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_out, double* fits_out, int* flags_out,
+                         int64_t* launches_out);
+/* Times `sweeps` sweeps from host_factors for each thread count, keeps the fastest, and
+ * restores host_factors.  ms_out (3 entries, may be null): 128, 256, 512 threads. */
+int cpals_batch_autotune(cpals_batch* b, const double* host_factors, int sweeps, int* threads_out, double* ms_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,10 +25,11 @@ from .api import (
     random_factors,
     sample_factor_matrices,
 )
+from .batched import BatchEngine
 from .engine import Engine
 
 __all__ = [
-    "CPD", "CPDFit", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
+    "BatchEngine", "CPD", "CPDFit", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
     "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
     "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices",
 ]

@@ -72,6 +72,15 @@ SIGNATURES = {
     "cpals_fused_flatten_sample": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _P]),
     "cpals_leverage_scores": (C.c_int, [_P, C.c_int, _DP]),
     "cpals_sampled_update": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, C.c_int]),
+    "cpals_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int64, _I64P, _I64P, _DP]),
+    "cpals_batch_destroy": (C.c_int, [_P]),
+    "cpals_batch_set_tensors": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "cpals_batch_set_factors": (C.c_int, [_P, _DP]),
+    "cpals_batch_get_factors": (C.c_int, [_P, _DP]),
+    "cpals_batch_set_threads": (C.c_int, [_P, C.c_int]),
+    "cpals_batch_optimize": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(C.c_int), _DP, C.POINTER(C.c_int),
+                                       _I64P]),
+    "cpals_batch_autotune": (C.c_int, [_P, _DP, C.c_int, C.POINTER(C.c_int), _DP]),
 }
 
 _lib = None

@@ -1,0 +1,116 @@
+"""Batched small decompositions on the device (libcpals ``cpals_batch_*``).
+
+Many independent order-3 CP-ALS problems of uneven shape and rank run together: one
+persistent kernel launch per ALS sweep, every tensor with its own FitCheck.  This replaces a
+host loop of ``decompose(A, rank)`` calls (decompose.jl:1-30) for small tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class BatchEngine:
+    """Device handle for a batch of order-3 tensors (dims: list of 3-tuples, ranks: list)."""
+
+    def __init__(self, dims, ranks, ref_norms, device=0):
+        self.lib = L.load()
+        self.dims = [tuple(int(x) for x in d) for d in dims]
+        self.ranks = [int(r) for r in ranks]
+        if len(self.dims) != len(self.ranks) or len(self.dims) != len(ref_norms):
+            raise ValueError("dims, ranks and ref_norms must have one entry per tensor")
+        self.count = len(self.dims)
+        d = np.ascontiguousarray(np.asarray(self.dims, dtype=np.int64).reshape(-1))
+        r = np.ascontiguousarray(np.asarray(self.ranks, dtype=np.int64))
+        nrm = np.ascontiguousarray(np.asarray(ref_norms, dtype=np.float64))
+        h = C.c_void_p()
+        L.check(self.lib.cpals_batch_create(C.byref(h), int(device), self.count, L.i64ptr(d), L.i64ptr(r),
+                                            L.dptr(nrm)), "cpals_batch_create")
+        self.h = h
+        self._foffs = []
+        off = 0
+        for dd, rr in zip(self.dims, self.ranks):
+            self._foffs.append(off)
+            off += (sum(dd) + 1) * rr
+        self._ftotal = off
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cpals_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tensors(self, tensors):
+        buf = np.concatenate([np.asarray(T, dtype=np.float32).reshape(-1, order="F") for T in tensors])
+        L.check(self.lib.cpals_batch_set_tensors(self.h, buf.ctypes.data_as(C.POINTER(C.c_float))),
+                "cpals_batch_set_tensors")
+        self._tensors_keep = buf
+
+    def pack_factors(self, factors, lams):
+        buf = np.empty(self._ftotal, dtype=np.float64)
+        for t, (F, lam) in enumerate(zip(factors, lams)):
+            parts = [np.asarray(f, dtype=np.float64).reshape(-1, order="F") for f in F]
+            parts.append(np.asarray(lam, dtype=np.float64))
+            v = np.concatenate(parts)
+            buf[self._foffs[t]:self._foffs[t] + v.size] = v
+        return buf
+
+    def unpack_factors(self, buf):
+        out = []
+        for t, (dd, R) in enumerate(zip(self.dims, self.ranks)):
+            o = self._foffs[t]
+            F = []
+            for I in dd:
+                F.append(np.reshape(buf[o:o + I * R], (I, R), order="F").copy())
+                o += I * R
+            out.append((F, buf[o:o + R].copy()))
+        return out
+
+    def set_factors(self, factors, lams):
+        buf = self.pack_factors(factors, lams)
+        L.check(self.lib.cpals_batch_set_factors(self.h, L.dptr(buf)), "cpals_batch_set_factors")
+        self._factors_keep = buf
+        return buf
+
+    def get_factors(self):
+        buf = np.empty(self._ftotal, dtype=np.float64)
+        L.check(self.lib.cpals_batch_get_factors(self.h, L.dptr(buf)), "cpals_batch_get_factors")
+        return self.unpack_factors(buf)
+
+    def set_threads(self, threads):
+        L.check(self.lib.cpals_batch_set_threads(self.h, int(threads)), "cpals_batch_set_threads")
+
+    def autotune(self, factors, lams, sweeps=2):
+        buf = self.pack_factors(factors, lams)
+        nt = C.c_int()
+        ms = np.zeros(3)
+        L.check(self.lib.cpals_batch_autotune(self.h, L.dptr(buf), int(sweeps), C.byref(nt), L.dptr(ms)),
+                "cpals_batch_autotune")
+        self._factors_keep = buf
+        return int(nt.value), {128: ms[0], 256: ms[1], 512: ms[2]}
+
+    def optimize(self, tol=1e-5, max_iter=200):
+        """FitCheck(tol, max_iter) per tensor; returns (sweeps, fits, flags, kernel launches)."""
+        sweeps = np.zeros(self.count, dtype=np.int32)
+        fits = np.zeros(self.count)
+        flags = np.zeros(self.count, dtype=np.int32)
+        launches = C.c_int64()
+        L.check(self.lib.cpals_batch_optimize(self.h, float(tol), int(max_iter),
+                                              sweeps.ctypes.data_as(C.POINTER(C.c_int)), L.dptr(fits),
+                                              flags.ctypes.data_as(C.POINTER(C.c_int)), C.byref(launches)),
+                "cpals_batch_optimize")
+        return sweeps, fits, flags, int(launches.value)

@@ -1,0 +1,763 @@
+// Batched CP-ALS: thousands of small independent order-3 decompositions of uneven shape
+// and rank, one persistent kernel launch per ALS sweep.
+//
+// Each CTA pulls tensor indices from a device work queue (largest tensors first) and runs
+// one full ALS sweep of that tensor in shared memory, with the reference's steps
+// (src/optimizers/als_optimizers/optimize.jl:15-32) for every mode n:
+//   M_n = T_(n) (F_b (.) F_a)          FP32 products, FP32 accumulation over one tensor
+//                                      slice, FP64 across slices
+//   V = G_a .* G_b                     FP64 (MttkrpAlgorithm.jl:18-31)
+//   X = M_n V^{-1}                     pivoted symmetric sweep of V (tol 1e-6) + FP64 product
+//   lambda, F_n = X / lambda, G_n      FP64 (row_norm.jl, standard/tensor.jl:46-49)
+// and after the last mode the fit and the tensor's own FitCheck (fit_check.jl:24-66).
+// Converged tensors are skipped by later launches.  The sweep is a CUDA graph (queue reset
+// + kernel); the host replays it in batches and polls the count of active tensors.
+//
+// Shared memory per CTA (Imax = largest mode size, Rmax = largest rank of the batch):
+//   slice   Imax^2 floats             one I0 x I1 slice of T
+//   F32     3 Imax Rmax floats        the factors in FP32 (MTTKRP operands)
+//   M       Imax Rmax doubles         MTTKRP result
+//   X       Imax Rmax doubles         solve result
+//   A       Rmax (Rmax|1) doubles     V, swept in place into -V^{-1}
+//   G       3 Rmax^2 doubles          Grams
+//   vecs    6 Rmax doubles
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "cpals_internal.cuh"
+
+namespace cpals {
+
+namespace {
+
+constexpr double kBatchTol = 1e-6;  // cholesky_epsilon (src/ITensorCPD.jl:2)
+
+struct BatchItem {
+  int64_t toff;  // tensor offset (elements)
+  int64_t foff;  // factor offset (doubles): F0, F1, F2 (I_m x R column-major), lambda [R]
+  int64_t goff;  // Gram offset (doubles): G0, G1, G2 (R x R each)
+  int I[3];
+  int R;
+  double ref_norm;
+};
+
+struct BatchCheck {  // fit_check.jl:5-20, per tensor
+  int iter, counter, done, sweeps;
+  int total_iter, rank_deficient, nan, pad;
+  double lastfit, final_fit, fit;
+};
+
+struct SmemLayout {
+  int Imax, Rmax, ld;
+  size_t slice, f32, M, X, A, G, vec, total;
+};
+
+__host__ __device__ inline size_t al16(size_t b) { return (b + 15) & ~size_t(15); }
+
+__host__ __device__ inline SmemLayout smem_layout(int Imax, int Rmax) {
+  SmemLayout L{};
+  L.Imax = Imax;
+  L.Rmax = (Rmax + 3) & ~3;  // FP32 factor rows of 16-byte multiples (float4 loads)
+  Rmax = L.Rmax;
+  L.ld = Rmax | 1;
+  size_t o = 0;
+  L.slice = o;
+  o += al16((size_t)Imax * (Imax | 1) * 4);
+  L.f32 = o;
+  o += al16((size_t)3 * Imax * Rmax * 4);
+  L.M = o;
+  o += al16((size_t)Imax * Rmax * 8);
+  L.X = o;
+  o += al16((size_t)Imax * Rmax * 8);
+  L.A = o;
+  o += al16((size_t)Rmax * L.ld * 8);
+  L.G = o;
+  o += al16((size_t)3 * Rmax * Rmax * 8);
+  L.vec = o;
+  o += al16((size_t)6 * Rmax * 8);
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = (lane < nw) ? red[lane] : 0.0;
+  for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ long long bkey(double v) {
+  const long long k = __double_as_longlong(v);
+  return (k & 0x7fffffffffffffffll) > 0x7ff0000000000000ll ? LLONG_MAX : k;
+}
+
+// One ALS sweep of tensor `it` by the whole CTA.
+__device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T, double* __restrict__ Fg,
+                                double* __restrict__ Gg, BatchCheck* __restrict__ chk, const SmemLayout& L,
+                                unsigned char* sm, double tol, int max_iter) {
+  __shared__ double red[32];
+  __shared__ int s_p, s_stop;
+  __shared__ double s_pinv;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int R = it.R, I0 = it.I[0], I1 = it.I[1], I2 = it.I[2];
+  const int Rm = L.Rmax;
+  float* S = reinterpret_cast<float*>(sm + L.slice);
+  float* F32 = reinterpret_cast<float*>(sm + L.f32);  // F32 + m*Imax*Rm: [I_m][R] row-major (ld Rm)
+  double* M = reinterpret_cast<double*>(sm + L.M);     // [I_n][Rm]
+  double* X = reinterpret_cast<double*>(sm + L.X);     // [I_n][Rm]
+  double* A = reinterpret_cast<double*>(sm + L.A);     // [R][ld]
+  double* G = reinterpret_cast<double*>(sm + L.G);     // 3 x [R][R]
+  double* vec = reinterpret_cast<double*>(sm + L.vec);
+  double* lam = vec;          // R
+  double* a_row = vec + Rm;   // pivot row
+  double* t_row = vec + 2 * Rm;
+  const int ld = L.ld;
+  const float* Tt = T + it.toff;
+  const int ldS = I0 | 1;
+  double* F0g = Fg + it.foff;
+  const int64_t fo[3] = {0, (int64_t)I0 * R, (int64_t)(I0 + I1) * R};
+  double* lamg = Fg + it.foff + (int64_t)(I0 + I1 + I2) * R;
+  // factors (FP32 copies, zero beyond column R) and Grams into shared memory
+  for (int e = tid; e < 3 * L.Imax * Rm; e += nt) F32[e] = 0.f;
+  __syncthreads();
+  for (int m = 0; m < 3; ++m)
+    for (int e = tid; e < it.I[m] * R; e += nt) {
+      const int i = e % it.I[m], r = e / it.I[m];
+      F32[(size_t)m * L.Imax * Rm + (size_t)i * Rm + r] = (float)F0g[fo[m] + e];
+    }
+  for (int e = tid; e < 3 * R * R; e += nt) G[e] = Gg[it.goff + e];
+  __syncthreads();
+  double inner = 0.0;
+  for (int n = 0; n < 3; ++n) {
+    const int In = it.I[n];
+    // ---- MTTKRP, slice by slice over the last mode: each slice S = T[:, :, k]
+    for (int e = tid; e < In * R; e += nt) M[(e / R) * Rm + e % R] = 0.0;
+    const float* Fa = F32 + (size_t)(n == 0 ? 1 : 0) * L.Imax * Rm;  // the other in-slice mode
+    const float* F2 = F32 + (size_t)2 * L.Imax * Rm;
+    for (int k = 0; k < I2; ++k) {
+      __syncthreads();
+      const float* Tk = Tt + (int64_t)k * I0 * I1;
+      // S[i + ldS j] with an odd leading dimension: column walks are free of bank conflicts
+      for (int e = tid; e < I0 * I1; e += nt) S[(e % I0) + ldS * (e / I0)] = Tk[e];
+      __syncthreads();
+      // Each thread takes one row of the output and four consecutive rank columns: one
+      // scalar slice load and one 16-byte factor load feed four FMAs.
+      const int R4 = (R + 3) >> 2;
+      if (n == 0) {
+        // M0[i][r] += F2[k][r] * sum_j S[i,j] F1[j][r]
+        for (int e = tid; e < I0 * R4; e += nt) {
+          const int i = e % I0, r0 = (e / I0) * 4;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int j = 0; j < I1; ++j) {
+            const float sv = S[i + ldS * j];
+            const float4 f = *reinterpret_cast<const float4*>(&Fa[j * Rm + r0]);
+            a.x = fmaf(sv, f.x, a.x);
+            a.y = fmaf(sv, f.y, a.y);
+            a.z = fmaf(sv, f.z, a.z);
+            a.w = fmaf(sv, f.w, a.w);
+          }
+          const float4 f2 = *reinterpret_cast<const float4*>(&F2[k * Rm + r0]);
+          double* Mi = M + i * Rm + r0;
+          Mi[0] += (double)(a.x * f2.x);
+          if (r0 + 1 < R) Mi[1] += (double)(a.y * f2.y);
+          if (r0 + 2 < R) Mi[2] += (double)(a.z * f2.z);
+          if (r0 + 3 < R) Mi[3] += (double)(a.w * f2.w);
+        }
+      } else {
+        // y[j][r] = sum_i S[i,j] F0[i][r]; mode 1: M1[j][r] += F2[k][r] y[j][r];
+        // mode 2: M2[k][r] = sum_j F1[j][r] y[j][r] (X holds the per-j terms)
+        const float* F1 = F32 + (size_t)1 * L.Imax * Rm;
+        for (int e = tid; e < I1 * R4; e += nt) {
+          const int j = e % I1, r0 = (e / I1) * 4;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int i = 0; i < I0; ++i) {
+            const float sv = S[i + ldS * j];
+            const float4 f = *reinterpret_cast<const float4*>(&Fa[i * Rm + r0]);
+            a.x = fmaf(sv, f.x, a.x);
+            a.y = fmaf(sv, f.y, a.y);
+            a.z = fmaf(sv, f.z, a.z);
+            a.w = fmaf(sv, f.w, a.w);
+          }
+          const float4 g = *reinterpret_cast<const float4*>(n == 1 ? &F2[k * Rm + r0] : &F1[j * Rm + r0]);
+          double* out = (n == 1) ? M + j * Rm + r0 : X + j * Rm + r0;
+          const double v0 = (double)(a.x * g.x), v1 = (double)(a.y * g.y), v2 = (double)(a.z * g.z),
+                       v3 = (double)(a.w * g.w);
+          if (n == 1) {
+            out[0] += v0;
+            if (r0 + 1 < R) out[1] += v1;
+            if (r0 + 2 < R) out[2] += v2;
+            if (r0 + 3 < R) out[3] += v3;
+          } else {
+            out[0] = v0;
+            if (r0 + 1 < R) out[1] = v1;
+            if (r0 + 2 < R) out[2] = v2;
+            if (r0 + 3 < R) out[3] = v3;
+          }
+        }
+        if (n == 2) {
+          __syncthreads();
+          for (int r = tid; r < R; r += nt) {
+            double s0 = 0.0, s1 = 0.0;
+            int j = 0;
+            for (; j + 1 < I1; j += 2) {
+              s0 += X[j * Rm + r];
+              s1 += X[(j + 1) * Rm + r];
+            }
+            if (j < I1) s0 += X[j * Rm + r];
+            M[k * Rm + r] = s0 + s1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- V = G_a .* G_b (mode order), upper triangle into A
+    const double* Ga = G + (size_t)(n == 0 ? 1 : 0) * R * R;
+    const double* Gb = G + (size_t)(n == 2 ? 1 : 2) * R * R;
+    for (int e = tid; e < R * R; e += nt) {
+      const int r = e / R, c = e - r * R;
+      if (c >= r) A[r * ld + c] = (1.0 * Ga[e]) * Gb[e];
+    }
+    __syncthreads();
+    // ---- pivoted symmetric sweep (same pivot rule and tolerance as dpstrf)
+    for (int i = tid; i < R; i += nt) vec[3 * Rm + i] = 0.0;  // swept flags
+    __syncthreads();
+    int rank = R;
+    for (int j = 0; j < R; ++j) {
+      if (warp == 0) {
+        long long bk = LLONG_MIN;
+        int bi = R;
+        for (int i = lane; i < R; i += 32) {
+          // the unswept diagonal entries; swept ones hold negative values (-1/d)
+          const double d = A[i * ld + i];
+          const long long key = (vec[3 * Rm + i] != 0.0) ? LLONG_MIN : bkey(d);
+          if (bi == R || key > bk) {
+            bk = key;
+            bi = i;
+          }
+        }
+        const int khi = (int)(bk >> 32);
+        const int mhi = __reduce_max_sync(0xffffffffu, khi);
+        const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
+        const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
+        const int p = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+        if (lane == 0) {
+          const int stop = (mk == LLONG_MAX) || !(mk > bkey(kBatchTol)) || p >= R;
+          s_stop = stop;
+          s_p = p;
+          if (!stop) s_pinv = 1.0 / __longlong_as_double(mk);
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+      if (s_stop) {
+        rank = j;
+        break;
+      }
+      const int k = s_p;
+      const double dk = s_pinv;
+      for (int i = tid; i < R; i += nt) {
+        const double av = (i <= k) ? A[i * ld + k] : A[k * ld + i];
+        a_row[i] = av;
+        t_row[i] = av * dk;
+      }
+      __syncthreads();
+      for (int e = tid; e < R * R; e += nt) {
+        const int i = e / R, c = e - i * R;
+        if (c < i) continue;
+        double v;
+        if (i == k && c == k) v = -dk;
+        else if (i == k) v = t_row[c];
+        else if (c == k) v = t_row[i];
+        else v = fma(-a_row[i], t_row[c], A[i * ld + c]);
+        A[i * ld + c] = v;
+      }
+      if (tid == 0) vec[3 * Rm + k] = 1.0;
+      __syncthreads();
+    }
+    // W = -A on the swept indices.  A rank-deficient V (a pivot <= 1e-6) keeps the basic
+    // solution: the unswept components of X are zero (the reference's pivoted-QR
+    // fallback, ldiv_solve.jl:20-21, returns its least-squares solution instead)
+    if (rank < R && tid == 0) chk->rank_deficient += 1;
+    __syncthreads();
+    // ---- X = M W (FP64): W(l, c) = -A(min, max) for swept l, c; 0 otherwise
+    for (int e = tid; e < In * R; e += nt) {
+      const int i = e / R, c = e - i * R;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      const bool cs = vec[3 * Rm + c] != 0.0;
+      int l = 0;
+      for (; l + 4 <= R; l += 4) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int ll = l + q;
+          const double w = (cs && vec[3 * Rm + ll] != 0.0) ? -((ll <= c) ? A[ll * ld + c] : A[c * ld + ll]) : 0.0;
+          const double mv = M[i * Rm + ll];
+          if (q == 0) s0 = fma(mv, w, s0);
+          else if (q == 1) s1 = fma(mv, w, s1);
+          else if (q == 2) s2 = fma(mv, w, s2);
+          else s3 = fma(mv, w, s3);
+        }
+      }
+      for (; l < R; ++l) {
+        const double w = (cs && vec[3 * Rm + l] != 0.0) ? -((l <= c) ? A[l * ld + c] : A[c * ld + l]) : 0.0;
+        s0 = fma(M[i * Rm + l], w, s0);
+      }
+      X[i * Rm + c] = (s0 + s1) + (s2 + s3);
+    }
+    __syncthreads();
+    // ---- <T, X> on the last mode (fit_check.jl:28)
+    if (n == 2) {
+      double p = 0.0;
+      for (int e = tid; e < In * R; e += nt) p += M[(e / R) * Rm + e % R] * X[(e / R) * Rm + e % R];
+      inner = block_sum_d(p, red);
+    }
+    // ---- lambda = column norms, F_n = X / lambda (row_norm.jl:4-24)
+    for (int r = warp; r < R; r += nt >> 5) {
+      double s = 0.0;
+      for (int i = lane; i < In; i += 32) s = fma(X[i * Rm + r], X[i * Rm + r], s);
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) lam[r] = sqrt(s);
+    }
+    __syncthreads();
+    float* Fn32 = F32 + (size_t)n * L.Imax * Rm;
+    for (int e = tid; e < In * R; e += nt) {
+      const int i = e / R, r = e - i * R;
+      // a column left at zero by a rank-deficient solve (basic solution) stays zero
+      const double f = (lam[r] > 0.0) ? X[i * Rm + r] / lam[r] : 0.0;
+      X[i * Rm + r] = f;
+      F0g[fo[n] + i + (int64_t)In * r] = f;
+      Fn32[i * Rm + r] = (float)f;
+    }
+    __syncthreads();
+    // ---- G_n = F_n^T F_n (standard/tensor.jl:46-49)
+    double* Gn = G + (size_t)n * R * R;
+    for (int e = tid; e < R * R; e += nt) {
+      const int r = e / R, c = e - r * R;
+      if (c < r) continue;
+      double s0 = 0.0, s1 = 0.0;
+      int i = 0;
+      for (; i + 1 < In; i += 2) {
+        s0 = fma(X[i * Rm + r], X[i * Rm + c], s0);
+        s1 = fma(X[(i + 1) * Rm + r], X[(i + 1) * Rm + c], s1);
+      }
+      if (i < In) s0 = fma(X[i * Rm + r], X[i * Rm + c], s0);
+      Gn[r * R + c] = s0 + s1;
+      Gn[c * R + r] = s0 + s1;
+    }
+    __syncthreads();
+  }
+  // ---- fit and FitCheck (fit_check.jl:24-66; converge_checks.jl:5-11)
+  double pf = 0.0;
+  for (int e = tid; e < R * R; e += nt) {
+    const int r = e / R, c = e - r * R;
+    pf += ((G[e] * G[R * R + e]) * G[2 * R * R + e]) * (lam[r] * lam[c]);
+  }
+  const double fact = block_sum_d(pf, red);
+  for (int e = tid; e < 3 * R * R; e += nt) Gg[it.goff + e] = G[e];
+  for (int r = tid; r < R; r += nt) lamg[r] = lam[r];
+  if (tid == 0) {
+    BatchCheck& c = *chk;
+    const double rn = it.ref_norm;
+    const double fit = 1.0 - sqrt(fabs(rn * rn + fact - 2.0 * fabs(inner))) / rn;
+    c.fit = fit;
+    c.sweeps += 1;
+    c.iter += 1;
+    const double dfit = fabs(c.lastfit - fit);
+    c.lastfit = fit;
+    if (isnan(fit)) {
+      c.nan = 1;
+      c.done = 1;
+    } else if (dfit < tol) {
+      c.counter += 1;
+      if (c.counter >= 2) {
+        c.total_iter = c.iter;
+        c.final_fit = fit;
+        c.done = 1;
+      }
+    } else {
+      c.counter = 0;
+    }
+    if (!c.done && c.iter >= max_iter) {
+      c.total_iter = c.iter;
+      c.final_fit = fit;
+      c.done = 1;
+    }
+  }
+  __syncthreads();
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_batch_sweep(const BatchItem* __restrict__ items, const int* __restrict__ order,
+                                                    int count, const float* __restrict__ T, double* __restrict__ F,
+                                                    double* __restrict__ G, BatchCheck* __restrict__ chk,
+                                                    unsigned* __restrict__ queue, SmemLayout L, double tol,
+                                                    int max_iter) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ int s_t;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_t = (int)atomicAdd(queue, 1u);
+    __syncthreads();
+    const int t = s_t;
+    if (t >= count) break;
+    const int id = order[t];
+    if (chk[id].done) continue;
+    batch_sweep_one(items[id], T, F, G, &chk[id], L, sm, tol, max_iter);
+  }
+}
+
+__global__ void k_batch_reset(unsigned* queue, const BatchCheck* chk, int count, int* active) {
+  // queue reset for the next launch, and the count of active tensors (read by the host)
+  __shared__ int s;
+  if (threadIdx.x == 0) s = 0;
+  __syncthreads();
+  int a = 0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) a += chk[i].done ? 0 : 1;
+  atomicAdd(&s, a);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *queue = 0u;
+    *active = s;
+  }
+}
+
+// Grams of the initial factors, and lambda / checks reset.
+__global__ void k_batch_init(const BatchItem* __restrict__ items, int count, double* __restrict__ F,
+                             double* __restrict__ G, BatchCheck* __restrict__ chk) {
+  for (int id = blockIdx.x; id < count; id += gridDim.x) {
+    const BatchItem it = items[id];
+    const int R = it.R;
+    int64_t off = it.foff;
+    for (int m = 0; m < 3; ++m) {
+      const double* Fm = F + off;
+      for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+        const int r = e / R, c = e % R;
+        double s = 0.0;
+        for (int i = 0; i < it.I[m]; ++i) s = fma(Fm[i + (int64_t)it.I[m] * r], Fm[i + (int64_t)it.I[m] * c], s);
+        G[it.goff + (int64_t)m * R * R + e] = s;
+      }
+      off += (int64_t)it.I[m] * R;
+    }
+    if (threadIdx.x == 0) {
+      BatchCheck c{};
+      c.lastfit = 1.0;  // fit_check.jl:16-20
+      chk[id] = c;
+    }
+  }
+}
+
+}  // namespace
+
+}  // namespace cpals
+
+using namespace cpals;
+
+struct cpals_batch {
+  int device = 0;
+  int64_t count = 0;
+  int Imax = 0, Rmax = 0;
+  std::vector<BatchItem> items;
+  std::vector<int> order;
+  int64_t tot_T = 0, tot_F = 0, tot_G = 0;
+  BatchItem* d_items = nullptr;
+  int* d_order = nullptr;
+  float* d_T = nullptr;
+  double* d_F = nullptr;
+  double* d_G = nullptr;
+  BatchCheck* d_chk = nullptr;
+  unsigned* d_queue = nullptr;
+  int* d_active = nullptr;
+  int* h_active = nullptr;
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int nt = 256;         // threads per CTA (autotuned)
+  int ctas_per_sm = 1;  // resident CTAs per SM (from the occupancy calculator)
+  double tol = 1e-5;
+  int max_iter = 200;
+  int num_sms = 0;
+  SmemLayout L{};
+  int64_t launches = 0;
+};
+
+namespace {
+
+int batch_launch(cpals_batch* b) {
+  const int grid = b->num_sms * b->ctas_per_sm;
+  switch (b->nt) {
+    case 128:
+      k_batch_sweep<128><<<grid, 128, b->L.total, b->st>>>(b->d_items, b->d_order, (int)b->count, b->d_T, b->d_F,
+                                                             b->d_G, b->d_chk, b->d_queue, b->L, b->tol, b->max_iter);
+      break;
+    case 256:
+      k_batch_sweep<256><<<grid, 256, b->L.total, b->st>>>(b->d_items, b->d_order, (int)b->count, b->d_T, b->d_F,
+                                                             b->d_G, b->d_chk, b->d_queue, b->L, b->tol, b->max_iter);
+      break;
+    case 512:
+      k_batch_sweep<512><<<grid, 512, b->L.total, b->st>>>(b->d_items, b->d_order, (int)b->count, b->d_T, b->d_F,
+                                                             b->d_G, b->d_chk, b->d_queue, b->L, b->tol, b->max_iter);
+      break;
+    default:
+      return CPALS_E_ARG;
+  }
+  k_batch_reset<<<1, 1024, 0, b->st>>>(b->d_queue, b->d_chk, (int)b->count, b->d_active);
+  b->launches += 2;
+  return cudaGetLastError() == cudaSuccess ? CPALS_OK : CPALS_E_CUDA;
+}
+
+int set_config(cpals_batch* b, int nt) {
+  const void* fn = nt == 128 ? (const void*)k_batch_sweep<128> : nt == 256 ? (const void*)k_batch_sweep<256>
+                                                                            : (const void*)k_batch_sweep<512>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->L.total) != cudaSuccess)
+    return CPALS_E_CUDA;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, b->L.total) != cudaSuccess || per_sm < 1)
+    return CPALS_E_UNSUPPORTED;
+  b->nt = nt;
+  b->ctas_per_sm = per_sm;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return CPALS_OK;
+}
+
+int build_graph(cpals_batch* b) {
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CPALS_E_CUDA;
+  const int64_t before = b->launches;
+  int rc = batch_launch(b);
+  b->launches = before;
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (rc != CPALS_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return rc != CPALS_OK ? rc : CPALS_E_CUDA;
+  }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  return e == cudaSuccess ? CPALS_OK : CPALS_E_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64_t* dims, const int64_t* ranks,
+                       const double* ref_norms) {
+  if (!out || count < 1 || !dims || !ranks || !ref_norms) return CPALS_E_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
+  cudaSetDevice(device);
+  cpals_batch* b = new cpals_batch();
+  b->device = device;
+  b->count = count;
+  b->items.resize(count);
+  for (int64_t t = 0; t < count; ++t) {
+    BatchItem& it = b->items[t];
+    for (int m = 0; m < 3; ++m) {
+      if (dims[3 * t + m] < 1 || dims[3 * t + m] > 4096) {
+        delete b;
+        return CPALS_E_ARG;
+      }
+      it.I[m] = (int)dims[3 * t + m];
+    }
+    if (ranks[t] < 1 || ranks[t] > 64 || !(ref_norms[t] > 0.0)) {
+      delete b;
+      return CPALS_E_ARG;
+    }
+    it.R = (int)ranks[t];
+    it.ref_norm = ref_norms[t];
+    it.toff = b->tot_T;
+    it.foff = b->tot_F;
+    it.goff = b->tot_G;
+    b->tot_T += (int64_t)it.I[0] * it.I[1] * it.I[2];
+    b->tot_F += (int64_t)(it.I[0] + it.I[1] + it.I[2] + 1) * it.R;
+    b->tot_G += (int64_t)3 * it.R * it.R;
+    b->Imax = std::max({b->Imax, it.I[0], it.I[1], it.I[2]});
+    b->Rmax = std::max(b->Rmax, it.R);
+  }
+  b->L = smem_layout(b->Imax, b->Rmax);
+  if (b->L.total > 227 * 1024) {
+    delete b;
+    return CPALS_E_UNSUPPORTED;
+  }
+  // largest work first (longest-processing-time order)
+  b->order.resize(count);
+  std::iota(b->order.begin(), b->order.end(), 0);
+  std::vector<double> work(count);
+  for (int64_t t = 0; t < count; ++t) {
+    const BatchItem& it = b->items[t];
+    work[t] = (double)it.I[0] * it.I[1] * it.I[2] * it.R + 3.0 * it.R * it.R * it.R * 20.0;
+  }
+  std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) { return work[a] > work[c]; });
+  cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+  bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMalloc(&b->d_items, sizeof(BatchItem) * count) == cudaSuccess &&
+            cudaMalloc(&b->d_order, sizeof(int) * count) == cudaSuccess &&
+            cudaMalloc(&b->d_T, sizeof(float) * b->tot_T) == cudaSuccess &&
+            cudaMalloc(&b->d_F, sizeof(double) * b->tot_F) == cudaSuccess &&
+            cudaMalloc(&b->d_G, sizeof(double) * b->tot_G) == cudaSuccess &&
+            cudaMalloc(&b->d_chk, sizeof(BatchCheck) * count) == cudaSuccess &&
+            cudaMalloc(&b->d_queue, sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc(&b->d_active, sizeof(int)) == cudaSuccess &&
+            cudaMallocHost(&b->h_active, sizeof(int)) == cudaSuccess;
+  if (!ok) {
+    cpals_batch_destroy(b);
+    return CPALS_E_CUDA;
+  }
+  cudaMemcpy(b->d_items, b->items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_order, b->order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+  cudaMemset(b->d_queue, 0, sizeof(unsigned));
+  cudaMemset(b->d_chk, 0, sizeof(BatchCheck) * count);
+  int rc = set_config(b, 256);
+  if (rc != CPALS_OK) rc = set_config(b, 128);
+  if (rc != CPALS_OK) {
+    cpals_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return CPALS_OK;
+}
+
+int cpals_batch_destroy(cpals_batch* b) {
+  if (!b) return CPALS_OK;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_items);
+  cudaFree(b->d_order);
+  cudaFree(b->d_T);
+  cudaFree(b->d_F);
+  cudaFree(b->d_G);
+  cudaFree(b->d_chk);
+  cudaFree(b->d_queue);
+  cudaFree(b->d_active);
+  if (b->h_active) cudaFreeHost(b->h_active);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return CPALS_OK;
+}
+
+int cpals_batch_set_tensors(cpals_batch* b, const float* host_concat) {
+  if (!b || !host_concat) return CPALS_E_ARG;
+  cudaSetDevice(b->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_T, host_concat, sizeof(float) * b->tot_T, cudaMemcpyHostToDevice, b->st));
+  return CPALS_OK;
+}
+
+int cpals_batch_set_factors(cpals_batch* b, const double* host_concat) {
+  if (!b || !host_concat) return CPALS_E_ARG;
+  cudaSetDevice(b->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_F, host_concat, sizeof(double) * b->tot_F, cudaMemcpyHostToDevice, b->st));
+  const int blocks = (int)std::min<int64_t>(b->count, 4096);
+  k_batch_init<<<blocks, 256, 0, b->st>>>(b->d_items, (int)b->count, b->d_F, b->d_G, b->d_chk);
+  CPALS_CUDA_TRY(cudaGetLastError());
+  CPALS_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->st));
+  b->launches += 1;
+  return CPALS_OK;
+}
+
+int cpals_batch_get_factors(cpals_batch* b, double* host_concat) {
+  if (!b || !host_concat) return CPALS_E_ARG;
+  cudaSetDevice(b->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(host_concat, b->d_F, sizeof(double) * b->tot_F, cudaMemcpyDeviceToHost, b->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
+  return CPALS_OK;
+}
+
+int cpals_batch_set_threads(cpals_batch* b, int threads) {
+  if (!b || (threads != 128 && threads != 256 && threads != 512)) return CPALS_E_ARG;
+  cudaSetDevice(b->device);
+  return set_config(b, threads);
+}
+
+int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_out, double* fits_out,
+                         int* flags_out, int64_t* launches_out) {
+  if (!b || max_iter < 1 || !(tol >= 0.0)) return CPALS_E_ARG;
+  cudaSetDevice(b->device);
+  if (b->tol != tol || b->max_iter != max_iter) {
+    b->tol = tol;
+    b->max_iter = max_iter;
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
+  if (!b->graph) {
+    int rc = build_graph(b);
+    if (rc != CPALS_OK) return rc;
+  }
+  int launched = 0, batch = 4;
+  const int64_t l0 = b->launches;
+  while (launched < max_iter) {
+    const int n = std::min(batch, max_iter - launched);
+    for (int k = 0; k < n; ++k) CPALS_CUDA_TRY(cudaGraphLaunch(b->graph, b->st));
+    b->launches += 2 * n;
+    launched += n;
+    CPALS_CUDA_TRY(cudaMemcpyAsync(b->h_active, b->d_active, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
+    if (*b->h_active == 0) break;
+    batch = std::min(batch * 2, 32);
+  }
+  std::vector<BatchCheck> h(b->count);
+  CPALS_CUDA_TRY(cudaMemcpy(h.data(), b->d_chk, sizeof(BatchCheck) * b->count, cudaMemcpyDeviceToHost));
+  int nan_any = 0;
+  for (int64_t t = 0; t < b->count; ++t) {
+    if (sweeps_out) sweeps_out[t] = h[t].sweeps;
+    if (fits_out) fits_out[t] = h[t].done ? h[t].final_fit : h[t].fit;
+    if (flags_out) flags_out[t] = (h[t].nan ? 1 : 0) | (h[t].rank_deficient ? 2 : 0) | (h[t].done ? 4 : 0);
+    nan_any |= h[t].nan;
+  }
+  if (launches_out) *launches_out = b->launches - l0;
+  return CPALS_OK;
+}
+
+// Autotuner: time `sweeps` sweeps of the batch (from its current factors) for each thread
+// count the shared-memory layout allows, keep the fastest.  The factors are restored from
+// `host_factors` after each trial.
+int cpals_batch_autotune(cpals_batch* b, const double* host_factors, int sweeps, int* threads_out,
+                         double* ms_out) {
+  if (!b || !host_factors || sweeps < 1) return CPALS_E_ARG;
+  cudaSetDevice(b->device);
+  const int cand[3] = {128, 256, 512};
+  double best = 1e300;
+  int best_nt = 0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int i = 0; i < 3; ++i) {
+    if (set_config(b, cand[i]) != CPALS_OK) continue;
+    int rc = cpals_batch_set_factors(b, host_factors);
+    if (rc != CPALS_OK) return rc;
+    cudaEventRecord(e0, b->st);
+    for (int s = 0; s < sweeps; ++s) {
+      rc = batch_launch(b);
+      if (rc != CPALS_OK) return rc;
+    }
+    cudaEventRecord(e1, b->st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_out) ms_out[i] = ms;
+    if (ms < best) {
+      best = ms;
+      best_nt = cand[i];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!best_nt) return CPALS_E_UNSUPPORTED;
+  int rc = set_config(b, best_nt);
+  if (rc == CPALS_OK) rc = cpals_batch_set_factors(b, host_factors);
+  if (threads_out) *threads_out = best_nt;
+  return rc;
+}
+
+}  // extern "C"

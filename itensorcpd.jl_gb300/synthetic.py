@@ -12,9 +12,15 @@ import numpy as np
 def congruent_factor(dim, rank, congruence, rng):
     """dim x rank, unit columns, A^T A = (1 - c) I + c 11^T (orthonormalised draws mixed by
     the transposed Cholesky factor of the congruence matrix)."""
-    Q, _ = np.linalg.qr(rng.standard_normal((dim, rank)))
+    Z = rng.standard_normal((dim, rank))
     C = (1.0 - congruence) * np.eye(rank) + congruence * np.ones((rank, rank))
-    return Q @ np.linalg.cholesky(C).T
+    if rank <= dim:
+        Q, _ = np.linalg.qr(Z)
+        return Q @ np.linalg.cholesky(C).T
+    # more columns than rows: the congruence can hold only approximately; unit-norm iid
+    # columns mixed by the same Cholesky factor, renormalised
+    A = (Z / np.linalg.norm(Z, axis=0)) @ np.linalg.cholesky(C).T
+    return A / np.linalg.norm(A, axis=0)
 
 
 def _khatri_rao(mats):

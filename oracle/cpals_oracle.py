@@ -449,10 +449,14 @@ def congruent_factor(dim, rank, congruence, rng) -> np.ndarray:
     Cholesky factor of C = (1 - c) I + c 11^T, so A^T A = C exactly.
     """
     Z = rng.standard_normal((dim, rank))
-    Q, _ = np.linalg.qr(Z)
     C = (1.0 - congruence) * np.eye(rank) + congruence * np.ones((rank, rank))
     L = np.linalg.cholesky(C)
-    return Q @ L.T
+    if rank <= dim:
+        Q, _ = np.linalg.qr(Z)
+        return Q @ L.T
+    # rank > dim: A^T A = C cannot hold; unit iid columns mixed by L, renormalised
+    A = (Z / np.linalg.norm(Z, axis=0)) @ L.T
+    return A / np.linalg.norm(A, axis=0)
 
 
 def lowrank_plus_noise(dims, rank, congruence, snr_db, rng, wmin=1.0, wmax=10.0, dtype=np.float32):

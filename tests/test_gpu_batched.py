@@ -1,0 +1,116 @@
+"""Batched small decompositions (cpals_batch_*) against the oracle, tensor by tensor.
+
+Each tensor of a batch of uneven shapes and ranks must follow the oracle's FP64 ALS from
+the same initial factors.  The batched MTTKRP multiplies FP32 tensor entries by FP32 factor
+copies with FP32 accumulation inside a slice (FP64 across slices), so per-sweep fits agree
+to ~1e-6 rather than FP64 rounding: the test bounds the final fit after a fixed number of
+sweeps by 2e-5, and FitCheck stopping sweeps by +-3 of the oracle's.
+"""
+import numpy as np
+import pytest
+
+from _data import det_factors
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def built(pkg):
+    import __graft_entry__
+
+    __graft_entry__.build()
+    return pkg
+
+
+def make_batch(oracle, count, seed, dmin=5, dmax=24, rmin=2, rmax=8):
+    rng = np.random.default_rng(seed)
+    dims, ranks, Ts, Fs, lams = [], [], [], [], []
+    for t in range(count):
+        d = tuple(int(x) for x in rng.integers(dmin, dmax + 1, size=3))
+        R = int(rng.integers(rmin, rmax + 1))
+        T, _, _ = oracle.lowrank_plus_noise(d, R, float(rng.uniform(0, 0.6)), float(rng.uniform(10, 40)), rng)
+        F, lam = det_factors(d, R, seed=1000 + t)
+        dims.append(d)
+        ranks.append(R)
+        Ts.append(T)
+        Fs.append(F)
+        lams.append(lam)
+    return dims, ranks, Ts, Fs, lams
+
+
+def test_batched_fixed_sweeps_match_oracle(built, oracle):
+    dims, ranks, Ts, Fs, lams = make_batch(oracle, 40, seed=1)
+    norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    with built.BatchEngine(dims, ranks, norms) as be:
+        be.set_tensors(Ts)
+        be.set_factors(Fs, lams)
+        sweeps, fits, flags, launches = be.optimize(tol=0.0, max_iter=6)
+        out = be.get_factors()
+    assert np.all(sweeps == 6) and np.all(flags & 4) and not np.any(flags & 1)
+    assert launches > 0
+    for t in range(len(Ts)):
+        chk = oracle.FitCheck(0.0, 6, norms[t])
+        F, lam, chk, _ = oracle.als_optimize(Ts[t].astype(np.float64), Fs[t], lams[t], check=chk)
+        assert abs(fits[t] - chk.trajectory[-1]) < 2e-5, (t, fits[t], chk.trajectory[-1])
+        # the factors themselves: unit columns and the same reconstruction
+        Fg, lg = out[t]
+        rec_g = oracle.reconstruct(Fg, lg)
+        rec_o = oracle.reconstruct(F, lam)
+        assert np.linalg.norm(rec_g - rec_o) / np.linalg.norm(rec_o) < 1e-3, t
+
+
+def test_batched_fitcheck_stopping(built, oracle):
+    dims, ranks, Ts, Fs, lams = make_batch(oracle, 24, seed=2)
+    norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    with built.BatchEngine(dims, ranks, norms) as be:
+        be.set_tensors(Ts)
+        be.set_factors(Fs, lams)
+        sweeps, fits, flags, _ = be.optimize(tol=1e-5, max_iter=200)
+    for t in range(len(Ts)):
+        chk = oracle.FitCheck(1e-5, 200, norms[t])
+        oracle.als_optimize(Ts[t].astype(np.float64), Fs[t], lams[t], check=chk)
+        n_or = len(chk.trajectory)
+        assert abs(int(sweeps[t]) - n_or) <= 3, (t, sweeps[t], n_or)
+        assert abs(fits[t] - chk.trajectory[-1]) < 1e-4, (t, fits[t], chk.trajectory[-1])
+
+
+def test_batched_autotune_and_thread_counts(built, oracle):
+    dims, ranks, Ts, Fs, lams = make_batch(oracle, 64, seed=3, dmin=16, dmax=40, rmin=4, rmax=16)
+    norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    res = {}
+    with built.BatchEngine(dims, ranks, norms) as be:
+        be.set_tensors(Ts)
+        nt, ms = be.autotune(Fs, lams, sweeps=2)
+        assert nt in (128, 256, 512)
+        for threads in (128, 256, 512):
+            be.set_threads(threads)
+            be.set_factors(Fs, lams)
+            _, fits, _, _ = be.optimize(tol=0.0, max_iter=4)
+            res[threads] = fits
+    # every output element is computed by one thread in a fixed order; only the
+    # block-wide sums of the fit depend on the warp count
+    assert np.max(np.abs(res[128] - res[512])) < 1e-12
+    assert np.max(np.abs(res[256] - res[512])) < 1e-12
+
+
+def test_batched_rank_deficient_stays_finite(built, oracle):
+    # a tensor whose initial factors repeat a column: V is singular, the sweep stops early
+    d, R = (9, 8, 7), 3
+    rng = np.random.default_rng(4)
+    T, _, _ = oracle.lowrank_plus_noise(d, R, 0.2, 30.0, rng)
+    F, lam = det_factors(d, R, seed=5)
+    for f in F:
+        f[:, 2] = f[:, 1]
+    with built.BatchEngine([d], [R], [float(np.linalg.norm(T))]) as be:
+        be.set_tensors([T])
+        be.set_factors([F], [lam])
+        sweeps, fits, flags, _ = be.optimize(tol=0.0, max_iter=3)
+    assert flags[0] & 2  # rank-deficient normal equations were met
+    assert not (flags[0] & 1) and np.isfinite(fits[0])
+
+
+def test_batched_rejects_bad_input(built):
+    with pytest.raises(Exception):
+        built.BatchEngine([(4, 5, 6)], [0], [1.0])
+    with pytest.raises(Exception):
+        built.BatchEngine([(4, 5, 6)], [3], [0.0])

@@ -49,7 +49,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparator and CPU baseline legs")
-    ap.add_argument("--workload", choices=["c2", "c3", "c4"], default="c2",
+    ap.add_argument("--c5-train", type=int, default=20000, help="c5: training decompositions")
+    ap.add_argument("--c5-eval", type=int, default=512, help="c5: held-out tensors")
+    ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
                     help="c2: 512^3 rank 64 (the headline line); c3: 128^4 rank 128, dimension tree, "
                          "plain and randomized paths; c4: 4096 small decompositions, batched")
     ap.add_argument("--profile-mttkrp", action="store_true",
@@ -349,6 +351,105 @@ def run_c4(args, pkg, device):
     print(json.dumps(line), flush=True)
 
 
+def run_c5(args, pkg, device):
+    """Learned warm start: 256^3 FP32 tensors, rank 32, congruence ~U[0,0.8], SNR ~U[10,40] dB,
+    generated on the device.  Sketch = MTTKRP with seeded Gaussian test matrices (32 columns
+    per mode) -> bases Q_n -> 32^3 core (engine MTTKRPs) -> Jennrich proposal -> MLP
+    correction (3072 -> 512 -> 512 -> 1024, BF16, FP32 accumulation), trained on the device on
+    ALS decompositions (ALS run from the generator's factors, 5 sweeps).  Judged on held-out
+    seeds against random init and against the proposal without the network: sweeps and GPU
+    time to reach 99% of the best fit any start attains within 100 sweeps."""
+    import torch
+
+    ws = pkg.warmstart
+    dims, R, S = (256, 256, 256), 32, 32
+    omegas = ws.gaussian_test_matrices(dims, S, seed=SEED + 5)
+    buf = torch.zeros(int(np.prod(dims)), dtype=torch.float32, device=f"cuda:{device}")
+
+    def prepare(eng, core_eng, seed):
+        rng = np.random.default_rng(seed)
+        cg, snr = float(rng.uniform(0, 0.8)), float(rng.uniform(10, 40))
+        facs, w = ws.synth_device(dims, R, cg, snr, rng, buf.data_ptr(), device=device)
+        eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
+        core_eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
+        nrm = float(buf.double().norm())
+        eng.timer_start()
+        Qs, _ = ws.sketch_bases(ws.sketch(eng, omegas))
+        prop = ws.jennrich(ws.core(core_eng, Qs), R, np.random.default_rng(seed + 7))
+        ms = eng.timer_stop()
+        return facs, w, nrm, Qs, prop, ms
+
+    X, Y = [], []
+    t0 = time.perf_counter()
+    with pkg.Engine(dims, R, dtype=np.float32, precision="bf16x3", device=device) as eng, \
+            pkg.Engine(dims, 256, dtype=np.float32, precision="bf16x3", device=device) as core_eng:
+        for s in range(args.c5_train):
+            facs, w, nrm, Qs, prop, _ = prepare(eng, core_eng, 1_000_000 + s)
+            eng.set_factors(facs, w)  # ALS from the generator's factors: the decomposition it reaches
+            eng.optimize(pkg.api._to_device_check(pkg.NoCheck(5)))
+            F, lam = eng.get_factors()
+            X.append(ws.features(prop))
+            Y.append(ws.targets(Qs, F, prop))
+        t_data = time.perf_counter() - t0
+        X = np.concatenate(X)
+        Y = np.concatenate(Y)
+        net = ws.WarmStartMLP((3 * S * R, 512, 512, S * R), device=device, seed=SEED)
+        nv = 3 * max(1, args.c5_train // 10)  # the last 10% of the training tensors calibrate the step
+        t1 = time.perf_counter()
+        losses = net.fit(X[:-nv], Y[:-nv], epochs=30, batch=256, lr=1e-3, seed=SEED)
+        scale = net.calibrate(X[-nv:], Y[-nv:])
+        val_mse = float(np.mean((net.forward(X[-nv:]) - Y[-nv:]) ** 2))
+        val_mse0 = float(np.mean(Y[-nv:] ** 2))
+        t_train = time.perf_counter() - t1
+        res = {k: {"sweeps": [], "ms": []} for k in ("random", "proposal", "learned")}
+        fallbacks = 0
+        for s in range(args.c5_eval):
+            facs, w, nrm, Qs, prop, ms_prop = prepare(eng, core_eng, 2_000_000 + s)
+            eng.timer_start()
+            Fw = ws.warm_factors(net, Qs, prop)
+            ms_net = eng.timer_stop()
+            Fp = ws.proposal_factors(Qs, prop)
+            fb = pkg.random_factors(dims, R, np.random.default_rng(s))[0]
+            fallbacks += int(Fw is None)
+            starts = {"random": (pkg.random_factors(dims, R, np.random.default_rng(3_000_000 + s))[0], 0.0),
+                      "proposal": (Fp if Fp is not None else fb, ms_prop),
+                      "learned": (Fw if Fw is not None else fb, ms_prop + ms_net)}
+            trajs, ms = {}, {}
+            for k, (F0, extra) in starts.items():
+                eng.set_factors(F0, np.ones(R))
+                eng.timer_start()
+                trajs[k] = eng.optimize(pkg.api._to_device_check(pkg.FitCheck(0.0, 100, nrm)))
+                ms[k] = (eng.timer_stop(), extra)
+            target = 0.99 * max(t.max() for t in trajs.values())
+            for k in res:
+                n = ws.sweeps_to_fit(trajs[k], target)
+                res[k]["sweeps"].append(n if n is not None else 101)
+                per = ms[k][0] / len(trajs[k])
+                res[k]["ms"].append(ms[k][1] + per * (n if n is not None else 101))
+    out = {}
+    for k, v in res.items():
+        sw = np.asarray(v["sweeps"])
+        out[k] = {"sweeps_p50": float(np.median(sw)), "sweeps_mean": float(sw.mean()),
+                  "sweeps_p90": float(np.percentile(sw, 90)), "reached_within_100": int(np.sum(sw <= 100)),
+                  "ms_to_target_p50": float(np.median(v["ms"])), "ms_to_target_mean": float(np.mean(v["ms"]))}
+    line = {
+        "metric": "sweeps_to_99pct_of_best_fit", "value": out["learned"]["sweeps_p50"], "unit": "sweeps",
+        "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "mlp bf16/f32-accumulate; als bf16x3 mttkrp, f64 solve", "data": "synthetic",
+        "config": {"workload": "warm_start_256cube_rank32_sketch32", "train": args.c5_train, "eval": args.c5_eval,
+                   "mlp": [3 * S * R, 512, 512, S * R]},
+        "c5": out, "fallbacks": fallbacks,
+        "gain_vs_random_p50": out["random"]["sweeps_p50"] / max(out["learned"]["sweeps_p50"], 1e-9),
+        "gain_vs_random_mean": out["random"]["sweeps_mean"] / max(out["learned"]["sweeps_mean"], 1e-9),
+        "gain_vs_proposal_mean": out["proposal"]["sweeps_mean"] / max(out["learned"]["sweeps_mean"], 1e-9),
+        "train": {"data_s": t_data, "train_s": t_train, "loss_first": float(np.mean(losses[:10])),
+                  "loss_last": float(np.mean(losses[-10:])), "samples": int(X.shape[0]) - nv,
+                  "validation_mse": val_mse, "validation_mse_of_zero_correction": val_mse0,
+                  "calibrated_step": scale},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -367,6 +468,10 @@ def main():
     if args.workload == "c4":
         if rank == 0:
             run_c4(args, pkg, local if world > 1 else 0)
+        return
+    if args.workload == "c5":
+        if rank == 0:
+            run_c5(args, pkg, local if world > 1 else 0)
         return
 
     dist = None

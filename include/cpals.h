@@ -204,6 +204,29 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
  * restores host_factors.  ms_out (3 entries, may be null): 128, 256, 512 threads. */
 int cpals_batch_autotune(cpals_batch* b, const double* host_factors, int sweeps, int* threads_out, double* ms_out);
 
+/* ---- seeded synthetic tensors on the device (no counterpart in the reference) ----
+ * T = sum_r w_r F_0(:,r) o F_1(:,r) o ... + Gaussian noise at snr_db (counter-based, from
+ * `seed`), FP32 column-major into the device buffer d_out (prod(dims) floats).  Factors:
+ * FP64 I_m x R column-major, concatenated.  snr_db <= -1000 disables the noise. */
+int cpals_synth_lowrank(int device, int order, const int64_t* dims, int64_t rank, const double* host_factors,
+                        const double* host_weights, double snr_db, uint64_t seed, float* d_out);
+
+/* ---- the warm-start network (no counterpart in the reference) ----
+ * A 3-layer MLP, widths[4] = {in, hidden1, hidden2, out}: BF16 weights and activations,
+ * FP32 accumulation, trained on the device (MSE loss, Adam).  Parameters are FP32:
+ * W1 [h1][in], b1, W2 [h2][h1], b2, W3 [out][h2], b3. */
+typedef struct cpals_mlp cpals_mlp;
+int cpals_mlp_create(cpals_mlp** out, int device, const int* widths);
+int cpals_mlp_destroy(cpals_mlp* m);
+int64_t cpals_mlp_num_params(cpals_mlp* m);
+int cpals_mlp_set_params(cpals_mlp* m, const float* host_params);
+int cpals_mlp_get_params(cpals_mlp* m, float* host_params);
+int cpals_mlp_forward(cpals_mlp* m, const float* host_x, int batch, float* host_y);
+int cpals_mlp_gradients(cpals_mlp* m, const float* host_x, const float* host_t, int batch, float* host_grads,
+                        double* loss_out);
+int cpals_mlp_set_dataset(cpals_mlp* m, const float* host_x, const float* host_t, int64_t n);
+int cpals_mlp_train(cpals_mlp* m, const int* host_idx, int steps, int batch, float lr, double* losses);
+
 #ifdef __cplusplus
 }
 #endif

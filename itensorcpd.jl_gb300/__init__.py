@@ -27,9 +27,11 @@ from .api import (
 )
 from .batched import BatchEngine
 from .engine import Engine
+from . import warmstart
+from .warmstart import WarmStartMLP
 
 __all__ = [
     "BatchEngine", "CPD", "CPDFit", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
     "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
-    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices",
+    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "WarmStartMLP", "warmstart",
 ]

@@ -47,6 +47,7 @@ class CpalsCheck(C.Structure):
 _P = C.c_void_p
 _I64P = C.POINTER(C.c_int64)
 _DP = C.POINTER(C.c_double)
+_FP = C.POINTER(C.c_float)
 SIGNATURES = {
     "cpals_version": (C.c_int, []),
     "cpals_status_string": (C.c_char_p, [C.c_int]),
@@ -81,6 +82,16 @@ SIGNATURES = {
     "cpals_batch_optimize": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(C.c_int), _DP, C.POINTER(C.c_int),
                                        _I64P]),
     "cpals_batch_autotune": (C.c_int, [_P, _DP, C.c_int, C.POINTER(C.c_int), _DP]),
+    "cpals_synth_lowrank": (C.c_int, [C.c_int, C.c_int, _I64P, C.c_int64, _DP, _DP, C.c_double, C.c_uint64, _P]),
+    "cpals_mlp_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(C.c_int)]),
+    "cpals_mlp_destroy": (C.c_int, [_P]),
+    "cpals_mlp_num_params": (C.c_int64, [_P]),
+    "cpals_mlp_set_params": (C.c_int, [_P, _FP]),
+    "cpals_mlp_get_params": (C.c_int, [_P, _FP]),
+    "cpals_mlp_forward": (C.c_int, [_P, _FP, C.c_int, _FP]),
+    "cpals_mlp_gradients": (C.c_int, [_P, _FP, _FP, C.c_int, _FP, _DP]),
+    "cpals_mlp_set_dataset": (C.c_int, [_P, _FP, _FP, C.c_int64]),
+    "cpals_mlp_train": (C.c_int, [_P, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_float, _DP]),
 }
 
 _lib = None

@@ -81,7 +81,8 @@ struct SolveInfo {
   int rank;      // rank reached by the pivoted Cholesky
   int fallback;  // 1 if the pivoted-QR path produced the solve operator
   int qr_rank;   // numerical rank found by the QR path
-  int pad;
+  int refine;    // 1: W is the FP32 sweep's inverse and V (FP64) is in the workspace; the
+                 // solve refines X once with the FP64 residual M - X V
 };
 
 // ---- launchers (defined in the kernel translation units) ----
@@ -94,8 +95,10 @@ cudaError_t launch_mttkrp_f64(const void* T, int tdtype, const FactorSet& fs, co
 
 // V = Hadamard of the Grams of every mode but `skip`; pivoted Cholesky (upper,
 // tol 1e-6) with a column-pivoted QR fallback.  Single CTA.
+// mixed = 1 (split-BF16 path, R <= 128): the sweep runs in FP32 first, and the FP64 sweep
+// only if the FP32 pivots signal ill-conditioning (info->refine tells the solve which).
 cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, double* work, double* U, int* piv,
-                             double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st);
+                             double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st, int mixed = 0);
 size_t factorize_work_doubles(int R);
 
 // Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and

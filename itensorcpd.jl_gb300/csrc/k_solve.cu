@@ -295,8 +295,11 @@ __device__ __forceinline__ bool key_is_nan(long long k) { return k == LLONG_MAX;
 __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int skip, int R, double* __restrict__ Aglob,
                                                   double* __restrict__ U, double* __restrict__ dinv,
                                                   int* __restrict__ piv, double* __restrict__ W,
-                                                  double* __restrict__ qwork, SolveInfo* info, DevCheck* chk) {
+                                                  double* __restrict__ qwork, SolveInfo* info, DevCheck* chk,
+                                                  int mixed) {
   if (done_flag(chk)) return;
+  if (mixed && info->refine) return;  // the FP32 sweep produced W
+  if (threadIdx.x == 0) info->refine = 0;
   extern __shared__ double smA[];
   // an odd leading dimension in shared memory keeps column accesses free of bank conflicts
   const int ld = (R <= 128) ? (R | 1) : R;
@@ -529,6 +532,166 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
   }
 }
 
+// ---------------- FP32 sweep (split-BF16 path) ----------------
+// The same pivoted symmetric sweep in FP32 (this part issues FP32 FMAs at 64x its FP64
+// rate, with ~4-cycle latency).  V is formed in FP64 exactly as above and kept in the
+// workspace; W = -A is the FP32 inverse.  The solve then refines X once with the FP64
+// residual (mixed-precision iterative refinement: X += (M - X V) W), which brings X to FP64
+// accuracy while kappa(V) eps_32 << 1.  A pivot below 1e-3 of the largest diagonal entry (or
+// a NaN, or a rank below R) leaves info->refine = 0 and the FP64 sweep takes over.
+__device__ __forceinline__ int fkey(float v) {
+  const int k = __float_as_int(v);
+  return (k & 0x7fffffff) > 0x7f800000 ? INT_MAX : k;
+}
+
+__global__ void __launch_bounds__(FT) k_factorize32(GramSet gs, int order, int skip, int R, double* __restrict__ Vg,
+                                                    double* __restrict__ W, SolveInfo* info, DevCheck* chk) {
+  if (done_flag(chk)) return;
+  extern __shared__ float smF[];
+  const int ld = R | 1;
+  float* A = smF;
+  __shared__ float s_a[128], s_t[128];
+  __shared__ unsigned char s_swept[128];
+  __shared__ float s_pv, s_pinv, s_maxd, s_minp;
+  __shared__ int s_p, s_stop;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int e0 = tid; e0 < R * R; e0 += 8 * FT) {
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = 1.0;
+    for (int m = 0; m < order; ++m) {
+      if (m == skip) continue;
+      const double* __restrict__ G = gs.G[m];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * FT;
+        if (e < R * R) v[q] *= G[e];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * FT;
+      if (e < R * R) {
+        const int r = e / R, c = e - r * R;
+        Vg[e] = v[q];  // FP64 V (symmetric) for the refinement
+        if (c >= r) A[r * ld + c] = (float)v[q];
+      }
+    }
+  }
+  for (int k = tid; k < R; k += blockDim.x) s_swept[k] = 0;
+  __syncthreads();
+  auto pick = [&](int bk, int bi) {
+    const int mk = __reduce_max_sync(0xffffffffu, bk);
+    const int p = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+    if (lane == 0) {
+      const float pv = __int_as_float(mk);
+      const int stop = (mk == INT_MAX) || !(pv > 1e-3f * s_maxd) || p >= R;
+      s_stop = stop;
+      s_p = p;
+      if (!stop) {
+        s_pv = pv;
+        s_pinv = 1.0f / pv;
+        s_minp = fminf(s_minp, pv);
+      }
+    }
+    __syncwarp();
+  };
+  if (warp == 0) {
+    int bk = INT_MIN, bi = R;
+    float md = 0.f;
+    for (int i = lane; i < R; i += 32) {
+      const float d = A[i * ld + i];
+      md = fmaxf(md, d);
+      const int key = fkey(d);
+      if (bi == R || key > bk) {
+        bk = key;
+        bi = i;
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, off));
+    if (lane == 0) {
+      s_maxd = md;
+      s_minp = INFINITY;
+    }
+    __syncwarp();
+    pick(bk, bi);
+  }
+  __syncthreads();
+  int ok = 1;
+  for (int j = 0; j < R; ++j) {
+    if (s_stop) {
+      ok = 0;
+      break;
+    }
+    const int k = s_p;
+    const float dk = s_pinv;
+    for (int i = tid; i < R; i += blockDim.x) {
+      const float a = (i <= k) ? A[i * ld + k] : A[k * ld + i];
+      s_a[i] = a;
+      s_t[i] = a * dk;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      if (tid == 0) s_swept[k] = 1;
+      int bk = INT_MIN, bi = R;
+      for (int i = lane; i < R; i += 32) {
+        if (i == k) {
+          A[i * ld + i] = -dk;
+          continue;
+        }
+        const float v = fmaf(-s_a[i], s_t[i], A[i * ld + i]);
+        A[i * ld + i] = v;
+        if (!s_swept[i]) {
+          const int key = fkey(v);
+          if (bi == R || key > bk) {
+            bk = key;
+            bi = i;
+          }
+        }
+      }
+      if (j + 1 < R) pick(bk, bi);
+    } else {
+      // strictly upper entries, rows paired as in the FP64 sweep; thread e of the update
+      // warps takes entries e, e + nthreads, ... of the (R-1) x (R-1) upper triangle
+      const int m = R - 1;
+      const int cnt = m * (m + 1) / 2;
+      const int ut = tid - 32, un = blockDim.x - 32;
+      for (int e = ut; e < cnt; e += un) {
+        // row pair q holds R entries: (q, q+1+t) for t < R-1-q, else (R-2-q, ...)
+        const int q = e / R, t = e - q * R;
+        int i, c;
+        if (t < R - 1 - q) {
+          i = q;
+          c = q + 1 + t;
+        } else {
+          i = R - 2 - q;
+          c = i + 1 + (t - (R - 1 - q));
+          if (i == q) continue;  // the middle row of an even R is listed once
+        }
+        float v;
+        if (i == k) v = s_t[c];
+        else if (c == k) v = s_t[i];
+        else v = fmaf(-s_a[i], s_t[c], A[i * ld + c]);
+        A[i * ld + c] = v;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    info->refine = ok;
+    if (ok) {
+      info->rank = R;
+      info->fallback = 0;
+      info->qr_rank = R;
+    }
+  }
+  if (!ok) return;
+  for (int e = tid; e < R * R; e += blockDim.x) {
+    const int r = e / R, c = e - r * R;
+    W[e] = -(double)((r <= c) ? A[r * ld + c] : A[c * ld + r]);
+  }
+}
+
 // ---------------- solve: X = M W^T ----------------
 // M rows are the split-K partial sums (added in split order, FP64); W^T is the solve
 // operator from the factorisation (V^{-1}, or the pivoted-QR least-squares operator),
@@ -542,13 +705,17 @@ constexpr int kSolveStageMaxR = 128;  // W^T (R^2 doubles) staged in shared memo
 template <typename PT>
 __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
                                                         const double* __restrict__ WT, double* __restrict__ X,
-                                                        double* __restrict__ inner_rows, const DevCheck* chk) {
+                                                        double* __restrict__ inner_rows, const DevCheck* chk,
+                                                        const SolveInfo* __restrict__ info,
+                                                        const double* __restrict__ Vg) {
   if (done_flag(chk)) return;
   extern __shared__ double sm[];
   double* Ms = sm;            // RB x R
   double* Ps = sm + RB * R;   // RB x R products for the fit
+  double* Xs = sm + 2 * RB * R;  // RB x R: X before the refinement, then the residual
   const bool staged = (R <= kSolveStageMaxR);
-  double* Ws = sm + 2 * RB * R;
+  const bool refine = info && info->refine;
+  double* Ws = sm + 3 * RB * R;
   const int tid = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * RB;
   const int rows = (In - r0 < (int64_t)RB) ? (int)(In - r0) : RB;
@@ -616,23 +783,49 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
   }
   __syncthreads();
   const double* W = staged ? Ws : WT;
-  for (int e = tid; e < nval; e += SOLVE_T) {
-    const int row = e / R, k = e - row * R;
-    const double* m = Ms + row * R;
+  // one output of A B for the row `row` of A (RB x R in shared memory), column k of B (R x R)
+  auto rowdot = [&](const double* Arow, const double* __restrict__ B, int k) {
     double a[8];
 #pragma unroll
     for (int t = 0; t < 8; ++t) a[t] = 0.0;
     int l = 0;
     for (; l + 8 <= R; l += 8) {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) a[t] = fma(m[l + t], W[(size_t)(l + t) * R + k], a[t]);
+      for (int t = 0; t < 8; ++t) a[t] = fma(Arow[l + t], B[(size_t)(l + t) * R + k], a[t]);
     }
 #pragma unroll
     for (int t = 0; t < 8; ++t)
-      if (l + t < R) a[t] = fma(m[l + t], W[(size_t)(l + t) * R + k], a[t]);
-    const double x = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-    X[base + e] = x;
-    Ps[e] = m[k] * x;
+      if (l + t < R) a[t] = fma(Arow[l + t], B[(size_t)(l + t) * R + k], a[t]);
+    return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+  };
+  if (refine) {
+    // mixed-precision iterative refinement with the FP32 inverse W and the FP64 V:
+    // X0 = M W, E = M - X0 V, X = X0 + E W
+    for (int e = tid; e < nval; e += SOLVE_T) {
+      const int row = e / R, k = e % R;
+      Xs[e] = rowdot(Ms + row * R, W, k);
+    }
+    __syncthreads();
+    for (int e = tid; e < nval; e += SOLVE_T) {
+      const int row = e / R, k = e % R;
+      Ps[e] = Ms[e] - rowdot(Xs + row * R, Vg, k);  // residual (Ps is free until the fit)
+    }
+    __syncthreads();
+    for (int e = tid; e < nval; e += SOLVE_T) {
+      const int row = e / R, k = e % R;
+      const double x = Xs[e] + rowdot(Ps + row * R, W, k);
+      X[base + e] = x;
+      Xs[e] = x;
+    }
+    __syncthreads();
+    for (int e = tid; e < nval; e += SOLVE_T) Ps[e] = Ms[e] * Xs[e];
+  } else {
+    for (int e = tid; e < nval; e += SOLVE_T) {
+      const int row = e / R, k = e % R;
+      const double x = rowdot(Ms + row * R, W, k);
+      X[base + e] = x;
+      Ps[e] = Ms[e] * x;
+    }
   }
   if (!inner_rows) return;
   __syncthreads();
@@ -981,8 +1174,8 @@ __global__ void k_reduce_partials(const PT* __restrict__ part, int S, int64_t n,
 size_t factorize_work_doubles(int R) { return 5 * (size_t)R * R + 4 * (size_t)R + 64; }
 
 cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, double* work, double* U, int* piv,
-                             double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st) {
-  // work layout: [Aglob R*R][dinv R][qwork 4R^2 + 3R + 64]
+                             double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st, int mixed) {
+  // work layout: [Aglob R*R (FP64 V of the FP32 sweep when R <= 128)][dinv R][qwork 4R^2 + 3R + 64]
   double* Aglob = work;
   double* dinv = work + (size_t)R * R;
   double* qwork = dinv + R;
@@ -990,9 +1183,16 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_factorize, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_factorize32, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 129 * 4);
     attr_set = true;
   }
-  k_factorize<<<1, FT, smem, st>>>(gs, order, skip, R, Aglob, U, dinv, piv, W, qwork, info, chk);
+  mixed = (mixed && R <= 128) ? 1 : 0;
+  if (mixed) {
+    k_factorize32<<<1, FT, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, Aglob, W, info, chk);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  k_factorize<<<1, FT, smem, st>>>(gs, order, skip, R, Aglob, U, dinv, piv, W, qwork, info, chk, mixed);
   return cudaGetLastError();
 }
 
@@ -1001,27 +1201,25 @@ static int solve_rows_per_block(int R) { return R >= 256 ? 1 : 256 / R; }
 cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
                               const double* U, const int* piv, const double* W, const SolveInfo* info, double* X,
                               double* inner_rows, const DevCheck* chk, cudaStream_t st) {
-  (void)work;
   (void)U;
   (void)piv;
-  (void)info;
   const int RB = solve_rows_per_block(R);
   dim3 grid((unsigned)((In + RB - 1) / RB));
-  size_t smem = (size_t)2 * RB * R * sizeof(double);
+  size_t smem = (size_t)3 * RB * R * sizeof(double);
   if (R <= kSolveStageMaxR) smem += (size_t)R * R * sizeof(double);
   static bool attr_set = false;
   if (!attr_set) {
-    const int mx = 2 * 256 * 8 + kSolveStageMaxR * kSolveStageMaxR * 8;
+    const int mx = 3 * 256 * 8 + kSolveStageMaxR * kSolveStageMaxR * 8;
     cudaFuncSetAttribute(k_solve_gemm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_solve_gemm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     attr_set = true;
   }
   if (part_is_f32)
     k_solve_gemm<float><<<grid, SOLVE_T, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X,
-                                                     inner_rows, chk);
+                                                     inner_rows, chk, info, work);
   else
     k_solve_gemm<double><<<grid, SOLVE_T, smem, st>>>(static_cast<const double*>(part), splits, In, R, RB, W, X,
-                                                      inner_rows, chk);
+                                                      inner_rows, chk, info, work);
   return cudaGetLastError();
 }
 

@@ -544,8 +544,10 @@ __device__ __forceinline__ int fkey(float v) {
   return (k & 0x7fffffff) > 0x7f800000 ? INT_MAX : k;
 }
 
-__global__ void __launch_bounds__(FT) k_factorize32(GramSet gs, int order, int skip, int R, double* __restrict__ Vg,
-                                                    double* __restrict__ W, SolveInfo* info, DevCheck* chk) {
+constexpr int FT32 = 512;    // FP32 sweep threads
+constexpr int kEnt32 = 24;   // entries per update thread (12 update warps, R <= 128)
+__global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int skip, int R, double* __restrict__ Vg,
+                                                      double* __restrict__ W, SolveInfo* info, DevCheck* chk) {
   if (done_flag(chk)) return;
   extern __shared__ float smF[];
   const int ld = R | 1;
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(FT) k_factorize32(GramSet gs, int order, int s
   __shared__ float s_pv, s_pinv, s_maxd, s_minp;
   __shared__ int s_p, s_stop;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int e0 = tid; e0 < R * R; e0 += 8 * FT) {
+  for (int e0 = tid; e0 < R * R; e0 += 8 * FT32) {
     double v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = 1.0;
@@ -564,13 +566,13 @@ __global__ void __launch_bounds__(FT) k_factorize32(GramSet gs, int order, int s
       const double* __restrict__ G = gs.G[m];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int e = e0 + q * FT;
+        const int e = e0 + q * FT32;
         if (e < R * R) v[q] *= G[e];
       }
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const int e = e0 + q * FT;
+      const int e = e0 + q * FT32;
       if (e < R * R) {
         const int r = e / R, c = e - r * R;
         Vg[e] = v[q];  // FP64 V (symmetric) for the refinement
@@ -617,6 +619,39 @@ __global__ void __launch_bounds__(FT) k_factorize32(GramSet gs, int order, int s
     pick(bk, bi);
   }
   __syncthreads();
+  // The sweep updates the same strictly-upper entries at every step, so each update thread
+  // (warps on schedulers 1-3, warp % 4 != 0: warp 0's look-ahead has scheduler 0 to itself)
+  // decodes its entries once: rows paired as in the FP64 sweep, entry f of the flattened
+  // (R-1) x (R-1) upper triangle, f = ut, ut + nut, ...; packed as (i << 16) | c.
+  const bool upd = (warp & 3) != 0;
+  const int ut = (warp >> 2) * 96 + ((warp & 3) - 1) * 32 + lane;  // 0 .. 383
+  const int nut = (FT32 >> 5) / 4 * 3 * 32;
+  int ent[kEnt32];
+  int nent = 0;
+  {
+    const int m = R - 1;
+    const int cnt = m * (m + 1) / 2;
+#pragma unroll
+    for (int q = 0; q < kEnt32; ++q) {
+      ent[q] = -1;
+      const int f = ut + q * nut;
+      if (upd && f < cnt) {
+        const int pq = f / R, t = f - pq * R;
+        int i, c;
+        if (t < R - 1 - pq) {
+          i = pq;
+          c = pq + 1 + t;
+        } else {
+          i = R - 2 - pq;
+          c = i + 1 + (t - (R - 1 - pq));
+        }
+        if (!(t >= R - 1 - pq && i == pq)) {  // the middle row of an even R is listed once
+          ent[q] = (i << 16) | c;
+          nent = q + 1;
+        }
+      }
+    }
+  }
   int ok = 1;
   for (int j = 0; j < R; ++j) {
     if (s_stop) {
@@ -650,29 +685,34 @@ __global__ void __launch_bounds__(FT) k_factorize32(GramSet gs, int order, int s
         }
       }
       if (j + 1 < R) pick(bk, bi);
-    } else {
-      // strictly upper entries, rows paired as in the FP64 sweep; thread e of the update
-      // warps takes entries e, e + nthreads, ... of the (R-1) x (R-1) upper triangle
-      const int m = R - 1;
-      const int cnt = m * (m + 1) / 2;
-      const int ut = tid - 32, un = blockDim.x - 32;
-      for (int e = ut; e < cnt; e += un) {
-        // row pair q holds R entries: (q, q+1+t) for t < R-1-q, else (R-2-q, ...)
-        const int q = e / R, t = e - q * R;
-        int i, c;
-        if (t < R - 1 - q) {
-          i = q;
-          c = q + 1 + t;
-        } else {
-          i = R - 2 - q;
-          c = i + 1 + (t - (R - 1 - q));
-          if (i == q) continue;  // the middle row of an even R is listed once
+    } else if (upd) {
+      // this thread's entries, six at a time with the loads issued first
+#pragma unroll
+      for (int q0 = 0; q0 < kEnt32; q0 += 6) {
+        if (q0 >= nent) break;
+        float av[6], xv[6], yv[6];
+#pragma unroll
+        for (int b = 0; b < 6; ++b) {
+          const int e = ent[q0 + b];
+          av[b] = xv[b] = yv[b] = 0.f;
+          if (e >= 0) {
+            const int i = e >> 16, c = e & 0xffff;
+            if (i == k) {
+              av[b] = s_t[c];
+            } else if (c == k) {
+              av[b] = s_t[i];
+            } else {
+              av[b] = A[i * ld + c];
+              xv[b] = s_a[i];
+              yv[b] = s_t[c];
+            }
+          }
         }
-        float v;
-        if (i == k) v = s_t[c];
-        else if (c == k) v = s_t[i];
-        else v = fmaf(-s_a[i], s_t[c], A[i * ld + c]);
-        A[i * ld + c] = v;
+#pragma unroll
+        for (int b = 0; b < 6; ++b) {
+          const int e = ent[q0 + b];
+          if (e >= 0) A[(e >> 16) * ld + (e & 0xffff)] = fmaf(-xv[b], yv[b], av[b]);
+        }
       }
     }
     __syncthreads();
@@ -712,10 +752,14 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
   extern __shared__ double sm[];
   double* Ms = sm;            // RB x R
   double* Ps = sm + RB * R;   // RB x R products for the fit
-  double* Xs = sm + 2 * RB * R;  // RB x R: X before the refinement, then the residual
+  double* Xs = sm + 2 * RB * R;  // RB x R: X before the refinement
+  float* Fs = reinterpret_cast<float*>(sm + 3 * RB * R);  // RB x R floats: M, then the residual
   const bool staged = (R <= kSolveStageMaxR);
   const bool refine = info && info->refine;
-  double* Ws = sm + 3 * RB * R;
+  double* St = sm + 3 * RB * R + (RB * R + 1) / 2;  // staging area
+  double* Ws = St;                                    // W (FP64 path)
+  float* W32 = reinterpret_cast<float*>(St);          // W (refinement: the FP32 sweep's inverse)
+  double* Vs = St + (R * R + 1) / 2;                  // V (refinement)
   const int tid = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * RB;
   const int rows = (In - r0 < (int64_t)RB) ? (int)(In - r0) : RB;
@@ -725,16 +769,24 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
   if (staged) {
     const int n = R * R;
     for (int e0 = tid; e0 < n; e0 += 8 * SOLVE_T) {
-      double w[8];
+      double w[8], v[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int e = e0 + q * SOLVE_T;
         w[q] = (e < n) ? __ldg(&WT[e]) : 0.0;
+        v[q] = (refine && e < n) ? __ldg(&Vg[e]) : 0.0;
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int e = e0 + q * SOLVE_T;
-        if (e < n) Ws[e] = w[q];
+        if (e < n) {
+          if (refine) {
+            W32[e] = (float)w[q];  // exact: the FP32 sweep's values
+            Vs[e] = v[q];
+          } else {
+            Ws[e] = w[q];
+          }
+        }
       }
     }
   }
@@ -799,26 +851,44 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
     return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
   };
   if (refine) {
-    // mixed-precision iterative refinement with the FP32 inverse W and the FP64 V:
-    // X0 = M W, E = M - X0 V, X = X0 + E W
+    // Mixed-precision iterative refinement with the FP32 inverse W and the FP64 V: only the
+    // residual needs FP64 (it cancels); X0 and the correction carry FP32 relative error,
+    // and the correction is ~kappa eps_32 smaller than X:
+    //   X0 = M W (FP32),  E = M - X0 V (FP64),  X = X0 + E W (FP32 product, FP64 sum)
+    auto rowdot32 = [&](const float* Arow, int k) {
+      float a[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) a[t] = 0.f;
+      int l = 0;
+      for (; l + 8 <= R; l += 8) {
+#pragma unroll
+        for (int t = 0; t < 8; ++t) a[t] = fmaf(Arow[l + t], W32[(size_t)(l + t) * R + k], a[t]);
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        if (l + t < R) a[t] = fmaf(Arow[l + t], W32[(size_t)(l + t) * R + k], a[t]);
+      return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    };
+    for (int e = tid; e < nval; e += SOLVE_T) Fs[e] = (float)Ms[e];
+    __syncthreads();
     for (int e = tid; e < nval; e += SOLVE_T) {
       const int row = e / R, k = e % R;
-      Xs[e] = rowdot(Ms + row * R, W, k);
+      Xs[e] = (double)rowdot32(Fs + row * R, k);
     }
     __syncthreads();
     for (int e = tid; e < nval; e += SOLVE_T) {
       const int row = e / R, k = e % R;
-      Ps[e] = Ms[e] - rowdot(Xs + row * R, Vg, k);  // residual (Ps is free until the fit)
+      Ps[e] = Ms[e] - rowdot(Xs + row * R, Vs, k);
     }
+    __syncthreads();
+    for (int e = tid; e < nval; e += SOLVE_T) Fs[e] = (float)Ps[e];
     __syncthreads();
     for (int e = tid; e < nval; e += SOLVE_T) {
       const int row = e / R, k = e % R;
-      const double x = Xs[e] + rowdot(Ps + row * R, W, k);
+      const double x = Xs[e] + (double)rowdot32(Fs + row * R, k);
       X[base + e] = x;
-      Xs[e] = x;
+      Ps[e] = Ms[e] * x;
     }
-    __syncthreads();
-    for (int e = tid; e < nval; e += SOLVE_T) Ps[e] = Ms[e] * Xs[e];
   } else {
     for (int e = tid; e < nval; e += SOLVE_T) {
       const int row = e / R, k = e % R;
@@ -1188,7 +1258,7 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   }
   mixed = (mixed && R <= 128) ? 1 : 0;
   if (mixed) {
-    k_factorize32<<<1, FT, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, Aglob, W, info, chk);
+    k_factorize32<<<1, FT32, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, Aglob, W, info, chk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -1205,11 +1275,12 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
   (void)piv;
   const int RB = solve_rows_per_block(R);
   dim3 grid((unsigned)((In + RB - 1) / RB));
-  size_t smem = (size_t)3 * RB * R * sizeof(double);
-  if (R <= kSolveStageMaxR) smem += (size_t)R * R * sizeof(double);
+  // M, products, X0 (doubles), M / residual (floats), then W (FP64, or FP32 + V in FP64)
+  size_t smem = (size_t)3 * RB * R * sizeof(double) + (size_t)((RB * R + 1) / 2) * sizeof(double);
+  if (R <= kSolveStageMaxR) smem += (size_t)((R * R + 1) / 2 + R * R) * sizeof(double);
   static bool attr_set = false;
   if (!attr_set) {
-    const int mx = 3 * 256 * 8 + kSolveStageMaxR * kSolveStageMaxR * 8;
+    const int mx = 3 * 256 * 8 + 128 * 8 + (kSolveStageMaxR * kSolveStageMaxR / 2 + kSolveStageMaxR * kSolveStageMaxR) * 8;
     cudaFuncSetAttribute(k_solve_gemm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_solve_gemm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     attr_set = true;

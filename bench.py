@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparator and CPU baseline legs")
+    ap.add_argument("--c4-count", type=int, default=4096, help="c4: tensors in the batch")
     ap.add_argument("--c5-train", type=int, default=20000, help="c5: training decompositions")
     ap.add_argument("--c5-eval", type=int, default=512, help="c5: held-out tensors")
     ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
@@ -308,8 +309,9 @@ def run_c4(args, pkg, device):
     from itensorcpd_gb300.synthetic import lowrank_plus_noise
 
     rng = np.random.default_rng(SEED + 4)
+    count = args.c4_count
     dims, ranks, Ts, Fs, lams, norms = [], [], [], [], [], []
-    for t in range(C4_COUNT):
+    for t in range(count):
         d = tuple(int(x) for x in rng.integers(16, 97, size=3))
         R = int(rng.integers(4, 33))
         T, _, _ = lowrank_plus_noise(d, R, float(rng.uniform(0, 0.6)), float(rng.uniform(10, 40)), rng)
@@ -333,10 +335,10 @@ def run_c4(args, pkg, device):
             runs.append(time.perf_counter() - t1)
         total_s = float(np.median(runs))
     line = {
-        "metric": "batched_cp_als_solves_per_s", "value": C4_COUNT / total_s, "unit": "solves/s", "n_gpus": 1,
+        "metric": "batched_cp_als_solves_per_s", "value": count / total_s, "unit": "solves/s", "n_gpus": 1,
         "steps": max(1, args.steps), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 mttkrp (f32 slices, f64 across slices), f64 solve/gram/fit", "data": "synthetic",
-        "config": {"workload": "batched_4096_order3_dims16-96_rank4-32_fitcheck1e-5_200", "count": C4_COUNT,
+        "config": {"workload": f"batched_{count}_order3_dims16-96_rank4-32_fitcheck1e-5_200", "count": count,
                    "elements": elems, "tensor_bytes": 4 * elems},
         "ms_per_batch": total_s * 1e3,
         "sweeps": {"p50": float(np.percentile(sweeps, 50)), "p99": float(np.percentile(sweeps, 99)),

@@ -53,8 +53,9 @@ struct BatchCheck {  // fit_check.jl:5-20, per tensor
 };
 
 struct SmemLayout {
-  int Imax, Rmax, ld;
+  int Imax, Rmax, ld, lm;  // lm: odd leading dimension (doubles) of M and X
   size_t slice, f32, M, X, A, G, vec, total;
+  size_t slice_bytes;      // one of the two slice buffers
 };
 
 __host__ __device__ inline size_t al16(size_t b) { return (b + 15) & ~size_t(15); }
@@ -65,15 +66,17 @@ __host__ __device__ inline SmemLayout smem_layout(int Imax, int Rmax) {
   L.Rmax = (Rmax + 3) & ~3;  // FP32 factor rows of 16-byte multiples (float4 loads)
   Rmax = L.Rmax;
   L.ld = Rmax | 1;
+  L.lm = Rmax + 1;  // Rmax is a multiple of 4: odd, so row walks of M and X are conflict-free
   size_t o = 0;
   L.slice = o;
-  o += al16((size_t)Imax * (Imax | 1) * 4);
+  L.slice_bytes = al16((size_t)Imax * (Imax | 1) * 4);
+  o += 2 * L.slice_bytes;  // double-buffered: slice k+1 loads while slice k is used
   L.f32 = o;
   o += al16((size_t)3 * Imax * Rmax * 4);
   L.M = o;
-  o += al16((size_t)Imax * Rmax * 8);
+  o += al16((size_t)Imax * L.lm * 8);
   L.X = o;
-  o += al16((size_t)Imax * Rmax * 8);
+  o += al16((size_t)Imax * L.lm * 8);
   L.A = o;
   o += al16((size_t)Rmax * L.ld * 8);
   L.G = o;
@@ -96,6 +99,14 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
   return t;
 }
 
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ long long bkey(double v) {
   const long long k = __double_as_longlong(v);
   return (k & 0x7fffffffffffffffll) > 0x7ff0000000000000ll ? LLONG_MAX : k;
@@ -111,6 +122,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int R = it.R, I0 = it.I[0], I1 = it.I[1], I2 = it.I[2];
   const int Rm = L.Rmax;
+  const int lm = L.lm;
   float* S = reinterpret_cast<float*>(sm + L.slice);
   float* F32 = reinterpret_cast<float*>(sm + L.f32);  // F32 + m*Imax*Rm: [I_m][R] row-major (ld Rm)
   double* M = reinterpret_cast<double*>(sm + L.M);     // [I_n][Rm]
@@ -141,14 +153,28 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   for (int n = 0; n < 3; ++n) {
     const int In = it.I[n];
     // ---- MTTKRP, slice by slice over the last mode: each slice S = T[:, :, k]
-    for (int e = tid; e < In * R; e += nt) M[(e / R) * Rm + e % R] = 0.0;
+    for (int e = tid; e < In * R; e += nt) M[(e / R) * lm + e % R] = 0.0;
     const float* Fa = F32 + (size_t)(n == 0 ? 1 : 0) * L.Imax * Rm;  // the other in-slice mode
     const float* F2 = F32 + (size_t)2 * L.Imax * Rm;
-    for (int k = 0; k < I2; ++k) {
-      __syncthreads();
+    // Slices are double-buffered: slice k+1 is copied (cp.async, 4 bytes per element) while
+    // slice k is used.  S[i + ldS j] has an odd leading dimension, so column walks are free
+    // of bank conflicts.
+    auto load_slice = [&](int k, float* dst) {
       const float* Tk = Tt + (int64_t)k * I0 * I1;
-      // S[i + ldS j] with an odd leading dimension: column walks are free of bank conflicts
-      for (int e = tid; e < I0 * I1; e += nt) S[(e % I0) + ldS * (e / I0)] = Tk[e];
+      for (int e = tid; e < I0 * I1; e += nt) cp_async4(dst + (e % I0) + ldS * (e / I0), Tk + e);
+      cp_async_commit();
+    };
+    float* Sbuf[2] = {S, S + L.slice_bytes / 4};
+    __syncthreads();  // the previous mode's reads of both buffers are done
+    load_slice(0, Sbuf[0]);
+    for (int k = 0; k < I2; ++k) {
+      const float* Sk = Sbuf[k & 1];
+      if (k + 1 < I2) {
+        load_slice(k + 1, Sbuf[(k + 1) & 1]);
+        cp_async_wait_1();
+      } else {
+        cp_async_wait_0();
+      }
       __syncthreads();
       // Each thread takes one row of the output and four consecutive rank columns: one
       // scalar slice load and one 16-byte factor load feed four FMAs.
@@ -159,7 +185,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
           const int i = e % I0, r0 = (e / I0) * 4;
           float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int j = 0; j < I1; ++j) {
-            const float sv = S[i + ldS * j];
+            const float sv = Sk[i + ldS * j];
             const float4 f = *reinterpret_cast<const float4*>(&Fa[j * Rm + r0]);
             a.x = fmaf(sv, f.x, a.x);
             a.y = fmaf(sv, f.y, a.y);
@@ -167,7 +193,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
             a.w = fmaf(sv, f.w, a.w);
           }
           const float4 f2 = *reinterpret_cast<const float4*>(&F2[k * Rm + r0]);
-          double* Mi = M + i * Rm + r0;
+          double* Mi = M + i * lm + r0;
           Mi[0] += (double)(a.x * f2.x);
           if (r0 + 1 < R) Mi[1] += (double)(a.y * f2.y);
           if (r0 + 2 < R) Mi[2] += (double)(a.z * f2.z);
@@ -181,7 +207,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
           const int j = e % I1, r0 = (e / I1) * 4;
           float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int i = 0; i < I0; ++i) {
-            const float sv = S[i + ldS * j];
+            const float sv = Sk[i + ldS * j];
             const float4 f = *reinterpret_cast<const float4*>(&Fa[i * Rm + r0]);
             a.x = fmaf(sv, f.x, a.x);
             a.y = fmaf(sv, f.y, a.y);
@@ -189,7 +215,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
             a.w = fmaf(sv, f.w, a.w);
           }
           const float4 g = *reinterpret_cast<const float4*>(n == 1 ? &F2[k * Rm + r0] : &F1[j * Rm + r0]);
-          double* out = (n == 1) ? M + j * Rm + r0 : X + j * Rm + r0;
+          double* out = (n == 1) ? M + j * lm + r0 : X + j * lm + r0;
           const double v0 = (double)(a.x * g.x), v1 = (double)(a.y * g.y), v2 = (double)(a.z * g.z),
                        v3 = (double)(a.w * g.w);
           if (n == 1) {
@@ -210,14 +236,15 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
             double s0 = 0.0, s1 = 0.0;
             int j = 0;
             for (; j + 1 < I1; j += 2) {
-              s0 += X[j * Rm + r];
-              s1 += X[(j + 1) * Rm + r];
+              s0 += X[j * lm + r];
+              s1 += X[(j + 1) * lm + r];
             }
-            if (j < I1) s0 += X[j * Rm + r];
-            M[k * Rm + r] = s0 + s1;
+            if (j < I1) s0 += X[j * lm + r];
+            M[k * lm + r] = s0 + s1;
           }
         }
       }
+      __syncthreads();  // slice k's buffer is refilled at iteration k+1
     }
     __syncthreads();
     // ---- V = G_a .* G_b (mode order), upper triangle into A
@@ -300,7 +327,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
         for (int q = 0; q < 4; ++q) {
           const int ll = l + q;
           const double w = (cs && vec[3 * Rm + ll] != 0.0) ? -((ll <= c) ? A[ll * ld + c] : A[c * ld + ll]) : 0.0;
-          const double mv = M[i * Rm + ll];
+          const double mv = M[i * lm + ll];
           if (q == 0) s0 = fma(mv, w, s0);
           else if (q == 1) s1 = fma(mv, w, s1);
           else if (q == 2) s2 = fma(mv, w, s2);
@@ -309,21 +336,21 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
       }
       for (; l < R; ++l) {
         const double w = (cs && vec[3 * Rm + l] != 0.0) ? -((l <= c) ? A[l * ld + c] : A[c * ld + l]) : 0.0;
-        s0 = fma(M[i * Rm + l], w, s0);
+        s0 = fma(M[i * lm + l], w, s0);
       }
-      X[i * Rm + c] = (s0 + s1) + (s2 + s3);
+      X[i * lm + c] = (s0 + s1) + (s2 + s3);
     }
     __syncthreads();
     // ---- <T, X> on the last mode (fit_check.jl:28)
     if (n == 2) {
       double p = 0.0;
-      for (int e = tid; e < In * R; e += nt) p += M[(e / R) * Rm + e % R] * X[(e / R) * Rm + e % R];
+      for (int e = tid; e < In * R; e += nt) p += M[(e / R) * lm + e % R] * X[(e / R) * lm + e % R];
       inner = block_sum_d(p, red);
     }
     // ---- lambda = column norms, F_n = X / lambda (row_norm.jl:4-24)
     for (int r = warp; r < R; r += nt >> 5) {
       double s = 0.0;
-      for (int i = lane; i < In; i += 32) s = fma(X[i * Rm + r], X[i * Rm + r], s);
+      for (int i = lane; i < In; i += 32) s = fma(X[i * lm + r], X[i * lm + r], s);
       for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
       if (lane == 0) lam[r] = sqrt(s);
     }
@@ -332,8 +359,8 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
     for (int e = tid; e < In * R; e += nt) {
       const int i = e / R, r = e - i * R;
       // a column left at zero by a rank-deficient solve (basic solution) stays zero
-      const double f = (lam[r] > 0.0) ? X[i * Rm + r] / lam[r] : 0.0;
-      X[i * Rm + r] = f;
+      const double f = (lam[r] > 0.0) ? X[i * lm + r] / lam[r] : 0.0;
+      X[i * lm + r] = f;
       F0g[fo[n] + i + (int64_t)In * r] = f;
       Fn32[i * Rm + r] = (float)f;
     }
@@ -346,10 +373,10 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
       double s0 = 0.0, s1 = 0.0;
       int i = 0;
       for (; i + 1 < In; i += 2) {
-        s0 = fma(X[i * Rm + r], X[i * Rm + c], s0);
-        s1 = fma(X[(i + 1) * Rm + r], X[(i + 1) * Rm + c], s1);
+        s0 = fma(X[i * lm + r], X[i * lm + c], s0);
+        s1 = fma(X[(i + 1) * lm + r], X[(i + 1) * lm + c], s1);
       }
-      if (i < In) s0 = fma(X[i * Rm + r], X[i * Rm + c], s0);
+      if (i < In) s0 = fma(X[i * lm + r], X[i * lm + c], s0);
       Gn[r * R + c] = s0 + s1;
       Gn[c * R + r] = s0 + s1;
     }

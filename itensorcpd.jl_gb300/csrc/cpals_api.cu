@@ -28,8 +28,6 @@ struct cpals_ctx {
   void* dT_owned = nullptr;
   bool T_set = false, F_set = false;
   double* F[kMaxOrder] = {};
-  float* F32t[kMaxOrder] = {};
-  int64_t ld32[kMaxOrder] = {};
   float* F32r[kMaxOrder] = {};  // row-major FP32 copies (tensor-core path)
   int64_t rpad = 0;
   double* G[kMaxOrder] = {};
@@ -48,6 +46,7 @@ struct cpals_ctx {
   double* W = nullptr;
   SolveInfo* info = nullptr;
   double* gpart = nullptr;
+  double* rgpart = nullptr;  // the solve blocks' partial Grams (null: the tiled Gram kernel)
   unsigned* gcnt = nullptr;
   int gS2[kMaxOrder] = {};
   double* inner_rows = nullptr;
@@ -172,17 +171,23 @@ int enqueue_sweep(cpals_ctx* c) {
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->st, c->ev_side[n], 0));
     // factorize, MTTKRP, solve, gram+finalize, normalize (+ BF16 factor tiles)
     c->launches += 5 + factor_tile_launches(c, n);
+    double* rg = c->rgpart;  // Gram partials from the solve blocks, reduced by launch_gram_rows
     if (c->dt)
       CPALS_CUDA_TRY(launch_solve_rows(c->Mdt, 0, 1, In, R, c->work, c->U, c->piv, c->W, c->info, c->X,
-                                       last ? c->inner_rows : nullptr, c->chk, c->st));
+                                       last ? c->inner_rows : nullptr, c->chk, c->st, rg));
     else
       CPALS_CUDA_TRY(launch_solve_rows(c->part, c->part_f32, c->splits[n], In, R, c->work, c->U, c->piv, c->W,
-                                       c->info, c->X, last ? c->inner_rows : nullptr, c->chk, c->st));
-    CPALS_CUDA_TRY(launch_gram_finalize(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->lam, c->lam_inv,
-                                        c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st));
+                                       c->info, c->X, last ? c->inner_rows : nullptr, c->chk, c->st, rg));
+    if (rg)
+      CPALS_CUDA_TRY(launch_gram_rows(rg, solve_blocks(In, R), R, c->gcnt + gram_tiles(R), c->Graw, c->lam,
+                                      c->lam_inv, c->G[n], gs, N, last, c->inner_rows, In, c->chk, c->traj,
+                                      c->traj_cap, c->st));
+    else
+      CPALS_CUDA_TRY(launch_gram_finalize(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->lam, c->lam_inv,
+                                          c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
-    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32t[n], c->ld32[n], c->F32r[n], c->rpad,
+    CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32r[n], c->rpad,
                                     c->Graw, c->G[n], last ? nullptr : c->chk, c->st));
     CPALS_CUDA_TRY(update_factor_tiles(c, n, last ? nullptr : c->chk));
   }
@@ -331,7 +336,6 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->Mdt);
   for (int m = 0; m < kMaxOrder; ++m) {
     cudaFree(c->F[m]);
-    cudaFree(c->F32t[m]);
     cudaFree(c->F32r[m]);
     cudaFree(c->G[m]);
     if (c->ev_main[m]) cudaEventDestroy(c->ev_main[m]);
@@ -349,6 +353,7 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->W);
   cudaFree(c->info);
   cudaFree(c->gpart);
+  cudaFree(c->rgpart);
   cudaFree(c->gcnt);
   cudaFree(c->inner_rows);
   cudaFree(c->chk);
@@ -449,10 +454,7 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
     }
     part_elems = std::max(part_elems, (size_t)c->splits[m] * dims[m] * R);
     c->gS2[m] = gram_splits(dims[m], (int)R, c->num_sms);
-    c->ld32[m] = c->tc ? tc_factor_ld(c->tc, m) : c->dt ? dt_factor_ld(c->dt, m) : dims[m];
     CK(dmalloc(&c->F[m], (size_t)dims[m] * R));
-    CK(dmalloc(&c->F32t[m], (size_t)c->ld32[m] * R));
-    CPALS_CUDA_TRY(cudaMemset(c->F32t[m], 0, sizeof(float) * c->ld32[m] * R));
     if (c->tc || (c->dt && mttkrp_mode == CPALS_MTTKRP_BF16X3)) {
       c->rpad = c->tc ? tc_factor_rpad(c->tc) : dt_factor_rpad(c->dt);
       CK(dmalloc(&c->F32r[m], (size_t)dims[m] * c->rpad));
@@ -485,6 +487,13 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   CK(dmalloc(&c->info, 1));
   CK(dmalloc(&c->gpart, (size_t)gram_tiles((int)R) * (maxS2 * 256 + 1)));
   CK(dmalloc(&c->gcnt, gram_tiles((int)R) + 1));
+  {
+    // partial Grams of the solve blocks, when they stay small (16M doubles)
+    const size_t T = (size_t)R * (R + 1) / 2;
+    size_t need = 0;
+    for (int m = 0; m < order; ++m) need = std::max(need, (size_t)solve_blocks(dims[m], (int)R) * T + (T + 31) / 32);
+    if (need <= (size_t(1) << 24)) CK(dmalloc(&c->rgpart, need));
+  }
   CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * (gram_tiles((int)R) + 1)));
   CK(dmalloc(&c->inner_rows, maxI));
   CK(dmalloc(&c->chk, 1));
@@ -552,7 +561,7 @@ int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const dou
     tmp.resize((size_t)c->dims[m] * R);
     colmajor_to_rowmajor_host(host_factors[m], c->dims[m], R, tmp.data());
     CPALS_CUDA_TRY(cudaMemcpyAsync(c->F[m], tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c->st));
-    CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32t[m], c->ld32[m], c->F32r[m],
+    CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32r[m],
                                     c->rpad, nullptr, nullptr, nullptr, c->st));
     CPALS_CUDA_TRY(update_factor_tiles(c, m, nullptr));
     CPALS_CUDA_TRY(launch_gram(c->F[m], c->dims[m], R, c->gS2[m], c->gpart, c->gcnt, c->G[m], nullptr, c->st));
@@ -850,7 +859,7 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
   const GramSet gs = gram_set(c);
   CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->lam_inv, c->G[mode], gs, c->order, 0, nullptr, In, nullptr,
                                  c->traj, c->traj_cap, c->st));
-  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[mode], c->F32t[mode], c->ld32[mode], c->F32r[mode],
+  CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[mode], c->F32r[mode],
                                   c->rpad, nullptr, nullptr, nullptr, c->st));
   CPALS_CUDA_TRY(update_factor_tiles(c, mode, nullptr));
   return check_derr(c);

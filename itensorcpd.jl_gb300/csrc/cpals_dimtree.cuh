@@ -15,8 +15,6 @@ int dt_set_tensor(DimTree* d, const void* T, cudaStream_t st);
 int* dt_error_flag(DimTree* d, int which);
 // Column count of the row-major FP32 factor copies (tensor-core path; 0 otherwise).
 int64_t dt_factor_rpad(const DimTree* d);
-// Leading dimension of the FP32 column-major factor copies.
-int64_t dt_factor_ld(const DimTree* d, int m);
 // Register the row-major FP32 factor copies of the four modes (tensor-core path).
 int dt_bind_factors(DimTree* d, const float* const* F32r);
 // Rebuild the BF16 factor tiles that mode m's new factor feeds (modes 0 and 2).

@@ -103,9 +103,19 @@ size_t factorize_work_doubles(int R);
 
 // Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and
 // (optionally) per-row sums of M .* X for the fit.  `work` is the factorize workspace.
+// With gram_part, every block also writes its rows' share of G = X^T X (upper triangle,
+// R(R+1)/2 doubles per block, solve_blocks(In, R) blocks) for launch_gram_rows.
 cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
                               const double* U, const int* piv, const double* W, const SolveInfo* info, double* X,
-                              double* inner_rows, const DevCheck* chk, cudaStream_t st);
+                              double* inner_rows, const DevCheck* chk, cudaStream_t st, double* gram_part = nullptr);
+int solve_blocks(int64_t In, int R);
+// G (Graw) from the solve blocks' partial Grams, then launch_finalize's work in the last
+// block (without G_n, which launch_normalize writes); gram_part needs room for
+// nblk * R(R+1)/2 + (R(R+1)/2 + 31)/32 doubles; counter: one zeroed unsigned.
+cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned* counter, double* Graw, double* lam,
+                             double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
+                             const double* inner_rows, int64_t In, DevCheck* chk, double* traj, int64_t traj_cap,
+                             cudaStream_t st);
 
 // G = X^T X (row-major X, In x R) over S2 row splits; part: gram_tiles(R)*S2*256 doubles,
 // counters: gram_tiles(R)+1 zero-initialised unsigneds (left zeroed after each launch).
@@ -128,12 +138,11 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st);
 
-// F = X .* (1 ./ lambda) (lam_inv may be null: plain copy), an FP32 column-major copy
-// [R][ld32], (when F32r is non-null) an FP32 row-major copy [In][rpad] and (when Gn is
-// non-null) the normalised Gram Gn = Graw ./ (lambda lambda^T).
-cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32t,
-                             int64_t ld32, float* F32r, int64_t rpad, const double* Graw, double* Gn,
-                             const DevCheck* chk, cudaStream_t st);
+// F = X .* (1 ./ lambda) (lam_inv may be null: plain copy), (when F32r is non-null) an
+// FP32 row-major copy [In][rpad] and (when Gn is non-null) the normalised Gram
+// Gn = Graw ./ (lambda lambda^T).
+cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
+                             int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st);
 
 // Row-major rows x cols -> row-major cols x rows (FP64).
 cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);

@@ -15,8 +15,6 @@ void tc_destroy(TcState* s);
 int tc_set_tensor(TcState* s, const void* T, cudaStream_t st);
 // Split-K slices of mode n (partials are float [splits][I_n][R]).
 int tc_splits(const TcState* s, int n);
-// Leading dimension (>= I_m, zero padded) of the FP32 column-major factor copies.
-int64_t tc_factor_ld(const TcState* s, int m);
 // Device error word of the tensor-core kernel (0 = ok; non-zero = a bounded wait expired).
 int* tc_error_flag(TcState* s);
 // Column count (>= R, zero padded) of the row-major FP32 factor copies.

@@ -162,7 +162,6 @@ int* dt_error_flag(DimTree* d, int which) {
 }
 
 int64_t dt_factor_rpad(const DimTree* d) { return d->tcA ? tc_factor_rpad(d->tcA) : 0; }
-int64_t dt_factor_ld(const DimTree* d, int m) { return d->tcA ? ((d->dims[m] + 63) / 64) * 64 : d->dims[m]; }
 
 int dt_bind_factors(DimTree* d, const float* const* F32r) {
   if (!d->tcA) return CPALS_OK;

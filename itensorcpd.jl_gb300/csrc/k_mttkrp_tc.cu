@@ -629,7 +629,6 @@ int tc_set_tensor(TcState* s, const void* T, cudaStream_t st) {
 }
 
 int tc_splits(const TcState* s, int n) { return s->plan[n].splits; }
-int64_t tc_factor_ld(const TcState* s, int m) { return round_up(s->dims[m], kChunk); }
 int* tc_error_flag(TcState* s) { return s->err; }
 
 cudaError_t tc_launch_mttkrp(TcState* s, int n, float* part, const DevCheck* chk, cudaStream_t st) {

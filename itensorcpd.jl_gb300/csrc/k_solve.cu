@@ -747,7 +747,8 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
                                                         const double* __restrict__ WT, double* __restrict__ X,
                                                         double* __restrict__ inner_rows, const DevCheck* chk,
                                                         const SolveInfo* __restrict__ info,
-                                                        const double* __restrict__ Vg) {
+                                                        const double* __restrict__ Vg,
+                                                        double* __restrict__ gpart) {
   if (done_flag(chk)) return;
   extern __shared__ double sm[];
   double* Ms = sm;            // RB x R
@@ -888,6 +889,7 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
       const double x = Xs[e] + (double)rowdot32(Fs + row * R, k);
       X[base + e] = x;
       Ps[e] = Ms[e] * x;
+      Xs[e] = x;  // (only this thread reads Xs[e] in this loop)
     }
   } else {
     for (int e = tid; e < nval; e += SOLVE_T) {
@@ -895,6 +897,33 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
       const double x = rowdot(Ms + row * R, W, k);
       X[base + e] = x;
       Ps[e] = Ms[e] * x;
+      Xs[e] = x;
+    }
+  }
+  if (gpart) {
+    // this block's share of G = X^T X: the upper triangle (rows paired: row p with row
+    // R-1-p, R+1 entries per pair), two accumulators over the block's rows
+    __syncthreads();
+    const int T = R * (R + 1) / 2;
+    double* gp = gpart + (size_t)blockIdx.x * T;
+    for (int e = tid; e < T; e += SOLVE_T) {
+      const int p = e / (R + 1), t = e - p * (R + 1);
+      int a, b;
+      if (t < R - p) {
+        a = p;
+        b = p + t;
+      } else {
+        a = R - 1 - p;
+        b = a + (t - (R - p));
+      }
+      double s0 = 0.0, s1 = 0.0;
+      int row = 0;
+      for (; row + 1 < rows; row += 2) {
+        s0 = fma(Xs[row * R + a], Xs[row * R + b], s0);
+        s1 = fma(Xs[(row + 1) * R + a], Xs[(row + 1) * R + b], s1);
+      }
+      if (row < rows) s0 = fma(Xs[row * R + a], Xs[row * R + b], s0);
+      gp[e] = s0 + s1;
     }
   }
   if (!inner_rows) return;
@@ -1187,6 +1216,66 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int6
   finalize_body(G, R, fa, true);
 }
 
+// G from the solve blocks' partial Grams: 32 upper-triangle entries per block, eight
+// slices of the partials per entry summed in block order and then across the slices in a
+// fixed order; the block's share of ||X||^2 goes to fa.fpart, and the last block to finish
+// runs finalize_body (lambda, fit, check).
+__global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gpart, int nblk, int R,
+                                                   double* __restrict__ G, unsigned* __restrict__ counter,
+                                                   const DevCheck* chk, FinalizeArgs fa) {
+  if (done_flag(chk)) return;
+  __shared__ double red[8][33];
+  __shared__ int s_last;
+  __shared__ double sv_t[32];
+  const int T = R * (R + 1) / 2;
+  const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
+  const int e = blockIdx.x * 32 + lane;
+  double a0 = 0.0, a1 = 0.0;
+  if (e < T) {
+    int b = sl;
+    for (; b + 8 < nblk; b += 16) {
+      a0 += gpart[(size_t)b * T + e];
+      a1 += gpart[(size_t)(b + 8) * T + e];
+    }
+    if (b < nblk) a0 += gpart[(size_t)b * T + e];
+  }
+  red[sl][lane] = a0 + a1;
+  __syncthreads();
+  double h = 0.0;
+  if (sl == 0 && e < T) {
+    double sum = 0.0;
+    for (int q = 0; q < 8; ++q) sum += red[q][lane];
+    const int p = e / (R + 1), t = e - p * (R + 1);
+    int a, c;
+    if (t < R - p) {
+      a = p;
+      c = p + t;
+    } else {
+      a = R - 1 - p;
+      c = a + (t - (R - p));
+    }
+    G[(size_t)a * R + c] = sum;
+    G[(size_t)c * R + a] = sum;
+    if (fa.last) {
+      h = (a == c) ? sum : 2.0 * sum;
+      for (int m = 0; m < fa.order; ++m)
+        if (m != fa.mode) h *= fa.gs.G[m][(size_t)a * R + c];
+    }
+  }
+  if (fa.last) {
+    const double tsum = block_tree_sum(h, sv_t);
+    if (threadIdx.x == 0) fa.fpart[blockIdx.x] = tsum;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) *counter = 0u;
+  finalize_body(G, R, fa, true);
+}
+
 __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Graw, int R, FinalizeArgs fa) {
   if (done_flag(fa.chk)) return;
   finalize_body(Graw, R, fa, false);
@@ -1194,7 +1283,7 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
 
 // ---------------- normalize ----------------
 __global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam_inv, int64_t In, int R,
-                            double* __restrict__ F, float* __restrict__ F32t, int64_t ld32, float* __restrict__ F32r,
+                            double* __restrict__ F, float* __restrict__ F32r,
                             int64_t rpad, const double* __restrict__ Graw, double* __restrict__ Gn,
                             const DevCheck* chk) {
   if (done_flag(chk)) return;
@@ -1205,7 +1294,6 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
     const int r = (int)(e % R);
     const double f = lam_inv ? X[e] * lam_inv[r] : X[e];
     F[e] = f;
-    if (F32t) F32t[(int64_t)r * ld32 + i] = (float)f;
     if (F32r) F32r[i * rpad + r] = (float)f;
   }
   // the normalised Gram G_n = Graw ./ (lambda lambda^T), by the reciprocals
@@ -1268,9 +1356,14 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
 
 static int solve_rows_per_block(int R) { return R >= 256 ? 1 : 256 / R; }
 
+int solve_blocks(int64_t In, int R) {
+  const int RB = solve_rows_per_block(R);
+  return (int)((In + RB - 1) / RB);
+}
+
 cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
                               const double* U, const int* piv, const double* W, const SolveInfo* info, double* X,
-                              double* inner_rows, const DevCheck* chk, cudaStream_t st) {
+                              double* inner_rows, const DevCheck* chk, cudaStream_t st, double* gram_part) {
   (void)U;
   (void)piv;
   const int RB = solve_rows_per_block(R);
@@ -1287,10 +1380,10 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
   }
   if (part_is_f32)
     k_solve_gemm<float><<<grid, SOLVE_T, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X,
-                                                     inner_rows, chk, info, work);
+                                                     inner_rows, chk, info, work, gram_part);
   else
     k_solve_gemm<double><<<grid, SOLVE_T, smem, st>>>(static_cast<const double*>(part), splits, In, R, RB, W, X,
-                                                      inner_rows, chk, info, work);
+                                                      inner_rows, chk, info, work, gram_part);
   return cudaGetLastError();
 }
 
@@ -1331,6 +1424,19 @@ cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, dou
   return cudaGetLastError();
 }
 
+cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned* counter, double* Graw, double* lam,
+                             double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
+                             const double* inner_rows, int64_t In, DevCheck* chk, double* traj, int64_t traj_cap,
+                             cudaStream_t st) {
+  const int T = R * (R + 1) / 2;
+  const int blocks = (T + 31) / 32;
+  // the blocks' shares of ||X||^2 follow the partial Grams
+  double* fpart = const_cast<double*>(gram_part) + (size_t)nblk * T;
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, fpart, blocks};
+  k_gram_rows<<<blocks, 256, 0, st>>>(gram_part, nblk, R, Graw, counter, chk, fa);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st) {
@@ -1339,12 +1445,12 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_
   return cudaGetLastError();
 }
 
-cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32t,
-                             int64_t ld32, float* F32r, int64_t rpad, const double* Graw, double* Gn,
+cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
+                             int64_t rpad, const double* Graw, double* Gn,
                              const DevCheck* chk, cudaStream_t st) {
   const int64_t n = In * R;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32t, ld32, F32r, rpad, Graw, Gn, chk);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32r, rpad, Graw, Gn, chk);
   return cudaGetLastError();
 }
 

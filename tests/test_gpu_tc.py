@@ -164,3 +164,55 @@ def test_bf16x3_final_fit_matches_fp64_at_512cube(built):
     d = abs(final["fp64"][0] - final["bf16x3"][0])
     print("512^3 converged: fp64", final["fp64"], "bf16x3", final["bf16x3"], "diff", d)
     assert d < 1e-6
+
+
+def _tracking(built, T, F, lam, R, sweeps):
+    nrm = float(np.linalg.norm(T.astype(np.float64)))
+    fits = {}
+    for prec in ("fp64", "bf16x3"):
+        with built.Engine(T.shape, R, dtype=np.float32, precision=prec) as eng:
+            eng.set_tensor(T)
+            eng.set_factors(F, lam)
+            fits[prec] = eng.optimize(built.api._to_device_check(built.FitCheck(0.0, sweeps, nrm)))
+    return fits
+
+
+def test_bf16x3_nearly_collinear_factors_fall_back_to_fp64_sweep(built, oracle):
+    # two components with column cosines 0.9999 in every mode: V's pivots fall far below
+    # 1e-3 of its diagonal, so the FP32 sweep hands over to the FP64 sweep.  The split-BF16
+    # MTTKRP's ~1e-7 relative error is amplified by kappa(V) (~1e4 here) in the solve,
+    # whatever its precision, so the fits agree to ~1e-4 rather than 1e-6
+    rng = np.random.default_rng(21)
+    dims, R = (48, 44, 40), 6
+    T, _, _ = oracle.lowrank_plus_noise(dims, R, 0.3, 30.0, rng)
+    F, lam = det_factors(dims, R, seed=22)
+    for f in F:
+        f[:, 1] = f[:, 0] + 0.014 * f[:, 1]
+        f /= np.linalg.norm(f, axis=0)
+    fits = _tracking(built, T, F, lam, R, 12)
+    assert np.all(np.isfinite(fits["bf16x3"]))
+    assert np.max(np.abs(fits["fp64"] - fits["bf16x3"])) < 1e-3
+
+
+def test_bf16x3_rank_above_128_tracks_fp64(built, oracle):
+    # R > 128: the FP32 sweep is not used (shared-memory limit); FP64 sweep on both engines
+    rng = np.random.default_rng(23)
+    dims, R = (150, 140, 36), 144
+    T, _, _ = oracle.lowrank_plus_noise(dims, 16, 0.2, 30.0, rng)
+    F, lam = det_factors(dims, R, seed=24)
+    fits = _tracking(built, T, F, lam, R, 4)
+    assert np.max(np.abs(fits["fp64"] - fits["bf16x3"])) < 1e-4
+
+
+def test_bf16x3_rank_deficient_normal_equations(built, oracle):
+    # repeated factor columns make V singular: FP32 sweep -> FP64 sweep -> pivoted-QR
+    # operator, as on the FP64 engine; both stay finite and agree
+    rng = np.random.default_rng(25)
+    dims, R = (30, 28, 26), 4
+    T, _, _ = oracle.lowrank_plus_noise(dims, R, 0.2, 30.0, rng)
+    F, lam = det_factors(dims, R, seed=26)
+    for f in F:
+        f[:, 3] = f[:, 2]
+    fits = _tracking(built, T, F, lam, R, 3)
+    assert np.all(np.isfinite(fits["bf16x3"])) and np.all(np.isfinite(fits["fp64"]))
+    assert np.max(np.abs(fits["fp64"] - fits["bf16x3"])) < 1e-3

@@ -128,11 +128,6 @@ cudaError_t update_factor_tiles(cpals_ctx* c, int m, const DevCheck* chk) {
   if (c->dt) return dt_update_factor(c->dt, m, c->F[m], chk, c->st);
   return cudaSuccess;
 }
-int factor_tile_launches(const cpals_ctx* c, int m) {
-  if (c->tc) return m <= 1 ? 1 : 0;
-  if (c->dt && c->mmode == CPALS_MTTKRP_BF16X3) return (m == 0 || m == 2) ? 1 : 0;
-  return 0;
-}
 
 cudaError_t enqueue_mttkrp(cpals_ctx* c, int n, const DevCheck* chk) {
   if (c->mmode == CPALS_MTTKRP_FP64)
@@ -169,8 +164,8 @@ int enqueue_sweep(cpals_ctx* c) {
       c->prof_used += 2;
     }
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->st, c->ev_side[n], 0));
-    // factorize, MTTKRP, solve, gram+finalize, normalize (+ BF16 factor tiles)
-    c->launches += 5 + factor_tile_launches(c, n);
+    // factorize, MTTKRP, solve, gram+finalize, normalize (which also writes the BF16 factor tiles)
+    c->launches += 5;
     double* rg = c->rgpart;  // Gram partials from the solve blocks, reduced by launch_gram_rows
     if (c->dt)
       CPALS_CUDA_TRY(launch_solve_rows(c->Mdt, 0, 1, In, R, c->work, c->U, c->piv, c->W, c->info, c->X,
@@ -187,9 +182,10 @@ int enqueue_sweep(cpals_ctx* c) {
                                           c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
+    // the BF16 factor tiles the tensor-core MTTKRP reads are written by the same kernel
+    const BtileDesc btd = c->tc ? tc_btile_desc(c->tc, n) : c->dt ? dt_btile_desc(c->dt, n) : BtileDesc{nullptr, 0, 0};
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32r[n], c->rpad,
-                                    c->Graw, c->G[n], last ? nullptr : c->chk, c->st));
-    CPALS_CUDA_TRY(update_factor_tiles(c, n, last ? nullptr : c->chk));
+                                    c->Graw, c->G[n], last ? nullptr : c->chk, c->st, btd));
   }
   return CPALS_OK;
 }

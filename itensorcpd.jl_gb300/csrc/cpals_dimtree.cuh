@@ -17,6 +17,8 @@ int* dt_error_flag(DimTree* d, int which);
 int64_t dt_factor_rpad(const DimTree* d);
 // Register the row-major FP32 factor copies of the four modes (tensor-core path).
 int dt_bind_factors(DimTree* d, const float* const* F32r);
+// Layout of the BF16 factor tiles mode m's new factor feeds (modes 0 and 2; else bt null).
+BtileDesc dt_btile_desc(const DimTree* d, int m);
 // Rebuild the BF16 factor tiles that mode m's new factor feeds (modes 0 and 2).
 cudaError_t dt_update_factor(DimTree* d, int m, const double* F, const DevCheck* chk, cudaStream_t st);
 // M_n (FP64 row-major [I_n][R]) from the FP64 row-major factors F.  Modes 0 and 2 (and 1,

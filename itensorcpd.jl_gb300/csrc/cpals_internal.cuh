@@ -138,11 +138,21 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st);
 
+// Where the tensor-core MTTKRP keeps the BF16 hi/lo tiles of a factor that is its fastest
+// reduction mode: tiles of nb columns x 64 rows, hi plane then lo plane, 128-byte rows
+// swizzled in 16-byte chunks (chunk c of row r at (c ^ (r & 7)) * 16).
+struct BtileDesc {
+  uint8_t* bt;   // null: no tiles
+  int nb;        // columns per tile
+  int n_blocks;  // column tiles
+};
+
 // F = X .* (1 ./ lambda) (lam_inv may be null: plain copy), (when F32r is non-null) an
-// FP32 row-major copy [In][rpad] and (when Gn is non-null) the normalised Gram
-// Gn = Graw ./ (lambda lambda^T).
+// FP32 row-major copy [In][rpad], (when Gn is non-null) the normalised Gram
+// Gn = Graw ./ (lambda lambda^T) and (when bt.bt is non-null) the BF16 factor tiles.
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
-                             int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st);
+                             int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st,
+                             BtileDesc bt = BtileDesc{nullptr, 0, 0});
 
 // Row-major rows x cols -> row-major cols x rows (FP64).
 cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);

@@ -25,6 +25,9 @@ int tc_bind_factors(TcState* s, const float* const* F32r);
 // Rebuild the BF16 hi/lo factor-block tiles of mode m (a no-op unless m is 0 or 1) from the FP64
 // row-major factor; skipped when the device check is done.
 cudaError_t tc_update_factor(TcState* s, int m, const double* F, const DevCheck* chk, cudaStream_t st);
+// Layout of mode m's BF16 factor tiles (bt null unless m is a planned fastest reduction
+// mode), for a kernel that writes them while it writes the factor.
+BtileDesc tc_btile_desc(const TcState* s, int m);
 // Launch the MTTKRP of mode n with the bound factor copies.
 cudaError_t tc_launch_mttkrp(TcState* s, int n, float* part, const DevCheck* chk, cudaStream_t st);
 

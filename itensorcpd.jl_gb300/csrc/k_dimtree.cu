@@ -181,6 +181,13 @@ cudaError_t dt_update_factor(DimTree* d, int m, const double* F, const DevCheck*
   return cudaSuccess;
 }
 
+BtileDesc dt_btile_desc(const DimTree* d, int m) {
+  if (!d->tcA) return BtileDesc{nullptr, 0, 0};
+  if (m == 2) return tc_btile_desc(d->tcA, 1);
+  if (m == 0) return tc_btile_desc(d->tcB, 0);
+  return BtileDesc{nullptr, 0, 0};
+}
+
 int dt_launches(const DimTree* d, int n, bool reuse) {
   (void)d;
   const bool full = (n == 0 || n == 2) || !reuse;

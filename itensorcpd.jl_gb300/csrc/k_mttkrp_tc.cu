@@ -595,6 +595,12 @@ int tc_bind_factors(TcState* s, const float* const* F32r) {
   return CPALS_OK;
 }
 
+BtileDesc tc_btile_desc(const TcState* s, int m) {
+  if (m > 1 || !s->btiles[m]) return BtileDesc{nullptr, 0, 0};
+  const TcModePlan& p = s->plan[s->plan[0].m_blocks ? 0 : (s->plan[1].m_blocks ? 1 : 2)];
+  return BtileDesc{s->btiles[m], p.nb, p.n_blocks};
+}
+
 cudaError_t tc_update_factor(TcState* s, int m, const double* F, const DevCheck* chk, cudaStream_t st) {
   if (m > 1 || !s->btiles[m]) return cudaSuccess;  // only planned fastest reduction modes feed the tensor core
   const TcModePlan& p = s->plan[s->plan[0].m_blocks ? 0 : (s->plan[1].m_blocks ? 1 : 2)];

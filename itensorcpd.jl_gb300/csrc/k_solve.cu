@@ -17,6 +17,8 @@
 // FP64 runs at 2 FMA/clk/SM on GB300, so every O(I_n R^2) piece is spread over many
 // CTAs; only the O(R^3) factorisation is a single CTA, and it runs on a side stream
 // concurrently with the MTTKRP of the same mode.
+#include <cuda_bf16.h>
+
 #include <climits>
 #include <cmath>
 
@@ -1285,7 +1287,7 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
 __global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam_inv, int64_t In, int R,
                             double* __restrict__ F, float* __restrict__ F32r,
                             int64_t rpad, const double* __restrict__ Graw, double* __restrict__ Gn,
-                            const DevCheck* chk) {
+                            const DevCheck* chk, BtileDesc btd) {
   if (done_flag(chk)) return;
   const int64_t n = In * R;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -1295,6 +1297,18 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
     const double f = lam_inv ? X[e] * lam_inv[r] : X[e];
     F[e] = f;
     if (F32r) F32r[i * rpad + r] = (float)f;
+    if (btd.bt) {
+      // hi = bf16(f), lo = bf16(f - hi), at row i of column r in its tile
+      const __nv_bfloat16 h = __double2bfloat16(f);
+      const __nv_bfloat16 l = __double2bfloat16(f - (double)__bfloat162float(h));
+      const int nblk = r / btd.nb, rr = r - nblk * btd.nb;
+      const int64_t fb = i >> 6;
+      const int kk = (int)(i & 63);
+      uint8_t* tile = btd.bt + (size_t)(fb * btd.n_blocks + nblk) * (2 * (size_t)btd.nb * 64 * 2);
+      const uint32_t off = (uint32_t)rr * 128u + ((uint32_t)((kk >> 3) ^ (rr & 7)) << 4) + (uint32_t)(kk & 7) * 2u;
+      *reinterpret_cast<__nv_bfloat16*>(tile + off) = h;
+      *reinterpret_cast<__nv_bfloat16*>(tile + (size_t)btd.nb * 64 * 2 + off) = l;
+    }
   }
   // the normalised Gram G_n = Graw ./ (lambda lambda^T), by the reciprocals
   if (Gn)
@@ -1446,11 +1460,11 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_
 }
 
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
-                             int64_t rpad, const double* Graw, double* Gn,
-                             const DevCheck* chk, cudaStream_t st) {
+                             int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st,
+                             BtileDesc bt) {
   const int64_t n = In * R;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32r, rpad, Graw, Gn, chk);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32r, rpad, Graw, Gn, chk, bt);
   return cudaGetLastError();
 }
 

@@ -43,8 +43,13 @@ namespace {
 
 constexpr int kChunk = 64;     // K values per stage (one 128-byte swizzle row of BF16)
 constexpr int kBlockM = 128;   // rows per CTA (one UMMA M)
-constexpr int kThreads = 192;  // 6 warps
-constexpr int kDrainWarps = 4;
+// Drain warps: one per TMEM lane quarter, or two (each taking half of the columns) when
+// the N block is a multiple of 64 wide, which halves the per-chunk drain latency and the
+// accumulator registers of the wide blocks.  Warps 0 and 1 produce and issue the MMAs.
+template <int NB>
+__host__ __device__ constexpr int tc_drain_warps() { return (NB % 64 == 0) ? 8 : 4; }
+template <int NB>
+__host__ __device__ constexpr int tc_threads() { return 64 + 32 * tc_drain_warps<NB>(); }
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kSmemLimit = 227 * 1024;
 
@@ -158,7 +163,7 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b, float* ra, flo
 
 // ---------------------------------------------------------------- the kernel
 template <int NBT>  // N-block width (a multiple of 16, at most 128): loops unroll exactly this far
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(tc_threads<NBT>(), 1)
     k_mttkrp_tc(const uint8_t* __restrict__ tiles, const uint8_t* __restrict__ btiles, TcModePlan p,
                 FactorPtrs32 fr, int R, float* __restrict__ part, const DevCheck* __restrict__ chk,
                 int* __restrict__ err) {
@@ -198,11 +203,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(smem_u32(&full_a[s]), 1);
-      mbar_init(smem_u32(&empty[s]), kDrainWarps);
+      mbar_init(smem_u32(&empty[s]), tc_drain_warps<NB>());
     }
     for (int b = 0; b < kBuf; ++b) {
       mbar_init(smem_u32(&acc_full[b]), 1);
-      mbar_init(smem_u32(&acc_empty[b]), kDrainWarps);
+      mbar_init(smem_u32(&acc_empty[b]), tc_drain_warps<NB>());
     }
     mbar_init(smem_u32(done_bar), 1);
     *abort_flag = 0;
@@ -290,13 +295,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       umma_commit(smem_u32(done_bar));
     }
   } else {
-    // ---------------- drainers (warps 2..5): per chunk, acc[r] += s(r) * (Th Kh + cross terms),
-    // promoted from TMEM into FP32 registers with round-to-nearest adds
+    // ---------------- drainers (warps 2..): per chunk, acc[r] += s(r) * (Th Kh + cross terms),
+    // promoted from TMEM into FP32 registers with round-to-nearest adds.  Warp w reads TMEM
+    // lane quarter w % 4 and, with two warps per quarter, half of the columns.
+    constexpr int NH = NB * 4 / tc_drain_warps<NB>();  // columns of this warp
     const int q = warp & 3;  // this warp's TMEM lane quarter
+    const int cb = ((warp - 2) >> 2) * NH;  // first column of this warp
     const int64_t row = (int64_t)mblk * kBlockM + q * 32 + lane;
-    float acc[NB];
+    float acc[NH];
 #pragma unroll
-    for (int j = 0; j < NB; ++j) acc[j] = 0.0f;
+    for (int j = 0; j < NH; ++j) acc[j] = 0.0f;
     bool ok = true;
     for (int it = 0; it < nloc && ok; ++it) {
       const int s = it % S;
@@ -314,13 +322,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         break;
       }
       tc_fence_after();
-      const float* orow = reinterpret_cast<const float*>(smem + (size_t)s * stage_bytes + 2 * a_bytes + 2 * b_bytes);
-      const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB);
+      const float* orow =
+          reinterpret_cast<const float*>(smem + (size_t)s * stage_bytes + 2 * a_bytes + 2 * b_bytes) + cb;
+      const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
+      // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
+      // budget is smaller: 320 threads)
+      constexpr int W = (tc_drain_warps<NB>() == 8) ? 16 : 32;
 #pragma unroll
-      for (int c0 = 0; c0 < NB; c0 += 32) {
-        constexpr int W = 32;
+      for (int c0 = 0; c0 < NH; c0 += W) {
         uint32_t vh[W], vl[W];
-        const bool full = (c0 + 32 <= NB);
+        const bool full = (W == 32) && (c0 + 32 <= NH);
         if (full) {
           tmem_ld32_nowait(base + (uint32_t)c0, vh);
           tmem_ld32_nowait(base + (uint32_t)(NB + c0), vl);
@@ -334,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int jo = 0; jo < p.n_outer; ++jo) {
 #pragma unroll
           for (int j = 0; j < W; j += 4) {
-            if (c0 + j < NB) {
+            if (c0 + j < NH) {
               const float4 o4 = *reinterpret_cast<const float4*>(orow + jo * NB + c0 + j);
               sc[j] *= o4.x;
               sc[j + 1] *= o4.y;
@@ -346,7 +357,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < W; ++j)
-          if (c0 + j < NB)
+          if (c0 + j < NH)
             acc[c0 + j] = fmaf(sc[j], __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
       }
       tc_fence_before();
@@ -363,10 +374,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       ok = got != 0;
     }
     if (row < p.In && (ok || nloc == 0)) {
-      float* out = part + ((int64_t)split * p.In + row) * R + n0;
+      float* out = part + ((int64_t)split * p.In + row) * R + n0 + cb;
 #pragma unroll
-      for (int j = 0; j < NB; ++j)
-        if (n0 + j < R) out[j] = acc[j];
+      for (int j = 0; j < NH; ++j)
+        if (n0 + cb + j < R) out[j] = acc[j];
     }
   }
   tc_fence_before();
@@ -647,7 +658,8 @@ cudaError_t tc_launch_mttkrp(TcState* s, int n, float* part, const DevCheck* chk
   switch (p.nb) {
 #define CPALS_TC_CASE(W)                                                                                           \
   case W:                                                                                                          \
-    k_mttkrp_tc<W><<<grid, kThreads, s->smem_bytes[n], st>>>(s->tiles[n], s->btiles[p.fmode], p, fr, (int)s->R, \
+    k_mttkrp_tc<W><<<grid, tc_threads<W>(), s->smem_bytes[n], st>>>(s->tiles[n], s->btiles[p.fmode], p, fr,       \
+                                                                    (int)s->R,                                  \
                                                             part, chk, s->err);                                   \
     break;
     CPALS_TC_CASE(16)

@@ -9,6 +9,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "cpals_internal.cuh"
@@ -78,6 +80,19 @@ struct cpals_ctx {
   int64_t launches = 0;
   int64_t sweep_launches = 0;  // kernel launches of one sweep (set when the graph is built)
 };
+
+cudaError_t set_smem_limit_once(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({dev, kernel})) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.insert({dev, kernel});
+  return e;
+}
 
 namespace {
 

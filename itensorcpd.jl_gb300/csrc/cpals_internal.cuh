@@ -170,6 +170,11 @@ cudaError_t launch_colmajor_to_rowmajor(const double* src, int64_t rows, int R, 
 cudaError_t launch_leverage_rows(const double* F, int64_t In, int R, const double* work, const double* U,
                                  const int* piv, const SolveInfo* info, double scale, double* probs, cudaStream_t st);
 
+// Raises a kernel's dynamic shared-memory limit on the current device, once per (device,
+// kernel) per process (thread-safe).  The attribute is per device, so a process that drives
+// several GPUs sets it on each.
+cudaError_t set_smem_limit_once(const void* kernel, int bytes);
+
 }  // namespace cpals
 
 #define CPALS_CUDA_TRY(expr)                                                            \

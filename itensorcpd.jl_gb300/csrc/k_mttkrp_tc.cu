@@ -586,14 +586,14 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     }
     cudaMemset(s->btiles[f], 0, s->btile_bytes[f]);
   }
-  cudaFuncSetAttribute(k_mttkrp_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<80>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<96>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<112>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  cudaFuncSetAttribute(k_mttkrp_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  const void* kernels[8] = {(const void*)k_mttkrp_tc<16>, (const void*)k_mttkrp_tc<32>, (const void*)k_mttkrp_tc<48>,
+                            (const void*)k_mttkrp_tc<64>, (const void*)k_mttkrp_tc<80>, (const void*)k_mttkrp_tc<96>,
+                            (const void*)k_mttkrp_tc<112>, (const void*)k_mttkrp_tc<128>};
+  for (const void* k : kernels)
+    if (set_smem_limit_once(k, (int)kSmemLimit) != cudaSuccess) {
+      tc_destroy(s);
+      return CPALS_E_CUDA;
+    }
   *out = s;
   return CPALS_OK;
 }

@@ -1352,12 +1352,9 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   double* dinv = work + (size_t)R * R;
   double* qwork = dinv + R;
   const size_t smem = (R <= 128) ? (size_t)R * (R | 1) * sizeof(double) : 0;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_factorize, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_factorize32, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 129 * 4);
-    attr_set = true;
-  }
+  cudaError_t ea = set_smem_limit_once((const void*)k_factorize, 200 * 1024);
+  if (ea == cudaSuccess) ea = set_smem_limit_once((const void*)k_factorize32, 128 * 129 * 4);
+  if (ea != cudaSuccess) return ea;
   mixed = (mixed && R <= 128) ? 1 : 0;
   if (mixed) {
     k_factorize32<<<1, FT32, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, Aglob, W, info, chk);
@@ -1385,12 +1382,11 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
   // M, products, X0 (doubles), M / residual (floats), then W (FP64, or FP32 + V in FP64)
   size_t smem = (size_t)3 * RB * R * sizeof(double) + (size_t)((RB * R + 1) / 2) * sizeof(double);
   if (R <= kSolveStageMaxR) smem += (size_t)((R * R + 1) / 2 + R * R) * sizeof(double);
-  static bool attr_set = false;
-  if (!attr_set) {
+  {
     const int mx = 3 * 256 * 8 + 128 * 8 + (kSolveStageMaxR * kSolveStageMaxR / 2 + kSolveStageMaxR * kSolveStageMaxR) * 8;
-    cudaFuncSetAttribute(k_solve_gemm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_solve_gemm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    attr_set = true;
+    cudaError_t ea = set_smem_limit_once((const void*)k_solve_gemm<float>, mx);
+    if (ea == cudaSuccess) ea = set_smem_limit_once((const void*)k_solve_gemm<double>, mx);
+    if (ea != cudaSuccess) return ea;
   }
   if (part_is_f32)
     k_solve_gemm<float><<<grid, SOLVE_T, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X,

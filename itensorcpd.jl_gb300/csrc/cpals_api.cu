@@ -81,7 +81,7 @@ struct cpals_ctx {
   int64_t sweep_launches = 0;  // kernel launches of one sweep (set when the graph is built)
 };
 
-cudaError_t set_smem_limit_once(const void* kernel, int bytes) {
+cudaError_t cpals::set_smem_limit_once(const void* kernel, int bytes) {
   static std::mutex mu;
   static std::set<std::pair<int, const void*>> done;
   int dev = 0;

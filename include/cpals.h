@@ -54,25 +54,33 @@ extern "C" {
 /* ---- convergence checks ---- */
 #define CPALS_CHECK_NONE 0 /* NoCheck, src/converge_checks/no_check.jl:1-20 */
 #define CPALS_CHECK_FIT 1  /* FitCheck, src/converge_checks/fit_check.jl:5-68 */
+#define CPALS_CHECK_DIFF 2 /* CPDiffCheck, src/converge_checks/cp_diff_check.jl:6-68 */
+#define CPALS_CHECK_ANGLE 3 /* CPAngleCheck, src/converge_checks/cp_angle_check.jl:6-68 */
 
 #define CPALS_MAX_ORDER 8
 
 typedef struct cpals_ctx cpals_ctx;
 
-/* Mirror of the mutable FitCheck / NoCheck structs (fit_check.jl:5-20, no_check.jl:1-9).
- * cpals_optimize reads it on entry and writes the updated fields back, so a
- * check object can be reused across calls as in the reference. */
+/* Mirror of the mutable check structs (fit_check.jl:5-20, no_check.jl:1-9,
+ * cp_diff_check.jl:6-18, cp_angle_check.jl:6-18).  cpals_optimize reads it on entry and
+ * writes the updated fields back, so a check object can be reused across calls as in the
+ * reference.  The previous iterate that CPDiffCheck / CPAngleCheck keep (PrevCP) stays
+ * on the device, in the handle; `has_prev` says whether it is set (PrevCP !== nothing),
+ * and cpals_get_prev / cpals_set_prev move it between handles. */
 typedef struct cpals_check {
-  int32_t kind;        /* CPALS_CHECK_NONE or CPALS_CHECK_FIT */
+  int32_t kind;        /* CPALS_CHECK_NONE, _FIT, _DIFF or _ANGLE */
   int32_t iter;        /* in/out */
-  int32_t counter;     /* in/out (FitCheck) */
+  int32_t counter;     /* in/out (FitCheck, CPDiffCheck, CPAngleCheck) */
   int32_t max_counter; /* sweeps allowed */
-  double tolerance;    /* FitCheck tol on |delta fit| */
+  double tolerance;    /* tol on |delta fit| (|delta angle| for CPAngleCheck) */
   double ref_norm;     /* FitCheck norm(T) */
-  double lastfit;      /* in/out; a new FitCheck starts at 1 */
+  double lastfit;      /* in/out; starts at 1 (CPAngleCheck: lastangle) */
   double final_fit;    /* out */
   int32_t total_iter;  /* out */
   int32_t sweeps_run;  /* out: sweeps executed by this call */
+  double norm_prev;    /* in/out: norm_prev_iter (CPDiffCheck ||prev||^2, CPAngleCheck ||prev||) */
+  int32_t has_prev;    /* in/out: 1 when the handle holds the previous iterate */
+  int32_t reserved;
 } cpals_check;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -109,9 +117,24 @@ int cpals_mttkrp(cpals_ctx* ctx, int mode, double* host_out);
 /* Run ALS sweeps with the given check: the loop of optimize
  * (src/optimizers/als_optimizers/optimize.jl:6-35) with compute_krp, solve_ls_problem,
  * row_norm, post_solve and check_converge on the device.  `fit_trajectory`
- * (may be NULL) receives one fit per sweep run, up to `traj_capacity` entries.
- * Returns CPALS_E_NAN if the fit became NaN. */
+ * (may be NULL) receives one fit per sweep run, up to `traj_capacity` entries:
+ * for CPDiffCheck the fit between consecutive iterates, for CPAngleCheck their angle,
+ * NaN for a sweep whose check only stored the iterate (PrevCP was nothing).
+ * Returns CPALS_E_NAN if a FitCheck fit became NaN (fit_check.jl:41). */
 int cpals_optimize(cpals_ctx* ctx, cpals_check* check, double* fit_trajectory, int64_t traj_capacity);
+
+/* One check_converge call of a CPDiffCheck / CPAngleCheck on the handle's current
+ * factors and lambda (cp_diff_check.jl:20-68, cp_angle_check.jl:20-68), for loops that
+ * update the factors themselves, such as the sampled solvers' loop
+ * (ProjectionAlgorithm.jl:15-54 passes these checks through).  *converged receives the
+ * check's return value and *value (may be NULL) the fit (angle) it computed, NaN when
+ * it only stored the iterate. */
+int cpals_check_converge(cpals_ctx* ctx, cpals_check* check, int* converged, double* value);
+/* The previous iterate held for CPDiffCheck / CPAngleCheck (PrevCP): factors I_n x R
+ * column-major and lambda.  get returns CPALS_E_STATE when none is held; set makes the
+ * handle hold the given one. */
+int cpals_get_prev(cpals_ctx* ctx, double* const* host_factors, double* host_lambda);
+int cpals_set_prev(cpals_ctx* ctx, const double* const* host_factors, const double* host_lambda);
 
 /* Number of normal-equation solves so far that took the pivoted-QR fallback
  * because the pivoted Cholesky was rank deficient (ldiv_solve.jl:17-22). */

@@ -2,12 +2,15 @@
 
 The compute path is libcpals.so (hand-written CUDA for sm_103a, C ABI in
 include/cpals.h); this package is the host side that mirrors the reference's
-``decompose`` / ``random_CPD`` / ``als_optimize`` / ``FitCheck`` / ``CPD`` interface.
+``decompose`` / ``random_CPD`` / ``als_optimize`` / ``FitCheck`` / ``CPDiffCheck`` /
+``CPAngleCheck`` / ``CPD`` interface.
 """
 from ._lib import CpalsError, load
 from .api import (
     CPD,
+    CPAngleCheck,
     CPDFit,
+    CPDiffCheck,
     ConvergeAlg,
     FitCheck,
     GB300Normal,
@@ -31,7 +34,7 @@ from . import warmstart
 from .warmstart import WarmStartMLP
 
 __all__ = [
-    "BatchEngine", "CPD", "CPDFit", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
+    "BatchEngine", "CPAngleCheck", "CPD", "CPDFit", "CPDiffCheck", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
     "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
     "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "WarmStartMLP", "warmstart",
 ]

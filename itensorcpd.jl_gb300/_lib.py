@@ -24,6 +24,8 @@ FLAG_NO_GRAPH = 1
 FLAG_DIMTREE = 2
 CHECK_NONE = 0
 CHECK_FIT = 1
+CHECK_DIFF = 2
+CHECK_ANGLE = 3
 
 
 class CpalsCheck(C.Structure):
@@ -40,6 +42,9 @@ class CpalsCheck(C.Structure):
         ("final_fit", C.c_double),
         ("total_iter", C.c_int32),
         ("sweeps_run", C.c_int32),
+        ("norm_prev", C.c_double),
+        ("has_prev", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -60,6 +65,9 @@ SIGNATURES = {
     "cpals_get_gram": (C.c_int, [_P, C.c_int, _DP]),
     "cpals_mttkrp": (C.c_int, [_P, C.c_int, _DP]),
     "cpals_optimize": (C.c_int, [_P, C.POINTER(CpalsCheck), _DP, C.c_int64]),
+    "cpals_check_converge": (C.c_int, [_P, C.POINTER(CpalsCheck), C.POINTER(C.c_int), _DP]),
+    "cpals_get_prev": (C.c_int, [_P, C.POINTER(_DP), _DP]),
+    "cpals_set_prev": (C.c_int, [_P, C.POINTER(_DP), _DP]),
     "cpals_fallback_count": (C.c_int, [_P, _I64P]),
     "cpals_synchronize": (C.c_int, [_P]),
     "cpals_timer_start": (C.c_int, [_P]),

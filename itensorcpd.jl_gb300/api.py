@@ -96,8 +96,44 @@ class NoCheck(ConvergeAlg):
     lastfit: float = -1.0
 
 
-def CPDFit(check: FitCheck) -> float:  # noqa: N802 - reference name
-    """fit_check.jl:68."""
+@dataclass
+class CPDiffCheck(ConvergeAlg):
+    """cp_diff_check.jl:6-18: the fit between consecutive iterates,
+    1 - ||T_n - T_{n-1}|| / ||T_{n-1}||, must change by less than ``tolerance`` on two
+    consecutive sweeps.  ``PrevCP`` is the previous iterate (a CPD) or None; the engine
+    keeps it on the device while it runs."""
+
+    tolerance: float
+    max_counter: int
+    iter: int = 0
+    counter: int = 0
+    norm_prev_iter: float = 0.0
+    PrevCP: object = None
+    lastfit: float = 1.0
+    final_fit: float = 0.0
+    total_iter: int = 0
+    trajectory: list = field(default_factory=list)
+
+
+@dataclass
+class CPAngleCheck(ConvergeAlg):
+    """cp_angle_check.jl:6-18: the angle acos(<T_n, T_{n-1}> / (||T_n|| ||T_{n-1}||))
+    must change by less than ``tolerance`` on two consecutive sweeps."""
+
+    tolerance: float
+    max_counter: int
+    iter: int = 0
+    counter: int = 0
+    norm_prev_iter: float = 0.0
+    PrevCP: object = None
+    lastangle: float = 1.0
+    final_fit: float = 0.0
+    total_iter: int = 0
+    trajectory: list = field(default_factory=list)
+
+
+def CPDFit(check) -> float:  # noqa: N802 - reference name
+    """fit_check.jl:68, cp_diff_check.jl:70, cp_angle_check.jl:70."""
     return check.final_fit
 
 
@@ -203,9 +239,55 @@ def _to_device_check(check) -> L.CpalsCheck:
         c.iter = int(check.iter)
         c.max_counter = int(check.max_counter)
         c.lastfit = float(check.lastfit)
+    elif isinstance(check, (CPDiffCheck, CPAngleCheck)):
+        angle = isinstance(check, CPAngleCheck)
+        c.kind = L.CHECK_ANGLE if angle else L.CHECK_DIFF
+        c.iter = int(check.iter)
+        c.counter = int(check.counter)
+        c.max_counter = int(check.max_counter)
+        c.tolerance = float(check.tolerance)
+        c.lastfit = float(check.lastangle if angle else check.lastfit)
+        c.final_fit = float(check.final_fit)
+        c.total_iter = int(check.total_iter)
+        c.norm_prev = float(check.norm_prev_iter)
+        c.has_prev = 0 if check.PrevCP is None else 1
     else:
-        raise NotImplementedError(f"{type(check).__name__} is not supported by the GPU engine (FitCheck, NoCheck)")
+        raise NotImplementedError(f"{type(check).__name__} is not supported by the GPU engine")
     return c
+
+
+def _prev_in(eng, check):
+    """Hand a held PrevCP of a CPDiffCheck / CPAngleCheck to the engine."""
+    if isinstance(check, (CPDiffCheck, CPAngleCheck)) and check.PrevCP is not None:
+        eng.set_prev(check.PrevCP.factors, check.PrevCP.lam)
+
+
+def _prev_out(eng, check, c: L.CpalsCheck):
+    """Copy the check's state back, PrevCP included (None once the check has reset)."""
+    angle = isinstance(check, CPAngleCheck)
+    check.iter = c.iter
+    check.counter = c.counter
+    if angle:
+        check.lastangle = c.lastfit
+    else:
+        check.lastfit = c.lastfit
+    check.final_fit = c.final_fit
+    check.total_iter = c.total_iter
+    check.norm_prev_iter = c.norm_prev
+    if c.has_prev:
+        fs, lam = eng.get_prev()
+        check.PrevCP = CPD(fs, lam, tuple(F.shape[0] for F in fs))
+    else:
+        check.PrevCP = None
+
+
+def _print_cross(rank, it0, traj, first_last):
+    """The reference's verbose line of cp_diff_check.jl:42-44 / cp_angle_check.jl:44-46."""
+    prev = first_last
+    for k, f in enumerate(traj, start=1):
+        if not np.isnan(f):
+            print(f"{rank}\t {it0 + k} \t {f} \t {abs(prev - f)}")
+            prev = f
 
 
 def _from_device_check(check, c: L.CpalsCheck, traj, rank, verbose):
@@ -222,6 +304,11 @@ def _from_device_check(check, c: L.CpalsCheck, traj, rank, verbose):
             for k, f in enumerate(traj, start=1):
                 print(f"{rank}\t {it0 + k} \t {f} \t {abs(prev - f)}")
                 prev = f
+    elif isinstance(check, (CPDiffCheck, CPAngleCheck)):
+        prev = check.lastangle if isinstance(check, CPAngleCheck) else check.lastfit
+        check.trajectory.extend(float(x) for x in traj)
+        if verbose:
+            _print_cross(rank, it0, traj, prev)
     else:
         check.iter = c.iter
         if verbose:
@@ -251,9 +338,12 @@ def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=Fa
         eng.set_tensor(T)
         eng.set_factors(cp.factors, cp.lam)
         c = _to_device_check(check)
+        _prev_in(eng, check)
         traj = eng.optimize(c)
         factors, lam = eng.get_factors()
-    _from_device_check(check, c, traj, R, verbose)
+        _from_device_check(check, c, traj, R, verbose)
+        if isinstance(check, (CPDiffCheck, CPAngleCheck)):
+            _prev_out(eng, check, c)
     if T.dtype == np.float32:
         factors = [F.astype(np.float32) for F in factors]
         lam = lam.astype(np.float32)
@@ -283,19 +373,36 @@ def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal):
         # ProjectionAlgorithm.jl:30-36: a FitCheck is not honoured by sampled solvers
         print(f"Warning: FitCheck is not enabled for {type(alg).__name__} will run {check.max_counter} iterations.")
     sweeps = max(0, int(check.max_counter) - int(check.iter))
+    cross = isinstance(check, (CPDiffCheck, CPAngleCheck))
     with Engine(T.shape, R, dtype=T.dtype, precision="fp64", device=device) as eng:
         eng.set_tensor(T)
         eng.set_factors(cp.factors, cp.lam)
         probs = [eng.leverage_scores(n) for n in range(N)]
+        if cross:  # ProjectionAlgorithm.jl:53: these checks run as for the exact solvers
+            c = _to_device_check(check)
+            _prev_in(eng, check)
+            first = check.lastangle if isinstance(check, CPAngleCheck) else check.lastfit
+            traj = []
         for s in range(sweeps):
             for n in range(N):
                 piv = sample_factor_matrices(alg.nsamples(n), n, probs, rng)
                 eng.sampled_update(n, piv, normal=normal)
                 probs[n] = eng.leverage_scores(n)
-            if verbose:
+            if cross:
+                done, val = eng.check_converge(c)
+                traj.append(val)
+                if done:
+                    break
+            elif verbose:
                 print(f"{R}\t{s + 1}")
         factors, lam = eng.get_factors()
-    check.iter = 0
+        if cross:
+            check.trajectory.extend(traj)
+            if verbose:
+                _print_cross(R, int(check.iter), traj, first)
+            _prev_out(eng, check, c)
+    if not cross:
+        check.iter = 0
     if T.dtype == np.float32:
         factors = [F.astype(np.float32) for F in factors]
         lam = lam.astype(np.float32)

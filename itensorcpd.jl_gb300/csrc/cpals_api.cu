@@ -79,6 +79,17 @@ struct cpals_ctx {
   int64_t prof_used = 0;
   int64_t launches = 0;
   int64_t sweep_launches = 0;  // kernel launches of one sweep (set when the graph is built)
+  // CPDiffCheck / CPAngleCheck: two previous-iterate buffers, the split cross Grams, the
+  // check kernel's block partials; cross_on appends the check to every sweep
+  double* prevF[2] = {};
+  double* prevLam[2] = {};
+  double* xpart = nullptr;
+  double* xred = nullptr;
+  unsigned* xcnt = nullptr;
+  int xS = 0;
+  int64_t prev_off[kMaxOrder] = {};
+  bool cross_on = false;
+  bool prev_valid = false;
 };
 
 cudaError_t cpals::set_smem_limit_once(const void* kernel, int bytes) {
@@ -151,6 +162,53 @@ cudaError_t enqueue_mttkrp(cpals_ctx* c, int n, const DevCheck* chk) {
   return tc_launch_mttkrp(c->tc, n, static_cast<float*>(c->part), chk, c->st);
 }
 
+int ensure_cross(cpals_ctx* c) {
+  if (c->xpart) return CPALS_OK;
+  const int R = (int)c->R;
+  int64_t tot = 0;
+  for (int m = 0; m < c->order; ++m) {
+    c->prev_off[m] = tot;
+    tot += c->dims[m] * R;
+  }
+  const int S = cross_splits(c->order, R, c->num_sms);
+  const int64_t RR = (int64_t)R * R;
+  if (dmalloc(&c->prevF[0], tot) != CPALS_OK || dmalloc(&c->prevF[1], tot) != CPALS_OK ||
+      dmalloc(&c->prevLam[0], R) != CPALS_OK || dmalloc(&c->prevLam[1], R) != CPALS_OK ||
+      dmalloc(&c->xred, 2 * ((RR + 255) / 256)) != CPALS_OK || dmalloc(&c->xcnt, 1) != CPALS_OK ||
+      dmalloc(&c->xpart, (int64_t)c->order * S * RR) != CPALS_OK)
+    return CPALS_E_CUDA;
+  CPALS_CUDA_TRY(cudaMemsetAsync(c->xcnt, 0, sizeof(unsigned), c->st));
+  c->xS = S;
+  return CPALS_OK;
+}
+
+CrossArgs cross_args(const cpals_ctx* c) {
+  CrossArgs a{};
+  for (int m = 0; m < c->order; ++m) {
+    a.F[m] = c->F[m];
+    a.G[m] = c->G[m];
+    a.dims[m] = c->dims[m];
+    a.off[m] = c->prev_off[m];
+  }
+  a.lam = c->lam;
+  a.prevF[0] = c->prevF[0];
+  a.prevF[1] = c->prevF[1];
+  a.prevLam[0] = c->prevLam[0];
+  a.prevLam[1] = c->prevLam[1];
+  a.order = c->order;
+  a.R = (int)c->R;
+  a.S = c->xS;
+  a.xpart = c->xpart;
+  a.red = c->xred;
+  a.counter = c->xcnt;
+  a.chk = c->chk;
+  a.traj = c->traj;
+  a.traj_cap = c->traj_cap;
+  return a;
+}
+
+bool is_cross_kind(int kind) { return kind == CPALS_CHECK_DIFF || kind == CPALS_CHECK_ANGLE; }
+
 int enqueue_sweep(cpals_ctx* c) {
   const int N = c->order;
   const int R = (int)c->R;
@@ -201,6 +259,10 @@ int enqueue_sweep(cpals_ctx* c) {
     const BtileDesc btd = c->tc ? tc_btile_desc(c->tc, n) : c->dt ? dt_btile_desc(c->dt, n) : BtileDesc{nullptr, 0, 0};
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32r[n], c->rpad,
                                     c->Graw, c->G[n], last ? nullptr : c->chk, c->st, btd));
+  }
+  if (c->cross_on) {  // check_converge of a CPDiffCheck / CPAngleCheck on the new iterate
+    CPALS_CUDA_TRY(launch_cp_check(cross_args(c), c->st));
+    c->launches += 2;
   }
   return CPALS_OK;
 }
@@ -376,6 +438,13 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->Ts);
   cudaFree(c->Spart);
   cudaFree(c->derr);
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(c->prevF[b]);
+    cudaFree(c->prevLam[b]);
+  }
+  cudaFree(c->xpart);
+  cudaFree(c->xred);
+  cudaFree(c->xcnt);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
   for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
@@ -644,14 +713,22 @@ int cpals_mttkrp(cpals_ctx* c, int mode, double* host_out) {
 
 int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int64_t traj_capacity) {
   if (!c || !check) return CPALS_E_ARG;
-  if (check->kind != CPALS_CHECK_NONE && check->kind != CPALS_CHECK_FIT) return CPALS_E_ARG;
+  if (check->kind != CPALS_CHECK_NONE && check->kind != CPALS_CHECK_FIT && !is_cross_kind(check->kind))
+    return CPALS_E_ARG;
   if (check->max_counter < 0) return CPALS_E_ARG;
   if (!c->T_set || !c->F_set) return CPALS_E_STATE;
   DeviceGuard g(c->device);
+  const bool cross = is_cross_kind(check->kind);
+  if (cross && check->has_prev && !c->prev_valid) return CPALS_E_STATE;
   const int64_t nmax = (int64_t)check->max_counter - check->iter;
   check->sweeps_run = 0;
   if (nmax <= 0) return CPALS_OK;
   if (ensure_traj(c, nmax) != CPALS_OK) return CPALS_E_CUDA;
+  if (cross && ensure_cross(c) != CPALS_OK) return CPALS_E_CUDA;
+  if (cross != c->cross_on) {
+    invalidate_graph(c);
+    c->cross_on = cross;
+  }
   // keep the device fallback counter, reset the rest from the host check
   CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
@@ -668,6 +745,8 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
   h.done = 0;
   h.nan_flag = 0;
   h.sweeps = 0;
+  h.norm_prev = check->norm_prev;
+  h.has_prev = cross ? check->has_prev : 0;
   CPALS_CUDA_TRY(cudaMemcpyAsync(c->chk, c->hchk, sizeof(DevCheck), cudaMemcpyHostToDevice, c->st));
   const bool use_graph = !(c->flags & CPALS_FLAG_NO_GRAPH) && !c->profiling;
   if (use_graph && !c->graph) {
@@ -700,6 +779,11 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
   check->final_fit = h.final_fit;
   check->total_iter = h.total_iter;
   check->sweeps_run = h.sweeps;
+  if (cross) {
+    check->norm_prev = h.norm_prev;
+    check->has_prev = h.has_prev;
+    c->prev_valid = h.has_prev != 0;
+  }
   if (fit_trajectory && traj_capacity > 0) {
     const int64_t n = std::min<int64_t>({(int64_t)h.sweeps, traj_capacity, c->traj_cap});
     if (n > 0) {
@@ -709,6 +793,99 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
   }
   if (h.nan_flag) return CPALS_E_NAN;
   return check_tc_err(c);
+}
+
+int cpals_check_converge(cpals_ctx* c, cpals_check* check, int* converged, double* value) {
+  if (!c || !check || !converged || !is_cross_kind(check->kind) || check->max_counter < 0) return CPALS_E_ARG;
+  if (!c->F_set) return CPALS_E_STATE;
+  if (check->has_prev && !c->prev_valid) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  if (ensure_traj(c, 1) != CPALS_OK || ensure_cross(c) != CPALS_OK) return CPALS_E_CUDA;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  DevCheck& h = *c->hchk;
+  h.kind = check->kind;
+  h.iter = check->iter;
+  h.counter = check->counter;
+  h.max_counter = check->max_counter;
+  h.tol = check->tolerance;
+  h.ref_norm = check->ref_norm;
+  h.lastfit = check->lastfit;
+  h.final_fit = check->final_fit;
+  h.total_iter = check->total_iter;
+  h.norm_prev = check->norm_prev;
+  h.has_prev = check->has_prev;
+  h.done = 0;
+  h.nan_flag = 0;
+  h.sweeps = 0;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->chk, c->hchk, sizeof(DevCheck), cudaMemcpyHostToDevice, c->st));
+  CPALS_CUDA_TRY(launch_cp_check(cross_args(c), c->st));
+  c->launches += 2;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  check->iter = h.iter;
+  check->counter = h.counter;
+  check->lastfit = h.lastfit;
+  check->final_fit = h.final_fit;
+  check->total_iter = h.total_iter;
+  check->norm_prev = h.norm_prev;
+  check->has_prev = h.has_prev;
+  check->sweeps_run = 0;
+  c->prev_valid = h.has_prev != 0;
+  *converged = h.done;
+  if (value) {
+    CPALS_CUDA_TRY(cudaMemcpyAsync(value, c->traj, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  }
+  return CPALS_OK;
+}
+
+int cpals_get_prev(cpals_ctx* c, double* const* host_factors, double* host_lambda) {
+  if (!c) return CPALS_E_ARG;
+  if (!c->prev_valid) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  const int sel = c->hchk->psel;
+  const int R = (int)c->R;
+  std::vector<double> tmp;
+  for (int m = 0; m < c->order; ++m) {
+    if (!host_factors || !host_factors[m]) continue;
+    tmp.resize((size_t)c->dims[m] * R);
+    CPALS_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c->prevF[sel] + c->prev_off[m], sizeof(double) * tmp.size(),
+                                   cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+    rowmajor_to_colmajor_host(tmp.data(), c->dims[m], R, host_factors[m]);
+  }
+  if (host_lambda) {
+    CPALS_CUDA_TRY(cudaMemcpyAsync(host_lambda, c->prevLam[sel], sizeof(double) * R, cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  }
+  return CPALS_OK;
+}
+
+int cpals_set_prev(cpals_ctx* c, const double* const* host_factors, const double* host_lambda) {
+  if (!c || !host_factors || !host_lambda) return CPALS_E_ARG;
+  for (int m = 0; m < c->order; ++m)
+    if (!host_factors[m]) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  if (ensure_cross(c) != CPALS_OK) return CPALS_E_CUDA;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  const int sel = c->hchk->psel;
+  const int R = (int)c->R;
+  std::vector<double> tmp;
+  for (int m = 0; m < c->order; ++m) {
+    tmp.resize((size_t)c->dims[m] * R);
+    colmajor_to_rowmajor_host(host_factors[m], c->dims[m], R, tmp.data());
+    CPALS_CUDA_TRY(cudaMemcpyAsync(c->prevF[sel] + c->prev_off[m], tmp.data(), sizeof(double) * tmp.size(),
+                                   cudaMemcpyHostToDevice, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));  // tmp is reused for the next mode
+  }
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->prevLam[sel], host_lambda, sizeof(double) * R, cudaMemcpyHostToDevice, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  c->prev_valid = true;
+  return CPALS_OK;
 }
 
 int cpals_fallback_count(cpals_ctx* c, int64_t* count) {

@@ -31,6 +31,11 @@ struct DevCheck {
   int nan_flag;
   int sweeps;  // sweeps whose check ran (index into the trajectory)
   long long fallbacks;  // pivoted-QR fallbacks taken by the normal-equation solve
+  // CPDiffCheck / CPAngleCheck: norm_prev_iter, PrevCP !== nothing, and which of the two
+  // previous-iterate buffers holds PrevCP (the other receives the current iterate)
+  double norm_prev;
+  int has_prev;
+  int psel;
 };
 
 struct FactorSet {
@@ -169,6 +174,30 @@ cudaError_t launch_fibers(const void* T, int tdtype, int order, int mode, const 
 cudaError_t launch_colmajor_to_rowmajor(const double* src, int64_t rows, int R, double* dst, cudaStream_t st);
 cudaError_t launch_leverage_rows(const double* F, int64_t In, int R, const double* work, const double* U,
                                  const int* piv, const SolveInfo* info, double scale, double* probs, cudaStream_t st);
+
+// CPDiffCheck / CPAngleCheck on the current iterate (k_cpcheck.cu).  The previous iterate
+// lives in prevF[psel] / prevLam[psel] (DevCheck::psel); the current one is copied into the
+// other buffer by the same launches.
+struct CrossArgs {
+  const double* F[kMaxOrder];  // current factors, row-major [I_m][R]
+  const double* G[kMaxOrder];  // their Grams F_m^T F_m
+  const double* lam;
+  double* prevF[2];            // modes concatenated, row-major, mode m at off[m]
+  double* prevLam[2];
+  int64_t dims[kMaxOrder];
+  int64_t off[kMaxOrder];
+  int order, R, S;             // S: row splits of each cross Gram
+  double* xpart;               // [order][S][R][R] partial cross Grams P_m^T F_m
+  double* red;                 // two doubles per block of the check kernel
+  unsigned* counter;           // zero between launches
+  DevCheck* chk;
+  double* traj;
+  int64_t traj_cap;
+};
+// Row splits of the cross Grams for about two blocks per SM.
+int cross_splits(int order, int R, int num_sms);
+// Two launches: the split cross Grams (and the copy of the iterate), then the check.
+cudaError_t launch_cp_check(const CrossArgs& a, cudaStream_t st);
 
 // Raises a kernel's dynamic shared-memory limit on the current device, once per (device,
 // kernel) per process (thread-safe).  The attribute is per device, so a process that drives

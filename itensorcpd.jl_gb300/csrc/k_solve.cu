@@ -1066,6 +1066,8 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
   const int64_t traj_cap = fa.traj_cap;
   if (tid != 0) return;
   DevCheck& k = *chk;
+  // CPDiffCheck / CPAngleCheck run after the sweep, on the normalised iterate (k_cpcheck.cu)
+  if (k.kind == CPALS_CHECK_DIFF || k.kind == CPALS_CHECK_ANGLE) return;
   double fit = NAN;
   if (k.ref_norm > 0.0) {
     const double rn = k.ref_norm;

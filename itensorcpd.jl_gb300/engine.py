@@ -83,6 +83,32 @@ class Engine:
         L.check(self.lib.cpals_get_factors(self.h, arr, L.dptr(lam)), "cpals_get_factors")
         return fs, lam
 
+    def get_prev(self):
+        """The previous iterate held for CPDiffCheck / CPAngleCheck (PrevCP)."""
+        fs = [np.empty((d, self.rank), dtype=np.float64, order="F") for d in self.dims]
+        lam = np.empty(self.rank, dtype=np.float64)
+        arr = (L._DP * self.order)(*[L.dptr(F) for F in fs])
+        L.check(self.lib.cpals_get_prev(self.h, arr, L.dptr(lam)), "cpals_get_prev")
+        return fs, lam
+
+    def set_prev(self, factors, lam):
+        fs = [np.asfortranarray(F, dtype=np.float64) for F in factors]
+        for F, d in zip(fs, self.dims):
+            if F.shape != (d, self.rank):
+                raise ValueError(f"factor shape {F.shape} != {(d, self.rank)}")
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        arr = (L._DP * self.order)(*[L.dptr(F) for F in fs])
+        L.check(self.lib.cpals_set_prev(self.h, arr, L.dptr(lam)), "cpals_set_prev")
+
+    def check_converge(self, chk: L.CpalsCheck):
+        """One CPDiffCheck / CPAngleCheck call on the current iterate (``chk`` updated in
+        place); returns (converged, value), value NaN when the call only stored the iterate."""
+        conv = C.c_int(0)
+        val = np.full(1, np.nan)
+        L.check(self.lib.cpals_check_converge(self.h, C.byref(chk), C.byref(conv), L.dptr(val)),
+                "cpals_check_converge")
+        return bool(conv.value), float(val[0])
+
     def gram(self, mode):
         G = np.empty((self.rank, self.rank), dtype=np.float64)
         L.check(self.lib.cpals_get_gram(self.h, int(mode), L.dptr(G)), "cpals_get_gram")

@@ -258,6 +258,105 @@ class FitCheck:
         return False
 
 
+def cp_cp_inner(prev_factors, prev_lam, factors, lam) -> float:
+    """<T_prev, T_curr> as the checks form it: prev_lam^T (P_1^T F_1 o P_2^T F_2 o ...) lam
+    (cp_cp_contract, src/algebra/cp_contract.jl:32-52, contracted with both lambdas,
+    cp_diff_check.jl:31)."""
+    inner = np.ones((prev_lam.shape[0], lam.shape[0]))
+    for P, F in zip(prev_factors, factors):
+        inner = inner * (P.T @ F)
+    return float(prev_lam @ inner @ lam)
+
+
+def _factor_grams(factors):
+    return [F.T @ F for F in factors]
+
+
+@dataclass
+class CPDiffCheck:
+    """src/converge_checks/cp_diff_check.jl:6-18 (mutable struct CPDiffCheck)."""
+
+    tolerance: float
+    max_counter: int
+    iter: int = 0
+    counter: int = 0
+    norm_prev_iter: float = 0.0
+    PrevCP: tuple | None = None  # (factors, lam) of the previous iterate
+    lastfit: float = 1.0
+    final_fit: float = 0.0
+    total_iter: int = 0
+    trajectory: list = field(default_factory=list)
+
+    def check_converge(self, factors, lam, grams=None, verbose=False) -> bool:
+        """cp_diff_check.jl:20-68."""
+        self.iter += 1
+        if self.PrevCP is None:
+            self.PrevCP = ([F.copy() for F in factors], lam.copy())
+            self.norm_prev_iter = norm_factors(_factor_grams(factors), lam)
+            self.trajectory.append(float("nan"))
+            return False
+        inner = cp_cp_inner(self.PrevCP[0], self.PrevCP[1], factors, lam)
+        fact_square = norm_factors(_factor_grams(factors), lam)
+        norm_res = math.sqrt(abs(self.norm_prev_iter + fact_square - 2 * abs(inner)))
+        curr_fit = 1.0 - norm_res / math.sqrt(abs(self.norm_prev_iter))
+        dfit = abs(self.lastfit - curr_fit)
+        self.lastfit = curr_fit
+        self.PrevCP = ([F.copy() for F in factors], lam.copy())
+        self.norm_prev_iter = fact_square
+        self.trajectory.append(curr_fit)
+        if verbose:
+            print(f"{lam.shape[0]}\t {self.iter} \t {curr_fit} \t {dfit}")
+        return self._count(dfit)
+
+    def _count(self, delta) -> bool:
+        """The counter logic shared by both checks (cp_diff_check.jl:46-66)."""
+        if delta < self.tolerance:
+            self.counter += 1
+            if self.counter >= 2:
+                self._reset()
+                return True
+        else:
+            self.counter = 0
+        if self.iter >= self.max_counter:
+            self._reset()
+        return False
+
+    def _reset(self):
+        self.total_iter = self.iter
+        self.iter = 0
+        self.counter = 0
+        self.final_fit = self.lastfit
+        self.lastfit = 0.0
+        self.PrevCP = None
+
+
+@dataclass
+class CPAngleCheck(CPDiffCheck):
+    """src/converge_checks/cp_angle_check.jl:6-18; ``lastfit`` plays ``lastangle``."""
+
+    def check_converge(self, factors, lam, grams=None, verbose=False) -> bool:
+        """cp_angle_check.jl:20-68."""
+        self.iter += 1
+        if self.PrevCP is None:
+            self.PrevCP = ([F.copy() for F in factors], lam.copy())
+            self.norm_prev_iter = math.sqrt(norm_factors(_factor_grams(factors), lam))
+            self.trajectory.append(float("nan"))
+            return False
+        numer = cp_cp_inner(self.PrevCP[0], self.PrevCP[1], factors, lam)
+        norm_curr = math.sqrt(norm_factors(_factor_grams(factors), lam))
+        theta = numer / (norm_curr * self.norm_prev_iter)
+        theta = 1.0 if theta > 1.0 else theta
+        curr_angle = math.acos(theta) if -1.0 <= theta else float("nan")
+        dangle = abs(self.lastfit - curr_angle)
+        self.lastfit = curr_angle
+        self.PrevCP = ([F.copy() for F in factors], lam.copy())
+        self.norm_prev_iter = norm_curr
+        self.trajectory.append(curr_angle)
+        if verbose:
+            print(f"{lam.shape[0]}\t {self.iter} \t {curr_angle} \t {dangle}")
+        return self._count(dangle)
+
+
 @dataclass
 class NoCheck:
     """src/converge_checks/no_check.jl:1-20."""

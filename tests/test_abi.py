@@ -3,6 +3,7 @@ import ctypes
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -62,3 +63,30 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.cpals_set_tensor(None, None) == -1
     assert lib.cpals_mttkrp(None, 0, None) == -1
     assert lib.cpals_optimize(None, None, None, 0) == -1
+
+
+def test_check_struct_mirrors_the_header(pkg):
+    # the ctypes mirror of cpals_check has the header's fields, in order, and its size
+    import re
+
+    from itensorcpd_gb300 import _lib as L
+
+    text = (ROOT / "include" / "cpals.h").read_text()
+    body = re.search(r"typedef struct cpals_check \{(.*?)\} cpals_check;", text, re.S).group(1)
+    names = re.findall(r"^\s*(?:int32_t|double)\s+(\w+);", body, re.M)
+    assert names == [f[0] for f in L.CpalsCheck._fields_]
+    assert ctypes.sizeof(L.CpalsCheck) == 72
+
+
+def test_diff_and_angle_checks_marshal_to_the_device_struct(pkg):
+    from itensorcpd_gb300 import CPAngleCheck, CPD, CPDiffCheck
+    from itensorcpd_gb300 import _lib as L
+    from itensorcpd_gb300.api import _to_device_check
+
+    d = CPDiffCheck(1e-5, 40)
+    c = _to_device_check(d)
+    assert (c.kind, c.max_counter, c.tolerance, c.lastfit, c.has_prev) == (L.CHECK_DIFF, 40, 1e-5, 1.0, 0)
+    a = CPAngleCheck(1e-4, 7, iter=2, counter=1, norm_prev_iter=3.5, lastangle=0.25,
+                     PrevCP=CPD([np.ones((2, 1))], np.ones(1)))
+    c = _to_device_check(a)
+    assert (c.kind, c.iter, c.counter, c.norm_prev, c.lastfit, c.has_prev) == (L.CHECK_ANGLE, 2, 1, 3.5, 0.25, 1)

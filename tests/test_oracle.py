@@ -192,3 +192,40 @@ def test_lev_score_sampled_converges(oracle):
     # sampled sweep reproduces them
     Ff, lf = oracle.lev_score_als(T, Ft, lt, 100, 1, np.random.default_rng(7), normal=False)
     assert np.linalg.norm(oracle.reconstruct(Ff, lf) - T) / np.linalg.norm(T) < 1e-10
+
+
+def test_cp_cp_inner_is_the_dense_inner_product(oracle):
+    # cp_contract.jl:32-52 contracted with both lambdas equals <reconstruct(P), reconstruct(F)>
+    dims = (6, 5, 4)
+    P, lp = det_factors(dims, 3, seed=41)
+    F, lf = det_factors(dims, 4, seed=42)
+    dense = float(np.sum(oracle.reconstruct(P, lp) * oracle.reconstruct(F, lf)))
+    assert abs(oracle.cp_cp_inner(P, lp, F, lf) - dense) <= 1e-12 * abs(dense)
+    assert abs(oracle.norm_factors([X.T @ X for X in F], lf) - float(np.sum(oracle.reconstruct(F, lf) ** 2))) <= 1e-10
+
+
+def test_diff_and_angle_checks_on_a_fixed_iterate(oracle):
+    # cp_diff_check.jl / cp_angle_check.jl: the first call stores PrevCP.  An unchanged
+    # iterate has fit 1, which already differs from the initial lastfit 1 by less than tol, so
+    # CPDiffCheck stops on call 3; its angle 0 differs from the initial lastangle 1, so
+    # CPAngleCheck counts from call 3 and stops on call 4.  Both reset their state.
+    dims = (7, 6, 5)
+    F, lam = det_factors(dims, 3, seed=43)
+    for cls, value, calls in ((oracle.CPDiffCheck, 1.0, 3), (oracle.CPAngleCheck, 0.0, 4)):
+        chk = cls(1e-6, 10)
+        results = [chk.check_converge(F, lam) for _ in range(calls)]
+        assert results == [False] * (calls - 1) + [True]
+        assert chk.PrevCP is None and chk.iter == 0 and chk.counter == 0 and chk.total_iter == calls
+        assert abs(chk.final_fit - value) <= 1e-7
+        assert np.isnan(chk.trajectory[0])
+
+
+def test_diff_check_resets_at_max_counter(oracle):
+    # cp_diff_check.jl:58-66: reaching max_counter resets iter, counter, lastfit and PrevCP
+    dims = (5, 4, 3)
+    chk = oracle.CPDiffCheck(1e-12, 3)
+    for k in range(3):
+        F, lam = det_factors(dims, 2, seed=50 + k)
+        assert chk.check_converge(F, lam) is False
+    assert chk.iter == 0 and chk.total_iter == 3 and chk.PrevCP is None and chk.lastfit == 0.0
+    assert chk.final_fit == chk.trajectory[-1]

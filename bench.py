@@ -574,6 +574,24 @@ def main():
     e2e_ms = max_over_ranks(eng.timer_stop())
     e2e_value = world * args.steps * SWEEPS / (e2e_ms / 1e3)
     fac_bytes = sum(d * RANK * 8 for d in DIMS) + RANK * 8
+
+    # ---- sweep time under each convergence check (tolerance 0, so none stops early)
+    checks = {}
+    if not args.no_extras and rank == 0:
+        for name, kind in (("FitCheck", L.CHECK_FIT), ("CPDiffCheck", L.CHECK_DIFF),
+                           ("CPAngleCheck", L.CHECK_ANGLE)):
+            for rep in range(2):  # the first run builds the check's sweep graph
+                eng.set_factors(F0, lam0)
+                c = nocheck()
+                c.kind = kind
+                c.tolerance = 0.0
+                c.lastfit = 1.0
+                c.max_counter = 100
+                eng.synchronize()
+                eng.timer_start()
+                eng.optimize(c)
+                t = eng.timer_stop()
+            checks[name] = 1e3 * t / max(1, c.sweeps_run)
     eng.close()
 
     extras = {}
@@ -587,6 +605,7 @@ def main():
         traj64 = e64.optimize(nocheck())
         ms64 = e64.timer_stop()
         e64.close()
+        extras["us_per_sweep_by_check"] = checks
         extras["fp64_gpu_sweeps_per_s"] = SWEEPS / (ms64 / 1e3)
         extras["final_fit_fp64"] = float(traj64[-1])
         extras["final_fit_diff_vs_fp64"] = abs(final_fit - float(traj64[-1]))

@@ -86,7 +86,9 @@ struct cpals_ctx {
   double* xpart = nullptr;
   double* xred = nullptr;
   unsigned* xcnt = nullptr;
-  int xS = 0;
+  int64_t xrows = 0;
+  int xS[kMaxOrder] = {};
+  int xSmax = 0;
   int64_t prev_off[kMaxOrder] = {};
   bool cross_on = false;
   bool prev_valid = false;
@@ -170,15 +172,21 @@ int ensure_cross(cpals_ctx* c) {
     c->prev_off[m] = tot;
     tot += c->dims[m] * R;
   }
-  const int S = cross_splits(c->order, R, c->num_sms);
+  const int64_t rows = cross_rows(c->order, c->dims, R, c->num_sms);
+  int smax = 1;
+  for (int m = 0; m < c->order; ++m) {
+    c->xS[m] = (int)((c->dims[m] + rows - 1) / rows);
+    smax = std::max(smax, c->xS[m]);
+  }
   const int64_t RR = (int64_t)R * R;
   if (dmalloc(&c->prevF[0], tot) != CPALS_OK || dmalloc(&c->prevF[1], tot) != CPALS_OK ||
       dmalloc(&c->prevLam[0], R) != CPALS_OK || dmalloc(&c->prevLam[1], R) != CPALS_OK ||
-      dmalloc(&c->xred, 2 * ((RR + 255) / 256)) != CPALS_OK || dmalloc(&c->xcnt, 1) != CPALS_OK ||
-      dmalloc(&c->xpart, (int64_t)c->order * S * RR) != CPALS_OK)
+      dmalloc(&c->xred, 2 * ((RR + 31) / 32)) != CPALS_OK || dmalloc(&c->xcnt, 1) != CPALS_OK ||
+      dmalloc(&c->xpart, (int64_t)c->order * smax * RR) != CPALS_OK)
     return CPALS_E_CUDA;
   CPALS_CUDA_TRY(cudaMemsetAsync(c->xcnt, 0, sizeof(unsigned), c->st));
-  c->xS = S;
+  c->xrows = rows;
+  c->xSmax = smax;
   return CPALS_OK;
 }
 
@@ -189,6 +197,7 @@ CrossArgs cross_args(const cpals_ctx* c) {
     a.G[m] = c->G[m];
     a.dims[m] = c->dims[m];
     a.off[m] = c->prev_off[m];
+    a.S[m] = c->xS[m];
   }
   a.lam = c->lam;
   a.prevF[0] = c->prevF[0];
@@ -197,7 +206,8 @@ CrossArgs cross_args(const cpals_ctx* c) {
   a.prevLam[1] = c->prevLam[1];
   a.order = c->order;
   a.R = (int)c->R;
-  a.S = c->xS;
+  a.rows = c->xrows;
+  a.Smax = c->xSmax;
   a.xpart = c->xpart;
   a.red = c->xred;
   a.counter = c->xcnt;

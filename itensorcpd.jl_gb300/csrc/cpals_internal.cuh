@@ -186,16 +186,19 @@ struct CrossArgs {
   double* prevLam[2];
   int64_t dims[kMaxOrder];
   int64_t off[kMaxOrder];
-  int order, R, S;             // S: row splits of each cross Gram
-  double* xpart;               // [order][S][R][R] partial cross Grams P_m^T F_m
+  int order, R;
+  int64_t rows;                // rows of one split
+  int S[kMaxOrder];            // splits of mode m: ceil(I_m / rows)
+  int Smax;
+  double* xpart;               // [order][Smax][R][R] partial cross Grams P_m^T F_m
   double* red;                 // two doubles per block of the check kernel
   unsigned* counter;           // zero between launches
   DevCheck* chk;
   double* traj;
   int64_t traj_cap;
 };
-// Row splits of the cross Grams for about two blocks per SM.
-int cross_splits(int order, int R, int num_sms);
+// Rows of one cross-Gram split (a multiple of 8) for about six blocks per SM.
+int64_t cross_rows(int order, const int64_t* dims, int R, int num_sms);
 // Two launches: the split cross Grams (and the copy of the iterate), then the check.
 cudaError_t launch_cp_check(const CrossArgs& a, cudaStream_t st);
 

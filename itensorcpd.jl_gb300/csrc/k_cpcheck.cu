@@ -7,11 +7,12 @@
 //   ||T_curr||^2     = lam^T (G_0 .* G_1 .* ...) lam      (norm_factors, converge_checks.jl:5-11)
 //
 // with P_m the previous iterate's factors and G_m = F_m^T F_m the Grams the sweep keeps.
-// The cross Grams are I_m x R by I_m x R FP64 products.  FP64 issue is the limit here, so
-// k_cross_gram cuts every cross Gram into 64 x 64 output tiles and S row splits, giving
-// about two blocks per SM, and writes the split partials; k_cp_check sums them in split
-// order, forms both quadratic forms, reduces them over its blocks in block order (the last
-// block to finish does this) and runs the check's update on one thread.
+// The cross Grams are I_m x R by I_m x R FP64 products, and FP64 issue (two DFMA per clock
+// per SM) is the limit: k_cross_gram cuts every cross Gram into 32 x 32 output tiles and
+// splits of 8k rows, about six blocks per SM of about 2 us each, and writes the split
+// partials.  k_cp_check sums the partials of 32 entries per block over 8 thread groups
+// (fixed order), forms both quadratic forms, reduces them over its blocks in block order
+// (the last block to finish does this) and runs the check's update on one thread.
 //
 // FP64 throughout: the fit between consecutive iterates, 1 - sqrt(|a + b - 2c|) / sqrt(a),
 // cancels to the size of the change, so lower precision would hide changes below 1e-4.
@@ -20,8 +21,8 @@
 namespace cpals {
 namespace {
 
-constexpr int XT = 64;  // output tile edge
-constexpr int XK = 16;  // rows staged per step
+constexpr int XT = 32;  // output tile edge
+constexpr int XK = 8;   // rows staged per step (a split is a multiple of XK rows)
 
 __device__ double warp_block_sum(double v, double* sv) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -35,21 +36,22 @@ __device__ double warp_block_sum(double v, double* sv) {
   return t;
 }
 
-// grid (S, nt*nt, order), 256 threads.  Block (s, tile, m) computes rows [r0, r1) of
-// P_m^T F_m for the 64 x 64 tile (ti, tj); the tile-0 blocks also copy those rows of F_m
-// (and block (0, 0, 0) lambda) into the buffer that becomes PrevCP.
+// grid (Smax, nt*nt, order), 256 threads.  Block (s, tile, m) computes rows [r0, r1) of
+// P_m^T F_m for the 32 x 32 tile (ti, tj), two by two outputs per thread; the tile-0
+// blocks also copy those rows of F_m (and block (0, 0, 0) lambda) into the buffer that
+// becomes PrevCP.
 __global__ void __launch_bounds__(256) k_cross_gram(CrossArgs a) {
   const DevCheck* chk = a.chk;
   if (chk->done) return;
+  const int s = blockIdx.x, tile = blockIdx.y, m = blockIdx.z;
+  if (s >= a.S[m]) return;
   __shared__ double ps[XK][XT];
   __shared__ double fs[XK][XT];
-  const int s = blockIdx.x, tile = blockIdx.y, m = blockIdx.z;
   const int R = a.R;
   const int nt = (R + XT - 1) / XT;
   const int ti = tile / nt, tj = tile - ti * nt;
   const int64_t In = a.dims[m];
-  const int64_t rows = (In + a.S - 1) / a.S;
-  const int64_t r0 = min(In, (int64_t)s * rows), r1 = min(In, r0 + rows);
+  const int64_t r0 = min(In, (int64_t)s * a.rows), r1 = min(In, r0 + a.rows);
   const int sel = chk->psel;
   const double* __restrict__ Fm = a.F[m];
   if (tile == 0) {
@@ -61,46 +63,34 @@ __global__ void __launch_bounds__(256) k_cross_gram(CrossArgs a) {
   if (!chk->has_prev) return;
   const double* __restrict__ Pm = a.prevF[sel] + a.off[m];
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  double acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  const int lk = threadIdx.x >> 5, lc = threadIdx.x & 31;  // staging: one row, one column
+  const int ca = ti * XT + lc, cb = tj * XT + lc;
+  double acc00 = 0.0, acc01 = 0.0, acc10 = 0.0, acc11 = 0.0;
   for (int64_t kk = r0; kk < r1; kk += XK) {
-#pragma unroll
-    for (int q = 0; q < (XK * XT) / 256; ++q) {
-      const int e = threadIdx.x + 256 * q;
-      const int k = e >> 6, c = e & (XT - 1);
-      const int64_t row = kk + k;
-      const int ca = ti * XT + c, cb = tj * XT + c;
-      ps[k][c] = (row < r1 && ca < R) ? Pm[row * R + ca] : 0.0;
-      fs[k][c] = (row < r1 && cb < R) ? Fm[row * R + cb] : 0.0;
-    }
+    const int64_t row = kk + lk;
+    ps[lk][lc] = (row < r1 && ca < R) ? Pm[row * R + ca] : 0.0;
+    fs[lk][lc] = (row < r1 && cb < R) ? Fm[row * R + cb] : 0.0;
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < XK; ++k) {
-      double pa[4], fb[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) pa[i] = ps[k][ty + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) fb[j] = fs[k][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(pa[i], fb[j], acc[i][j]);
+      const double p0 = ps[k][ty], p1 = ps[k][ty + 16];
+      const double f0 = fs[k][tx], f1 = fs[k][tx + 16];
+      acc00 = fma(p0, f0, acc00);
+      acc01 = fma(p0, f1, acc01);
+      acc10 = fma(p1, f0, acc10);
+      acc11 = fma(p1, f1, acc11);
     }
     __syncthreads();
   }
-  double* __restrict__ out = a.xpart + ((int64_t)m * a.S + s) * (int64_t)R * R;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int r = ti * XT + ty + 16 * i;
-    if (r >= R) continue;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int c = tj * XT + tx + 16 * j;
-      if (c < R) out[(int64_t)r * R + c] = acc[i][j];
-    }
+  double* __restrict__ out = a.xpart + ((int64_t)m * a.Smax + s) * (int64_t)R * R;
+  const int r_0 = ti * XT + ty, r_1 = r_0 + 16, c_0 = tj * XT + tx, c_1 = c_0 + 16;
+  if (r_0 < R) {
+    if (c_0 < R) out[(int64_t)r_0 * R + c_0] = acc00;
+    if (c_1 < R) out[(int64_t)r_0 * R + c_1] = acc01;
+  }
+  if (r_1 < R) {
+    if (c_0 < R) out[(int64_t)r_1 * R + c_0] = acc10;
+    if (c_1 < R) out[(int64_t)r_1 * R + c_1] = acc11;
   }
 }
 
@@ -158,42 +148,60 @@ __device__ void cp_check_update(DevCheck& k, double inner, double self, double* 
   }
 }
 
-// grid ceil(R*R / 256), 256 threads.  Thread e = (r, c) forms
-// lam_prev[r] lam[c] prod_m sum_s xpart[m][s][r][c] and lam[r] lam[c] prod_m G_m[r][c].
+// grid ceil(R*R / 32), 256 threads: 32 entries e = (r, c) per block, 8 groups of split
+// indices (s = g, g + 8, ...).  Warp 0 then forms lam_prev[r] lam[c] prod_m C_m[r][c] and
+// lam[r] lam[c] prod_m G_m[r][c] for its entries.
 __global__ void __launch_bounds__(256) k_cp_check(CrossArgs a) {
   DevCheck* chk = a.chk;
   if (chk->done) return;
+  __shared__ double sp[8][33];
   __shared__ double sv[8];
   __shared__ int s_last;
   const int R = a.R;
   const int64_t RR = (int64_t)R * R;
   const int sel = chk->psel;
   const int has_prev = chk->has_prev;
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double inner = 0.0, self = 0.0;
-  if (e < RR) {
-    const int r = (int)(e / R), c = (int)(e - (int64_t)r * R);
-    double g = a.lam[r] * a.lam[c];
-    for (int m = 0; m < a.order; ++m) g *= a.G[m][e];
-    self = g;
-    if (has_prev) {
-      double h = a.prevLam[sel][r] * a.lam[c];
-      for (int m = 0; m < a.order; ++m) {
-        const double* __restrict__ xp = a.xpart + (int64_t)m * a.S * RR + e;
-        double x = 0.0;
-        for (int s = 0; s < a.S; ++s) x += xp[(int64_t)s * RR];
-        h *= x;
+  const int j = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int64_t e = (int64_t)blockIdx.x * 32 + j;
+  const bool valid = e < RR;
+  double h = 1.0;
+  if (has_prev) {
+    for (int m = 0; m < a.order; ++m) {
+      double x = 0.0;
+      if (valid) {
+        const double* __restrict__ xp = a.xpart + (int64_t)m * a.Smax * RR + e;
+        for (int s = g; s < a.S[m]; s += 8) x += xp[(int64_t)s * RR];
       }
-      inner = h;
+      sp[g][j] = x;
+      __syncthreads();
+      if (g == 0) {
+        double t = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) t += sp[q][j];
+        h *= t;
+      }
+      __syncthreads();
     }
   }
-  inner = warp_block_sum(inner, sv);
-  self = warp_block_sum(self, sv);
-  if (threadIdx.x == 0) {
-    a.red[2 * blockIdx.x] = inner;
-    a.red[2 * blockIdx.x + 1] = self;
-    __threadfence();
-    s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+  if (g == 0) {
+    double inner = 0.0, self = 0.0;
+    if (valid) {
+      const int r = (int)(e / R), c = (int)(e - (int64_t)r * R);
+      double gm = a.lam[r] * a.lam[c];
+      for (int m = 0; m < a.order; ++m) gm *= a.G[m][e];
+      self = gm;
+      if (has_prev) inner = a.prevLam[sel][r] * h * a.lam[c];
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      inner += __shfl_xor_sync(0xffffffffu, inner, off);
+      self += __shfl_xor_sync(0xffffffffu, self, off);
+    }
+    if (j == 0) {
+      a.red[2 * blockIdx.x] = inner;
+      a.red[2 * blockIdx.x + 1] = self;
+      __threadfence();
+      s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+    }
   }
   __syncthreads();
   if (!s_last) return;
@@ -212,20 +220,23 @@ __global__ void __launch_bounds__(256) k_cp_check(CrossArgs a) {
 
 }  // namespace
 
-int cross_splits(int order, int R, int num_sms) {
-  const int nt = (R + XT - 1) / XT;
-  const int per = order * nt * nt;
-  const int s = (2 * num_sms + per - 1) / per;
-  return s < 1 ? 1 : (s > 64 ? 64 : s);
+int64_t cross_rows(int order, const int64_t* dims, int R, int num_sms) {
+  const int64_t nt = (R + XT - 1) / XT;
+  int64_t units = 0;  // rows x tiles over all modes
+  for (int m = 0; m < order; ++m) units += dims[m] * nt * nt;
+  const int64_t target = 6 * (int64_t)num_sms;
+  int64_t rows = (units + target - 1) / target;
+  rows = (rows + XK - 1) / XK * XK;
+  return rows < XK ? XK : rows;
 }
 
 cudaError_t launch_cp_check(const CrossArgs& a, cudaStream_t st) {
   const int nt = (a.R + XT - 1) / XT;
-  k_cross_gram<<<dim3(a.S, nt * nt, a.order), 256, 0, st>>>(a);
+  k_cross_gram<<<dim3(a.Smax, nt * nt, a.order), 256, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int64_t RR = (int64_t)a.R * a.R;
-  k_cp_check<<<(unsigned)((RR + 255) / 256), 256, 0, st>>>(a);
+  k_cp_check<<<(unsigned)((RR + 31) / 32), 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -7,6 +7,7 @@ include/cpals.h); this package is the host side that mirrors the reference's
 """
 from ._lib import CpalsError, load
 from .api import (
+    BlockLevScoreSampled,
     CPD,
     CPAngleCheck,
     CPDFit,
@@ -26,6 +27,7 @@ from .api import (
     increase_cpd_rank,
     random_CPD,
     random_factors,
+    block_sample_factor_matrices,
     sample_factor_matrices,
 )
 from .batched import BatchEngine
@@ -34,7 +36,7 @@ from . import warmstart
 from .warmstart import WarmStartMLP
 
 __all__ = [
-    "BatchEngine", "CPAngleCheck", "CPD", "CPDFit", "CPDiffCheck", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
+    "BatchEngine", "BlockLevScoreSampled", "CPAngleCheck", "CPD", "CPDFit", "CPDiffCheck", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
     "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
-    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "WarmStartMLP", "warmstart",
+    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "block_sample_factor_matrices", "WarmStartMLP", "warmstart",
 ]

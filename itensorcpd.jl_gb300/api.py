@@ -178,6 +178,26 @@ class LevScoreSampled(ProjectionAlgorithm):
     def nsamples(self, mode: int) -> int:
         return self.NSamples[0] if len(self.NSamples) == 1 else self.NSamples[mode]
 
+    def sample(self, mode: int, probs, rng) -> np.ndarray:
+        """project_krp's draw (randomized/krp_lev_score_sampled.jl:20-37)."""
+        return sample_factor_matrices(self.nsamples(mode), mode, probs, rng)
+
+
+class BlockLevScoreSampled(LevScoreSampled):
+    """randomized/krp_lev_score_sampled.jl:64-77: leverage-score sampling that draws runs of
+    ``Blocks`` consecutive indices of the first sampled mode (an int or a per-mode tuple)."""
+
+    def __init__(self, n=0, m=1):
+        super().__init__(n)
+        self.Blocks = tuple(m) if isinstance(m, (tuple, list)) else (int(m),)
+
+    def blocks(self, mode: int) -> int:
+        return self.Blocks[0] if len(self.Blocks) == 1 else self.Blocks[mode]
+
+    def sample(self, mode: int, probs, rng) -> np.ndarray:
+        """project_krp of BlockLevScoreSampled (randomized/krp_lev_score_sampled.jl:80-98)."""
+        return block_sample_factor_matrices(self.nsamples(mode), probs, self.blocks(mode), mode, rng)
+
 
 # ---------------------------------------------------------------------------
 # Initial guesses (src/cpd.jl:85-119)
@@ -333,7 +353,9 @@ def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=Fa
     check = NoCheck(100 if maxiter is None else maxiter) if check is None else check
     R = cp_rank(cp)
     if isinstance(alg, ProjectionAlgorithm):
-        return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal)
+        return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal,
+                                   stop_resample=int(kwargs.get("stop_resample", -1)),
+                                   on_pivots=kwargs.get("on_pivots"))
     with Engine(T.shape, R, dtype=T.dtype, precision=alg.precision, device=device, dimtree=alg.dimtree) as eng:
         eng.set_tensor(T)
         eng.set_factors(cp.factors, cp.lam)
@@ -362,10 +384,61 @@ def sample_factor_matrices(nsamps, skip, probs, rng):
     return np.asfortranarray(np.stack(cols, axis=1).astype(np.int64))
 
 
-def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal):
-    """LevScoreSampled: compute_als (optimizers/.../krp_lev_score_sampled.jl:1-40) and the
-    per-mode project_krp / matricize_tensor / solve / post_solve of
-    algorithms/.../randomized/krp_lev_score_sampled.jl:87-125, resampling every mode."""
+def _draw(p, size, rng):
+    w = np.abs(p)
+    return rng.choice(len(p), size=size, p=w / w.sum()) + 1
+
+
+def block_sample_factor_matrices(nsamps, probs, block_size, skip, rng):
+    """probability.jl:61-108: the first sampled mode (mode 0, or mode 1 when ``skip`` is 0)
+    is cut into floor(I / block_size) blocks, the first I mod block_size of them one index
+    longer, each weighted by its summed probability.  For each of nsamps // block_size
+    draws, a block is drawn and expanded into consecutive rows that share one independent
+    draw of the other modes; rows past nsamps are dropped, and rows the blocks leave empty
+    get independent draws of every mode.  Returns nsamps x (N-1) 1-based indices, in the
+    column order of ``sample_factor_matrices``.  Draws stay on the host."""
+    N = len(probs)
+    block_size = int(block_size)
+    if block_size < 1:
+        raise ValueError("block size must be positive")
+    bf = 1 if skip == 0 else 0
+    others = [m for m in range(N) if m != skip and m != bf]
+    fast = np.abs(np.asarray(probs[bf], dtype=np.float64))
+    nblocks, resid = divmod(len(fast), block_size)
+    lens = np.array([block_size + (i < resid) for i in range(nblocks)], dtype=np.int64)
+    starts = np.concatenate([[1], 1 + np.cumsum(lens)]).astype(np.int64)  # 1-based block starts
+    bprob = np.array([fast[starts[i] - 1:starts[i + 1] - 1].sum() for i in range(nblocks)])
+    n_iter = nsamps // block_size
+    out = np.empty((nsamps, N - 1), dtype=np.int64)
+    m = 0
+    if n_iter > 0:
+        if nblocks == 0:
+            raise ValueError("block size exceeds the extent of the blocked mode")
+        other_draws = [_draw(probs[o], n_iter, rng) for o in others]
+        blk = rng.choice(nblocks, size=n_iter, p=bprob / bprob.sum())
+        for i in range(n_iter):
+            if m >= nsamps:
+                break
+            b = blk[i]
+            cnt = min(int(lens[b]), nsamps - m)
+            out[m:m + cnt, 0] = starts[b] + np.arange(cnt)
+            for j, d in enumerate(other_draws):
+                out[m:m + cnt, j + 1] = d[i]
+            m += cnt
+    if m < nsamps:
+        tail = nsamps - m
+        for j, mode in enumerate([bf] + others):
+            out[m:, j] = _draw(probs[mode], tail, rng)
+    return np.asfortranarray(out)
+
+
+def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal, stop_resample=-1, on_pivots=None):
+    """LevScoreSampled / BlockLevScoreSampled: compute_als (optimizers/.../krp_lev_score_sampled.jl:1-40,
+    42-80: initial leverage weights and one draw per mode) and the per-mode project_krp /
+    matricize_tensor / solve / post_solve of algorithms/.../randomized/krp_lev_score_sampled.jl:20-58,
+    80-106.  A mode draws new pivots while stop_resample < 0 or stop_resample > iter(als)
+    (the check's iteration count); otherwise it reuses its last pivots.  ``on_pivots(mode,
+    pivots)`` (optional) sees every mode's pivots before its solve."""
     rng = np.random.default_rng(3) if rng is None else rng
     R = cp_rank(cp)
     N = T.ndim
@@ -378,15 +451,21 @@ def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal):
         eng.set_tensor(T)
         eng.set_factors(cp.factors, cp.lam)
         probs = [eng.leverage_scores(n) for n in range(N)]
+        pivots = [alg.sample(n, probs, rng) for n in range(N)]
         if cross:  # ProjectionAlgorithm.jl:53: these checks run as for the exact solvers
             c = _to_device_check(check)
             _prev_in(eng, check)
             first = check.lastangle if isinstance(check, CPAngleCheck) else check.lastfit
             traj = []
         for s in range(sweeps):
+            it = int(c.iter) if cross else int(check.iter) + s
+            resample = stop_resample < 0 or stop_resample > it
             for n in range(N):
-                piv = sample_factor_matrices(alg.nsamples(n), n, probs, rng)
-                eng.sampled_update(n, piv, normal=normal)
+                if resample:
+                    pivots[n] = alg.sample(n, probs, rng)
+                if on_pivots is not None:
+                    on_pivots(n, pivots[n])
+                eng.sampled_update(n, pivots[n], normal=normal)
                 probs[n] = eng.leverage_scores(n)
             if cross:
                 done, val = eng.check_converge(c)

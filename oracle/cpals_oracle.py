@@ -502,6 +502,53 @@ def sample_factor_matrices(nsamps, skip, probs, rng: np.random.Generator) -> np.
     return np.stack(cols, axis=1).astype(np.int64)
 
 
+def block_sample_factor_matrices(nsamps, probs, block_size, skip, rng) -> np.ndarray:
+    """probability.jl:61-108, loop for loop (1-based output, ``skip`` 0-based).
+
+    The blocked mode is the first sampled one.  Its indices are cut into
+    nblocks = I // block_size blocks, the first I % block_size one longer
+    (probability.jl:71-82); each of nsamps // block_size iterations draws the other modes
+    once (sample_single_col_from_factors, :17-19) and one block, and writes the block's
+    consecutive indices with those draws until nsamps rows are written (:86-100); rows left
+    empty get independent draws of every sampled mode (:101-105)."""
+    N = len(probs)
+    sampled = np.zeros((nsamps, N - 1), dtype=np.int64)
+    bf = 1 if skip == 0 else 0
+    blocked = np.abs(np.asarray(probs[bf], dtype=np.float64))
+    size_fast = len(blocked)
+    nblocks, resid = size_fast // block_size, size_fast % block_size
+    block_prob, block_starts = [], [1]
+    m = 1
+    for i in range(1, nblocks + 1):
+        ln = block_size + (1 if i <= resid else 0)
+        block_prob.append(blocked[m - 1:m - 1 + ln].sum())
+        m += ln
+        block_starts.append(m)
+
+    def draw(p):
+        w = np.abs(p) / np.sum(np.abs(p))
+        return int(rng.choice(len(p), p=w)) + 1
+
+    def single_col():
+        return [draw(probs[k]) for k in range(N) if k != skip]
+
+    m = 1
+    for _ in range(nsamps // block_size):
+        other = single_col()
+        bp = np.array(block_prob)
+        b = int(rng.choice(len(bp), p=bp / bp.sum())) + 1
+        start, end = block_starts[b - 1], block_starts[b]
+        for j in range(1, end - start + 1):
+            if m > nsamps:
+                m += 1
+                break
+            sampled[m - 1, :] = [start + j - 1] + other[1:]
+            m += 1
+    for i in range(m, nsamps + 1):
+        sampled[i - 1, :] = single_col()
+    return sampled
+
+
 def sampled_solve(S: np.ndarray, Ts: np.ndarray, normal: bool):
     """solve_ls_problem(::ProjectionAlgorithm), randomized/ProjectionAlgorithm.jl:57-68.
 
@@ -515,18 +562,22 @@ def sampled_solve(S: np.ndarray, Ts: np.ndarray, normal: bool):
     return Xt.T.copy()
 
 
-def lev_score_als(T, factors, lam, nsamps, sweeps, rng, normal=False, record=None):
+def lev_score_als(T, factors, lam, nsamps, sweeps, rng, normal=False, record=None, block_size=None):
     """LevScoreSampled path: optimizers/.../randomized/krp_lev_score_sampled.jl:1-40 and
     algorithms/.../randomized/krp_lev_score_sampled.jl:20-58 (resample every mode, stop_resample = -1),
     run for a fixed number of sweeps (a FitCheck is not honoured, ProjectionAlgorithm.jl:30-51).
     ``record`` receives the per-mode pivots so a device run can replay them.
+    ``block_size`` switches to BlockLevScoreSampled's draw (probability.jl:61-108).
     """
     factors = [np.array(F, dtype=np.float64) for F in factors]
     N = T.ndim
     probs = [leverage_score_probabilities(F) for F in factors]
     for _ in range(sweeps):
         for n in range(N):
-            piv = sample_factor_matrices(nsamps, n, probs, rng)
+            if block_size is None:
+                piv = sample_factor_matrices(nsamps, n, probs, rng)
+            else:
+                piv = block_sample_factor_matrices(nsamps, probs, block_size, n, rng)
             others = [factors[m] for m in range(N) if m != n]
             S = pivot_hadamard(others, piv)
             Ts = fused_flatten_sample(T, n, piv)

@@ -251,8 +251,10 @@ def test_lev_score_sampled_api(built, oracle):
     dims = (12, 13, 3)
     Ft, lt = det_factors(dims, 5, seed=31)
     T = np.asfortranarray(oracle.reconstruct(Ft, lt))
+    # best of five tries (the reference's multiple_tries helper, rand_cp_als.jl:1-14): from
+    # this start a sampled run often stalls near 0.12, as the oracle's runs do
     best = 1.0
-    for trial in range(3):
+    for trial in range(5):
         cp = built.CPD(*det_factors(dims, 5, seed=32))
         opt = built.als_optimize(T, cp, alg=built.LevScoreSampled(100), check=built.NoCheck(100), normal=True,
                                  rng=np.random.default_rng(100 + trial))

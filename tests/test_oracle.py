@@ -229,3 +229,72 @@ def test_diff_check_resets_at_max_counter(oracle):
         assert chk.check_converge(F, lam) is False
     assert chk.iter == 0 and chk.total_iter == 3 and chk.PrevCP is None and chk.lastfit == 0.0
     assert chk.final_fit == chk.trajectory[-1]
+
+
+@pytest.mark.parametrize("impl", ["api", "oracle"])
+def test_block_sampling_structure_and_block_weights(oracle, pkg, impl):
+    # probability.jl:61-108 with I = 13 and block_size 5: two blocks of 6 (13 // 5 = 2,
+    # 13 % 5 = 3 > 2 so both are one longer), starting at 1 and 7; index 13 is never drawn
+    # inside a block.  Block draws follow the summed leverage weights of each block.
+    rng = np.random.default_rng(9)
+    probs = [np.abs(rng.standard_normal(d)) for d in (13, 9, 4)]
+    sampler = pkg.block_sample_factor_matrices if impl == "api" else oracle.block_sample_factor_matrices
+    nsamps, b = 6000, 5
+    S = sampler(nsamps, probs, b, 2, np.random.default_rng(1))  # skip mode 2: mode 0 is blocked
+    assert S.shape == (nsamps, 2) and S.dtype == np.int64
+    assert S[:, 0].min() >= 1 and S[:, 0].max() <= 13 and S[:, 1].min() >= 1 and S[:, 1].max() <= 9
+    w = probs[0] / probs[0].sum()
+    bprob = np.array([w[0:6].sum(), w[6:12].sum()])
+    starts = []
+    # 6000 // 5 = 1200 block draws of 6 rows each overflow nsamps after 1000 blocks
+    i = 0
+    while i < nsamps:
+        s0 = S[i, 0]
+        assert s0 in (1, 7)
+        n = min(6, nsamps - i)
+        np.testing.assert_array_equal(S[i:i + n, 0], s0 + np.arange(n))
+        assert np.all(S[i:i + n, 1] == S[i, 1])
+        starts.append(s0)
+        i += n
+    assert len(starts) == 1000
+    freq = np.mean(np.array(starts) == 1)
+    assert abs(freq - bprob[0]) < 4 * np.sqrt(bprob[0] * bprob[1] / len(starts))
+
+
+@pytest.mark.parametrize("impl", ["api", "oracle"])
+def test_block_sampling_fills_the_tail_with_independent_draws(oracle, pkg, impl):
+    # block size 4 on a mode of 10: 10 // 4 = 2 blocks, 10 % 4 = 2 so both have 5 indices
+    # (starts 1 and 6).  nsamps 11 gives 11 // 4 = 2 block draws, i.e. rows 1-5 and 6-10,
+    # and row 11 is an independent draw.  nsamps below the block size gives only
+    # independent draws.
+    probs = [np.ones(10), np.ones(6), np.ones(3)]
+    sampler = pkg.block_sample_factor_matrices if impl == "api" else oracle.block_sample_factor_matrices
+    S = sampler(11, probs, 4, 1, np.random.default_rng(2))  # skip mode 1: mode 0 is blocked
+    for r0 in (0, 5):
+        assert S[r0, 0] in (1, 6)
+        np.testing.assert_array_equal(S[r0:r0 + 5, 0], S[r0, 0] + np.arange(5))
+        assert np.all(S[r0:r0 + 5, 1] == S[r0, 1])
+    assert 1 <= S[10, 0] <= 10 and 1 <= S[10, 1] <= 3
+    S = sampler(3, probs, 4, 0, np.random.default_rng(3))  # skip mode 0: mode 1 is blocked
+    assert S.shape == (3, 2) and S[:, 0].max() <= 6 and S[:, 1].max() <= 3
+
+
+def test_block_sampling_rejects_blocks_longer_than_the_mode(pkg):
+    with pytest.raises(ValueError):
+        pkg.block_sample_factor_matrices(20, [np.ones(3), np.ones(4), np.ones(5)], 5, 2, np.random.default_rng(0))
+    with pytest.raises(ValueError):
+        pkg.block_sample_factor_matrices(20, [np.ones(3), np.ones(4)], 0, 1, np.random.default_rng(0))
+
+
+def test_block_lev_score_sampled_converges(oracle):
+    # test/rand_cp_als.jl:219-225: BlockLevScoreSampled(100, 1) and (100, 3) on the exact
+    # rank-5 12x13x3 target reach a relative error below 0.1 (best of three tries, 100 sweeps)
+    dims = (12, 13, 3)
+    Ft, lt = det_factors(dims, 5, seed=31)
+    T = np.asfortranarray(oracle.reconstruct(Ft, lt))
+    F, lam = det_factors(dims, 5, seed=32)
+    for b in (1, 3):
+        best = min(np.linalg.norm(oracle.reconstruct(*oracle.lev_score_als(
+            T, F, lam, 100, 100, np.random.default_rng(100 + t), normal=True, block_size=b)) - T) / np.linalg.norm(T)
+            for t in range(3))
+        assert best < 0.1

@@ -101,6 +101,12 @@ int cpals_set_tensor(cpals_ctx* ctx, const void* host_tensor);
 /* Use a column-major tensor already resident on the handle's device (borrowed). */
 int cpals_set_tensor_device(cpals_ctx* ctx, const void* device_tensor);
 
+/* The device copy of the target the handle uses (owned or borrowed), for another handle's
+ * cpals_set_tensor_device: the rank-adaptive decompose (decompose.jl:32-69) runs one
+ * handle per rank on one upload.  The pointer lives as long as this handle (owned) or the
+ * caller's buffer (borrowed).  CPALS_E_STATE before a tensor is set. */
+int cpals_tensor_device(cpals_ctx* ctx, const void** device_tensor);
+
 /* Copy factors (each I_n x R column-major) and lambda (R) in / out.  Setting
  * factors also recomputes the Grams, as compute_als does
  * (optimizers/als_optimizers/standard/tensor.jl:3-14). */

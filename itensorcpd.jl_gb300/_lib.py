@@ -60,6 +60,7 @@ SIGNATURES = {
     "cpals_destroy": (C.c_int, [_P]),
     "cpals_set_tensor": (C.c_int, [_P, _P]),
     "cpals_set_tensor_device": (C.c_int, [_P, _P]),
+    "cpals_tensor_device": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "cpals_set_factors": (C.c_int, [_P, C.POINTER(_DP), _DP]),
     "cpals_get_factors": (C.c_int, [_P, C.POINTER(_DP), _DP]),
     "cpals_get_gram": (C.c_int, [_P, C.c_int, _DP]),

@@ -356,8 +356,12 @@ def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=Fa
         return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal,
                                    stop_resample=int(kwargs.get("stop_resample", -1)),
                                    on_pivots=kwargs.get("on_pivots"))
+    source = kwargs.get("tensor_source")  # an Engine holding T on the device (decompose's rank loop)
     with Engine(T.shape, R, dtype=T.dtype, precision=alg.precision, device=device, dimtree=alg.dimtree) as eng:
-        eng.set_tensor(T)
+        if source is not None:
+            eng.set_tensor_from(source)
+        else:
+            eng.set_tensor(T)
         eng.set_factors(cp.factors, cp.lam)
         c = _to_device_check(check)
         _prev_in(eng, check)
@@ -504,15 +508,26 @@ def decompose(A, rank, max_rank=None, *, solver=None, rng=None, alg=None, check=
     current = int(start_rank)
     cpd = random_CPD(T, current, rng)
     check = FitCheck(1e-3, 100, float(np.linalg.norm(T))) if check is None else check
-    while True:
-        cpd = als_optimize(T, cpd, alg=alg, check=check, maxiter=maxiter, verbose=verbose, rng=rng, **kwargs)
-        check.iter = 0
-        if 1.0 - CPDFit(check) < epsilon:
-            return cpd
-        current += int(rank_step)
-        if verbose:
-            print(f"\nIncreasing rank to: {current}")
-        if current > int(max_rank):
-            print(f"Optimization Failed to converge within rank {max_rank}")
-            return cpd
-        cpd = increase_cpd_rank(cpd, current, rng)
+    # one upload of T for every rank: a rank-1 handle owns the device copy and each rank's
+    # handle borrows it (the sampled solvers build their own)
+    holder = None
+    if not isinstance(alg, ProjectionAlgorithm):
+        holder = Engine(T.shape, 1, dtype=T.dtype, precision="fp64", device=kwargs.get("device", 0))
+        holder.set_tensor(T)
+        kwargs = dict(kwargs, tensor_source=holder)
+    try:
+        while True:
+            cpd = als_optimize(T, cpd, alg=alg, check=check, maxiter=maxiter, verbose=verbose, rng=rng, **kwargs)
+            check.iter = 0
+            if 1.0 - CPDFit(check) < epsilon:
+                return cpd
+            current += int(rank_step)
+            if verbose:
+                print(f"\nIncreasing rank to: {current}")
+            if current > int(max_rank):
+                print(f"Optimization Failed to converge within rank {max_rank}")
+                return cpd
+            cpd = increase_cpd_rank(cpd, current, rng)
+    finally:
+        if holder is not None:
+            holder.close()

@@ -641,6 +641,13 @@ int cpals_set_tensor_device(cpals_ctx* c, const void* device_tensor) {
   return CPALS_OK;
 }
 
+int cpals_tensor_device(cpals_ctx* c, const void** device_tensor) {
+  if (!c || !device_tensor) return CPALS_E_ARG;
+  if (!c->T_set || !c->dT) return CPALS_E_STATE;
+  *device_tensor = c->dT;
+  return CPALS_OK;
+}
+
 int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const double* host_lambda) {
   if (!c || !host_factors) return CPALS_E_ARG;
   DeviceGuard g(c->device);

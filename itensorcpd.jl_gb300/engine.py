@@ -64,6 +64,18 @@ class Engine:
         self._tensor_ref = keepalive
         L.check(self.lib.cpals_set_tensor_device(self.h, C.c_void_p(int(ptr))), "cpals_set_tensor_device")
 
+    def tensor_device_ptr(self) -> int:
+        """Device address of the tensor this handle uses."""
+        ptr = C.c_void_p()
+        L.check(self.lib.cpals_tensor_device(self.h, C.byref(ptr)), "cpals_tensor_device")
+        return int(ptr.value)
+
+    def set_tensor_from(self, other: "Engine"):
+        """Borrow ``other``'s device tensor (same extents and element type): no host copy."""
+        if other.dims != self.dims or other.dtype != self.dtype:
+            raise ValueError("the source handle holds a tensor of another shape or element type")
+        self.set_tensor_device(other.tensor_device_ptr(), keepalive=other)
+
     def set_factors(self, factors, lam=None):
         fs = [np.asfortranarray(F, dtype=np.float64) for F in factors]
         for F, d in zip(fs, self.dims):

@@ -170,6 +170,36 @@ def test_decompose_api_and_rank_adaptive(built, oracle):
         built.decompose(T, 3, solver=object())
 
 
+def test_rank_adaptive_decompose_uploads_once(built, oracle):
+    """decompose.jl:32-69 on one device copy of T: every rank's handle borrows it, and the
+    result equals a loop of als_optimize / increase_cpd_rank that uploads T per rank."""
+    F, _ = det_factors((16, 15, 14), 4, seed=13)
+    T = np.asfortranarray(oracle.reconstruct(F, np.array([4.0, 3.0, 2.0, 1.0])).astype(np.float32))
+    nrm = float(np.linalg.norm(T))
+    cp = built.decompose(T, 1e-4, 5, check=built.FitCheck(1e-7, 60, nrm), start_rank=2,
+                         rng=np.random.default_rng(5), alg=built.GB300Normal())
+    rng = np.random.default_rng(5)
+    chk = built.FitCheck(1e-7, 60, nrm)
+    ref = built.random_CPD(T, 2, rng)
+    for r in range(2, 6):
+        ref = built.als_optimize(T, ref, alg=built.GB300Normal(), check=chk, rng=rng)
+        chk.iter = 0
+        if 1.0 - built.CPDFit(chk) < 1e-4 or r == 5:
+            break
+        ref = built.increase_cpd_rank(ref, r + 1, rng)
+    assert built.cp_rank(cp) == built.cp_rank(ref)
+    for a, b in zip(cp.factors, ref.factors):
+        np.testing.assert_array_equal(a, b)
+    # the borrowed pointer is the owner's
+    with built.Engine(T.shape, 1, dtype=np.float32) as owner, built.Engine(T.shape, 3, dtype=np.float32,
+                                                                            precision="bf16x3") as e:
+        with pytest.raises(built.CpalsError):
+            owner.tensor_device_ptr()  # no tensor yet
+        owner.set_tensor(T)
+        e.set_tensor_from(owner)
+        assert e.tensor_device_ptr() == owner.tensor_device_ptr()
+
+
 # ---------------- randomized path: bit-exact gathers ----------------
 @pytest.mark.parametrize("dims,mode", [((100, 150, 200), 0), ((100, 150, 200), 2), ((5, 6, 7, 8), 1),
                                        ((9, 4), 1)])

@@ -535,125 +535,136 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 }
 
 // ---------------- FP32 sweep (split-BF16 path) ----------------
-// The same pivoted symmetric sweep in FP32 (this part issues FP32 FMAs at 64x its FP64
+// A pivoted symmetric sweep in FP32 (this part issues FP32 FMAs at 64x its FP64
 // rate, with ~4-cycle latency).  V is formed in FP64 exactly as above and kept in the
 // workspace; W = -A is the FP32 inverse.  The solve then refines X once with the FP64
 // residual (mixed-precision iterative refinement: X += (M - X V) W), which brings X to FP64
 // accuracy while kappa(V) eps_32 << 1.  A pivot below 1e-3 of the largest diagonal entry (or
 // a NaN, or a rank below R) leaves info->refine = 0 and the FP64 sweep takes over.
-__device__ __forceinline__ int fkey(float v) {
-  const int k = __float_as_int(v);
-  return (k & 0x7fffffff) > 0x7f800000 ? INT_MAX : k;
-}
 
-constexpr int FT32 = 512;    // FP32 sweep threads
-constexpr int kEnt32 = 24;   // entries per update thread (12 update warps, R <= 128)
+// Layout and schedule.  The symmetric A lives in registers: thread t of warps 0-3 holds
+// columns 4 (t >> 2) .. + 3, rows 32 (t & 3) .. + 31 (both triangles).  The sweep keeps A
+// exactly symmetric by updating with u = a sqrt(1 / d_k) (a = column k, d_k the pivot):
+//   A(i,c) -= u_i u_c  for i, c != k;  with u_k = (1 - 1/d_k) / sqrt(1/d_k) the same FMA
+// leaves A(i,k) = a_i / d_k and A(k,c) = a_c / d_k (Gauss-Jordan form); the pivot's own
+// entry, -1 / d_k, and every diagonal entry are tracked by warp 4 in s_d.  Per pivot: the
+// four owners of column k publish u (a uniform switch picks the column: no dynamic register
+// indexing) -> barrier -> owners update their 128 entries; warp 4 updates the diagonal and
+// picks the next pivot -> barrier.  The pivot is the largest unswept diagonal entry, the
+// lowest index among values equal to 2^-16 relative (a packed key, one warp max); any choice
+// is fine here because the solve refines X in FP64, and a pivot below 1e-3 of the largest
+// diagonal entry hands the factorisation to the FP64 sweep.  Warps 5-7 help form V and
+// write W.  (A probe of this schedule on one SM: 0.84 k cycles per pivot at R = 128, the
+// earlier one-entry-per-thread sweep 2.6 k.)
+constexpr int FT32 = 256;
+constexpr int kOwnWarps32 = 4, kPivWarp32 = 4;
+__device__ __forceinline__ int pivot_key(float v, int i) {
+  const int b = __float_as_int(v);
+  if ((b & 0x7fffffff) > 0x7f800000) return INT_MAX;  // NaN first: it stops the sweep
+  return (b & ~0x7f) | (127 - i);
+}
+__device__ __forceinline__ int upad(int i) { return i + 4 * (i >> 5); }  // row quarters 36 floats apart
+template <int C>
+__device__ __forceinline__ void publish_u(const float (&acc)[4][32], float sc, float* s_u, int qr) {
+  float4* dst = reinterpret_cast<float4*>(s_u + 36 * qr);
+#pragma unroll
+  for (int v = 0; v < 8; ++v)
+    dst[v] = make_float4(acc[C][4 * v] * sc, acc[C][4 * v + 1] * sc, acc[C][4 * v + 2] * sc, acc[C][4 * v + 3] * sc);
+}
 __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int skip, int R, double* __restrict__ Vg,
                                                       double* __restrict__ W, SolveInfo* info, DevCheck* chk) {
   if (done_flag(chk)) return;
   extern __shared__ float smF[];
   const int ld = R | 1;
   float* A = smF;
-  __shared__ float s_a[128], s_t[128];
-  __shared__ unsigned char s_swept[128];
-  __shared__ float s_pv, s_pinv, s_maxd, s_minp;
+  __shared__ __align__(16) float s_u[144];
+  __shared__ __align__(16) float s_d[128];
+  __shared__ float s_uk, s_sc;
   __shared__ int s_p, s_stop;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int e0 = tid; e0 < R * R; e0 += 8 * FT32) {
-    double v[8];
+  // V = Hadamard product of the other modes' Grams (FP64, in mode order); every mode's
+  // loads are issued before the products
+  for (int e0 = tid; e0 < R * R; e0 += 4 * FT32) {
+    double g[kMaxOrder][4];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] = 1.0;
-    for (int m = 0; m < order; ++m) {
-      if (m == skip) continue;
-      const double* __restrict__ G = gs.G[m];
+    for (int m = 0; m < kMaxOrder; ++m) {
+      const bool use = (m < order) && (m != skip);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
+      for (int q = 0; q < 4; ++q) {
         const int e = e0 + q * FT32;
-        if (e < R * R) v[q] *= G[e];
+        g[m][q] = (use && e < R * R) ? gs.G[m][e] : 1.0;
       }
     }
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < 4; ++q) {
       const int e = e0 + q * FT32;
+      double v = 1.0;
+#pragma unroll
+      for (int m = 0; m < kMaxOrder; ++m) v *= g[m][q];
       if (e < R * R) {
         const int r = e / R, c = e - r * R;
-        Vg[e] = v[q];  // FP64 V (symmetric) for the refinement
-        if (c >= r) A[r * ld + c] = (float)v[q];
+        Vg[e] = v;  // FP64 V (symmetric) for the refinement
+        if (c >= r) A[r * ld + c] = (float)v;
       }
     }
   }
-  for (int k = tid; k < R; k += blockDim.x) s_swept[k] = 0;
+  for (int k = tid; k < 144; k += blockDim.x) {
+    s_u[k] = 0.f;
+    if (k < 128) s_d[k] = 0.f;
+  }
   __syncthreads();
-  auto pick = [&](int bk, int bi) {
-    const int mk = __reduce_max_sync(0xffffffffu, bk);
-    const int p = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+  const int cg = tid >> 2, qr = tid & 3;
+  const bool own = warp < kOwnWarps32 && 4 * cg < R && 32 * qr < R;
+  float acc[4][32];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int i = 32 * qr + j, col = 4 * cg + c;
+      acc[c][j] = (own && i < R && col < R) ? ((i <= col) ? A[i * ld + col] : A[col * ld + i]) : 0.f;
+    }
+  // warp 4: diagonal entries 4 lane .. 4 lane + 3 (registers and s_d), swept flags, pivot
+  unsigned swept = 0;
+  float r_dk = 0.f, r_maxd = 0.f;
+  auto pick = [&](const float* dv) {
+    int best = INT_MIN;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = 4 * lane + q;
+      const int key = (i < R && !((swept >> q) & 1u)) ? pivot_key(dv[q], i) : INT_MIN;
+      best = max(best, key);
+    }
+    const int mk = __reduce_max_sync(0xffffffffu, best);
+    const int p = (mk == INT_MAX || mk == INT_MIN) ? 0 : 127 - (mk & 0x7f);
+    const int q = p & 3;
+    const float mine = (q == 0) ? dv[0] : (q == 1) ? dv[1] : (q == 2) ? dv[2] : dv[3];
+    const float pv = __shfl_sync(0xffffffffu, mine, p >> 2);
+    const int stop = (mk == INT_MAX) || (mk == INT_MIN) || !(pv > 1e-3f * r_maxd) || p >= R;
+    const float sc = rsqrtf(pv);  // sqrt(1 / d_k)
+    const float dk = sc * sc;
+    r_dk = dk;
     if (lane == 0) {
-      const float pv = __int_as_float(mk);
-      const int stop = (mk == INT_MAX) || !(pv > 1e-3f * s_maxd) || p >= R;
       s_stop = stop;
       s_p = p;
-      if (!stop) {
-        s_pv = pv;
-        s_pinv = 1.0f / pv;
-        s_minp = fminf(s_minp, pv);
-      }
+      s_sc = sc;
+      s_uk = (1.0f - dk) * pv * sc;  // (1 - 1/d_k) / sqrt(1/d_k)
     }
-    __syncwarp();
   };
-  if (warp == 0) {
-    int bk = INT_MIN, bi = R;
+  if (warp == kPivWarp32) {
+    float dv[4];
     float md = 0.f;
-    for (int i = lane; i < R; i += 32) {
-      const float d = A[i * ld + i];
-      md = fmaxf(md, d);
-      const int key = fkey(d);
-      if (bi == R || key > bk) {
-        bk = key;
-        bi = i;
-      }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = 4 * lane + q;
+      dv[q] = (i < R) ? A[i * ld + i] : 0.f;
+      s_d[i] = dv[q];
+      md = fmaxf(md, dv[q]);
     }
     for (int off = 16; off > 0; off >>= 1) md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, off));
-    if (lane == 0) {
-      s_maxd = md;
-      s_minp = INFINITY;
-    }
-    __syncwarp();
-    pick(bk, bi);
+    r_maxd = md;
+    pick(dv);
   }
   __syncthreads();
-  // The sweep updates the same strictly-upper entries at every step, so each update thread
-  // (warps on schedulers 1-3, warp % 4 != 0: warp 0's look-ahead has scheduler 0 to itself)
-  // decodes its entries once: rows paired as in the FP64 sweep, entry f of the flattened
-  // (R-1) x (R-1) upper triangle, f = ut, ut + nut, ...; packed as (i << 16) | c.
-  const bool upd = (warp & 3) != 0;
-  const int ut = (warp >> 2) * 96 + ((warp & 3) - 1) * 32 + lane;  // 0 .. 383
-  const int nut = (FT32 >> 5) / 4 * 3 * 32;
-  int ent[kEnt32];
-  int nent = 0;
-  {
-    const int m = R - 1;
-    const int cnt = m * (m + 1) / 2;
-#pragma unroll
-    for (int q = 0; q < kEnt32; ++q) {
-      ent[q] = -1;
-      const int f = ut + q * nut;
-      if (upd && f < cnt) {
-        const int pq = f / R, t = f - pq * R;
-        int i, c;
-        if (t < R - 1 - pq) {
-          i = pq;
-          c = pq + 1 + t;
-        } else {
-          i = R - 2 - pq;
-          c = i + 1 + (t - (R - 1 - pq));
-        }
-        if (!(t >= R - 1 - pq && i == pq)) {  // the middle row of an even R is listed once
-          ent[q] = (i << 16) | c;
-          nent = q + 1;
-        }
-      }
-    }
-  }
   int ok = 1;
   for (int j = 0; j < R; ++j) {
     if (s_stop) {
@@ -661,61 +672,45 @@ __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int
       break;
     }
     const int k = s_p;
-    const float dk = s_pinv;
-    for (int i = tid; i < R; i += blockDim.x) {
-      const float a = (i <= k) ? A[i * ld + k] : A[k * ld + i];
-      s_a[i] = a;
-      s_t[i] = a * dk;
+    if (own && cg == (k >> 2)) {  // publish u for column k
+      const float sc = s_sc;
+      switch (k & 3) {
+        case 0: publish_u<0>(acc, sc, s_u, qr); break;
+        case 1: publish_u<1>(acc, sc, s_u, qr); break;
+        case 2: publish_u<2>(acc, sc, s_u, qr); break;
+        default: publish_u<3>(acc, sc, s_u, qr); break;
+      }
+      if ((k >> 5) == qr) s_u[upad(k)] = s_uk;
     }
     __syncthreads();
-    if (warp == 0) {
-      if (tid == 0) s_swept[k] = 1;
-      int bk = INT_MIN, bi = R;
-      for (int i = lane; i < R; i += 32) {
-        if (i == k) {
-          A[i * ld + i] = -dk;
-          continue;
-        }
-        const float v = fmaf(-s_a[i], s_t[i], A[i * ld + i]);
-        A[i * ld + i] = v;
-        if (!s_swept[i]) {
-          const int key = fkey(v);
-          if (bi == R || key > bk) {
-            bk = key;
-            bi = i;
-          }
+    if (own) {
+      const float4 uc = *reinterpret_cast<const float4*>(s_u + upad(4 * cg));
+      const float ucs[4] = {uc.x, uc.y, uc.z, uc.w};
+      const float4* src = reinterpret_cast<const float4*>(s_u + 36 * qr);
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        const float4 x = src[v];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          acc[c][4 * v] = fmaf(-x.x, ucs[c], acc[c][4 * v]);
+          acc[c][4 * v + 1] = fmaf(-x.y, ucs[c], acc[c][4 * v + 1]);
+          acc[c][4 * v + 2] = fmaf(-x.z, ucs[c], acc[c][4 * v + 2]);
+          acc[c][4 * v + 3] = fmaf(-x.w, ucs[c], acc[c][4 * v + 3]);
         }
       }
-      if (j + 1 < R) pick(bk, bi);
-    } else if (upd) {
-      // this thread's entries, six at a time with the loads issued first
+    } else if (warp == kPivWarp32) {
+      const float4 u4 = reinterpret_cast<const float4*>(s_u + 4 * (lane >> 3))[lane];
+      const float4 d4 = reinterpret_cast<const float4*>(s_d)[lane];
+      float dv[4] = {fmaf(-u4.x, u4.x, d4.x), fmaf(-u4.y, u4.y, d4.y), fmaf(-u4.z, u4.z, d4.z),
+                     fmaf(-u4.w, u4.w, d4.w)};
 #pragma unroll
-      for (int q0 = 0; q0 < kEnt32; q0 += 6) {
-        if (q0 >= nent) break;
-        float av[6], xv[6], yv[6];
-#pragma unroll
-        for (int b = 0; b < 6; ++b) {
-          const int e = ent[q0 + b];
-          av[b] = xv[b] = yv[b] = 0.f;
-          if (e >= 0) {
-            const int i = e >> 16, c = e & 0xffff;
-            if (i == k) {
-              av[b] = s_t[c];
-            } else if (c == k) {
-              av[b] = s_t[i];
-            } else {
-              av[b] = A[i * ld + c];
-              xv[b] = s_a[i];
-              yv[b] = s_t[c];
-            }
-          }
-        }
-#pragma unroll
-        for (int b = 0; b < 6; ++b) {
-          const int e = ent[q0 + b];
-          if (e >= 0) A[(e >> 16) * ld + (e & 0xffff)] = fmaf(-xv[b], yv[b], av[b]);
-        }
+      for (int q = 0; q < 4; ++q) {
+        const bool isk = (4 * lane + q) == k;
+        dv[q] = isk ? -r_dk : dv[q];
+        swept |= isk ? (1u << q) : 0u;
       }
+      reinterpret_cast<float4*>(s_d)[lane] = make_float4(dv[0], dv[1], dv[2], dv[3]);
+      if (j + 1 < R) pick(dv);
     }
     __syncthreads();
   }
@@ -727,11 +722,15 @@ __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int
       info->qr_rank = R;
     }
   }
-  if (!ok) return;
-  for (int e = tid; e < R * R; e += blockDim.x) {
-    const int r = e / R, c = e - r * R;
-    W[e] = -(double)((r <= c) ? A[r * ld + c] : A[c * ld + r]);
-  }
+  if (!ok || !own) return;
+  // W = -A: column-major = row-major (A is exactly symmetric); the diagonal from s_d
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int jj = 0; jj < 32; ++jj) {
+      const int i = 32 * qr + jj, col = 4 * cg + c;
+      if (i < R && col < R) W[(size_t)col * R + i] = (i == col) ? -(double)s_d[i] : -(double)acc[c][jj];
+    }
 }
 
 // ---------------- solve: X = M W^T ----------------

@@ -86,8 +86,8 @@ struct SolveInfo {
   int rank;      // rank reached by the pivoted Cholesky
   int fallback;  // 1 if the pivoted-QR path produced the solve operator
   int qr_rank;   // numerical rank found by the QR path
-  int refine;    // 1: W is the FP32 sweep's inverse and V (FP64) is in the workspace; the
-                 // solve refines X once with the FP64 residual M - X V
+  int refine;    // 1: the FP32 sweep's inverse W and V = V_hi + V_lo (FP32) are in the
+                 // workspace; the solve refines X once with the residual M - X V
 };
 
 // ---- launchers (defined in the kernel translation units) ----

@@ -19,6 +19,7 @@
 // concurrently with the MTTKRP of the same mode.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 
@@ -558,6 +559,14 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // earlier one-entry-per-thread sweep 2.6 k.)
 constexpr int FT32 = 256;
 constexpr int kOwnWarps32 = 4, kPivWarp32 = 4;
+// The refinement's FP32 operands, written by the FP32 sweep into the workspace after the
+// FP64 factorisation's area: [W | V_hi | V_lo], each R^2 floats padded to a multiple of four
+// (16-byte aligned, so the solve stages them with 16-byte asynchronous copies).  V = V_hi +
+// V_lo to 2^-48 relative.
+__host__ __device__ inline int rr4(int R) { return (R * R + 3) & ~3; }
+__host__ __device__ inline size_t ops32_offset_doubles(int R) {
+  return (5 * (size_t)R * R + 4 * (size_t)R + 64 + 1) & ~(size_t)1;
+}
 __device__ __forceinline__ int pivot_key(float v, int i) {
   const int b = __float_as_int(v);
   if ((b & 0x7fffffff) > 0x7f800000) return INT_MAX;  // NaN first: it stops the sweep
@@ -571,8 +580,8 @@ __device__ __forceinline__ void publish_u(const float (&acc)[4][32], float sc, f
   for (int v = 0; v < 8; ++v)
     dst[v] = make_float4(acc[C][4 * v] * sc, acc[C][4 * v + 1] * sc, acc[C][4 * v + 2] * sc, acc[C][4 * v + 3] * sc);
 }
-__global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int skip, int R, double* __restrict__ Vg,
-                                                      double* __restrict__ W, SolveInfo* info, DevCheck* chk) {
+__global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int skip, int R, float* __restrict__ ops,
+                                                      SolveInfo* info, DevCheck* chk) {
   if (done_flag(chk)) return;
   extern __shared__ float smF[];
   const int ld = R | 1;
@@ -603,8 +612,10 @@ __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int
       for (int m = 0; m < kMaxOrder; ++m) v *= g[m][q];
       if (e < R * R) {
         const int r = e / R, c = e - r * R;
-        Vg[e] = v;  // FP64 V (symmetric) for the refinement
-        if (c >= r) A[r * ld + c] = (float)v;
+        const float vh = (float)v;
+        ops[rr4(R) + e] = vh;  // V = V_hi + V_lo for the refinement's residual
+        ops[2 * rr4(R) + e] = (float)(v - (double)vh);
+        if (c >= r) A[r * ld + c] = vh;
       }
     }
   }
@@ -723,13 +734,13 @@ __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int
     }
   }
   if (!ok || !own) return;
-  // W = -A: column-major = row-major (A is exactly symmetric); the diagonal from s_d
+  // W = -A (FP32): column-major = row-major (A is exactly symmetric); the diagonal from s_d
 #pragma unroll
   for (int c = 0; c < 4; ++c)
 #pragma unroll
     for (int jj = 0; jj < 32; ++jj) {
       const int i = 32 * qr + jj, col = 4 * cg + c;
-      if (i < R && col < R) W[(size_t)col * R + i] = (i == col) ? -(double)s_d[i] : -(double)acc[c][jj];
+      if (i < R && col < R) ops[(size_t)col * R + i] = (i == col) ? -s_d[i] : -acc[c][jj];
     }
 }
 
@@ -748,47 +759,51 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
                                                         const double* __restrict__ WT, double* __restrict__ X,
                                                         double* __restrict__ inner_rows, const DevCheck* chk,
                                                         const SolveInfo* __restrict__ info,
-                                                        const double* __restrict__ Vg,
+                                                        const float* __restrict__ ops,
                                                         double* __restrict__ gpart) {
   if (done_flag(chk)) return;
   extern __shared__ double sm[];
   double* Ms = sm;            // RB x R
   double* Ps = sm + RB * R;   // RB x R products for the fit
   double* Xs = sm + 2 * RB * R;  // RB x R: X before the refinement
+  const int fw = ((RB * R + 3) & ~3) / 2;                 // doubles per RB x R float array
   float* Fs = reinterpret_cast<float*>(sm + 3 * RB * R);  // RB x R floats: M, then the residual
+  float* X0f = reinterpret_cast<float*>(sm + 3 * RB * R + fw);  // RB x R floats: X0
   const bool staged = (R <= kSolveStageMaxR);
   const bool refine = info && info->refine;
-  double* St = sm + 3 * RB * R + (RB * R + 1) / 2;  // staging area
-  double* Ws = St;                                    // W (FP64 path)
-  float* W32 = reinterpret_cast<float*>(St);          // W (refinement: the FP32 sweep's inverse)
-  double* Vs = St + (R * R + 1) / 2;                  // V (refinement)
+  double* St = sm + ((3 * RB * R + 2 * fw + 1) & ~1);  // staging area (16-byte aligned)
+  double* Ws = St;                        // W (FP64 path)
+  float* W32 = reinterpret_cast<float*>(St);  // refinement: [W | V_hi | V_lo] (FP32 sweep)
+  const float* Vh = W32 + rr4(R);
+  const float* Vl = W32 + 2 * rr4(R);
   const int tid = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * RB;
   const int rows = (In - r0 < (int64_t)RB) ? (int)(In - r0) : RB;
   const int nval = rows * R;
   const int64_t base = r0 * R;
   const int64_t sstride = In * R;
-  if (staged) {
+  if (refine) {
+    // 16-byte asynchronous copies of [W | V_hi | V_lo]; they land while M is summed below
+    const int n16 = 3 * rr4(R) / 4;
+    const char* src = reinterpret_cast<const char*>(ops);
+    const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(W32));
+    for (int c = tid; c < n16; c += SOLVE_T)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u * c), "l"(src + 16 * (size_t)c)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  } else if (staged) {
     const int n = R * R;
     for (int e0 = tid; e0 < n; e0 += 8 * SOLVE_T) {
-      double w[8], v[8];
+      double w[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int e = e0 + q * SOLVE_T;
         w[q] = (e < n) ? __ldg(&WT[e]) : 0.0;
-        v[q] = (refine && e < n) ? __ldg(&Vg[e]) : 0.0;
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int e = e0 + q * SOLVE_T;
-        if (e < n) {
-          if (refine) {
-            W32[e] = (float)w[q];  // exact: the FP32 sweep's values
-            Vs[e] = v[q];
-          } else {
-            Ws[e] = w[q];
-          }
-        }
+        if (e < n) Ws[e] = w[q];
       }
     }
   }
@@ -835,6 +850,7 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
       Ms[e] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
     }
   }
+  if (refine) asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
   const double* W = staged ? Ws : WT;
   // one output of A B for the row `row` of A (RB x R in shared memory), column k of B (R x R)
@@ -853,10 +869,35 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
     return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
   };
   if (refine) {
-    // Mixed-precision iterative refinement with the FP32 inverse W and the FP64 V: only the
-    // residual needs FP64 (it cancels); X0 and the correction carry FP32 relative error,
-    // and the correction is ~kappa eps_32 smaller than X:
-    //   X0 = M W (FP32),  E = M - X0 V (FP64),  X = X0 + E W (FP32 product, FP64 sum)
+    // Mixed-precision iterative refinement with the FP32 inverse W: only the residual needs
+    // more than FP32 (it cancels); X0 and the correction carry FP32 relative error, and the
+    // correction is ~kappa eps_32 smaller than X:
+    //   X0 = M W (FP32),  E = M - X0 V,  X = X0 + E W (FP32 product, FP64 sum).
+    // X0 V is a compensated FP32 dot product (Dot2, Ogita, Rump and Oishi 2005): X0 is
+    // exact in FP32, V = V_hi + V_lo, each X0 V_hi term is split exactly into product and
+    // error (one FMA) and summed with an error-free TwoSum, X0 V_lo is added in FP32.  The
+    // result is as accurate as an FP64 dot product (~2^-48 relative to sum |X0| |V|), at
+    // FP32 rates (this part issues FP32 64x faster than FP64).
+    auto dot2 = [&](const float* x, int k) {
+      float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+      auto term = [&](float xv, int l, float& s, float& c) {
+        const float vh = Vh[(size_t)l * R + k];
+        const float p = xv * vh;
+        const float pe = fmaf(xv, vh, -p);
+        const float t = s + p;
+        const float z = t - s;
+        const float e = (s - (t - z)) + (p - z);
+        s = t;
+        c = fmaf(xv, Vl[(size_t)l * R + k], c + (pe + e));
+      };
+      int l = 0;
+      for (; l + 2 <= R; l += 2) {
+        term(x[l], l, s0, c0);
+        term(x[l + 1], l + 1, s1, c1);
+      }
+      if (l < R) term(x[l], l, s0, c0);
+      return ((double)s0 + (double)s1) + ((double)c0 + (double)c1);
+    };
     auto rowdot32 = [&](const float* Arow, int k) {
       float a[8];
 #pragma unroll
@@ -875,12 +916,14 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
     __syncthreads();
     for (int e = tid; e < nval; e += SOLVE_T) {
       const int row = e / R, k = e % R;
-      Xs[e] = (double)rowdot32(Fs + row * R, k);
+      const float x0 = rowdot32(Fs + row * R, k);
+      X0f[e] = x0;
+      Xs[e] = (double)x0;
     }
     __syncthreads();
     for (int e = tid; e < nval; e += SOLVE_T) {
       const int row = e / R, k = e % R;
-      Ps[e] = Ms[e] - rowdot(Xs + row * R, Vs, k);
+      Ps[e] = Ms[e] - dot2(X0f + row * R, k);
     }
     __syncthreads();
     for (int e = tid; e < nval; e += SOLVE_T) Fs[e] = (float)Ps[e];
@@ -1032,8 +1075,8 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
   double ps[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) ps[q] = 0.0;
-  if (fa.fpart && tid == 0)
-    for (int t = 0; t < fa.ntiles; ++t) ps[t & 7] += __ldcg(&fa.fpart[t]);
+  if (fa.fpart)  // one partial per thread, summed by the block's tree below
+    for (int t = tid; t < fa.ntiles; t += nt) ps[0] += __ldcg(&fa.fpart[t]);
   for (int e0 = tid; !fa.fpart && e0 < n; e0 += 8 * nt) {
     double h[8];
 #pragma unroll
@@ -1233,16 +1276,21 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
   const int T = R * (R + 1) / 2;
   const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
-  double a0 = 0.0, a1 = 0.0;
+  // warp sl sums partials sl, sl + 8, ...: four accumulators, four loads in flight
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
   if (e < T) {
     int b = sl;
-    for (; b + 8 < nblk; b += 16) {
-      a0 += gpart[(size_t)b * T + e];
-      a1 += gpart[(size_t)(b + 8) * T + e];
+    for (; b + 24 < nblk; b += 32) {
+      const double v0 = gpart[(size_t)b * T + e], v1 = gpart[(size_t)(b + 8) * T + e];
+      const double v2 = gpart[(size_t)(b + 16) * T + e], v3 = gpart[(size_t)(b + 24) * T + e];
+      a0 += v0;
+      a1 += v1;
+      a2 += v2;
+      a3 += v3;
     }
-    if (b < nblk) a0 += gpart[(size_t)b * T + e];
+    for (; b < nblk; b += 8) a0 += gpart[(size_t)b * T + e];
   }
-  red[sl][lane] = a0 + a1;
+  red[sl][lane] = (a0 + a1) + (a2 + a3);
   __syncthreads();
   double h = 0.0;
   if (sl == 0 && e < T) {
@@ -1344,7 +1392,7 @@ __global__ void k_reduce_partials(const PT* __restrict__ part, int S, int64_t n,
 
 }  // namespace
 
-size_t factorize_work_doubles(int R) { return 5 * (size_t)R * R + 4 * (size_t)R + 64; }
+size_t factorize_work_doubles(int R) { return ops32_offset_doubles(R) + (3 * (size_t)rr4(R) + 1) / 2; }
 
 cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, double* work, double* U, int* piv,
                              double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st, int mixed) {
@@ -1358,7 +1406,8 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   if (ea != cudaSuccess) return ea;
   mixed = (mixed && R <= 128) ? 1 : 0;
   if (mixed) {
-    k_factorize32<<<1, FT32, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, Aglob, W, info, chk);
+    float* ops = reinterpret_cast<float*>(work + ops32_offset_doubles(R));
+    k_factorize32<<<1, FT32, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, ops, info, chk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -1380,21 +1429,24 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
   (void)piv;
   const int RB = solve_rows_per_block(R);
   dim3 grid((unsigned)((In + RB - 1) / RB));
-  // M, products, X0 (doubles), M / residual (floats), then W (FP64, or FP32 + V in FP64)
-  size_t smem = (size_t)3 * RB * R * sizeof(double) + (size_t)((RB * R + 1) / 2) * sizeof(double);
-  if (R <= kSolveStageMaxR) smem += (size_t)((R * R + 1) / 2 + R * R) * sizeof(double);
+  // M, products, X (doubles), M / residual and X0 (floats), then W (FP64) or the
+  // refinement's [W | V_hi | V_lo] (FP32)
+  const size_t fw = (size_t)((RB * R + 3) & ~3) / 2;
+  size_t smem = ((size_t)3 * RB * R + 2 * fw + 1) * sizeof(double);
+  if (R <= kSolveStageMaxR) smem += std::max((size_t)R * R * sizeof(double), (size_t)3 * rr4(R) * sizeof(float));
   {
-    const int mx = 3 * 256 * 8 + 128 * 8 + (kSolveStageMaxR * kSolveStageMaxR / 2 + kSolveStageMaxR * kSolveStageMaxR) * 8;
+    const int mx = (3 * 256 + 2 * 128 + 1) * 8 + 3 * rr4(kSolveStageMaxR) * 4;
     cudaError_t ea = set_smem_limit_once((const void*)k_solve_gemm<float>, mx);
     if (ea == cudaSuccess) ea = set_smem_limit_once((const void*)k_solve_gemm<double>, mx);
     if (ea != cudaSuccess) return ea;
   }
+  const float* ops = reinterpret_cast<const float*>(work + ops32_offset_doubles(R));
   if (part_is_f32)
     k_solve_gemm<float><<<grid, SOLVE_T, smem, st>>>(static_cast<const float*>(part), splits, In, R, RB, W, X,
-                                                     inner_rows, chk, info, work, gram_part);
+                                                     inner_rows, chk, info, ops, gram_part);
   else
     k_solve_gemm<double><<<grid, SOLVE_T, smem, st>>>(static_cast<const double*>(part), splits, In, R, RB, W, X,
-                                                      inner_rows, chk, info, work, gram_part);
+                                                      inner_rows, chk, info, ops, gram_part);
   return cudaGetLastError();
 }
 

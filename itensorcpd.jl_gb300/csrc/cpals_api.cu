@@ -31,6 +31,7 @@ struct cpals_ctx {
   bool T_set = false, F_set = false;
   double* F[kMaxOrder] = {};
   float* F32r[kMaxOrder] = {};  // row-major FP32 copies (tensor-core path)
+  float* F32lo[kMaxOrder] = {};  // their FP32 remainders F - F32r (dimension tree, tensor-core path)
   int64_t rpad = 0;
   double* G[kMaxOrder] = {};
   double* lam = nullptr;
@@ -268,7 +269,7 @@ int enqueue_sweep(cpals_ctx* c) {
     // the BF16 factor tiles the tensor-core MTTKRP reads are written by the same kernel
     const BtileDesc btd = c->tc ? tc_btile_desc(c->tc, n) : c->dt ? dt_btile_desc(c->dt, n) : BtileDesc{nullptr, 0, 0};
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32r[n], c->rpad,
-                                    c->Graw, c->G[n], last ? nullptr : c->chk, c->st, btd));
+                                    c->Graw, c->G[n], last ? nullptr : c->chk, c->st, btd, c->F32lo[n]));
   }
   if (c->cross_on) {  // check_converge of a CPDiffCheck / CPAngleCheck on the new iterate
     CPALS_CUDA_TRY(launch_cp_check(cross_args(c), c->st));
@@ -420,6 +421,7 @@ int cpals_destroy(cpals_ctx* c) {
   for (int m = 0; m < kMaxOrder; ++m) {
     cudaFree(c->F[m]);
     cudaFree(c->F32r[m]);
+    cudaFree(c->F32lo[m]);
     cudaFree(c->G[m]);
     if (c->ev_main[m]) cudaEventDestroy(c->ev_main[m]);
     if (c->ev_side[m]) cudaEventDestroy(c->ev_side[m]);
@@ -549,13 +551,21 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
       c->rpad = c->tc ? tc_factor_rpad(c->tc) : dt_factor_rpad(c->dt);
       CK(dmalloc(&c->F32r[m], (size_t)dims[m] * c->rpad));
       CPALS_CUDA_TRY(cudaMemset(c->F32r[m], 0, sizeof(float) * dims[m] * c->rpad));
+      if (c->dt) {
+        CK(dmalloc(&c->F32lo[m], (size_t)dims[m] * c->rpad));
+        CPALS_CUDA_TRY(cudaMemset(c->F32lo[m], 0, sizeof(float) * dims[m] * c->rpad));
+      }
     }
     CK(dmalloc(&c->G[m], (size_t)R * R));
   }
   if (c->tc || c->dt) {
     const float* fr[kMaxOrder] = {};
-    for (int m = 0; m < order; ++m) fr[m] = c->F32r[m];
-    CK(c->tc ? tc_bind_factors(c->tc, fr) : dt_bind_factors(c->dt, fr));
+    const float* fl[kMaxOrder] = {};
+    for (int m = 0; m < order; ++m) {
+      fr[m] = c->F32r[m];
+      fl[m] = c->F32lo[m];
+    }
+    CK(c->tc ? tc_bind_factors(c->tc, fr) : dt_bind_factors(c->dt, fr, fl));
   }
   if (c->dt) CK(dmalloc(&c->Mdt, (size_t)maxI * R));
   c->part_f32 = (mttkrp_mode == CPALS_MTTKRP_BF16X3) && !c->dt;
@@ -659,7 +669,8 @@ int cpals_set_factors(cpals_ctx* c, const double* const* host_factors, const dou
     colmajor_to_rowmajor_host(host_factors[m], c->dims[m], R, tmp.data());
     CPALS_CUDA_TRY(cudaMemcpyAsync(c->F[m], tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c->st));
     CPALS_CUDA_TRY(launch_normalize(c->F[m], nullptr, c->dims[m], R, c->F[m], c->F32r[m],
-                                    c->rpad, nullptr, nullptr, nullptr, c->st));
+                                    c->rpad, nullptr, nullptr, nullptr, c->st, BtileDesc{nullptr, 0, 0},
+                                    c->F32lo[m]));
     CPALS_CUDA_TRY(update_factor_tiles(c, m, nullptr));
     CPALS_CUDA_TRY(launch_gram(c->F[m], c->dims[m], R, c->gS2[m], c->gpart, c->gcnt, c->G[m], nullptr, c->st));
     c->launches += 2;
@@ -1065,7 +1076,8 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
   CPALS_CUDA_TRY(launch_finalize(c->Graw, R, c->lam, c->lam_inv, c->G[mode], gs, c->order, 0, nullptr, In, nullptr,
                                  c->traj, c->traj_cap, c->st));
   CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[mode], c->F32r[mode],
-                                  c->rpad, nullptr, nullptr, nullptr, c->st));
+                                  c->rpad, nullptr, nullptr, nullptr, c->st, BtileDesc{nullptr, 0, 0},
+                                  c->F32lo[mode]));
   CPALS_CUDA_TRY(update_factor_tiles(c, mode, nullptr));
   return check_derr(c);
 }

@@ -16,7 +16,7 @@ int* dt_error_flag(DimTree* d, int which);
 // Column count of the row-major FP32 factor copies (tensor-core path; 0 otherwise).
 int64_t dt_factor_rpad(const DimTree* d);
 // Register the row-major FP32 factor copies of the four modes (tensor-core path).
-int dt_bind_factors(DimTree* d, const float* const* F32r);
+int dt_bind_factors(DimTree* d, const float* const* F32r, const float* const* F32lo);
 // Layout of the BF16 factor tiles mode m's new factor feeds (modes 0 and 2; else bt null).
 BtileDesc dt_btile_desc(const DimTree* d, int m);
 // Rebuild the BF16 factor tiles that mode m's new factor feeds (modes 0 and 2).

@@ -154,10 +154,11 @@ struct BtileDesc {
 
 // F = X .* (1 ./ lambda) (lam_inv may be null: plain copy), (when F32r is non-null) an
 // FP32 row-major copy [In][rpad], (when Gn is non-null) the normalised Gram
-// Gn = Graw ./ (lambda lambda^T) and (when bt.bt is non-null) the BF16 factor tiles.
+// Gn = Graw ./ (lambda lambda^T), (when bt.bt is non-null) the BF16 factor tiles and (when
+// F32lo is non-null) the FP32 remainder F - (float)F in the F32r layout.
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
                              int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st,
-                             BtileDesc bt = BtileDesc{nullptr, 0, 0});
+                             BtileDesc bt = BtileDesc{nullptr, 0, 0}, float* F32lo = nullptr);
 
 // Row-major rows x cols -> row-major cols x rows (FP64).
 cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);

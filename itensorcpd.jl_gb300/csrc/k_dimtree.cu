@@ -9,8 +9,11 @@
 // In ALS order P_L depends only on F2, F3 (fixed while modes 0 and 1 update) and P_R on the
 // updated F0, F1 (fixed while modes 2 and 3 update), so a sweep streams T twice instead of
 // four times.  The full contractions run on the same kernels as the plain path (tcgen05
-// split-BF16 for FP32 tensors, the FP64 SIMT kernel otherwise); their split-K partials are
-// reduced into P (FP64) and the small contractions run in FP64.
+// split-BF16 for FP32 tensors, the FP64 SIMT kernel otherwise).  On the FP64 path the
+// split-K partials are reduced into P (FP64) and the small contractions run in FP64.  On the
+// tensor-core path the FP32 partials are summed with compensation into P as an unevaluated
+// FP32 pair hi + lo (no FP64 operation), and the small contractions are compensated FP32
+// dot products of P with the factor's FP32 hi / lo rows: FP64-grade sums at FP32 rates.
 #include <algorithm>
 #include <cstring>
 
@@ -44,6 +47,87 @@ __global__ void k_dt_reduce(const PT* __restrict__ part, int S, int64_t n, doubl
       P[e] = s;
     }
   }
+}
+
+// P2 = the compensated FP32 sum of the FP32 split-K partials, kept as {hi, lo} (Fast2Sum
+// of the Neumaier sum and its compensation).
+__global__ void k_dt_reduce_df(const float* __restrict__ part, int S, int64_t n, float2* __restrict__ P2,
+                               const DevCheck* chk) {
+  if (dt_done(chk)) return;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f, c = 0.0f;
+    for (int sp = 0; sp < S; ++sp) {
+      const float p = part[(int64_t)sp * n + e];
+      const float t = s + p;
+      c += (fabsf(s) >= fabsf(p)) ? ((s - t) + p) : ((p - t) + s);
+      s = t;
+    }
+    const float hi = s + c;
+    P2[e] = make_float2(hi, c - (hi - s));
+  }
+}
+
+// The small contraction on the tensor-core path: out[i][r] = sum_j P[row(i, j)][r] F[j][r]
+// with P = {hi, lo} and F = Fh + Fl (FP32 rows, stride rpad), as a compensated FP32 dot
+// product (Dot2, Ogita, Rump and Oishi 2005: each hi x hi product split exactly by one FMA,
+// summed by TwoSum; the cross terms added in FP32).  Block: two output rows x 32 ranks; warp
+// w takes row 2 blockIdx.x + (w & 1) and the quarter w >> 1 of the summed index; the four
+// quarters are combined in order.
+__device__ __forceinline__ void dot2_term(float xh, float xl, float yh, float yl, float& s, float& c) {
+  const float p = xh * yh;
+  const float pe = fmaf(xh, yh, -p);
+  const float t = s + p;
+  const float z = t - s;
+  const float e = (s - (t - z)) + (p - z);
+  s = t;
+  c = fmaf(xh, yl, fmaf(xl, yh, c + (pe + e)));
+}
+__global__ void __launch_bounds__(256) k_dt_contract_df(const float2* __restrict__ P, int64_t Ia, int64_t Ib, int R,
+                                                        const float* __restrict__ Fh, const float* __restrict__ Fl,
+                                                        int64_t rpad, int which, double* __restrict__ out,
+                                                        const DevCheck* chk) {
+  if (dt_done(chk)) return;
+  __shared__ float2 red[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nI = which ? Ib : Ia, nsum = which ? Ia : Ib;
+  const int64_t i = 2 * (int64_t)blockIdx.x + (w & 1);
+  const int r = blockIdx.y * 32 + lane;
+  const int64_t nq = (nsum + 3) / 4;
+  const int64_t j0 = (w >> 1) * nq, j1 = min(nsum, j0 + nq);
+  float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+  if (i < nI && r < R) {
+    int64_t j = j0;
+    for (; j + 2 <= j1; j += 2) {
+      const int64_t ra = which ? j + Ia * i : i + Ia * j;
+      const int64_t rb = which ? (j + 1) + Ia * i : i + Ia * (j + 1);
+      const float2 xa = P[ra * R + r], xb = P[rb * R + r];
+      dot2_term(xa.x, xa.y, Fh[j * rpad + r], Fl[j * rpad + r], s0, c0);
+      dot2_term(xb.x, xb.y, Fh[(j + 1) * rpad + r], Fl[(j + 1) * rpad + r], s1, c1);
+    }
+    if (j < j1) {
+      const int64_t ra = which ? j + Ia * i : i + Ia * j;
+      const float2 xa = P[ra * R + r];
+      dot2_term(xa.x, xa.y, Fh[j * rpad + r], Fl[j * rpad + r], s0, c0);
+    }
+  }
+  // (s0, c0) + (s1, c1) with one TwoSum
+  {
+    const float t = s0 + s1, z = t - s0;
+    const float e = (s0 - (t - z)) + (s1 - z);
+    red[w][lane] = make_float2(t, (c0 + c1) + e);
+  }
+  __syncthreads();
+  if (w >= 2 || i >= nI || r >= R) return;
+  float s = red[w][lane].x, c = red[w][lane].y;
+#pragma unroll
+  for (int q = 1; q < 4; ++q) {
+    const float2 v = red[w + 2 * q][lane];
+    const float t = s + v.x, z = t - s;
+    const float e = (s - (t - z)) + (v.x - z);
+    s = t;
+    c += v.y + e;
+  }
+  out[i * R + r] = (double)s + (double)c;
 }
 
 // out[i][r] = sum_j P[(which ? j + Ia i : i + Ia j)][r] F[j][r]: contract P (rows a + Ia b)
@@ -95,8 +179,11 @@ struct DimTree {
   int64_t cpsA = 0, cpsB = 0;
   const void* dT = nullptr;  // the device tensor (FP64 path)
   void* part = nullptr;  // split-K partials of the full contractions
-  double* PL = nullptr;  // [I0*I1][R]
+  double* PL = nullptr;  // [I0*I1][R] (FP64, or {hi, lo} FP32 pairs on the tensor-core path)
   double* PR = nullptr;  // [I2*I3][R]
+  const float* Fh[4] = {};  // tensor-core path: the factors' FP32 rows (hi) and remainders (lo)
+  const float* Fl[4] = {};
+  int64_t rpad = 0;
 };
 
 int dt_create(DimTree** out, const int64_t* dims, int64_t R, int mmode, int tdtype, int num_sms) {
@@ -163,8 +250,13 @@ int* dt_error_flag(DimTree* d, int which) {
 
 int64_t dt_factor_rpad(const DimTree* d) { return d->tcA ? tc_factor_rpad(d->tcA) : 0; }
 
-int dt_bind_factors(DimTree* d, const float* const* F32r) {
+int dt_bind_factors(DimTree* d, const float* const* F32r, const float* const* F32lo) {
   if (!d->tcA) return CPALS_OK;
+  for (int m = 0; m < 4; ++m) {
+    d->Fh[m] = F32r[m];
+    d->Fl[m] = F32lo[m];
+  }
+  d->rpad = tc_factor_rpad(d->tcA);
   // view A, mode 0: fastest reduction mode = view mode 1 (F2), outer = view mode 2 (F3)
   const float* fa[kMaxOrder] = {nullptr, F32r[2], F32r[3]};
   // view B, mode 2: fastest reduction mode = view mode 0 (F0), outer = view mode 1 (F1)
@@ -209,7 +301,8 @@ cudaError_t dt_mttkrp(DimTree* d, int n, const double* const* F, bool reuse, dou
       cudaError_t e = tc_launch_mttkrp(tc, vm, static_cast<float*>(d->part), chk, st);
       if (e != cudaSuccess) return e;
       S = tc_splits(tc, vm);
-      k_dt_reduce<float><<<grid_for(rows * R), 256, 0, st>>>(static_cast<const float*>(d->part), S, rows * R, P, chk);
+      k_dt_reduce_df<<<grid_for(rows * R), 256, 0, st>>>(static_cast<const float*>(d->part), S, rows * R,
+                                                          reinterpret_cast<float2*>(P), chk);
     } else {
       FactorSet fs{};
       if (left) {
@@ -234,9 +327,16 @@ cudaError_t dt_mttkrp(DimTree* d, int n, const double* const* F, bool reuse, dou
   const int64_t Ia = left ? d->dims[0] : d->dims[2];
   const int64_t Ib = left ? d->dims[1] : d->dims[3];
   const int which = (n == 1 || n == 3) ? 1 : 0;  // modes 1, 3 contract over the first index
-  const double* Fc = F[(n == 0) ? 1 : (n == 1) ? 0 : (n == 2) ? 3 : 2];
-  const int64_t nout = (which ? Ib : Ia) * R;
-  k_dt_contract<<<grid_for(nout), 256, 0, st>>>(P, Ia, Ib, R, Fc, which, M, chk);
+  const int fc = (n == 0) ? 1 : (n == 1) ? 0 : (n == 2) ? 3 : 2;
+  if (d->tcA) {
+    const int64_t nI = which ? Ib : Ia;
+    const dim3 grid((unsigned)((nI + 1) / 2), (unsigned)((R + 31) / 32));
+    k_dt_contract_df<<<grid, 256, 0, st>>>(reinterpret_cast<const float2*>(P), Ia, Ib, R, d->Fh[fc], d->Fl[fc],
+                                          d->rpad, which, M, chk);
+  } else {
+    const int64_t nout = (which ? Ib : Ia) * R;
+    k_dt_contract<<<grid_for(nout), 256, 0, st>>>(P, Ia, Ib, R, F[fc], which, M, chk);
+  }
   return cudaGetLastError();
 }
 

@@ -1336,7 +1336,7 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
 __global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam_inv, int64_t In, int R,
                             double* __restrict__ F, float* __restrict__ F32r,
                             int64_t rpad, const double* __restrict__ Graw, double* __restrict__ Gn,
-                            const DevCheck* chk, BtileDesc btd) {
+                            const DevCheck* chk, BtileDesc btd, float* __restrict__ F32lo) {
   if (done_flag(chk)) return;
   const int64_t n = In * R;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -1346,6 +1346,7 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
     const double f = lam_inv ? X[e] * lam_inv[r] : X[e];
     F[e] = f;
     if (F32r) F32r[i * rpad + r] = (float)f;
+    if (F32lo) F32lo[i * rpad + r] = (float)(f - (double)(float)f);  // f = hi + lo to 2^-48
     if (btd.bt) {
       // hi = bf16(f), lo = bf16(f - hi), at row i of column r in its tile
       const __nv_bfloat16 h = __double2bfloat16(f);
@@ -1510,10 +1511,10 @@ cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_
 
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
                              int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st,
-                             BtileDesc bt) {
+                             BtileDesc bt, float* F32lo) {
   const int64_t n = In * R;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32r, rpad, Graw, Gn, chk, bt);
+  k_normalize<<<blocks, 256, 0, st>>>(X, lam_inv, In, R, F, F32r, rpad, Graw, Gn, chk, bt, F32lo);
   return cudaGetLastError();
 }
 

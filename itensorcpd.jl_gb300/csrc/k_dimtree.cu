@@ -26,26 +26,14 @@ namespace {
 
 __device__ __forceinline__ bool dt_done(const DevCheck* chk) { return chk != nullptr && chk->done; }
 
-// P = sum of the split-K partials (float: compensated FP32 sum finished in FP64).
-template <typename PT>
-__global__ void k_dt_reduce(const PT* __restrict__ part, int S, int64_t n, double* __restrict__ P,
+// P = sum of the FP64 split-K partials (FP64 path).
+__global__ void k_dt_reduce(const double* __restrict__ part, int S, int64_t n, double* __restrict__ P,
                             const DevCheck* chk) {
   if (dt_done(chk)) return;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    if constexpr (sizeof(PT) == 4) {
-      float s = 0.0f, c = 0.0f;
-      for (int sp = 0; sp < S; ++sp) {
-        const float p = part[(int64_t)sp * n + e];
-        const float t = s + p;
-        c += (fabsf(s) >= fabsf(p)) ? ((s - t) + p) : ((p - t) + s);
-        s = t;
-      }
-      P[e] = (double)s + (double)c;
-    } else {
-      double s = 0.0;
-      for (int sp = 0; sp < S; ++sp) s += (double)part[(int64_t)sp * n + e];
-      P[e] = s;
-    }
+    double s = 0.0;
+    for (int sp = 0; sp < S; ++sp) s += part[(int64_t)sp * n + e];
+    P[e] = s;
   }
 }
 
@@ -317,8 +305,7 @@ cudaError_t dt_mttkrp(DimTree* d, int n, const double* const* F, bool reuse, dou
       cudaError_t e = launch_mttkrp_f64(d->dT, d->tdtype, fs, g, R, S, left ? d->cpsA : d->cpsB,
                                         static_cast<double*>(d->part), chk, st);
       if (e != cudaSuccess) return e;
-      k_dt_reduce<double><<<grid_for(rows * R), 256, 0, st>>>(static_cast<const double*>(d->part), S, rows * R, P,
-                                                              chk);
+      k_dt_reduce<<<grid_for(rows * R), 256, 0, st>>>(static_cast<const double*>(d->part), S, rows * R, P, chk);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

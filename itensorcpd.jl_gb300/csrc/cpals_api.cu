@@ -231,7 +231,7 @@ int enqueue_sweep(cpals_ctx* c) {
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_main[n], 0));
     const int mixed = (c->mmode == CPALS_MTTKRP_BF16X3 && R <= 128) ? 1 : 0;
     CPALS_CUDA_TRY(launch_factorize(gs, N, n, R, c->work, c->U, c->piv, c->W, c->info, c->chk, c->side, mixed));
-    c->launches += mixed;  // the FP32 sweep
+    c->launches += 2 * mixed;  // V for the FP32 sweep, the FP32 sweep
     CPALS_CUDA_TRY(cudaEventRecord(c->ev_side[n], c->side));
     const bool prof = c->profiling && c->prof_used + 2 <= (int64_t)c->prof_ev.size();
     if (prof) CPALS_CUDA_TRY(cudaEventRecord(c->prof_ev[c->prof_used], c->st));

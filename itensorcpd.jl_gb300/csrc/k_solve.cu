@@ -554,10 +554,10 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // picks the next pivot -> barrier.  The pivot is the largest unswept diagonal entry, the
 // lowest index among values equal to 2^-16 relative (a packed key, one warp max); any choice
 // is fine here because the solve refines X in FP64, and a pivot below 1e-3 of the largest
-// diagonal entry hands the factorisation to the FP64 sweep.  Warps 5-7 help form V and
-// write W.  (A probe of this schedule on one SM: 0.84 k cycles per pivot at R = 128, the
-// earlier one-entry-per-thread sweep 2.6 k.)
-constexpr int FT32 = 256;
+// diagonal entry hands the factorisation to the FP64 sweep.  V is formed beforehand by
+// k_form_v32 over the whole grid.  (A probe of this schedule on one SM: 0.84 k cycles per
+// pivot at R = 128, the earlier one-entry-per-thread sweep 2.6 k.)
+constexpr int FT32 = 160;
 constexpr int kOwnWarps32 = 4, kPivWarp32 = 4;
 // The refinement's FP32 operands, written by the FP32 sweep into the workspace after the
 // FP64 factorisation's area: [W | V_hi | V_lo], each R^2 floats padded to a multiple of four
@@ -580,45 +580,31 @@ __device__ __forceinline__ void publish_u(const float (&acc)[4][32], float sc, f
   for (int v = 0; v < 8; ++v)
     dst[v] = make_float4(acc[C][4 * v] * sc, acc[C][4 * v + 1] * sc, acc[C][4 * v + 2] * sc, acc[C][4 * v + 3] * sc);
 }
-__global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int skip, int R, float* __restrict__ ops,
-                                                      SolveInfo* info, DevCheck* chk) {
+// V = Hadamard product of the other modes' Grams (FP64, in mode order, as the FP64 sweep
+// forms it), written as the FP32 pair V_hi + V_lo into the refinement operands.  One
+// thread per entry over the whole grid: the FP64 products run on every SM instead of on
+// the sweep's single CTA.
+__global__ void __launch_bounds__(256) k_form_v32(GramSet gs, int order, int skip, int R, float* __restrict__ ops,
+                                                  const DevCheck* chk) {
   if (done_flag(chk)) return;
-  extern __shared__ float smF[];
-  const int ld = R | 1;
-  float* A = smF;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= R * R) return;
+  double v = 1.0;
+  for (int m = 0; m < order; ++m)
+    if (m != skip) v *= gs.G[m][e];
+  const float vh = (float)v;
+  ops[rr4(R) + e] = vh;
+  ops[2 * rr4(R) + e] = (float)(v - (double)vh);
+}
+
+__global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__ ops, SolveInfo* info, DevCheck* chk) {
+  if (done_flag(chk)) return;
   __shared__ __align__(16) float s_u[144];
   __shared__ __align__(16) float s_d[128];
   __shared__ float s_uk, s_sc;
   __shared__ int s_p, s_stop;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // V = Hadamard product of the other modes' Grams (FP64, in mode order); every mode's
-  // loads are issued before the products
-  for (int e0 = tid; e0 < R * R; e0 += 4 * FT32) {
-    double g[kMaxOrder][4];
-#pragma unroll
-    for (int m = 0; m < kMaxOrder; ++m) {
-      const bool use = (m < order) && (m != skip);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int e = e0 + q * FT32;
-        g[m][q] = (use && e < R * R) ? gs.G[m][e] : 1.0;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = e0 + q * FT32;
-      double v = 1.0;
-#pragma unroll
-      for (int m = 0; m < kMaxOrder; ++m) v *= g[m][q];
-      if (e < R * R) {
-        const int r = e / R, c = e - r * R;
-        const float vh = (float)v;
-        ops[rr4(R) + e] = vh;  // V = V_hi + V_lo for the refinement's residual
-        ops[2 * rr4(R) + e] = (float)(v - (double)vh);
-        if (c >= r) A[r * ld + c] = vh;
-      }
-    }
-  }
+  const float* __restrict__ Vh = ops + rr4(R);  // V_hi from k_form_v32 (its upper triangle is used)
   for (int k = tid; k < 144; k += blockDim.x) {
     s_u[k] = 0.f;
     if (k < 128) s_d[k] = 0.f;
@@ -632,7 +618,7 @@ __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       const int i = 32 * qr + j, col = 4 * cg + c;
-      acc[c][j] = (own && i < R && col < R) ? ((i <= col) ? A[i * ld + col] : A[col * ld + i]) : 0.f;
+      acc[c][j] = (own && i < R && col < R) ? ((i <= col) ? Vh[(size_t)i * R + col] : Vh[(size_t)col * R + i]) : 0.f;
     }
   // warp 4: diagonal entries 4 lane .. 4 lane + 3 (registers and s_d), swept flags, pivot
   unsigned swept = 0;
@@ -667,7 +653,7 @@ __global__ void __launch_bounds__(FT32) k_factorize32(GramSet gs, int order, int
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int i = 4 * lane + q;
-      dv[q] = (i < R) ? A[i * ld + i] : 0.f;
+      dv[q] = (i < R) ? Vh[(size_t)i * R + i] : 0.f;
       s_d[i] = dv[q];
       md = fmaxf(md, dv[q]);
     }
@@ -1403,12 +1389,12 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   double* qwork = dinv + R;
   const size_t smem = (R <= 128) ? (size_t)R * (R | 1) * sizeof(double) : 0;
   cudaError_t ea = set_smem_limit_once((const void*)k_factorize, 200 * 1024);
-  if (ea == cudaSuccess) ea = set_smem_limit_once((const void*)k_factorize32, 128 * 129 * 4);
   if (ea != cudaSuccess) return ea;
   mixed = (mixed && R <= 128) ? 1 : 0;
   if (mixed) {
     float* ops = reinterpret_cast<float*>(work + ops32_offset_doubles(R));
-    k_factorize32<<<1, FT32, (size_t)R * (R | 1) * sizeof(float), st>>>(gs, order, skip, R, ops, info, chk);
+    k_form_v32<<<(R * R + 255) / 256, 256, 0, st>>>(gs, order, skip, R, ops, chk);
+    k_factorize32<<<1, FT32, 0, st>>>(R, ops, info, chk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

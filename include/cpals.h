@@ -142,6 +142,29 @@ int cpals_check_converge(cpals_ctx* ctx, cpals_check* check, int* converged, dou
 int cpals_get_prev(cpals_ctx* ctx, double* const* host_factors, double* host_lambda);
 int cpals_set_prev(cpals_ctx* ctx, const double* const* host_factors, const double* host_lambda);
 
+/* ---- sparse sign embeddings and sketched matricization ---- */
+
+/* An l x n oblivious sparse sign embedding Omega, zeta nonzeros per column, each +-1/sqrt(zeta),
+ * generated on the device and written to host arrays of n*zeta entries: column c's entries
+ * are rows[c*zeta + k] (0-based, as the reference's C generators leave them) and
+ * vals[c*zeta + k]; colstarts (n+1 entries, may be NULL) receives c*zeta, as theirs does.
+ * injective = 0: zeta distinct uniform rows per column (sparse_sign, src/algebra/sparse_sign.c);
+ * injective = 1: one uniform row in each of zeta near-equal row blocks (sparsestack,
+ * src/algebra/sparsestack.c).  zeta is clamped to l.  The draws come from a counter-based
+ * generator keyed by `seed`, so the same seed gives the same embedding on any device; the
+ * reference's rand() stream is not reproduced.  Replaces sparse_sign_call
+ * (src/algebra/SEQRCS.jl:41-60). */
+int cpals_sparse_sign(int device, int64_t l, int64_t n, int zeta, int injective, uint64_t seed, int32_t* rows,
+                      double* vals, int32_t* colstarts);
+
+/* A_sk = T_(mode) Omega^T (I_mode x l, column-major FP64) for the handle's tensor, with Omega
+ * given by host arrays of n*zeta entries as above (n = product of the other extents, their
+ * indices fused first-fastest): sketched_matricization(T, k, l, rows, vals, s)
+ * (src/algebra/pivot_mapping.jl:111-140).  Each output column sums its entries in entry order,
+ * as the reference does. */
+int cpals_sketched_matricization(cpals_ctx* ctx, int mode, int64_t l, int zeta, const int32_t* rows,
+                                 const double* vals, double* host_out);
+
 /* Number of normal-equation solves so far that took the pivoted-QR fallback
  * because the pivoted Cholesky was rank deficient (ldiv_solve.jl:17-22). */
 int cpals_fallback_count(cpals_ctx* ctx, int64_t* count);

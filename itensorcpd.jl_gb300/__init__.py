@@ -29,6 +29,8 @@ from .api import (
     random_factors,
     block_sample_factor_matrices,
     sample_factor_matrices,
+    sketched_matricization,
+    sparse_sign_matrix,
 )
 from .batched import BatchEngine
 from .engine import Engine
@@ -38,5 +40,5 @@ from .warmstart import WarmStartMLP
 __all__ = [
     "BatchEngine", "BlockLevScoreSampled", "CPAngleCheck", "CPD", "CPDFit", "CPDiffCheck", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
     "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
-    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "block_sample_factor_matrices", "WarmStartMLP", "warmstart",
+    "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "block_sample_factor_matrices", "sparse_sign_matrix", "sketched_matricization", "WarmStartMLP", "warmstart",
 ]

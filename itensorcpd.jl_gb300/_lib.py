@@ -69,6 +69,9 @@ SIGNATURES = {
     "cpals_check_converge": (C.c_int, [_P, C.POINTER(CpalsCheck), C.POINTER(C.c_int), _DP]),
     "cpals_get_prev": (C.c_int, [_P, C.POINTER(_DP), _DP]),
     "cpals_set_prev": (C.c_int, [_P, C.POINTER(_DP), _DP]),
+    "cpals_sparse_sign": (C.c_int, [C.c_int, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_uint64,
+                                    C.POINTER(C.c_int32), _DP, C.POINTER(C.c_int32)]),
+    "cpals_sketched_matricization": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_int32), _DP, _DP]),
     "cpals_fallback_count": (C.c_int, [_P, _I64P]),
     "cpals_synchronize": (C.c_int, [_P]),
     "cpals_timer_start": (C.c_int, [_P]),

@@ -7,6 +7,7 @@ reference's (first index fastest in memory is handled by the binding).
 """
 from __future__ import annotations
 
+import ctypes as C
 import warnings
 from dataclasses import dataclass, field
 
@@ -490,6 +491,45 @@ def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal, stop_re
         factors = [F.astype(np.float32) for F in factors]
         lam = lam.astype(np.float32)
     return CPD(factors, lam, T.shape)
+
+
+def sparse_sign_matrix(l, n, s, rows=None, vals=None, *, omega=False, injective=False, seed=0, device=0):
+    """SEQRCS.jl:29-39: an l x n sparse sign embedding with s nonzeros per column, generated
+    on the device (``cpals_sparse_sign``; counter-based draws keyed by ``seed``).  ``rows``
+    (Int32, n * s) and ``vals`` (Float64, n * s) are filled in place when given; rows end
+    1-based, as the reference leaves them.  Returns the scipy sparse matrix when ``omega``,
+    else (rows, vals)."""
+    lib = L.load()
+    n, s = int(n), int(s)
+    s_eff = min(s, int(l))
+    rows = np.empty(n * s, dtype=np.int32) if rows is None else rows
+    vals = np.empty(n * s, dtype=np.float64) if vals is None else vals
+    if rows.dtype != np.int32 or vals.dtype != np.float64 or rows.size < n * s_eff or vals.size < n * s_eff:
+        raise TypeError("rows must be Int32 and vals Float64 arrays of n * s entries")
+    colstarts = np.empty(n + 1, dtype=np.int32)
+    L.check(lib.cpals_sparse_sign(int(device), int(l), n, s, 1 if injective else 0, int(seed) & (2**64 - 1),
+                                  rows.ctypes.data_as(C.POINTER(C.c_int32)), L.dptr(vals),
+                                  colstarts.ctypes.data_as(C.POINTER(C.c_int32))), "cpals_sparse_sign")
+    rows[: n * s_eff] += 1
+    if omega:
+        import scipy.sparse as sp
+
+        cols = np.repeat(np.arange(n), s_eff)
+        return sp.csc_matrix((vals[: n * s_eff], (rows[: n * s_eff] - 1, cols)), shape=(int(l), n))
+    return rows, vals
+
+
+def sketched_matricization(T, k, l, rows, vals, s, device=0):
+    """pivot_mapping.jl:111-140: A_sk = T_(k) Omega^T (I_k x l) for the embedding in 1-based
+    ``rows`` / ``vals`` (n * s entries, n the product of the other extents).  ``k`` is the
+    0-based mode.  Runs on the device through ``cpals_sketched_matricization``."""
+    T = _prepare_target(T)
+    r0 = np.ascontiguousarray(rows, dtype=np.int64) - 1
+    if r0.size and (r0.min() < 0 or r0.max() >= int(l)):
+        raise ValueError("rows must be 1-based and at most l")
+    with Engine(T.shape, 1, dtype=T.dtype, precision="fp64", device=device) as eng:
+        eng.set_tensor(T)
+        return eng.sketched_matricization(int(k), int(l), r0.astype(np.int32), vals, int(s))
 
 
 def decompose(A, rank, max_rank=None, *, solver=None, rng=None, alg=None, check=None, maxiter=None, verbose=False,

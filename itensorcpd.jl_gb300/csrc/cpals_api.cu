@@ -7,6 +7,7 @@
 // stream concurrently with the MTTKRP of mode n; events fork and join the streams, and
 // a whole sweep is captured once into a CUDA graph and replayed.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -914,6 +915,90 @@ int cpals_set_prev(cpals_ctx* c, const double* const* host_factors, const double
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
   c->prev_valid = true;
   return CPALS_OK;
+}
+
+int cpals_sparse_sign(int device, int64_t l, int64_t n, int zeta, int injective, uint64_t seed, int32_t* rows,
+                      double* vals, int32_t* colstarts) {
+  if (l < 1 || l > INT32_MAX || n < 0 || zeta < 1 || !rows || !vals) return CPALS_E_ARG;
+  if (zeta > l) zeta = (int)l;  // as the reference's generators clamp it
+  if (colstarts)
+    for (int64_t c = 0; c <= n; ++c) colstarts[c] = (int32_t)(c * zeta);
+  if (n == 0) return CPALS_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return CPALS_E_CUDA;
+  const size_t nnz = (size_t)n * zeta;
+  int32_t* drows = nullptr;
+  double* dvals = nullptr;
+  int rc = CPALS_OK;
+  if (dmalloc(&drows, nnz) != CPALS_OK || dmalloc(&dvals, nnz) != CPALS_OK) {
+    rc = CPALS_E_CUDA;
+  } else {
+    cudaError_t e = launch_sparse_sign(l, n, zeta, injective ? 1 : 0, seed, drows, dvals, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(rows, drows, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(vals, dvals, sizeof(double) * nnz, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "libcpals: sparse sign embedding failed: %s\n", cudaGetErrorString(e));
+      rc = CPALS_E_CUDA;
+    }
+  }
+  cudaFree(drows);
+  cudaFree(dvals);
+  return rc;
+}
+
+int cpals_sketched_matricization(cpals_ctx* c, int mode, int64_t l, int zeta, const int32_t* rows,
+                                 const double* vals, double* host_out) {
+  if (!c || mode < 0 || mode >= c->order || l < 1 || zeta < 1 || zeta > l || !rows || !vals || !host_out)
+    return CPALS_E_ARG;
+  if (!c->T_set) return CPALS_E_STATE;
+  const int64_t In = c->dims[mode];
+  int64_t n = 1, stride = 1;
+  for (int m = 0; m < c->order; ++m)
+    if (m != mode) n *= c->dims[m];
+  for (int m = 0; m < mode; ++m) stride *= c->dims[m];
+  const int64_t nnz = n * zeta;
+  // group the entries by output column, keeping entry order (the reference's dict_rows)
+  std::vector<int64_t> seg((size_t)l + 1, 0);
+  for (int64_t p = 0; p < nnz; ++p) {
+    if (rows[p] < 0 || rows[p] >= l) return CPALS_E_ARG;
+    ++seg[(size_t)rows[p] + 1];
+  }
+  for (int64_t j = 0; j < l; ++j) seg[(size_t)j + 1] += seg[(size_t)j];
+  std::vector<int64_t> fill(seg.begin(), seg.end() - 1), pos((size_t)std::max<int64_t>(nnz, 1));
+  std::vector<double> v((size_t)std::max<int64_t>(nnz, 1));
+  for (int64_t p = 0; p < nnz; ++p) {
+    const int64_t col = p / zeta;  // column of Omega = fused index of the other modes
+    const int64_t slot = fill[(size_t)rows[p]]++;
+    pos[(size_t)slot] = (col / stride) * stride * In + (col % stride);
+    v[(size_t)slot] = vals[p];
+  }
+  DeviceGuard g(c->device);
+  int64_t *dseg = nullptr, *dpos = nullptr;
+  double *dv = nullptr, *dout = nullptr;
+  int rc = CPALS_OK;
+  if (dmalloc(&dseg, (size_t)l + 1) != CPALS_OK || dmalloc(&dpos, pos.size()) != CPALS_OK ||
+      dmalloc(&dv, v.size()) != CPALS_OK || dmalloc(&dout, (size_t)(In * l)) != CPALS_OK) {
+    rc = CPALS_E_CUDA;
+  } else {
+    cudaError_t e = cudaMemcpyAsync(dseg, seg.data(), sizeof(int64_t) * seg.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dpos, pos.data(), sizeof(int64_t) * pos.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = launch_sketch_gather(c->dT, c->tdtype, In, stride, dseg, dpos, dv, l, dout, c->st);
+    if (e == cudaSuccess) {
+      c->launches += 1;
+      e = cudaMemcpyAsync(host_out, dout, sizeof(double) * (size_t)(In * l), cudaMemcpyDeviceToHost, c->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "libcpals: sketched matricization failed: %s\n", cudaGetErrorString(e));
+      rc = CPALS_E_CUDA;
+    }
+  }
+  cudaFree(dseg);
+  cudaFree(dpos);
+  cudaFree(dv);
+  cudaFree(dout);
+  return rc;
 }
 
 int cpals_fallback_count(cpals_ctx* c, int64_t* count) {

@@ -203,6 +203,14 @@ int64_t cross_rows(int order, const int64_t* dims, int R, int num_sms);
 // Two launches: the split cross Grams (and the copy of the iterate), then the check.
 cudaError_t launch_cp_check(const CrossArgs& a, cudaStream_t st);
 
+// Sparse sign embedding (k_sketch.cu): n columns of zeta (row, +-1/sqrt(zeta)) entries.
+cudaError_t launch_sparse_sign(int64_t l, int64_t n, int zeta, int injective, uint64_t seed, int32_t* rows,
+                               double* vals, cudaStream_t st);
+// out (In x l, column-major) = sum over each output column's entries p (seg[j] .. seg[j+1])
+// of v[p] times the fibre starting at T[pos[p]] with element stride `stride`.
+cudaError_t launch_sketch_gather(const void* T, int tdtype, int64_t In, int64_t stride, const int64_t* seg,
+                                 const int64_t* pos, const double* v, int64_t l, double* out, cudaStream_t st);
+
 // Raises a kernel's dynamic shared-memory limit on the current device, once per (device,
 // kernel) per process (thread-safe).  The attribute is per device, so a process that drives
 // several GPUs sets it on each.

@@ -121,6 +121,17 @@ class Engine:
                 "cpals_check_converge")
         return bool(conv.value), float(val[0])
 
+    def sketched_matricization(self, mode, l, rows, vals, zeta):
+        """A_sk = T_(mode) Omega^T (I_mode x l) for the embedding given by 0-based ``rows`` and
+        ``vals`` (n * zeta entries, column c's at c * zeta ...)."""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        out = np.empty((self.dims[mode], int(l)), dtype=np.float64, order="F")
+        L.check(self.lib.cpals_sketched_matricization(self.h, int(mode), int(l), int(zeta),
+                                                      rows.ctypes.data_as(C.POINTER(C.c_int32)), L.dptr(vals),
+                                                      L.dptr(out)), "cpals_sketched_matricization")
+        return out
+
     def gram(self, mode):
         G = np.empty((self.rank, self.rank), dtype=np.float64)
         L.check(self.lib.cpals_get_gram(self.h, int(mode), L.dptr(G)), "cpals_get_gram")

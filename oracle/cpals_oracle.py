@@ -590,6 +590,75 @@ def lev_score_als(T, factors, lam, nsamps, sweeps, rng, normal=False, record=Non
 
 
 # ---------------------------------------------------------------------------
+# Sparse sign embeddings and the sketched matricization
+# ---------------------------------------------------------------------------
+def sparse_embedding(l, n, s, rows1, vals) -> np.ndarray:
+    """The dense l x n Omega of an embedding given as the reference leaves it after
+    sparse_sign_matrix (SEQRCS.jl:29-39): column c's s entries at rows1[c*s : c*s+s] (1-based)
+    with values vals[c*s : c*s+s]."""
+    om = np.zeros((l, n))
+    cols = np.repeat(np.arange(n), s)
+    np.add.at(om, (np.asarray(rows1[: n * s], dtype=np.int64) - 1, cols), np.asarray(vals[: n * s]))
+    return om
+
+
+def sketched_matricization(T, k, l, rows1, vals, s) -> np.ndarray:
+    """src/algebra/pivot_mapping.jl:111-140, step for step (k 0-based, rows1 1-based).
+
+    The entries are grouped by output column in entry order (dict_rows); entry p belongs to
+    column alpha = p div s + (p mod s > 0) of Omega (1-based p), whose fibre starts at
+    transform_alpha_to_vectorized_tensor_position (pivot_mapping.jl:52-55); output column j
+    is the dot product of the fibres at each mode-k index with the entries' values."""
+    v = np.asarray(T).reshape(-1, order="F")
+    didx = T.shape[k]
+    stride = int(np.prod(T.shape[:k], dtype=np.int64))
+    As = np.zeros((didx, l))
+    groups = {j: [] for j in range(1, l + 1)}
+    for p, j in enumerate(np.asarray(rows1), start=1):
+        groups[int(j)].append(p)
+    for j in range(1, l + 1):
+        nzs = np.asarray(groups[j], dtype=np.int64)
+        if nzs.size == 0:
+            continue
+        alpha = nzs // s + (nzs % s > 0)
+        tt = (alpha - 1) // stride
+        pos = tt * stride * didx + (alpha - tt * stride)  # 1-based positions
+        m2 = np.asarray(vals)[nzs - 1]
+        for i in range(didx):
+            As[i, j - 1] = np.dot(v[pos - 1 + stride * i], m2)
+    return As
+
+
+def load_ref_sparse_sign():
+    """The reference's own generators, compiled by build_oracle.py into _ref/ (None when the
+    reference checkout was not available to build them).  Returns (sparse_sign, sparsestack),
+    each called as f(l, n, zeta, vals, rows, colstarts) on numpy arrays, as SEQRCS.jl:41-60
+    calls them; their rand() stream is srand-seeded by the caller."""
+    import ctypes
+    from pathlib import Path
+
+    lib_path = Path(__file__).resolve().parent / "_ref" / "libsparse_sign.so"
+    if not lib_path.exists():
+        return None
+    lib = ctypes.CDLL(str(lib_path))
+    libc = ctypes.CDLL(None)
+    argt = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+
+    def wrap(fn):
+        fn.argtypes = argt
+        fn.restype = None
+
+        def call(l, n, zeta, vals, rows, colstarts, seed=1):
+            libc.srand(ctypes.c_uint(seed))
+            fn(int(l), int(n), int(zeta), vals.ctypes.data_as(argt[3]), rows.ctypes.data_as(argt[4]),
+               colstarts.ctypes.data_as(argt[5]))
+        return call
+
+    return wrap(lib.sparse_sign), wrap(lib.sparsestack)
+
+
+# ---------------------------------------------------------------------------
 # Synthetic low-rank-plus-noise generator (the benchmark workloads' tensors)
 # ---------------------------------------------------------------------------
 def congruent_factor(dim, rank, congruence, rng) -> np.ndarray:

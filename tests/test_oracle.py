@@ -298,3 +298,57 @@ def test_block_lev_score_sampled_converges(oracle):
             T, F, lam, 100, 100, np.random.default_rng(100 + t), normal=True, block_size=b)) - T) / np.linalg.norm(T)
             for t in range(3))
         assert best < 0.1
+
+
+def _embedding_structure(l, n, s, rows0, vals, injective):
+    """The structure both reference generators produce (sparse_sign.c, sparsestack.c)."""
+    a = 1.0 / np.sqrt(s)
+    R = np.asarray(rows0[: n * s]).reshape(n, s)
+    assert R.min() >= 0 and R.max() < l
+    assert np.all(np.abs(np.abs(np.asarray(vals[: n * s])) - a) < 1e-15)
+    assert all(len(set(r)) == s for r in R)  # distinct rows in every column
+    if injective:  # one row in each of s near-equal blocks, in block order
+        q, r = divmod(l, s)
+        starts = np.array([j * (q + 1) if j < r else r * (q + 1) + (j - r) * q for j in range(s)])
+        sizes = np.array([q + 1 if j < r else q for j in range(s)])
+        assert np.all(R >= starts[None, :]) and np.all(R < (starts + sizes)[None, :])
+
+
+@pytest.mark.parametrize("injective", [False, True])
+def test_reference_sparse_sign_generators_structure(oracle, injective):
+    # the reference's own C generators, compiled from its sources by oracle/build_oracle.py:
+    # these are the rules the device generator must follow (SEQRCS_test.jl:7-16)
+    ref = oracle.load_ref_sparse_sign()
+    if ref is None:
+        pytest.skip("reference generators not built (no reference checkout)")
+    fn = ref[1] if injective else ref[0]
+    for (l, n, s) in [(1200, 1000, 8), (50, 300, 4), (7, 40, 7), (13, 25, 5)]:
+        rows = np.empty(n * s, np.int32)
+        vals = np.empty(n * s)
+        cs = np.empty(n + 1, np.int32)
+        fn(l, n, s, vals, rows, cs, seed=11)
+        np.testing.assert_array_equal(cs, np.arange(n + 1) * s)
+        _embedding_structure(l, n, s, rows, vals, injective)
+
+
+def test_oracle_sketched_matricization_is_the_dense_product(oracle):
+    # test/pivot_mapping.jl:110-119 and test/SEQRCS_test.jl:24-25: the sketch equals
+    # T_(k) Omega^T; Omega from the reference generator when it is built
+    rng = np.random.default_rng(4)
+    ref = oracle.load_ref_sparse_sign()
+    for dims in [(3, 6, 8, 2), (7, 5), (4, 3, 5)]:
+        T = np.asfortranarray(rng.standard_normal(dims))
+        for k in range(len(dims)):
+            n = int(np.prod([d for m, d in enumerate(dims) if m != k]))
+            l, s = 11, 3
+            rows = np.empty(n * s, np.int32)
+            vals = np.empty(n * s)
+            if ref is not None:
+                ref[0](l, n, s, vals, rows, np.empty(n + 1, np.int32), seed=5 + k)
+            else:
+                rows[:] = np.concatenate([rng.choice(l, s, replace=False) for _ in range(n)])
+                vals[:] = rng.choice([-1.0, 1.0], n * s) / np.sqrt(s)
+            om = oracle.sparse_embedding(l, n, s, rows + 1, vals)
+            want = oracle.unfold(T, k) @ om.T
+            got = oracle.sketched_matricization(T, k, l, rows + 1, vals, s)
+            assert np.linalg.norm(got - want) <= 1e-12 * max(1.0, np.linalg.norm(want))

@@ -31,9 +31,22 @@ from .api import (
     sample_factor_matrices,
     sketched_matricization,
     sparse_sign_matrix,
+    ALS,
+    KSEQRCSPivProjected,
+    QRPivProjected,
+    SEQRCS,
+    SEQRCSPivProjected,
+    compute_als,
+    copy_alg,
+    omega_hadamard,
+    optimize,
+    qrcp,
+    start,
+    stop,
+    update_samples,
 )
 from .batched import BatchEngine
-from .engine import Engine
+from .engine import Engine, QRCPResult
 from . import warmstart
 from .warmstart import WarmStartMLP
 
@@ -41,4 +54,6 @@ __all__ = [
     "BatchEngine", "BlockLevScoreSampled", "CPAngleCheck", "CPD", "CPDFit", "CPDiffCheck", "ConvergeAlg", "CpalsError", "Engine", "FitCheck", "GB300Normal", "KRPFreeNormal", "KRPNormal",
     "LevScoreSampled", "MttkrpAlgorithm", "NoCheck", "ProjectionAlgorithm", "als_optimize", "cp_rank", "decompose",
     "increase_cpd_rank", "load", "random_CPD", "random_factors", "sample_factor_matrices", "block_sample_factor_matrices", "sparse_sign_matrix", "sketched_matricization", "WarmStartMLP", "warmstart",
+    "ALS", "KSEQRCSPivProjected", "QRCPResult", "QRPivProjected", "SEQRCS", "SEQRCSPivProjected", "compute_als",
+    "copy_alg", "omega_hadamard", "optimize", "qrcp", "start", "stop", "update_samples",
 ]

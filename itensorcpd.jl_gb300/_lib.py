@@ -72,6 +72,15 @@ SIGNATURES = {
     "cpals_sparse_sign": (C.c_int, [C.c_int, C.c_int64, C.c_int64, C.c_int, C.c_int, C.c_uint64,
                                     C.POINTER(C.c_int32), _DP, C.POINTER(C.c_int32)]),
     "cpals_sketched_matricization": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_int32), _DP, _DP]),
+    "cpals_qrcp": (C.c_int, [C.c_int, C.c_int64, C.c_int64, _DP, C.c_int64, C.c_int64, C.c_double, _I64P, _DP,
+                             _I64P, _DP, _DP]),
+    "cpals_unfolding_qrcp": (C.c_int, [_P, C.c_int, C.c_int64, _I64P, C.c_int64, C.c_int64, C.c_double, _I64P,
+                                       _DP, _I64P, _DP, _DP]),
+    "cpals_krp_qrcp": (C.c_int, [_P, C.c_int, C.c_int64, _I64P, C.c_int64, C.c_int64, C.c_double, _I64P, _DP,
+                                 _I64P, _DP, _DP]),
+    "cpals_omega_hadamard": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_int32), _DP, _DP]),
+    "cpals_seqrcs": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_int32), _DP, C.c_int64,
+                               C.c_int, C.c_int, C.c_double, _I64P, _DP, _I64P, _I64P, _DP, _DP]),
     "cpals_fallback_count": (C.c_int, [_P, _I64P]),
     "cpals_synchronize": (C.c_int, [_P]),
     "cpals_timer_start": (C.c_int, [_P]),

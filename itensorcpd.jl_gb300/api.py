@@ -7,6 +7,7 @@ reference's (first index fastest in memory is handled by the binding).
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import warnings
 from dataclasses import dataclass, field
@@ -14,7 +15,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib as L
-from .engine import Engine
+from .engine import Engine, QRCPResult
 
 
 # ---------------------------------------------------------------------------
@@ -353,6 +354,9 @@ def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=Fa
     alg = KRPFreeNormal() if alg is None else alg
     check = NoCheck(100 if maxiter is None else maxiter) if check is None else check
     R = cp_rank(cp)
+    if isinstance(alg, PivotBasedSolvers):
+        als = compute_als(T, cp, alg=alg, check=check, rng=rng, device=device, **kwargs)
+        return optimize(cp, als, verbose=verbose, device=device)
     if isinstance(alg, ProjectionAlgorithm):
         return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal,
                                    stop_resample=int(kwargs.get("stop_resample", -1)),
@@ -437,26 +441,24 @@ def block_sample_factor_matrices(nsamps, probs, block_size, skip, rng):
     return np.asfortranarray(out)
 
 
-def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal, stop_resample=-1, on_pivots=None):
-    """LevScoreSampled / BlockLevScoreSampled: compute_als (optimizers/.../krp_lev_score_sampled.jl:1-40,
-    42-80: initial leverage weights and one draw per mode) and the per-mode project_krp /
-    matricize_tensor / solve / post_solve of algorithms/.../randomized/krp_lev_score_sampled.jl:20-58,
-    80-106.  A mode draws new pivots while stop_resample < 0 or stop_resample > iter(als)
-    (the check's iteration count); otherwise it reuses its last pivots.  ``on_pivots(mode,
-    pivots)`` (optional) sees every mode's pivots before its solve."""
-    rng = np.random.default_rng(3) if rng is None else rng
+def _sampled_loop(T, cp, alg_name, check, verbose, device, normal, begin, pivots_for, after=None):
+    """The sweep loop of the ProjectionAlgorithm solvers (optimize.jl:15-32 with
+    randomized/ProjectionAlgorithm.jl:6-68): for every sweep and mode, ``pivots_for(mode, it)``
+    gives the mode's pivots (1-based multi-coordinates), ``cpals_sampled_update`` runs
+    project_krp / matricize_tensor / solve_ls_problem / row_norm on the device, then
+    ``after(mode, eng)``.  ``begin(eng)`` runs once, with the tensor and factors set.  A FitCheck
+    is not honoured (ProjectionAlgorithm.jl:30-36: a warning, then max_counter sweeps);
+    CPDiffCheck / CPAngleCheck run on the device after every sweep."""
     R = cp_rank(cp)
     N = T.ndim
     if isinstance(check, FitCheck) and check.iter == 0:
-        # ProjectionAlgorithm.jl:30-36: a FitCheck is not honoured by sampled solvers
-        print(f"Warning: FitCheck is not enabled for {type(alg).__name__} will run {check.max_counter} iterations.")
+        print(f"Warning: FitCheck is not enabled for {alg_name} will run {check.max_counter} iterations.")
     sweeps = max(0, int(check.max_counter) - int(check.iter))
     cross = isinstance(check, (CPDiffCheck, CPAngleCheck))
     with Engine(T.shape, R, dtype=T.dtype, precision="fp64", device=device) as eng:
         eng.set_tensor(T)
         eng.set_factors(cp.factors, cp.lam)
-        probs = [eng.leverage_scores(n) for n in range(N)]
-        pivots = [alg.sample(n, probs, rng) for n in range(N)]
+        begin(eng)
         if cross:  # ProjectionAlgorithm.jl:53: these checks run as for the exact solvers
             c = _to_device_check(check)
             _prev_in(eng, check)
@@ -464,14 +466,10 @@ def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal, stop_re
             traj = []
         for s in range(sweeps):
             it = int(c.iter) if cross else int(check.iter) + s
-            resample = stop_resample < 0 or stop_resample > it
             for n in range(N):
-                if resample:
-                    pivots[n] = alg.sample(n, probs, rng)
-                if on_pivots is not None:
-                    on_pivots(n, pivots[n])
-                eng.sampled_update(n, pivots[n], normal=normal)
-                probs[n] = eng.leverage_scores(n)
+                eng.sampled_update(n, pivots_for(n, it), normal=normal)
+                if after is not None:
+                    after(n, eng)
             if cross:
                 done, val = eng.check_converge(c)
                 traj.append(val)
@@ -491,6 +489,34 @@ def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal, stop_re
         factors = [F.astype(np.float32) for F in factors]
         lam = lam.astype(np.float32)
     return CPD(factors, lam, T.shape)
+
+
+def _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal, stop_resample=-1, on_pivots=None):
+    """LevScoreSampled / BlockLevScoreSampled: compute_als (optimizers/.../krp_lev_score_sampled.jl:1-40,
+    42-80: initial leverage weights and one draw per mode) and the per-mode project_krp /
+    matricize_tensor / solve / post_solve of algorithms/.../randomized/krp_lev_score_sampled.jl:20-58,
+    80-106.  A mode draws new pivots while stop_resample < 0 or stop_resample > iter(als)
+    (the check's iteration count); otherwise it reuses its last pivots.  ``on_pivots(mode,
+    pivots)`` (optional) sees every mode's pivots before its solve."""
+    rng = np.random.default_rng(3) if rng is None else rng
+    N = T.ndim
+    state = {}
+
+    def begin(eng):
+        state["probs"] = [eng.leverage_scores(n) for n in range(N)]
+        state["pivots"] = [alg.sample(n, state["probs"], rng) for n in range(N)]
+
+    def pivots_for(n, it):
+        if stop_resample < 0 or stop_resample > it:
+            state["pivots"][n] = alg.sample(n, state["probs"], rng)
+        if on_pivots is not None:
+            on_pivots(n, state["pivots"][n])
+        return state["pivots"][n]
+
+    def after(n, eng):
+        state["probs"][n] = eng.leverage_scores(n)
+
+    return _sampled_loop(T, cp, type(alg).__name__, check, verbose, device, normal, begin, pivots_for, after)
 
 
 def sparse_sign_matrix(l, n, s, rows=None, vals=None, *, omega=False, injective=False, seed=0, device=0):
@@ -530,6 +556,357 @@ def sketched_matricization(T, k, l, rows, vals, s, device=0):
     with Engine(T.shape, 1, dtype=T.dtype, precision="fp64", device=device) as eng:
         eng.set_tensor(T)
         return eng.sketched_matricization(int(k), int(l), r0.astype(np.int32), vals, int(s))
+
+
+# ---------------------------------------------------------------------------
+# Column-pivoted QR, SE-QRCS and the QR-pivoted projection solvers
+# (src/algebra/SEQRCS.jl, algorithms/.../randomized/qr_lev_score_sampled.jl,
+#  optimizers/.../randomized/qr_lev_score_sampled.jl)
+# ---------------------------------------------------------------------------
+def qrcp(A, *, ncand=0, max_steps=0, stop_ratio=-1.0, device=0):
+    """qr(A, ColumnNorm()) on the device (``cpals_qrcp``): returns a QRCPResult whose
+    ``Q, R, p`` are LAPACK xGEQP3's (p 1-based).  ``ncand`` limits the pivots to the first
+    columns, ``max_steps`` / ``stop_ratio`` end the factorization early."""
+    A = np.asfortranarray(np.asarray(A, dtype=np.float64))
+    if A.ndim != 2 or A.size == 0:
+        raise ValueError("A must be a nonempty matrix")
+    m, n = A.shape
+    lib = L.load()
+    kcap = min(m, n)
+    perm = np.empty(n, dtype=np.int64)
+    rdiag = np.empty(kcap, dtype=np.float64)
+    steps = np.zeros(1, dtype=np.int64)
+    R = np.empty(kcap * n, dtype=np.float64)
+    Q = np.empty(m * kcap, dtype=np.float64)
+    L.check(lib.cpals_qrcp(int(device), m, n, L.dptr(A), int(ncand), int(max_steps), float(stop_ratio),
+                           L.i64ptr(perm), L.dptr(rdiag), L.i64ptr(steps), L.dptr(R), L.dptr(Q)), "cpals_qrcp")
+    return QRCPResult.make(perm, rdiag, int(steps[0]), m, n, R, Q)
+
+
+def _embedding(l, n, s, injective, seed, device):
+    """An l x n sparse sign embedding from the device generator: 0-based rows, vals, s_eff."""
+    rows, vals = sparse_sign_matrix(l, n, s, injective=injective, seed=seed, device=device)
+    s_eff = min(int(s), int(l))
+    return rows[: n * s_eff] - 1, vals[: n * s_eff], s_eff
+
+
+def _other_dims(dims, mode):
+    return [d for m, d in enumerate(dims) if m != mode]
+
+
+def SEQRCS(A, mode=None, l=None, s=None, t=None, *, compute_r=True, use_omega=False, injective=False,  # noqa: N802
+           rows=None, vals=None, seed=0, stop_ratio=-1.0, device=0):
+    """SE-QRCS (src/algebra/SEQRCS.jl:83-240) on the device.  ``SEQRCS(T, mode, l, s, t)``
+    pivots the mode unfolding of the tensor T (``mode`` 0-based); ``SEQRCS(factors, l, s, t)``
+    (a list of I_m x R matrices) pivots the transposed Khatri-Rao product of the factors
+    (SEQRCS.jl:184-240).  The embedding comes from the device generator (``seed``) unless
+    1-based ``rows`` / ``vals`` are given.  Returns a QRCPResult: ``Q, R, p = SEQRCS(...)``; R is
+    None unless ``compute_r``, and ``rdiag`` always holds diag(R) of the subset's QR."""
+    krp = isinstance(A, (list, tuple))
+    if krp:
+        l, s, t = mode, l, s
+        factors = [np.asarray(F, dtype=np.float64) for F in A]
+        R = factors[0].shape[1]
+        dims = tuple(F.shape[0] for F in factors) + (1,)
+        kmode = len(factors)
+    else:
+        T = _prepare_target(A)
+        dims = T.shape
+        kmode = int(mode)
+    n = int(np.prod(_other_dims(dims, kmode)))
+    if rows is None:
+        r0, v, s_eff = _embedding(l, n, s, injective, seed, device)
+    else:
+        s_eff = min(int(s), int(l))
+        r0 = np.ascontiguousarray(rows, dtype=np.int64)[: n * s_eff] - 1
+        v = np.ascontiguousarray(vals, dtype=np.float64)[: n * s_eff]
+    if krp:
+        # the KRP path always selects with the explicit Omega (SEQRCS.jl:203-205): column order
+        with Engine(dims, R, dtype=np.float64, precision="fp64", device=device) as eng:
+            eng.set_factors(list(factors) + [np.ones((1, R))], np.ones(R))
+            return eng.seqrcs(1, kmode, l, r0, v, s_eff, t, sorted_subset=True, compute_r=compute_r,
+                              stop_ratio=stop_ratio)
+    with Engine(dims, 1, dtype=T.dtype, precision="fp64", device=device) as eng:
+        eng.set_tensor(T)
+        return eng.seqrcs(0, kmode, l, r0, v, s_eff, t, sorted_subset=use_omega, compute_r=compute_r,
+                          stop_ratio=stop_ratio)
+
+
+def omega_hadamard(factors, rows, vals, l, s, device=0):
+    """omega_hadamard (src/algebra/had_contract.jl:300-326): Omega times the Khatri-Rao product
+    of ``factors`` (I_m x R matrices, the first index fastest), l x R, for the embedding in
+    1-based ``rows`` / ``vals``."""
+    factors = [np.asarray(F, dtype=np.float64) for F in factors]
+    R = factors[0].shape[1]
+    dims = tuple(F.shape[0] for F in factors) + (1,)
+    n = int(np.prod(dims))
+    s_eff = min(int(s), int(l))
+    r0 = np.ascontiguousarray(rows, dtype=np.int64)[: n * s_eff] - 1
+    with Engine(dims, R, dtype=np.float64, precision="fp64", device=device) as eng:
+        eng.set_factors(list(factors) + [np.ones((1, R))], np.ones(R))
+        return eng.omega_hadamard(len(factors), l, r0, np.asarray(vals, dtype=np.float64)[: n * s_eff], s_eff)
+
+
+def _range_arg(x):
+    if isinstance(x, (tuple, list)):
+        return tuple(int(v) for v in x)
+    return int(x)
+
+
+class _PivotBased(ProjectionAlgorithm):
+    """Start / End of the pivot range (1-based, inclusive; End 0 = every column), one value
+    or one per mode (qr_lev_score_sampled.jl:9-20)."""
+
+    def __init__(self, start, end):
+        self.Start = _range_arg(start)
+        self.End = _range_arg(end)
+
+    def _per_mode(self, v, mode):
+        return v if isinstance(v, int) else (v[0] if len(v) == 1 else v[mode])
+
+
+class QRPivProjected(_PivotBased):
+    """qr_lev_score_sampled.jl:9-20: projection by the pivots of the column-pivoted QR of each
+    mode unfolding.  ``QRPivProjected()`` = (1, 0), ``(n)`` = (1, n), ``((n1, n2, ...))`` =
+    per-mode ends from 1, ``(start, end)``."""
+
+    def __init__(self, *args):
+        if len(args) == 0:
+            start, end = 1, 0
+        elif len(args) == 1:
+            end = args[0]
+            start = tuple(1 for _ in end) if isinstance(end, (tuple, list)) else 1
+        else:
+            start, end = args
+        super().__init__(start, end)
+
+
+class _RandomModes(_PivotBased):
+    def __init__(self, *args):
+        if len(args) == 0:
+            start, end, rr, rank_vect = 1, 0, None, None
+        elif len(args) == 1:
+            end = args[0]
+            start, rr, rank_vect = (tuple(1 for _ in end) if isinstance(end, (tuple, list)) else 1), None, None
+        else:
+            start, end = args[0], args[1]
+            rr = args[2] if len(args) > 2 else None
+            rank_vect = args[3] if len(args) > 3 else None
+        super().__init__(start, end)
+        if rr is not None and not isinstance(rr, (tuple, list)):
+            rr = (rr,)
+        self.random_modes = None if rr is None else tuple(int(m) for m in rr)
+        if rank_vect is None or isinstance(rank_vect, dict):
+            self.rank_vect = rank_vect
+        else:
+            rv = rank_vect if isinstance(rank_vect, (tuple, list)) else (rank_vect,)
+            if len(rv) == 1 and len(self.random_modes) > 1:
+                rv = tuple(rv) * len(self.random_modes)  # Dict(rrmodes .=> Tuple(r)) broadcasts a scalar
+            self.rank_vect = dict(zip(self.random_modes, (int(r) for r in rv)))
+
+
+class SEQRCSPivProjected(_RandomModes):
+    """qr_lev_score_sampled.jl:25-48: QRPivProjected with SE-QRCS pivots on ``random_modes``
+    (mode numbers from 1, as in the reference); ``rank_vect`` gives each such mode's sketch
+    pivot count t."""
+
+
+class KSEQRCSPivProjected(_RandomModes):
+    """qr_lev_score_sampled.jl:51-82: pivots from the Khatri-Rao product of a preliminary
+    leverage-score ALS solution (SE-QRCS on ``random_modes``, the KRP's pivoted QR elsewhere)."""
+
+
+PivotBasedSolvers = (QRPivProjected, SEQRCSPivProjected, KSEQRCSPivProjected)
+
+
+def start(alg):
+    return alg.Start
+
+
+def stop(alg):
+    return alg.End
+
+
+def copy_alg(alg, new_start=0, new_end=0):
+    """qr_lev_score_sampled.jl:18-20, 45-47, 79-81: the algorithm with a new pivot range
+    (0 keeps the old one)."""
+    zero = (lambda v: all(int(x) == 0 for x in v)) if isinstance(new_start, (tuple, list)) else (lambda v: int(v) == 0)
+    st = alg.Start if zero(new_start) else _range_arg(new_start)
+    zero = (lambda v: all(int(x) == 0 for x in v)) if isinstance(new_end, (tuple, list)) else (lambda v: int(v) == 0)
+    en = alg.End if zero(new_end) else _range_arg(new_end)
+    out = copy.copy(alg)
+    out.Start, out.End = st, en
+    return out
+
+
+class ALS:
+    """The ALS state compute_als builds for the pivot-based solvers: the target, the algorithm,
+    ``additional_items`` (the reference's extra_args keys) and the check."""
+
+    def __init__(self, target, mttkrp_alg, additional_items, check):
+        self.target = target
+        self.mttkrp_alg = mttkrp_alg
+        self.additional_items = additional_items
+        self.check = check
+
+
+def _pivot_range(alg, mode, dRis):
+    """qr_lev_score_sampled.jl:48-56: the (start, end) of the pivots a mode keeps."""
+    int_end = alg._per_mode(stop(alg), mode)
+    int_end = dRis if int_end == 0 else int_end
+    int_end = min(int_end, dRis)
+    int_start = alg._per_mode(start(alg), mode)
+    if not (0 < int_start <= int_end):
+        raise AssertionError("int_start > 0 && int_start <= int_end")
+    return int_start, int_end
+
+
+def _effective_rank(rdiag, trunc_tol):
+    d = np.abs(np.asarray(rdiag, dtype=np.float64))
+    if d.size == 0:
+        return 0
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return int(np.sum(d / d.max() > trunc_tol))
+
+
+def _arrange(p, meff, shuffle_pivots, rng):
+    """p1 = p[1:meff] kept, the rest shuffled (qr_lev_score_sampled.jl:29-34)."""
+    p = np.asarray(p, dtype=np.int64)
+    rest = p[meff:]
+    if shuffle_pivots:
+        rest = rest[rng.permutation(rest.size)]
+    return np.concatenate([p[:meff], rest])
+
+
+def _column_to_multi_coords(cols1, dims):
+    """column_to_multi_coords (pivot_mapping.jl:17-35): 1-based linear column ids of the
+    other modes (the first fastest) to 1-based coordinates, one row per id."""
+    c = np.asarray(cols1, dtype=np.int64) - 1
+    out = np.empty((c.size, len(dims)), dtype=np.int64)
+    for k, d in enumerate(dims):
+        out[:, k] = c % d + 1
+        c = c // d
+    return out
+
+
+def compute_als(target, cp: CPD, alg=None, check=None, *, shuffle_pivots=True, trunc_tol=0.01, normal=True,
+                injective=False, guess_num_levs=None, prelim_sample_size=None, prelim_niter=10, rng=None, seed=None,
+                device=0, **kwargs) -> ALS:
+    """compute_als of the pivot-based solvers (optimizers/.../randomized/qr_lev_score_sampled.jl:1-281):
+    per mode, the column-pivoted QR of the mode unfolding (QRPivProjected), SE-QRCS on the
+    random modes (SEQRCSPivProjected), or of the Khatri-Rao product of a preliminary
+    leverage-score ALS solution (KSEQRCSPivProjected); the effective rank meff (the number of
+    |r_jj| / max |r_jj| above trunc_tol); the first meff pivots kept and the rest shuffled; the
+    pivots start..end as the mode's projector.  Pivot factorizations run on the device; the
+    shuffles and the embedding seeds come from ``rng``."""
+    if not isinstance(alg, PivotBasedSolvers):
+        raise TypeError("compute_als here builds the pivot-based solvers' state")
+    T = _prepare_target(target)
+    rng = np.random.default_rng(3) if rng is None else rng
+    N = T.ndim
+    stop_ratio = float(trunc_tol) if shuffle_pivots else -1.0
+    random_modes = tuple(getattr(alg, "random_modes", None) or ())
+    rank_sk = getattr(alg, "rank_vect", None)
+    ref_pivs, pivots, projectors, eff = [], [], [], []
+
+    def finish(n, res):
+        dims_o = _other_dims(T.shape, n)
+        dRis = int(np.prod(dims_o))
+        ref_pivs.append(np.asarray(res.p, dtype=np.int64).copy())
+        meff = _effective_rank(res.rdiag, trunc_tol)
+        eff.append(meff)
+        p = _arrange(res.p, meff, shuffle_pivots, rng)
+        pv = _column_to_multi_coords(p, dims_o)
+        pivots.append(pv)
+        s0, e0 = _pivot_range(alg, n, dRis)
+        projectors.append(pv[s0 - 1: e0].copy())
+
+    def sketch_params(n, int_end):
+        m = T.shape[n]
+        k_sk = int_end if rank_sk is None else int(rank_sk[n + 1])
+        l = int(round(3 * m * np.log(m)))
+        s = int(round(np.log(m)))
+        return l, max(s, 1), k_sk
+
+    if isinstance(alg, KSEQRCSPivProjected):
+        # a preliminary leverage-score ALS puts the factors near T's leverage structure
+        # (qr_lev_score_sampled.jl:196-207)
+        if guess_num_levs is None:
+            base = cp
+            nsamp = 10 * cp_rank(cp) if prelim_sample_size is None else int(prelim_sample_size)
+        else:
+            base = random_CPD(T, int(guess_num_levs), rng)
+            nsamp = 10 * cp_rank(cp) if prelim_sample_size is None else int(prelim_sample_size)
+        upd = als_optimize(T, base, alg=LevScoreSampled(nsamp), check=NoCheck(int(prelim_niter)), normal=True,
+                           stop_resample=0, rng=rng, device=device)
+        Rk = cp_rank(upd)
+        with Engine(T.shape, Rk, dtype=np.float64, precision="fp64", device=device) as eng:
+            eng.set_factors([np.asarray(F, dtype=np.float64) for F in upd.factors], np.asarray(upd.lam, np.float64))
+            for n in range(N):
+                dRis = int(np.prod(_other_dims(T.shape, n)))
+                _, int_end = _pivot_range(alg, n, dRis)
+                if (n + 1) in random_modes:
+                    l, s, k_sk = sketch_params(n, int_end)
+                    sd = int(rng.integers(0, 2**63)) if seed is None else int(seed) + n
+                    r0, v, s_eff = _embedding(l, dRis, s, injective, sd, device)
+                    res = eng.seqrcs(1, n, l, r0, v, s_eff, k_sk, sorted_subset=True, stop_ratio=stop_ratio)
+                else:
+                    res = eng.krp_qrcp(n, stop_ratio=stop_ratio)
+                finish(n, res)
+    else:
+        with Engine(T.shape, 1, dtype=T.dtype, precision="fp64", device=device) as eng:
+            eng.set_tensor(T)
+            for n in range(N):
+                dRis = int(np.prod(_other_dims(T.shape, n)))
+                _, int_end = _pivot_range(alg, n, dRis)
+                if isinstance(alg, SEQRCSPivProjected) and (n + 1) in random_modes:
+                    l, s, k_sk = sketch_params(n, int_end)
+                    sd = int(rng.integers(0, 2**63)) if seed is None else int(seed) + n
+                    r0, v, s_eff = _embedding(l, dRis, s, injective, sd, device)
+                    res = eng.seqrcs(0, n, l, r0, v, s_eff, k_sk, sorted_subset=False, stop_ratio=stop_ratio)
+                else:
+                    res = eng.unfolding_qrcp(n, stop_ratio=stop_ratio)
+                finish(n, res)
+    items = {
+        "ref_projectors": ref_pivs,
+        "projects": pivots,
+        "projects_tensors": projectors,
+        "effective_ranks": eff,
+        "normal": bool(normal),
+    }
+    return ALS(T, alg, items, NoCheck(100) if check is None else check)
+
+
+def update_samples(target, als: ALS, new_num_end, reshuffle=False, new_num_start=0, rng=None) -> ALS:
+    """update_samples (algorithms/.../randomized/qr_lev_score_sampled.jl:93-144): the same pivots
+    with a new range; ``reshuffle`` redraws the order of the pivots past each mode's effective
+    rank."""
+    if not isinstance(als.mttkrp_alg, PivotBasedSolvers):
+        raise AssertionError("als.mttkrp_alg isa PivotBasedSolvers")
+    rng = np.random.default_rng() if rng is None else rng
+    T = _prepare_target(target)
+    alg = copy_alg(als.mttkrp_alg, new_num_start, new_num_end)
+    items = dict(als.additional_items)
+    pivots = [p.copy() for p in items["projects"]]
+    projectors = []
+    for pos, (p, meff) in enumerate(zip(items["ref_projectors"], items["effective_ranks"])):
+        dims_o = _other_dims(T.shape, pos)
+        if reshuffle:
+            pivots[pos] = _column_to_multi_coords(_arrange(p, meff, True, rng), dims_o)
+        s0, e0 = _pivot_range(alg, pos, int(np.prod(dims_o)))
+        projectors.append(pivots[pos][s0 - 1: e0].copy())
+    items["projects"] = pivots
+    items["projects_tensors"] = projectors
+    return ALS(als.target, alg, items, als.check)
+
+
+def optimize(cp: CPD, als: ALS, verbose=False, device=0) -> CPD:
+    """optimize (optimize.jl:6-35) for an ALS built by compute_als: every sweep solves each
+    mode's projected problem at its fixed pivots."""
+    T = als.target
+    proj = als.additional_items["projects_tensors"]
+    return _sampled_loop(T, cp, type(als.mttkrp_alg).__name__, als.check, verbose, device,
+                         als.additional_items["normal"], lambda eng: None, lambda n, it: proj[n])
 
 
 def decompose(A, rank, max_rank=None, *, solver=None, rng=None, alg=None, check=None, maxiter=None, verbose=False,

@@ -1001,6 +1001,418 @@ int cpals_sketched_matricization(cpals_ctx* c, int mode, int64_t l, int zeta, co
   return rc;
 }
 
+// ---- column-pivoted QR, SE-QRCS ----
+}  // extern "C"
+
+namespace {
+
+// Device buffers of one column-pivoted QR of an m x n matrix (filled by the caller into A).
+struct QrcpBuffers {
+  double *A = nullptr, *vn1 = nullptr, *vn2 = nullptr, *vbuf = nullptr, *taus = nullptr, *rdiag = nullptr;
+  double* Q = nullptr;
+  int64_t* perm = nullptr;
+  QrcpArg* part = nullptr;
+  QrcpState* st = nullptr;
+  QrcpBuffers() = default;
+  QrcpBuffers(const QrcpBuffers&) = delete;
+  QrcpBuffers& operator=(const QrcpBuffers&) = delete;
+  ~QrcpBuffers() {
+    cudaFree(A);
+    cudaFree(vn1);
+    cudaFree(vn2);
+    cudaFree(vbuf);
+    cudaFree(taus);
+    cudaFree(rdiag);
+    cudaFree(Q);
+    cudaFree(perm);
+    cudaFree(part);
+    cudaFree(st);
+  }
+  int alloc(int64_t m, int64_t n, int64_t kmax, int num_sms) {
+    if (dmalloc(&A, (size_t)(m * n)) != CPALS_OK || dmalloc(&vn1, (size_t)n) != CPALS_OK ||
+        dmalloc(&vn2, (size_t)n) != CPALS_OK || dmalloc(&vbuf, (size_t)m) != CPALS_OK ||
+        dmalloc(&taus, (size_t)kmax) != CPALS_OK || dmalloc(&rdiag, (size_t)kmax) != CPALS_OK ||
+        dmalloc(&perm, (size_t)n) != CPALS_OK || dmalloc(&part, (size_t)qrcp_parts(n, num_sms)) != CPALS_OK ||
+        dmalloc(&st, 1) != CPALS_OK)
+      return CPALS_E_CUDA;
+    return CPALS_OK;
+  }
+};
+
+int64_t qrcp_kmax(int64_t m, int64_t ncand, int64_t max_steps) {
+  int64_t k = std::min(m, ncand);
+  if (max_steps > 0) k = std::min(k, max_steps);
+  return k;
+}
+
+// Factors b.A (m x n, filled) and copies out: perm0 (n, 0-based original column of each
+// position), rdiag (steps), steps, and when non-null R (steps x n, column-major, zero below
+// the diagonal) and Q (m x steps).
+int qrcp_run(QrcpBuffers& b, int64_t m, int64_t n, int64_t ncand, int64_t kmax, double stop_ratio, int num_sms,
+             cudaStream_t st, int64_t* perm0, double* rdiag, int64_t* steps, double* R, double* Q) {
+  QrcpJob q{};
+  q.A = b.A;
+  q.m = m;
+  q.n = n;
+  q.ncand = ncand;
+  q.kmax = kmax;
+  q.stop_ratio = stop_ratio;
+  q.vn1 = b.vn1;
+  q.vn2 = b.vn2;
+  q.vbuf = b.vbuf;
+  q.taus = b.taus;
+  q.rdiag = b.rdiag;
+  q.perm = b.perm;
+  q.part = b.part;
+  q.st = b.st;
+  q.num_sms = num_sms;
+  CPALS_CUDA_TRY(launch_qrcp_init(q, st));
+  QrcpState hs{};
+  for (int64_t j = 0; j < kmax;) {
+    // with a stopping ratio, look at the state every 32 steps; the steps after a stop return at once
+    const int64_t j1 = stop_ratio >= 0.0 ? std::min(kmax, j + 32) : kmax;
+    for (; j < j1; ++j) CPALS_CUDA_TRY(launch_qrcp_step(q, j, st));
+    if (j < kmax) {
+      CPALS_CUDA_TRY(cudaMemcpyAsync(&hs, b.st, sizeof(QrcpState), cudaMemcpyDeviceToHost, st));
+      CPALS_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hs.done) break;
+    }
+  }
+  CPALS_CUDA_TRY(cudaMemcpyAsync(&hs, b.st, sizeof(QrcpState), cudaMemcpyDeviceToHost, st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(st));
+  const int64_t k = hs.steps;
+  *steps = k;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(perm0, b.perm, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st));
+  if (k > 0) CPALS_CUDA_TRY(cudaMemcpyAsync(rdiag, b.rdiag, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+  if (R && k > 0)
+    CPALS_CUDA_TRY(cudaMemcpy2DAsync(R, sizeof(double) * k, b.A, sizeof(double) * m, sizeof(double) * k, n,
+                                     cudaMemcpyDeviceToHost, st));
+  if (Q && k > 0) {
+    if (dmalloc(&b.Q, (size_t)(m * k)) != CPALS_OK) return CPALS_E_CUDA;
+    CPALS_CUDA_TRY(launch_qr_form_q(b.A, m, k, b.taus, b.Q, num_sms, st));
+    CPALS_CUDA_TRY(cudaMemcpyAsync(Q, b.Q, sizeof(double) * m * k, cudaMemcpyDeviceToHost, st));
+  }
+  CPALS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (R)
+    for (int64_t c = 0; c < std::min(k, n); ++c)
+      for (int64_t r = c + 1; r < k; ++r) R[c * k + r] = 0.0;
+  return CPALS_OK;
+}
+
+int64_t other_extent(const cpals_ctx* c, int mode) {
+  int64_t n = 1;
+  for (int m = 0; m < c->order; ++m)
+    if (m != mode) n *= c->dims[m];
+  return n;
+}
+
+// Validates 1-based column ids (or none) and uploads them 0-based; ncols <= 0 with no ids
+// means every column.
+int upload_cols(int64_t n, int64_t ncols, const int64_t* cols1, int64_t** dcols, int64_t* count, cudaStream_t st) {
+  *dcols = nullptr;
+  if (!cols1) {
+    if (ncols > 0 && ncols != n) return CPALS_E_ARG;
+    *count = n;
+    return CPALS_OK;
+  }
+  if (ncols <= 0) return CPALS_E_ARG;
+  std::vector<int64_t> h((size_t)ncols);
+  for (int64_t i = 0; i < ncols; ++i) {
+    if (cols1[i] < 1 || cols1[i] > n) return CPALS_E_ARG;
+    h[(size_t)i] = cols1[i] - 1;
+  }
+  if (dmalloc(dcols, (size_t)ncols) != CPALS_OK) return CPALS_E_CUDA;
+  CPALS_CUDA_TRY(cudaMemcpyAsync(*dcols, h.data(), sizeof(int64_t) * ncols, cudaMemcpyHostToDevice, st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(st));
+  *count = ncols;
+  return CPALS_OK;
+}
+
+// Fills dst (m x ncols) with columns dcols (0-based; all when null) of the mode unfolding
+// (source 0) or of the transposed Khatri-Rao product of the other factors (source 1).
+cudaError_t fill_columns(cpals_ctx* c, int source, int mode, const int64_t* dcols, int64_t ncols, double* dst) {
+  if (source == 0) {
+    int64_t stride = 1;
+    for (int m = 0; m < mode; ++m) stride *= c->dims[m];
+    return launch_unfold_cols(c->dT, c->tdtype, c->dims[mode], stride, dcols, ncols, dst, c->st);
+  }
+  return launch_krp_cols(factor_set(c), c->order, mode, c->dims, dcols, ncols, (int)c->R, dst, c->st);
+}
+
+int source_ready(const cpals_ctx* c, int source) {
+  if (source == 0) return c->T_set ? CPALS_OK : CPALS_E_STATE;
+  if (source == 1) return c->F_set ? CPALS_OK : CPALS_E_STATE;
+  return CPALS_E_ARG;
+}
+
+int matrix_qrcp(cpals_ctx* c, int source, int mode, int64_t ncols, const int64_t* cols1, int64_t ncand,
+                int64_t max_steps, double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R,
+                double* Q) {
+  if (!c || mode < 0 || mode >= c->order || !perm || !rdiag || !steps) return CPALS_E_ARG;
+  int rc = source_ready(c, source);
+  if (rc != CPALS_OK) return rc;
+  DeviceGuard g(c->device);
+  const int64_t m = source == 0 ? c->dims[mode] : c->R;
+  int64_t* dcols = nullptr;
+  int64_t n = 0;
+  rc = upload_cols(other_extent(c, mode), ncols, cols1, &dcols, &n, c->st);
+  if (rc == CPALS_OK) {
+    ncand = (ncand <= 0 || ncand > n) ? n : ncand;
+    const int64_t kmax = qrcp_kmax(m, ncand, max_steps);
+    QrcpBuffers b;
+    std::vector<int64_t> p0((size_t)n);
+    rc = b.alloc(m, n, kmax, c->num_sms);
+    if (rc == CPALS_OK) {
+      cudaError_t e = fill_columns(c, source, mode, dcols, n, b.A);
+      rc = (e == cudaSuccess) ? qrcp_run(b, m, n, ncand, kmax, stop_ratio, c->num_sms, c->st, p0.data(), rdiag, steps,
+                                         R, Q)
+                              : CPALS_E_CUDA;
+      if (e != cudaSuccess) fprintf(stderr, "libcpals: column gather failed: %s\n", cudaGetErrorString(e));
+    }
+    if (rc == CPALS_OK)
+      for (int64_t i = 0; i < n; ++i) perm[i] = p0[(size_t)i] + 1;
+  }
+  cudaFree(dcols);
+  return rc;
+}
+
+// Entries of Omega grouped by row, each row's entries in ascending column (entry) order.
+struct OmegaRows {
+  std::vector<int64_t> seg, col;
+  std::vector<double> val;
+};
+int group_omega_rows(int64_t l, int64_t n, int zeta, const int32_t* rows, const double* vals, OmegaRows& o) {
+  const int64_t nnz = n * zeta;
+  o.seg.assign((size_t)l + 1, 0);
+  for (int64_t p = 0; p < nnz; ++p) {
+    if (rows[p] < 0 || rows[p] >= l) return CPALS_E_ARG;
+    ++o.seg[(size_t)rows[p] + 1];
+  }
+  for (int64_t j = 0; j < l; ++j) o.seg[(size_t)j + 1] += o.seg[(size_t)j];
+  std::vector<int64_t> fill(o.seg.begin(), o.seg.end() - 1);
+  o.col.assign((size_t)std::max<int64_t>(nnz, 1), 0);
+  o.val.assign((size_t)std::max<int64_t>(nnz, 1), 0.0);
+  for (int64_t p = 0; p < nnz; ++p) {
+    const int64_t slot = fill[(size_t)rows[p]]++;
+    o.col[(size_t)slot] = p / zeta;
+    o.val[(size_t)slot] = vals[p];
+  }
+  return CPALS_OK;
+}
+
+// The sketch of SE-QRCS into b.A (m x l): T_(mode) Omega^T (source 0) or (Omega KRP)^T (source 1).
+int fill_sketch(cpals_ctx* c, int source, int mode, int64_t l, const OmegaRows& o, double* dst) {
+  int64_t *dseg = nullptr, *dcol = nullptr, *dpos = nullptr;
+  double* dv = nullptr;
+  int rc = CPALS_OK;
+  std::vector<int64_t> pos;
+  if (source == 0) {
+    int64_t stride = 1;
+    for (int m = 0; m < mode; ++m) stride *= c->dims[m];
+    const int64_t In = c->dims[mode];
+    pos.resize(o.col.size());
+    for (size_t p = 0; p < o.col.size(); ++p) pos[p] = (o.col[p] / stride) * stride * In + (o.col[p] % stride);
+  }
+  const std::vector<int64_t>& idx = source == 0 ? pos : o.col;
+  if (dmalloc(&dseg, o.seg.size()) != CPALS_OK || dmalloc(&dcol, idx.size()) != CPALS_OK ||
+      dmalloc(&dv, o.val.size()) != CPALS_OK) {
+    rc = CPALS_E_CUDA;
+  } else {
+    cudaError_t e = cudaMemcpyAsync(dseg, o.seg.data(), sizeof(int64_t) * o.seg.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dcol, idx.data(), sizeof(int64_t) * idx.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dv, o.val.data(), sizeof(double) * o.val.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) {
+      if (source == 0) {
+        int64_t stride = 1;
+        for (int m = 0; m < mode; ++m) stride *= c->dims[m];
+        e = launch_sketch_gather(c->dT, c->tdtype, c->dims[mode], stride, dseg, dcol, dv, l, dst, c->st);
+      } else {
+        e = launch_omega_hadamard(factor_set(c), c->order, mode, c->dims, dseg, dcol, dv, l, (int)c->R, dst, 1,
+                                  c->R, c->st);
+      }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "libcpals: SE-QRCS sketch failed: %s\n", cudaGetErrorString(e));
+      rc = CPALS_E_CUDA;
+    }
+  }
+  cudaFree(dseg);
+  cudaFree(dcol);
+  cudaFree(dpos);
+  cudaFree(dv);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpals_qrcp(int device, int64_t m, int64_t n, const double* A, int64_t ncand, int64_t max_steps,
+               double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R, double* Q) {
+  if (m < 1 || n < 1 || !A || !perm || !rdiag || !steps) return CPALS_E_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return CPALS_E_CUDA;
+  int num_sms = 0;
+  if (cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CPALS_E_CUDA;
+  ncand = (ncand <= 0 || ncand > n) ? n : ncand;
+  const int64_t kmax = qrcp_kmax(m, ncand, max_steps);
+  QrcpBuffers b;
+  if (b.alloc(m, n, kmax, num_sms) != CPALS_OK) return CPALS_E_CUDA;
+  CPALS_CUDA_TRY(cudaMemcpy(b.A, A, sizeof(double) * m * n, cudaMemcpyHostToDevice));
+  std::vector<int64_t> p0((size_t)n);
+  const int rc = qrcp_run(b, m, n, ncand, kmax, stop_ratio, num_sms, 0, p0.data(), rdiag, steps, R, Q);
+  if (rc == CPALS_OK)
+    for (int64_t i = 0; i < n; ++i) perm[i] = p0[(size_t)i] + 1;
+  return rc;
+}
+
+int cpals_unfolding_qrcp(cpals_ctx* c, int mode, int64_t ncols, const int64_t* cols, int64_t ncand, int64_t max_steps,
+                         double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R, double* Q) {
+  return matrix_qrcp(c, 0, mode, ncols, cols, ncand, max_steps, stop_ratio, perm, rdiag, steps, R, Q);
+}
+
+int cpals_krp_qrcp(cpals_ctx* c, int mode, int64_t ncols, const int64_t* cols, int64_t ncand, int64_t max_steps,
+                   double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R, double* Q) {
+  return matrix_qrcp(c, 1, mode, ncols, cols, ncand, max_steps, stop_ratio, perm, rdiag, steps, R, Q);
+}
+
+int cpals_omega_hadamard(cpals_ctx* c, int mode, int64_t l, int zeta, const int32_t* rows, const double* vals,
+                         double* host_out) {
+  if (!c || mode < 0 || mode >= c->order || l < 1 || zeta < 1 || zeta > l || !rows || !vals || !host_out)
+    return CPALS_E_ARG;
+  if (!c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  OmegaRows o;
+  int rc = group_omega_rows(l, other_extent(c, mode), zeta, rows, vals, o);
+  if (rc != CPALS_OK) return rc;
+  double* dout = nullptr;
+  if (dmalloc(&dout, (size_t)(l * c->R)) != CPALS_OK) return CPALS_E_CUDA;
+  // l x R column-major: entry (j, r) at j + l r
+  int64_t *dseg = nullptr, *dcol = nullptr;
+  double* dv = nullptr;
+  if (dmalloc(&dseg, o.seg.size()) != CPALS_OK || dmalloc(&dcol, o.col.size()) != CPALS_OK ||
+      dmalloc(&dv, o.val.size()) != CPALS_OK) {
+    rc = CPALS_E_CUDA;
+  } else {
+    cudaError_t e = cudaMemcpyAsync(dseg, o.seg.data(), sizeof(int64_t) * o.seg.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dcol, o.col.data(), sizeof(int64_t) * o.col.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dv, o.val.data(), sizeof(double) * o.val.size(), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess)
+      e = launch_omega_hadamard(factor_set(c), c->order, mode, c->dims, dseg, dcol, dv, l, (int)c->R, dout, l, 1,
+                                c->st);
+    if (e == cudaSuccess) {
+      c->launches += 1;
+      e = cudaMemcpyAsync(host_out, dout, sizeof(double) * l * c->R, cudaMemcpyDeviceToHost, c->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "libcpals: omega_hadamard failed: %s\n", cudaGetErrorString(e));
+      rc = CPALS_E_CUDA;
+    }
+  }
+  cudaFree(dseg);
+  cudaFree(dcol);
+  cudaFree(dv);
+  cudaFree(dout);
+  return rc;
+}
+
+int cpals_seqrcs(cpals_ctx* c, int source, int mode, int64_t l, int zeta, const int32_t* rows, const double* vals,
+                 int64_t t, int sorted_subset, int compute_r, double stop_ratio, int64_t* perm, double* rdiag,
+                 int64_t* steps, int64_t* nsubset, double* R, double* Q) {
+  if (!c || mode < 0 || mode >= c->order || l < 1 || zeta < 1 || zeta > l || !rows || !vals || t < 1 || t > l ||
+      !perm || !rdiag || !steps || !nsubset)
+    return CPALS_E_ARG;
+  if (compute_r && (!R || !Q)) return CPALS_E_ARG;
+  int rc = source_ready(c, source);
+  if (rc != CPALS_OK) return rc;
+  DeviceGuard g(c->device);
+  const int64_t m = source == 0 ? c->dims[mode] : c->R;
+  const int64_t n = other_extent(c, mode);
+  OmegaRows o;
+  rc = group_omega_rows(l, n, zeta, rows, vals, o);
+  if (rc != CPALS_OK) return rc;
+  // stage 1: pivoted QR of the sketch (m x l); its first t pivots are rows of Omega
+  std::vector<int64_t> psk((size_t)l);
+  {
+    QrcpBuffers b;
+    const int64_t kmax = qrcp_kmax(m, l, t);
+    if (b.alloc(m, l, kmax, c->num_sms) != CPALS_OK) return CPALS_E_CUDA;
+    rc = fill_sketch(c, source, mode, l, o, b.A);
+    if (rc != CPALS_OK) return rc;
+    std::vector<double> rd1((size_t)kmax);
+    int64_t k1 = 0;
+    rc = qrcp_run(b, m, l, l, kmax, -1.0, c->num_sms, c->st, psk.data(), rd1.data(), &k1, nullptr, nullptr);
+    if (rc != CPALS_OK) return rc;
+  }
+  // the columns of Omega with an entry in a selected row: in pivot order then column order,
+  // first occurrence kept (SEQRCS.jl:155-157), or in column order (SEQRCS.jl:107-108, 204-205)
+  std::vector<int64_t> subset;
+  std::vector<char> in((size_t)n, 0);
+  if (sorted_subset) {
+    std::vector<char> sel((size_t)l, 0);
+    for (int64_t q = 0; q < t; ++q) sel[(size_t)psk[(size_t)q]] = 1;
+    for (int64_t col = 0; col < n; ++col)
+      for (int k = 0; k < zeta; ++k)
+        if (sel[(size_t)rows[col * zeta + k]]) {
+          in[(size_t)col] = 1;
+          subset.push_back(col);
+          break;
+        }
+  } else {
+    for (int64_t q = 0; q < t; ++q) {
+      const int64_t row = psk[(size_t)q];
+      for (int64_t p = o.seg[(size_t)row]; p < o.seg[(size_t)row + 1]; ++p) {
+        const int64_t col = o.col[(size_t)p];
+        if (!in[(size_t)col]) {
+          in[(size_t)col] = 1;
+          subset.push_back(col);
+        }
+      }
+    }
+  }
+  const int64_t nsub = (int64_t)subset.size();
+  *nsubset = nsub;
+  std::vector<int64_t> order = subset;  // matrix columns: the subset, then (with R) the rest ascending
+  if (compute_r)
+    for (int64_t col = 0; col < n; ++col)
+      if (!in[(size_t)col]) order.push_back(col);
+  const int64_t ncols = (int64_t)order.size();
+  if (nsub == 0) {  // no column reaches the selected rows: p is every column ascending
+    *steps = 0;
+    for (int64_t col = 0; col < n; ++col) perm[col] = col + 1;
+    return CPALS_OK;
+  }
+  // stage 2: pivoted QR of those columns, pivots among the subset
+  int64_t* dcols = nullptr;
+  if (dmalloc(&dcols, (size_t)ncols) != CPALS_OK) return CPALS_E_CUDA;
+  std::vector<int64_t> p0((size_t)ncols);
+  {
+    QrcpBuffers b;
+    const int64_t kmax = qrcp_kmax(m, nsub, 0);
+    rc = b.alloc(m, ncols, kmax, c->num_sms);
+    if (rc == CPALS_OK) {
+      cudaError_t e = cudaMemcpyAsync(dcols, order.data(), sizeof(int64_t) * ncols, cudaMemcpyHostToDevice, c->st);
+      if (e == cudaSuccess) e = fill_columns(c, source, mode, dcols, ncols, b.A);
+      rc = (e == cudaSuccess) ? qrcp_run(b, m, ncols, nsub, kmax, compute_r ? -1.0 : stop_ratio, c->num_sms, c->st,
+                                         p0.data(), rdiag, steps, compute_r ? R : nullptr, compute_r ? Q : nullptr)
+                              : CPALS_E_CUDA;
+    }
+  }
+  cudaFree(dcols);
+  if (rc != CPALS_OK) return rc;
+  // p = vcat(subset[p_subset], the other columns ascending)
+  int64_t w = 0;
+  for (int64_t q = 0; q < nsub; ++q) perm[w++] = order[(size_t)p0[(size_t)q]] + 1;
+  for (int64_t col = 0; col < n; ++col)
+    if (!in[(size_t)col]) perm[w++] = col + 1;
+  return CPALS_OK;
+}
+
 int cpals_fallback_count(cpals_ctx* c, int64_t* count) {
   if (!c || !count) return CPALS_E_ARG;
   DeviceGuard g(c->device);

@@ -211,6 +211,50 @@ cudaError_t launch_sparse_sign(int64_t l, int64_t n, int zeta, int injective, ui
 cudaError_t launch_sketch_gather(const void* T, int tdtype, int64_t In, int64_t stride, const int64_t* seg,
                                  const int64_t* pos, const double* v, int64_t l, double* out, cudaStream_t st);
 
+// Column-pivoted QR (k_qrcp.cu).  A (m x n, column-major FP64) is factored in place; pivots
+// are chosen among columns [0, ncand); at most kmax steps, fewer when a step's |r_jj| is at
+// most stop_ratio |r_00| (stop_ratio < 0: never).  part holds qrcp_parts(n) entries.
+struct QrcpArg {
+  double v;
+  int64_t i;
+};
+struct QrcpState {
+  double r00, tau;
+  int64_t steps;   // steps run
+  int64_t active;  // j + 1 for the step whose reflector is current
+  int done, pad;
+};
+struct KrpDims {
+  int64_t dims[kMaxOrder];
+};
+struct QrcpJob {
+  double* A;
+  int64_t m, n, ncand, kmax;
+  double stop_ratio;
+  double *vn1, *vn2, *vbuf, *taus, *rdiag;
+  int64_t* perm;  // 0-based original column of each position
+  QrcpArg* part;
+  QrcpState* st;
+  int num_sms;
+};
+int qrcp_parts(int64_t n, int num_sms);
+cudaError_t launch_qrcp_init(const QrcpJob& q, cudaStream_t st);
+cudaError_t launch_qrcp_step(const QrcpJob& q, int64_t j, cudaStream_t st);
+// Q (m x k) = H_0 ... H_{k-1} [I; 0] from the factored A and its taus.
+cudaError_t launch_qr_form_q(const double* A, int64_t m, int64_t k, const double* taus, double* Q, int num_sms,
+                             cudaStream_t st);
+// out (In x ncols) = the columns cols (0-based, identity when null) of the mode unfolding whose
+// fibres start at (col / stride) stride In + col % stride with element stride `stride`.
+cudaError_t launch_unfold_cols(const void* T, int tdtype, int64_t In, int64_t stride, const int64_t* cols,
+                               int64_t ncols, double* out, cudaStream_t st);
+// out (R x ncols) = rows cols of the Khatri-Rao product of the factors other than `mode`, transposed.
+cudaError_t launch_krp_cols(const FactorSet& fs, int order, int mode, const int64_t* dims, const int64_t* cols,
+                            int64_t ncols, int R, double* out, cudaStream_t st);
+// out[r sr + j sj] = sum over Omega's row j (entries seg[j] .. seg[j+1]) of v[p] KRP(cols[p], r).
+cudaError_t launch_omega_hadamard(const FactorSet& fs, int order, int mode, const int64_t* dims, const int64_t* seg,
+                                  const int64_t* cols, const double* v, int64_t l, int R, double* out, int64_t sr,
+                                  int64_t sj, cudaStream_t st);
+
 // Raises a kernel's dynamic shared-memory limit on the current device, once per (device,
 // kernel) per process (thread-safe).  The attribute is per device, so a process that drives
 // several GPUs sets it on each.

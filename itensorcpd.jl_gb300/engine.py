@@ -8,6 +8,32 @@ import numpy as np
 from . import _lib as L
 
 
+class QRCPResult:
+    """A column-pivoted QR: ``p`` (1-based column order, Julia's ``F.p``), ``rdiag`` (diag of R
+    for the ``steps`` run), and when asked ``R`` (steps x n) and ``Q`` (m x steps).  Unpacks as
+    ``Q, R, p`` like the reference's ``SEQRCS``."""
+
+    def __init__(self):
+        self.p = self.rdiag = self.R = self.Q = None
+        self.steps = 0
+        self.nsubset = None
+
+    @classmethod
+    def make(cls, perm, rdiag, steps, m, n, R, Q):
+        r = cls()
+        r.p = perm
+        r.steps = steps
+        r.rdiag = rdiag[:steps].copy()
+        if R is not None:
+            r.R = R[: steps * n].reshape((steps, n), order="F").copy()
+        if Q is not None:
+            r.Q = Q[: m * steps].reshape((m, steps), order="F").copy()
+        return r
+
+    def __iter__(self):
+        return iter((self.Q, self.R, self.p))
+
+
 class Engine:
     """Device state of one CP-ALS problem: the tensor, factors, Grams and the check.
 
@@ -131,6 +157,66 @@ class Engine:
                                                       rows.ctypes.data_as(C.POINTER(C.c_int32)), L.dptr(vals),
                                                       L.dptr(out)), "cpals_sketched_matricization")
         return out
+
+    # ---- column-pivoted QR, SE-QRCS ----
+    def _qrcp_call(self, fn, name, mode, m, n, cols, ncand, max_steps, stop_ratio, want_r, want_q):
+        c = None if cols is None else np.ascontiguousarray(cols, dtype=np.int64)
+        ncols = n if c is None else c.size
+        perm = np.empty(ncols, dtype=np.int64)
+        kcap = max(1, min(m, ncols))
+        rdiag = np.empty(kcap, dtype=np.float64)
+        steps = np.zeros(1, dtype=np.int64)
+        R = np.empty(kcap * ncols, dtype=np.float64) if want_r else None
+        Q = np.empty(m * kcap, dtype=np.float64) if want_q else None
+        L.check(fn(self.h, int(mode), int(ncols), None if c is None else L.i64ptr(c), int(ncand), int(max_steps),
+                   float(stop_ratio), L.i64ptr(perm), L.dptr(rdiag), L.i64ptr(steps),
+                   None if R is None else L.dptr(R), None if Q is None else L.dptr(Q)), name)
+        return QRCPResult.make(perm, rdiag, int(steps[0]), m, ncols, R, Q)
+
+    def unfolding_qrcp(self, mode, cols=None, ncand=0, max_steps=0, stop_ratio=-1.0, want_r=False, want_q=False):
+        """Column-pivoted QR of T_(mode) (or its columns ``cols``, 1-based)."""
+        n = int(np.prod([d for m, d in enumerate(self.dims) if m != mode]))
+        return self._qrcp_call(self.lib.cpals_unfolding_qrcp, "cpals_unfolding_qrcp", mode, self.dims[mode], n, cols,
+                               ncand, max_steps, stop_ratio, want_r, want_q)
+
+    def krp_qrcp(self, mode, cols=None, ncand=0, max_steps=0, stop_ratio=-1.0, want_r=False, want_q=False):
+        """Column-pivoted QR of the transposed Khatri-Rao product of the factors other than ``mode``."""
+        n = int(np.prod([d for m, d in enumerate(self.dims) if m != mode]))
+        return self._qrcp_call(self.lib.cpals_krp_qrcp, "cpals_krp_qrcp", mode, self.rank, n, cols, ncand,
+                               max_steps, stop_ratio, want_r, want_q)
+
+    def omega_hadamard(self, mode, l, rows, vals, zeta):
+        """Omega (KRP of the factors other than ``mode``), l x R, for 0-based ``rows`` / ``vals``."""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        out = np.empty((int(l), self.rank), dtype=np.float64, order="F")
+        L.check(self.lib.cpals_omega_hadamard(self.h, int(mode), int(l), int(zeta),
+                                              rows.ctypes.data_as(C.POINTER(C.c_int32)), L.dptr(vals), L.dptr(out)),
+                "cpals_omega_hadamard")
+        return out
+
+    def seqrcs(self, source, mode, l, rows, vals, zeta, t, sorted_subset=False, compute_r=False, stop_ratio=-1.0):
+        """SE-QRCS of T_(mode) (source 0) or of the transposed KRP of the other factors (source 1)."""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        m = self.dims[mode] if source == 0 else self.rank
+        n = int(np.prod([d for k, d in enumerate(self.dims) if k != mode]))
+        perm = np.empty(n, dtype=np.int64)
+        kcap = max(1, min(m, n))
+        rdiag = np.empty(kcap, dtype=np.float64)
+        steps = np.zeros(1, dtype=np.int64)
+        nsub = np.zeros(1, dtype=np.int64)
+        R = np.empty(kcap * n, dtype=np.float64) if compute_r else None
+        Q = np.empty(m * kcap, dtype=np.float64) if compute_r else None
+        L.check(self.lib.cpals_seqrcs(self.h, int(source), int(mode), int(l), int(zeta),
+                                      rows.ctypes.data_as(C.POINTER(C.c_int32)), L.dptr(vals), int(t),
+                                      int(bool(sorted_subset)), int(bool(compute_r)), float(stop_ratio),
+                                      L.i64ptr(perm), L.dptr(rdiag), L.i64ptr(steps), L.i64ptr(nsub),
+                                      None if R is None else L.dptr(R), None if Q is None else L.dptr(Q)),
+                "cpals_seqrcs")
+        res = QRCPResult.make(perm, rdiag, int(steps[0]), m, n, R, Q)
+        res.nsubset = int(nsub[0])
+        return res
 
     def gram(self, mode):
         G = np.empty((self.rank, self.rank), dtype=np.float64)

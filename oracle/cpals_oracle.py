@@ -659,6 +659,205 @@ def load_ref_sparse_sign():
 
 
 # ---------------------------------------------------------------------------
+# Column-pivoted QR, SE-QRCS, omega_hadamard, the pivot-based solvers
+# ---------------------------------------------------------------------------
+def qrcp_lapack(A):
+    """qr(A, ColumnNorm()) as the reference calls it (LinearAlgebra's pivoted QR is LAPACK
+    xGEQP3; scipy binds the same routine): Q (m x k), R (k x n), p (1-based), k = min(m, n)."""
+    import scipy.linalg
+
+    Q, R, p = scipy.linalg.qr(np.asarray(A, dtype=np.float64), mode="economic", pivoting=True)
+    return Q, R, p.astype(np.int64) + 1
+
+
+def qrcp_loop(A, kmax=None, ncand=None, stop_ratio=-1.0):
+    """Businger-Golub QR with column pivoting, one step at a time, with xGEQP3's pivot rule
+    (largest partial norm, the first position on ties) and xLAQP2's norm downdating with its
+    sqrt(eps) recompute safeguard; reflectors in xLARFG's convention.  Pivots are chosen
+    among the first ``ncand`` columns; ``kmax`` steps at most; the run ends after the first
+    step with |r_jj| <= stop_ratio |r_00| (stop_ratio >= 0).  Returns (p 1-based, rdiag,
+    R (k x n), Q (m x k)).  Small cases only."""
+    A = np.array(A, dtype=np.float64)
+    m, n = A.shape
+    ncand = n if ncand is None or ncand <= 0 else min(int(ncand), n)
+    kmax = min(m, ncand) if kmax is None or kmax <= 0 else min(int(kmax), m, ncand)
+    perm = np.arange(n)
+    vn1 = np.sqrt(np.sum(A * A, axis=0))
+    vn2 = vn1.copy()
+    tol3z = math.sqrt(np.finfo(np.float64).eps)
+    rdiag, taus = [], []
+    for j in range(kmax):
+        p = j + int(np.argmax(vn1[j:ncand]))
+        if p != j:
+            A[:, [j, p]] = A[:, [p, j]]
+            perm[[j, p]] = perm[[p, j]]
+            vn1[p], vn2[p] = vn1[j], vn2[j]
+        alpha = A[j, j]
+        x = A[j + 1:, j]
+        s2 = float(x @ x)
+        if s2 > 0.0:
+            beta = -math.copysign(math.sqrt(alpha * alpha + s2), alpha)
+            tau = (beta - alpha) / beta
+            A[j + 1:, j] = x * (1.0 / (alpha - beta))
+        else:
+            beta, tau = alpha, 0.0
+        A[j, j] = beta
+        rdiag.append(beta)
+        taus.append(tau)
+        if j + 1 < n:
+            v = np.concatenate([[1.0], A[j + 1:, j]])
+            w = v @ A[j:, j + 1:]
+            A[j:, j + 1:] -= tau * np.outer(v, w)
+            c = np.arange(j + 1, ncand)
+            c = c[vn1[c] != 0.0]
+            if c.size:
+                temp = np.maximum(1.0 - (np.abs(A[j, c]) / vn1[c]) ** 2, 0.0)
+                temp2 = temp * (vn1[c] / vn2[c]) ** 2
+                rec = temp2 <= tol3z
+                cr = c[rec]
+                if j + 1 < m:
+                    vn1[cr] = np.sqrt(np.sum(A[j + 1:, cr] ** 2, axis=0))
+                else:
+                    vn1[cr] = 0.0
+                vn2[cr] = vn1[cr]
+                ck = c[~rec]
+                vn1[ck] = vn1[ck] * np.sqrt(temp[~rec])
+        if stop_ratio >= 0.0 and not (abs(beta) > stop_ratio * abs(rdiag[0])):
+            break
+    k = len(rdiag)
+    R = np.triu(A[:k, :])
+    Q = np.eye(m, k)
+    for j in range(k - 1, -1, -1):
+        v = np.concatenate([[1.0], A[j + 1:, j]])
+        Q[j:, j:] -= taus[j] * np.outer(v, v @ Q[j:, j:])
+    return perm + 1, np.array(rdiag), R, Q
+
+
+def _embedding_row_lists(l, n, s, rows1):
+    """Columns of Omega (0-based, ascending) with an entry in each row."""
+    lists = [[] for _ in range(l)]
+    r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
+    for c in range(n):
+        for j in r[c]:
+            lists[int(j)].append(c)
+    return lists
+
+
+def seqrcs(T, k, l, s, t, rows1, vals, use_omega=False, compute_r=True):
+    """SE-QRCS of the mode-k unfolding (src/algebra/SEQRCS.jl:89-182; k 0-based): the first t
+    pivots of the pivoted QR of the sketch T_(k) Omega^T; the columns of Omega with an entry
+    in those rows (use_omega: in column order, SEQRCS.jl:107-108; else for each pivot row in
+    order, its columns ascending, first occurrence kept, SEQRCS.jl:155-157); the pivoted QR
+    of those columns of T_(k); p = vcat(subset[p_subset], the other columns).  With
+    compute_r, R = hcat(R_subset, Q^T A_rem).  Returns (Q, R, p 1-based, diag(R_subset))."""
+    A = unfold(np.asarray(T, dtype=np.float64), k)
+    n = A.shape[1]
+    Ask = sketched_matricization(np.asarray(T, dtype=np.float64), k, l, rows1, vals, s)
+    _, _, psk = qrcp_lapack(Ask)
+    psk = psk[:t] - 1
+    lists = _embedding_row_lists(l, n, s, rows1)
+    if use_omega:
+        sel = set(int(p) for p in psk)
+        r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
+        subset = [c for c in range(n) if any(int(j) in sel for j in r[c])]
+    else:
+        subset, seen = [], set()
+        for p in psk:
+            for c in lists[int(p)]:
+                if c not in seen:
+                    seen.add(c)
+                    subset.append(c)
+    subset = np.asarray(subset, dtype=np.int64)
+    rem = np.setdiff1d(np.arange(n), subset)
+    if subset.size == 0:
+        return None, None, rem + 1, np.zeros(0)
+    Q, R, ps = qrcp_lapack(A[:, subset])
+    p = np.concatenate([subset[ps - 1], rem]) + 1
+    rd = np.diag(R).copy()
+    if compute_r:
+        R = np.hstack([R, Q.T @ A[:, rem]])
+    return Q, R, p, rd
+
+
+def omega_hadamard(mats, l, s, rows1, vals) -> np.ndarray:
+    """src/algebra/had_contract.jl:300-326: row j of the l x R result is the sum over Omega's
+    row j (columns ascending) of the signed Khatri-Rao rows, each the product of the factor
+    rows in order."""
+    dims = [F.shape[0] for F in mats]
+    n = int(np.prod(dims))
+    R = mats[0].shape[1]
+    lists = _embedding_row_lists(l, n, s, rows1)
+    val = {}
+    r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
+    v = np.asarray(vals[: n * s]).reshape(n, s)
+    for c in range(n):
+        for q in range(s):
+            val[(int(r[c, q]), c)] = v[c, q]
+    out = np.zeros((l, R))
+    for j in range(l):
+        cols = np.asarray(lists[j], dtype=np.int64)
+        if cols.size == 0:
+            continue
+        piv = column_to_multi_coords(cols + 1, dims)
+        kr = pivot_hadamard(mats, piv)
+        signs = np.array([val[(j, int(c))] for c in cols])
+        out[j] = np.sum(kr * signs[:, None], axis=0)
+    return out
+
+
+def seqrcs_krp(mats, l, s, t, rows1, vals, compute_r=True):
+    """SE-QRCS of the transposed Khatri-Rao product of ``mats`` (src/algebra/SEQRCS.jl:184-240):
+    the sketch omega_hadamard(mats, Omega), the first t pivots of the pivoted QR of its
+    transpose, the columns of Omega with an entry in those rows (column order), the pivoted QR
+    of those KRP rows transposed, p = vcat(subset[p_subset], the rest).  Returns (Q, R, p
+    1-based, diag(R_subset))."""
+    dims = [F.shape[0] for F in mats]
+    n = int(np.prod(dims))
+    Ask = omega_hadamard(mats, l, s, rows1, vals)
+    _, _, psk = qrcp_lapack(Ask.T.copy())
+    sel = set(int(p) - 1 for p in psk[:t])
+    r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
+    subset = np.asarray([c for c in range(n) if any(int(j) in sel for j in r[c])], dtype=np.int64)
+    rem = np.setdiff1d(np.arange(n), subset)
+    if subset.size == 0:
+        return None, None, rem + 1, np.zeros(0)
+    K = khatri_rao(mats)  # n x R, rows in column_to_multi_coords order
+    Q, R, ps = qrcp_lapack(K[subset].T.copy())
+    p = np.concatenate([subset[ps - 1], rem]) + 1
+    rd = np.diag(R).copy()
+    if compute_r:
+        R = np.hstack([R, Q.T @ K[rem].T])
+    return Q, R, p, rd
+
+
+def effective_rank(rdiag, trunc_tol) -> int:
+    """meff = sum(abs.(dr) ./ maximum(abs.(dr)) .> trunc_tol) (qr_lev_score_sampled.jl:26)."""
+    d = np.abs(np.asarray(rdiag, dtype=np.float64))
+    if d.size == 0:
+        return 0
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return int(np.sum(d / d.max() > trunc_tol))
+
+
+def projected_als(T, factors, lam, projectors, sweeps, normal=True, record=None):
+    """The pivot-based solvers' sweeps (optimize.jl:15-32 with qr_lev_score_sampled.jl:146-162
+    and ProjectionAlgorithm.jl:57-68): every mode solves its projected least-squares problem
+    at fixed pivots (``projectors[n]``, 1-based multi-coordinates) and row-normalizes."""
+    factors = [np.array(F, dtype=np.float64) for F in factors]
+    N = T.ndim
+    for _ in range(sweeps):
+        for n in range(N):
+            others = [factors[m] for m in range(N) if m != n]
+            S = pivot_hadamard(others, projectors[n])
+            Ts = fused_flatten_sample(T, n, projectors[n])
+            X = sampled_solve(S, Ts, normal)
+            factors[n], lam = row_norm(X)
+            if record is not None:
+                record.append({"mode": n, "factor": factors[n].copy(), "lam": lam.copy()})
+    return factors, lam
+
+
+# ---------------------------------------------------------------------------
 # Synthetic low-rank-plus-noise generator (the benchmark workloads' tensors)
 # ---------------------------------------------------------------------------
 def congruent_factor(dim, rank, congruence, rng) -> np.ndarray:

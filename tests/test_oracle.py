@@ -352,3 +352,90 @@ def test_oracle_sketched_matricization_is_the_dense_product(oracle):
             want = oracle.unfold(T, k) @ om.T
             got = oracle.sketched_matricization(T, k, l, rows + 1, vals, s)
             assert np.linalg.norm(got - want) <= 1e-12 * max(1.0, np.linalg.norm(want))
+
+
+# ---- column-pivoted QR, omega_hadamard, SE-QRCS (oracle restatements) ----
+def _np_sparse_sign(l, n, s, rng):
+    """A sparse_sign-layout embedding drawn with numpy (s distinct rows per column), 1-based."""
+    rows = np.concatenate([rng.choice(l, size=s, replace=False) for _ in range(n)]).astype(np.int32) + 1
+    vals = np.where(rng.random(n * s) < 0.5, -1.0, 1.0) / np.sqrt(s)
+    return rows, vals
+
+
+@pytest.mark.parametrize("shape", [(30, 50), (50, 30), (7, 7), (1, 9), (9, 1), (40, 200)])
+def test_qrcp_loop_is_lapack_geqp3(oracle, shape):
+    """The step-by-step restatement (the device's rule: largest partial norm, xLAQP2 downdating)
+    picks the pivots LAPACK's xGEQP3 picks, and the same R and Q."""
+    A = np.random.default_rng(sum(shape)).standard_normal(shape)
+    p, rd, R, Q = oracle.qrcp_loop(A)
+    Q2, R2, p2 = oracle.qrcp_lapack(A)
+    np.testing.assert_array_equal(p, p2)
+    np.testing.assert_allclose(R, R2, rtol=0, atol=1e-13 * np.abs(A).max())
+    np.testing.assert_allclose(Q, Q2, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(rd, np.diag(R2), rtol=1e-13)
+
+
+def test_qrcp_loop_low_rank_and_early_stop(oracle):
+    """Rank 5 plus 1e-9 noise: the same pivots as xGEQP3 throughout; a stopping ratio ends the
+    run one step after the last |r_jj| above it (qr_lev_score_sampled.jl:26 counts meff)."""
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((40, 5)) @ rng.standard_normal((5, 300)) + 1e-9 * rng.standard_normal((40, 300))
+    p, rd, _, _ = oracle.qrcp_loop(A)
+    _, R2, p2 = oracle.qrcp_lapack(A)
+    np.testing.assert_array_equal(p, p2)
+    assert oracle.effective_rank(rd, 0.01) == oracle.effective_rank(np.diag(R2), 0.01) == 5
+    p3, rd3, _, _ = oracle.qrcp_loop(A, stop_ratio=0.01)
+    assert rd3.size == 6 and oracle.effective_rank(rd3, 0.01) == 5
+    np.testing.assert_array_equal(p3[:6], p2[:6])
+    p4, _, _, _ = oracle.qrcp_loop(A, ncand=100)
+    assert set(p4[:40]) <= set(range(1, 101))
+
+
+def test_oracle_omega_hadamard_is_the_dense_product(oracle):
+    """test/pivot_mapping.jl:120-160: omega_hadamard(factors, Omega) = Omega * KRP."""
+    rng = np.random.default_rng(5)
+    mats = [rng.standard_normal((d, 10)) for d in (3, 6, 8)]
+    n = 3 * 6 * 8
+    l, s = 31, 3
+    rows, vals = _np_sparse_sign(l, n, s, rng)
+    got = oracle.omega_hadamard(mats, l, s, rows, vals)
+    ref = oracle.sparse_embedding(l, n, s, rows, vals) @ oracle.khatri_rao(mats)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def _qr_error(A, Q, R, p, k):
+    return np.linalg.norm(A[:, p - 1] - Q[:, :k] @ R[:k, :], 2) / np.linalg.norm(A, 2)
+
+
+def test_oracle_seqrcs_reference_property(oracle):
+    """test/SEQRCS_test.jl:31-50: for a 50 x 10000 Gaussian matrix, the rank-40 error of SE-QRCS
+    (l = 2500, s = 1, t = 40; both subset orders) is within 1e-2 of the pivoted QR's."""
+    rng = np.random.default_rng(6)
+    A = rng.standard_normal((50, 10000))
+    k = 40
+    Qa, Ra, pa = oracle.qrcp_lapack(A)
+    err_act = _qr_error(A, Qa, Ra, pa, k)
+    T = np.asfortranarray(A)
+    for use_omega in (False, True):
+        rows, vals = _np_sparse_sign(2500, 10000, 1, rng)
+        Q, R, p, rd = oracle.seqrcs(T, 0, 2500, 1, 40, rows, vals, use_omega=use_omega)
+        assert sorted(p) == list(range(1, 10001))
+        assert abs(_qr_error(A, Q, R, p, k) - err_act) <= 1e-2
+        np.testing.assert_allclose(np.abs(rd), np.abs(np.diag(R)[: rd.size]), rtol=1e-14)
+
+
+def test_oracle_seqrcs_of_the_krp(oracle):
+    """test/SEQRCS_test.jl:52-68 compares SE-QRCS of a KRP given by its factors with SE-QRCS of
+    the explicit KRP matrix (rank-40 errors within 1e-2, each with its own embedding).  With
+    the same embedding the two are the same computation (the KRP path selects its subset in
+    column order, as the matrix path does with the explicit Omega), so the pivots agree and the
+    errors agree to rounding."""
+    rng = np.random.default_rng(7)
+    mats = [rng.standard_normal((100, 50)), rng.standard_normal((100, 50))]
+    K = oracle.khatri_rao(mats)  # 10000 x 50
+    Kt = np.asfortranarray(K.T)
+    rows, vals = _np_sparse_sign(2500, 10000, 1, rng)
+    Q, R, p, _ = oracle.seqrcs(Kt, 0, 2500, 1, 40, rows, vals, use_omega=True)
+    Qf, Rf, pf, _ = oracle.seqrcs_krp(mats, 2500, 1, 40, rows, vals)
+    np.testing.assert_array_equal(pf, p)
+    assert abs(_qr_error(Kt, Qf, Rf, pf, 40) - _qr_error(Kt, Q, R, p, 40)) <= 1e-10

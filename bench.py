@@ -52,9 +52,10 @@ def parse():
     ap.add_argument("--c4-count", type=int, default=4096, help="c4: tensors in the batch")
     ap.add_argument("--c5-train", type=int, default=20000, help="c5: training decompositions")
     ap.add_argument("--c5-eval", type=int, default=512, help="c5: held-out tensors")
-    ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5", "qrcp"], default="c2",
                     help="c2: 512^3 rank 64 (the headline line); c3: 128^4 rank 128, dimension tree, "
-                         "plain and randomized paths; c4: 4096 small decompositions, batched")
+                         "plain and randomized paths; c4: 4096 small decompositions, batched; qrcp: the "
+                         "QR-pivoted solvers' pivot factorizations of the 512^3 tensor's unfoldings")
     ap.add_argument("--profile-mttkrp", action="store_true",
                     help="only set up the workload and run one MTTKRP per mode (a small case for ncu)")
     return ap.parse_args()
@@ -299,6 +300,57 @@ def run_c3(args, pkg, L, device):
     del keep
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (non-tensor), nominal: no measured FP64 peak is on file
+
+
+def run_qrcp(args, pkg, device):
+    """The pivot factorizations of QRPivProjected / SEQRCSPivProjected on the headline tensor
+    (512^3 FP32, rank 64 + 20 dB noise): the column-pivoted QR of each 512 x 262144 mode
+    unfolding (every step; device FP64), and SE-QRCS of mode 0 (l = round(3 m ln m) = 9582,
+    s = round(ln m) = 6, t = 512).  Host wall clock around each synchronous C-ABI call, so the
+    figures include the gather of the unfolding and the copies of the pivots.  CPU leg:
+    LAPACK's xGEQP3 (scipy, all host threads) on a 512 x 16384 column sample, scaled by the
+    column count (the factorization's cost is linear in n at fixed m)."""
+    import scipy.linalg
+
+    T = make_tensor(pkg)
+    m, n = 512, 512 * 512
+    flops = 2.0 * m * m * n - 2.0 * m ** 3 / 3.0  # Householder QR of an m x n matrix, m < n
+    out = {"modes": []}
+    with pkg.Engine(DIMS, 1, dtype=np.float32, precision="fp64", device=device) as e:
+        e.set_tensor(T)
+        e.unfolding_qrcp(0, max_steps=8)  # warm-up: allocation paths, module load
+        for k in range(3):
+            t0 = time.perf_counter()
+            res = e.unfolding_qrcp(k)
+            dt = time.perf_counter() - t0
+            out["modes"].append({"mode": k, "ms": dt * 1e3, "steps": res.steps,
+                                 "gflops": flops / dt / 1e9, "meff_at_0.01": int(np.sum(
+                                     np.abs(res.rdiag) / np.abs(res.rdiag).max() > 0.01))})
+        rows, vals = pkg.sparse_sign_matrix(9582, n, 6, seed=SEED)
+        t0 = time.perf_counter()
+        sq = e.seqrcs(0, 0, 9582, rows[: n * 6] - 1, vals[: n * 6], 6, 512)
+        out["seqrcs_mode0"] = {"ms": (time.perf_counter() - t0) * 1e3, "subset_columns": sq.nsubset,
+                               "l": 9582, "s": 6, "t": 512}
+    best = min(x["ms"] for x in out["modes"])
+    A = np.asfortranarray(T.reshape(m, n, order="F")[:, :16384].astype(np.float64))
+    t0 = time.perf_counter()
+    scipy.linalg.qr(A, mode="r", pivoting=True)
+    cpu_s = (time.perf_counter() - t0) * (n / 16384)
+    line = {
+        "metric": "qrcp_unfolding_ms", "value": best, "unit": "ms", "n_gpus": 1, "steps": 3, "warmup": 1,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "qrcp_512x262144_unfoldings_of_512cube_fp32_rank64_noise_20dB", "m": m, "n": n},
+        "qrcp": out,
+        "fp64": {"achieved_tflops": flops / (best / 1e3) / 1e12, "peak_tflops": FP64_NOMINAL_TFLOPS,
+                 "frac": flops / (best / 1e3) / 1e12 / FP64_NOMINAL_TFLOPS, "peak_kind": "nominal"},
+        "cpu_baseline": {"value": cpu_s * 1e3, "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "scipy (LAPACK xGEQP3) on columns 1..16384 of the mode-0 unfolding, scaled "
+                                   "by 262144 / 16384"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 C4_COUNT = 4096
 
 
@@ -470,6 +522,10 @@ def main():
     if args.workload == "c4":
         if rank == 0:
             run_c4(args, pkg, local if world > 1 else 0)
+        return
+    if args.workload == "qrcp":
+        if rank == 0:
+            run_qrcp(args, pkg, local if world > 1 else 0)
         return
     if args.workload == "c5":
         if rank == 0:

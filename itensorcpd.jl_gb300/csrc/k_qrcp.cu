@@ -181,9 +181,51 @@ __global__ void __launch_bounds__(1024) k_qrcp_reflect(double* __restrict__ A, i
   }
 }
 
-// Step j, the grid: apply H_j to columns j+1 .. n-1, downdate the candidates' norms, and write
+// xLAQP2's downdate of the partial norm of this lane's pending column pc (x0 = its new row-j
+// entry, r_jc), and the column's entry into the lane's argmax.  The warp keeps one pending
+// column per lane and runs the 32 downdates together, one per lane, instead of 32 copies of
+// each.  xLAQP2 tests (1 - (x0/a)^2)(a/b)^2 <= sqrt(eps) and scales a by sqrt(1 - (x0/a)^2);
+// here the same quantities without divisions: max(a^2 - x0^2, 0) <= sqrt(eps) b^2, and
+// a = sqrt(max(a^2 - x0^2, 0)).  When the test fires the lane recomputes the norm from the
+// trailing entries of its column.
+__device__ __forceinline__ void downdate_lane(double px0, int64_t& pc, const double* __restrict__ A, int64_t m,
+                                              int64_t j, int64_t len, double* __restrict__ vn1,
+                                              double* __restrict__ vn2, int64_t ncand, double& bv, int64_t& bi) {
+  __syncwarp();  // the warp's stores to its columns are visible to every lane
+  if (pc >= 0 && pc < ncand) {
+    double a = vn1[pc], b = vn2[pc];
+    if (a != 0.0) {
+      double s = fma(-px0, px0, a * a);
+      s = s > 0.0 ? s : 0.0;
+      if (s <= kTol3z * (b * b)) {
+        const double* __restrict__ x = A + pc * m + j;
+        double t0 = 0.0, t1 = 0.0;
+        int64_t i = 1;
+        for (; i + 1 < len; i += 2) {
+          t0 = fma(x[i], x[i], t0);
+          t1 = fma(x[i + 1], x[i + 1], t1);
+        }
+        if (i < len) t0 = fma(x[i], x[i], t0);
+        a = sqrt(t0 + t1);
+        b = a;
+      } else {
+        a = sqrt(s);
+      }
+      vn1[pc] = a;
+      vn2[pc] = b;
+    }
+    if (better(a, pc, bv, bi)) {
+      bv = a;
+      bi = pc;
+    }
+  }
+  pc = -1;
+}
+
+// Step j, the grid: apply H_j to columns j+1 .. n-1// Step j, the grid: apply H_j to columns j+1 .. n-1, downdate the candidates' norms, and write
 // this block's argmax partial.  CH > 0: the warp holds rows j .. m-1 of its column in CH
-// registers per lane (m - j <= 32 CH); CH == 0: two passes over global memory.
+// registers per lane (m - j <= 32 CH); CH == 0: two passes over global memory.  Two FMAs per
+// entry (w = v^T x, then the update); the norm downdates run one per lane (downdate_lane).
 template <int CH>
 __global__ void __launch_bounds__(QW * 32) k_qrcp_apply(double* __restrict__ A, int64_t m, int64_t n, int64_t ncand,
                                                         int64_t j, double* __restrict__ vn1, double* __restrict__ vn2,
@@ -196,66 +238,57 @@ __global__ void __launch_bounds__(QW * 32) k_qrcp_apply(double* __restrict__ A, 
   const double* __restrict__ v = vbuf + j;
   double bv = -1.0;
   int64_t bi = INT64_MAX;
+  double px0 = 0.0;  // this lane's pending column and its new row-j entry
+  int64_t pc = -1;
+  int slot = 0;
   for (int64_t c = j + 1 + (int64_t)blockIdx.x * QW + w; c < n; c += (int64_t)gridDim.x * QW) {
     double* __restrict__ x = A + c * m + j;
-    double x0 = 0.0, tail = 0.0;  // the new x_0, and sum of the new x_i^2 for i >= 1
+    double x0;
     if constexpr (CH > 0) {
       double xr[CH];
-      double d = 0.0;
+      double d0 = 0.0, d1 = 0.0;  // two chains halve the dependent FMA latency
 #pragma unroll
       for (int q = 0; q < CH; ++q) {
         const int64_t i = lane + 32 * q;
         xr[q] = (i < len) ? x[i] : 0.0;
-        if (i < len) d = fma(v[i], xr[q], d);
+        if (i < len) {
+          if (q & 1)
+            d1 = fma(v[i], xr[q], d1);
+          else
+            d0 = fma(v[i], xr[q], d0);
+        }
       }
-      const double t = tau * warp_sum(d);
+      const double t = tau * warp_sum(d0 + d1);
 #pragma unroll
       for (int q = 0; q < CH; ++q) {
         const int64_t i = lane + 32 * q;
         if (i < len) {
           xr[q] = fma(-t, v[i], xr[q]);
           x[i] = xr[q];
-          if (i >= 1) tail = fma(xr[q], xr[q], tail);
         }
       }
       x0 = __shfl_sync(FULL, xr[0], 0);
     } else {
-      double d = 0.0;
-      for (int64_t i = lane; i < len; i += 32) d = fma(v[i], x[i], d);
-      const double t = tau * warp_sum(d);
-      for (int64_t i = lane; i < len; i += 32) {
-        const double y = fma(-t, v[i], x[i]);
-        x[i] = y;
-        if (i >= 1) tail = fma(y, y, tail);
+      double d0 = 0.0, d1 = 0.0;
+      for (int64_t i = lane; i < len; i += 64) {
+        d0 = fma(v[i], x[i], d0);
+        if (i + 32 < len) d1 = fma(v[i + 32], x[i + 32], d1);
       }
+      const double t = tau * warp_sum(d0 + d1);
+      for (int64_t i = lane; i < len; i += 32) x[i] = fma(-t, v[i], x[i]);
       __syncwarp();
       x0 = x[0];
     }
-    if (c < ncand) {
-      double a = vn1[c], b = vn2[c];
-      if (a != 0.0) {
-        double temp = fabs(x0) / a;
-        temp = 1.0 - temp * temp;
-        temp = temp < 0.0 ? 0.0 : temp;
-        const double ratio = a / b;
-        const double temp2 = temp * ratio * ratio;
-        if (temp2 <= kTol3z) {
-          a = (len > 1) ? sqrt(warp_sum(tail)) : 0.0;
-          b = a;
-        } else {
-          a *= sqrt(temp);
-        }
-        if (lane == 0) {
-          vn1[c] = a;
-          vn2[c] = b;
-        }
-      }
-      if (better(a, c, bv, bi)) {
-        bv = a;
-        bi = c;
-      }
+    if (lane == slot) {
+      px0 = x0;
+      pc = c;
+    }
+    if (++slot == 32) {
+      downdate_lane(px0, pc, A, m, j, len, vn1, vn2, ncand, bv, bi);
+      slot = 0;
     }
   }
+  if (slot > 0) downdate_lane(px0, pc, A, m, j, len, vn1, vn2, ncand, bv, bi);
   block_best(bv, bi);
   if (threadIdx.x == 0) part[blockIdx.x] = QrcpArg{bv, bi};
 }

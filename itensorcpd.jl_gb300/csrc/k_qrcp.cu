@@ -222,17 +222,23 @@ __device__ __forceinline__ void downdate_lane(double px0, int64_t& pc, const dou
   pc = -1;
 }
 
-// Step j, the grid: apply H_j to columns j+1 .. n-1// Step j, the grid: apply H_j to columns j+1 .. n-1, downdate the candidates' norms, and write
-// this block's argmax partial.  CH > 0: the warp holds rows j .. m-1 of its column in CH
-// registers per lane (m - j <= 32 CH); CH == 0: two passes over global memory.  Two FMAs per
-// entry (w = v^T x, then the update); the norm downdates run one per lane (downdate_lane).
-template <int CH>
+// Step j, the grid: apply H_j to columns j+1 .. n-1, downdate the candidates' norms, and write
+// this block's argmax partial.  A warp takes 32 / LPC columns at a time, LPC lanes each; a lane
+// holds rows j + s, j + s + LPC, ... of its column in CH registers (m - j <= LPC CH).  CH == 0
+// (LPC = 32): two passes over global memory.  Two FMAs per entry (w = v^T x, then the update);
+// the reduction of w takes log2(LPC) shuffle steps shared by the warp's columns, and the norm
+// downdates run one per lane (downdate_lane).
+template <int LPC, int CH>
 __global__ void __launch_bounds__(QW * 32) k_qrcp_apply(double* __restrict__ A, int64_t m, int64_t n, int64_t ncand,
                                                         int64_t j, double* __restrict__ vn1, double* __restrict__ vn2,
                                                         const double* __restrict__ vbuf, const QrcpState* st,
                                                         QrcpArg* __restrict__ part) {
+  static_assert(LPC == 8 || LPC == 16 || LPC == 32, "lanes per column");
+  static_assert(CH > 0 || LPC == 32, "the two-pass form uses whole warps");
+  constexpr int G = 32 / LPC;  // columns per warp step
   if (st->active != j + 1) return;  // step j's reflector was not formed
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane / LPC, sl = lane % LPC;
   const double tau = st->tau;
   const int64_t len = m - j;
   const double* __restrict__ v = vbuf + j;
@@ -241,33 +247,40 @@ __global__ void __launch_bounds__(QW * 32) k_qrcp_apply(double* __restrict__ A, 
   double px0 = 0.0;  // this lane's pending column and its new row-j entry
   int64_t pc = -1;
   int slot = 0;
-  for (int64_t c = j + 1 + (int64_t)blockIdx.x * QW + w; c < n; c += (int64_t)gridDim.x * QW) {
-    double* __restrict__ x = A + c * m + j;
+  const int64_t wstride = (int64_t)gridDim.x * QW * G;
+  for (int64_t base = j + 1 + ((int64_t)blockIdx.x * QW + w) * G; base < n; base += wstride) {
+    const int64_t c = base + g;
+    const bool live = c < n;
+    double* __restrict__ x = A + (live ? c : base) * m + j;
     double x0;
     if constexpr (CH > 0) {
       double xr[CH];
       double d0 = 0.0, d1 = 0.0;  // two chains halve the dependent FMA latency
 #pragma unroll
       for (int q = 0; q < CH; ++q) {
-        const int64_t i = lane + 32 * q;
-        xr[q] = (i < len) ? x[i] : 0.0;
-        if (i < len) {
+        const int64_t i = sl + (int64_t)LPC * q;
+        const bool in = live && i < len;
+        xr[q] = in ? x[i] : 0.0;
+        if (in) {
           if (q & 1)
             d1 = fma(v[i], xr[q], d1);
           else
             d0 = fma(v[i], xr[q], d0);
         }
       }
-      const double t = tau * warp_sum(d0 + d1);
+      double d = d0 + d1;
+#pragma unroll
+      for (int off = LPC / 2; off; off >>= 1) d += __shfl_xor_sync(FULL, d, off);
+      const double t = tau * d;
 #pragma unroll
       for (int q = 0; q < CH; ++q) {
-        const int64_t i = lane + 32 * q;
-        if (i < len) {
+        const int64_t i = sl + (int64_t)LPC * q;
+        if (live && i < len) {
           xr[q] = fma(-t, v[i], xr[q]);
           x[i] = xr[q];
         }
       }
-      x0 = __shfl_sync(FULL, xr[0], 0);
+      x0 = xr[0];  // row j of column c, held by sub-lane 0 of each group
     } else {
       double d0 = 0.0, d1 = 0.0;
       for (int64_t i = lane; i < len; i += 64) {
@@ -279,11 +292,16 @@ __global__ void __launch_bounds__(QW * 32) k_qrcp_apply(double* __restrict__ A, 
       __syncwarp();
       x0 = x[0];
     }
-    if (lane == slot) {
-      px0 = x0;
-      pc = c;
+    // hand the G new columns to lanes slot .. slot + G - 1 for their downdates
+    const int rel = lane - slot;
+    const bool mine = rel >= 0 && rel < G;
+    const double got = __shfl_sync(FULL, x0, mine ? rel * LPC : 0);
+    if (mine && base + rel < n) {
+      px0 = got;
+      pc = base + rel;
     }
-    if (++slot == 32) {
+    slot += G;
+    if (slot == 32) {
       downdate_lane(px0, pc, A, m, j, len, vn1, vn2, ncand, bv, bi);
       slot = 0;
     }
@@ -430,14 +448,18 @@ cudaError_t launch_qrcp_step(const QrcpJob& q, int64_t j, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   if (j + 1 >= q.n) return cudaSuccess;  // no trailing columns
   const int64_t len = q.m - j;
-  if (len <= 32 * 4)
-    k_qrcp_apply<4><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+  if (len <= 8 * 4)
+    k_qrcp_apply<8, 4><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+  else if (len <= 8 * 16)
+    k_qrcp_apply<8, 16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+  else if (len <= 16 * 16)
+    k_qrcp_apply<16, 16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   else if (len <= 32 * 16)
-    k_qrcp_apply<16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+    k_qrcp_apply<32, 16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   else if (len <= 32 * 32)
-    k_qrcp_apply<32><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+    k_qrcp_apply<32, 32><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   else
-    k_qrcp_apply<0><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+    k_qrcp_apply<32, 0><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   return cudaGetLastError();
 }
 

@@ -348,17 +348,22 @@ def _prepare_target(target):
 
 
 def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=False, device=0, rng=None,
-                 normal=False, **kwargs) -> CPD:
-    """als_optimizer.jl:15-25 / 37-55: default alg KRPFreeNormal, default check NoCheck(maxiter or 100)."""
+                 normal=None, **kwargs) -> CPD:
+    """als_optimizer.jl:15-25 / 37-55: default alg KRPFreeNormal, default check NoCheck(maxiter or 100).
+    ``normal`` defaults as the algorithm's compute_als does: false for the leverage-score
+    solvers (krp_lev_score_sampled.jl:7, 48), true for the QR-pivoted ones
+    (qr_lev_score_sampled.jl:9, 88, 186)."""
     T = _prepare_target(target)
     alg = KRPFreeNormal() if alg is None else alg
     check = NoCheck(100 if maxiter is None else maxiter) if check is None else check
     R = cp_rank(cp)
     if isinstance(alg, PivotBasedSolvers):
+        if normal is not None:
+            kwargs["normal"] = normal
         als = compute_als(T, cp, alg=alg, check=check, rng=rng, device=device, **kwargs)
         return optimize(cp, als, verbose=verbose, device=device)
     if isinstance(alg, ProjectionAlgorithm):
-        return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, normal,
+        return _lev_score_optimize(T, cp, alg, check, verbose, device, rng, bool(normal),
                                    stop_resample=int(kwargs.get("stop_resample", -1)),
                                    on_pivots=kwargs.get("on_pivots"))
     source = kwargs.get("tensor_source")  # an Engine holding T on the device (decompose's rank loop)
@@ -545,10 +550,30 @@ def sparse_sign_matrix(l, n, s, rows=None, vals=None, *, omega=False, injective=
     return rows, vals
 
 
-def sketched_matricization(T, k, l, rows, vals, s, device=0):
+def _omega_entries(omega):
+    """(l, 1-based rows, vals, s) of an explicit sparse embedding (a scipy sparse l x n matrix
+    with the same number s of stored entries in every column, as sparse_sign_matrix(...;
+    omega=true) builds it), in the column-major entry order the generators write."""
+    import scipy.sparse as sp
+
+    if not sp.issparse(omega):
+        raise TypeError("omega must be a scipy sparse matrix")
+    om = sp.csc_matrix(omega)
+    om.sort_indices()
+    counts = np.diff(om.indptr)
+    if counts.size == 0 or np.any(counts != counts[0]) or counts[0] < 1:
+        raise ValueError("every column of omega must hold the same number (>= 1) of entries")
+    return om.shape[0], om.indices.astype(np.int32) + 1, om.data.astype(np.float64), int(counts[0])
+
+
+def sketched_matricization(T, k, l, rows=None, vals=None, s=None, device=0):
     """pivot_mapping.jl:111-140: A_sk = T_(k) Omega^T (I_k x l) for the embedding in 1-based
     ``rows`` / ``vals`` (n * s entries, n the product of the other extents).  ``k`` is the
-    0-based mode.  Runs on the device through ``cpals_sketched_matricization``."""
+    0-based mode.  ``sketched_matricization(T, k, omega)`` with a scipy sparse Omega is the
+    form of pivot_mapping.jl:90-108.  Runs on the device through
+    ``cpals_sketched_matricization``."""
+    if rows is None and not isinstance(l, (int, np.integer)):
+        l, rows, vals, s = _omega_entries(l)
     T = _prepare_target(T)
     r0 = np.ascontiguousarray(rows, dtype=np.int64) - 1
     if r0.size and (r0.min() < 0 or r0.max() >= int(l)):
@@ -632,10 +657,12 @@ def SEQRCS(A, mode=None, l=None, s=None, t=None, *, compute_r=True, use_omega=Fa
                           stop_ratio=stop_ratio)
 
 
-def omega_hadamard(factors, rows, vals, l, s, device=0):
+def omega_hadamard(factors, rows, vals=None, l=None, s=None, device=0):
     """omega_hadamard (src/algebra/had_contract.jl:300-326): Omega times the Khatri-Rao product
     of ``factors`` (I_m x R matrices, the first index fastest), l x R, for the embedding in
-    1-based ``rows`` / ``vals``."""
+    1-based ``rows`` / ``vals``, or ``omega_hadamard(factors, omega)`` with a scipy sparse Omega."""
+    if vals is None:
+        l, rows, vals, s = _omega_entries(rows)
     factors = [np.asarray(F, dtype=np.float64) for F in factors]
     R = factors[0].shape[1]
     dims = tuple(F.shape[0] for F in factors) + (1,)

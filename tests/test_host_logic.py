@@ -75,3 +75,23 @@ def test_update_samples_keeps_or_reshuffles(pkg):
         np.testing.assert_array_equal(a3.additional_items["projects_tensors"][n], got[:12])
     with pytest.raises(AssertionError):
         pkg.update_samples(T, pkg.ALS(T, pkg.LevScoreSampled(4), items, pkg.NoCheck(1)), 5)
+
+
+def test_explicit_omega_entries(pkg):
+    """The explicit-Omega forms (pivot_mapping.jl:90-108, had_contract.jl:300) read a sparse
+    Omega back into the generators' entry layout."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(3)
+    l, n, s = 11, 7, 3
+    rows = np.concatenate([np.sort(rng.choice(l, s, replace=False)) for _ in range(n)]).astype(np.int32) + 1
+    vals = rng.choice([-1.0, 1.0], n * s) / np.sqrt(s)
+    om = sp.csc_matrix((vals, (rows - 1, np.repeat(np.arange(n), s))), shape=(l, n))
+    l2, r2, v2, s2 = pkg.api._omega_entries(om)
+    assert (l2, s2) == (l, s)
+    np.testing.assert_array_equal(r2, rows)
+    np.testing.assert_array_equal(v2, vals)
+    # a column with one entry fewer
+    short = sp.csc_matrix((vals[1:], (rows[1:] - 1, np.repeat(np.arange(n), s)[1:])), shape=(l, n))
+    with pytest.raises(ValueError):
+        pkg.api._omega_entries(short)

@@ -101,3 +101,18 @@ def test_sketch_keeps_singular_values(built):
     sk = built.sketched_matricization(At, 0, l, rows, vals, s)  # (m x l) = A^T Omega^T
     ratio = np.linalg.svd(sk.T, compute_uv=False) / np.linalg.svd(A, compute_uv=False)
     assert np.all((0.5 <= ratio) & (ratio <= 1.5))
+
+
+def test_explicit_omega_forms(built, oracle):
+    """pivot_mapping.jl:90-108 and had_contract.jl:300: the forms taking the sparse Omega
+    (sparse_sign_matrix(...; omega=true)) give the entry forms' results."""
+    dims = (6, 7, 5)
+    T = np.asfortranarray(det_normal(41, dims))
+    n = 7 * 5
+    l, s = 20, 3
+    rows, vals = built.sparse_sign_matrix(l, n, s, seed=4)
+    om = built.sparse_sign_matrix(l, n, s, seed=4, omega=True)
+    np.testing.assert_array_equal(built.sketched_matricization(T, 0, om),
+                                  built.sketched_matricization(T, 0, l, rows, vals, s))
+    mats = [det_normal(42, (7, 4)), det_normal(43, (5, 4))]
+    np.testing.assert_array_equal(built.omega_hadamard(mats, om), built.omega_hadamard(mats, rows, vals, l, s))

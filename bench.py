@@ -681,6 +681,22 @@ def main():
         extras["converged"] = {"sweeps": 200, "fit_bf16x3": conv["bf16x3"][0], "fit_fp64": conv["fp64"][0],
                                "last10_change_bf16x3": conv["bf16x3"][1], "last10_change_fp64": conv["fp64"][1],
                                "final_fit_diff": abs(conv["bf16x3"][0] - conv["fp64"][0])}
+        # the QR-pivoted solvers' pivot factorization of the mode-0 unfolding (512 x 262144, FP64;
+        # every step, LAPACK xGEQP3's pivots); recorded, never fatal to the headline line
+        try:
+            with pkg.Engine(DIMS, 1, dtype=np.float32, precision="fp64", device=device) as eq:
+                eq.set_tensor(T_host)
+                eq.unfolding_qrcp(0, max_steps=8)
+                t0 = time.perf_counter()
+                rq = eq.unfolding_qrcp(0)
+                dq = time.perf_counter() - t0
+            mq, nq = DIMS[0], DIMS[1] * DIMS[2]
+            fq = 2.0 * mq * mq * nq - 2.0 * mq ** 3 / 3.0
+            extras["qrcp_mode0_unfolding"] = {"ms": dq * 1e3, "steps": rq.steps, "shape": [mq, nq],
+                                              "fp64_tflops": fq / dq / 1e12,
+                                              "timing": "host wall clock of the synchronous C-ABI call"}
+        except Exception as exc:
+            extras["qrcp_mode0_unfolding"] = {"error": str(exc)}
         cpu = cpu_baseline_sample(pkg, T_host)
     else:
         cpu = None

@@ -1202,7 +1202,7 @@ int group_omega_rows(int64_t l, int64_t n, int zeta, const int32_t* rows, const 
 
 // The sketch of SE-QRCS into b.A (m x l): T_(mode) Omega^T (source 0) or (Omega KRP)^T (source 1).
 int fill_sketch(cpals_ctx* c, int source, int mode, int64_t l, const OmegaRows& o, double* dst) {
-  int64_t *dseg = nullptr, *dcol = nullptr, *dpos = nullptr;
+  int64_t *dseg = nullptr, *dcol = nullptr;
   double* dv = nullptr;
   int rc = CPALS_OK;
   std::vector<int64_t> pos;
@@ -1241,7 +1241,6 @@ int fill_sketch(cpals_ctx* c, int source, int mode, int64_t l, const OmegaRows& 
   }
   cudaFree(dseg);
   cudaFree(dcol);
-  cudaFree(dpos);
   cudaFree(dv);
   return rc;
 }

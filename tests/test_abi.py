@@ -90,3 +90,35 @@ def test_diff_and_angle_checks_marshal_to_the_device_struct(pkg):
                      PrevCP=CPD([np.ones((2, 1))], np.ones(1)))
     c = _to_device_check(a)
     assert (c.kind, c.iter, c.counter, c.norm_prev, c.lastfit, c.has_prev) == (L.CHECK_ANGLE, 2, 1, 3.5, 0.25, 1)
+
+
+def test_pivot_and_sketch_entries_reject_bad_arguments_before_touching_a_device(lib):
+    """Argument checks of the QRCP / SE-QRCS / sketch entries run before any CUDA call."""
+    A = np.zeros(6)
+    perm = np.zeros(3, dtype=np.int64)
+    rd = np.zeros(3)
+    k = np.zeros(1, dtype=np.int64)
+    def P(a):  # a typed pointer, as the loaded signatures expect
+        ct = {np.dtype(np.float64): ctypes.c_double, np.dtype(np.int64): ctypes.c_int64,
+              np.dtype(np.int32): ctypes.c_int32}[a.dtype]
+        return a.ctypes.data_as(ctypes.POINTER(ct))
+
+    assert lib.cpals_qrcp(0, 0, 3, P(A), 0, 0, -1.0, P(perm), P(rd), P(k), None, None) == -1  # m = 0
+    assert lib.cpals_qrcp(0, 2, 0, P(A), 0, 0, -1.0, P(perm), P(rd), P(k), None, None) == -1  # n = 0
+    assert lib.cpals_qrcp(0, 2, 3, None, 0, 0, -1.0, P(perm), P(rd), P(k), None, None) == -1  # no matrix
+    assert lib.cpals_qrcp(0, 2, 3, P(A), 0, 0, -1.0, None, P(rd), P(k), None, None) == -1  # no perm
+    for fn in (lib.cpals_unfolding_qrcp, lib.cpals_krp_qrcp):
+        assert fn(None, 0, 0, None, 0, 0, -1.0, P(perm), P(rd), P(k), None, None) == -1
+    rows = np.zeros(4, dtype=np.int32)
+    vals = np.zeros(4)
+    ns = np.zeros(1, dtype=np.int64)
+    assert lib.cpals_seqrcs(None, 0, 0, 4, 1, P(rows), P(vals), 2, 0, 0, -1.0, P(perm), P(rd), P(k), P(ns),
+                            None, None) == -1
+    assert lib.cpals_omega_hadamard(None, 0, 4, 1, P(rows), P(vals), P(A)) == -1
+    assert lib.cpals_sketched_matricization(None, 0, 4, 1, P(rows), P(vals), P(A)) == -1
+    cs = np.zeros(5, dtype=np.int32)
+    assert lib.cpals_sparse_sign(0, 0, 4, 1, 0, 1, P(rows), P(vals), P(cs)) == -1  # l = 0
+    assert lib.cpals_sparse_sign(0, 4, -1, 1, 0, 1, P(rows), P(vals), P(cs)) == -1  # n < 0
+    assert lib.cpals_sparse_sign(0, 4, 4, 0, 0, 1, P(rows), P(vals), P(cs)) == -1  # zeta = 0
+    # n = 0 is a valid empty embedding: colstarts = [0], no device work
+    assert lib.cpals_sparse_sign(0, 4, 0, 2, 0, 1, P(rows), P(vals), P(cs)) == 0 and cs[0] == 0

@@ -28,6 +28,16 @@ Parity pinning
     by the caller instead);
   - the contraction order chosen inside ITensors.jl.
   Both are pinned to tolerance only.
+* The pivot solvers and SE-QRCS take pivots from LinearAlgebra's qr(A, ColumnNorm()), which
+  is LAPACK xGEQP3, a third-party routine (no Manifest.toml pins its version).
+  - ``qrcp_lapack`` calls the same routine through scipy.
+  - ``qrcp_loop`` restates it one step at a time: the largest partial norm with ties to the
+    first position, xLAQP2's norm downdate with the sqrt(eps) recompute, and xLARFG's
+    reflector.
+  - ``tests/test_oracle.py`` checks that the loop gives xGEQP3's pivots exactly, and its R
+    and Q to rounding.
+  - The sparse sign generators are pinned by the reference's own C sources: ``build_oracle.py``
+    compiles them into ``_ref/``, and the tests check the layouts against them.
 """
 from __future__ import annotations
 

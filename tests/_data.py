@@ -46,3 +46,15 @@ def det_factors(dims, rank, seed):
         lam = np.sqrt(np.sum(X * X, axis=0))
         factors.append(X / lam[None, :])
     return factors, lam
+
+
+def golden_qrcp_matrix(case):
+    """The matrix of one qrcp_pivots.json case, rebuilt from its seeds."""
+    if "tensor_dims" in case:
+        T = np.asfortranarray(det_normal(case["seed"], case["tensor_dims"]))
+        k = case["mode"]
+        return np.reshape(np.moveaxis(T, k, 0), (T.shape[k], -1), order="F")
+    if "seeds" in case:  # rank 5 (40 x 5 times 5 x 300) plus 1e-9 noise
+        a, b, c = case["seeds"]
+        return det_normal(a, (40, 5)) @ det_normal(b, (5, 300)) + 1e-9 * det_normal(c, (40, 300))
+    return det_normal(case["seed"], case["shape"])

@@ -103,12 +103,57 @@ def lev_small():
     return out
 
 
+def qrcp_pivots():
+    # qr(A, ColumnNorm()) (LAPACK xGEQP3, which the pivot solvers and SEQRCS call) on seeded
+    # matrices: Gaussian, a mode-1 unfolding, and rank 5 with 1e-9 noise (first 6 pivots only;
+    # the rest sit at the noise level).  Pivots 1-based, |diag(R)|.
+    out = []
+    for name, seed, shape in (("gauss_30x50", 51, (30, 50)), ("gauss_64x40", 52, (64, 40)),
+                              ("gauss_1x9", 53, (1, 9))):
+        A = det_normal(seed, shape)
+        _, R, p = oracle.qrcp_lapack(A)
+        out.append({"name": name, "seed": seed, "shape": list(shape), "p": p.tolist(),
+                    "absdiag": np.abs(np.diag(R)).tolist(), "compare": p.size})
+    dims = (8, 9, 10)
+    T = np.asfortranarray(det_normal(54, dims))
+    _, R, p = oracle.qrcp_lapack(oracle.unfold(T, 1))
+    out.append({"name": "unfold_8x9x10_mode1", "seed": 54, "tensor_dims": list(dims), "mode": 1, "p": p.tolist(),
+                "absdiag": np.abs(np.diag(R)).tolist(), "compare": p.size})
+    A = det_normal(55, (40, 5)) @ det_normal(56, (5, 300)) + 1e-9 * det_normal(57, (40, 300))
+    _, R, p = oracle.qrcp_lapack(A)
+    out.append({"name": "rank5_noise_40x300", "seeds": [55, 56, 57], "shape": [40, 300], "p": p.tolist(),
+                "absdiag": np.abs(np.diag(R)).tolist(), "compare": 6})
+    return out
+
+
+def seqrcs_small():
+    # SEQRCS.jl:139-182 (subset in pivot order) on a seeded 20x30x10 tensor, mode 0,
+    # l = round(3 m ln m) = 180, s = round(ln m) = 3, t = 8, with a stored embedding of the
+    # sparse_sign layout (3 distinct rows per column, +-1/sqrt(3)).
+    dims, k = (20, 30, 10), 0
+    T = np.asfortranarray(det_normal(61, dims))
+    m = dims[k]
+    n = int(np.prod(dims)) // m
+    l, s, t = int(round(3 * m * np.log(m))), int(round(np.log(m))), 8
+    rng = np.random.default_rng(62)
+    rows = np.concatenate([rng.choice(l, size=s, replace=False) for _ in range(n)]).astype(np.int64) + 1
+    vals = np.where(rng.random(n * s) < 0.5, -1.0, 1.0) / np.sqrt(s)
+    out = {"tensor_dims": list(dims), "seed": 61, "mode": k, "l": l, "s": s, "t": t,
+           "rows": rows.tolist(), "vals": vals.tolist(), "cases": []}
+    for use_omega in (False, True):
+        _, _, p, rd = oracle.seqrcs(T, k, l, s, t, rows, vals, use_omega=use_omega, compute_r=False)
+        out["cases"].append({"use_omega": use_omega, "p": p.tolist(), "absdiag": np.abs(rd).tolist()})
+    return out
+
+
 def main():
     (HERE / "index_maps.json").write_text(json.dumps(index_maps()))
     (HERE / "als_small.json").write_text(json.dumps(als_small()))
     (HERE / "als_c1.json").write_text(json.dumps(als_c1()))
     (HERE / "rank_deficient.json").write_text(json.dumps(rank_deficient()))
     (HERE / "lev_small.json").write_text(json.dumps(lev_small()))
+    (HERE / "qrcp_pivots.json").write_text(json.dumps(qrcp_pivots()))
+    (HERE / "seqrcs_small.json").write_text(json.dumps(seqrcs_small()))
     for p in sorted(HERE.glob("*.json")):
         print(p.name, p.stat().st_size)
 

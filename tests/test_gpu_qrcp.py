@@ -281,3 +281,31 @@ def test_pivot_solvers_interpolate_a_known_low_rank(built, oracle):
     for kw in (dict(), dict(normal=False), dict(normal=False, injective=True), dict(normal=True, injective=True)):
         assert multiple_tries(built, A, cp, exact_error, alg=built.KSEQRCSPivProjected(1, (1200,), (1, 2, 3), 5),
                               check=built.CPDiffCheck(1e-5, 100), **kw)
+
+
+def test_device_reproduces_golden_pivots(built, golden_dir):
+    """The committed xGEQP3 pivots and SE-QRCS permutations (tests/golden/) from the device."""
+    import json
+
+    from _data import golden_qrcp_matrix
+
+    for case in json.loads((golden_dir / "qrcp_pivots.json").read_text()):
+        A = golden_qrcp_matrix(case)
+        k = case["compare"]
+        if "tensor_dims" in case:
+            T = np.asfortranarray(det_normal(case["seed"], case["tensor_dims"]))
+            with built.Engine(T.shape, 1, dtype=np.float64, precision="fp64") as e:
+                e.set_tensor(T)
+                res = e.unfolding_qrcp(case["mode"])
+        else:
+            res = built.qrcp(A)
+        np.testing.assert_array_equal(res.p[:k], case["p"][:k], err_msg=case["name"])
+        np.testing.assert_allclose(np.abs(res.rdiag[:k]), case["absdiag"][:k], rtol=0,
+                                   atol=1e-12 * np.linalg.norm(A))
+    g = json.loads((golden_dir / "seqrcs_small.json").read_text())
+    T = np.asfortranarray(det_normal(g["seed"], g["tensor_dims"]))
+    for case in g["cases"]:
+        res = built.SEQRCS(T, g["mode"], g["l"], g["s"], g["t"], rows=np.asarray(g["rows"]), vals=np.asarray(g["vals"]),
+                           use_omega=case["use_omega"], compute_r=False)
+        np.testing.assert_array_equal(res.p, case["p"])
+        np.testing.assert_allclose(np.abs(res.rdiag), case["absdiag"], rtol=0, atol=1e-12 * np.linalg.norm(T))

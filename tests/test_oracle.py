@@ -439,3 +439,29 @@ def test_oracle_seqrcs_of_the_krp(oracle):
     Qf, Rf, pf, _ = oracle.seqrcs_krp(mats, 2500, 1, 40, rows, vals)
     np.testing.assert_array_equal(pf, p)
     assert abs(_qr_error(Kt, Qf, Rf, pf, 40) - _qr_error(Kt, Q, R, p, 40)) <= 1e-10
+
+
+def test_qrcp_golden_pivots(oracle, golden_dir):
+    """The committed xGEQP3 pivots (tests/golden/qrcp_pivots.json): scipy's LAPACK and the
+    step-by-step restatement both reproduce them."""
+    from _data import golden_qrcp_matrix
+
+    for case in json.loads((golden_dir / "qrcp_pivots.json").read_text()):
+        A = golden_qrcp_matrix(case)
+        k = case["compare"]
+        _, R, p = oracle.qrcp_lapack(A)
+        p2, rd, _, _ = oracle.qrcp_loop(A)
+        np.testing.assert_array_equal(p[:k], case["p"][:k], err_msg=case["name"])
+        np.testing.assert_array_equal(p2[:k], case["p"][:k], err_msg=case["name"])
+        np.testing.assert_allclose(np.abs(rd[:k]), case["absdiag"][:k], rtol=0, atol=1e-12 * np.linalg.norm(A))
+
+
+def test_seqrcs_golden(oracle, golden_dir):
+    """tests/golden/seqrcs_small.json: SE-QRCS of a seeded tensor with a stored embedding."""
+    g = json.loads((golden_dir / "seqrcs_small.json").read_text())
+    T = np.asfortranarray(det_normal(g["seed"], g["tensor_dims"]))
+    for case in g["cases"]:
+        _, _, p, rd = oracle.seqrcs(T, g["mode"], g["l"], g["s"], g["t"], np.asarray(g["rows"]),
+                                    np.asarray(g["vals"]), use_omega=case["use_omega"], compute_r=False)
+        np.testing.assert_array_equal(p, case["p"])
+        np.testing.assert_allclose(np.abs(rd), case["absdiag"], rtol=0, atol=1e-12 * np.linalg.norm(T))

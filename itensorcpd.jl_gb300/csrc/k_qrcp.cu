@@ -454,8 +454,8 @@ cudaError_t launch_qrcp_step(const QrcpJob& q, int64_t j, cudaStream_t st) {
     k_qrcp_apply<8, 16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   else if (len <= 16 * 16)
     k_qrcp_apply<16, 16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
-  else if (len <= 32 * 16)
-    k_qrcp_apply<32, 16><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
+  else if (len <= 16 * 32)
+    k_qrcp_apply<16, 32><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   else if (len <= 32 * 32)
     k_qrcp_apply<32, 32><<<g, QW * 32, 0, st>>>(q.A, q.m, q.n, q.ncand, j, q.vn1, q.vn2, q.vbuf, q.st, q.part);
   else

@@ -125,6 +125,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def replica_max(dist, x, device=0):
+    """The whole-job clock: the maximum of a per-rank time over all ranks (x itself when there
+    is no process group).  NCCL reduces on the rank's GPU, gloo on the host."""
+    if dist is None:
+        return x
+    import torch
+
+    dev = f"cuda:{device}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, steps, sweeps, ms):
+    """Whole-job sweeps/s of `world` replicas that each ran steps x sweeps in at most `ms`."""
+    return world * steps * sweeps / (ms / 1e3)
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -547,13 +565,7 @@ def main():
             dist.barrier()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_max(dist, x, device)
 
     T_host, keep = pinned_like(DIMS)
     make_tensor(pkg, out=T_host)
@@ -599,7 +611,7 @@ def main():
     launches = eng.launch_count() - l0
     ms = max_over_ranks(ms)
     final_fit = float(traj[-1])
-    value = world * args.steps * SWEEPS / (ms / 1e3)
+    value = replica_value(world, args.steps, SWEEPS, ms)
 
     # ---- MTTKRP kernel duration (CUDA events around every launch, one profiled step)
     eng.set_profiling(True)
@@ -628,7 +640,7 @@ def main():
     for _ in range(args.steps):
         step_e2e()
     e2e_ms = max_over_ranks(eng.timer_stop())
-    e2e_value = world * args.steps * SWEEPS / (e2e_ms / 1e3)
+    e2e_value = replica_value(world, args.steps, SWEEPS, e2e_ms)
     fac_bytes = sum(d * RANK * 8 for d in DIMS) + RANK * 8
 
     # ---- sweep time under each convergence check (tolerance 0, so none stops early)

@@ -169,8 +169,8 @@ int cpals_sketched_matricization(cpals_ctx* ctx, int mode, int64_t l, int zeta, 
  * QR with column pivoting in FP64 on the device, with LAPACK xGEQP3's pivot rule (largest
  * partial column norm, lowest position on ties) and norm downdating, replacing
  * qr(A, ColumnNorm()) where the reference takes pivots from it
- * (src/optimizers/als_optimizers/randomized/qr_lev_score_sampled.jl:24, 124, 233;
- * src/algebra/SEQRCS.jl:101, 115, 147, 161, 198, 213).  Common arguments:
+ * (src/optimizers/als_optimizers/randomized/qr_lev_score_sampled.jl:23, 127, 243;
+ * src/algebra/SEQRCS.jl:101, 117, 152, 166, 198, 221).  Common arguments:
  *   ncand      pivots are chosen among the first ncand columns (<= 0: all); the other
  *              columns only receive the reflectors (so R's columns past ncand are Q^T A_rest);
  *   max_steps  at most this many Householder steps (<= 0: min(m, ncand));
@@ -185,13 +185,13 @@ int cpals_qrcp(int device, int64_t m, int64_t n, const double* A, int64_t ncand,
 /* The same on columns of the resident tensor's mode unfolding T_(mode) (I_mode x prod of the
  * other extents, columns numbered as Julia's reshape(array(T, (i, Ris...)), ...) does):
  * the ncols columns cols (1-based), or every column when cols is NULL.  Replaces the
- * qr(Tmat, ColumnNorm()) of qr_lev_score_sampled.jl:19-24 and the A_subset QR of
- * SEQRCS.jl:161. */
+ * qr(Tmat, ColumnNorm()) of qr_lev_score_sampled.jl:22-23, 126-127 and the A_subset QR of
+ * SEQRCS.jl:117, 166. */
 int cpals_unfolding_qrcp(cpals_ctx* ctx, int mode, int64_t ncols, const int64_t* cols, int64_t ncand,
                          int64_t max_steps, double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps,
                          double* R, double* Q);
 /* The same on columns of the transposed Khatri-Rao product of the held factors other than
- * `mode` (R x prod of the other extents; qr_lev_score_sampled.jl:228-233). */
+ * `mode` (R x prod of the other extents; qr_lev_score_sampled.jl:240-243). */
 int cpals_krp_qrcp(cpals_ctx* ctx, int mode, int64_t ncols, const int64_t* cols, int64_t ncand, int64_t max_steps,
                    double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R, double* Q);
 /* omega_hadamard (src/algebra/had_contract.jl:300-326): Omega times the Khatri-Rao product of
@@ -204,8 +204,8 @@ int cpals_omega_hadamard(cpals_ctx* ctx, int mode, int64_t l, int zeta, const in
  * than `mode` (m = R).  n = prod of the other extents.  Stage 1 sketches with the embedding
  * (rows 0-based, vals) and takes the first t pivots of the pivoted QR of the m x l sketch;
  * the columns of Omega with an entry in one of those rows form the subset, in pivot order
- * then column order with repeats dropped (sorted_subset = 0, SEQRCS.jl:155-157) or in column
- * order (sorted_subset = 1, SEQRCS.jl:107-108, 204-205); *nsubset = its size.  Stage 2 is the
+ * then column order with repeats dropped (sorted_subset = 0, SEQRCS.jl:158-159) or in column
+ * order (sorted_subset = 1, SEQRCS.jl:109-111, 205-207); *nsubset = its size.  Stage 2 is the
  * pivoted QR of the subset's columns: perm (n, 1-based) = vcat(subset[p_subset], the other
  * columns ascending), rdiag its diagonal (up to min(m, nsubset) entries).  compute_r != 0 also
  * returns R (steps x n: the subset's R, then Q^T times the other columns) and Q (m x steps)

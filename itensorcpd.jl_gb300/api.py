@@ -352,7 +352,7 @@ def als_optimize(target, cp: CPD, alg=None, check=None, maxiter=None, verbose=Fa
     """als_optimizer.jl:15-25 / 37-55: default alg KRPFreeNormal, default check NoCheck(maxiter or 100).
     ``normal`` defaults as the algorithm's compute_als does: false for the leverage-score
     solvers (krp_lev_score_sampled.jl:7, 48), true for the QR-pivoted ones
-    (qr_lev_score_sampled.jl:9, 88, 186)."""
+    (optimizers/.../randomized/qr_lev_score_sampled.jl:9, 88, 186)."""
     T = _prepare_target(target)
     alg = KRPFreeNormal() if alg is None else alg
     check = NoCheck(100 if maxiter is None else maxiter) if check is None else check
@@ -646,7 +646,7 @@ def SEQRCS(A, mode=None, l=None, s=None, t=None, *, compute_r=True, use_omega=Fa
         r0 = np.ascontiguousarray(rows, dtype=np.int64)[: n * s_eff] - 1
         v = np.ascontiguousarray(vals, dtype=np.float64)[: n * s_eff]
     if krp:
-        # the KRP path always selects with the explicit Omega (SEQRCS.jl:203-205): column order
+        # the KRP path always selects with the explicit Omega (SEQRCS.jl:205-207): column order
         with Engine(dims, R, dtype=np.float64, precision="fp64", device=device) as eng:
             eng.set_factors(list(factors) + [np.ones((1, R))], np.ones(R))
             return eng.seqrcs(1, kmode, l, r0, v, s_eff, t, sorted_subset=True, compute_r=compute_r,
@@ -682,7 +682,7 @@ def _range_arg(x):
 
 class _PivotBased(ProjectionAlgorithm):
     """Start / End of the pivot range (1-based, inclusive; End 0 = every column), one value
-    or one per mode (qr_lev_score_sampled.jl:9-20)."""
+    or one per mode (algorithms/.../randomized/qr_lev_score_sampled.jl:10-22)."""
 
     def __init__(self, start, end):
         self.Start = _range_arg(start)
@@ -693,7 +693,7 @@ class _PivotBased(ProjectionAlgorithm):
 
 
 class QRPivProjected(_PivotBased):
-    """qr_lev_score_sampled.jl:9-20: projection by the pivots of the column-pivoted QR of each
+    """algorithms/.../randomized/qr_lev_score_sampled.jl:10-22: projection by the pivots of the column-pivoted QR of each
     mode unfolding.  ``QRPivProjected()`` = (1, 0), ``(n)`` = (1, n), ``((n1, n2, ...))`` =
     per-mode ends from 1, ``(start, end)``."""
 
@@ -733,13 +733,13 @@ class _RandomModes(_PivotBased):
 
 
 class SEQRCSPivProjected(_RandomModes):
-    """qr_lev_score_sampled.jl:25-48: QRPivProjected with SE-QRCS pivots on ``random_modes``
+    """algorithms/.../randomized/qr_lev_score_sampled.jl:28-50: QRPivProjected with SE-QRCS pivots on ``random_modes``
     (mode numbers from 1, as in the reference); ``rank_vect`` gives each such mode's sketch
     pivot count t."""
 
 
 class KSEQRCSPivProjected(_RandomModes):
-    """qr_lev_score_sampled.jl:51-82: pivots from the Khatri-Rao product of a preliminary
+    """algorithms/.../randomized/qr_lev_score_sampled.jl:61-83: pivots from the Khatri-Rao product of a preliminary
     leverage-score ALS solution (SE-QRCS on ``random_modes``, the KRP's pivoted QR elsewhere)."""
 
 
@@ -755,7 +755,7 @@ def stop(alg):
 
 
 def copy_alg(alg, new_start=0, new_end=0):
-    """qr_lev_score_sampled.jl:18-20, 45-47, 79-81: the algorithm with a new pivot range
+    """algorithms/.../randomized/qr_lev_score_sampled.jl:21-22, 49-50, 82-83: the algorithm with a new pivot range
     (0 keeps the old one)."""
     zero = (lambda v: all(int(x) == 0 for x in v)) if isinstance(new_start, (tuple, list)) else (lambda v: int(v) == 0)
     st = alg.Start if zero(new_start) else _range_arg(new_start)
@@ -778,7 +778,7 @@ class ALS:
 
 
 def _pivot_range(alg, mode, dRis):
-    """qr_lev_score_sampled.jl:48-56: the (start, end) of the pivots a mode keeps."""
+    """optimizers/.../randomized/qr_lev_score_sampled.jl:51-58: the (start, end) of the pivots a mode keeps."""
     int_end = alg._per_mode(stop(alg), mode)
     int_end = dRis if int_end == 0 else int_end
     int_end = min(int_end, dRis)
@@ -797,7 +797,7 @@ def _effective_rank(rdiag, trunc_tol):
 
 
 def _arrange(p, meff, shuffle_pivots, rng):
-    """p1 = p[1:meff] kept, the rest shuffled (qr_lev_score_sampled.jl:29-34)."""
+    """p1 = p[1:meff] kept, the rest shuffled (optimizers/.../randomized/qr_lev_score_sampled.jl:40-44)."""
     p = np.asarray(p, dtype=np.int64)
     rest = p[meff:]
     if shuffle_pivots:
@@ -857,7 +857,7 @@ def compute_als(target, cp: CPD, alg=None, check=None, *, shuffle_pivots=True, t
 
     if isinstance(alg, KSEQRCSPivProjected):
         # a preliminary leverage-score ALS puts the factors near T's leverage structure
-        # (qr_lev_score_sampled.jl:196-207)
+        # (optimizers/.../randomized/qr_lev_score_sampled.jl:194-202)
         if guess_num_levs is None:
             base = cp
             nsamp = 10 * cp_rank(cp) if prelim_sample_size is None else int(prelim_sample_size)
@@ -905,7 +905,7 @@ def compute_als(target, cp: CPD, alg=None, check=None, *, shuffle_pivots=True, t
 
 
 def update_samples(target, als: ALS, new_num_end, reshuffle=False, new_num_start=0, rng=None) -> ALS:
-    """update_samples (algorithms/.../randomized/qr_lev_score_sampled.jl:93-144): the same pivots
+    """update_samples (algorithms/.../randomized/qr_lev_score_sampled.jl:95-149): the same pivots
     with a new range; ``reshuffle`` redraws the order of the pivots past each mode's effective
     rank."""
     if not isinstance(als.mttkrp_alg, PivotBasedSolvers):

@@ -1349,7 +1349,7 @@ int cpals_seqrcs(cpals_ctx* c, int source, int mode, int64_t l, int zeta, const 
     if (rc != CPALS_OK) return rc;
   }
   // the columns of Omega with an entry in a selected row: in pivot order then column order,
-  // first occurrence kept (SEQRCS.jl:155-157), or in column order (SEQRCS.jl:107-108, 204-205)
+  // first occurrence kept (SEQRCS.jl:158-159), or in column order (SEQRCS.jl:109-111, 205-207)
   std::vector<int64_t> subset;
   std::vector<char> in((size_t)n, 0);
   if (sorted_subset) {

@@ -756,8 +756,8 @@ def _embedding_row_lists(l, n, s, rows1):
 def seqrcs(T, k, l, s, t, rows1, vals, use_omega=False, compute_r=True):
     """SE-QRCS of the mode-k unfolding (src/algebra/SEQRCS.jl:89-182; k 0-based): the first t
     pivots of the pivoted QR of the sketch T_(k) Omega^T; the columns of Omega with an entry
-    in those rows (use_omega: in column order, SEQRCS.jl:107-108; else for each pivot row in
-    order, its columns ascending, first occurrence kept, SEQRCS.jl:155-157); the pivoted QR
+    in those rows (use_omega: in column order, SEQRCS.jl:109-111; else for each pivot row in
+    order, its columns ascending, first occurrence kept, SEQRCS.jl:158-159); the pivoted QR
     of those columns of T_(k); p = vcat(subset[p_subset], the other columns).  With
     compute_r, R = hcat(R_subset, Q^T A_rem).  Returns (Q, R, p 1-based, diag(R_subset))."""
     A = unfold(np.asarray(T, dtype=np.float64), k)
@@ -841,7 +841,7 @@ def seqrcs_krp(mats, l, s, t, rows1, vals, compute_r=True):
 
 
 def effective_rank(rdiag, trunc_tol) -> int:
-    """meff = sum(abs.(dr) ./ maximum(abs.(dr)) .> trunc_tol) (qr_lev_score_sampled.jl:26)."""
+    """meff = sum(abs.(dr) ./ maximum(abs.(dr)) .> trunc_tol) (optimizers/.../randomized/qr_lev_score_sampled.jl:28)."""
     d = np.abs(np.asarray(rdiag, dtype=np.float64))
     if d.size == 0:
         return 0
@@ -850,7 +850,7 @@ def effective_rank(rdiag, trunc_tol) -> int:
 
 
 def projected_als(T, factors, lam, projectors, sweeps, normal=True, record=None):
-    """The pivot-based solvers' sweeps (optimize.jl:15-32 with qr_lev_score_sampled.jl:146-162
+    """The pivot-based solvers' sweeps (optimize.jl:15-32 with algorithms/.../randomized/qr_lev_score_sampled.jl:151-166
     and ProjectionAlgorithm.jl:57-68): every mode solves its projected least-squares problem
     at fixed pivots (``projectors[n]``, 1-based multi-coordinates) and row-normalizes."""
     factors = [np.array(F, dtype=np.float64) for F in factors]

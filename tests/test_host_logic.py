@@ -23,7 +23,7 @@ def test_pivot_solver_structs_and_ranges(pkg):
     assert k.rank_vect == {1: 10, 2: 10, 3: 10}
     c = pkg.copy_alg(k, 0, 600)
     assert isinstance(c, pkg.KSEQRCSPivProjected) and c.random_modes == (1, 2, 3) and pkg.stop(c) == 600
-    # qr_lev_score_sampled.jl:48-56: end 0 = every column, clamped to the column count
+    # optimizers/.../randomized/qr_lev_score_sampled.jl:51-58: end 0 = every column, clamped to the column count
     assert api._pivot_range(pkg.QRPivProjected(), 0, 1200) == (1, 1200)
     assert api._pivot_range(pkg.QRPivProjected(5000), 0, 1200) == (1, 1200)
     assert api._pivot_range(pkg.QRPivProjected((1, 3, 2), (10, 20, 30)), 1, 100) == (3, 20)
@@ -47,7 +47,7 @@ def test_effective_rank_and_arrangement(pkg):
 
 
 def test_update_samples_keeps_or_reshuffles(pkg):
-    """update_samples (qr_lev_score_sampled.jl:93-144): a new range on the same pivots, or the
+    """update_samples (algorithms/.../randomized/qr_lev_score_sampled.jl:95-149): a new range on the same pivots, or the
     order past meff redrawn."""
     api = pkg.api
     dims = (4, 5, 6)

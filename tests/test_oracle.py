@@ -377,7 +377,7 @@ def test_qrcp_loop_is_lapack_geqp3(oracle, shape):
 
 def test_qrcp_loop_low_rank_and_early_stop(oracle):
     """Rank 5 plus 1e-9 noise: the same pivots as xGEQP3 throughout; a stopping ratio ends the
-    run one step after the last |r_jj| above it (qr_lev_score_sampled.jl:26 counts meff)."""
+    run one step after the last |r_jj| above it (optimizers/.../randomized/qr_lev_score_sampled.jl:28 counts meff)."""
     rng = np.random.default_rng(4)
     A = rng.standard_normal((40, 5)) @ rng.standard_normal((5, 300)) + 1e-9 * rng.standard_normal((40, 300))
     p, rd, _, _ = oracle.qrcp_loop(A)

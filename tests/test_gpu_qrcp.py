@@ -145,7 +145,7 @@ def qr_error(A, Q, R, p, k):
 
 
 def test_seqrcs_reference_property(built, oracle):
-    """test/SEQRCS_test.jl:31-68: the rank-40 error of SE-QRCS of a 50 x 10000 Gaussian matrix
+    """test/SEQRCS_test.jl:32-64: the rank-40 error of SE-QRCS of a 50 x 10000 Gaussian matrix
     (l = 2500, s = 1, t = 40) is within 1e-2 of the pivoted QR's, with either subset order; the
     KRP path equals the explicit-KRP path on the same embedding."""
     A = det_normal(11, (50, 10000))

@@ -2,7 +2,7 @@
 
 The generator follows the reference's C generators' rules (src/algebra/sparse_sign.c,
 src/algebra/sparsestack.c); its draws come from a counter-based stream, so the checks are
-the structure (as test/SEQRCS_test.jl:7-16 checks it), reproducibility per seed, and the
+the structure (as test/SEQRCS_test.jl:13-18 checks it), reproducibility per seed, and the
 distribution of rows and signs.  The sketched matricization
 (src/algebra/pivot_mapping.jl:111-140) must equal the oracle's restatement and the dense
 product T_(k) Omega^T within 1e-12 relative (FP64 sums in the reference's entry order).
@@ -41,7 +41,7 @@ def structure(l, n, s, rows1, vals, injective):
 
 @pytest.mark.parametrize("injective", [False, True])
 def test_sparse_sign_structure_and_reproducibility(built, injective):
-    """SEQRCS_test.jl:7-16: s nonzeros in every column, values +-1/sqrt(s); the same seed
+    """SEQRCS_test.jl:13-18: s nonzeros in every column, values +-1/sqrt(s); the same seed
     gives the same embedding, another seed another one."""
     for (l, n, s) in [(1200, 10000, 8), (50, 300, 4), (7, 40, 7), (13, 25, 5), (5, 9, 9)]:
         rows, vals = built.sparse_sign_matrix(l, n, s, injective=injective, seed=17)
@@ -92,7 +92,7 @@ def test_sketched_matricization_matches_oracle(built, oracle, dims, dt):
 
 
 def test_sketch_keeps_singular_values(built):
-    """test/SEQRCS_test.jl:17-28: a 10000 x 10 Gaussian matrix sketched to 1200 rows with 8
+    """test/SEQRCS_test.jl:20-28: a 10000 x 10 Gaussian matrix sketched to 1200 rows with 8
     nonzeros per column keeps its singular values within a factor [0.5, 1.5]."""
     m, n, s, l = 10, 10000, 8, 1200
     A = det_normal(77, (n, m))

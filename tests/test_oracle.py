@@ -317,7 +317,7 @@ def _embedding_structure(l, n, s, rows0, vals, injective):
 @pytest.mark.parametrize("injective", [False, True])
 def test_reference_sparse_sign_generators_structure(oracle, injective):
     # the reference's own C generators, compiled from its sources by oracle/build_oracle.py:
-    # these are the rules the device generator must follow (SEQRCS_test.jl:7-16)
+    # these are the rules the device generator must follow (SEQRCS_test.jl:13-18)
     ref = oracle.load_ref_sparse_sign()
     if ref is None:
         pytest.skip("reference generators not built (no reference checkout)")
@@ -408,7 +408,7 @@ def _qr_error(A, Q, R, p, k):
 
 
 def test_oracle_seqrcs_reference_property(oracle):
-    """test/SEQRCS_test.jl:31-50: for a 50 x 10000 Gaussian matrix, the rank-40 error of SE-QRCS
+    """test/SEQRCS_test.jl:32-47: for a 50 x 10000 Gaussian matrix, the rank-40 error of SE-QRCS
     (l = 2500, s = 1, t = 40; both subset orders) is within 1e-2 of the pivoted QR's."""
     rng = np.random.default_rng(6)
     A = rng.standard_normal((50, 10000))
@@ -425,7 +425,7 @@ def test_oracle_seqrcs_reference_property(oracle):
 
 
 def test_oracle_seqrcs_of_the_krp(oracle):
-    """test/SEQRCS_test.jl:52-68 compares SE-QRCS of a KRP given by its factors with SE-QRCS of
+    """test/SEQRCS_test.jl:49-64 compares SE-QRCS of a KRP given by its factors with SE-QRCS of
     the explicit KRP matrix (rank-40 errors within 1e-2, each with its own embedding).  With
     the same embedding the two are the same computation (the KRP path selects its subset in
     column order, as the matrix path does with the explicit Omega), so the pivots agree and the

@@ -117,7 +117,7 @@ int cpals_get_gram(cpals_ctx* ctx, int mode, double* host_gram);
 
 /* MTTKRP of `mode` with the current factors: M_n = T_(n) (KRP of the other factors),
  * I_n x R column-major.  Replaces matricize_tensor(::KRPFreeNormal / ::KRPNormal)
- * (src/algorithms/als_algorithms/standard/tensor.jl:52-84). */
+ * (src/algorithms/als_algorithms/standard/tensor.jl:12-44). */
 int cpals_mttkrp(cpals_ctx* ctx, int mode, double* host_out);
 
 /* Run ALS sweeps with the given check: the loop of optimize
@@ -275,7 +275,7 @@ int cpals_leverage_scores(cpals_ctx* ctx, int mode, double* host_probs);
 /* One LevScoreSampled mode update with host-drawn pivots: sampled KRP gather,
  * sampled fibre gather, solve_ls_problem(::ProjectionAlgorithm) (normal != 0:
  * (S^T S) X = (T_s S)^T; else the tall least-squares problem), row_norm
- * (randomized/ProjectionAlgorithm.jl:57-68, randomized/krp_lev_score_sampled.jl:87-125). */
+ * (randomized/ProjectionAlgorithm.jl:57-68, randomized/krp_lev_score_sampled.jl:20-57). */
 int cpals_sampled_update(cpals_ctx* ctx, int mode, const int64_t* pivots, int64_t nsamps, int normal);
 
 /* ---- batched small decompositions ----

@@ -135,7 +135,7 @@ class CPAngleCheck(ConvergeAlg):
 
 
 def CPDFit(check) -> float:  # noqa: N802 - reference name
-    """fit_check.jl:68, cp_diff_check.jl:70, cp_angle_check.jl:70."""
+    """fit_check.jl:68, cp_diff_check.jl:73, cp_angle_check.jl:75."""
     return check.final_fit
 
 
@@ -148,11 +148,11 @@ class MttkrpAlgorithm:
 
 
 class KRPFreeNormal(MttkrpAlgorithm):
-    """Normal-equation ALS, the reference default (standard/tensor.jl:70-89); FP64 MTTKRP on the GPU."""
+    """Normal-equation ALS, the reference default (standard/tensor.jl:27-49); FP64 MTTKRP on the GPU."""
 
 
 class KRPNormal(MttkrpAlgorithm):
-    """Normal-equation ALS with an explicit KRP in the reference (standard/tensor.jl:50-65).
+    """Normal-equation ALS with an explicit KRP in the reference (standard/tensor.jl:10-25).
     On the GPU the KRP is never materialised; the arithmetic is the same FP64 MTTKRP."""
 
 
@@ -202,7 +202,7 @@ class BlockLevScoreSampled(LevScoreSampled):
 
 
 # ---------------------------------------------------------------------------
-# Initial guesses (src/cpd.jl:85-119)
+# Initial guesses (src/cpd.jl:48-84)
 # ---------------------------------------------------------------------------
 def _row_norm_host(X):
     lam = np.sqrt(np.sum(X * X, axis=0))
@@ -210,7 +210,7 @@ def _row_norm_host(X):
 
 
 def random_factors(dims, rank, rng=None, dtype=np.float64):
-    """cpd.jl:85-97: iid N(0,1) I_n x R factors (column-major draw order), each
+    """cpd.jl:48-61: iid N(0,1) I_n x R factors (column-major draw order), each
     column-normalised; lambda is that of the last factor.  ``rng`` defaults to a
     generator seeded with 3, as the reference defaults to MersenneTwister(3)."""
     rng = np.random.default_rng(3) if rng is None else rng
@@ -223,7 +223,7 @@ def random_factors(dims, rank, rng=None, dtype=np.float64):
 
 
 def random_CPD(target, rank, rng=None) -> CPD:  # noqa: N802 - reference name
-    """cpd.jl:100-119."""
+    """cpd.jl:63-84."""
     T = np.asarray(target)
     factors, lam = random_factors(T.shape, int(rank), rng, dtype=T.dtype if T.dtype in (np.float32, np.float64)
                                   else np.float64)

@@ -2,8 +2,8 @@
 //
 // Computes M_n(i, r) = sum_{k} T_(n)(i, k) * KRP(k, r) for the mode-n unfolding of
 // a column-major tensor (the product that matricize_tensor(::KRPFreeNormal) forms
-// with R tensor-times-vector chains, src/algorithms/als_algorithms/standard/tensor.jl:72-84,
-// and matricize_tensor(::KRPNormal) with an explicit KRP, tensor.jl:52-60).
+// with R tensor-times-vector chains, src/algorithms/als_algorithms/standard/tensor.jl:32-44,
+// and matricize_tensor(::KRPNormal) with an explicit KRP, tensor.jl:12-20).
 //
 // The reduction index space is cut into chunks of CH consecutive values of the
 // fastest reduction mode f at fixed values of the other reduction modes.  Inside

@@ -2,7 +2,7 @@
 //
 // M_n(i, r) = sum_k T_(n)(i, k) KRP(k, r), the contraction that
 // matricize_tensor(::KRPFreeNormal / ::KRPNormal) forms
-// (src/algorithms/als_algorithms/standard/tensor.jl:52-84), computed as
+// (src/algorithms/als_algorithms/standard/tensor.jl:12-44), computed as
 //   T ~ Th + Tl,  KRP ~ Kh + Kl  (BF16 hi/lo, round to nearest),
 //   M ~ Th Kh + Th Kl + Tl Kh   (three BF16 tensor-core products).
 //

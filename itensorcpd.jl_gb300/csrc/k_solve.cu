@@ -10,7 +10,7 @@
 //   gram       : X^T X by 16x16 tiles of the upper triangle over row splits, each tile
 //                reduced by its last block in split order (deterministic).
 //   finalize   : lambda = column norms (row_norm.jl:4-24), G_n = F_n^T F_n (post_solve,
-//                standard/tensor.jl:86-89); after the last mode the fit and the
+//                standard/tensor.jl:22-25, 46-49); after the last mode the fit and the
 //                FitCheck / NoCheck update (fit_check.jl:24-66, no_check.jl:11-19).
 //   normalize  : F_n = X ./ lambda, plus the FP32 column-major copy the tensor-core
 //                MTTKRP reads.

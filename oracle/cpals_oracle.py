@@ -61,7 +61,7 @@ def row_norm(X: np.ndarray):
 
 
 def random_factors(dims, rank, rng: np.random.Generator):
-    """src/cpd.jl:85-97.
+    """src/cpd.jl:48-61.
 
     One iid N(0,1) I_n x R matrix per mode, filled in column-major draw order as
     Julia's ``randn`` fills it.  Each is column-normalised; the returned lambda
@@ -76,7 +76,7 @@ def random_factors(dims, rank, rng: np.random.Generator):
 
 
 def gram(F: np.ndarray) -> np.ndarray:
-    """post_solve, src/algorithms/als_algorithms/standard/tensor.jl:86-89: G = F^T F."""
+    """post_solve, src/algorithms/als_algorithms/standard/tensor.jl:22-25, 46-49: G = F^T F."""
     return F.T @ F
 
 
@@ -97,7 +97,7 @@ def hadamard_of_grams(grams, skip: int) -> np.ndarray:
 # MTTKRP
 # ---------------------------------------------------------------------------
 def mttkrp_krp_free(T: np.ndarray, factors, mode: int) -> np.ndarray:
-    """matricize_tensor(::KRPFreeNormal), standard/tensor.jl:72-84 with
+    """matricize_tensor(::KRPFreeNormal), standard/tensor.jl:32-44 with
     had_contract(list, r), src/algebra/had_contract.jl:72-124.
 
     For every rank column r, T is contracted with the vectors F_m[:, r] of every
@@ -121,7 +121,7 @@ def mttkrp_krp_free(T: np.ndarray, factors, mode: int) -> np.ndarray:
 
 
 def khatri_rao(mats) -> np.ndarray:
-    """had_contract(factors, r) of the KRPNormal path, standard/tensor.jl:52-60.
+    """had_contract(factors, r) of the KRPNormal path, standard/tensor.jl:12-20.
 
     Rows are indexed by the multi-index of ``mats`` with the FIRST matrix's row
     index fastest (column-major fusion of the remaining modes).
@@ -139,7 +139,7 @@ def unfold(T: np.ndarray, mode: int) -> np.ndarray:
 
 
 def mttkrp_krp(T: np.ndarray, factors, mode: int) -> np.ndarray:
-    """matricize_tensor(::KRPNormal), standard/tensor.jl:52-60: T_(n) * KRP."""
+    """matricize_tensor(::KRPNormal), standard/tensor.jl:12-20: T_(n) * KRP."""
     others = [factors[m] for m in range(T.ndim) if m != mode]
     return unfold(T, mode) @ khatri_rao(others)
 
@@ -400,7 +400,7 @@ def als_optimize(T, factors, lam, check=None, maxiter=None, alg="krp", verbose=F
     both compute the same MTTKRP and differ only in rounding order.
     ``record`` (optional list) receives per-sweep dicts with the MTTKRP of every
     mode, for per-call parity checks.  ``work_dtype`` is the factors' element type
-    (the reference keeps the target's element type, cpd.jl:100-105; FP64 by default
+    (the reference keeps the target's element type, cpd.jl:63-78; FP64 by default
     here for parity work).
     Returns (factors, lam, check, n_fallbacks).
     """

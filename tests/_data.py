@@ -39,7 +39,7 @@ def det_normal(seed: int, shape) -> np.ndarray:
 
 
 def det_factors(dims, rank, seed):
-    """random_factors (src/cpd.jl:85-97) with det_normal draws: unit columns, lambda of the last."""
+    """random_factors (src/cpd.jl:48-61) with det_normal draws: unit columns, lambda of the last."""
     factors, lam = [], None
     for k, d in enumerate(dims):
         X = det_normal(seed * 1000 + k, (d, rank))

@@ -15,8 +15,8 @@
    correction of each mode's coefficients; the start is F_n = Q_n (C_n + dC_n), columns
    normalised: it lies inside the sketched column range.
 
-Random-init ALS stays the fallback and the judge: the warm start changes only the starting
-point, ALS still runs to its convergence check, and a degenerate start (non-finite values
+Random-init ALS stays the fallback, and ALS decides when to stop: the warm start changes only
+the starting point, ALS still runs to its convergence check, and a degenerate start (non-finite values
 or a zero column) falls back to the reference's random start.
 """
 from __future__ import annotations

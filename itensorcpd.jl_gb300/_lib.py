@@ -79,6 +79,8 @@ SIGNATURES = {
     "cpals_krp_qrcp": (C.c_int, [_P, C.c_int, C.c_int64, _I64P, C.c_int64, C.c_int64, C.c_double, _I64P, _DP,
                                  _I64P, _DP, _DP]),
     "cpals_omega_hadamard": (C.c_int, [_P, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_int32), _DP, _DP]),
+    "cpals_seqrcs_subset": (C.c_int, [C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_int32), C.c_int64, _I64P, C.c_int,
+                                      _I64P, _I64P]),
     "cpals_seqrcs": (C.c_int, [_P, C.c_int, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_int32), _DP, C.c_int64,
                                C.c_int, C.c_int, C.c_double, _I64P, _DP, _I64P, _I64P, _DP, _DP]),
     "cpals_fallback_count": (C.c_int, [_P, _I64P]),

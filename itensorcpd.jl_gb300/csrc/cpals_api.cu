@@ -1200,6 +1200,37 @@ int group_omega_rows(int64_t l, int64_t n, int zeta, const int32_t* rows, const 
   return CPALS_OK;
 }
 
+// The columns of Omega (0-based) with an entry in one of the rows psk[0..t) (0-based), in pivot
+// order then column order with repeats dropped (SEQRCS.jl:158-159), or in column order
+// (sorted, SEQRCS.jl:109-111, 205-207); in[col] marks the members.
+void seqrcs_subset(int64_t l, int64_t n, int zeta, const int32_t* rows, const OmegaRows& o, int64_t t,
+                   const int64_t* psk, int sorted, std::vector<int64_t>& subset, std::vector<char>& in) {
+  subset.clear();
+  in.assign((size_t)n, 0);
+  if (sorted) {
+    std::vector<char> sel((size_t)l, 0);
+    for (int64_t q = 0; q < t; ++q) sel[(size_t)psk[q]] = 1;
+    for (int64_t col = 0; col < n; ++col)
+      for (int k = 0; k < zeta; ++k)
+        if (sel[(size_t)rows[col * zeta + k]]) {
+          in[(size_t)col] = 1;
+          subset.push_back(col);
+          break;
+        }
+  } else {
+    for (int64_t q = 0; q < t; ++q) {
+      const int64_t row = psk[q];
+      for (int64_t p = o.seg[(size_t)row]; p < o.seg[(size_t)row + 1]; ++p) {
+        const int64_t col = o.col[(size_t)p];
+        if (!in[(size_t)col]) {
+          in[(size_t)col] = 1;
+          subset.push_back(col);
+        }
+      }
+    }
+  }
+}
+
 // The sketch of SE-QRCS into b.A (m x l): T_(mode) Omega^T (source 0) or (Omega KRP)^T (source 1).
 int fill_sketch(cpals_ctx* c, int source, int mode, int64_t l, const OmegaRows& o, double* dst) {
   int64_t *dseg = nullptr, *dcol = nullptr;
@@ -1248,6 +1279,26 @@ int fill_sketch(cpals_ctx* c, int source, int mode, int64_t l, const OmegaRows& 
 }  // namespace
 
 extern "C" {
+
+int cpals_seqrcs_subset(int64_t l, int64_t n, int zeta, const int32_t* rows, int64_t t, const int64_t* psk,
+                        int sorted_subset, int64_t* subset, int64_t* nsubset) {
+  if (l < 1 || n < 0 || zeta < 1 || zeta > l || (n > 0 && !rows) || t < 1 || !psk || !subset || !nsubset)
+    return CPALS_E_ARG;
+  std::vector<int64_t> p0((size_t)t);
+  for (int64_t q = 0; q < t; ++q) {
+    if (psk[q] < 1 || psk[q] > l) return CPALS_E_ARG;
+    p0[(size_t)q] = psk[q] - 1;
+  }
+  OmegaRows o;
+  const int rc = group_omega_rows(l, n, zeta, rows, std::vector<double>((size_t)(n * zeta), 0.0).data(), o);
+  if (rc != CPALS_OK) return rc;
+  std::vector<int64_t> sub;
+  std::vector<char> in;
+  seqrcs_subset(l, n, zeta, rows, o, t, p0.data(), sorted_subset, sub, in);
+  for (size_t i = 0; i < sub.size(); ++i) subset[i] = sub[i] + 1;
+  *nsubset = (int64_t)sub.size();
+  return CPALS_OK;
+}
 
 int cpals_qrcp(int device, int64_t m, int64_t n, const double* A, int64_t ncand, int64_t max_steps,
                double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R, double* Q) {
@@ -1348,32 +1399,9 @@ int cpals_seqrcs(cpals_ctx* c, int source, int mode, int64_t l, int zeta, const 
     rc = qrcp_run(b, m, l, l, kmax, -1.0, c->num_sms, c->st, psk.data(), rd1.data(), &k1, nullptr, nullptr);
     if (rc != CPALS_OK) return rc;
   }
-  // the columns of Omega with an entry in a selected row: in pivot order then column order,
-  // first occurrence kept (SEQRCS.jl:158-159), or in column order (SEQRCS.jl:109-111, 205-207)
   std::vector<int64_t> subset;
-  std::vector<char> in((size_t)n, 0);
-  if (sorted_subset) {
-    std::vector<char> sel((size_t)l, 0);
-    for (int64_t q = 0; q < t; ++q) sel[(size_t)psk[(size_t)q]] = 1;
-    for (int64_t col = 0; col < n; ++col)
-      for (int k = 0; k < zeta; ++k)
-        if (sel[(size_t)rows[col * zeta + k]]) {
-          in[(size_t)col] = 1;
-          subset.push_back(col);
-          break;
-        }
-  } else {
-    for (int64_t q = 0; q < t; ++q) {
-      const int64_t row = psk[(size_t)q];
-      for (int64_t p = o.seg[(size_t)row]; p < o.seg[(size_t)row + 1]; ++p) {
-        const int64_t col = o.col[(size_t)p];
-        if (!in[(size_t)col]) {
-          in[(size_t)col] = 1;
-          subset.push_back(col);
-        }
-      }
-    }
-  }
+  std::vector<char> in;
+  seqrcs_subset(l, n, zeta, rows, o, t, psk.data(), sorted_subset, subset, in);
   const int64_t nsub = (int64_t)subset.size();
   *nsubset = nsub;
   std::vector<int64_t> order = subset;  // matrix columns: the subset, then (with R) the rest ascending

@@ -753,6 +753,25 @@ def _embedding_row_lists(l, n, s, rows1):
     return lists
 
 
+def seqrcs_subset(l, n, s, rows1, psk1, use_omega) -> np.ndarray:
+    """The SE-QRCS column subset (1-based) for sketch pivots psk1 (1-based rows of Omega):
+    use_omega, the columns of omega[p_sk, :] with a nonzero, in column order
+    (SEQRCS.jl:109-111, 205-207); otherwise, for each pivot row in order, the columns
+    holding it, ascending, with repeats dropped (SEQRCS.jl:158-159)."""
+    r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
+    if use_omega:
+        sel = set(int(p) - 1 for p in psk1)
+        return np.asarray([c + 1 for c in range(n) if any(int(j) in sel for j in r[c])], dtype=np.int64)
+    lists = _embedding_row_lists(l, n, s, rows1)
+    subset, seen = [], set()
+    for p in psk1:
+        for c in lists[int(p) - 1]:
+            if c not in seen:
+                seen.add(c)
+                subset.append(c + 1)
+    return np.asarray(subset, dtype=np.int64)
+
+
 def seqrcs(T, k, l, s, t, rows1, vals, use_omega=False, compute_r=True):
     """SE-QRCS of the mode-k unfolding (src/algebra/SEQRCS.jl:89-182; k 0-based): the first t
     pivots of the pivoted QR of the sketch T_(k) Omega^T; the columns of Omega with an entry
@@ -764,20 +783,7 @@ def seqrcs(T, k, l, s, t, rows1, vals, use_omega=False, compute_r=True):
     n = A.shape[1]
     Ask = sketched_matricization(np.asarray(T, dtype=np.float64), k, l, rows1, vals, s)
     _, _, psk = qrcp_lapack(Ask)
-    psk = psk[:t] - 1
-    lists = _embedding_row_lists(l, n, s, rows1)
-    if use_omega:
-        sel = set(int(p) for p in psk)
-        r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
-        subset = [c for c in range(n) if any(int(j) in sel for j in r[c])]
-    else:
-        subset, seen = [], set()
-        for p in psk:
-            for c in lists[int(p)]:
-                if c not in seen:
-                    seen.add(c)
-                    subset.append(c)
-    subset = np.asarray(subset, dtype=np.int64)
+    subset = seqrcs_subset(l, n, s, rows1, psk[:t], use_omega) - 1
     rem = np.setdiff1d(np.arange(n), subset)
     if subset.size == 0:
         return None, None, rem + 1, np.zeros(0)
@@ -825,9 +831,7 @@ def seqrcs_krp(mats, l, s, t, rows1, vals, compute_r=True):
     n = int(np.prod(dims))
     Ask = omega_hadamard(mats, l, s, rows1, vals)
     _, _, psk = qrcp_lapack(Ask.T.copy())
-    sel = set(int(p) - 1 for p in psk[:t])
-    r = np.asarray(rows1[: n * s], dtype=np.int64).reshape(n, s) - 1
-    subset = np.asarray([c for c in range(n) if any(int(j) in sel for j in r[c])], dtype=np.int64)
+    subset = seqrcs_subset(l, n, s, rows1, psk[:t], True) - 1
     rem = np.setdiff1d(np.arange(n), subset)
     if subset.size == 0:
         return None, None, rem + 1, np.zeros(0)

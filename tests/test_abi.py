@@ -122,3 +122,30 @@ def test_pivot_and_sketch_entries_reject_bad_arguments_before_touching_a_device(
     assert lib.cpals_sparse_sign(0, 4, 4, 0, 0, 1, P(rows), P(vals), P(cs)) == -1  # zeta = 0
     # n = 0 is a valid empty embedding: colstarts = [0], no device work
     assert lib.cpals_sparse_sign(0, 4, 0, 2, 0, 1, P(rows), P(vals), P(cs)) == 0 and cs[0] == 0
+
+
+def test_seqrcs_subset_matches_the_oracle(lib, oracle):
+    """cpals_seqrcs_subset (host code, no device) selects the oracle's SE-QRCS subset in both
+    orders (SEQRCS.jl:109-111, 158-159, 205-207), including repeated and empty pivot rows."""
+    rng = np.random.default_rng(9)
+
+    def P(a, ct):
+        return a.ctypes.data_as(ctypes.POINTER(ct))
+
+    for (l, n, s, t) in [(20, 50, 3, 5), (7, 40, 2, 7), (30, 10, 1, 12), (9, 1, 4, 3)]:
+        rows1 = np.concatenate([rng.choice(l, size=s, replace=False) for _ in range(n)]).astype(np.int32) + 1
+        psk = rng.choice(l, size=t, replace=False).astype(np.int64) + 1
+        rows0 = (rows1 - 1).astype(np.int32)
+        for sorted_subset in (0, 1):
+            out = np.zeros(n, dtype=np.int64)
+            cnt = np.zeros(1, dtype=np.int64)
+            assert lib.cpals_seqrcs_subset(l, n, s, P(rows0, ctypes.c_int32), t, P(psk, ctypes.c_int64), sorted_subset,
+                                           P(out, ctypes.c_int64), P(cnt, ctypes.c_int64)) == 0
+            ref = oracle.seqrcs_subset(l, n, s, rows1, psk, bool(sorted_subset))
+            np.testing.assert_array_equal(out[: cnt[0]], ref)
+    bad = np.array([5], dtype=np.int64)  # a pivot row beyond l
+    rows0 = np.zeros(3, dtype=np.int32)
+    out = np.zeros(3, dtype=np.int64)
+    cnt = np.zeros(1, dtype=np.int64)
+    assert lib.cpals_seqrcs_subset(4, 3, 1, P(rows0, ctypes.c_int32), 1, P(bad, ctypes.c_int64), 0,
+                                   P(out, ctypes.c_int64), P(cnt, ctypes.c_int64)) == -1

@@ -95,3 +95,19 @@ def test_explicit_omega_entries(pkg):
     short = sp.csc_matrix((vals[1:], (rows[1:] - 1, np.repeat(np.arange(n), s)[1:])), shape=(l, n))
     with pytest.raises(ValueError):
         pkg.api._omega_entries(short)
+
+
+def test_bench_sweeps_to_fit():
+    """The bench's sweeps-to-fit report: the first sweep reaching each target, None when none does."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+    import bench
+
+    assert bench.sweeps_to_fit([0.1, 0.5, 0.9, 0.95], 0.9) == 3
+    assert bench.sweeps_to_fit([0.1, 0.5], 0.99) is None
+    rep = bench.sweeps_to_fit_report({"bf16x3": [0.2, 0.8, 0.899, 0.9], "fp64": [0.2, 0.85, 0.9, 0.9]})
+    assert rep["absolute"] == {"bf16x3": None, "fp64": None}
+    assert rep["relative_target"] == pytest.approx(0.891)
+    assert rep["relative"] == {"bf16x3": 3, "fp64": 3}

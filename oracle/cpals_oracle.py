@@ -572,22 +572,31 @@ def sampled_solve(S: np.ndarray, Ts: np.ndarray, normal: bool):
     return Xt.T.copy()
 
 
-def lev_score_als(T, factors, lam, nsamps, sweeps, rng, normal=False, record=None, block_size=None):
+def lev_score_als(T, factors, lam, nsamps, sweeps, rng, normal=False, record=None, block_size=None,
+                  stop_resample=-1):
     """LevScoreSampled path: optimizers/.../randomized/krp_lev_score_sampled.jl:1-40 and
-    algorithms/.../randomized/krp_lev_score_sampled.jl:20-58 (resample every mode, stop_resample = -1),
-    run for a fixed number of sweeps (a FitCheck is not honoured, ProjectionAlgorithm.jl:30-51).
+    algorithms/.../randomized/krp_lev_score_sampled.jl:20-58, run for a fixed number of sweeps
+    (a FitCheck is not honoured, ProjectionAlgorithm.jl:30-51).  With stop_resample < 0 every
+    mode draws new pivots every sweep; otherwise compute_als draws once per mode up front
+    and a sweep s draws again only while stop_resample > s (krp_lev_score_sampled.jl:24-25).
     ``record`` receives the per-mode pivots so a device run can replay them.
     ``block_size`` switches to BlockLevScoreSampled's draw (probability.jl:61-108).
     """
     factors = [np.array(F, dtype=np.float64) for F in factors]
     N = T.ndim
     probs = [leverage_score_probabilities(F) for F in factors]
-    for _ in range(sweeps):
+
+    def draw(n):
+        if block_size is None:
+            return sample_factor_matrices(nsamps, n, probs, rng)
+        return block_sample_factor_matrices(nsamps, probs, block_size, n, rng)
+
+    held = [draw(n) for n in range(N)] if stop_resample >= 0 else [None] * N
+    for sweep in range(sweeps):
         for n in range(N):
-            if block_size is None:
-                piv = sample_factor_matrices(nsamps, n, probs, rng)
-            else:
-                piv = block_sample_factor_matrices(nsamps, probs, block_size, n, rng)
+            if stop_resample < 0 or stop_resample > sweep:
+                held[n] = draw(n)
+            piv = held[n]
             others = [factors[m] for m in range(N) if m != n]
             S = pivot_hadamard(others, piv)
             Ts = fused_flatten_sample(T, n, piv)
@@ -868,6 +877,92 @@ def projected_als(T, factors, lam, projectors, sweeps, normal=True, record=None)
             factors[n], lam = row_norm(X)
             if record is not None:
                 record.append({"mode": n, "factor": factors[n].copy(), "lam": lam.copy()})
+    return factors, lam
+
+
+def np_sparse_sign(l, n, s, rng, injective=False):
+    """A sparse sign embedding drawn with numpy in the layouts of the reference's C generators
+    (src/algebra/sparse_sign.c: s distinct uniform rows per column; sparsestack.c: one uniform
+    row in each of s near-equal blocks), values +-1/sqrt(s), rows 1-based; s is clamped to l."""
+    s = min(int(s), int(l))
+    if injective:
+        q, r = divmod(l, s)
+        starts = np.array([j * (q + 1) if j < r else r * (q + 1) + (j - r) * q for j in range(s)])
+        sizes = np.array([q + 1 if j < r else q for j in range(s)])
+        rows = (starts[None, :] + (rng.random((n, s)) * sizes[None, :]).astype(np.int64)).reshape(-1)
+    else:
+        rows = np.concatenate([rng.choice(l, size=s, replace=False) for _ in range(n)])
+    vals = np.where(rng.random(n * s) < 0.5, -1.0, 1.0) / np.sqrt(s)
+    return rows.astype(np.int64) + 1, vals, s
+
+
+def kseqrcs_prelim(T, factors, lam, rng, prelim_niter=10, nsamps=None):
+    """The preliminary solve of KSEQRCSPivProjected's compute_als
+    (optimizers/.../randomized/qr_lev_score_sampled.jl:194-202): LevScoreSampled(10 R),
+    NoCheck(prelim_niter), normal equations, stop_resample = 0."""
+    R = factors[0].shape[1]
+    return lev_score_als(T, factors, lam, 10 * R if nsamps is None else nsamps, prelim_niter, rng, normal=True,
+                         stop_resample=0)
+
+
+def pivot_solver_setup(T, kind, start=1, end=0, random_modes=(), rank_vect=None, trunc_tol=0.01,
+                       shuffle_pivots=True, injective=False, rng=None, krp_factors=None):
+    """compute_als of the QR-pivoted solvers (optimizers/.../randomized/qr_lev_score_sampled.jl:1-281):
+    kind "qr" (QRPivProjected: pivoted QR of each unfolding), "seqrcs" (SEQRCSPivProjected:
+    SE-QRCS on the 1-based ``random_modes``), "kseqrcs" (KSEQRCSPivProjected: SE-QRCS of the KRP
+    of ``krp_factors`` on the random modes, its pivoted QR elsewhere).  Per mode: meff = the
+    count of |r_jj| / max |r_jj| above trunc_tol, p[1:meff] kept and the rest shuffled, the
+    pivots as 1-based multi-coordinates, and rows start..end (end 0 = all, clamped) as the
+    projector.  Returns (projectors, effective ranks, 1-based column pivots)."""
+    rng = np.random.default_rng(3) if rng is None else rng
+    N = T.ndim
+    projectors, effs, refs = [], [], []
+    for n in range(N):
+        dims_o = [d for m, d in enumerate(T.shape) if m != n]
+        dRis = int(np.prod(dims_o))
+        e = end if isinstance(end, int) else (end[0] if len(end) == 1 else end[n])
+        int_end = dRis if e == 0 else min(e, dRis)
+        st = start if isinstance(start, int) else (start[0] if len(start) == 1 else start[n])
+        assert 0 < st <= int_end
+        m = T.shape[n]
+        rand = (n + 1) in tuple(random_modes or ())
+        if rand:
+            l, s = int(round(3 * m * np.log(m))), max(1, int(round(np.log(m))))
+            t = int_end if rank_vect is None else int(rank_vect[n + 1])
+            rows1, vals, s = np_sparse_sign(l, dRis, s, rng, injective)
+        if kind == "qr" or (kind == "seqrcs" and not rand):
+            _, R, p = qrcp_lapack(unfold(T, n))
+            dr = np.diag(R)
+        elif kind == "seqrcs":
+            _, _, p, dr = seqrcs(T, n, l, s, t, rows1, vals, use_omega=False, compute_r=False)
+        elif rand:
+            others = [krp_factors[k] for k in range(N) if k != n]
+            _, _, p, dr = seqrcs_krp(others, l, s, t, rows1, vals, compute_r=False)
+        else:
+            others = [krp_factors[k] for k in range(N) if k != n]
+            _, R, p = qrcp_lapack(khatri_rao(others).T.copy())
+            dr = np.diag(R)
+        refs.append(np.asarray(p, dtype=np.int64))
+        meff = effective_rank(dr, trunc_tol)
+        effs.append(meff)
+        rest = np.asarray(p[meff:], dtype=np.int64)
+        if shuffle_pivots:
+            rest = rest[rng.permutation(rest.size)]
+        pp = np.concatenate([np.asarray(p[:meff], dtype=np.int64), rest])
+        projectors.append(column_to_multi_coords(pp, dims_o)[st - 1: int_end])
+    return projectors, effs, refs
+
+
+def projected_als_check(T, factors, lam, projectors, check, normal=True):
+    """optimize (optimize.jl:15-32) for a pivot-based solver: projected sweeps at fixed pivots
+    until a CPDiffCheck / CPAngleCheck stops them, or check.max_counter sweeps under a FitCheck
+    or NoCheck, which the projection solvers do not evaluate (ProjectionAlgorithm.jl:30-51)."""
+    factors = [np.array(F, dtype=np.float64) for F in factors]
+    cross = isinstance(check, CPDiffCheck)
+    for _ in range(int(check.max_counter)):
+        factors, lam = projected_als(T, factors, lam, projectors, 1, normal)
+        if cross and check.check_converge(factors, lam):
+            break
     return factors, lam
 
 

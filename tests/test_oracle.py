@@ -465,3 +465,68 @@ def test_seqrcs_golden(oracle, golden_dir):
                                     np.asarray(g["vals"]), use_omega=case["use_omega"], compute_r=False)
         np.testing.assert_array_equal(p, case["p"])
         np.testing.assert_allclose(np.abs(rd), case["absdiag"], rtol=0, atol=1e-12 * np.linalg.norm(T))
+
+
+def test_oracle_pivot_solvers_interpolate_a_known_low_rank(oracle):
+    """test/rand_cp_als.jl:72-96 on the oracle: a rank-10 model of an exactly rank-20 20x30x40
+    tensor under CPDiffCheck(1e-5, 100).  QRPivProjected(1200) and KSEQRCSPivProjected((1),
+    (1200,), (1,2,3), 5) (best of up to ten tries, rand_cp_als.jl:1-14) reach errors within 10%
+    of exact ALS's."""
+    dims = (20, 30, 40)
+    Ft, lt = det_factors(dims, 20, seed=21)
+    A = np.asfortranarray(oracle.reconstruct(Ft, lt))
+    F0, l0 = det_factors(dims, 10, seed=22)
+
+    def err(F, lam):
+        return np.linalg.norm(A - oracle.reconstruct(F, lam)) / np.linalg.norm(A)
+
+    Fe, le, _, _ = oracle.als_optimize(A, F0, l0, check=oracle.CPDiffCheck(1e-5, 100))
+    exact = err(Fe, le)
+    proj, eff, refs = oracle.pivot_solver_setup(A, "qr", end=1200, rng=np.random.default_rng(1))
+    assert [p.shape[0] for p in proj] == [1200, 800, 600]
+    assert all(sorted(r) == list(range(1, r.size + 1)) for r in refs)
+    Fq, lq = oracle.projected_als_check(A, F0, l0, proj, oracle.CPDiffCheck(1e-5, 100))
+    assert abs(exact - err(Fq, lq)) / exact < 0.1
+    ok = False
+    for i in range(10):
+        rng = np.random.default_rng(100 + i)
+        Fp, lp = oracle.kseqrcs_prelim(A, F0, l0, rng)
+        proj, eff, _ = oracle.pivot_solver_setup(A, "kseqrcs", end=1200, random_modes=(1, 2, 3),
+                                                 rank_vect={1: 5, 2: 5, 3: 5}, rng=rng, krp_factors=Fp)
+        Fk, lk = oracle.projected_als_check(A, F0, l0, proj, oracle.CPDiffCheck(1e-5, 100))
+        if abs(exact - err(Fk, lk)) / exact < 0.1:
+            ok = True
+            break
+    assert ok
+    # With end = 1200 every mode keeps all its columns, so the runs above equal exact ALS.
+    # With fewer pivots the projection is real: 400 pivots per mode (a third to two thirds of
+    # the columns) keep both solvers, and 200 keep QRPivProjected, within 10% of exact ALS.
+    for kind, end in (("qr", 400), ("qr", 200), ("kseqrcs", 400)):
+        rng = np.random.default_rng(5)
+        kw = {}
+        if kind == "kseqrcs":
+            Fp, lp = oracle.kseqrcs_prelim(A, F0, l0, rng)
+            kw = dict(random_modes=(1, 2, 3), rank_vect={1: 5, 2: 5, 3: 5}, krp_factors=Fp)
+        proj, _, _ = oracle.pivot_solver_setup(A, kind, end=end, rng=rng, **kw)
+        assert all(p.shape[0] == end for p in proj)
+        F, lam = oracle.projected_als_check(A, F0, l0, proj, oracle.CPDiffCheck(1e-5, 100))
+        assert abs(exact - err(F, lam)) / exact < 0.1, (kind, end)
+
+
+def test_oracle_np_sparse_sign_layouts(oracle):
+    """The oracle's numpy embedding follows the generators' two layouts (sparse_sign.c,
+    sparsestack.c) and clamps s to l."""
+    rng = np.random.default_rng(4)
+    for inj in (False, True):
+        rows, vals, s = oracle.np_sparse_sign(17, 60, 4, rng, injective=inj)
+        R = rows.reshape(60, 4) - 1
+        assert s == 4 and R.min() >= 0 and R.max() < 17
+        assert all(len(set(r)) == 4 for r in R)
+        assert np.all(np.abs(vals) == 0.5)
+        if inj:
+            q, r = divmod(17, 4)
+            starts = [j * (q + 1) if j < r else r * (q + 1) + (j - r) * q for j in range(4)]
+            ends = [starts[j] + (q + 1 if j < r else q) for j in range(4)]
+            assert all(starts[j] <= R[c, j] < ends[j] for c in range(60) for j in range(4))
+    rows, vals, s = oracle.np_sparse_sign(3, 5, 7, rng)
+    assert s == 3 and all(sorted(r) == [1, 2, 3] for r in rows.reshape(5, 3))

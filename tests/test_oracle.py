@@ -530,3 +530,23 @@ def test_oracle_np_sparse_sign_layouts(oracle):
             assert all(starts[j] <= R[c, j] < ends[j] for c in range(60) for j in range(4))
     rows, vals, s = oracle.np_sparse_sign(3, 5, 7, rng)
     assert s == 3 and all(sorted(r) == [1, 2, 3] for r in rows.reshape(5, 3))
+
+
+def test_oracle_pivot_solvers_rank400_against_exact_als(oracle):
+    """test/rand_cp_als.jl:38-70 on the oracle: 20x30x40 Gaussian tensor, rank 400,
+    FitCheck(1e-6, 20) (not evaluated by the projection solvers: 20 sweeps).  QRPivProjected(800)
+    with trunc_tol 0.001 reconstructs within 1e-2 of exact ALS, SEQRCSPivProjected(1, 800,
+    (1,2,3), (100,100,100)) within 1e-1 (normal equations; the tall form is the same
+    least-squares problem and the GPU tests run it)."""
+    dims = (20, 30, 40)
+    T = np.asfortranarray(det_normal(5, dims))
+    F, lam = det_factors(dims, 400, seed=6)
+    nT = float(np.linalg.norm(T))
+    Fe, le, _, _ = oracle.als_optimize(T, F, lam, check=oracle.FitCheck(1e-6, 20, nT))
+    ref = oracle.reconstruct(Fe, le)
+    for kind, tol, bound, kw in (("qr", 0.001, 1e-2, {}),
+                                 ("seqrcs", 0.01, 1e-1, dict(random_modes=(1, 2, 3),
+                                                             rank_vect={1: 100, 2: 100, 3: 100}))):
+        proj, _, _ = oracle.pivot_solver_setup(T, kind, end=800, trunc_tol=tol, rng=np.random.default_rng(2), **kw)
+        Fp, lp = oracle.projected_als_check(T, F, lam, proj, oracle.FitCheck(1e-6, 20, nT))
+        assert np.linalg.norm(ref - oracle.reconstruct(Fp, lp)) / np.linalg.norm(ref) < bound, kind

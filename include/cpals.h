@@ -210,6 +210,9 @@ int cpals_omega_hadamard(cpals_ctx* ctx, int mode, int64_t l, int zeta, const in
  * columns ascending), rdiag its diagonal (up to min(m, nsubset) entries).  compute_r != 0 also
  * returns R (steps x n: the subset's R, then Q^T times the other columns) and Q (m x steps)
  * and runs every step; otherwise stop_ratio applies. */
+int cpals_seqrcs(cpals_ctx* ctx, int source, int mode, int64_t l, int zeta, const int32_t* rows, const double* vals,
+                 int64_t t, int sorted_subset, int compute_r, double stop_ratio, int64_t* perm, double* rdiag,
+                 int64_t* steps, int64_t* nsubset, double* R, double* Q);
 /* The SE-QRCS column subset alone (host only, no device call): the columns of Omega (n * zeta
  * entries, 0-based rows as cpals_sparse_sign writes them) with an entry in one of the t rows
  * psk (1-based, the sketch's first pivots), in pivot order then column order with repeats
@@ -218,9 +221,6 @@ int cpals_omega_hadamard(cpals_ctx* ctx, int mode, int64_t l, int zeta, const in
  * count.  cpals_seqrcs selects its subset with the same code. */
 int cpals_seqrcs_subset(int64_t l, int64_t n, int zeta, const int32_t* rows, int64_t t, const int64_t* psk,
                         int sorted_subset, int64_t* subset, int64_t* nsubset);
-int cpals_seqrcs(cpals_ctx* ctx, int source, int mode, int64_t l, int zeta, const int32_t* rows, const double* vals,
-                 int64_t t, int sorted_subset, int compute_r, double stop_ratio, int64_t* perm, double* rdiag,
-                 int64_t* steps, int64_t* nsubset, double* R, double* Q);
 
 /* Number of normal-equation solves so far that took the pivoted-QR fallback
  * because the pivoted Cholesky was rank deficient (ldiv_solve.jl:17-22). */

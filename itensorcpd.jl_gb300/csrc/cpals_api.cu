@@ -111,19 +111,6 @@ cudaError_t cpals::set_smem_limit_once(const void* kernel, int bytes) {
 
 namespace {
 
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    cudaGetDevice(&prev);
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    cudaGetDevice(&cur);
-    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-  }
-};
-
 FactorSet factor_set(const cpals_ctx* c) {
   FactorSet fs{};
   for (int m = 0; m < c->order; ++m) fs.F[m] = c->F[m];
@@ -478,9 +465,9 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   int64_t numel = 1, maxI = 0;
   for (int m = 0; m < order; ++m) {
     if (dims[m] < 1 || dims[m] > (int64_t(1) << 31)) return CPALS_E_ARG;
+    if (dims[m] > (int64_t(1) << 40) / numel) return CPALS_E_ARG;  // at most 2^40 elements
     numel *= dims[m];
     maxI = std::max(maxI, dims[m]);
-    if (numel > (int64_t(1) << 40)) return CPALS_E_ARG;
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
@@ -924,7 +911,9 @@ int cpals_sparse_sign(int device, int64_t l, int64_t n, int zeta, int injective,
   if (colstarts)
     for (int64_t c = 0; c <= n; ++c) colstarts[c] = (int32_t)(c * zeta);
   if (n == 0) return CPALS_OK;
-  if (cudaSetDevice(device) != cudaSuccess) return CPALS_E_CUDA;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
+  DeviceGuard g(device);
   const size_t nnz = (size_t)n * zeta;
   int32_t* drows = nullptr;
   double* dvals = nullptr;
@@ -1303,7 +1292,9 @@ int cpals_seqrcs_subset(int64_t l, int64_t n, int zeta, const int32_t* rows, int
 int cpals_qrcp(int device, int64_t m, int64_t n, const double* A, int64_t ncand, int64_t max_steps,
                double stop_ratio, int64_t* perm, double* rdiag, int64_t* steps, double* R, double* Q) {
   if (m < 1 || n < 1 || !A || !perm || !rdiag || !steps) return CPALS_E_ARG;
-  if (cudaSetDevice(device) != cudaSuccess) return CPALS_E_CUDA;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
+  DeviceGuard guard(device);
   int num_sms = 0;
   if (cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CPALS_E_CUDA;
   ncand = (ncand <= 0 || ncand > n) ? n : ncand;

@@ -255,6 +255,23 @@ cudaError_t launch_omega_hadamard(const FactorSet& fs, int order, int mode, cons
                                   const int64_t* cols, const double* v, int64_t l, int R, double* out, int64_t sr,
                                   int64_t sj, cudaStream_t st);
 
+// Makes `dev` the current device for the scope of an entry point and restores the
+// caller's device on exit, so a call never leaves another device current.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 // Raises a kernel's dynamic shared-memory limit on the current device, once per (device,
 // kernel) per process (thread-safe).  The attribute is per device, so a process that drives
 // several GPUs sets it on each.

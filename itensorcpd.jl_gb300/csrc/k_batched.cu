@@ -583,7 +583,7 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
   *out = nullptr;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
-  cudaSetDevice(device);
+  DeviceGuard guard(device);
   cpals_batch* b = new cpals_batch();
   b->device = device;
   b->count = count;
@@ -674,14 +674,14 @@ int cpals_batch_destroy(cpals_batch* b) {
 
 int cpals_batch_set_tensors(cpals_batch* b, const float* host_concat) {
   if (!b || !host_concat) return CPALS_E_ARG;
-  cudaSetDevice(b->device);
+  DeviceGuard guard(b->device);
   CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_T, host_concat, sizeof(float) * b->tot_T, cudaMemcpyHostToDevice, b->st));
   return CPALS_OK;
 }
 
 int cpals_batch_set_factors(cpals_batch* b, const double* host_concat) {
   if (!b || !host_concat) return CPALS_E_ARG;
-  cudaSetDevice(b->device);
+  DeviceGuard guard(b->device);
   CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_F, host_concat, sizeof(double) * b->tot_F, cudaMemcpyHostToDevice, b->st));
   const int blocks = (int)std::min<int64_t>(b->count, 4096);
   k_batch_init<<<blocks, 256, 0, b->st>>>(b->d_items, (int)b->count, b->d_F, b->d_G, b->d_chk);
@@ -693,7 +693,7 @@ int cpals_batch_set_factors(cpals_batch* b, const double* host_concat) {
 
 int cpals_batch_get_factors(cpals_batch* b, double* host_concat) {
   if (!b || !host_concat) return CPALS_E_ARG;
-  cudaSetDevice(b->device);
+  DeviceGuard guard(b->device);
   CPALS_CUDA_TRY(cudaMemcpyAsync(host_concat, b->d_F, sizeof(double) * b->tot_F, cudaMemcpyDeviceToHost, b->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
   return CPALS_OK;
@@ -701,14 +701,14 @@ int cpals_batch_get_factors(cpals_batch* b, double* host_concat) {
 
 int cpals_batch_set_threads(cpals_batch* b, int threads) {
   if (!b || (threads != 128 && threads != 256 && threads != 512)) return CPALS_E_ARG;
-  cudaSetDevice(b->device);
+  DeviceGuard guard(b->device);
   return set_config(b, threads);
 }
 
 int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_out, double* fits_out,
                          int* flags_out, int64_t* launches_out) {
   if (!b || max_iter < 1 || !(tol >= 0.0)) return CPALS_E_ARG;
-  cudaSetDevice(b->device);
+  DeviceGuard guard(b->device);
   if (b->tol != tol || b->max_iter != max_iter) {
     b->tol = tol;
     b->max_iter = max_iter;
@@ -752,7 +752,7 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
 int cpals_batch_autotune(cpals_batch* b, const double* host_factors, int sweeps, int* threads_out,
                          double* ms_out) {
   if (!b || !host_factors || sweeps < 1) return CPALS_E_ARG;
-  cudaSetDevice(b->device);
+  DeviceGuard guard(b->device);
   const int cand[3] = {128, 256, 512};
   double best = 1e300;
   int best_nt = 0;

@@ -290,7 +290,9 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
   for (int i = 0; i < 4; ++i)
     if (widths[i] < 1 || widths[i] > 65536) return CPALS_E_ARG;
   *out = nullptr;
-  if (cudaSetDevice(device) != cudaSuccess) return CPALS_E_CUDA;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
+  DeviceGuard guard(device);
   cpals_mlp* m = new cpals_mlp();
   m->device = device;
   for (int i = 0; i < 4; ++i) m->w[i] = widths[i];
@@ -321,7 +323,7 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
 
 int cpals_mlp_destroy(cpals_mlp* m) {
   if (!m) return CPALS_OK;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   for (void* q : {(void*)m->p, (void*)m->g, (void*)m->m1, (void*)m->m2, (void*)m->pb, (void*)m->x, (void*)m->t,
                   (void*)m->h1, (void*)m->h2, (void*)m->y, (void*)m->dy, (void*)m->dh2, (void*)m->dh1,
                   (void*)m->xb, (void*)m->h1b, (void*)m->h2b, (void*)m->dyb, (void*)m->dh2b, (void*)m->dh1b,
@@ -337,7 +339,7 @@ int64_t cpals_mlp_num_params(cpals_mlp* m) { return m ? m->np : -1; }
 // FP32 parameters: W1 [h1][in], b1, W2 [h2][h1], b2, W3 [out][h2], b3; resets Adam.
 int cpals_mlp_set_params(cpals_mlp* m, const float* host_params) {
   if (!m || !host_params) return CPALS_E_ARG;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->p, host_params, 4 * m->np, cudaMemcpyHostToDevice, m->st));
   CPALS_CUDA_TRY(cudaMemsetAsync(m->m1, 0, 4 * m->np, m->st));
   CPALS_CUDA_TRY(cudaMemsetAsync(m->m2, 0, 4 * m->np, m->st));
@@ -349,7 +351,7 @@ int cpals_mlp_set_params(cpals_mlp* m, const float* host_params) {
 
 int cpals_mlp_get_params(cpals_mlp* m, float* host_params) {
   if (!m || !host_params) return CPALS_E_ARG;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   CPALS_CUDA_TRY(cudaMemcpyAsync(host_params, m->p, 4 * m->np, cudaMemcpyDeviceToHost, m->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));
   return CPALS_OK;
@@ -358,7 +360,7 @@ int cpals_mlp_get_params(cpals_mlp* m, float* host_params) {
 // Forward pass of B host inputs (FP32 [B][in]) into host outputs (FP32 [B][out]).
 int cpals_mlp_forward(cpals_mlp* m, const float* host_x, int B, float* host_y) {
   if (!m || !host_x || !host_y || B < 1) return CPALS_E_ARG;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   if (ensure_batch(m, B) != CPALS_OK) return CPALS_E_CUDA;
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->x, host_x, 4LL * B * m->w[0], cudaMemcpyHostToDevice, m->st));
   k_to_bf16<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->x, (int64_t)B * m->w[0], m->xb);
@@ -372,7 +374,7 @@ int cpals_mlp_forward(cpals_mlp* m, const float* host_x, int B, float* host_y) {
 int cpals_mlp_gradients(cpals_mlp* m, const float* host_x, const float* host_t, int B, float* host_grads,
                         double* loss_out) {
   if (!m || !host_x || !host_t || !host_grads || B < 1) return CPALS_E_ARG;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   if (ensure_batch(m, B) != CPALS_OK) return CPALS_E_CUDA;
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->x, host_x, 4LL * B * m->w[0], cudaMemcpyHostToDevice, m->st));
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->t, host_t, 4LL * B * m->w[3], cudaMemcpyHostToDevice, m->st));
@@ -389,7 +391,7 @@ int cpals_mlp_gradients(cpals_mlp* m, const float* host_x, const float* host_t, 
 // Device copy of a training set (FP32 inputs [N][in], targets [N][out]).
 int cpals_mlp_set_dataset(cpals_mlp* m, const float* host_x, const float* host_t, int64_t N) {
   if (!m || !host_x || !host_t || N < 1) return CPALS_E_ARG;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   cudaFree(m->dx);
   cudaFree(m->dt);
   m->dx = m->dt = nullptr;
@@ -405,7 +407,7 @@ int cpals_mlp_set_dataset(cpals_mlp* m, const float* host_x, const float* host_t
 // idx[s*B .. s*B+B-1].  losses (may be null) receives each step's mean loss.
 int cpals_mlp_train(cpals_mlp* m, const int* host_idx, int steps, int B, float lr, double* losses) {
   if (!m || !host_idx || steps < 1 || B < 1 || !m->dx) return CPALS_E_ARG;
-  cudaSetDevice(m->device);
+  DeviceGuard guard(m->device);
   if (ensure_batch(m, B) != CPALS_OK) return CPALS_E_CUDA;
   for (int64_t i = 0; i < (int64_t)steps * B; ++i)
     if (host_idx[i] < 0 || host_idx[i] >= m->dn) return CPALS_E_ARG;

@@ -197,15 +197,20 @@ extern "C" int cpals_mttkrp_fp64_noalloc(int order, const int64_t* dims, int64_t
   if (order < 2 || order > kMaxOrder || !dims || !d_factors || !d_tensor || !d_out) return CPALS_E_ARG;
   if (mode < 0 || mode >= order || rank < 1) return CPALS_E_ARG;
   if (tensor_dtype != CPALS_DTYPE_F64 && tensor_dtype != CPALS_DTYPE_F32) return CPALS_E_ARG;
+  int64_t numel = 1;
   for (int m = 0; m < order; ++m) {
     if (dims[m] < 1 || dims[m] > (int64_t(1) << 31)) return CPALS_E_ARG;
     if (m != mode && !d_factors[m]) return CPALS_E_ARG;
+    if (dims[m] > (int64_t(1) << 40) / numel) return CPALS_E_ARG;  // at most 2^40 elements
+    numel *= dims[m];
   }
   // The partial sums of one split need In * R doubles; the array must hold at least one.
-  if (dims[mode] * rank > kNoAllocScratchDoubles) {
+  // Compared by division: In * rank could overflow for a huge rank.
+  if (rank > kNoAllocScratchDoubles / dims[mode]) {
     fprintf(stderr,
-            "libcpals: cpals_mttkrp_fp64_noalloc: I_mode * rank = %lld exceeds the %lld-double scratch array\n",
-            (long long)(dims[mode] * rank), (long long)kNoAllocScratchDoubles);
+            "libcpals: cpals_mttkrp_fp64_noalloc: I_mode = %lld times rank = %lld exceeds the %lld-double scratch "
+            "array\n",
+            (long long)dims[mode], (long long)rank, (long long)kNoAllocScratchDoubles);
     return CPALS_E_ARG;
   }
   int dev = 0;

@@ -17,18 +17,21 @@
 // stored in the order the CTAs consume them.  A stage is one contiguous 32 KB bulk copy
 // and every CTA streams one contiguous region (4 bytes per element, the FP32 size).
 //
-// CTA (10 warps): warp 0 issues per stage the tile bulk copy, a TMA load of the FP32
-// factor block F_f[k0:k0+64, n0:n0+NB] (landing in the stage's B region) and bulk copies
-// of the outer factor rows; warps 2-5 turn the FP32 block, in place, into the KRP tile
-// (NB x 64, BF16 hi/lo, swizzled K-major); warp 1 issues tcgen05.mma.kind::f16
-// (M = 128, N = NB, K = 16).  The tensor core's FP32 accumulation rounds toward zero,
-// which over long chains shrinks the result (about 0.5 ulp per accumulation), so each
-// chunk accumulates into fresh, double-buffered TMEM accumulators -- Th Kh (4 steps) and
-// the small Th Kl + Tl Kh -- and warps 6-9 promote them every chunk into FP32 registers
-// with round-to-nearest adds.  The reduction range is split across CTAs; each writes
-// FP32 partials part[split][I_n][R], reduced in FP64 (in split order) by the solve
-// kernel.  Every wait is bounded: on expiry the kernel records an error code, drains
-// its own copies in flight (bounded), frees TMEM and returns.
+// CTA (6 or 10 warps).  Warp 0 is the producer: per stage it issues three kinds of
+// cp.async.bulk copies into a 2-4 stage mbarrier ring -- the 32 KB unfolding tile (hi, lo),
+// the prebuilt BF16 hi/lo factor-block tile of F_f[k0:k0+64, n0:n0+NB] (written by
+// k_build_btiles, or by the normalisation kernel when the factor is updated in a sweep) and
+// the FP32 rows of the outer factors.  Warp 1 issues tcgen05.mma.kind::f16 (M = 128, K = 16,
+// four steps per chunk): one N = 2 NB product Th [Bh | Bl] and one N = NB product Tl Bh.
+// The tensor core's FP32 accumulation rounds toward zero, which over long chains shrinks
+// the result (about 0.5 ulp per accumulation), so each chunk accumulates into fresh TMEM
+// accumulators (2 or 4 buffers), and the drain warps (4, or 8 when NB is a multiple of 64:
+// one or two per TMEM lane quarter) read them with tcgen05.ld, scale them by the product
+// of the outer rows and accumulate in FP32 registers with round-to-nearest adds.  A stage
+// is released when every drain warp has read its outer rows.  The reduction range is split
+// across CTAs; each writes FP32 partials part[split][I_n][R], reduced by the solve kernel.
+// Every wait is bounded: on expiry the kernel records an error code, drains its own copies
+// in flight (bounded), frees TMEM and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>

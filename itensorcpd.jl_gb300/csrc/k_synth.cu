@@ -69,7 +69,9 @@ int cpals_synth_lowrank(int device, int order, const int64_t* dims, int64_t rank
                         const double* host_weights, double snr_db, uint64_t seed, float* d_out) {
   if (order < 1 || order > kMaxOrder || !dims || rank < 1 || !host_factors || !host_weights || !d_out)
     return CPALS_E_ARG;
-  if (cudaSetDevice(device) != cudaSuccess) return CPALS_E_CUDA;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CPALS_E_CUDA;
+  DeviceGuard guard(device);
   SynthGeom g{};
   int64_t off = 0;
   g.numel = 1;

@@ -4,21 +4,36 @@ Compiles the reference's own sparse sign embedding generators, src/algebra/spars
 src/algebra/sparsestack.c of ITensorCPD.jl, from the reference checkout where it lies, into
 oracle/_ref/libsparse_sign.so, with the reference's own compile line (deps/build.jl:15-17:
 gcc -O3 -fPIC -shared).  Only the tests load it, to pin the structural rules the device
-generator follows.  Without the checkout (as on a GPU machine) nothing is built.
+generator follows.
+
+The checkout is the directory named by the environment variable ITENSORCPD_REFERENCE (or the
+``--reference DIR`` argument), else a checkout called ``reference`` beside this repository.
+Without a checkout nothing is built.
 """
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 from pathlib import Path
 
-REF_SRC = Path("/root/reference/src/algebra")
 OUT_DIR = Path(__file__).resolve().parent / "_ref"
 SOURCES = ("sparse_sign.c", "sparsestack.c")
 
 
-def build() -> Path | None:
-    srcs = [REF_SRC / f for f in SOURCES]
+def reference_dir(explicit: str | None = None) -> Path:
+    """The reference checkout: the argument, else $ITENSORCPD_REFERENCE, else ../reference."""
+    if explicit:
+        return Path(explicit)
+    env = os.environ.get("ITENSORCPD_REFERENCE")
+    if env:
+        return Path(env)
+    return Path(__file__).resolve().parent.parent.parent / "reference"
+
+
+def build(reference: str | None = None) -> Path | None:
+    src_dir = reference_dir(reference) / "src" / "algebra"
+    srcs = [src_dir / f for f in SOURCES]
     if not all(p.exists() for p in srcs) or shutil.which("gcc") is None:
         return None
     OUT_DIR.mkdir(exist_ok=True)
@@ -30,4 +45,7 @@ def build() -> Path | None:
 
 
 if __name__ == "__main__":
-    print(build())
+    import sys
+
+    ref = sys.argv[sys.argv.index("--reference") + 1] if "--reference" in sys.argv else None
+    print(build(ref))

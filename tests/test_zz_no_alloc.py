@@ -51,9 +51,16 @@ def _noalloc(lib, torch, T, F, mode, R):
     return out.cpu().numpy().reshape(T.shape[mode], R, order="F")
 
 
-@pytest.mark.parametrize("dims,R,dt", [((37, 45, 29), 20, np.float64), ((64, 70, 33, 5), 48, np.float32),
-                                       ((100, 100, 100), 50, np.float64)])
-def test_noalloc_matches_handle_mttkrp_on_two_calls(pkg, lib, dims, R, dt):
+# (40000, 6, 5) at rank 52: mode 0 needs I_0 * R = 2,080,000 of the array's 2,097,152 doubles,
+# so one split's partial sums nearly fill it.  (The entry point also lowers the split count
+# when several splits would not fit; with GB300's 152 SMs its split rule never asks for more
+# than fit, so that branch only runs on GPUs with far more SMs.)
+CASES = [((37, 45, 29), 20, np.float64), ((64, 70, 33, 5), 48, np.float32), ((100, 100, 100), 50, np.float64),
+         ((40000, 6, 5), 52, np.float64)]
+
+
+@pytest.mark.parametrize("dims,R,dt", CASES)
+def test_noalloc_matches_handle_mttkrp_on_two_calls(pkg, lib, oracle, dims, R, dt):
     torch = pytest.importorskip("torch")
     T = np.asfortranarray(det_normal(5 + R, dims).astype(dt))
     F, lam = det_factors(dims, R, seed=R)
@@ -65,6 +72,9 @@ def test_noalloc_matches_handle_mttkrp_on_two_calls(pkg, lib, dims, R, dt):
         for n in range(len(dims)):
             got = _noalloc(lib, torch, T, F, n, R)
             assert rel(got, ref[n]) <= TOL, (call, n, rel(got, ref[n]))
+            # and directly against the oracle's explicit Khatri-Rao GEMM
+            want = oracle.mttkrp_krp(T.astype(np.float64), F, n)
+            assert rel(got, want) <= TOL, (call, n, rel(got, want))
 
 
 def test_noalloc_rejects_sizes_beyond_the_array(lib):
@@ -77,4 +87,11 @@ def test_noalloc_rejects_sizes_beyond_the_array(lib):
     ptrs[1] = p
     ptrs[2] = p
     st = lib.cpals_mttkrp_fp64_noalloc(3, L.i64ptr(dims), 64, 0, L.DTYPE_F64, C.c_void_p(1), ptrs, p, None)
+    assert st == L.CPALS_E_ARG
+    # a rank so large that I_0 * rank would overflow 64 bits is rejected as well
+    st = lib.cpals_mttkrp_fp64_noalloc(3, L.i64ptr(dims), 1 << 62, 0, L.DTYPE_F64, C.c_void_p(1), ptrs, p, None)
+    assert st == L.CPALS_E_ARG
+    # as is a tensor of more than 2^40 elements
+    big = np.asarray((1 << 21, 1 << 20, 2), dtype=np.int64)
+    st = lib.cpals_mttkrp_fp64_noalloc(3, L.i64ptr(big), 1, 2, L.DTYPE_F64, C.c_void_p(1), ptrs, p, None)
     assert st == L.CPALS_E_ARG

@@ -256,19 +256,22 @@ ORACLE_PARITY_SWEEPS = 3
 
 
 def oracle_parity(T, ref_norm, F0, lam0, gpu_trajs, sweeps=ORACLE_PARITY_SWEEPS):
-    """Fit trajectory of the oracle (FP64 KRP-free ALS, the reference's default algorithm,
-    optimize.jl:15-32 with FitCheck's fit, fit_check.jl:24-32) over the first `sweeps`
-    sweeps from F0, lam0, and the largest per-sweep difference of each GPU trajectory."""
+    """Fit trajectory of the oracle (FP64 normal-equation ALS, optimize.jl:15-32, with the
+    MTTKRP as KRPNormal forms it, standard/tensor.jl:12-20, and FitCheck's fit,
+    fit_check.jl:24-32) over the first `sweeps` sweeps from F0, lam0, and the largest per-sweep
+    difference of each GPU trajectory.  (KRPFreeNormal computes the same MTTKRP in another
+    order; on the host it streams the tensor once per rank column, some 100x slower here.)"""
     sys.path.insert(0, str(ROOT / "oracle"))
     import cpals_oracle as oracle  # the checker
 
     chk = oracle.FitCheck(0.0, sweeps, ref_norm)
     t0 = time.perf_counter()
-    oracle.als_optimize(T, F0, lam0, check=chk, alg="krp_free", work_dtype=np.float64)
+    oracle.als_optimize(np.asarray(T, dtype=np.float64), F0, lam0, check=chk, alg="krp", work_dtype=np.float64)
     dt = time.perf_counter() - t0
     ref = np.asarray(chk.trajectory[:sweeps], dtype=np.float64)
     out = {"sweeps": int(ref.size), "oracle_fits": [float(x) for x in ref], "oracle_s": dt,
-           "oracle": "FP64 KRP-free normal-equation ALS (numpy), same tensor and start"}
+           "oracle": "FP64 normal-equation ALS with the explicit Khatri-Rao MTTKRP (numpy/OpenBLAS), same "
+                     "tensor and start"}
     for name, tr in gpu_trajs.items():
         g = np.asarray(tr[:ref.size], dtype=np.float64)
         out[f"{name}_max_abs"] = float(np.max(np.abs(g - ref)))
@@ -331,27 +334,102 @@ def run_c3(args, pkg, L, device):
     for key, passes in (("dimtree", 2), ("plain", 4)):
         out[key]["tensor_passes_per_sweep"] = passes
         out[key]["alg_bytes_per_sweep_gb"] = passes * tbytes / 1e9
-    # randomized ALS: 16384 samples per mode, one sweep = four sampled solves
-    api = pkg.api
-    cp = pkg.CPD([f.copy() for f in F0], lam0.copy())
+        out[key]["sweep_gbs"] = passes * tbytes * out[key]["sweeps_per_s"] / 1e9
+    # roofline of the full MTTKRP launch (k_mttkrp_tc, N block 128): the plain engine launches
+    # one per mode; CUDA events around every launch in profiling mode
+    peak, peak_kind = load_peaks()
+    mt_s = out["plain"]["mttkrp_ms_per_mode_avg"] / 1e3
+    alg_bytes = float(np.mean([mttkrp_alg_bytes(C3_DIMS, C3_RANK, n) for n in range(4)]))
+    achieved = alg_bytes / mt_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": peak_kind, "kernel": "k_mttkrp_tc<128> (one full pass of T)",
+                "alg_bytes_per_launch": alg_bytes, "avg_launch_us": mt_s * 1e6,
+                "tflops_3_products": 3 * 2.0 * np.prod(C3_DIMS) * C3_RANK / mt_s / 1e12}
+    # end to end through the public API: the pinned host tensor copied in (with the tile
+    # streams rebuilt), C3_SWEEPS dimension-tree sweeps, factors copied out, every step
+    with pkg.Engine(C3_DIMS, C3_RANK, dtype=np.float32, precision="bf16x3", device=device, dimtree=True) as e:
+        def e2e_step():
+            e.set_tensor(T_host)
+            e.set_factors(F0, lam0)
+            e.optimize(nocheck(C3_SWEEPS))
+            return e.get_factors()
+
+        e2e_step()
+        e.synchronize()
+        e.timer_start()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_ms = e.timer_stop()
+    fac_bytes = sum(d * C3_RANK * 8 for d in C3_DIMS) + C3_RANK * 8
+    e2e = {"value": args.steps * C3_SWEEPS / (e2e_ms / 1e3), "unit": "sweeps/s",
+           "h2d_bytes_per_step": int(T_host.nbytes + fac_bytes), "d2h_bytes_per_step": int(fac_bytes)}
+    # randomized ALS, device-timed: 16384 leverage-score samples per mode drawn on the host
+    # (probability.jl:23-33), each mode's gathers and sampled solve timed by CUDA events on the
+    # engine's stream; the tensor stays resident
+    nsamps, nrand = 16384, 3
+    alg = pkg.LevScoreSampled(nsamps)
+    rng7 = np.random.default_rng(7)
+    with pkg.Engine(C3_DIMS, C3_RANK, dtype=np.float32, precision="fp64", device=device) as e:
+        e.set_tensor(T_host)
+        e.set_factors(F0, lam0)
+        probs = [e.leverage_scores(n) for n in range(4)]
+
+        def sampled_sweep():
+            for n in range(4):
+                e.sampled_update(n, alg.sample(n, probs, rng7))
+                probs[n] = e.leverage_scores(n)
+
+        sampled_sweep()  # warm-up: buffers sized, kernels loaded
+        e.set_profiling(True)
+        t0 = time.perf_counter()
+        for _ in range(nrand):
+            sampled_sweep()
+        wall = time.perf_counter() - t0
+        upd_ms, gat_ms, nupd = e.profile_read_sampled()
+        e.set_profiling(False)
+    gbytes = nsamps * C3_DIMS[0] * 4 + nsamps * C3_RANK * 8 + nsamps * 3 * 8  # per update
+    out["randomized"] = {
+        "samples_per_mode": nsamps, "sweeps": nrand, "updates_timed": nupd,
+        "device_sweeps_per_s": nrand / (upd_ms / 1e3), "device_ms_per_update": upd_ms / max(1, nupd),
+        "gather_us_per_update": 1e3 * gat_ms / max(1, nupd),
+        "gather_gbs": gbytes * nupd / (gat_ms / 1e3) / 1e9, "gather_bytes_per_update": gbytes,
+        "host_wall_sweeps_per_s": nrand / wall,
+        "note": "device figures: CUDA events from the pivot upload to the new factor of every mode "
+                "update; the leverage probabilities (a thin QR per mode, probability.jl:3-10) and the host "
+                "draws are outside them and inside the host-wall figure.  Gather bytes: sampled fibres "
+                "(FP32) and Khatri-Rao rows (FP64) written, plus the indices."}
+    # CPU baselines: the oracle's KRP-free MTTKRP (the reference default, standard/tensor.jl:32-44)
+    # on the full tensor for 16 of the 128 rank columns of mode 0, scaled to a sweep (4 modes x
+    # 128 columns; the solves are negligible); and one sampled sweep of the oracle
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cpals_oracle as oracle
+
+    ncols = 16
+    Fs = [f[:, :ncols].astype(np.float32) for f in F0]
     t0 = time.perf_counter()
-    api.als_optimize(T_host, cp, alg=pkg.LevScoreSampled(16384), check=pkg.NoCheck(1), device=device,
-                     rng=np.random.default_rng(7))
-    t_first = time.perf_counter() - t0
+    oracle.mttkrp_krp_free(T_host, Fs, 0)
+    cpu_s = (time.perf_counter() - t0) * (C3_RANK / ncols) * 4
+    cpu = {"value": 1.0 / cpu_s, "unit": "sweeps/s", "cores": os.cpu_count() or 1, "kind": "port",
+           "sample": f"KRP-free MTTKRP of mode 0 for {ncols} of {C3_RANK} rank columns on the full 128^4 FP32 "
+                     f"tensor (numpy/OpenBLAS, all host threads), scaled by {C3_RANK // ncols} x 4 modes"}
+    Fo = [f.copy() for f in F0]
     t0 = time.perf_counter()
-    nrand = 3
-    res = api.als_optimize(T_host, cp, alg=pkg.LevScoreSampled(16384), check=pkg.NoCheck(nrand), device=device,
-                           rng=np.random.default_rng(7))
-    t_rand = time.perf_counter() - t0
-    out["randomized"] = {"samples_per_mode": 16384, "sweeps_per_s": nrand / t_rand,
-                         "note": "host wall clock through the Python API, including host sampling and tensor "
-                                 "upload per call; first call (with setup) took %.3f s" % t_first}
+    oracle.lev_score_als(T_host, Fo, lam0.copy(), nsamps, 1, np.random.default_rng(7))
+    out["randomized"]["cpu_baseline"] = {"value": 1.0 / (time.perf_counter() - t0), "unit": "sweeps/s",
+                                         "cores": os.cpu_count() or 1, "kind": "port",
+                                         "sample": "one LevScoreSampled sweep of the oracle (numpy gathers "
+                                                   "and solves, 16384 samples per mode)"}
     line = {
         "metric": "cp_als_sweeps_per_s", "value": out["dimtree"]["sweeps_per_s"], "unit": "sweeps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16x3/f32-accumulate mttkrp, f64 solve", "data": "synthetic",
         "config": {"workload": "cpals_128x128x128x128_fp32_rank128_lowrank_noise_30dB_dimtree", "dims": list(C3_DIMS),
-                   "rank": C3_RANK, "congruence": 0.3, "snr_db": 30.0, "sweeps_per_step": C3_SWEEPS},
+                   "rank": C3_RANK, "congruence": 0.3, "snr_db": 30.0, "sweeps_per_step": C3_SWEEPS,
+                   "l2": "inputs larger than L2 (tensor 1.07 GB)"},
+        "roofline": roofline,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": out["dimtree"]["gpu_launches"],
         "c3": out,
         "speedup_dimtree_vs_plain": out["dimtree"]["sweeps_per_s"] / out["plain"]["sweeps_per_s"],
         "speedup_dimtree_vs_fp64_gpu": out["dimtree"]["sweeps_per_s"] / out["fp64_gpu"]["sweeps_per_s"],
@@ -435,9 +513,14 @@ def run_c4(args, pkg, device):
         lams.append(lam)
         norms.append(float(np.linalg.norm(T.astype(np.float64))))
     elems = sum(int(np.prod(d)) for d in dims)
+    # the tensors concatenated once into pinned host memory (the e2e leg copies them in every step)
+    cat, keep = pinned_like((elems,))
+    off = 0
+    for T in Ts:
+        cat[off:off + T.size] = np.asarray(T, dtype=np.float32).reshape(-1, order="F")
+        off += T.size
     with pkg.BatchEngine(dims, ranks, norms, device=device) as be:
-        t0 = time.perf_counter()
-        be.set_tensors(Ts)
+        be.set_tensors_concat(cat)
         nt, tune_ms = be.autotune(Fs, lams, sweeps=2)
         runs = []
         for _ in range(max(1, args.steps)):
@@ -446,6 +529,47 @@ def run_c4(args, pkg, device):
             sweeps, fits, flags, launches = be.optimize(tol=1e-5, max_iter=200)
             runs.append(time.perf_counter() - t1)
         total_s = float(np.median(runs))
+        # end to end through the public API: tensors in, initial factors in, solve, factors out
+        e2e_runs = []
+        for _ in range(max(1, args.steps)):
+            t1 = time.perf_counter()
+            be.set_tensors_concat(cat)
+            be.set_factors(Fs, lams)
+            be.optimize(tol=1e-5, max_iter=200)
+            be.get_factors()
+            e2e_runs.append(time.perf_counter() - t1)
+        e2e_s = float(np.median(e2e_runs))
+    fac_bytes = 8 * sum((sum(d) + 1) * R for d, R in zip(dims, ranks))
+    # algorithmic HBM bytes of the whole job: each sweep of a tensor streams it three times (one
+    # MTTKRP per mode) and reads and writes its factors
+    alg_bytes = float(sum(int(sw) * (3 * 4 * int(np.prod(d)) + 2 * 8 * (sum(d) + 1) * R)
+                          for sw, d, R in zip(sweeps, dims, ranks)))
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / total_s / 1e9
+    # baselines on a bounded subset (the first 64 tensors): a host loop of the single-tensor
+    # GPU engine (decompose per tensor, src/decompose.jl:1-30, FitCheck(1e-5, 200)), and the
+    # CPU oracle (KRP-free normal-equation ALS, the reference default) on the first 16
+    sub = min(64, count)
+    t1 = time.perf_counter()
+    for t in range(sub):
+        with pkg.Engine(dims[t], ranks[t], dtype=np.float32, precision="fp64", device=device) as e:
+            e.set_tensor(Ts[t])
+            e.set_factors(Fs[t], lams[t])
+            c = pkg._lib.CpalsCheck()
+            c.kind, c.tolerance, c.max_counter, c.ref_norm, c.lastfit = pkg._lib.CHECK_FIT, 1e-5, 200, norms[t], 1.0
+            e.optimize(c)
+            e.get_factors()
+    loop_s = time.perf_counter() - t1
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cpals_oracle as oracle
+
+    csub = min(16, count)
+    t1 = time.perf_counter()
+    for t in range(csub):
+        oracle.als_optimize(Ts[t], Fs[t], lams[t], check=oracle.FitCheck(1e-5, 200, norms[t]), alg="krp_free",
+                            work_dtype=np.float32)
+    cpu_s = time.perf_counter() - t1
+    del keep
     line = {
         "metric": "batched_cp_als_solves_per_s", "value": count / total_s, "unit": "solves/s", "n_gpus": 1,
         "steps": max(1, args.steps), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -456,6 +580,17 @@ def run_c4(args, pkg, device):
         "sweeps": {"p50": float(np.percentile(sweeps, 50)), "p99": float(np.percentile(sweeps, 99)),
                    "max": int(sweeps.max()), "mean": float(sweeps.mean())},
         "sweep_launches": launches // 2, "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_kind,
+                     "kernel": "k_batch_sweep (whole job: every sweep streams each tensor 3 times)"},
+        "e2e": {"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(4 * elems + fac_bytes),
+                "d2h_bytes_per_step": int(fac_bytes)},
+        "cpu_baseline": {"value": csub / cpu_s, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"the oracle's KRP-free ALS with FitCheck(1e-5, 200) on the first {csub} "
+                                   "tensors, one after another (numpy/OpenBLAS, all host threads)"},
+        "gpu_loop_baseline": {"value": sub / loop_s, "unit": "solves/s", "tensors": sub,
+                              "what": "a host loop of the single-tensor engine (FP64 MTTKRP, FitCheck(1e-5, 200)): "
+                                      "handle, tensor upload, solve, factors out, per tensor"},
         "autotune": {"threads": nt, "ms_per_2_sweeps": {str(k): float(v) for k, v in tune_ms.items()}},
         "stopped_by_fitcheck": int(np.sum((flags & 4) != 0) - np.sum(sweeps >= 200)),
         "hit_200_sweeps": int(np.sum(sweeps >= 200)), "nan": int(np.sum(flags & 1)),

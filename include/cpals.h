@@ -129,13 +129,34 @@ int cpals_mttkrp(cpals_ctx* ctx, int mode, double* host_out);
  * Returns CPALS_E_NAN if a FitCheck fit became NaN (fit_check.jl:41). */
 int cpals_optimize(cpals_ctx* ctx, cpals_check* check, double* fit_trajectory, int64_t traj_capacity);
 
-/* One check_converge call of a CPDiffCheck / CPAngleCheck on the handle's current
- * factors and lambda (cp_diff_check.jl:20-68, cp_angle_check.jl:20-68), for loops that
- * update the factors themselves, such as the sampled solvers' loop
- * (ProjectionAlgorithm.jl:15-54 passes these checks through).  *converged receives the
- * check's return value and *value (may be NULL) the fit (angle) it computed, NaN when
- * it only stored the iterate. */
+/* One mode of an ALS sweep on the device, for a sweep loop the caller drives (optimize,
+ * src/optimizers/als_optimizers/optimize.jl:19-27): compute_krp (the Hadamard product of the
+ * other modes' Grams, MttkrpAlgorithm.jl:18-31), matricize_tensor (the MTTKRP,
+ * standard/tensor.jl:12-44), solve_ls_problem (MttkrpAlgorithm.jl:34-41, ldiv_solve.jl:4-29),
+ * row_norm (row_norm.jl:4-24) and post_solve (standard/tensor.jl:22-25, 46-49).  M_n stays on
+ * the device.  On the last mode the terms of the fit are saved for cpals_check_converge, as
+ * save_mttkrp does (MttkrpAlgorithm.jl:5-14, fit_check.jl:22).  host_solution (may be NULL)
+ * receives the solve's result before normalisation, X = F_n diag(lambda), I_n x R
+ * column-major, for a caller that keeps its own copy of the factors; with NULL the call
+ * returns once the work is enqueued.  `order` calls (modes 0..order-1) followed by
+ * cpals_check_converge equal one sweep of cpals_optimize bit for bit. */
+int cpals_mode_update(cpals_ctx* ctx, int mode, double* host_solution);
+
+/* One check_converge call on the handle's current state (MttkrpAlgorithm.jl:5-14), for
+ * loops that update the factors themselves.  FitCheck / NoCheck (fit_check.jl:24-66,
+ * no_check.jl:11-20): the fit from the terms the last cpals_mode_update of the last mode
+ * saved (CPALS_E_STATE when there is none newer than the last check); CPALS_E_NAN when a
+ * FitCheck fit is NaN.  CPDiffCheck / CPAngleCheck (cp_diff_check.jl:20-68,
+ * cp_angle_check.jl:20-68): on the handle's current factors and lambda, as the sampled
+ * solvers' loop needs (ProjectionAlgorithm.jl:15-54 passes these checks through).
+ * *converged receives the check's return value and *value (may be NULL) the fit (angle)
+ * it computed, NaN when it only stored the iterate. */
 int cpals_check_converge(cpals_ctx* ctx, cpals_check* check, int* converged, double* value);
+
+/* norm(T) of the handle's tensor, from ||T||^2 computed on the device as a double-double
+ * when the tensor was set (what FitCheck's ref_norm is given, fit_check.jl:14-19).  norm2
+ * (may be NULL, 2 entries) receives ||T||^2 as hi + lo.  CPALS_E_NAN for a non-finite tensor. */
+int cpals_tensor_norm(cpals_ctx* ctx, double* norm, double* norm2);
 /* The previous iterate held for CPDiffCheck / CPAngleCheck (PrevCP): factors I_n x R
  * column-major and lambda.  get returns CPALS_E_STATE when none is held; set makes the
  * handle hold the given one. */
@@ -239,6 +260,10 @@ int cpals_timer_stop(cpals_ctx* ctx, double* elapsed_ms);
  * kernel time and the number of timed launches since profiling was switched on. */
 int cpals_set_profiling(cpals_ctx* ctx, int on);
 int cpals_profile_read(cpals_ctx* ctx, double* mttkrp_ms, int64_t* launches);
+/* In profiling mode every cpals_sampled_update also records CUDA events: *update_ms receives
+ * the summed device time of the updates (pivot upload to the new factor), *gather_ms that of
+ * their two gathers (sampled KRP rows and fibres), *updates how many were timed. */
+int cpals_profile_read_sampled(cpals_ctx* ctx, double* update_ms, double* gather_ms, int64_t* updates);
 /* Kernel launches enqueued by this handle so far (every libcpals kernel). */
 int cpals_launch_count(cpals_ctx* ctx, int64_t* launches);
 

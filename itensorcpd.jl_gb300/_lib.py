@@ -92,6 +92,9 @@ SIGNATURES = {
     "cpals_launch_count": (C.c_int, [_P, _I64P]),
     "cpals_mttkrp_fp64_noalloc": (C.c_int, [C.c_int, _I64P, C.c_int64, C.c_int, C.c_int, _P, C.POINTER(_DP), _DP,
                                             _P]),
+    "cpals_mode_update": (C.c_int, [_P, C.c_int, _DP]),
+    "cpals_profile_read_sampled": (C.c_int, [_P, _DP, _DP, _I64P]),
+    "cpals_tensor_norm": (C.c_int, [_P, _DP, _DP]),
     "cpals_pivot_hadamard": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _DP]),
     "cpals_fused_flatten_sample": (C.c_int, [_P, C.c_int, _I64P, C.c_int64, _P]),
     "cpals_leverage_scores": (C.c_int, [_P, C.c_int, _DP]),

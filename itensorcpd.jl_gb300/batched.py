@@ -56,6 +56,13 @@ class BatchEngine:
 
     def set_tensors(self, tensors):
         buf = np.concatenate([np.asarray(T, dtype=np.float32).reshape(-1, order="F") for T in tensors])
+        self.set_tensors_concat(buf)
+
+    def set_tensors_concat(self, buf):
+        """The tensors already concatenated column-major in one FP32 host buffer (pinned for
+        the fastest copy)."""
+        if buf.dtype != np.float32 or not buf.flags.c_contiguous:
+            raise TypeError("expected one contiguous float32 buffer")
         L.check(self.lib.cpals_batch_set_tensors(self.h, buf.ctypes.data_as(C.POINTER(C.c_float))),
                 "cpals_batch_set_tensors")
         self._tensors_keep = buf

@@ -53,7 +53,8 @@ struct cpals_ctx {
   double* rgpart = nullptr;  // the solve blocks' partial Grams (null: the tiled Gram kernel)
   unsigned* gcnt = nullptr;
   int gS2[kMaxOrder] = {};
-  double* inner_rows = nullptr;
+  double* inner_rows = nullptr;  // two doubles (a double-double) per row
+  double* nrm = nullptr;         // scratch of the ||T||^2 kernels
   DevCheck* chk = nullptr;
   DevCheck* hchk = nullptr;  // pinned mirror
   double* traj = nullptr;
@@ -79,6 +80,8 @@ struct cpals_ctx {
   bool profiling = false;
   std::vector<cudaEvent_t> prof_ev;  // pairs
   int64_t prof_used = 0;
+  std::vector<cudaEvent_t> samp_ev;  // per sampled update: start, gathers start, gathers end, end
+  int64_t samp_used = 0;
   int64_t launches = 0;
   int64_t sweep_launches = 0;  // kernel launches of one sweep (set when the graph is built)
   // CPDiffCheck / CPAngleCheck: two previous-iterate buffers, the split cross Grams, the
@@ -208,11 +211,15 @@ CrossArgs cross_args(const cpals_ctx* c) {
 
 bool is_cross_kind(int kind) { return kind == CPALS_CHECK_DIFF || kind == CPALS_CHECK_ANGLE; }
 
-int enqueue_sweep(cpals_ctx* c) {
+// One mode of the sweep: compute_krp, matricize_tensor, solve_ls_problem, row_norm and
+// post_solve of optimize (optimize.jl:19-27).  On the last mode the fit's terms are saved in
+// the device check; run_check = 1 also runs the check's update there (the fused sweep),
+// run_check = 0 leaves it to launch_check_step (a caller-driven sweep).
+int enqueue_mode(cpals_ctx* c, int n, int run_check) {
   const int N = c->order;
   const int R = (int)c->R;
   const GramSet gs = gram_set(c);
-  for (int n = 0; n < N; ++n) {
+  {
     const int last = (n == N - 1);
     const int64_t In = c->dims[n];
     CPALS_CUDA_TRY(cudaEventRecord(c->ev_main[n], c->st));
@@ -248,16 +255,25 @@ int enqueue_sweep(cpals_ctx* c) {
     if (rg)
       CPALS_CUDA_TRY(launch_gram_rows(rg, solve_blocks(In, R), R, c->gcnt + gram_tiles(R), c->Graw, c->lam,
                                       c->lam_inv, c->G[n], gs, N, last, c->inner_rows, In, c->chk, c->traj,
-                                      c->traj_cap, c->st));
+                                      c->traj_cap, c->st, run_check));
     else
       CPALS_CUDA_TRY(launch_gram_finalize(c->X, In, R, c->gS2[n], c->gpart, c->gcnt, c->Graw, c->lam, c->lam_inv,
-                                          c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st));
+                                          c->G[n], gs, N, last, c->inner_rows, c->chk, c->traj, c->traj_cap, c->st,
+                                          run_check));
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
     // the BF16 factor tiles the tensor-core MTTKRP reads are written by the same kernel
     const BtileDesc btd = c->tc ? tc_btile_desc(c->tc, n) : c->dt ? dt_btile_desc(c->dt, n) : BtileDesc{nullptr, 0, 0};
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32r[n], c->rpad,
                                     c->Graw, c->G[n], last ? nullptr : c->chk, c->st, btd, c->F32lo[n]));
+  }
+  return CPALS_OK;
+}
+
+int enqueue_sweep(cpals_ctx* c) {
+  for (int n = 0; n < c->order; ++n) {
+    const int rc = enqueue_mode(c, n, 1);
+    if (rc != CPALS_OK) return rc;
   }
   if (c->cross_on) {  // check_converge of a CPDiffCheck / CPAngleCheck on the new iterate
     CPALS_CUDA_TRY(launch_cp_check(cross_args(c), c->st));
@@ -429,6 +445,7 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->rgpart);
   cudaFree(c->gcnt);
   cudaFree(c->inner_rows);
+  cudaFree(c->nrm);
   cudaFree(c->chk);
   if (c->hchk) cudaFreeHost(c->hchk);
   cudaFree(c->traj);
@@ -448,6 +465,7 @@ int cpals_destroy(cpals_ctx* c) {
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
   for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->samp_ev) cudaEventDestroy(e);
   if (c->st) cudaStreamDestroy(c->st);
   if (c->side) cudaStreamDestroy(c->side);
   delete c;
@@ -573,17 +591,17 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   CK(dmalloc(&c->piv, R));
   CK(dmalloc(&c->W, (size_t)R * R));
   CK(dmalloc(&c->info, 1));
-  CK(dmalloc(&c->gpart, (size_t)gram_tiles((int)R) * (maxS2 * 256 + 1)));
+  CK(dmalloc(&c->gpart, gram_finalize_part_doubles(maxS2, (int)R)));
   CK(dmalloc(&c->gcnt, gram_tiles((int)R) + 1));
   {
     // partial Grams of the solve blocks, when they stay small (16M doubles)
-    const size_t T = (size_t)R * (R + 1) / 2;
     size_t need = 0;
-    for (int m = 0; m < order; ++m) need = std::max(need, (size_t)solve_blocks(dims[m], (int)R) * T + (T + 31) / 32);
+    for (int m = 0; m < order; ++m) need = std::max(need, gram_rows_part_doubles(solve_blocks(dims[m], (int)R), (int)R));
     if (need <= (size_t(1) << 24)) CK(dmalloc(&c->rgpart, need));
   }
   CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * (gram_tiles((int)R) + 1)));
-  CK(dmalloc(&c->inner_rows, maxI));
+  CK(dmalloc(&c->inner_rows, 2 * maxI));
+  CK(dmalloc(&c->nrm, norm2_scratch_doubles()));
   CK(dmalloc(&c->chk, 1));
   CPALS_CUDA_TRY(cudaMemset(c->chk, 0, sizeof(DevCheck)));
   CK(dmalloc(&c->derr, 1));
@@ -601,6 +619,9 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
 static int after_tensor_set(cpals_ctx* c) {
   c->T_set = true;
   invalidate_graph(c);
+  // ||T||^2 as a double-double, for the compensated fit
+  CPALS_CUDA_TRY(launch_tensor_norm2(c->dT, c->tdtype, c->numel, c->nrm, c->chk, c->num_sms, c->st));
+  c->launches += (c->tdtype == CPALS_DTYPE_F32) ? 3 : 2;
   if (c->tc) {
     int rc = tc_set_tensor(c->tc, c->dT, c->st);
     if (rc != CPALS_OK) return rc;
@@ -727,6 +748,48 @@ int cpals_mttkrp(cpals_ctx* c, int mode, double* host_out) {
   return check_tc_err(c);
 }
 
+int cpals_mode_update(cpals_ctx* c, int mode, double* host_solution) {
+  if (!c || mode < 0 || mode >= c->order) return CPALS_E_ARG;
+  if (!c->T_set || !c->F_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  // A converged cpals_optimize leaves `done` set, which makes the sweep kernels return at
+  // once; a caller-driven sweep has no such stop.
+  CPALS_CUDA_TRY(cudaMemsetAsync(&c->chk->done, 0, sizeof(int), c->st));
+  int rc = enqueue_mode(c, mode, 0);
+  if (rc != CPALS_OK) return rc;
+  if (host_solution) {
+    const int64_t In = c->dims[mode];
+    std::vector<double> tmp((size_t)In * c->R);
+    CPALS_CUDA_TRY(cudaMemcpyAsync(tmp.data(), c->X, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+    rowmajor_to_colmajor_host(tmp.data(), In, c->R, host_solution);
+    return check_tc_err(c);
+  }
+  return CPALS_OK;
+}
+
+int cpals_tensor_norm(cpals_ctx* c, double* norm, double* norm2) {
+  if (!c || !norm) return CPALS_E_ARG;
+  if (!c->T_set) return CPALS_E_STATE;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  const DevCheck& h = *c->hchk;
+  if (!h.t2_valid) return CPALS_E_NAN;
+  // sqrt of the double-double with one Newton correction
+  double r = std::sqrt(h.t2_hi);
+  if (r > 0.0) {
+    const double rr = r * r, rre = std::fma(r, r, -rr);
+    r += (((h.t2_hi - rr) - rre) + h.t2_lo) / (2.0 * r);
+  }
+  *norm = r;
+  if (norm2) {
+    norm2[0] = h.t2_hi;
+    norm2[1] = h.t2_lo;
+  }
+  return CPALS_OK;
+}
+
 int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int64_t traj_capacity) {
   if (!c || !check) return CPALS_E_ARG;
   if (check->kind != CPALS_CHECK_NONE && check->kind != CPALS_CHECK_FIT && !is_cross_kind(check->kind))
@@ -812,14 +875,18 @@ int cpals_optimize(cpals_ctx* c, cpals_check* check, double* fit_trajectory, int
 }
 
 int cpals_check_converge(cpals_ctx* c, cpals_check* check, int* converged, double* value) {
-  if (!c || !check || !converged || !is_cross_kind(check->kind) || check->max_counter < 0) return CPALS_E_ARG;
+  if (!c || !check || !converged || check->max_counter < 0) return CPALS_E_ARG;
+  const bool cross = is_cross_kind(check->kind);
+  if (!cross && check->kind != CPALS_CHECK_FIT && check->kind != CPALS_CHECK_NONE) return CPALS_E_ARG;
   if (!c->F_set) return CPALS_E_STATE;
-  if (check->has_prev && !c->prev_valid) return CPALS_E_STATE;
+  if (cross && check->has_prev && !c->prev_valid) return CPALS_E_STATE;
   DeviceGuard g(c->device);
-  if (ensure_traj(c, 1) != CPALS_OK || ensure_cross(c) != CPALS_OK) return CPALS_E_CUDA;
+  if (ensure_traj(c, 1) != CPALS_OK || (cross && ensure_cross(c) != CPALS_OK)) return CPALS_E_CUDA;
   CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
   DevCheck& h = *c->hchk;
+  // FitCheck / NoCheck read the terms the last mode's cpals_mode_update saved
+  if (!cross && !h.terms_ready) return CPALS_E_STATE;
   h.kind = check->kind;
   h.iter = check->iter;
   h.counter = check->counter;
@@ -835,8 +902,13 @@ int cpals_check_converge(cpals_ctx* c, cpals_check* check, int* converged, doubl
   h.nan_flag = 0;
   h.sweeps = 0;
   CPALS_CUDA_TRY(cudaMemcpyAsync(c->chk, c->hchk, sizeof(DevCheck), cudaMemcpyHostToDevice, c->st));
-  CPALS_CUDA_TRY(launch_cp_check(cross_args(c), c->st));
-  c->launches += 2;
+  if (cross) {
+    CPALS_CUDA_TRY(launch_cp_check(cross_args(c), c->st));
+    c->launches += 2;
+  } else {
+    CPALS_CUDA_TRY(launch_check_step(c->chk, c->traj, c->traj_cap, c->st));
+    c->launches += 1;
+  }
   CPALS_CUDA_TRY(cudaMemcpyAsync(c->hchk, c->chk, sizeof(DevCheck), cudaMemcpyDeviceToHost, c->st));
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
   check->iter = h.iter;
@@ -844,15 +916,18 @@ int cpals_check_converge(cpals_ctx* c, cpals_check* check, int* converged, doubl
   check->lastfit = h.lastfit;
   check->final_fit = h.final_fit;
   check->total_iter = h.total_iter;
-  check->norm_prev = h.norm_prev;
-  check->has_prev = h.has_prev;
   check->sweeps_run = 0;
-  c->prev_valid = h.has_prev != 0;
+  if (cross) {
+    check->norm_prev = h.norm_prev;
+    check->has_prev = h.has_prev;
+    c->prev_valid = h.has_prev != 0;
+  }
   *converged = h.done;
   if (value) {
     CPALS_CUDA_TRY(cudaMemcpyAsync(value, c->traj, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
   }
+  if (h.nan_flag && check->kind == CPALS_CHECK_FIT) return CPALS_E_NAN;
   return CPALS_OK;
 }
 
@@ -1476,10 +1551,31 @@ int cpals_set_profiling(cpals_ctx* c, int on) {
   if (on && c->prof_ev.empty()) {
     c->prof_ev.resize(2 * 8192);
     for (auto& e : c->prof_ev) CPALS_CUDA_TRY(cudaEventCreate(&e));
+    c->samp_ev.resize(4 * 1024);
+    for (auto& e : c->samp_ev) CPALS_CUDA_TRY(cudaEventCreate(&e));
   }
   CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
   c->profiling = on != 0;
   c->prof_used = 0;
+  c->samp_used = 0;
+  return CPALS_OK;
+}
+
+int cpals_profile_read_sampled(cpals_ctx* c, double* update_ms, double* gather_ms, int64_t* updates) {
+  if (!c || !update_ms || !gather_ms || !updates) return CPALS_E_ARG;
+  DeviceGuard g(c->device);
+  CPALS_CUDA_TRY(cudaStreamSynchronize(c->st));
+  double tu = 0.0, tg = 0.0;
+  for (int64_t k = 0; k + 3 < c->samp_used; k += 4) {
+    float a = 0.0f, b = 0.0f;
+    CPALS_CUDA_TRY(cudaEventElapsedTime(&a, c->samp_ev[k], c->samp_ev[k + 3]));
+    CPALS_CUDA_TRY(cudaEventElapsedTime(&b, c->samp_ev[k + 1], c->samp_ev[k + 2]));
+    tu += a;
+    tg += b;
+  }
+  *update_ms = tu;
+  *gather_ms = tg;
+  *updates = c->samp_used / 4;
   return CPALS_OK;
 }
 
@@ -1551,14 +1647,20 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
   if (!c) return CPALS_E_ARG;
   if (!c->T_set || !c->F_set) return CPALS_E_STATE;
   DeviceGuard g(c->device);
+  // profiling: device time of the whole update (pivot upload included) and of the gathers
+  const bool prof = c->profiling && c->samp_used + 4 <= (int64_t)c->samp_ev.size();
+  cudaEvent_t* ev = prof ? &c->samp_ev[c->samp_used] : nullptr;
+  if (prof) CPALS_CUDA_TRY(cudaEventRecord(ev[0], c->st));
   int rc = upload_pivots(c, mode, pivots, nsamps);
   if (rc != CPALS_OK) return rc;
   const int R = (int)c->R;
   const int64_t In = c->dims[mode];
   // S (sampled KRP rows) and T_s (sampled fibres)
+  if (prof) CPALS_CUDA_TRY(cudaEventRecord(ev[1], c->st));
   CPALS_CUDA_TRY(launch_pivot_hadamard(factor_set(c), c->order, mode, c->dims, c->dpiv, nsamps, R, c->Scol, c->derr,
                                        c->st));
   CPALS_CUDA_TRY(launch_fibers(c->dT, c->tdtype, c->order, mode, c->dims, c->dpiv, nsamps, c->Ts, c->derr, c->st));
+  if (prof) CPALS_CUDA_TRY(cudaEventRecord(ev[2], c->st));
   CPALS_CUDA_TRY(launch_colmajor_to_rowmajor(c->Scol, nsamps, R, c->Srow, c->st));
   // A = S^T S (the Gram partial buffer holds up to max(gS2) splits)
   const int s2 = std::min(gram_splits(nsamps, R, c->num_sms), *std::max_element(c->gS2, c->gS2 + c->order));
@@ -1594,6 +1696,10 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
                                   c->rpad, nullptr, nullptr, nullptr, c->st, BtileDesc{nullptr, 0, 0},
                                   c->F32lo[mode]));
   CPALS_CUDA_TRY(update_factor_tiles(c, mode, nullptr));
+  if (prof) {
+    CPALS_CUDA_TRY(cudaEventRecord(ev[3], c->st));
+    c->samp_used += 4;
+  }
   return check_derr(c);
 }
 

@@ -36,7 +36,52 @@ struct DevCheck {
   double norm_prev;
   int has_prev;
   int psel;
+  // ||T||^2 of the handle's tensor as an unevaluated sum t2_hi + t2_lo, computed on the
+  // device whenever the tensor is set (t2_valid = 0: not available, e.g. a non-finite entry)
+  double t2_hi, t2_lo;
+  int t2_valid;
+  // The fit's terms from the last mode's update, as double-doubles: <T, X> (the saved
+  // MTTKRP against the new factor, fit_check.jl:22-28) and ||X||^2 (converge_checks.jl:5-11).
+  // terms_ready says they are newer than the last check that read them.
+  int terms_ready;
+  double inner_hi, inner_lo, fsq_hi, fsq_lo;
 };
+
+// ---- double-double arithmetic: error-free transformations (Knuth's TwoSum, Dekker's
+// FastTwoSum, the FMA form of TwoProduct; Ogita, Rump and Oishi 2005) ----
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ DD dd_two_sum(double a, double b) {
+  const double s = a + b;
+  const double z = s - a;
+  return DD{s, (a - (s - z)) + (b - z)};
+}
+__device__ __forceinline__ DD dd_fast_two_sum(double a, double b) {  // |a| >= |b|
+  const double s = a + b;
+  return DD{s, b - (s - a)};
+}
+__device__ __forceinline__ DD dd_two_prod(double a, double b) {
+  const double p = a * b;
+  return DD{p, fma(a, b, -p)};
+}
+// (a + b) with relative error O(2^-104): two TwoSums, renormalised
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  DD s = dd_two_sum(a.hi, b.hi);
+  const DD t = dd_two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = dd_fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return dd_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ DD dd_mul_d(DD a, double b) {
+  DD p = dd_two_prod(a.hi, b);
+  p.lo = fma(a.lo, b, p.lo);
+  return dd_fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ DD dd_shfl_xor(DD a, int off) {
+  return DD{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)};
+}
 
 struct FactorSet {
   const double* F[kMaxOrder];  // FP64 factors, row-major [I_n][R]
@@ -107,7 +152,7 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
 size_t factorize_work_doubles(int R);
 
 // Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and
-// (optionally) per-row sums of M .* X for the fit.  `work` is the factorize workspace.
+// (optionally) per-row sums of M .* X for the fit, as double-doubles (two doubles per row).  `work` is the factorize workspace.
 // With gram_part, every block also writes its rows' share of G = X^T X (upper triangle,
 // R(R+1)/2 doubles per block, solve_blocks(In, R) blocks) for launch_gram_rows.
 cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
@@ -117,10 +162,14 @@ int solve_blocks(int64_t In, int R);
 // G (Graw) from the solve blocks' partial Grams, then launch_finalize's work in the last
 // block (without G_n, which launch_normalize writes); gram_part needs room for
 // nblk * R(R+1)/2 + (R(R+1)/2 + 31)/32 doubles; counter: one zeroed unsigned.
+// run_check = 0 leaves the check's update to launch_check_step (a caller-driven sweep).
 cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned* counter, double* Graw, double* lam,
                              double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
                              const double* inner_rows, int64_t In, DevCheck* chk, double* traj, int64_t traj_cap,
-                             cudaStream_t st);
+                             cudaStream_t st, int run_check = 1);
+// Room in gram_part: nblk * R(R+1)/2 doubles of partial Grams, then two doubles per block of
+// launch_gram_rows for the ||X||^2 shares.
+size_t gram_rows_part_doubles(int nblk, int R);
 
 // G = X^T X (row-major X, In x R) over S2 row splits; part: gram_tiles(R)*S2*256 doubles,
 // counters: gram_tiles(R)+1 zero-initialised unsigneds (left zeroed after each launch).
@@ -135,10 +184,26 @@ cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part
 cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters,
                                  double* Graw, double* lam, double* lam_inv, double* Gn, const GramSet& gs, int order,
                                  int last, const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap,
-                                 cudaStream_t st);
+                                 cudaStream_t st, int run_check = 1);
+// Room in part for launch_gram_finalize: the tile partials and two doubles per tile.
+size_t gram_finalize_part_doubles(int S2, int R);
+
+// The check's update (FitCheck / NoCheck) from the terms the last mode's update saved in
+// chk, as the fused finalize runs it; one thread.
+cudaError_t launch_check_step(DevCheck* chk, double* traj, int64_t traj_cap, cudaStream_t st);
+
+// ||T||^2 as a double-double into chk->t2_hi / t2_lo (t2_valid = 1), for the compensated
+// fit.  FP32 tensors: the squares are exact 48-bit integers times powers of two, summed
+// exactly in 128-bit fixed point anchored at the largest exponent (two passes: the largest
+// |entry|, then the sum; integer work only).  FP64 tensors: TwoProduct squares summed in
+// double-double.  scratch: norm2_scratch_doubles() doubles.
+size_t norm2_scratch_doubles();
+cudaError_t launch_tensor_norm2(const void* T, int tdtype, int64_t n, double* scratch, DevCheck* chk, int num_sms,
+                                cudaStream_t st);
 
 // lambda = sqrt(diag Graw), G_n = Graw ./ (lambda lambda^T); on the last mode also the fit
-// and the device check update (trajectory entry per sweep).
+// and the device check update (trajectory entry per sweep).  inner_rows holds two doubles
+// (a double-double) per row.
 cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st);

@@ -918,7 +918,6 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
       const int row = e / R, k = e % R;
       const double x = Xs[e] + (double)rowdot32(Fs + row * R, k);
       X[base + e] = x;
-      Ps[e] = Ms[e] * x;
       Xs[e] = x;  // (only this thread reads Xs[e] in this loop)
     }
   } else {
@@ -926,7 +925,6 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
       const int row = e / R, k = e % R;
       const double x = rowdot(Ms + row * R, W, k);
       X[base + e] = x;
-      Ps[e] = Ms[e] * x;
       Xs[e] = x;
     }
   }
@@ -958,19 +956,17 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
   }
   if (!inner_rows) return;
   __syncthreads();
-  // per-row sum of M .* X: one warp per row, a tree over the lanes
+  // per-row sum of M .* X for the fit's <T, X>, as a double-double: each product split
+  // exactly by TwoProduct, summed error-free along the row and across the lanes
   const int lane = tid & 31, warp = tid >> 5, nw = SOLVE_T >> 5;
   for (int row = warp; row < rows; row += nw) {
-    double sa = 0.0, sb = 0.0;
-    int kk = lane;
-    for (; kk + 32 < R; kk += 64) {
-      sa += Ps[row * R + kk];
-      sb += Ps[row * R + kk + 32];
+    DD v{0.0, 0.0};
+    for (int kk = lane; kk < R; kk += 32) v = dd_add(v, dd_two_prod(Ms[row * R + kk], Xs[row * R + kk]));
+    for (int off = 16; off > 0; off >>= 1) v = dd_add(v, dd_shfl_xor(v, off));
+    if (lane == 0) {
+      inner_rows[2 * (r0 + row)] = v.hi;
+      inner_rows[2 * (r0 + row) + 1] = v.lo;
     }
-    if (kk < R) sa += Ps[row * R + kk];
-    double v = sa + sb;
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    if (lane == 0) inner_rows[r0 + row] = v;
   }
 }
 
@@ -988,6 +984,102 @@ __device__ double block_tree_sum(double v, double* sv) {
   return t;
 }
 
+// Block-wide double-double sum (a fixed tree: lanes, then warps); every thread gets it.
+__device__ DD block_sum_dd(DD v, double* sv) {  // sv: 64 doubles
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) v = dd_add(v, dd_shfl_xor(v, off));
+  __syncthreads();
+  if (lane == 0) {
+    sv[2 * w] = v.hi;
+    sv[2 * w + 1] = v.lo;
+  }
+  __syncthreads();
+  DD t = (lane < nw) ? DD{sv[2 * lane], sv[2 * lane + 1]} : DD{0.0, 0.0};
+  for (int off = 16; off > 0; off >>= 1) t = dd_add(t, dd_shfl_xor(t, off));
+  __syncthreads();
+  return t;
+}
+
+// The fit 1 - ||T - X|| / ||T|| with ||T - X||^2 = ||T||^2 + ||X||^2 - 2 |<T, X>|
+// (fit_check.jl:26-32), from the saved double-double terms.  Near fit -> 1 the three terms
+// cancel, so the combination is done in double-double arithmetic and the square root gets
+// one Newton correction from the double-double radicand.  ||T||^2 is the device's own
+// double-double when ref_norm is norm(T) (equal to it within 1e-15 relative), else the
+// exact square of ref_norm.
+__device__ double compensated_fit(const DevCheck& k) {
+  const double rn = k.ref_norm;
+  if (!(rn > 0.0)) return NAN;
+  DD rn2;
+  if (k.t2_valid && fabs(rn - sqrt(k.t2_hi)) <= 1e-15 * rn)
+    rn2 = DD{k.t2_hi, k.t2_lo};
+  else
+    rn2 = dd_two_prod(rn, rn);
+  DD inner{k.inner_hi, k.inner_lo};
+  if (inner.hi < 0.0) inner = DD{-inner.hi, -inner.lo};
+  DD s = dd_add(rn2, DD{k.fsq_hi, k.fsq_lo});
+  s = dd_add(s, DD{-2.0 * inner.hi, -2.0 * inner.lo});
+  if (s.hi < 0.0) s = DD{-s.hi, -s.lo};
+  double r = sqrt(s.hi);
+  if (r > 0.0) {
+    const DD rr = dd_two_prod(r, r);
+    r += (((s.hi - rr.hi) - rr.lo) + s.lo) / (2.0 * r);
+  }
+  return 1.0 - r / rn;
+}
+
+// The check's update after a sweep (FitCheck fit_check.jl:24-66, NoCheck no_check.jl:11-20)
+// from the terms in k; writes the trajectory entry.
+__device__ void check_update(DevCheck& k, double* traj, int64_t traj_cap) {
+  // CPDiffCheck / CPAngleCheck run after the sweep, on the normalised iterate (k_cpcheck.cu)
+  if (k.kind == CPALS_CHECK_DIFF || k.kind == CPALS_CHECK_ANGLE) return;
+  const double fit = compensated_fit(k);
+  k.terms_ready = 0;
+  if (k.sweeps < traj_cap) traj[k.sweeps] = fit;
+  k.sweeps += 1;
+  if (k.kind == CPALS_CHECK_FIT) {
+    k.iter += 1;
+    const double dfit = fabs(k.lastfit - fit);
+    k.lastfit = fit;
+    if (isnan(fit)) {
+      k.nan_flag = 1;
+      k.done = 1;
+      return;
+    }
+    if (dfit < k.tol) {
+      k.counter += 1;
+      if (k.counter >= 2) {
+        k.total_iter = k.iter;
+        k.iter = 0;
+        k.counter = 0;
+        k.final_fit = k.lastfit;
+        k.lastfit = 0.0;
+        k.done = 1;
+        return;
+      }
+    } else {
+      k.counter = 0;
+    }
+    if (k.iter >= k.max_counter) {
+      k.total_iter = k.iter;
+      k.iter = 0;
+      k.counter = 0;
+      k.final_fit = k.lastfit;
+      k.lastfit = 0.0;
+    }
+  } else {
+    k.iter += 1;
+    k.lastfit = fit;
+    if (k.iter == k.max_counter) {
+      k.iter = 0;
+      k.done = 1;
+    }
+  }
+}
+
+__global__ void k_check_step(DevCheck* chk, double* traj, int64_t traj_cap) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) check_update(*chk, traj, traj_cap);
+}
+
 struct FinalizeArgs {
   double* lam;
   double* lam_inv;
@@ -1001,8 +1093,9 @@ struct FinalizeArgs {
   double* traj;
   int64_t traj_cap;
   int mode;       // the mode whose raw Gram is being finalised
-  double* fpart;  // per-tile partials of ||X||^2 (fused path), or null
+  double* fpart;  // per-tile double-double partials of ||X||^2 (fused path), or null
   int ntiles;
+  int run_check;  // 0: only save the fit's terms (a caller-driven sweep runs the check)
 };
 
 // lambda = sqrt(diag Graw) (one reciprocal square root per column), G_n = Graw ./
@@ -1044,104 +1137,34 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
     }
   }
   if (!fa.last) return;
-  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28)
-  double ia = 0.0, ib = 0.0;
-  {
-    int64_t i = tid;
-    for (; i + nt < fa.In; i += 2 * nt) {
-      ia += fa.inner_rows[i];
-      ib += fa.inner_rows[i + nt];
-    }
-    if (i < fa.In) ia += fa.inner_rows[i];
-  }
-  const double inner = block_tree_sum(ia + ib, sv);
+  __shared__ double sv2[64];
+  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28), summed in
+  // double-double from the solve's per-row double-doubles
+  DD ia{0.0, 0.0};
+  for (int64_t i = tid; i < fa.In; i += nt) ia = dd_add(ia, DD{fa.inner_rows[2 * i], fa.inner_rows[2 * i + 1]});
+  const DD inner = block_sum_dd(ia, sv2);
   // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11).  With the
-  // per-tile partials (fused path) it is their sum in tile order; otherwise the products
-  // of eight elements are formed side by side.
-  double ps[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) ps[q] = 0.0;
-  if (fa.fpart)  // one partial per thread, summed by the block's tree below
-    for (int t = tid; t < fa.ntiles; t += nt) ps[0] += __ldcg(&fa.fpart[t]);
-  for (int e0 = tid; !fa.fpart && e0 < n; e0 += 8 * nt) {
-    double h[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int e = e0 + q * nt;
-      h[q] = (e < n) ? fa.gs.G[0][e] : 0.0;
-    }
-    for (int m = 1; m < fa.order; ++m) {
-      const double* __restrict__ Gm = fa.gs.G[m];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int e = e0 + q * nt;
-        if (e < n) h[q] *= Gm[e];
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int e = e0 + q * nt;
-      if (e < n) {
-        const int r = e / R, c = e - r * R;
-        ps[q] += h[q] * (s_lam[r] * s_lam[c]);
-      }
-    }
+  // per-tile partials (fused path) it is their double-double sum in tile order; otherwise
+  // each term is formed as a double-double product.
+  DD ps{0.0, 0.0};
+  if (fa.fpart)
+    for (int t = tid; t < fa.ntiles; t += nt)
+      ps = dd_add(ps, DD{__ldcg(&fa.fpart[2 * t]), __ldcg(&fa.fpart[2 * t + 1])});
+  for (int e = tid; !fa.fpart && e < n; e += nt) {
+    DD h{fa.gs.G[0][e], 0.0};
+    for (int m = 1; m < fa.order; ++m) h = dd_mul_d(h, fa.gs.G[m][e]);
+    const int r = e / R, c = e - r * R;
+    ps = dd_add(ps, dd_mul_d(dd_mul_d(h, s_lam[r]), s_lam[c]));
   }
-  const double fact_square =
-      block_tree_sum(((ps[0] + ps[1]) + (ps[2] + ps[3])) + ((ps[4] + ps[5]) + (ps[6] + ps[7])), sv);
-  DevCheck* chk = fa.chk;
-  double* traj = fa.traj;
-  const int64_t traj_cap = fa.traj_cap;
+  const DD fact_square = block_sum_dd(ps, sv2);
   if (tid != 0) return;
-  DevCheck& k = *chk;
-  // CPDiffCheck / CPAngleCheck run after the sweep, on the normalised iterate (k_cpcheck.cu)
-  if (k.kind == CPALS_CHECK_DIFF || k.kind == CPALS_CHECK_ANGLE) return;
-  double fit = NAN;
-  if (k.ref_norm > 0.0) {
-    const double rn = k.ref_norm;
-    const double nr = sqrt(fabs(rn * rn + fact_square - 2.0 * fabs(inner)));
-    fit = 1.0 - nr / rn;
-  }
-  if (k.sweeps < traj_cap) traj[k.sweeps] = fit;
-  k.sweeps += 1;
-  if (k.kind == CPALS_CHECK_FIT) {
-    k.iter += 1;
-    const double dfit = fabs(k.lastfit - fit);
-    k.lastfit = fit;
-    if (isnan(fit)) {
-      k.nan_flag = 1;
-      k.done = 1;
-      return;
-    }
-    if (dfit < k.tol) {
-      k.counter += 1;
-      if (k.counter >= 2) {
-        k.total_iter = k.iter;
-        k.iter = 0;
-        k.counter = 0;
-        k.final_fit = k.lastfit;
-        k.lastfit = 0.0;
-        k.done = 1;
-        return;
-      }
-    } else {
-      k.counter = 0;
-    }
-    if (k.iter >= k.max_counter) {
-      k.total_iter = k.iter;
-      k.iter = 0;
-      k.counter = 0;
-      k.final_fit = k.lastfit;
-      k.lastfit = 0.0;
-    }
-  } else {
-    k.iter += 1;
-    k.lastfit = fit;
-    if (k.iter == k.max_counter) {
-      k.iter = 0;
-      k.done = 1;
-    }
-  }
+  DevCheck& k = *fa.chk;
+  k.inner_hi = inner.hi;
+  k.inner_lo = inner.lo;
+  k.fsq_hi = fact_square.hi;
+  k.fsq_lo = fact_square.lo;
+  k.terms_ready = 1;
+  if (fa.run_check) check_update(k, fa.traj, fa.traj_cap);
 }
 
 
@@ -1228,15 +1251,19 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int6
   if (fa.last) {
     // this tile's share of ||X||^2 = sum(Graw .* prod_{m != mode} G_m) (lambda_r lambda_c
     // times the normalised Gram of this mode is its raw Gram); off-diagonal tiles count twice
-    double h = 0.0;
+    // (double-double products and sums: the fit's terms cancel near fit -> 1)
+    DD h{0.0, 0.0};
     if (r1 < R && r2 < R) {
-      h = (ti == tj) ? sum : 2.0 * sum;
+      h.hi = (ti == tj) ? sum : 2.0 * sum;
       for (int m = 0; m < fa.order; ++m)
-        if (m != fa.mode) h *= fa.gs.G[m][(size_t)r1 * R + r2];
+        if (m != fa.mode) h = dd_mul_d(h, fa.gs.G[m][(size_t)r1 * R + r2]);
     }
-    __shared__ double sv_t[32];
-    const double tsum = block_tree_sum(h, sv_t);
-    if (threadIdx.x == 0) fa.fpart[tile] = tsum;
+    __shared__ double sv_t[64];
+    const DD tsum = block_sum_dd(h, sv_t);
+    if (threadIdx.x == 0) {
+      fa.fpart[2 * tile] = tsum.hi;
+      fa.fpart[2 * tile + 1] = tsum.lo;
+    }
   }
   __threadfence();
   __syncthreads();
@@ -1258,7 +1285,7 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
   if (done_flag(chk)) return;
   __shared__ double red[8][33];
   __shared__ int s_last;
-  __shared__ double sv_t[32];
+  __shared__ double sv_t[64];
   const int T = R * (R + 1) / 2;
   const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
@@ -1278,7 +1305,7 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
   }
   red[sl][lane] = (a0 + a1) + (a2 + a3);
   __syncthreads();
-  double h = 0.0;
+  DD h{0.0, 0.0};
   if (sl == 0 && e < T) {
     double sum = 0.0;
     for (int q = 0; q < 8; ++q) sum += red[q][lane];
@@ -1293,15 +1320,18 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
     }
     G[(size_t)a * R + c] = sum;
     G[(size_t)c * R + a] = sum;
-    if (fa.last) {
-      h = (a == c) ? sum : 2.0 * sum;
+    if (fa.last) {  // this entry's share of ||X||^2, a double-double product
+      h.hi = (a == c) ? sum : 2.0 * sum;
       for (int m = 0; m < fa.order; ++m)
-        if (m != fa.mode) h *= fa.gs.G[m][(size_t)a * R + c];
+        if (m != fa.mode) h = dd_mul_d(h, fa.gs.G[m][(size_t)a * R + c]);
     }
   }
   if (fa.last) {
-    const double tsum = block_tree_sum(h, sv_t);
-    if (threadIdx.x == 0) fa.fpart[blockIdx.x] = tsum;
+    const DD tsum = block_sum_dd(h, sv_t);
+    if (threadIdx.x == 0) {
+      fa.fpart[2 * blockIdx.x] = tsum.hi;
+      fa.fpart[2 * blockIdx.x + 1] = tsum.lo;
+    }
   }
   __threadfence();
   __syncthreads();
@@ -1377,7 +1407,133 @@ __global__ void k_reduce_partials(const PT* __restrict__ part, int S, int64_t n,
   }
 }
 
+// ---------------- ||T||^2 as a double-double ----------------
+// FP32 tensors.  GB300 issues FP64 some 60 times slower than FP32 and integer work, so the
+// exact sum uses integers: an FP32 entry is m 2^(e - 150) (m: 24-bit significand, e: biased
+// exponent, 1 for subnormals), its square the 48-bit integer m^2 times 2^(2(e - 150)).  With
+// e_max the exponent of the largest |entry|, each square is added into a 128-bit fixed-point
+// sum in units of 2^(2(e_max - 150) - 32): shifted left by 32 - 2(e_max - e) bits (right when
+// negative; bits below the unit, less than 2^-78 of the largest square each, are dropped).
+// A square is below 2^80 units, so 2^40 entries stay below 2^120: no overflow.  Integer sums
+// are associative, so the result does not depend on the order of the atomics.
+constexpr int kNormMaxBlocks = 1024;
+
+__global__ void __launch_bounds__(256) k_absmax_bits(const float* __restrict__ T, int64_t n,
+                                                     unsigned* __restrict__ out) {
+  unsigned m = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    m = max(m, __float_as_uint(T[i]) & 0x7fffffffu);  // |x| orders as its bit pattern
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void __launch_bounds__(256) k_sumsq_f32(const float* __restrict__ T, int64_t n,
+                                                   const unsigned* __restrict__ maxbits,
+                                                   unsigned long long* __restrict__ acc) {
+  const unsigned mb = *maxbits;
+  if (mb == 0u || mb >= 0x7f800000u) return;  // all zero, or a non-finite entry
+  const int emax = (int)(mb >> 23) + ((mb >> 23) == 0u ? 1 : 0);
+  unsigned __int128 a = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const unsigned u = __float_as_uint(T[i]) & 0x7fffffffu;
+    const unsigned e = u >> 23;
+    const unsigned long long mm = (unsigned long long)((u & 0x7fffffu) | (e ? 0x800000u : 0u));
+    const unsigned long long sq = mm * mm;  // < 2^48, exact
+    const int sh = 32 - 2 * (emax - ((int)e + (e == 0u ? 1 : 0)));
+    if (sh >= 0)
+      a += (unsigned __int128)sq << sh;
+    else if (sh > -64)
+      a += (unsigned __int128)(sq >> (-sh));
+  }
+  unsigned long long lo = (unsigned long long)a, hi = (unsigned long long)(a >> 64);
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, off);
+    const unsigned long long ohi = __shfl_xor_sync(0xffffffffu, hi, off);
+    const unsigned long long nlo = lo + olo;
+    hi += ohi + (nlo < lo ? 1ull : 0ull);
+    lo = nlo;
+  }
+  if ((threadIdx.x & 31) == 0 && (lo | hi)) {
+    const unsigned long long old = atomicAdd(&acc[0], lo);
+    atomicAdd(&acc[1], hi + ((old + lo) < old ? 1ull : 0ull));
+  }
+}
+
+// FP64 tensors: TwoProduct squares summed in double-double, one partial per block.
+__global__ void __launch_bounds__(256) k_sumsq_f64(const double* __restrict__ T, int64_t n,
+                                                   double* __restrict__ part) {
+  __shared__ double sv[64];
+  DD a{0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double x = T[i];
+    a = dd_add(a, dd_two_prod(x, x));
+  }
+  const DD b = block_sum_dd(a, sv);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = b.hi;
+    part[2 * blockIdx.x + 1] = b.lo;
+  }
+}
+
+__device__ DD dd_from_u64(unsigned long long u) {  // exact: both halves and their sum fit
+  return dd_two_sum((double)(u >> 32) * 4294967296.0, (double)(u & 0xffffffffull));
+}
+
+__global__ void k_norm2_finish(int is_f32, const unsigned* __restrict__ maxbits,
+                               const unsigned long long* __restrict__ acc, const double* __restrict__ part,
+                               int nblk, DevCheck* chk) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  DD t{0.0, 0.0};
+  int valid = 1;
+  if (is_f32) {
+    const unsigned mb = *maxbits;
+    if (mb >= 0x7f800000u) {
+      valid = 0;
+    } else if (mb != 0u) {
+      const int emax = (int)(mb >> 23) + ((mb >> 23) == 0u ? 1 : 0);
+      DD h = dd_from_u64(acc[1]);
+      h = DD{ldexp(h.hi, 64), ldexp(h.lo, 64)};
+      t = dd_add(h, dd_from_u64(acc[0]));
+      const int sc = 2 * (emax - 150) - 32;
+      t = DD{ldexp(t.hi, sc), ldexp(t.lo, sc)};
+    }
+  } else {
+    for (int b = 0; b < nblk; ++b) t = dd_add(t, DD{part[2 * b], part[2 * b + 1]});
+    valid = isfinite(t.hi) ? 1 : 0;
+  }
+  chk->t2_hi = t.hi;
+  chk->t2_lo = t.lo;
+  chk->t2_valid = valid;
+}
+
 }  // namespace
+
+size_t norm2_scratch_doubles() { return 4 + 2 * (size_t)kNormMaxBlocks; }
+
+cudaError_t launch_tensor_norm2(const void* T, int tdtype, int64_t n, double* scratch, DevCheck* chk, int num_sms,
+                                cudaStream_t st) {
+  // scratch: [0, 2) the 128-bit sum, [2] the largest |entry|'s bits, [4, ...) block partials
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(scratch);
+  unsigned* maxbits = reinterpret_cast<unsigned*>(scratch + 2);
+  double* part = scratch + 4;
+  const int64_t want = (n + 255) / 256;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, std::min(kNormMaxBlocks, 8 * num_sms)));
+  cudaError_t e = cudaMemsetAsync(scratch, 0, 4 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  if (tdtype == CPALS_DTYPE_F32) {
+    const float* Tf = static_cast<const float*>(T);
+    k_absmax_bits<<<blocks, 256, 0, st>>>(Tf, n, maxbits);
+    k_sumsq_f32<<<blocks, 256, 0, st>>>(Tf, n, maxbits, acc);
+    k_norm2_finish<<<1, 32, 0, st>>>(1, maxbits, acc, part, 0, chk);
+  } else {
+    k_sumsq_f64<<<blocks, 256, 0, st>>>(static_cast<const double*>(T), n, part);
+    k_norm2_finish<<<1, 32, 0, st>>>(0, maxbits, acc, part, blocks, chk);
+  }
+  return cudaGetLastError();
+}
 
 size_t factorize_work_doubles(int R) { return ops32_offset_doubles(R) + (3 * (size_t)rr4(R) + 1) / 2; }
 
@@ -1460,29 +1616,37 @@ cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part
   return cudaGetLastError();
 }
 
+size_t gram_finalize_part_doubles(int S2, int R) { return (size_t)gram_tiles(R) * ((size_t)S2 * 256 + 2); }
+
 cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters,
                                  double* Graw, double* lam, double* lam_inv, double* Gn, const GramSet& gs, int order,
                                  int last, const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, int run_check) {
   const int64_t rps = (In + S2 - 1) / S2;
   dim3 grid((unsigned)gram_tiles(R), (unsigned)S2);
   const int ntiles = gram_tiles(R);
-  // per-tile partials of ||X||^2 live after the tile partial sums
+  // per-tile double-double partials of ||X||^2 live after the tile partial sums
   FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1,
-                  part + (size_t)ntiles * S2 * 256, ntiles};
+                  part + (size_t)ntiles * S2 * 256, ntiles, run_check};
   k_gram<true><<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, Graw, chk, fa);
   return cudaGetLastError();
+}
+
+size_t gram_rows_part_doubles(int nblk, int R) {
+  const size_t T = (size_t)R * (R + 1) / 2;
+  return (size_t)nblk * T + 2 * ((T + 31) / 32);
 }
 
 cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned* counter, double* Graw, double* lam,
                              double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
                              const double* inner_rows, int64_t In, DevCheck* chk, double* traj, int64_t traj_cap,
-                             cudaStream_t st) {
+                             cudaStream_t st, int run_check) {
   const int T = R * (R + 1) / 2;
   const int blocks = (T + 31) / 32;
-  // the blocks' shares of ||X||^2 follow the partial Grams
+  // the blocks' double-double shares of ||X||^2 follow the partial Grams
   double* fpart = const_cast<double*>(gram_part) + (size_t)nblk * T;
-  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, fpart, blocks};
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, fpart, blocks,
+                  run_check};
   k_gram_rows<<<blocks, 256, 0, st>>>(gram_part, nblk, R, Graw, counter, chk, fa);
   return cudaGetLastError();
 }
@@ -1490,8 +1654,13 @@ cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned*
 cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st) {
-  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, nullptr, 0};
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, nullptr, 0, 1};
   k_finalize<<<1, 256, 0, st>>>(Graw, R, fa);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_step(DevCheck* chk, double* traj, int64_t traj_cap, cudaStream_t st) {
+  k_check_step<<<1, 32, 0, st>>>(chk, traj, traj_cap);
   return cudaGetLastError();
 }
 

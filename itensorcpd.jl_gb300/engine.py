@@ -139,13 +139,36 @@ class Engine:
         L.check(self.lib.cpals_set_prev(self.h, arr, L.dptr(lam)), "cpals_set_prev")
 
     def check_converge(self, chk: L.CpalsCheck):
-        """One CPDiffCheck / CPAngleCheck call on the current iterate (``chk`` updated in
-        place); returns (converged, value), value NaN when the call only stored the iterate."""
+        """One check_converge call (``chk`` updated in place); returns (converged, value).
+        FitCheck / NoCheck read the terms the last mode_update of the last mode saved;
+        CPDiffCheck / CPAngleCheck run on the current iterate (value NaN when the call only
+        stored it).  A NaN FitCheck fit raises "Error NAN", as fit_check.jl:40-42 throws."""
         conv = C.c_int(0)
         val = np.full(1, np.nan)
-        L.check(self.lib.cpals_check_converge(self.h, C.byref(chk), C.byref(conv), L.dptr(val)),
-                "cpals_check_converge")
+        st = self.lib.cpals_check_converge(self.h, C.byref(chk), C.byref(conv), L.dptr(val))
+        if st == L.CPALS_E_NAN:
+            raise FloatingPointError("Error NAN")
+        L.check(st, "cpals_check_converge")
         return bool(conv.value), float(val[0])
+
+    def mode_update(self, mode, want_solution=False):
+        """One mode of a sweep on the device (compute_krp, matricize_tensor, solve_ls_problem,
+        row_norm, post_solve).  With ``want_solution`` returns the solve's result before
+        normalisation, X = F_n diag(lambda) (I_n x R), else None."""
+        X = np.empty((self.dims[mode], self.rank), dtype=np.float64, order="F") if want_solution else None
+        L.check(self.lib.cpals_mode_update(self.h, int(mode), L.dptr(X) if X is not None else None),
+                "cpals_mode_update")
+        return X
+
+    def tensor_norm(self):
+        """(norm(T), ||T||^2 as (hi, lo)) from the device's double-double sum of squares."""
+        nrm = C.c_double()
+        t2 = np.zeros(2)
+        st = self.lib.cpals_tensor_norm(self.h, C.byref(nrm), L.dptr(t2))
+        if st == L.CPALS_E_NAN:
+            raise FloatingPointError("the tensor has a non-finite entry")
+        L.check(st, "cpals_tensor_norm")
+        return float(nrm.value), (float(t2[0]), float(t2[1]))
 
     def sketched_matricization(self, mode, l, rows, vals, zeta):
         """A_sk = T_(mode) Omega^T (I_mode x l) for the embedding given by 0-based ``rows`` and
@@ -263,6 +286,13 @@ class Engine:
         ms, n = C.c_double(), C.c_int64()
         L.check(self.lib.cpals_profile_read(self.h, C.byref(ms), C.byref(n)), "cpals_profile_read")
         return ms.value, int(n.value)
+
+    def profile_read_sampled(self):
+        """(device ms of the timed sampled updates, ms of their gathers, updates timed)."""
+        u, g, n = C.c_double(), C.c_double(), np.zeros(1, dtype=np.int64)
+        L.check(self.lib.cpals_profile_read_sampled(self.h, C.byref(u), C.byref(g), L.i64ptr(n)),
+                "cpals_profile_read_sampled")
+        return float(u.value), float(g.value), int(n[0])
 
     def launch_count(self) -> int:
         n = C.c_int64()

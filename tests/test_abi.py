@@ -63,6 +63,18 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.cpals_set_tensor(None, None) == -1
     assert lib.cpals_mttkrp(None, 0, None) == -1
     assert lib.cpals_optimize(None, None, None, 0) == -1
+    assert lib.cpals_mode_update(None, 0, None) == -1
+    assert lib.cpals_tensor_norm(None, None, None) == -1
+    assert lib.cpals_check_converge(None, None, None, None) == -1
+
+
+def test_create_rejects_more_than_2_40_elements_without_overflow(lib):
+    # 2^21 * 2^20 * 2^21 would overflow a 64-bit product checked after multiplying
+    h = ctypes.c_void_p()
+    big = (ctypes.c_int64 * 3)(1 << 21, 1 << 20, 1 << 21)
+    assert lib.cpals_create(ctypes.byref(h), 0, 3, big, 4, 0, 0, 0) == -1
+    big4 = (ctypes.c_int64 * 4)(1 << 31, 1 << 31, 1 << 31, 1 << 31)
+    assert lib.cpals_create(ctypes.byref(h), 0, 4, big4, 4, 0, 0, 0) == -1
 
 
 def test_check_struct_mirrors_the_header(pkg):

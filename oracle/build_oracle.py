@@ -1,4 +1,7 @@
-"""Build recipe for the oracle's reference binaries (TEST INFRASTRUCTURE ONLY).
+"""Build recipe for the oracle's compiled parts (TEST INFRASTRUCTURE ONLY).
+
+``build_cpu`` compiles cpals_cpu.cpp, the C++/OpenMP GEMM-form ALS that the bench times as a
+CPU baseline, into oracle/_build/libcpals_cpu.so.
 
 Compiles the reference's own sparse sign embedding generators, src/algebra/sparse_sign.c and
 src/algebra/sparsestack.c of ITensorCPD.jl, from the reference checkout where it lies, into
@@ -31,7 +34,26 @@ def reference_dir(explicit: str | None = None) -> Path:
     return Path(__file__).resolve().parent.parent.parent / "reference"
 
 
+CPU_SRC = Path(__file__).resolve().parent / "cpals_cpu.cpp"
+CPU_LIB = Path(__file__).resolve().parent / "_build" / "libcpals_cpu.so"
+
+
+def build_cpu() -> Path | None:
+    """The C++/OpenMP GEMM-form ALS (cpals_cpu.cpp), the compiled CPU baseline."""
+    if shutil.which("g++") is None:
+        return None
+    if CPU_LIB.exists() and CPU_LIB.stat().st_mtime >= CPU_SRC.stat().st_mtime:
+        return CPU_LIB
+    CPU_LIB.parent.mkdir(exist_ok=True)
+    tmp = CPU_LIB.with_suffix(".so.tmp")
+    subprocess.run(["g++", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c++17", "-o", str(tmp), str(CPU_SRC)],
+                   check=True)
+    os.replace(tmp, CPU_LIB)
+    return CPU_LIB
+
+
 def build(reference: str | None = None) -> Path | None:
+    build_cpu()
     src_dir = reference_dir(reference) / "src" / "algebra"
     srcs = [src_dir / f for f in SOURCES]
     if not all(p.exists() for p in srcs) or shutil.which("gcc") is None:

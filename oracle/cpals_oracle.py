@@ -677,6 +677,45 @@ def load_ref_sparse_sign():
     return wrap(lib.sparse_sign), wrap(lib.sparsestack)
 
 
+def cpu_als_sweeps(T, factors, lam, sweeps, ref_norm=None, threads=0):
+    """The compiled CPU baseline (cpals_cpu.cpp: order-3 normal-equation ALS with the MTTKRP
+    in GEMM form, KRPNormal, OpenMP), built by build_oracle.py into _build/.  Returns
+    (factors, lam, fits) after `sweeps` sweeps from the given start, or None when the
+    library has not been built."""
+    import ctypes
+    from pathlib import Path
+
+    lib_path = Path(__file__).resolve().parent / "_build" / "libcpals_cpu.so"
+    if not lib_path.exists() or T.ndim != 3:
+        return None
+    lib = ctypes.CDLL(str(lib_path))
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.cpu_als_sweeps.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
+                                   dp, dp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int]
+    lib.cpu_als_sweeps.restype = ctypes.c_int
+    Tc = np.asfortranarray(T)
+    dtype = 0 if Tc.dtype == np.float64 else 1
+    if Tc.dtype not in (np.float64, np.float32):
+        Tc = np.asfortranarray(Tc, dtype=np.float64)
+        dtype = 0
+    dims = np.asarray(Tc.shape, dtype=np.int64)
+    R = factors[0].shape[1]
+    buf = np.concatenate([np.asarray(F, dtype=np.float64).reshape(-1, order="F") for F in factors])
+    lm = np.array(lam, dtype=np.float64)
+    fits = np.full(max(1, sweeps), np.nan)
+    rn = float(np.linalg.norm(Tc.reshape(-1).astype(np.float64))) if ref_norm is None else float(ref_norm)
+    st = lib.cpu_als_sweeps(dtype, Tc.ctypes.data, dims.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(R),
+                            buf.ctypes.data_as(dp), lm.ctypes.data_as(dp), int(sweeps), rn,
+                            fits.ctypes.data_as(dp), int(threads))
+    if st != 0:
+        raise ValueError("cpu_als_sweeps rejected its arguments")
+    out, o = [], 0
+    for d in Tc.shape:
+        out.append(buf[o:o + d * R].reshape(d, R, order="F").copy())
+        o += d * R
+    return out, lm, fits[:sweeps]
+
+
 # ---------------------------------------------------------------------------
 # Column-pivoted QR, SE-QRCS, omega_hadamard, the pivot-based solvers
 # ---------------------------------------------------------------------------

@@ -550,3 +550,29 @@ def test_oracle_pivot_solvers_rank400_against_exact_als(oracle):
         proj, _, _ = oracle.pivot_solver_setup(T, kind, end=800, trunc_tol=tol, rng=np.random.default_rng(2), **kw)
         Fp, lp = oracle.projected_als_check(T, F, lam, proj, oracle.FitCheck(1e-6, 20, nT))
         assert np.linalg.norm(ref - oracle.reconstruct(Fp, lp)) / np.linalg.norm(ref) < bound, kind
+
+
+@pytest.mark.parametrize("dt,tol", [(np.float64, 1e-10), (np.float32, 2e-5)])
+def test_compiled_cpu_baseline_follows_the_oracle(oracle, dt, tol):
+    # the C++/OpenMP GEMM-form ALS (the bench's compiled CPU baseline) gives the oracle's fit
+    # trajectory: the same algorithm, the MTTKRP in another summation order (and, for FP32
+    # tensors, FP32 products)
+    import importlib.util
+
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    spec = importlib.util.spec_from_file_location("build_oracle", root / "oracle" / "build_oracle.py")
+    bo = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bo)
+    if bo.build_cpu() is None:
+        pytest.skip("g++ not available")
+    rng = np.random.default_rng(12)
+    dims, R = (23, 19, 17), 6
+    T = np.asfortranarray(rng.standard_normal(dims).astype(dt))
+    F, lam = oracle.random_factors(dims, R, np.random.default_rng(3))
+    ref_norm = float(np.linalg.norm(T.astype(np.float64)))
+    chk = oracle.FitCheck(0.0, 8, ref_norm)
+    oracle.als_optimize(T.astype(np.float64), F, lam, check=chk, alg="krp", work_dtype=np.float64)
+    Fc, lc, fits = oracle.cpu_als_sweeps(T, F, lam, 8, ref_norm, threads=4)
+    assert np.max(np.abs(fits - np.asarray(chk.trajectory))) < tol

@@ -53,7 +53,7 @@ struct cpals_ctx {
   double* rgpart = nullptr;  // the solve blocks' partial Grams (null: the tiled Gram kernel)
   unsigned* gcnt = nullptr;
   int gS2[kMaxOrder] = {};
-  double* inner_rows = nullptr;  // two doubles (a double-double) per row
+  double* inner_rows = nullptr;  // three words per row: an exact fixed-point row sum
   double* nrm = nullptr;         // scratch of the ||T||^2 kernels
   DevCheck* chk = nullptr;
   DevCheck* hchk = nullptr;  // pinned mirror
@@ -600,7 +600,7 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
     if (need <= (size_t(1) << 24)) CK(dmalloc(&c->rgpart, need));
   }
   CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * (gram_tiles((int)R) + 1)));
-  CK(dmalloc(&c->inner_rows, 2 * maxI));
+  CK(dmalloc(&c->inner_rows, 3 * maxI));
   CK(dmalloc(&c->nrm, norm2_scratch_doubles()));
   CK(dmalloc(&c->chk, 1));
   CPALS_CUDA_TRY(cudaMemset(c->chk, 0, sizeof(DevCheck)));
@@ -621,7 +621,7 @@ static int after_tensor_set(cpals_ctx* c) {
   invalidate_graph(c);
   // ||T||^2 as a double-double, for the compensated fit
   CPALS_CUDA_TRY(launch_tensor_norm2(c->dT, c->tdtype, c->numel, c->nrm, c->chk, c->num_sms, c->st));
-  c->launches += (c->tdtype == CPALS_DTYPE_F32) ? 3 : 2;
+  c->launches += 3;
   if (c->tc) {
     int rc = tc_set_tensor(c->tc, c->dT, c->st);
     if (rc != CPALS_OK) return rc;

@@ -40,48 +40,70 @@ struct DevCheck {
   // device whenever the tensor is set (t2_valid = 0: not available, e.g. a non-finite entry)
   double t2_hi, t2_lo;
   int t2_valid;
-  // The fit's terms from the last mode's update, as double-doubles: <T, X> (the saved
-  // MTTKRP against the new factor, fit_check.jl:22-28) and ||X||^2 (converge_checks.jl:5-11).
-  // terms_ready says they are newer than the last check that read them.
+  // The fit's terms from the last mode's update, as exact 128-bit fixed-point sums (lo, hi
+  // words and the base, see Fx below): <T, X> (the saved MTTKRP against the new factor,
+  // fit_check.jl:22-28) and ||X||^2 (converge_checks.jl:5-11).  terms_ready says they are
+  // newer than the last check that read them.
   int terms_ready;
-  double inner_hi, inner_lo, fsq_hi, fsq_lo;
+  int inner_base, fsq_base;
+  unsigned long long inner_lo, fsq_lo;
+  long long inner_hi, fsq_hi;
 };
 
-// ---- double-double arithmetic: error-free transformations (Knuth's TwoSum, Dekker's
-// FastTwoSum, the FMA form of TwoProduct; Ogita, Rump and Oishi 2005) ----
+// ---- exact sums of doubles in 128-bit fixed point (integer pipe) ----
+// GB300 issues FP64 at 2 operations per clock per SM with a dependent latency of some 128
+// cycles, so compensated FP64 sums (chains of a dozen dependent operations per add) cost tens
+// of microseconds on one SM.  Integer adds cost a few cycles.  A finite double
+// v = +-m 2^(e - 1075) (m < 2^53, e = max(biased exponent, 1)) is added exactly as the integer
+// m 2^(e - base) into a signed 128-bit accumulator whose unit is 2^(base - 1075); with
+// base = e_max - 40 (e_max over the summed terms) the largest term stays below 2^93, so 2^34
+// terms fit, and a term far below the largest drops its bits under 2^-92 of it.  The sums
+// are exact otherwise, and independent of the order of the adds.
+constexpr int kFxHead = 40;
+constexpr int kFxBad = 4096;  // base marking a non-finite term: the sum is NaN
+__device__ __forceinline__ int fx_exp(double v) {
+  const int e = (int)((__double_as_longlong(v) >> 52) & 0x7ff);
+  return e == 0 ? 1 : e;  // 0x7ff: non-finite
+}
+__device__ __forceinline__ __int128 fx_term(double v, int base) {
+  const long long b = __double_as_longlong(v);
+  const int eb = (int)((b >> 52) & 0x7ff);
+  const unsigned long long m = (unsigned long long)(b & 0xFFFFFFFFFFFFFll) | (eb ? (1ull << 52) : 0ull);
+  const int sh = (eb ? eb : 1) - base;
+  __int128 t = 0;
+  if (sh >= 0)
+    t = (__int128)m << (sh < 80 ? sh : 80);
+  else if (sh > -64)
+    t = (__int128)(m >> (-sh));
+  return (b < 0) ? -t : t;
+}
+__device__ __forceinline__ __int128 fx_shfl_xor(__int128 q, int off) {
+  const unsigned long long lo = __shfl_xor_sync(0xffffffffu, (unsigned long long)q, off);
+  const long long hi = __shfl_xor_sync(0xffffffffu, (long long)(q >> 64), off);
+  return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+__device__ __forceinline__ __int128 fx_warp_sum(__int128 q) {
+  for (int off = 16; off > 0; off >>= 1) q += fx_shfl_xor(q, off);
+  return q;
+}
+// q 2^(from - 1075) re-expressed in units of 2^(to - 1075), to >= from (low bits dropped)
+__device__ __forceinline__ __int128 fx_align(__int128 q, int from, int to) {
+  const int d = to - from;
+  return d >= 127 ? (__int128)0 : (q >> d);
+}
+// q 2^(base - 1075) rounded to a double (two conversions and one add: within 2 ulps)
+__device__ __forceinline__ double fx_to_double(__int128 q, int base) {
+  const bool neg = q < 0;
+  const unsigned __int128 a = neg ? (unsigned __int128)(-q) : (unsigned __int128)q;
+  const double d = fma((double)(unsigned long long)(a >> 64), 18446744073709551616.0,
+                       (double)(unsigned long long)a);
+  return ldexp(neg ? -d : d, base - 1075);
+}
+
+// An unevaluated sum hi + lo (a double-double), as ||T||^2 is kept.
 struct DD {
   double hi, lo;
 };
-__device__ __forceinline__ DD dd_two_sum(double a, double b) {
-  const double s = a + b;
-  const double z = s - a;
-  return DD{s, (a - (s - z)) + (b - z)};
-}
-__device__ __forceinline__ DD dd_fast_two_sum(double a, double b) {  // |a| >= |b|
-  const double s = a + b;
-  return DD{s, b - (s - a)};
-}
-__device__ __forceinline__ DD dd_two_prod(double a, double b) {
-  const double p = a * b;
-  return DD{p, fma(a, b, -p)};
-}
-// (a + b) with relative error O(2^-104): two TwoSums, renormalised
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-  DD s = dd_two_sum(a.hi, b.hi);
-  const DD t = dd_two_sum(a.lo, b.lo);
-  s.lo += t.hi;
-  s = dd_fast_two_sum(s.hi, s.lo);
-  s.lo += t.lo;
-  return dd_fast_two_sum(s.hi, s.lo);
-}
-__device__ __forceinline__ DD dd_mul_d(DD a, double b) {
-  DD p = dd_two_prod(a.hi, b);
-  p.lo = fma(a.lo, b, p.lo);
-  return dd_fast_two_sum(p.hi, p.lo);
-}
-__device__ __forceinline__ DD dd_shfl_xor(DD a, int off) {
-  return DD{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)};
-}
 
 struct FactorSet {
   const double* F[kMaxOrder];  // FP64 factors, row-major [I_n][R]
@@ -152,7 +174,7 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
 size_t factorize_work_doubles(int R);
 
 // Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and
-// (optionally) per-row sums of M .* X for the fit, as double-doubles (two doubles per row).  `work` is the factorize workspace.
+// (optionally) per-row sums of M .* X for the fit, exact in fixed point (three words per row).  `work` is the factorize workspace.
 // With gram_part, every block also writes its rows' share of G = X^T X (upper triangle,
 // R(R+1)/2 doubles per block, solve_blocks(In, R) blocks) for launch_gram_rows.
 cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
@@ -167,8 +189,8 @@ cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned*
                              double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
                              const double* inner_rows, int64_t In, DevCheck* chk, double* traj, int64_t traj_cap,
                              cudaStream_t st, int run_check = 1);
-// Room in gram_part: nblk * R(R+1)/2 doubles of partial Grams, then two doubles per block of
-// launch_gram_rows for the ||X||^2 shares.
+// Room in gram_part: nblk * R(R+1)/2 doubles of partial Grams, then three words per block of
+// launch_gram_rows for the ||X||^2 shares (exact fixed-point sums).
 size_t gram_rows_part_doubles(int nblk, int R);
 
 // G = X^T X (row-major X, In x R) over S2 row splits; part: gram_tiles(R)*S2*256 doubles,
@@ -185,25 +207,24 @@ cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, dou
                                  double* Graw, double* lam, double* lam_inv, double* Gn, const GramSet& gs, int order,
                                  int last, const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap,
                                  cudaStream_t st, int run_check = 1);
-// Room in part for launch_gram_finalize: the tile partials and two doubles per tile.
+// Room in part for launch_gram_finalize: the tile partials and three words per tile.
 size_t gram_finalize_part_doubles(int S2, int R);
 
 // The check's update (FitCheck / NoCheck) from the terms the last mode's update saved in
 // chk, as the fused finalize runs it; one thread.
 cudaError_t launch_check_step(DevCheck* chk, double* traj, int64_t traj_cap, cudaStream_t st);
 
-// ||T||^2 as a double-double into chk->t2_hi / t2_lo (t2_valid = 1), for the compensated
-// fit.  FP32 tensors: the squares are exact 48-bit integers times powers of two, summed
-// exactly in 128-bit fixed point anchored at the largest exponent (two passes: the largest
-// |entry|, then the sum; integer work only).  FP64 tensors: TwoProduct squares summed in
-// double-double.  scratch: norm2_scratch_doubles() doubles.
+// ||T||^2 as a double-double into chk->t2_hi / t2_lo (t2_valid = 1), for the fit.  Two
+// passes: the largest |entry|, then the squares summed exactly in 128-bit fixed point
+// anchored at it (FP32 entries: m^2 is an exact 48-bit integer; FP64 entries: each square
+// split exactly by TwoProduct, both parts added).  scratch: norm2_scratch_doubles() doubles.
 size_t norm2_scratch_doubles();
 cudaError_t launch_tensor_norm2(const void* T, int tdtype, int64_t n, double* scratch, DevCheck* chk, int num_sms,
                                 cudaStream_t st);
 
 // lambda = sqrt(diag Graw), G_n = Graw ./ (lambda lambda^T); on the last mode also the fit
 // and the device check update (trajectory entry per sweep).  inner_rows holds two doubles
-// (a double-double) per row.
+// per row: an exact fixed-point row sum (lo, hi words and its base).
 cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st);

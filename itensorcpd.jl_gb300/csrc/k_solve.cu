@@ -536,29 +536,25 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 }
 
 // ---------------- FP32 sweep (split-BF16 path) ----------------
-// A pivoted symmetric sweep in FP32 (this part issues FP32 FMAs at 64x its FP64
-// rate, with ~4-cycle latency).  V is formed in FP64 exactly as above and kept in the
-// workspace; W = -A is the FP32 inverse.  The solve then refines X once with the FP64
-// residual (mixed-precision iterative refinement: X += (M - X V) W), which brings X to FP64
-// accuracy while kappa(V) eps_32 << 1.  A pivot below 1e-3 of the largest diagonal entry (or
-// a NaN, or a rank below R) leaves info->refine = 0 and the FP64 sweep takes over.
-
-// Layout and schedule.  The symmetric A lives in registers: thread t of warps 0-3 holds
-// columns 4 (t >> 2) .. + 3, rows 32 (t & 3) .. + 31 (both triangles).  The sweep keeps A
-// exactly symmetric by updating with u = a sqrt(1 / d_k) (a = column k, d_k the pivot):
-//   A(i,c) -= u_i u_c  for i, c != k;  with u_k = (1 - 1/d_k) / sqrt(1/d_k) the same FMA
-// leaves A(i,k) = a_i / d_k and A(k,c) = a_c / d_k (Gauss-Jordan form); the pivot's own
-// entry, -1 / d_k, and every diagonal entry are tracked by warp 4 in s_d.  Per pivot: the
-// four owners of column k publish u (a uniform switch picks the column: no dynamic register
-// indexing) -> barrier -> owners update their 128 entries; warp 4 updates the diagonal and
-// picks the next pivot -> barrier.  The pivot is the largest unswept diagonal entry, the
-// lowest index among values equal to 2^-16 relative (a packed key, one warp max); any choice
-// is fine here because the solve refines X in FP64, and a pivot below 1e-3 of the largest
-// diagonal entry hands the factorisation to the FP64 sweep.  V is formed beforehand by
-// k_form_v32 over the whole grid.  (A probe of this schedule on one SM: 0.84 k cycles per
-// pivot at R = 128, the earlier one-entry-per-thread sweep 2.6 k.)
-constexpr int FT32 = 160;
-constexpr int kOwnWarps32 = 4, kPivWarp32 = 4;
+// A blocked symmetric sweep in FP32 (this part issues FP32 FMAs at 64x its FP64 rate).  V is
+// formed in FP64 exactly as above and kept in the workspace; W = V^{-1} in FP32 goes beside
+// it.  The solve then refines X once with a compensated residual (mixed-precision iterative
+// refinement: X += (M - X V) W), which brings X to FP64 accuracy while kappa(V) eps_32 << 1.
+// A pivot below 1e-3 of the largest diagonal entry (or a NaN) leaves info->refine = 0 and the
+// FP64 pivoted sweep takes over, as it does for every rank-deficient V.
+//
+// The sweep operator (Goodnight 1979) on an index block P of a symmetric A, with D = A_PP:
+//   A_PP <- -D^{-1},  A_iP <- A_iP D^{-1} (= B_i),  A_ij <- A_ij - B_i A_Pj   (i, j not in P)
+// is the composition of the single-index sweeps over P; after every block A = -V^{-1}.  The
+// indices are swept in blocks of 32 in their natural order (V is symmetric positive definite
+// whenever this path is taken; any pivot order is sound because the solve refines X):
+//   (a) warp 0 sweeps D in shared memory, one index at a time, rows split over the lanes;
+//   (b) all warps form B = A_{.P} D^{-1} and keep A_{.P} (both transposed, 32 x R);
+//   (c) all warps apply the rank-32 update to the rest of A in 4 x 4 register tiles and write
+//       the swept blocks back.
+// That is three barriers per block (twelve at R = 128) instead of two per index.
+constexpr int FT32 = 512;
+constexpr int kBlk32 = 32;
 // The refinement's FP32 operands, written by the FP32 sweep into the workspace after the
 // FP64 factorisation's area: [W | V_hi | V_lo], each R^2 floats padded to a multiple of four
 // (16-byte aligned, so the solve stages them with 16-byte asynchronous copies).  V = V_hi +
@@ -567,18 +563,10 @@ __host__ __device__ inline int rr4(int R) { return (R * R + 3) & ~3; }
 __host__ __device__ inline size_t ops32_offset_doubles(int R) {
   return (5 * (size_t)R * R + 4 * (size_t)R + 64 + 1) & ~(size_t)1;
 }
-__device__ __forceinline__ int pivot_key(float v, int i) {
-  const int b = __float_as_int(v);
-  if ((b & 0x7fffffff) > 0x7f800000) return INT_MAX;  // NaN first: it stops the sweep
-  return (b & ~0x7f) | (127 - i);
-}
-__device__ __forceinline__ int upad(int i) { return i + 4 * (i >> 5); }  // row quarters 36 floats apart
-template <int C>
-__device__ __forceinline__ void publish_u(const float (&acc)[4][32], float sc, float* s_u, int qr) {
-  float4* dst = reinterpret_cast<float4*>(s_u + 36 * qr);
-#pragma unroll
-  for (int v = 0; v < 8; ++v)
-    dst[v] = make_float4(acc[C][4 * v] * sc, acc[C][4 * v + 1] * sc, acc[C][4 * v + 2] * sc, acc[C][4 * v + 3] * sc);
+__host__ __device__ inline int ld32(int R) { return ((R + 3) & ~3) + 4; }  // row stride of A, B^T, C^T
+__host__ __device__ inline size_t factorize32_smem_bytes(int R) {
+  const int ld = ld32(R);
+  return sizeof(float) * ((size_t)R * ld + 2 * (size_t)kBlk32 * ld + (size_t)kBlk32 * 33 + 64);
 }
 // V = Hadamard product of the other modes' Grams (FP64, in mode order, as the FP64 sweep
 // forms it), written as the FP32 pair V_hi + V_lo into the refinement operands.  One
@@ -599,118 +587,132 @@ __global__ void __launch_bounds__(256) k_form_v32(GramSet gs, int order, int ski
 
 __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__ ops, SolveInfo* info, DevCheck* chk) {
   if (done_flag(chk)) return;
-  __shared__ __align__(16) float s_u[144];
-  __shared__ __align__(16) float s_d[128];
-  __shared__ float s_uk, s_sc;
-  __shared__ int s_p, s_stop;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const float* __restrict__ Vh = ops + rr4(R);  // V_hi from k_form_v32 (its upper triangle is used)
-  for (int k = tid; k < 144; k += blockDim.x) {
-    s_u[k] = 0.f;
-    if (k < 128) s_d[k] = 0.f;
+  extern __shared__ __align__(16) float fsm[];
+  const int ld = ld32(R);
+  float* A = fsm;                            // R x ld, row-major, both triangles
+  float* Bt = A + (size_t)R * ld;            // 32 x ld: B^T, row p = column p of B = A_{.P} D^{-1}
+  float* Ct = Bt + (size_t)kBlk32 * ld;      // 32 x ld: A_{.P}^T before the block
+  float* Dm = Ct + (size_t)kBlk32 * ld;      // 32 x 33: the diagonal block, swept in place
+  float* misc = Dm + kBlk32 * 33;            // [0]: pivot threshold, [1]: failure flag
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+  const float* __restrict__ Vh = ops + rr4(R);  // V_hi from k_form_v32
+  const int Rp = (R + 3) & ~3;
+  for (int e = tid; e < R * ld; e += nt) {
+    const int i = e / ld, j = e - i * ld;
+    A[e] = (j < R) ? Vh[(size_t)i * R + j] : 0.f;
   }
-  __syncthreads();
-  const int cg = tid >> 2, qr = tid & 3;
-  const bool own = warp < kOwnWarps32 && 4 * cg < R && 32 * qr < R;
-  float acc[4][32];
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int i = 32 * qr + j, col = 4 * cg + c;
-      acc[c][j] = (own && i < R && col < R) ? ((i <= col) ? Vh[(size_t)i * R + col] : Vh[(size_t)col * R + i]) : 0.f;
-    }
-  // warp 4: diagonal entries 4 lane .. 4 lane + 3 (registers and s_d), swept flags, pivot
-  unsigned swept = 0;
-  float r_dk = 0.f, r_maxd = 0.f;
-  auto pick = [&](const float* dv) {
-    int best = INT_MIN;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = 4 * lane + q;
-      const int key = (i < R && !((swept >> q) & 1u)) ? pivot_key(dv[q], i) : INT_MIN;
-      best = max(best, key);
-    }
-    const int mk = __reduce_max_sync(0xffffffffu, best);
-    const int p = (mk == INT_MAX || mk == INT_MIN) ? 0 : 127 - (mk & 0x7f);
-    const int q = p & 3;
-    const float mine = (q == 0) ? dv[0] : (q == 1) ? dv[1] : (q == 2) ? dv[2] : dv[3];
-    const float pv = __shfl_sync(0xffffffffu, mine, p >> 2);
-    const int stop = (mk == INT_MAX) || (mk == INT_MIN) || !(pv > 1e-3f * r_maxd) || p >= R;
-    const float sc = rsqrtf(pv);  // sqrt(1 / d_k)
-    const float dk = sc * sc;
-    r_dk = dk;
-    if (lane == 0) {
-      s_stop = stop;
-      s_p = p;
-      s_sc = sc;
-      s_uk = (1.0f - dk) * pv * sc;  // (1 - 1/d_k) / sqrt(1/d_k)
-    }
-  };
-  if (warp == kPivWarp32) {
-    float dv[4];
+  for (int e = tid; e < 2 * kBlk32 * ld; e += nt) Bt[e] = 0.f;  // (Ct follows Bt)
+  if (warp == 0) {
     float md = 0.f;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = 4 * lane + q;
-      dv[q] = (i < R) ? Vh[(size_t)i * R + i] : 0.f;
-      s_d[i] = dv[q];
-      md = fmaxf(md, dv[q]);
-    }
+    for (int i = lane; i < R; i += 32) md = fmaxf(md, Vh[(size_t)i * R + i]);
     for (int off = 16; off > 0; off >>= 1) md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, off));
-    r_maxd = md;
-    pick(dv);
+    if (lane == 0) {
+      misc[0] = 1e-3f * md;
+      misc[1] = 0.f;
+    }
   }
   __syncthreads();
-  int ok = 1;
-  for (int j = 0; j < R; ++j) {
-    if (s_stop) {
-      ok = 0;
-      break;
-    }
-    const int k = s_p;
-    if (own && cg == (k >> 2)) {  // publish u for column k
-      const float sc = s_sc;
-      switch (k & 3) {
-        case 0: publish_u<0>(acc, sc, s_u, qr); break;
-        case 1: publish_u<1>(acc, sc, s_u, qr); break;
-        case 2: publish_u<2>(acc, sc, s_u, qr); break;
-        default: publish_u<3>(acc, sc, s_u, qr); break;
+  const int ntile = Rp / 4;
+  for (int p0 = 0; p0 < R; p0 += kBlk32) {
+    const int pb = min(kBlk32, R - p0);
+    // (a) sweep of the diagonal block D = A_PP by warp 0: lane i owns row i of Dm
+    if (warp == 0) {
+      for (int e = lane; e < pb * pb; e += 32) Dm[(e / pb) * 33 + e % pb] = A[(size_t)(p0 + e / pb) * ld + p0 + e % pb];
+      __syncwarp();
+      const float thr = misc[0];
+      bool bad = false;
+      for (int k = 0; k < pb; ++k) {
+        const float d = Dm[k * 33 + k];
+        bad = bad || !(d > thr) || !(d < INFINITY);
+        const float rd = 1.0f / d;
+        const float f = (lane < pb) ? Dm[lane * 33 + k] * rd : 0.f;  // D(i, k) / d
+        __syncwarp();
+        if (lane < pb && lane != k) {
+          float* row = Dm + lane * 33;
+          const float* rk = Dm + k * 33;
+          for (int c = 0; c < pb; ++c)
+            if (c != k) row[c] = fmaf(-f, rk[c], row[c]);
+          row[k] = f;
+        }
+        __syncwarp();
+        if (lane < pb) Dm[k * 33 + lane] = (lane == k) ? -rd : f;  // row k: D(k, c) / d (symmetric)
+        __syncwarp();
       }
-      if ((k >> 5) == qr) s_u[upad(k)] = s_uk;
+      if (lane == 0 && bad) misc[1] = 1.f;
     }
     __syncthreads();
-    if (own) {
-      const float4 uc = *reinterpret_cast<const float4*>(s_u + upad(4 * cg));
-      const float ucs[4] = {uc.x, uc.y, uc.z, uc.w};
-      const float4* src = reinterpret_cast<const float4*>(s_u + 36 * qr);
+    if (misc[1] != 0.f) break;
+    // (b) B = A_{.P} D^{-1} (D^{-1} = -Dm) and C = A_{.P}, both transposed, for every row i
+    for (int e = tid; e < kBlk32 * R; e += nt) {
+      const int q = e & 31, i = e >> 5;  // lanes take the 32 block columns of one row
+      float b = 0.f, c = 0.f;
+      if (q < pb) {
+        const float* Ai = A + (size_t)i * ld + p0;
+        c = Ai[q];
+        for (int pp = 0; pp < pb; ++pp) b = fmaf(Ai[pp], -Dm[pp * 33 + q], b);
+      }
+      Bt[(size_t)q * ld + i] = b;
+      Ct[(size_t)q * ld + i] = c;
+    }
+    __syncthreads();
+    // (c) the rank-pb update of the rest, and the swept blocks written back, in 4 x 4 tiles
+    // (tiles never straddle the block: it starts at a multiple of 32)
+    for (int t = tid; t < ntile * ntile; t += nt) {
+      const int ti = t / ntile, tj = t - ti * ntile;
+      const int i0 = 4 * ti, j0 = 4 * tj;
+      const bool inI = (i0 >= p0 && i0 < p0 + pb), inJ = (j0 >= p0 && j0 < p0 + pb);
+      float v[4][4];
+      if (inI && inJ) {
 #pragma unroll
-      for (int v = 0; v < 8; ++v) {
-        const float4 x = src[v];
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          acc[c][4 * v] = fmaf(-x.x, ucs[c], acc[c][4 * v]);
-          acc[c][4 * v + 1] = fmaf(-x.y, ucs[c], acc[c][4 * v + 1]);
-          acc[c][4 * v + 2] = fmaf(-x.z, ucs[c], acc[c][4 * v + 2]);
-          acc[c][4 * v + 3] = fmaf(-x.w, ucs[c], acc[c][4 * v + 3]);
+          for (int b = 0; b < 4; ++b)
+            v[a][b] = (i0 + a < p0 + pb && j0 + b < p0 + pb) ? Dm[(i0 + a - p0) * 33 + (j0 + b - p0)] : 0.f;
+      } else if (inI) {  // A_Pj = B_j^T
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const float4 x = *reinterpret_cast<const float4*>(Bt + (size_t)(i0 + a - p0) * ld + j0);
+          v[a][0] = x.x;
+          v[a][1] = x.y;
+          v[a][2] = x.z;
+          v[a][3] = x.w;
+        }
+      } else if (inJ) {  // A_iP = B_i
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const float4 x = *reinterpret_cast<const float4*>(Bt + (size_t)(j0 + b - p0) * ld + i0);
+          v[0][b] = x.x;
+          v[1][b] = x.y;
+          v[2][b] = x.z;
+          v[3][b] = x.w;
+        }
+      } else {  // A_ij - sum_p B(i, p) C(j, p)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const float4 x = *reinterpret_cast<const float4*>(A + (size_t)(i0 + a) * ld + j0);
+          v[a][0] = x.x;
+          v[a][1] = x.y;
+          v[a][2] = x.z;
+          v[a][3] = x.w;
+        }
+        for (int pp = 0; pp < pb; ++pp) {
+          const float4 bi = *reinterpret_cast<const float4*>(Bt + (size_t)pp * ld + i0);
+          const float4 cj = *reinterpret_cast<const float4*>(Ct + (size_t)pp * ld + j0);
+          const float bv[4] = {bi.x, bi.y, bi.z, bi.w}, cv[4] = {cj.x, cj.y, cj.z, cj.w};
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) v[a][b] = fmaf(-bv[a], cv[b], v[a][b]);
         }
       }
-    } else if (warp == kPivWarp32) {
-      const float4 u4 = reinterpret_cast<const float4*>(s_u + 4 * (lane >> 3))[lane];
-      const float4 d4 = reinterpret_cast<const float4*>(s_d)[lane];
-      float dv[4] = {fmaf(-u4.x, u4.x, d4.x), fmaf(-u4.y, u4.y, d4.y), fmaf(-u4.z, u4.z, d4.z),
-                     fmaf(-u4.w, u4.w, d4.w)};
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const bool isk = (4 * lane + q) == k;
-        dv[q] = isk ? -r_dk : dv[q];
-        swept |= isk ? (1u << q) : 0u;
-      }
-      reinterpret_cast<float4*>(s_d)[lane] = make_float4(dv[0], dv[1], dv[2], dv[3]);
-      if (j + 1 < R) pick(dv);
+      for (int a = 0; a < 4; ++a)
+        if (i0 + a < R) *reinterpret_cast<float4*>(A + (size_t)(i0 + a) * ld + j0) =
+            make_float4(v[a][0], v[a][1], v[a][2], v[a][3]);
     }
     __syncthreads();
   }
+  const int ok = (misc[1] == 0.f) ? 1 : 0;
   if (tid == 0) {
     info->refine = ok;
     if (ok) {
@@ -719,15 +721,12 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
       info->qr_rank = R;
     }
   }
-  if (!ok || !own) return;
-  // W = -A (FP32): column-major = row-major (A is exactly symmetric); the diagonal from s_d
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-#pragma unroll
-    for (int jj = 0; jj < 32; ++jj) {
-      const int i = 32 * qr + jj, col = 4 * cg + c;
-      if (i < R && col < R) ops[(size_t)col * R + i] = (i == col) ? -s_d[i] : -acc[c][jj];
-    }
+  if (!ok) return;
+  // W = -A (FP32): column-major = row-major (A is symmetric)
+  for (int e = tid; e < R * R; e += nt) {
+    const int c = e / R, i = e - c * R;
+    ops[e] = -A[(size_t)i * ld + c];
+  }
 }
 
 // ---------------- solve: X = M W^T ----------------
@@ -956,16 +955,23 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
   }
   if (!inner_rows) return;
   __syncthreads();
-  // per-row sum of M .* X for the fit's <T, X>, as a double-double: each product split
-  // exactly by TwoProduct, summed error-free along the row and across the lanes
+  // per-row sum of M .* X for the fit's <T, X>, exact in 128-bit fixed point (one warp per
+  // row: the row's largest exponent, then the integer sum); stored as (lo, hi, base)
   const int lane = tid & 31, warp = tid >> 5, nw = SOLVE_T >> 5;
+  long long* ir = reinterpret_cast<long long*>(inner_rows);
   for (int row = warp; row < rows; row += nw) {
-    DD v{0.0, 0.0};
-    for (int kk = lane; kk < R; kk += 32) v = dd_add(v, dd_two_prod(Ms[row * R + kk], Xs[row * R + kk]));
-    for (int off = 16; off > 0; off >>= 1) v = dd_add(v, dd_shfl_xor(v, off));
+    int emax = 1;
+    for (int kk = lane; kk < R; kk += 32) emax = max(emax, fx_exp(Ms[row * R + kk] * Xs[row * R + kk]));
+    emax = __reduce_max_sync(0xffffffffu, emax);
+    const int base = (emax == 0x7ff) ? kFxBad : emax - kFxHead;
+    __int128 q = 0;
+    if (base != kFxBad)
+      for (int kk = lane; kk < R; kk += 32) q += fx_term(Ms[row * R + kk] * Xs[row * R + kk], base);
+    q = fx_warp_sum(q);
     if (lane == 0) {
-      inner_rows[2 * (r0 + row)] = v.hi;
-      inner_rows[2 * (r0 + row) + 1] = v.lo;
+      ir[3 * (r0 + row)] = (long long)(unsigned long long)q;
+      ir[3 * (r0 + row) + 1] = (long long)(q >> 64);
+      ir[3 * (r0 + row) + 2] = base;
     }
   }
 }
@@ -984,47 +990,67 @@ __device__ double block_tree_sum(double v, double* sv) {
   return t;
 }
 
-// Block-wide double-double sum (a fixed tree: lanes, then warps); every thread gets it.
-__device__ DD block_sum_dd(DD v, double* sv) {  // sv: 64 doubles
+// Block-wide helpers for the exact fixed-point sums: the largest int, and the sum of the
+// threads' 128-bit values (every thread gets both).
+__device__ int block_max_int(int v, int* si) {  // si: 32 ints
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int off = 16; off > 0; off >>= 1) v = dd_add(v, dd_shfl_xor(v, off));
+  v = __reduce_max_sync(0xffffffffu, v);
   __syncthreads();
-  if (lane == 0) {
-    sv[2 * w] = v.hi;
-    sv[2 * w + 1] = v.lo;
-  }
+  if (lane == 0) si[w] = v;
   __syncthreads();
-  DD t = (lane < nw) ? DD{sv[2 * lane], sv[2 * lane + 1]} : DD{0.0, 0.0};
-  for (int off = 16; off > 0; off >>= 1) t = dd_add(t, dd_shfl_xor(t, off));
+  int t = (lane < nw) ? si[lane] : INT_MIN;
+  t = __reduce_max_sync(0xffffffffu, t);
   __syncthreads();
   return t;
 }
+__device__ __int128 block_sum_fx(__int128 q, long long* sl) {  // sl: 64 words
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  q = fx_warp_sum(q);
+  __syncthreads();
+  if (lane == 0) {
+    sl[2 * w] = (long long)(unsigned long long)q;
+    sl[2 * w + 1] = (long long)(q >> 64);
+  }
+  __syncthreads();
+  __int128 t = 0;
+  if (lane < nw)
+    t = (__int128)(((unsigned __int128)(unsigned long long)sl[2 * lane + 1] << 64) |
+                   (unsigned long long)sl[2 * lane]);
+  t = fx_warp_sum(t);
+  __syncthreads();
+  return t;
+}
+__device__ __forceinline__ __int128 fx_join(unsigned long long lo, long long hi) {
+  return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
 
 // The fit 1 - ||T - X|| / ||T|| with ||T - X||^2 = ||T||^2 + ||X||^2 - 2 |<T, X>|
-// (fit_check.jl:26-32), from the saved double-double terms.  Near fit -> 1 the three terms
-// cancel, so the combination is done in double-double arithmetic and the square root gets
-// one Newton correction from the double-double radicand.  ||T||^2 is the device's own
-// double-double when ref_norm is norm(T) (equal to it within 1e-15 relative), else the
-// exact square of ref_norm.
+// (fit_check.jl:26-32).  Near fit -> 1 the three terms cancel, so the combination is done
+// exactly: <T, X> and ||X||^2 arrive as exact fixed-point sums, ||T||^2 (the device's own,
+// when ref_norm is norm(T) to 1e-15 relative; else the exact square of ref_norm) joins them at
+// a common base, and only the small result is rounded to a double.
 __device__ double compensated_fit(const DevCheck& k) {
   const double rn = k.ref_norm;
   if (!(rn > 0.0)) return NAN;
-  DD rn2;
-  if (k.t2_valid && fabs(rn - sqrt(k.t2_hi)) <= 1e-15 * rn)
-    rn2 = DD{k.t2_hi, k.t2_lo};
-  else
-    rn2 = dd_two_prod(rn, rn);
-  DD inner{k.inner_hi, k.inner_lo};
-  if (inner.hi < 0.0) inner = DD{-inner.hi, -inner.lo};
-  DD s = dd_add(rn2, DD{k.fsq_hi, k.fsq_lo});
-  s = dd_add(s, DD{-2.0 * inner.hi, -2.0 * inner.lo});
-  if (s.hi < 0.0) s = DD{-s.hi, -s.lo};
-  double r = sqrt(s.hi);
-  if (r > 0.0) {
-    const DD rr = dd_two_prod(r, r);
-    r += (((s.hi - rr.hi) - rr.lo) + s.lo) / (2.0 * r);
+  double ta, tb;
+  if (k.t2_valid && fabs(rn - sqrt(k.t2_hi)) <= 1e-15 * rn) {
+    ta = k.t2_hi;
+    tb = k.t2_lo;
+  } else {
+    ta = rn * rn;
+    tb = fma(rn, rn, -ta);
   }
-  return 1.0 - r / rn;
+  if (k.inner_base == kFxBad || k.fsq_base == kFxBad || !isfinite(ta)) return NAN;
+  const int tbase = fx_exp(ta) - kFxHead;
+  const int c = max(max(k.inner_base, k.fsq_base), tbase) + 2;  // (+2: room for the sum)
+  const __int128 t2 = fx_align(fx_term(ta, tbase) + fx_term(tb, tbase), tbase, c);
+  __int128 in = fx_align(fx_join(k.inner_lo, k.inner_hi), k.inner_base, c);
+  if (in < 0) in = -in;
+  const __int128 fs = fx_align(fx_join(k.fsq_lo, k.fsq_hi), k.fsq_base, c);
+  __int128 r2 = t2 + fs - 2 * in;
+  if (r2 < 0) r2 = -r2;
+  const double nr = sqrt(fx_to_double(r2, c));
+  return 1.0 - nr / rn;
 }
 
 // The check's update after a sweep (FitCheck fit_check.jl:24-66, NoCheck no_check.jl:11-20)
@@ -1087,13 +1113,13 @@ struct FinalizeArgs {
   GramSet gs;
   int order;
   int last;
-  const double* inner_rows;
+  const long long* inner_rows_fx;  // per row: an exact fixed-point sum (lo, hi, base)
   int64_t In;
   DevCheck* chk;
   double* traj;
   int64_t traj_cap;
   int mode;       // the mode whose raw Gram is being finalised
-  double* fpart;  // per-tile double-double partials of ||X||^2 (fused path), or null
+  double* fpart;  // per-tile (per-block) exact shares of ||X||^2 (lo, hi, base), or null
   int ntiles;
   int run_check;  // 0: only save the fit's terms (a caller-driven sweep runs the check)
 };
@@ -1137,32 +1163,57 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
     }
   }
   if (!fa.last) return;
-  __shared__ double sv2[64];
-  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28), summed in
-  // double-double from the solve's per-row double-doubles
-  DD ia{0.0, 0.0};
-  for (int64_t i = tid; i < fa.In; i += nt) ia = dd_add(ia, DD{fa.inner_rows[2 * i], fa.inner_rows[2 * i + 1]});
-  const DD inner = block_sum_dd(ia, sv2);
-  // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11).  With the
-  // per-tile partials (fused path) it is their double-double sum in tile order; otherwise
-  // each term is formed as a double-double product.
-  DD ps{0.0, 0.0};
-  if (fa.fpart)
-    for (int t = tid; t < fa.ntiles; t += nt)
-      ps = dd_add(ps, DD{__ldcg(&fa.fpart[2 * t]), __ldcg(&fa.fpart[2 * t + 1])});
-  for (int e = tid; !fa.fpart && e < n; e += nt) {
-    DD h{fa.gs.G[0][e], 0.0};
-    for (int m = 1; m < fa.order; ++m) h = dd_mul_d(h, fa.gs.G[m][e]);
-    const int r = e / R, c = e - r * R;
-    ps = dd_add(ps, dd_mul_d(dd_mul_d(h, s_lam[r]), s_lam[c]));
+  __shared__ int si[32];
+  __shared__ long long sl[64];
+  // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28): the rows' exact
+  // fixed-point sums, aligned to the largest row base (+8: room for 2^36 rows) and added
+  const long long* ir = fa.inner_rows_fx;
+  int bmax = INT_MIN;
+  for (int64_t i = tid; i < fa.In; i += nt) bmax = max(bmax, (int)ir[3 * i + 2]);
+  bmax = block_max_int(bmax, si);
+  const int ib = (bmax == kFxBad) ? kFxBad : bmax + 8;
+  __int128 qi = 0;
+  if (ib != kFxBad)
+    for (int64_t i = tid; i < fa.In; i += nt)
+      qi += fx_align(fx_join((unsigned long long)ir[3 * i], ir[3 * i + 1]), (int)ir[3 * i + 2], ib);
+  const __int128 inner = block_sum_fx(qi, sl);
+  // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11): with the per-tile
+  // (per-block) shares of the fused path, their exact sums; otherwise each term formed here
+  int fb;
+  __int128 qf = 0;
+  if (fa.fpart) {
+    const long long* fp = reinterpret_cast<const long long*>(fa.fpart);
+    int m = INT_MIN;
+    for (int t = tid; t < fa.ntiles; t += nt) m = max(m, (int)__ldcg(&fp[3 * t + 2]));
+    m = block_max_int(m, si);
+    fb = (m == kFxBad) ? kFxBad : m + 8;
+    if (fb != kFxBad)
+      for (int t = tid; t < fa.ntiles; t += nt)
+        qf += fx_align(fx_join((unsigned long long)__ldcg(&fp[3 * t]), __ldcg(&fp[3 * t + 1])),
+                       (int)__ldcg(&fp[3 * t + 2]), fb);
+  } else {
+    auto term = [&](int e) {
+      double h = fa.gs.G[0][e];
+      for (int m = 1; m < fa.order; ++m) h *= fa.gs.G[m][e];
+      const int r = e / R, c2 = e - r * R;
+      return h * s_lam[r] * s_lam[c2];
+    };
+    int m = 1;
+    for (int e = tid; e < n; e += nt) m = max(m, fx_exp(term(e)));
+    m = block_max_int(m, si);
+    fb = (m == 0x7ff) ? kFxBad : m - kFxHead + 8;
+    if (fb != kFxBad)
+      for (int e = tid; e < n; e += nt) qf += fx_term(term(e), fb);
   }
-  const DD fact_square = block_sum_dd(ps, sv2);
+  const __int128 fact_square = block_sum_fx(qf, sl);
   if (tid != 0) return;
   DevCheck& k = *fa.chk;
-  k.inner_hi = inner.hi;
-  k.inner_lo = inner.lo;
-  k.fsq_hi = fact_square.hi;
-  k.fsq_lo = fact_square.lo;
+  k.inner_lo = (unsigned long long)inner;
+  k.inner_hi = (long long)(inner >> 64);
+  k.inner_base = ib;
+  k.fsq_lo = (unsigned long long)fact_square;
+  k.fsq_hi = (long long)(fact_square >> 64);
+  k.fsq_base = fb;
   k.terms_ready = 1;
   if (fa.run_check) check_update(k, fa.traj, fa.traj_cap);
 }
@@ -1251,18 +1302,23 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ X, int6
   if (fa.last) {
     // this tile's share of ||X||^2 = sum(Graw .* prod_{m != mode} G_m) (lambda_r lambda_c
     // times the normalised Gram of this mode is its raw Gram); off-diagonal tiles count twice
-    // (double-double products and sums: the fit's terms cancel near fit -> 1)
-    DD h{0.0, 0.0};
+    // (an exact fixed-point sum: the fit's terms cancel near fit -> 1)
+    double h = 0.0;
     if (r1 < R && r2 < R) {
-      h.hi = (ti == tj) ? sum : 2.0 * sum;
+      h = (ti == tj) ? sum : 2.0 * sum;
       for (int m = 0; m < fa.order; ++m)
-        if (m != fa.mode) h = dd_mul_d(h, fa.gs.G[m][(size_t)r1 * R + r2]);
+        if (m != fa.mode) h *= fa.gs.G[m][(size_t)r1 * R + r2];
     }
-    __shared__ double sv_t[64];
-    const DD tsum = block_sum_dd(h, sv_t);
+    __shared__ int si_t[32];
+    __shared__ long long sl_t[64];
+    const int em = block_max_int(fx_exp(h), si_t);
+    const int base = (em == 0x7ff) ? kFxBad : em - kFxHead;
+    const __int128 q = block_sum_fx(base == kFxBad ? (__int128)0 : fx_term(h, base), sl_t);
     if (threadIdx.x == 0) {
-      fa.fpart[2 * tile] = tsum.hi;
-      fa.fpart[2 * tile + 1] = tsum.lo;
+      long long* fp = reinterpret_cast<long long*>(fa.fpart);
+      fp[3 * tile] = (long long)(unsigned long long)q;
+      fp[3 * tile + 1] = (long long)(q >> 64);
+      fp[3 * tile + 2] = base;
     }
   }
   __threadfence();
@@ -1285,7 +1341,6 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
   if (done_flag(chk)) return;
   __shared__ double red[8][33];
   __shared__ int s_last;
-  __shared__ double sv_t[64];
   const int T = R * (R + 1) / 2;
   const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
@@ -1305,7 +1360,7 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
   }
   red[sl][lane] = (a0 + a1) + (a2 + a3);
   __syncthreads();
-  DD h{0.0, 0.0};
+  double h = 0.0;
   if (sl == 0 && e < T) {
     double sum = 0.0;
     for (int q = 0; q < 8; ++q) sum += red[q][lane];
@@ -1320,17 +1375,21 @@ __global__ void __launch_bounds__(256) k_gram_rows(const double* __restrict__ gp
     }
     G[(size_t)a * R + c] = sum;
     G[(size_t)c * R + a] = sum;
-    if (fa.last) {  // this entry's share of ||X||^2, a double-double product
-      h.hi = (a == c) ? sum : 2.0 * sum;
+    if (fa.last) {  // this entry's share of ||X||^2
+      h = (a == c) ? sum : 2.0 * sum;
       for (int m = 0; m < fa.order; ++m)
-        if (m != fa.mode) h = dd_mul_d(h, fa.gs.G[m][(size_t)a * R + c]);
+        if (m != fa.mode) h *= fa.gs.G[m][(size_t)a * R + c];
     }
   }
-  if (fa.last) {
-    const DD tsum = block_sum_dd(h, sv_t);
-    if (threadIdx.x == 0) {
-      fa.fpart[2 * blockIdx.x] = tsum.hi;
-      fa.fpart[2 * blockIdx.x + 1] = tsum.lo;
+  if (fa.last && sl == 0) {  // the block's 32 shares (warp 0), summed exactly in fixed point
+    const int em = __reduce_max_sync(0xffffffffu, fx_exp(h));
+    const int base = (em == 0x7ff) ? kFxBad : em - kFxHead;
+    const __int128 q = fx_warp_sum(base == kFxBad ? (__int128)0 : fx_term(h, base));
+    if (lane == 0) {
+      long long* fp = reinterpret_cast<long long*>(fa.fpart);
+      fp[3 * blockIdx.x] = (long long)(unsigned long long)q;
+      fp[3 * blockIdx.x + 1] = (long long)(q >> 64);
+      fp[3 * blockIdx.x + 2] = base;
     }
   }
   __threadfence();
@@ -1416,8 +1475,6 @@ __global__ void k_reduce_partials(const PT* __restrict__ part, int S, int64_t n,
 // negative; bits below the unit, less than 2^-78 of the largest square each, are dropped).
 // A square is below 2^80 units, so 2^40 entries stay below 2^120: no overflow.  Integer sums
 // are associative, so the result does not depend on the order of the atomics.
-constexpr int kNormMaxBlocks = 1024;
-
 __global__ void __launch_bounds__(256) k_absmax_bits(const float* __restrict__ T, int64_t n,
                                                      unsigned* __restrict__ out) {
   unsigned m = 0;
@@ -1461,48 +1518,75 @@ __global__ void __launch_bounds__(256) k_sumsq_f32(const float* __restrict__ T, 
   }
 }
 
-// FP64 tensors: TwoProduct squares summed in double-double, one partial per block.
+// FP64 tensors: the same two passes; each square is split exactly by TwoProduct
+// (x^2 = p + e) and both parts are added in 128-bit fixed point anchored at the largest
+// square (6 more bits of headroom: 2^40 entries).
+__global__ void __launch_bounds__(256) k_absmax_bits64(const double* __restrict__ T, int64_t n,
+                                                       unsigned long long* __restrict__ out) {
+  unsigned long long m = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    m = max(m, (unsigned long long)__double_as_longlong(T[i]) & 0x7fffffffffffffffull);
+  for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__device__ __forceinline__ int sumsq64_base(unsigned long long mb) {
+  if (mb >= 0x7ff0000000000000ull) return kFxBad;
+  const double x = __longlong_as_double((long long)mb);
+  const double p = x * x;
+  if (!(p < INFINITY)) return kFxBad;
+  return fx_exp(p) - kFxHead + 6;
+}
+
 __global__ void __launch_bounds__(256) k_sumsq_f64(const double* __restrict__ T, int64_t n,
-                                                   double* __restrict__ part) {
-  __shared__ double sv[64];
-  DD a{0.0, 0.0};
+                                                   const unsigned long long* __restrict__ maxbits,
+                                                   unsigned long long* __restrict__ acc) {
+  const int base = sumsq64_base(*maxbits);
+  if (base == kFxBad || *maxbits == 0ull) return;
+  __int128 q = 0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const double x = T[i];
-    a = dd_add(a, dd_two_prod(x, x));
+    const double p = x * x;
+    q += fx_term(p, base) + fx_term(fma(x, x, -p), base);
   }
-  const DD b = block_sum_dd(a, sv);
-  if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = b.hi;
-    part[2 * blockIdx.x + 1] = b.lo;
+  q = fx_warp_sum(q);
+  const unsigned long long lo = (unsigned long long)q, hi = (unsigned long long)(q >> 64);
+  if ((threadIdx.x & 31) == 0 && (lo | hi)) {  // 128-bit two's complement add, carry by hand
+    const unsigned long long old = atomicAdd(&acc[0], lo);
+    atomicAdd(&acc[1], hi + ((old + lo) < old ? 1ull : 0ull));
   }
 }
 
-__device__ DD dd_from_u64(unsigned long long u) {  // exact: both halves and their sum fit
-  return dd_two_sum((double)(u >> 32) * 4294967296.0, (double)(u & 0xffffffffull));
+// q 2^(base - 1075) as a double-double (hi rounded, lo the exact remainder rounded)
+__device__ DD fx_to_dd(__int128 q, int base) {
+  const double hi = fx_to_double(q, base);
+  return DD{hi, fx_to_double(q - fx_term(hi, base), base)};
 }
 
-__global__ void k_norm2_finish(int is_f32, const unsigned* __restrict__ maxbits,
-                               const unsigned long long* __restrict__ acc, const double* __restrict__ part,
-                               int nblk, DevCheck* chk) {
+__global__ void k_norm2_finish(int is_f32, const void* __restrict__ maxbits,
+                               const unsigned long long* __restrict__ acc, DevCheck* chk) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   DD t{0.0, 0.0};
   int valid = 1;
+  const __int128 q = (__int128)(((unsigned __int128)acc[1] << 64) | acc[0]);
   if (is_f32) {
-    const unsigned mb = *maxbits;
+    const unsigned mb = *static_cast<const unsigned*>(maxbits);
     if (mb >= 0x7f800000u) {
       valid = 0;
     } else if (mb != 0u) {
+      // units of 2^(2(e_max - 150) - 32) = 2^(base - 1075)
       const int emax = (int)(mb >> 23) + ((mb >> 23) == 0u ? 1 : 0);
-      DD h = dd_from_u64(acc[1]);
-      h = DD{ldexp(h.hi, 64), ldexp(h.lo, 64)};
-      t = dd_add(h, dd_from_u64(acc[0]));
-      const int sc = 2 * (emax - 150) - 32;
-      t = DD{ldexp(t.hi, sc), ldexp(t.lo, sc)};
+      t = fx_to_dd(q, 2 * (emax - 150) - 32 + 1075);
     }
   } else {
-    for (int b = 0; b < nblk; ++b) t = dd_add(t, DD{part[2 * b], part[2 * b + 1]});
-    valid = isfinite(t.hi) ? 1 : 0;
+    const unsigned long long mb = *static_cast<const unsigned long long*>(maxbits);
+    const int base = sumsq64_base(mb);
+    if (base == kFxBad)
+      valid = 0;
+    else if (mb != 0ull)
+      t = fx_to_dd(q, base);
   }
   chk->t2_hi = t.hi;
   chk->t2_lo = t.lo;
@@ -1511,26 +1595,27 @@ __global__ void k_norm2_finish(int is_f32, const unsigned* __restrict__ maxbits,
 
 }  // namespace
 
-size_t norm2_scratch_doubles() { return 4 + 2 * (size_t)kNormMaxBlocks; }
+size_t norm2_scratch_doubles() { return 4; }
 
 cudaError_t launch_tensor_norm2(const void* T, int tdtype, int64_t n, double* scratch, DevCheck* chk, int num_sms,
                                 cudaStream_t st) {
-  // scratch: [0, 2) the 128-bit sum, [2] the largest |entry|'s bits, [4, ...) block partials
+  // scratch: [0, 2) the 128-bit sum, [2] the largest |entry|'s bits
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(scratch);
-  unsigned* maxbits = reinterpret_cast<unsigned*>(scratch + 2);
-  double* part = scratch + 4;
+  void* maxbits = scratch + 2;
   const int64_t want = (n + 255) / 256;
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, std::min(kNormMaxBlocks, 8 * num_sms)));
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, 8 * (int64_t)num_sms));
   cudaError_t e = cudaMemsetAsync(scratch, 0, 4 * sizeof(double), st);
   if (e != cudaSuccess) return e;
   if (tdtype == CPALS_DTYPE_F32) {
     const float* Tf = static_cast<const float*>(T);
-    k_absmax_bits<<<blocks, 256, 0, st>>>(Tf, n, maxbits);
-    k_sumsq_f32<<<blocks, 256, 0, st>>>(Tf, n, maxbits, acc);
-    k_norm2_finish<<<1, 32, 0, st>>>(1, maxbits, acc, part, 0, chk);
+    k_absmax_bits<<<blocks, 256, 0, st>>>(Tf, n, static_cast<unsigned*>(maxbits));
+    k_sumsq_f32<<<blocks, 256, 0, st>>>(Tf, n, static_cast<const unsigned*>(maxbits), acc);
+    k_norm2_finish<<<1, 32, 0, st>>>(1, maxbits, acc, chk);
   } else {
-    k_sumsq_f64<<<blocks, 256, 0, st>>>(static_cast<const double*>(T), n, part);
-    k_norm2_finish<<<1, 32, 0, st>>>(0, maxbits, acc, part, blocks, chk);
+    const double* Td = static_cast<const double*>(T);
+    k_absmax_bits64<<<blocks, 256, 0, st>>>(Td, n, static_cast<unsigned long long*>(maxbits));
+    k_sumsq_f64<<<blocks, 256, 0, st>>>(Td, n, static_cast<const unsigned long long*>(maxbits), acc);
+    k_norm2_finish<<<1, 32, 0, st>>>(0, maxbits, acc, chk);
   }
   return cudaGetLastError();
 }
@@ -1549,8 +1634,11 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
   mixed = (mixed && R <= 128) ? 1 : 0;
   if (mixed) {
     float* ops = reinterpret_cast<float*>(work + ops32_offset_doubles(R));
+    const size_t sm32 = factorize32_smem_bytes(R);
+    cudaError_t eb = set_smem_limit_once((const void*)k_factorize32, (int)factorize32_smem_bytes(128));
+    if (eb != cudaSuccess) return eb;
     k_form_v32<<<(R * R + 255) / 256, 256, 0, st>>>(gs, order, skip, R, ops, chk);
-    k_factorize32<<<1, FT32, 0, st>>>(R, ops, info, chk);
+    k_factorize32<<<1, FT32, sm32, st>>>(R, ops, info, chk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -1616,7 +1704,7 @@ cudaError_t launch_gram(const double* X, int64_t In, int R, int S2, double* part
   return cudaGetLastError();
 }
 
-size_t gram_finalize_part_doubles(int S2, int R) { return (size_t)gram_tiles(R) * ((size_t)S2 * 256 + 2); }
+size_t gram_finalize_part_doubles(int S2, int R) { return (size_t)gram_tiles(R) * ((size_t)S2 * 256 + 3); }
 
 cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, double* part, unsigned* counters,
                                  double* Graw, double* lam, double* lam_inv, double* Gn, const GramSet& gs, int order,
@@ -1626,15 +1714,15 @@ cudaError_t launch_gram_finalize(const double* X, int64_t In, int R, int S2, dou
   dim3 grid((unsigned)gram_tiles(R), (unsigned)S2);
   const int ntiles = gram_tiles(R);
   // per-tile double-double partials of ||X||^2 live after the tile partial sums
-  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1,
-                  part + (size_t)ntiles * S2 * 256, ntiles, run_check};
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, reinterpret_cast<const long long*>(inner_rows), In, chk,
+                  traj, traj_cap, order - 1, part + (size_t)ntiles * S2 * 256, ntiles, run_check};
   k_gram<true><<<grid, 256, 0, st>>>(X, In, R, S2, rps, part, counters, Graw, chk, fa);
   return cudaGetLastError();
 }
 
 size_t gram_rows_part_doubles(int nblk, int R) {
   const size_t T = (size_t)R * (R + 1) / 2;
-  return (size_t)nblk * T + 2 * ((T + 31) / 32);
+  return (size_t)nblk * T + 3 * ((T + 31) / 32);
 }
 
 cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned* counter, double* Graw, double* lam,
@@ -1645,8 +1733,8 @@ cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned*
   const int blocks = (T + 31) / 32;
   // the blocks' double-double shares of ||X||^2 follow the partial Grams
   double* fpart = const_cast<double*>(gram_part) + (size_t)nblk * T;
-  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, fpart, blocks,
-                  run_check};
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, reinterpret_cast<const long long*>(inner_rows), In, chk,
+                  traj, traj_cap, order - 1, fpart, blocks, run_check};
   k_gram_rows<<<blocks, 256, 0, st>>>(gram_part, nblk, R, Graw, counter, chk, fa);
   return cudaGetLastError();
 }
@@ -1654,7 +1742,8 @@ cudaError_t launch_gram_rows(const double* gram_part, int nblk, int R, unsigned*
 cudaError_t launch_finalize(const double* Graw, int R, double* lam, double* lam_inv, double* Gn, const GramSet& gs,
                             int order, int last, const double* inner_rows, int64_t In, DevCheck* chk, double* traj,
                             int64_t traj_cap, cudaStream_t st) {
-  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, inner_rows, In, chk, traj, traj_cap, order - 1, nullptr, 0, 1};
+  FinalizeArgs fa{lam, lam_inv, Gn, gs, order, last, reinterpret_cast<const long long*>(inner_rows), In, chk,
+                  traj, traj_cap, order - 1, nullptr, 0, 1};
   k_finalize<<<1, 256, 0, st>>>(Graw, R, fa);
   return cudaGetLastError();
 }

@@ -60,6 +60,7 @@ struct cpals_ctx {
   double* traj = nullptr;
   int64_t traj_cap = 0;
   cudaGraphExec_t graph = nullptr;
+  const void* graph_dT = nullptr;  // the tensor address the graph's kernels were captured with
   // randomized path
   int64_t* dpiv = nullptr;
   int64_t piv_cap = 0;
@@ -299,6 +300,7 @@ int build_graph(cpals_ctx* c) {
   e = cudaGraphInstantiate(&c->graph, g, 0);
   cudaGraphDestroy(g);
   CPALS_CUDA_TRY(e);
+  c->graph_dT = c->dT;
   return CPALS_OK;
 }
 
@@ -618,7 +620,9 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
 
 static int after_tensor_set(cpals_ctx* c) {
   c->T_set = true;
-  invalidate_graph(c);
+  // The sweep graph reads the tensor only through its address (FP64 MTTKRP) or through the
+  // tile streams rebuilt in place below, so a new tensor at the same address keeps it.
+  if (c->graph_dT != c->dT) invalidate_graph(c);
   // ||T||^2 as a double-double, for the compensated fit
   CPALS_CUDA_TRY(launch_tensor_norm2(c->dT, c->tdtype, c->numel, c->nrm, c->chk, c->num_sms, c->st));
   c->launches += 3;

@@ -60,7 +60,12 @@ struct TcModePlan {
   int mode, fmode, n_outer, m_blocks, n_blocks, splits, stages, nb, tmem_cols, rpad;
   int64_t In, If, nfb, nchunks, chunks_per_split;
   int64_t sn, sf;              // element strides of mode n and of f in the tensor
-  uint32_t stage_bytes;
+  uint32_t stage_bytes;        // stride of the ring's stages
+  // Resident factor-block tiles: all nfb B tiles of the CTA's N block are loaded once, at
+  // bres_off, and a stage holds only the 32 KB unfolding tile; the outer rows then have their
+  // own ring (obytes per stage, at orow_off).  ctl_off: barriers and flags.
+  int bres;
+  uint32_t bres_off, orow_off, obytes, ctl_off;
   int64_t outer_dims[kMaxOrder];
   int64_t outer_stride[kMaxOrder];  // element stride of each outer mode in the tensor
   int outer_modes[kMaxOrder];
@@ -185,14 +190,24 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
   constexpr uint32_t b_bytes = NB * kChunk * 2;       // one BF16 factor-block tile (hi or lo)
   constexpr uint32_t o_bytes = NB * 4;                // one outer factor row slice
   const uint32_t stage_bytes = p.stage_bytes;
-  uint8_t* ctl = smem + (size_t)S * stage_bytes;
+  const bool bres = p.bres != 0;
+  uint8_t* ctl = smem + p.ctl_off;
   uint64_t* full_a = reinterpret_cast<uint64_t*>(ctl);  // [4] stage data landed
   uint64_t* empty = full_a + 4;                          // [4] stage consumed (MMAs done, rows read)
   uint64_t* acc_full = empty + 4;                        // [4] chunk accumulators ready
   uint64_t* acc_empty = acc_full + 4;                    // [4] chunk accumulators drained
   uint64_t* done_bar = acc_empty + 4;
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(done_bar + 1);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done_bar + 2);
+  uint64_t* bres_bar = done_bar + 1;                     // resident B tiles landed
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bres_bar + 1);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bres_bar + 2);
+  // where stage s keeps its unfolding tile, the B tile of chunk fb, and its outer rows
+  auto stage_a = [&](int s) { return smem + (size_t)s * stage_bytes; };
+  auto b_tile = [&](int s, int64_t fb) {
+    return bres ? smem + p.bres_off + (size_t)fb * (2 * b_bytes) : stage_a(s) + 2 * a_bytes;
+  };
+  auto outer_rows = [&](int s) {
+    return bres ? smem + p.orow_off + (size_t)s * p.obytes : stage_a(s) + 2 * a_bytes + 2 * b_bytes;
+  };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mblk = blockIdx.x % p.m_blocks;
@@ -213,6 +228,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
       mbar_init(smem_u32(&acc_empty[b]), tc_drain_warps<NB>());
     }
     mbar_init(smem_u32(done_bar), 1);
+    mbar_init(smem_u32(bres_bar), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -231,8 +247,15 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
     // ---------------- producer: unfolding tile, factor-block tile, outer rows
     if (lane == 0) {
       int issued = 0;
-      const uint32_t tx = 2 * a_bytes + 2 * b_bytes + (uint32_t)p.n_outer * o_bytes;
+      const uint32_t tx = 2 * a_bytes + (bres ? 0u : 2 * b_bytes) + (uint32_t)p.n_outer * o_bytes;
       const uint8_t* src_tiles = tiles + ((size_t)mblk * p.nchunks + c_begin) * (2 * a_bytes);
+      if (bres && nloc > 0) {  // every B tile of this N block, once
+        const uint32_t bar = smem_u32(bres_bar);
+        mbar_expect_tx(bar, (uint32_t)p.nfb * 2 * b_bytes);
+        for (int64_t fb = 0; fb < p.nfb; ++fb)
+          bulk_load(smem_u32(b_tile(0, fb)), btiles + ((size_t)fb * p.n_blocks + nblk) * (2 * b_bytes), 2 * b_bytes,
+                    bar);
+      }
       for (int it = 0; it < nloc; ++it) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
@@ -244,13 +267,14 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         const int64_t c = c_begin + it;
         const int64_t fb = c % p.nfb;
         int64_t o = c / p.nfb;
-        uint8_t* st = smem + (size_t)s * stage_bytes;
+        uint8_t* st = stage_a(s);
         const uint32_t bar = smem_u32(&full_a[s]);
         mbar_expect_tx(bar, tx);
         bulk_load(smem_u32(st), src_tiles + (size_t)it * (2 * a_bytes), 2 * a_bytes, bar);
-        bulk_load(smem_u32(st + 2 * a_bytes), btiles + ((size_t)fb * p.n_blocks + nblk) * (2 * b_bytes), 2 * b_bytes,
-                  bar);
-        uint8_t* orow = st + 2 * a_bytes + 2 * b_bytes;
+        if (!bres)
+          bulk_load(smem_u32(st + 2 * a_bytes), btiles + ((size_t)fb * p.n_blocks + nblk) * (2 * b_bytes),
+                    2 * b_bytes, bar);
+        uint8_t* orow = outer_rows(s);
         for (int j = 0; j < p.n_outer; ++j) {
           const int64_t id = o % p.outer_dims[j];
           o /= p.outer_dims[j];
@@ -263,6 +287,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         // drain this CTA's own copies in flight before the shared memory goes away
         for (int it = max(0, issued - S); it < issued; ++it)
           (void)mbar_wait(smem_u32(&full_a[it % S]), (uint32_t)((it / S) & 1), reinterpret_cast<volatile int*>(err + 1));
+        if (bres && nloc > 0) (void)mbar_wait(smem_u32(bres_bar), 0u, reinterpret_cast<volatile int*>(err + 1));
       }
     }
   } else if (warp == 1) {
@@ -271,7 +296,11 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
     // together, a second N = NB product adds Tl Bh onto the cross terms.
     if (lane == 0) {
       const uint32_t idesc_w = idesc_bf16(kBlockM, 2 * NB), idesc_n = idesc_bf16(kBlockM, NB);
-      for (int it = 0; it < nloc; ++it) {
+      if (bres && nloc > 0 && !mbar_wait(smem_u32(bres_bar), 0u, abort_flag)) {
+        atomicCAS(err, 0, 2);
+        *abort_flag = 1;
+      }
+      for (int it = 0; it < nloc && !*abort_flag; ++it) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
         const int b = it % kBuf;
@@ -283,8 +312,8 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
           break;
         }
         tc_fence_after();
-        uint8_t* st = smem + (size_t)s * stage_bytes;
-        const uint32_t ah = smem_u32(st), al = ah + a_bytes, bh = al + a_bytes;
+        const uint32_t ah = smem_u32(stage_a(s)), al = ah + a_bytes;
+        const uint32_t bh = smem_u32(b_tile(s, (c_begin + it) % p.nfb));
         const uint32_t acc_h = tmem + (uint32_t)(b * kAcc * NB), acc_l = acc_h + (uint32_t)NB;
 #pragma unroll
         for (int kk = 0; kk < kChunk / 16; ++kk) {
@@ -325,8 +354,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         break;
       }
       tc_fence_after();
-      const float* orow =
-          reinterpret_cast<const float*>(smem + (size_t)s * stage_bytes + 2 * a_bytes + 2 * b_bytes) + cb;
+      const float* orow = reinterpret_cast<const float*>(outer_rows(s)) + cb;
       const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
       // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
       // budget is smaller: 320 threads)
@@ -560,16 +588,36 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     splits = std::min<int64_t>(splits, p.nchunks);
     p.chunks_per_split = (p.nchunks + splits - 1) / splits;
     p.splits = (int)((p.nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
-    // stage: A hi | A lo | B hi | B lo | outer rows
-    const size_t sb = (size_t)2 * kBlockM * kChunk * 2 + (size_t)2 * nb * kChunk * 2 + (size_t)p.n_outer * nb * 4;
-    p.stage_bytes = (uint32_t)round_up((int64_t)sb, 1024);
+    // Resident B tiles (all nfb of them, loaded once) when they leave room for at least three
+    // 32 KB unfolding stages: a stage then streams 32 KB instead of 32 KB + the B tile.
+    // Otherwise each stage is A hi | A lo | B hi | B lo | outer rows.
     const size_t ctl_bytes = 1024 + 256;  // alignment slack + barriers and flags
-    p.stages = (int)std::min<size_t>(4, (kSmemLimit - ctl_bytes) / p.stage_bytes);
+    const size_t a2 = (size_t)2 * kBlockM * kChunk * 2;
+    const size_t b2 = (size_t)2 * nb * kChunk * 2;
+    const size_t ob = (size_t)round_up((int64_t)p.n_outer * nb * 4, 16);
+    const size_t bres_bytes = (size_t)p.nfb * b2;
+    const size_t room = (kSmemLimit > ctl_bytes + bres_bytes + 4 * ob) ? kSmemLimit - ctl_bytes - bres_bytes - 4 * ob : 0;
+    const int res_stages = (int)std::min<size_t>(4, room / a2);
+    if (res_stages >= 3) {
+      p.bres = 1;
+      p.stages = res_stages;
+      p.stage_bytes = (uint32_t)a2;
+      p.bres_off = (uint32_t)(p.stages * a2);
+      p.orow_off = p.bres_off + (uint32_t)bres_bytes;
+      p.obytes = (uint32_t)ob;
+      p.ctl_off = p.orow_off + (uint32_t)(p.stages * ob);
+    } else {
+      const size_t sb = a2 + b2 + (size_t)p.n_outer * nb * 4;
+      p.bres = 0;
+      p.stage_bytes = (uint32_t)round_up((int64_t)sb, 1024);
+      p.stages = (int)std::min<size_t>(4, (kSmemLimit - ctl_bytes) / p.stage_bytes);
+      p.ctl_off = (uint32_t)(p.stages * (size_t)p.stage_bytes);
+    }
     if (p.stages < 2 || p.nchunks >= (int64_t(1) << 31)) {
       tc_destroy(s);
       return CPALS_E_UNSUPPORTED;
     }
-    s->smem_bytes[n] = ctl_bytes + (size_t)p.stages * p.stage_bytes;
+    s->smem_bytes[n] = ctl_bytes + p.ctl_off;
     s->tile_bytes[n] = (size_t)p.m_blocks * p.nchunks * (2 * kBlockM * kChunk * 2);
     if (cudaMalloc(&s->tiles[n], s->tile_bytes[n]) != cudaSuccess) {
       tc_destroy(s);

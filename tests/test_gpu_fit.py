@@ -51,9 +51,9 @@ def test_tensor_norm2_is_exact_to_double_double(built, dt):
     with built.Engine(dims, 3, dtype=dt) as eng:
         eng.set_tensor(T)
         nrm, (hi, lo) = eng.tensor_norm()
-    # FP32: exact but for the bits below 2^-78 of the largest square, which entries 2^16 and
-    # more below the largest drop (at most n 2^-78 relative); FP64: double-double
-    bound = T.size * 2.0 ** -78 if dt == np.float32 else 2.0 ** -90
+    # exact but for the bits each square drops below a fixed fraction of the largest square:
+    # 2^-78 for FP32 entries, 2^-86 for FP64 (TwoProduct parts): at most n times that, relative
+    bound = T.size * (2.0 ** -78 if dt == np.float32 else 2.0 ** -86)
     assert dd_error(hi, lo, exact) < bound
     assert abs(nrm - math.sqrt(float(exact))) <= 2 * EPS * nrm
 

@@ -290,3 +290,31 @@ def test_lev_score_sampled_api(built, oracle):
                                  rng=np.random.default_rng(100 + trial))
         best = min(best, rel(oracle.reconstruct(opt.factors, opt.lam), T))
     assert best < 0.1
+
+
+@pytest.mark.parametrize("prec,dt", [("fp64", np.float64), ("bf16x3", np.float32)])
+def test_second_tensor_on_the_same_handle_is_the_one_decomposed(built, prec, dt):
+    # the sweep graph survives a new tensor at the same device address; the next optimize
+    # must use the new contents (compared with a fresh handle on the second tensor)
+    from itensorcpd_gb300 import _lib as L
+
+    dims, R = (24, 20, 18), 4
+    Ta = np.asfortranarray(det_normal(31, dims).astype(dt))
+    Tb = np.asfortranarray(det_normal(32, dims).astype(dt))
+    F, lam = det_factors(dims, R, seed=9)
+
+    def run(eng, T):
+        eng.set_tensor(T)
+        eng.set_factors(F, lam)
+        c = L.CpalsCheck()
+        c.kind, c.max_counter, c.ref_norm = L.CHECK_NONE, 4, float(np.linalg.norm(T.astype(np.float64)))
+        return eng.optimize(c), eng.get_factors()
+
+    with built.Engine(dims, R, dtype=dt, precision=prec) as e1, built.Engine(dims, R, dtype=dt, precision=prec) as e2:
+        run(e1, Ta)
+        tr1, (F1, l1) = run(e1, Tb)
+        tr2, (F2, l2) = run(e2, Tb)
+    assert np.array_equal(tr1, tr2)
+    assert np.array_equal(l1, l2)
+    for a, b in zip(F1, F2):
+        assert np.array_equal(a, b)

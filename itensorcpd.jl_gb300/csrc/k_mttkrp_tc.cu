@@ -588,9 +588,11 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     splits = std::min<int64_t>(splits, p.nchunks);
     p.chunks_per_split = (p.nchunks + splits - 1) / splits;
     p.splits = (int)((p.nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
-    // Resident B tiles (all nfb of them, loaded once) when they leave room for at least three
-    // 32 KB unfolding stages: a stage then streams 32 KB instead of 32 KB + the B tile.
-    // Otherwise each stage is A hi | A lo | B hi | B lo | outer rows.
+    // Resident B tiles (all nfb of them, loaded once) when they leave room for four 32 KB
+    // unfolding stages: a stage then streams 32 KB instead of 32 KB + the B tile.  With fewer
+    // stages the unfolding bytes in flight drop, and the kernel is bound by them (at 512^3
+    // R = 64, resident tiles with three stages took 120 us a launch against 110 us with four
+    // stages of A + B).  Otherwise each stage is A hi | A lo | B hi | B lo | outer rows.
     const size_t ctl_bytes = 1024 + 256;  // alignment slack + barriers and flags
     const size_t a2 = (size_t)2 * kBlockM * kChunk * 2;
     const size_t b2 = (size_t)2 * nb * kChunk * 2;
@@ -598,7 +600,7 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     const size_t bres_bytes = (size_t)p.nfb * b2;
     const size_t room = (kSmemLimit > ctl_bytes + bres_bytes + 4 * ob) ? kSmemLimit - ctl_bytes - bres_bytes - 4 * ob : 0;
     const int res_stages = (int)std::min<size_t>(4, room / a2);
-    if (res_stages >= 3) {
+    if (res_stages >= 4) {
       p.bres = 1;
       p.stages = res_stages;
       p.stage_bytes = (uint32_t)a2;

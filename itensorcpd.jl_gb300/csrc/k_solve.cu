@@ -615,44 +615,60 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
   const int ntile = Rp / 4;
   for (int p0 = 0; p0 < R; p0 += kBlk32) {
     const int pb = min(kBlk32, R - p0);
-    // (a) sweep of the diagonal block D = A_PP by warp 0: lane i owns row i of Dm
+    // (a) sweep of the diagonal block D = A_PP by warp 0: lane i holds row i in registers;
+    // the pivot row reaches every lane by shuffles, and a dynamic column is picked out by an
+    // unrolled select (no dynamically indexed registers)
     if (warp == 0) {
-      for (int e = lane; e < pb * pb; e += 32) Dm[(e / pb) * 33 + e % pb] = A[(size_t)(p0 + e / pb) * ld + p0 + e % pb];
-      __syncwarp();
+      float r[kBlk32];
+#pragma unroll
+      for (int c = 0; c < kBlk32; ++c) r[c] = (lane < pb && c < pb) ? A[(size_t)(p0 + lane) * ld + p0 + c] : 0.f;
       const float thr = misc[0];
       bool bad = false;
       for (int k = 0; k < pb; ++k) {
-        const float d = Dm[k * 33 + k];
+        float dik = 0.f;
+#pragma unroll
+        for (int c = 0; c < kBlk32; ++c) dik = (c == k) ? r[c] : dik;  // D(i, k)
+        const float d = __shfl_sync(0xffffffffu, dik, k);
         bad = bad || !(d > thr) || !(d < INFINITY);
         const float rd = 1.0f / d;
-        const float f = (lane < pb) ? Dm[lane * 33 + k] * rd : 0.f;  // D(i, k) / d
-        __syncwarp();
-        if (lane < pb && lane != k) {
-          float* row = Dm + lane * 33;
-          const float* rk = Dm + k * 33;
-          for (int c = 0; c < pb; ++c)
-            if (c != k) row[c] = fmaf(-f, rk[c], row[c]);
-          row[k] = f;
+        const float f = dik * rd;
+#pragma unroll
+        for (int c = 0; c < kBlk32; ++c) {
+          const float rkc = __shfl_sync(0xffffffffu, r[c], k);  // D(k, c)
+          if (lane == k)
+            r[c] = (c == k) ? -rd : rkc * rd;
+          else
+            r[c] = (c == k) ? f : fmaf(-f, rkc, r[c]);
         }
-        __syncwarp();
-        if (lane < pb) Dm[k * 33 + lane] = (lane == k) ? -rd : f;  // row k: D(k, c) / d (symmetric)
-        __syncwarp();
+      }
+      if (lane < pb) {
+#pragma unroll
+        for (int c = 0; c < kBlk32; ++c) Dm[lane * 33 + c] = r[c];
       }
       if (lane == 0 && bad) misc[1] = 1.f;
     }
     __syncthreads();
     if (misc[1] != 0.f) break;
-    // (b) B = A_{.P} D^{-1} (D^{-1} = -Dm) and C = A_{.P}, both transposed, for every row i
-    for (int e = tid; e < kBlk32 * R; e += nt) {
-      const int q = e & 31, i = e >> 5;  // lanes take the 32 block columns of one row
-      float b = 0.f, c = 0.f;
-      if (q < pb) {
-        const float* Ai = A + (size_t)i * ld + p0;
-        c = Ai[q];
-        for (int pp = 0; pp < pb; ++pp) b = fmaf(Ai[pp], -Dm[pp * 33 + q], b);
+    // (b) B = A_{.P} D^{-1} (D^{-1} = -Dm) and C = A_{.P}, both transposed, for every row i:
+    // lane q keeps column q of D^{-1} in registers, the warps take the rows
+    {
+      float dcol[kBlk32];
+#pragma unroll
+      for (int pp = 0; pp < kBlk32; ++pp) dcol[pp] = (lane < pb && pp < pb) ? -Dm[pp * 33 + lane] : 0.f;
+      for (int i = warp; i < R; i += nt >> 5) {
+        const float4* ai = reinterpret_cast<const float4*>(A + (size_t)i * ld + p0);
+        float b = 0.f;
+#pragma unroll
+        for (int v = 0; v < kBlk32 / 4; ++v) {
+          const float4 x = ai[v];
+          b = fmaf(x.x, dcol[4 * v], b);
+          b = fmaf(x.y, dcol[4 * v + 1], b);
+          b = fmaf(x.z, dcol[4 * v + 2], b);
+          b = fmaf(x.w, dcol[4 * v + 3], b);
+        }
+        Bt[(size_t)lane * ld + i] = b;
+        Ct[(size_t)lane * ld + i] = (lane < pb) ? A[(size_t)i * ld + p0 + lane] : 0.f;
       }
-      Bt[(size_t)q * ld + i] = b;
-      Ct[(size_t)q * ld + i] = c;
     }
     __syncthreads();
     // (c) the rank-pb update of the rest, and the swept blocks written back, in 4 x 4 tiles
@@ -1491,20 +1507,33 @@ __global__ void __launch_bounds__(256) k_sumsq_f32(const float* __restrict__ T, 
   const unsigned mb = *maxbits;
   if (mb == 0u || mb >= 0x7f800000u) return;  // all zero, or a non-finite entry
   const int emax = (int)(mb >> 23) + ((mb >> 23) == 0u ? 1 : 0);
-  unsigned __int128 a = 0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const unsigned u = __float_as_uint(T[i]) & 0x7fffffffu;
+  // the 128-bit sum as two 64-bit words, the shifts written out (a term is below 2^80)
+  unsigned long long lo = 0, hi = 0;
+  auto add = [&](float x) {
+    const unsigned u = __float_as_uint(x) & 0x7fffffffu;
     const unsigned e = u >> 23;
     const unsigned long long mm = (unsigned long long)((u & 0x7fffffu) | (e ? 0x800000u : 0u));
     const unsigned long long sq = mm * mm;  // < 2^48, exact
     const int sh = 32 - 2 * (emax - ((int)e + (e == 0u ? 1 : 0)));
-    if (sh >= 0)
-      a += (unsigned __int128)sq << sh;
-    else if (sh > -64)
-      a += (unsigned __int128)(sq >> (-sh));
+    const unsigned long long t = (sh >= 0) ? sq : ((sh > -64) ? (sq >> (-sh)) : 0ull);
+    const int sl = sh > 0 ? sh : 0;  // 0 .. 32
+    const unsigned long long tlo = t << sl;
+    const unsigned long long thi = sl ? (t >> (64 - sl)) : 0ull;
+    lo += tlo;
+    hi += thi + (lo < tlo ? 1ull : 0ull);
+  };
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t tid0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool al16 = (reinterpret_cast<uintptr_t>(T) & 15) == 0;
+  const int64_t n4 = al16 ? n / 4 : 0;
+  for (int64_t i = tid0; i < n4; i += stride) {  // 16-byte loads
+    const float4 v = reinterpret_cast<const float4*>(T)[i];
+    add(v.x);
+    add(v.y);
+    add(v.z);
+    add(v.w);
   }
-  unsigned long long lo = (unsigned long long)a, hi = (unsigned long long)(a >> 64);
+  for (int64_t i = 4 * n4 + tid0; i < n; i += stride) add(T[i]);
   for (int off = 16; off > 0; off >>= 1) {
     const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, off);
     const unsigned long long ohi = __shfl_xor_sync(0xffffffffu, hi, off);

@@ -54,6 +54,12 @@ struct cpals_ctx {
   unsigned* gcnt = nullptr;
   int gS2[kMaxOrder] = {};
   double* inner_rows = nullptr;  // three words per row: an exact fixed-point row sum
+  // the fused mode tail (one cooperative launch per mode): its grid barrier, its error word,
+  // whether it is in use, and per mode whether its blocks fit on the device at once
+  GridBar* gbar = nullptr;
+  int* tail_err = nullptr;
+  bool fused_tail = true;
+  bool tail_fits[kMaxOrder] = {};
   double* nrm = nullptr;         // scratch of the ||T||^2 kernels
   DevCheck* chk = nullptr;
   DevCheck* hchk = nullptr;  // pinned mirror
@@ -212,6 +218,11 @@ CrossArgs cross_args(const cpals_ctx* c) {
 
 bool is_cross_kind(int kind) { return kind == CPALS_CHECK_DIFF || kind == CPALS_CHECK_ANGLE; }
 
+bool stream_capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
 // One mode of the sweep: compute_krp, matricize_tensor, solve_ls_problem, row_norm and
 // post_solve of optimize (optimize.jl:19-27).  On the last mode the fit's terms are saved in
 // the device check; run_check = 1 also runs the check's update there (the fused sweep),
@@ -247,6 +258,27 @@ int enqueue_mode(cpals_ctx* c, int n, int run_check) {
     // factorize, MTTKRP, solve, gram+finalize, normalize (which also writes the BF16 factor tiles)
     c->launches += 5;
     double* rg = c->rgpart;  // Gram partials from the solve blocks, reduced by launch_gram_rows
+    const BtileDesc btd = c->tc ? tc_btile_desc(c->tc, n) : c->dt ? dt_btile_desc(c->dt, n) : BtileDesc{nullptr, 0, 0};
+    if (rg && c->fused_tail && c->tail_fits[n]) {
+      // solve, Gram, lambda, normalisation (and the fit on the last mode) in one launch
+      const void* part = c->dt ? (const void*)c->Mdt : c->part;
+      const int pf32 = c->dt ? 0 : c->part_f32;
+      const int sp = c->dt ? 1 : c->splits[n];
+      cudaError_t e = launch_mode_tail(part, pf32, sp, In, R, c->work, c->W, c->info, c->X, rg, c->F[n], c->F32r[n],
+                                       c->F32lo[n], c->rpad, btd, c->Graw, c->lam, c->lam_inv, c->G[n], gs, N, last,
+                                       c->inner_rows, c->chk, c->traj, c->traj_cap, c->gbar, c->tail_err,
+                                       c->num_sms, run_check, c->st);
+      if (e == cudaSuccess) {
+        c->launches -= 2;  // factorize, MTTKRP and the tail: three launches, not five
+        return CPALS_OK;
+      }
+      if (e != cudaErrorNotSupported) {
+        (void)cudaGetLastError();
+        fprintf(stderr, "libcpals: fused mode tail refused (%s); using the separate kernels\n", cudaGetErrorString(e));
+        return CPALS_E_UNSUPPORTED;  // the caller retries without it
+      }
+      c->tail_fits[n] = false;
+    }
     if (c->dt)
       CPALS_CUDA_TRY(launch_solve_rows(c->Mdt, 0, 1, In, R, c->work, c->U, c->piv, c->W, c->info, c->X,
                                        last ? c->inner_rows : nullptr, c->chk, c->st, rg));
@@ -264,7 +296,6 @@ int enqueue_mode(cpals_ctx* c, int n, int run_check) {
     // The last mode's normalisation ignores `done`: it is idempotent (X and lambda are
     // left untouched by the early-returning kernels of later sweeps).
     // the BF16 factor tiles the tensor-core MTTKRP reads are written by the same kernel
-    const BtileDesc btd = c->tc ? tc_btile_desc(c->tc, n) : c->dt ? dt_btile_desc(c->dt, n) : BtileDesc{nullptr, 0, 0};
     CPALS_CUDA_TRY(launch_normalize(c->X, c->lam_inv, In, R, c->F[n], c->F32r[n], c->rpad,
                                     c->Graw, c->G[n], last ? nullptr : c->chk, c->st, btd, c->F32lo[n]));
   }
@@ -273,7 +304,11 @@ int enqueue_mode(cpals_ctx* c, int n, int run_check) {
 
 int enqueue_sweep(cpals_ctx* c) {
   for (int n = 0; n < c->order; ++n) {
-    const int rc = enqueue_mode(c, n, 1);
+    int rc = enqueue_mode(c, n, 1);
+    if (rc == CPALS_E_UNSUPPORTED && c->fused_tail && !stream_capturing(c->st)) {
+      c->fused_tail = false;  // the cooperative launch was refused: the separate kernels from now on
+      rc = enqueue_mode(c, n, 1);
+    }
     if (rc != CPALS_OK) return rc;
   }
   if (c->cross_on) {  // check_converge of a CPDiffCheck / CPAngleCheck on the new iterate
@@ -292,6 +327,13 @@ int build_graph(cpals_ctx* c) {
   c->sweep_launches = c->launches - before;
   c->launches = before;  // capture enqueues nothing; replays are counted
   cudaError_t e = cudaStreamEndCapture(c->st, &g);
+  if (rc == CPALS_E_UNSUPPORTED && c->fused_tail) {
+    // the cooperative tail could not be captured: capture the separate kernels instead
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    c->fused_tail = false;
+    return build_graph(c);
+  }
   if (rc != CPALS_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -360,8 +402,18 @@ int upload_pivots(cpals_ctx* c, int mode, const int64_t* pivots, int64_t nsamps)
   return CPALS_OK;
 }
 
-// Reads and clears the tensor-core kernel's error word (after a stream sync).
+// Reads and clears the tensor-core kernels' and the fused tail's error words (after a
+// stream sync).
 int check_tc_err(cpals_ctx* c) {
+  if (c->tail_err) {
+    int h = 0;
+    CPALS_CUDA_TRY(cudaMemcpy(&h, c->tail_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+      fprintf(stderr, "libcpals: a grid barrier of the fused mode tail gave up (bounded wait expired)\n");
+      CPALS_CUDA_TRY(cudaMemset(c->tail_err, 0, sizeof(int)));
+      return CPALS_E_DEVICE;
+    }
+  }
   int* flags[2] = {c->tc ? tc_error_flag(c->tc) : nullptr, nullptr};
   if (c->dt) {
     flags[0] = dt_error_flag(c->dt, 0);
@@ -448,6 +500,8 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->gcnt);
   cudaFree(c->inner_rows);
   cudaFree(c->nrm);
+  cudaFree(c->gbar);
+  cudaFree(c->tail_err);
   cudaFree(c->chk);
   if (c->hchk) cudaFreeHost(c->hchk);
   cudaFree(c->traj);
@@ -598,12 +652,25 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   {
     // partial Grams of the solve blocks, when they stay small (16M doubles)
     size_t need = 0;
-    for (int m = 0; m < order; ++m) need = std::max(need, gram_rows_part_doubles(solve_blocks(dims[m], (int)R), (int)R));
+    for (int m = 0; m < order; ++m) {
+      const int nb = solve_blocks(dims[m], (int)R);
+      need = std::max({need, gram_rows_part_doubles(nb, (int)R), mode_tail_part_doubles(nb, (int)R)});
+      c->tail_fits[m] = true;  // until a launch says otherwise
+    }
     if (need <= (size_t(1) << 24)) CK(dmalloc(&c->rgpart, need));
   }
   CPALS_CUDA_TRY(cudaMemset(c->gcnt, 0, sizeof(unsigned) * (gram_tiles((int)R) + 1)));
   CK(dmalloc(&c->inner_rows, 3 * maxI));
   CK(dmalloc(&c->nrm, norm2_scratch_doubles()));
+  CK(dmalloc(&c->gbar, 1));
+  CK(dmalloc(&c->tail_err, 1));
+  CPALS_CUDA_TRY(cudaMemset(c->gbar, 0, sizeof(GridBar)));
+  CPALS_CUDA_TRY(cudaMemset(c->tail_err, 0, sizeof(int)));
+  {
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+    c->fused_tail = coop != 0;
+  }
   CK(dmalloc(&c->chk, 1));
   CPALS_CUDA_TRY(cudaMemset(c->chk, 0, sizeof(DevCheck)));
   CK(dmalloc(&c->derr, 1));
@@ -760,6 +827,10 @@ int cpals_mode_update(cpals_ctx* c, int mode, double* host_solution) {
   // once; a caller-driven sweep has no such stop.
   CPALS_CUDA_TRY(cudaMemsetAsync(&c->chk->done, 0, sizeof(int), c->st));
   int rc = enqueue_mode(c, mode, 0);
+  if (rc == CPALS_E_UNSUPPORTED && c->fused_tail) {
+    c->fused_tail = false;
+    rc = enqueue_mode(c, mode, 0);
+  }
   if (rc != CPALS_OK) return rc;
   if (host_solution) {
     const int64_t In = c->dims[mode];

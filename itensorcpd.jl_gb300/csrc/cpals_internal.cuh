@@ -148,6 +148,13 @@ inline ModeGeom make_geom(int order, const int64_t* dims, int mode, int64_t chun
   return g;
 }
 
+// A grid-wide barrier for cooperative launches (sense-reversing: `count` is back at zero
+// after every barrier, `gen` counts them).  Zero-initialised once.
+struct GridBar {
+  unsigned count;
+  unsigned gen;
+};
+
 // Status of one normal-equation factorisation (written by the factorize kernel).
 struct SolveInfo {
   int rank;      // rank reached by the pivoted Cholesky
@@ -245,6 +252,20 @@ struct BtileDesc {
 cudaError_t launch_normalize(const double* X, const double* lam_inv, int64_t In, int R, double* F, float* F32r,
                              int64_t rpad, const double* Graw, double* Gn, const DevCheck* chk, cudaStream_t st,
                              BtileDesc bt = BtileDesc{nullptr, 0, 0}, float* F32lo = nullptr);
+
+// The mode's tail in one cooperative launch: the solve, the Gram, lambda, the new factor (and
+// its FP32 / BF16 copies), G_n, and on the last mode the fit (and the check when run_check).
+// gram_part: mode_tail_part_doubles(solve_blocks(In, R), R) doubles; bar: a zeroed GridBar;
+// err: set when a grid barrier's bounded wait expired.  cudaErrorNotSupported when the
+// blocks cannot all be resident: the caller runs launch_solve_rows, launch_gram_rows and
+// launch_normalize instead.
+cudaError_t launch_mode_tail(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
+                             const double* W, const SolveInfo* info, double* X, double* gram_part, double* F,
+                             float* F32r, float* F32lo, int64_t rpad, BtileDesc btd, double* Graw, double* lam,
+                             double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
+                             const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap, GridBar* bar,
+                             int* err, int num_sms, int run_check, cudaStream_t st);
+size_t mode_tail_part_doubles(int nblk, int R);
 
 // Row-major rows x cols -> row-major cols x rows (FP64).
 cudaError_t launch_transpose_f64(const double* src, int64_t rows, int64_t cols, double* dst, cudaStream_t st);

@@ -300,7 +300,8 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         atomicCAS(err, 0, 2);
         *abort_flag = 1;
       }
-      for (int it = 0; it < nloc && !*abort_flag; ++it) {
+      int64_t fbm = (c_begin % p.nfb);  // the chunk's factor block, kept without a division per chunk
+      for (int it = 0; it < nloc && !*abort_flag; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
         const int b = it % kBuf;
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         }
         tc_fence_after();
         const uint32_t ah = smem_u32(stage_a(s)), al = ah + a_bytes;
-        const uint32_t bh = smem_u32(b_tile(s, (c_begin + it) % p.nfb));
+        const uint32_t bh = smem_u32(b_tile(s, fbm));
         const uint32_t acc_h = tmem + (uint32_t)(b * kAcc * NB), acc_l = acc_h + (uint32_t)NB;
 #pragma unroll
         for (int kk = 0; kk < kChunk / 16; ++kk) {

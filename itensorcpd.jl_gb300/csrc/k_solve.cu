@@ -755,15 +755,14 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
 // and each output by eight.  Per-row sums of M .* X (a tree over the row) feed the fit.
 constexpr int SOLVE_T = 256;
 constexpr int kSolveStageMaxR = 128;  // W^T (R^2 doubles) staged in shared memory up to here
+// The solve of one block of RB rows (the block index `blk`); the rows' X stays in shared
+// memory (sm + 2 RB R) for a caller that continues with it.
 template <typename PT>
-__global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
-                                                        const double* __restrict__ WT, double* __restrict__ X,
-                                                        double* __restrict__ inner_rows, const DevCheck* chk,
-                                                        const SolveInfo* __restrict__ info,
-                                                        const float* __restrict__ ops,
-                                                        double* __restrict__ gpart) {
-  if (done_flag(chk)) return;
-  extern __shared__ double sm[];
+__device__ __forceinline__ void solve_rows_body(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
+                                                const double* __restrict__ WT, double* __restrict__ X,
+                                                double* __restrict__ inner_rows, const SolveInfo* __restrict__ info,
+                                                const float* __restrict__ ops, double* __restrict__ gpart, int blk,
+                                                double* sm) {
   double* Ms = sm;            // RB x R
   double* Ps = sm + RB * R;   // RB x R products for the fit
   double* Xs = sm + 2 * RB * R;  // RB x R: X before the refinement
@@ -778,7 +777,7 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
   const float* Vh = W32 + rr4(R);
   const float* Vl = W32 + 2 * rr4(R);
   const int tid = threadIdx.x;
-  const int64_t r0 = (int64_t)blockIdx.x * RB;
+  const int64_t r0 = (int64_t)blk * RB;
   const int rows = (In - r0 < (int64_t)RB) ? (int)(In - r0) : RB;
   const int nval = rows * R;
   const int64_t base = r0 * R;
@@ -948,7 +947,7 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
     // R-1-p, R+1 entries per pair), two accumulators over the block's rows
     __syncthreads();
     const int T = R * (R + 1) / 2;
-    double* gp = gpart + (size_t)blockIdx.x * T;
+    double* gp = gpart + (size_t)blk * T;
     for (int e = tid; e < T; e += SOLVE_T) {
       const int p = e / (R + 1), t = e - p * (R + 1);
       int a, b;
@@ -990,6 +989,18 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
       ir[3 * (r0 + row) + 2] = base;
     }
   }
+}
+
+template <typename PT>
+__global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ part, int S, int64_t In, int R, int RB,
+                                                        const double* __restrict__ WT, double* __restrict__ X,
+                                                        double* __restrict__ inner_rows, const DevCheck* chk,
+                                                        const SolveInfo* __restrict__ info,
+                                                        const float* __restrict__ ops,
+                                                        double* __restrict__ gpart) {
+  if (done_flag(chk)) return;
+  extern __shared__ double sm[];
+  solve_rows_body<PT>(part, S, In, R, RB, WT, X, inner_rows, info, ops, gpart, blockIdx.x, sm);
 }
 
 // ---------------- gram + finalize ----------------
@@ -1145,6 +1156,8 @@ struct FinalizeArgs {
 // and the device FitCheck / NoCheck update.  One block; loads are issued eight at a
 // time (a single FP64 dependent chain costs ~128 cycles per step here).  `coherent`
 // reads Graw through L2 (written by other blocks of the same launch).
+__device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam);
+
 __device__ void finalize_body(const double* __restrict__ Graw, int R, const FinalizeArgs& fa, bool coherent) {
   __shared__ double sv[32];
   __shared__ double s_lam[CPALS_MAX_RANK_SOLVE];
@@ -1179,19 +1192,29 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
     }
   }
   if (!fa.last) return;
+  finalize_fit(R, fa, s_lam);
+}
+
+// The fit's terms on the last mode (and the check's update when fa.run_check): <T, X> from the
+// rows' exact sums, ||X||^2 from the per-tile (per-block) shares or, without them, from the
+// Grams and lambda (lam: R values visible to the whole block).  One block.
+__device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int n = R * R;
   __shared__ int si[32];
   __shared__ long long sl[64];
   // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28): the rows' exact
   // fixed-point sums, aligned to the largest row base (+8: room for 2^36 rows) and added
   const long long* ir = fa.inner_rows_fx;
   int bmax = INT_MIN;
-  for (int64_t i = tid; i < fa.In; i += nt) bmax = max(bmax, (int)ir[3 * i + 2]);
+  for (int64_t i = tid; i < fa.In; i += nt) bmax = max(bmax, (int)__ldcg(&ir[3 * i + 2]));
   bmax = block_max_int(bmax, si);
   const int ib = (bmax == kFxBad) ? kFxBad : bmax + 8;
   __int128 qi = 0;
   if (ib != kFxBad)
     for (int64_t i = tid; i < fa.In; i += nt)
-      qi += fx_align(fx_join((unsigned long long)ir[3 * i], ir[3 * i + 1]), (int)ir[3 * i + 2], ib);
+      qi += fx_align(fx_join((unsigned long long)__ldcg(&ir[3 * i]), __ldcg(&ir[3 * i + 1])), (int)__ldcg(&ir[3 * i + 2]),
+                     ib);
   const __int128 inner = block_sum_fx(qi, sl);
   // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11): with the per-tile
   // (per-block) shares of the fused path, their exact sums; otherwise each term formed here
@@ -1212,7 +1235,7 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
       double h = fa.gs.G[0][e];
       for (int m = 1; m < fa.order; ++m) h *= fa.gs.G[m][e];
       const int r = e / R, c2 = e - r * R;
-      return h * s_lam[r] * s_lam[c2];
+      return h * lam[r] * lam[c2];
     };
     int m = 1;
     for (int e = tid; e < n; e += nt) m = max(m, fx_exp(term(e)));
@@ -1424,6 +1447,28 @@ __global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ Gra
 }
 
 // ---------------- normalize ----------------
+// Entry (i, r) of the new factor f = X(i, r) / lambda_r and its copies: the FP32 row-major
+// copy, its FP32 remainder, and the BF16 hi / lo pair in the tensor-core MTTKRP's tile.
+__device__ __forceinline__ void store_factor_entry(int64_t i, int r, int R, double f, double* __restrict__ F,
+                                                   float* __restrict__ F32r, float* __restrict__ F32lo, int64_t rpad,
+                                                   const BtileDesc& btd) {
+  F[i * R + r] = f;
+  if (F32r) F32r[i * rpad + r] = (float)f;
+  if (F32lo) F32lo[i * rpad + r] = (float)(f - (double)(float)f);  // f = hi + lo to 2^-48
+  if (btd.bt) {
+    // hi = bf16(f), lo = bf16(f - hi), at row i of column r in its tile
+    const __nv_bfloat16 h = __double2bfloat16(f);
+    const __nv_bfloat16 l = __double2bfloat16(f - (double)__bfloat162float(h));
+    const int nblk = r / btd.nb, rr = r - nblk * btd.nb;
+    const int64_t fb = i >> 6;
+    const int kk = (int)(i & 63);
+    uint8_t* tile = btd.bt + (size_t)(fb * btd.n_blocks + nblk) * (2 * (size_t)btd.nb * 64 * 2);
+    const uint32_t off = (uint32_t)rr * 128u + ((uint32_t)((kk >> 3) ^ (rr & 7)) << 4) + (uint32_t)(kk & 7) * 2u;
+    *reinterpret_cast<__nv_bfloat16*>(tile + off) = h;
+    *reinterpret_cast<__nv_bfloat16*>(tile + (size_t)btd.nb * 64 * 2 + off) = l;
+  }
+}
+
 __global__ void k_normalize(const double* __restrict__ X, const double* __restrict__ lam_inv, int64_t In, int R,
                             double* __restrict__ F, float* __restrict__ F32r,
                             int64_t rpad, const double* __restrict__ Graw, double* __restrict__ Gn,
@@ -1435,21 +1480,7 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
     const int64_t i = e / R;
     const int r = (int)(e % R);
     const double f = lam_inv ? X[e] * lam_inv[r] : X[e];
-    F[e] = f;
-    if (F32r) F32r[i * rpad + r] = (float)f;
-    if (F32lo) F32lo[i * rpad + r] = (float)(f - (double)(float)f);  // f = hi + lo to 2^-48
-    if (btd.bt) {
-      // hi = bf16(f), lo = bf16(f - hi), at row i of column r in its tile
-      const __nv_bfloat16 h = __double2bfloat16(f);
-      const __nv_bfloat16 l = __double2bfloat16(f - (double)__bfloat162float(h));
-      const int nblk = r / btd.nb, rr = r - nblk * btd.nb;
-      const int64_t fb = i >> 6;
-      const int kk = (int)(i & 63);
-      uint8_t* tile = btd.bt + (size_t)(fb * btd.n_blocks + nblk) * (2 * (size_t)btd.nb * 64 * 2);
-      const uint32_t off = (uint32_t)rr * 128u + ((uint32_t)((kk >> 3) ^ (rr & 7)) << 4) + (uint32_t)(kk & 7) * 2u;
-      *reinterpret_cast<__nv_bfloat16*>(tile + off) = h;
-      *reinterpret_cast<__nv_bfloat16*>(tile + (size_t)btd.nb * 64 * 2 + off) = l;
-    }
+    store_factor_entry(i, r, R, f, F, F32r, F32lo, rpad, btd);
   }
   // the normalised Gram G_n = Graw ./ (lambda lambda^T), by the reciprocals
   if (Gn)
@@ -1457,6 +1488,158 @@ __global__ void k_normalize(const double* __restrict__ X, const double* __restri
       const int r = (int)(e / R), c = (int)(e % R);
       Gn[e] = Graw[e] * lam_inv[r] * lam_inv[c];
     }
+}
+
+// ---------------- the fused mode tail: solve, Gram, lambda, normalisation ----------------
+// One cooperative launch per mode (all blocks resident) in place of the solve, the Gram
+// reduction and the normalisation kernels, with two grid barriers:
+//   1. each block solves its RB rows (X stays in shared memory) and writes its partial Gram;
+//   2. the blocks split the R(R+1)/2 Gram entries: each sums its entries over the blocks'
+//      partials, writes Graw, and lambda, 1 / lambda for the diagonal ones; on the last mode
+//      also its exact share of ||X||^2;
+//   3. each block normalises its rows from shared memory and writes G_n entries; on the last
+//      mode block 0 then runs the finalize step (the fit and the check).
+// The barrier waits are bounded: on expiry the kernel records an error and carries on (the
+// host reports CPALS_E_DEVICE); it never waits forever.
+constexpr uint32_t kGridSpin = 1u << 22;
+__device__ __forceinline__ void grid_barrier(GridBar* b, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = &b->gen;
+    const unsigned g0 = *gen;
+    __threadfence();
+    if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+      b->count = 0u;
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      uint32_t it = 0;
+      while (*gen == g0) {
+        if (++it > kGridSpin) {
+          atomicExch(err, 1);
+          break;
+        }
+        if (it > 64) __nanosleep(128);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+struct TailArgs {
+  const void* part;
+  int part_f32, S, R, RB;
+  int64_t In;
+  const double* WT;
+  const SolveInfo* info;
+  const float* ops;
+  double* X;
+  double* gpart;  // nblk * R(R+1)/2 partial Grams, then 3 words per block (||X||^2 shares)
+  double* F;
+  float* F32r;
+  float* F32lo;
+  int64_t rpad;
+  BtileDesc btd;
+  GridBar* bar;
+  int* err;
+  double* Graw;
+  FinalizeArgs fa;  // lambda, 1 / lambda, G_n, the Grams, the fit's inputs
+};
+
+template <typename PT>
+__global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
+  if (done_flag(a.fa.chk)) return;  // uniform: only block 0 sets `done`, after every block passed barrier 2
+  extern __shared__ double sm[];
+  const int R = a.R, RB = a.RB, tid = threadIdx.x, nt = blockDim.x;
+  const int nblk = gridDim.x;
+  const int T = R * (R + 1) / 2;
+  // ---- 1: the rows' solve (X stays in shared memory), the block's partial Gram, the rows'
+  // <T, X> terms on the last mode
+  double* inner = a.fa.last ? const_cast<double*>(reinterpret_cast<const double*>(a.fa.inner_rows_fx)) : nullptr;
+  solve_rows_body<PT>(static_cast<const PT*>(a.part), a.S, a.In, R, RB, a.WT, a.X, inner, a.info, a.ops, a.gpart,
+                      blockIdx.x, sm);
+  grid_barrier(a.bar, a.err);
+  // ---- 2: Gram entries [e0, e1) of this block, each summed over the blocks' partials in
+  // block order (eight slices of the partials, then the slices in order), 32 entries at a time
+  const int per = (T + nblk - 1) / nblk;
+  const int e0 = min(T, blockIdx.x * per), e1 = min(T, e0 + per);
+  __shared__ double red[8][33];
+  const int lane = tid & 31, sl = tid >> 5;
+  auto entry = [&](int e, int& r, int& c) {  // the upper-triangle pairing of the partial Grams
+    const int p = e / (R + 1), t = e - p * (R + 1);
+    if (t < R - p) {
+      r = p;
+      c = p + t;
+    } else {
+      r = R - 1 - p;
+      c = r + (t - (R - p));
+    }
+  };
+  for (int eb = e0; eb < e1; eb += 32) {
+    const int e = eb + lane;
+    double acc = 0.0;
+    if (e < e1)
+      for (int b = sl; b < nblk; b += 8) acc += __ldcg(&a.gpart[(size_t)b * T + e]);
+    red[sl][lane] = acc;
+    __syncthreads();
+    if (sl == 0 && e < e1) {
+      double sum = 0.0;
+      for (int q = 0; q < 8; ++q) sum += red[q][lane];
+      int r, c;
+      entry(e, r, c);
+      a.Graw[(size_t)r * R + c] = sum;
+      a.Graw[(size_t)c * R + r] = sum;
+      if (r == c) {
+        const double ri = rsqrt(sum);
+        a.fa.lam[r] = sum * ri;
+        a.fa.lam_inv[r] = ri;
+      }
+    }
+    __syncthreads();
+  }
+  if (a.fa.last && sl == 0) {
+    // this block's share of ||X||^2 = sum over its entries of Graw .* prod_{m != mode} G_m
+    // (off-diagonal entries twice), exact in fixed point; each lane reads back the entries
+    // it wrote above
+    auto share = [&](int e) {
+      int r, c;
+      entry(e, r, c);
+      double v = a.Graw[(size_t)r * R + c];
+      v = (r == c) ? v : 2.0 * v;
+      for (int m = 0; m < a.fa.order; ++m)
+        if (m != a.fa.mode) v *= a.fa.gs.G[m][(size_t)r * R + c];
+      return v;
+    };
+    int em = 1;
+    for (int e = e0 + lane; e < e1; e += 32) em = max(em, fx_exp(share(e)));
+    em = __reduce_max_sync(0xffffffffu, em);
+    const int base = (em == 0x7ff) ? kFxBad : em - kFxHead;
+    __int128 q = 0;
+    if (base != kFxBad)
+      for (int e = e0 + lane; e < e1; e += 32) q += fx_term(share(e), base);
+    q = fx_warp_sum(q);
+    if (lane == 0) {
+      long long* fp = reinterpret_cast<long long*>(a.fa.fpart);
+      fp[3 * blockIdx.x] = (long long)(unsigned long long)q;
+      fp[3 * blockIdx.x + 1] = (long long)(q >> 64);
+      fp[3 * blockIdx.x + 2] = base;
+    }
+  }
+  grid_barrier(a.bar, a.err);
+  // ---- 3: normalise this block's rows (X in shared memory) and write G_n entries
+  const int64_t r0 = (int64_t)blockIdx.x * RB;
+  const int rows = (a.In - r0 < (int64_t)RB) ? (int)(a.In - r0) : RB;
+  const double* Xs = sm + 2 * RB * R;
+  for (int e = tid; e < rows * R; e += nt) {
+    const int row = e / R, r = e - row * R;
+    store_factor_entry(r0 + row, r, R, Xs[e] * __ldcg(&a.fa.lam_inv[r]), a.F, a.F32r, a.F32lo, a.rpad, a.btd);
+  }
+  for (int e = blockIdx.x * nt + tid; e < R * R; e += nblk * nt) {
+    const int r = e / R, c = e - r * R;
+    a.fa.Gn[e] = __ldcg(&a.Graw[e]) * __ldcg(&a.fa.lam_inv[r]) * __ldcg(&a.fa.lam_inv[c]);
+  }
+  if (a.fa.last && blockIdx.x == 0) finalize_fit(R, a.fa, nullptr);  // fpart is set: lam unused
 }
 
 __global__ void k_transpose(const double* __restrict__ src, int64_t rows, int64_t cols, double* __restrict__ dst) {
@@ -1709,6 +1892,60 @@ cudaError_t launch_solve_rows(const void* part, int part_is_f32, int splits, int
                                                       inner_rows, chk, info, ops, gram_part);
   return cudaGetLastError();
 }
+
+// The fused tail's shared memory is the solve's; it runs when every block of rows can be
+// resident at once (a cooperative launch).  Returns cudaErrorNotSupported when it cannot,
+// and the caller takes the three-kernel path.
+cudaError_t launch_mode_tail(const void* part, int part_is_f32, int splits, int64_t In, int R, const double* work,
+                             const double* W, const SolveInfo* info, double* X, double* gram_part, double* F,
+                             float* F32r, float* F32lo, int64_t rpad, BtileDesc btd, double* Graw, double* lam,
+                             double* lam_inv, double* Gn, const GramSet& gs, int order, int last,
+                             const double* inner_rows, DevCheck* chk, double* traj, int64_t traj_cap, GridBar* bar,
+                             int* err, int num_sms, int run_check, cudaStream_t st) {
+  const int RB = solve_rows_per_block(R);
+  const int nblk = solve_blocks(In, R);
+  const size_t fw = (size_t)((RB * R + 3) & ~3) / 2;
+  size_t smem = ((size_t)3 * RB * R + 2 * fw + 1) * sizeof(double);
+  if (R <= kSolveStageMaxR) smem += std::max((size_t)R * R * sizeof(double), (size_t)3 * rr4(R) * sizeof(float));
+  const void* kfn = part_is_f32 ? (const void*)k_mode_tail<float> : (const void*)k_mode_tail<double>;
+  {
+    const int mx = (3 * 256 + 2 * 128 + 1) * 8 + 3 * rr4(kSolveStageMaxR) * 4;
+    cudaError_t ea = set_smem_limit_once(kfn, mx);
+    if (ea != cudaSuccess) return ea;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, SOLVE_T, smem);
+  if (e != cudaSuccess) return e;
+  if ((int64_t)per_sm * num_sms < nblk) return cudaErrorNotSupported;
+  const int T = R * (R + 1) / 2;
+  TailArgs a{};
+  a.part = part;
+  a.part_f32 = part_is_f32;
+  a.S = splits;
+  a.R = R;
+  a.RB = RB;
+  a.In = In;
+  a.WT = W;
+  a.info = info;
+  a.ops = reinterpret_cast<const float*>(work + ops32_offset_doubles(R));
+  a.X = X;
+  a.gpart = gram_part;
+  a.F = F;
+  a.F32r = F32r;
+  a.F32lo = F32lo;
+  a.rpad = rpad;
+  a.btd = btd;
+  a.bar = bar;
+  a.err = err;
+  a.Graw = Graw;
+  // the blocks' exact shares of ||X||^2 follow the partial Grams (3 words per block)
+  a.fa = FinalizeArgs{lam, lam_inv, Gn, gs, order, last, reinterpret_cast<const long long*>(inner_rows), In, chk,
+                      traj, traj_cap, order - 1, gram_part + (size_t)nblk * T, nblk, run_check};
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel(kfn, dim3((unsigned)nblk), dim3(SOLVE_T), args, smem, st);
+}
+
+size_t mode_tail_part_doubles(int nblk, int R) { return (size_t)nblk * R * (R + 1) / 2 + 3 * (size_t)nblk; }
 
 int gram_tiles(int R) {
   const int nt = (R + GT - 1) / GT;

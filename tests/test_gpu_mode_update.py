@@ -128,3 +128,20 @@ def test_mode_update_after_a_converged_optimize_still_updates(built):
         e.mode_update(0)
         after, _ = e.get_factors()
         assert not np.array_equal(before[0], after[0])
+
+
+def test_a_sweep_runs_one_fused_tail_per_mode(built):
+    # per mode: the factorisation, the MTTKRP and one cooperative launch for the solve, the
+    # Gram, lambda and the normalisation (the fit included on the last mode)
+    from itensorcpd_gb300 import _lib as L
+
+    dims, R = (40, 30, 20), 6
+    T = np.asfortranarray(det_normal(8, dims))
+    F0, lam0 = det_factors(dims, R, seed=8)
+    with built.Engine(dims, R) as e:
+        e.set_tensor(T)
+        e.set_factors(F0, lam0)
+        c = fitcheck(L, float(np.linalg.norm(T)), 3)
+        l0 = e.launch_count()
+        e.optimize(c)
+        assert e.launch_count() - l0 == 3 * 3 * len(dims)

@@ -442,8 +442,8 @@ __global__ void __launch_bounds__(NT) k_batch_sweep(const BatchItem* __restrict_
   }
 }
 
-__global__ void k_batch_reset(unsigned* queue, const BatchCheck* chk, int count, int* active) {
-  // queue reset for the next launch, and the count of active tensors (read by the host)
+__global__ void k_batch_reset(unsigned* queue, int nqueue, const BatchCheck* chk, int count, int* active) {
+  // queue resets for the next launch, and the count of active tensors (read by the host)
   __shared__ int s;
   if (threadIdx.x == 0) s = 0;
   __syncthreads();
@@ -451,10 +451,8 @@ __global__ void k_batch_reset(unsigned* queue, const BatchCheck* chk, int count,
   for (int i = threadIdx.x; i < count; i += blockDim.x) a += chk[i].done ? 0 : 1;
   atomicAdd(&s, a);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    *queue = 0u;
-    *active = s;
-  }
+  if (threadIdx.x < nqueue) queue[threadIdx.x] = 0u;
+  if (threadIdx.x == 0) *active = s;
 }
 
 // Grams of the initial factors, and lambda / checks reset.
@@ -488,6 +486,21 @@ __global__ void k_batch_init(const BatchItem* __restrict__ items, int count, dou
 
 using namespace cpals;
 
+// A size class of the batch: the tensors order[begin, end) (largest work first), swept by one
+// persistent launch with a shared-memory layout sized to the class's largest extent and rank,
+// so that small tensors get several CTAs per SM.  Classes run concurrently on their own streams.
+struct BatchClass {
+  int begin = 0, end = 0;
+  int Imax = 0, Rmax = 0;
+  SmemLayout L{};
+  int nt = 256;
+  int ctas_per_sm = 1;
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  float ms_alone = 0.f;  // the autotuner's time for this class alone
+};
+constexpr int kMaxBatchClasses = 4;
+
 struct cpals_batch {
   int device = 0;
   int64_t count = 0;
@@ -513,48 +526,112 @@ struct cpals_batch {
   int num_sms = 0;
   SmemLayout L{};
   int64_t launches = 0;
+  // the schedule: one class (every tensor, layout L) or the classes by CTAs per SM
+  std::vector<BatchClass> cls;
+  std::vector<int> order_one, order_split;  // LPT order of the single class; by class, then LPT
+  std::vector<BatchClass> split;           // the candidate classes
+  cudaEvent_t fork = nullptr;
 };
 
 namespace {
 
-int batch_launch(cpals_batch* b) {
-  const int grid = b->num_sms * b->ctas_per_sm;
-  switch (b->nt) {
+const void* sweep_fn(int nt) {
+  return nt == 128 ? (const void*)k_batch_sweep<128> : nt == 256 ? (const void*)k_batch_sweep<256>
+                                                                 : (const void*)k_batch_sweep<512>;
+}
+
+// One class's persistent launch on stream st (queue slot q).
+int class_launch(cpals_batch* b, const BatchClass& c, int q, cudaStream_t st) {
+  const int n = c.end - c.begin;
+  if (n <= 0) return CPALS_OK;
+  const int grid = std::min(b->num_sms * c.ctas_per_sm, n);
+  const int* order = b->d_order + c.begin;
+  switch (c.nt) {
     case 128:
-      k_batch_sweep<128><<<grid, 128, b->L.total, b->st>>>(b->d_items, b->d_order, (int)b->count, b->d_T, b->d_F,
-                                                             b->d_G, b->d_chk, b->d_queue, b->L, b->tol, b->max_iter);
+      k_batch_sweep<128><<<grid, 128, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
+                                                          b->d_queue + q, c.L, b->tol, b->max_iter);
       break;
     case 256:
-      k_batch_sweep<256><<<grid, 256, b->L.total, b->st>>>(b->d_items, b->d_order, (int)b->count, b->d_T, b->d_F,
-                                                             b->d_G, b->d_chk, b->d_queue, b->L, b->tol, b->max_iter);
+      k_batch_sweep<256><<<grid, 256, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
+                                                          b->d_queue + q, c.L, b->tol, b->max_iter);
       break;
     case 512:
-      k_batch_sweep<512><<<grid, 512, b->L.total, b->st>>>(b->d_items, b->d_order, (int)b->count, b->d_T, b->d_F,
-                                                             b->d_G, b->d_chk, b->d_queue, b->L, b->tol, b->max_iter);
+      k_batch_sweep<512><<<grid, 512, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
+                                                          b->d_queue + q, c.L, b->tol, b->max_iter);
       break;
     default:
       return CPALS_E_ARG;
   }
-  k_batch_reset<<<1, 1024, 0, b->st>>>(b->d_queue, b->d_chk, (int)b->count, b->d_active);
-  b->launches += 2;
+  b->launches += 1;
   return cudaGetLastError() == cudaSuccess ? CPALS_OK : CPALS_E_CUDA;
 }
 
-int set_config(cpals_batch* b, int nt) {
-  const void* fn = nt == 128 ? (const void*)k_batch_sweep<128> : nt == 256 ? (const void*)k_batch_sweep<256>
-                                                                            : (const void*)k_batch_sweep<512>;
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->L.total) != cudaSuccess)
+// One sweep of every active tensor: the classes' launches forked from and joined back to the
+// batch's stream, then the queue resets and the active count.
+int batch_launch(cpals_batch* b) {
+  const int nc = (int)b->cls.size();
+  if (nc == 1) {
+    int rc = class_launch(b, b->cls[0], 0, b->st);
+    if (rc != CPALS_OK) return rc;
+  } else {
+    if (cudaEventRecord(b->fork, b->st) != cudaSuccess) return CPALS_E_CUDA;
+    for (int i = 0; i < nc; ++i) {
+      BatchClass& c = b->cls[i];
+      if (cudaStreamWaitEvent(c.st, b->fork, 0) != cudaSuccess) return CPALS_E_CUDA;
+      int rc = class_launch(b, c, i, c.st);
+      if (rc != CPALS_OK) return rc;
+      if (cudaEventRecord(c.done, c.st) != cudaSuccess || cudaStreamWaitEvent(b->st, c.done, 0) != cudaSuccess)
+        return CPALS_E_CUDA;
+    }
+  }
+  k_batch_reset<<<1, 1024, 0, b->st>>>(b->d_queue, kMaxBatchClasses, b->d_chk, (int)b->count, b->d_active);
+  b->launches += 1;
+  return cudaGetLastError() == cudaSuccess ? CPALS_OK : CPALS_E_CUDA;
+}
+
+// Thread count of class c: sets the kernel's shared-memory limit and the resident CTAs per SM.
+int class_config(BatchClass& c, int nt) {
+  const void* fn = sweep_fn(nt);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
     return CPALS_E_CUDA;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, b->L.total) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, c.L.total) != cudaSuccess || per_sm < 1)
     return CPALS_E_UNSUPPORTED;
-  b->nt = nt;
-  b->ctas_per_sm = per_sm;
+  c.nt = nt;
+  c.ctas_per_sm = per_sm;
+  return CPALS_OK;
+}
+
+void drop_graph(cpals_batch* b) {
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
+}
+
+// Makes `classes` (with `order`) the schedule: uploads the order, rebuilds the graph later.
+int use_schedule(cpals_batch* b, const std::vector<BatchClass>& classes, const std::vector<int>& order) {
+  CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
+  CPALS_CUDA_TRY(cudaMemcpy(b->d_order, order.data(), sizeof(int) * b->count, cudaMemcpyHostToDevice));
+  b->cls = classes;
+  drop_graph(b);
   return CPALS_OK;
+}
+
+// The single class with nt threads per CTA (the whole batch, the batch-wide layout).
+int set_config(cpals_batch* b, int nt) {
+  BatchClass c;
+  c.begin = 0;
+  c.end = (int)b->count;
+  c.Imax = b->Imax;
+  c.Rmax = b->Rmax;
+  c.L = b->L;
+  c.st = b->st;
+  int rc = class_config(c, nt);
+  if (rc != CPALS_OK) return rc;
+  b->nt = nt;
+  b->ctas_per_sm = c.ctas_per_sm;
+  return use_schedule(b, {c}, b->order_one);
 }
 
 int build_graph(cpals_batch* b) {
@@ -626,6 +703,32 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
     work[t] = (double)it.I[0] * it.I[1] * it.I[2] * it.R + 3.0 * it.R * it.R * it.R * 20.0;
   }
   std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) { return work[a] > work[c]; });
+  b->order_one = b->order;
+  // The candidate split: by the CTAs per SM a tensor's own layout allows (1 to 4, at the
+  // batch's largest rank), one class per value; LPT order inside each class.
+  {
+    std::vector<int> cps(count);
+    for (int64_t t = 0; t < count; ++t) {
+      const BatchItem& it = b->items[t];
+      const size_t tot = smem_layout(std::max({it.I[0], it.I[1], it.I[2]}), b->Rmax).total;
+      cps[t] = (int)std::max<size_t>(1, std::min<size_t>(kMaxBatchClasses, (227 * 1024) / tot));
+    }
+    for (int k = 1; k <= kMaxBatchClasses; ++k) {
+      BatchClass c;
+      c.begin = (int)b->order_split.size();
+      for (int t : b->order)
+        if (cps[t] == k) {
+          b->order_split.push_back(t);
+          c.Imax = std::max({c.Imax, b->items[t].I[0], b->items[t].I[1], b->items[t].I[2]});
+          c.Rmax = std::max(c.Rmax, b->items[t].R);
+        }
+      c.end = (int)b->order_split.size();
+      if (c.end > c.begin) {
+        c.L = smem_layout(c.Imax, c.Rmax);
+        b->split.push_back(c);
+      }
+    }
+  }
   cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
   bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
             cudaMalloc(&b->d_items, sizeof(BatchItem) * count) == cudaSuccess &&
@@ -634,16 +737,20 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
             cudaMalloc(&b->d_F, sizeof(double) * b->tot_F) == cudaSuccess &&
             cudaMalloc(&b->d_G, sizeof(double) * b->tot_G) == cudaSuccess &&
             cudaMalloc(&b->d_chk, sizeof(BatchCheck) * count) == cudaSuccess &&
-            cudaMalloc(&b->d_queue, sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc(&b->d_queue, sizeof(unsigned) * kMaxBatchClasses) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
             cudaMalloc(&b->d_active, sizeof(int)) == cudaSuccess &&
             cudaMallocHost(&b->h_active, sizeof(int)) == cudaSuccess;
+  for (BatchClass& c : b->split)
+    ok = ok && cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming) == cudaSuccess;
   if (!ok) {
     cpals_batch_destroy(b);
     return CPALS_E_CUDA;
   }
   cudaMemcpy(b->d_items, b->items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_order, b->order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
-  cudaMemset(b->d_queue, 0, sizeof(unsigned));
+  cudaMemset(b->d_queue, 0, sizeof(unsigned) * kMaxBatchClasses);
   cudaMemset(b->d_chk, 0, sizeof(BatchCheck) * count);
   int rc = set_config(b, 256);
   if (rc != CPALS_OK) rc = set_config(b, 128);
@@ -667,6 +774,11 @@ int cpals_batch_destroy(cpals_batch* b) {
   cudaFree(b->d_queue);
   cudaFree(b->d_active);
   if (b->h_active) cudaFreeHost(b->h_active);
+  for (BatchClass& c : b->split) {
+    if (c.st) cudaStreamDestroy(c.st);
+    if (c.done) cudaEventDestroy(c.done);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return CPALS_OK;
@@ -686,7 +798,7 @@ int cpals_batch_set_factors(cpals_batch* b, const double* host_concat) {
   const int blocks = (int)std::min<int64_t>(b->count, 4096);
   k_batch_init<<<blocks, 256, 0, b->st>>>(b->d_items, (int)b->count, b->d_F, b->d_G, b->d_chk);
   CPALS_CUDA_TRY(cudaGetLastError());
-  CPALS_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->st));
+  CPALS_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned) * kMaxBatchClasses, b->st));
   b->launches += 1;
   return CPALS_OK;
 }
@@ -726,7 +838,7 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
   while (launched < max_iter) {
     const int n = std::min(batch, max_iter - launched);
     for (int k = 0; k < n; ++k) CPALS_CUDA_TRY(cudaGraphLaunch(b->graph, b->st));
-    b->launches += 2 * n;
+    b->launches += (int64_t)(b->cls.size() + 1) * n;
     launched += n;
     CPALS_CUDA_TRY(cudaMemcpyAsync(b->h_active, b->d_active, sizeof(int), cudaMemcpyDeviceToHost, b->st));
     CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));

@@ -625,20 +625,26 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
       const float thr = misc[0];
       bool bad = false;
       for (int k = 0; k < pb; ++k) {
-        float dik = 0.f;
+        // D(i, k): one nonzero among 32 selected terms, summed as a depth-5 tree (exact)
+        float t[kBlk32];
 #pragma unroll
-        for (int c = 0; c < kBlk32; ++c) dik = (c == k) ? r[c] : dik;  // D(i, k)
+        for (int c = 0; c < kBlk32; ++c) t[c] = (c == k) ? r[c] : 0.f;
+#pragma unroll
+        for (int w = kBlk32 / 2; w > 0; w >>= 1)
+#pragma unroll
+          for (int c = 0; c < w; ++c) t[c] += t[c + w];
+        const float dik = t[0];
         const float d = __shfl_sync(0xffffffffu, dik, k);
         bad = bad || !(d > thr) || !(d < INFINITY);
         const float rd = 1.0f / d;
         const float f = dik * rd;
+        const bool me = (lane == k);  // row k itself: per-lane selects, no divergent branch
+        const float pk = me ? -rd : f;
 #pragma unroll
         for (int c = 0; c < kBlk32; ++c) {
           const float rkc = __shfl_sync(0xffffffffu, r[c], k);  // D(k, c)
-          if (lane == k)
-            r[c] = (c == k) ? -rd : rkc * rd;
-          else
-            r[c] = (c == k) ? f : fmaf(-f, rkc, r[c]);
+          const float v = me ? rkc * rd : fmaf(-f, rkc, r[c]);
+          r[c] = (c == k) ? pk : v;
         }
       }
       if (lane < pb) {

@@ -540,6 +540,7 @@ def run_c4(args, pkg, device):
     with pkg.BatchEngine(dims, ranks, norms, device=device) as be:
         be.set_tensors_concat(cat)
         nt, tune_ms = be.autotune(Fs, lams, sweeps=2)
+        sched, split_ms = be.schedule()
         runs = []
         for _ in range(max(1, args.steps)):
             be.set_factors(Fs, lams)
@@ -609,7 +610,8 @@ def run_c4(args, pkg, device):
         "gpu_loop_baseline": {"value": sub / loop_s, "unit": "solves/s", "tensors": sub,
                               "what": "a host loop of the single-tensor engine (FP64 MTTKRP, FitCheck(1e-5, 200)): "
                                       "handle, tensor upload, solve, factors out, per tensor"},
-        "autotune": {"threads": nt, "ms_per_2_sweeps": {str(k): float(v) for k, v in tune_ms.items()}},
+        "autotune": {"threads": nt, "one_class_ms_per_2_sweeps": {str(k): float(v) for k, v in tune_ms.items()},
+                     "split_ms_per_2_sweeps": split_ms, "classes": sched},
         "stopped_by_fitcheck": int(np.sum((flags & 4) != 0) - np.sum(sweeps >= 200)),
         "hit_200_sweeps": int(np.sum(sweeps >= 200)), "nan": int(np.sum(flags & 1)),
         "rank_deficient": int(np.sum((flags & 2) != 0)),

@@ -334,9 +334,18 @@ int cpals_batch_set_threads(cpals_batch* b, int threads);
  * final fit, flags (1 NaN fit, 2 rank-deficient normal equations met, 4 stopped). */
 int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_out, double* fits_out, int* flags_out,
                          int64_t* launches_out);
-/* Times `sweeps` sweeps from host_factors for each thread count, keeps the fastest, and
- * restores host_factors.  ms_out (3 entries, may be null): 128, 256, 512 threads. */
+/* Autotuner of the launch schedule, timing `sweeps` sweeps from host_factors per candidate (and
+ * restoring host_factors): one class of every tensor at 128, 256 and 512 threads per CTA
+ * (ms_out, 3 entries, may be null), and a split into size classes by the CTAs per SM each
+ * tensor's shared-memory layout allows (1 to 4), each class with its own layout, thread count
+ * (chosen by timing the class alone) and stream, the classes running concurrently.  The
+ * fastest schedule is kept; threads_out receives its largest thread count. */
 int cpals_batch_autotune(cpals_batch* b, const double* host_factors, int sweeps, int* threads_out, double* ms_out);
+/* The schedule in use: *nclass classes; info (6 entries per class, may be null): tensors,
+ * largest extent, largest rank, threads per CTA, resident CTAs per SM, and the class's time
+ * alone in microseconds (0 when not timed); *ms_split (may be null) the split schedule's time
+ * in the last autotune (< 0 when not tried). */
+int cpals_batch_schedule(cpals_batch* b, int* nclass, int64_t* info, double* ms_split);
 
 /* ---- seeded synthetic tensors on the device (no counterpart in the reference) ----
  * T = sum_r w_r F_0(:,r) o F_1(:,r) o ... + Gaussian noise at snr_db (counter-based, from

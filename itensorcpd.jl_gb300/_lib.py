@@ -108,6 +108,7 @@ SIGNATURES = {
     "cpals_batch_optimize": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(C.c_int), _DP, C.POINTER(C.c_int),
                                        _I64P]),
     "cpals_batch_autotune": (C.c_int, [_P, _DP, C.c_int, C.POINTER(C.c_int), _DP]),
+    "cpals_batch_schedule": (C.c_int, [_P, C.POINTER(C.c_int), _I64P, _DP]),
     "cpals_synth_lowrank": (C.c_int, [C.c_int, C.c_int, _I64P, C.c_int64, _DP, _DP, C.c_double, C.c_uint64, _P]),
     "cpals_mlp_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(C.c_int)]),
     "cpals_mlp_destroy": (C.c_int, [_P]),

@@ -110,6 +110,17 @@ class BatchEngine:
         self._factors_keep = buf
         return int(nt.value), {128: ms[0], 256: ms[1], 512: ms[2]}
 
+    def schedule(self):
+        """The launch schedule in use: a list of per-class dicts (tensors, largest extent, largest
+        rank, threads, CTAs per SM, microseconds alone) and the split schedule's autotune time."""
+        n = C.c_int()
+        info = np.zeros(6 * 4, dtype=np.int64)
+        ms = C.c_double()
+        L.check(self.lib.cpals_batch_schedule(self.h, C.byref(n), L.i64ptr(info), C.byref(ms)), "cpals_batch_schedule")
+        keys = ("tensors", "max_extent", "max_rank", "threads", "ctas_per_sm", "us_alone")
+        classes = [dict(zip(keys, (int(x) for x in info[6 * i:6 * i + 6]))) for i in range(n.value)]
+        return classes, float(ms.value)
+
     def optimize(self, tol=1e-5, max_iter=200):
         """FitCheck(tol, max_iter) per tensor; returns (sweeps, fits, flags, kernel launches)."""
         sweeps = np.zeros(self.count, dtype=np.int32)

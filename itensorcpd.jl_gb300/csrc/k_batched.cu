@@ -531,6 +531,7 @@ struct cpals_batch {
   std::vector<int> order_one, order_split;  // LPT order of the single class; by class, then LPT
   std::vector<BatchClass> split;           // the candidate classes
   cudaEvent_t fork = nullptr;
+  double ms_split = -1.0;  // the autotuner's time for the split schedule (< 0: not tried)
 };
 
 namespace {
@@ -858,45 +859,118 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
   return CPALS_OK;
 }
 
-// Autotuner: time `sweeps` sweeps of the batch (from its current factors) for each thread
-// count the shared-memory layout allows, keep the fastest.  The factors are restored from
-// `host_factors` after each trial.
+// Autotuner.  Schedules tried, each timed over `sweeps` sweeps from host_factors (restored
+// after every trial):
+//   - one class (every tensor, the batch-wide layout) with 128, 256 and 512 threads per CTA;
+//   - the split by CTAs per SM: each class's thread count chosen by timing the class alone,
+//     then the classes together, concurrently on their own streams.
+// The fastest schedule is kept.  ms_out (3 entries, may be null): the one-class trials.
 int cpals_batch_autotune(cpals_batch* b, const double* host_factors, int sweeps, int* threads_out,
                          double* ms_out) {
   if (!b || !host_factors || sweeps < 1) return CPALS_E_ARG;
   DeviceGuard guard(b->device);
-  const int cand[3] = {128, 256, 512};
-  double best = 1e300;
-  int best_nt = 0;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (int i = 0; i < 3; ++i) {
-    if (set_config(b, cand[i]) != CPALS_OK) continue;
+  auto timed = [&](float* ms) -> int {  // `sweeps` sweeps under the current schedule
     int rc = cpals_batch_set_factors(b, host_factors);
     if (rc != CPALS_OK) return rc;
     cudaEventRecord(e0, b->st);
-    for (int s = 0; s < sweeps; ++s) {
+    for (int s2 = 0; s2 < sweeps; ++s2) {
       rc = batch_launch(b);
       if (rc != CPALS_OK) return rc;
     }
     cudaEventRecord(e1, b->st);
     cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    return CPALS_OK;
+  };
+  const int cand[3] = {128, 256, 512};
+  float best = 3.0e38f;
+  int best_nt = 0;
+  for (int i = 0; i < 3; ++i) {
+    if (ms_out) ms_out[i] = -1.0;
+    if (set_config(b, cand[i]) != CPALS_OK) continue;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
+    int rc = timed(&ms);
+    if (rc != CPALS_OK) return rc;
     if (ms_out) ms_out[i] = ms;
     if (ms < best) {
       best = ms;
       best_nt = cand[i];
     }
   }
+  b->ms_split = -1.0;
+  if (b->split.size() > 1) {
+    std::vector<BatchClass> sp = b->split;
+    bool ok = true;
+    for (BatchClass& c : sp) {
+      float cbest = 3.0e38f;
+      int cnt = 0;
+      for (int nt : cand) {
+        BatchClass t = c;
+        if (class_config(t, nt) != CPALS_OK) continue;
+        t.st = b->st;  // alone, on the batch's stream
+        if (use_schedule(b, {t}, b->order_split) != CPALS_OK) return CPALS_E_CUDA;
+        float ms = 0.f;
+        int rc = timed(&ms);
+        if (rc != CPALS_OK) return rc;
+        if (ms < cbest) {
+          cbest = ms;
+          cnt = nt;
+        }
+      }
+      if (!cnt || class_config(c, cnt) != CPALS_OK) {
+        ok = false;
+        break;
+      }
+      c.ms_alone = cbest;
+    }
+    if (ok) {
+      if (use_schedule(b, sp, b->order_split) != CPALS_OK) return CPALS_E_CUDA;
+      float ms = 0.f;
+      int rc = timed(&ms);
+      if (rc != CPALS_OK) return rc;
+      b->ms_split = ms;
+      if (ms < best) {
+        best = ms;
+        best_nt = 0;  // the split schedule stays in place
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (!best_nt) return CPALS_E_UNSUPPORTED;
-  int rc = set_config(b, best_nt);
+  int rc = CPALS_OK;
+  if (best_nt) {
+    rc = set_config(b, best_nt);
+  } else if (best > 2.9e38f) {
+    return CPALS_E_UNSUPPORTED;
+  }
   if (rc == CPALS_OK) rc = cpals_batch_set_factors(b, host_factors);
-  if (threads_out) *threads_out = best_nt;
+  if (threads_out) {
+    int nt = 0;
+    for (const BatchClass& c : b->cls) nt = std::max(nt, c.nt);
+    *threads_out = nt;
+  }
   return rc;
+}
+
+int cpals_batch_schedule(cpals_batch* b, int* nclass, int64_t* info, double* ms_split) {
+  if (!b || !nclass) return CPALS_E_ARG;
+  *nclass = (int)b->cls.size();
+  if (info)
+    for (size_t i = 0; i < b->cls.size(); ++i) {
+      const BatchClass& c = b->cls[i];
+      int64_t* r = info + 6 * i;
+      r[0] = c.end - c.begin;
+      r[1] = c.Imax;
+      r[2] = c.Rmax;
+      r[3] = c.nt;
+      r[4] = c.ctas_per_sm;
+      r[5] = (int64_t)(1000.0 * c.ms_alone);  // microseconds, 0 when not timed alone
+    }
+  if (ms_split) *ms_split = b->ms_split;
+  return CPALS_OK;
 }
 
 }  // extern "C"

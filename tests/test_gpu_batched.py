@@ -93,6 +93,28 @@ def test_batched_autotune_and_thread_counts(built, oracle):
     assert np.max(np.abs(res[256] - res[512])) < 1e-12
 
 
+def test_batched_split_schedule_matches_one_class(built, oracle):
+    # extents 16..96: the tensors' own layouts allow 1 to 4 CTAs per SM, so the autotuner has
+    # a split schedule to try; whichever it keeps, every tensor is solved once, as one class
+    # solves it (only the fit's block sums depend on the warp count)
+    dims, ranks, Ts, Fs, lams = make_batch(oracle, 40, seed=7, dmin=16, dmax=96, rmin=4, rmax=16)
+    norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    with built.BatchEngine(dims, ranks, norms) as be:
+        be.set_tensors(Ts)
+        be.autotune(Fs, lams, sweeps=2)
+        classes, split_ms = be.schedule()
+        assert sum(c["tensors"] for c in classes) == len(dims)
+        assert split_ms > 0  # more than one size class existed, so the split was timed
+        be.set_factors(Fs, lams)
+        sw_a, fits_a, _, _ = be.optimize(tol=0.0, max_iter=4)
+        be.set_threads(256)
+        assert len(be.schedule()[0]) == 1
+        be.set_factors(Fs, lams)
+        sw_1, fits_1, _, _ = be.optimize(tol=0.0, max_iter=4)
+    assert np.array_equal(sw_a, sw_1)
+    assert np.max(np.abs(fits_a - fits_1)) < 1e-12
+
+
 def test_batched_rank_deficient_stays_finite(built, oracle):
     # a tensor whose initial factors repeat a column: V is singular, the sweep stops early
     d, R = (9, 8, 7), 3

@@ -623,66 +623,114 @@ def run_c4(args, pkg, device):
 def run_c5(args, pkg, device):
     """Learned warm start: 256^3 FP32 tensors, rank 32, congruence ~U[0,0.8], SNR ~U[10,40] dB,
     generated on the device.  Sketch = MTTKRP with seeded Gaussian test matrices (32 columns
-    per mode) -> bases Q_n -> 32^3 core (engine MTTKRPs) -> Jennrich proposal -> MLP
-    correction (3072 -> 512 -> 512 -> 1024, BF16, FP32 accumulation), trained on the device on
-    ALS decompositions (ALS run from the generator's factors, 5 sweeps).  Judged on held-out
-    seeds against random init and against the proposal without the network: sweeps and GPU
-    time to reach 99% of the best fit any start attains within 100 sweeps."""
+    per mode) -> bases Q_n -> 32^3 core (engine MTTKRPs) -> Jennrich proposal P.  The batched
+    solver runs ALS on the training tensors' cores from P, many cores per launch: one sweep
+    gives the network's input step D = P1 - P, convergence its target P* - P.  MLP
+    (6144 -> 512 -> 512 -> 1024, BF16, FP32 accumulation, tcgen05 GEMMs) trained on the
+    device.  Judged on held-out seeds: sweeps and time to reach 99% of the best fit any start
+    attains within 100 sweeps, for random init (the reference's start), the proposal, the
+    proposal after one core sweep (the network's input alone), the learned start and the
+    teacher (the core ALS run to convergence)."""
     import torch
 
     ws = pkg.warmstart
     dims, R, S = (256, 256, 256), 32, 32
     omegas = ws.gaussian_test_matrices(dims, S, seed=SEED + 5)
     buf = torch.zeros(int(np.prod(dims)), dtype=torch.float32, device=f"cuda:{device}")
+    chunk = 1000  # cores per batched solve while the training set is made
+    teacher_sweeps, teacher_tol = 300, 1e-8
 
     def prepare(eng, core_eng, seed):
         rng = np.random.default_rng(seed)
         cg, snr = float(rng.uniform(0, 0.8)), float(rng.uniform(10, 40))
-        facs, w = ws.synth_device(dims, R, cg, snr, rng, buf.data_ptr(), device=device)
+        ws.synth_device(dims, R, cg, snr, rng, buf.data_ptr(), device=device)
         eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
         core_eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
         nrm = float(buf.double().norm())
-        eng.timer_start()
+        t0 = time.perf_counter()
         Qs, _ = ws.sketch_bases(ws.sketch(eng, omegas))
-        prop = ws.jennrich(ws.core(core_eng, Qs), R, np.random.default_rng(seed + 7))
-        ms = eng.timer_stop()
-        return facs, w, nrm, Qs, prop, ms
+        G = ws.core(core_eng, Qs)
+        prop = ws.jennrich(G, R, np.random.default_rng(seed + 7))
+        return nrm, Qs, G, prop, 1e3 * (time.perf_counter() - t0)
 
     X, Y = [], []
+    n_train = args.c5_train
     t0 = time.perf_counter()
+    t_core = 0.0
     with pkg.Engine(dims, R, dtype=np.float32, precision="bf16x3", device=device) as eng, \
             pkg.Engine(dims, 256, dtype=np.float32, precision="bf16x3", device=device) as core_eng:
-        for s in range(args.c5_train):
-            facs, w, nrm, Qs, prop, _ = prepare(eng, core_eng, 1_000_000 + s)
-            eng.set_factors(facs, w)  # ALS from the generator's factors: the decomposition it reaches
-            eng.optimize(pkg.api._to_device_check(pkg.NoCheck(5)))
-            F, lam = eng.get_factors()
-            X.append(ws.features(prop))
-            Y.append(ws.targets(Qs, F, prop))
+        be_chunk = None
+        teacher_used = []
+        for c0 in range(0, n_train, chunk):
+            nc = min(chunk, n_train - c0)
+            Gs, props = [], []
+            for s in range(c0, c0 + nc):
+                _, _, G, prop, _ = prepare(eng, core_eng, 1_000_000 + s)
+                Gs.append(G)
+                props.append(prop)
+            if be_chunk is None or be_chunk.count != nc:
+                if be_chunk is not None:
+                    be_chunk.close()
+                be_chunk = pkg.BatchEngine([(S, S, S)] * nc, [R] * nc, [1.0] * nc, device=device)
+            t1 = time.perf_counter()
+            P1, _ = ws.core_als(be_chunk, Gs, props, 1)
+            Ps, sw = ws.core_als(be_chunk, Gs, props, teacher_sweeps, tol=teacher_tol)
+            t_core += time.perf_counter() - t1
+            teacher_used.extend(int(x) for x in sw)
+            X.append((props, [[a - b for a, b in zip(p1, p)] for p1, p in zip(P1, props)]))
+            Y.append(Ps)
+        if be_chunk is not None:
+            be_chunk.close()
         t_data = time.perf_counter() - t0
-        X = np.concatenate(X)
-        Y = np.concatenate(Y)
-        net = ws.WarmStartMLP((3 * S * R, 512, 512, S * R), device=device, seed=SEED)
-        nv = 3 * max(1, args.c5_train // 10)  # the last 10% of the training tensors calibrate the step
+        props = [p for x in X for p in x[0]]
+        steps = [d for x in X for d in x[1]]
+        solved = [c for y in Y for c in y]
+        step_scale = float(np.sqrt(np.mean([np.mean(np.square(d)) for D in steps for d in D])))
+        Xf = ws.features(props, steps, step_scale)
+        Yf = ws.targets(props, solved, step_scale)
+        net = ws.WarmStartMLP((6 * S * R, 512, 512, S * R), device=device, seed=SEED)
+        net.step_scale = step_scale
+        nv = 3 * max(1, n_train // 10)  # the last 10% of the training tensors calibrate the step
         t1 = time.perf_counter()
-        losses = net.fit(X[:-nv], Y[:-nv], epochs=30, batch=256, lr=1e-3, seed=SEED)
-        scale = net.calibrate(X[-nv:], Y[-nv:])
-        val_mse = float(np.mean((net.forward(X[-nv:]) - Y[-nv:]) ** 2))
-        val_mse0 = float(np.mean(Y[-nv:] ** 2))
+        losses = net.fit(Xf[:-nv], Yf[:-nv], epochs=30, batch=256, lr=1e-3, seed=SEED)
+        scale = net.calibrate(Xf[-nv:], Yf[-nv:])
+        pred = net.forward(Xf[-nv:])
+        val_mse = float(np.mean((pred - Yf[-nv:]) ** 2))
+        val_mse0 = float(np.mean(Yf[-nv:] ** 2))
+        # the network's input alone, as a predictor of the target: the step itself, least-squares scaled
+        Dv = Xf[-nv:, S * R:2 * S * R].astype(np.float64)
+        a_ls = float(np.sum(Dv * Yf[-nv:]) / max(np.sum(Dv * Dv), 1e-300))
+        val_mse_step = float(np.mean((a_ls * Dv - Yf[-nv:]) ** 2))
         t_train = time.perf_counter() - t1
-        res = {k: {"sweeps": [], "ms": []} for k in ("random", "proposal", "learned")}
+        train_ms, flops_step = net.train_stats(256)
+        train_ms = net.fit_ms
+        # per-step rate of the tensor-core GEMMs over the device time of the training launches
+        achieved = flops_step * net.fit_steps / (train_ms * 1e-3) / 1e12
+
+        keys = ("random", "proposal", "one_core_sweep", "learned", "core_als")
+        res = {k: {"sweeps": [], "ms": []} for k in keys}
         fallbacks = 0
+        e2e_ms = []
+        be1 = pkg.BatchEngine([(S, S, S)], [R], [1.0], device=device)
         for s in range(args.c5_eval):
-            facs, w, nrm, Qs, prop, ms_prop = prepare(eng, core_eng, 2_000_000 + s)
-            eng.timer_start()
-            Fw = ws.warm_factors(net, Qs, prop)
-            ms_net = eng.timer_stop()
-            Fp = ws.proposal_factors(Qs, prop)
+            nrm, Qs, G, prop, ms_prop = prepare(eng, core_eng, 2_000_000 + s)
+            t1 = time.perf_counter()
+            (p1,), _ = ws.core_als(be1, [G], [prop], 1)
+            ms_p1 = 1e3 * (time.perf_counter() - t1)
+            t1 = time.perf_counter()
+            Cl = ws.learned_coefficients(net, [prop], [[a - b for a, b in zip(p1, prop)]])[0]
+            ms_net = 1e3 * (time.perf_counter() - t1)
+            t1 = time.perf_counter()
+            (pst,), _ = ws.core_als(be1, [G], [prop], teacher_sweeps, tol=teacher_tol)
+            ms_teacher = 1e3 * (time.perf_counter() - t1)
             fb = pkg.random_factors(dims, R, np.random.default_rng(s))[0]
-            fallbacks += int(Fw is None)
-            starts = {"random": (pkg.random_factors(dims, R, np.random.default_rng(3_000_000 + s))[0], 0.0),
-                      "proposal": (Fp if Fp is not None else fb, ms_prop),
-                      "learned": (Fw if Fw is not None else fb, ms_prop + ms_net)}
+            cand = {"proposal": (ws.lift(Qs, prop), ms_prop), "one_core_sweep": (ws.lift(Qs, p1), ms_prop + ms_p1),
+                    "learned": (ws.lift(Qs, Cl), ms_prop + ms_p1 + ms_net),
+                    "core_als": (ws.lift(Qs, pst), ms_prop + ms_teacher)}
+            starts = {"random": (pkg.random_factors(dims, R, np.random.default_rng(3_000_000 + s))[0], 0.0)}
+            for k, (F0, extra) in cand.items():
+                fallbacks += int(F0 is None and k == "learned")
+                starts[k] = (F0 if F0 is not None else fb, extra)
             trajs, ms = {}, {}
             for k, (F0, extra) in starts.items():
                 eng.set_factors(F0, np.ones(R))
@@ -695,26 +743,81 @@ def run_c5(args, pkg, device):
                 res[k]["sweeps"].append(n if n is not None else 101)
                 per = ms[k][0] / len(trajs[k])
                 res[k]["ms"].append(ms[k][1] + per * (n if n is not None else 101))
+            if s < 32:
+                # end to end through the public API for the learned start: the tensor from pinned
+                # host memory, the start, ALS to the target's sweep count, the factors back
+                host = buf.cpu().pin_memory()
+                n_l = res["learned"]["sweeps"][-1]
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                buf.copy_(host, non_blocking=True)
+                eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
+                core_eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
+                Qs2, _ = ws.sketch_bases(ws.sketch(eng, omegas))
+                G2 = ws.core(core_eng, Qs2)
+                prop2 = ws.jennrich(G2, R, np.random.default_rng(2_000_000 + s + 7))
+                (q1,), _ = ws.core_als(be1, [G2], [prop2], 1)
+                F2 = ws.lift(Qs2, ws.learned_coefficients(net, [prop2], [[a - b for a, b in zip(q1, prop2)]])[0])
+                eng.set_factors(F2 if F2 is not None else fb, np.ones(R))
+                eng.optimize(pkg.api._to_device_check(pkg.NoCheck(min(n_l, 100))))
+                eng.get_factors()
+                e2e_ms.append(1e3 * (time.perf_counter() - t1))
+        be1.close()
     out = {}
     for k, v in res.items():
         sw = np.asarray(v["sweeps"])
         out[k] = {"sweeps_p50": float(np.median(sw)), "sweeps_mean": float(sw.mean()),
                   "sweeps_p90": float(np.percentile(sw, 90)), "reached_within_100": int(np.sum(sw <= 100)),
                   "ms_to_target_p50": float(np.median(v["ms"])), "ms_to_target_mean": float(np.mean(v["ms"]))}
+    # CPU baseline: the reference's start (random init) with the compiled CPU ALS, priced by a
+    # bounded sample of 2 sweeps on one 256^3 rank-32 tensor of the workload
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cpals_oracle as oracle
+
+    Tcpu = np.reshape(buf.cpu().numpy(), dims, order="F")
+    Fc, lc = oracle.random_factors(dims, R, np.random.default_rng(5))
+    cpu = None
+    try:
+        oracle.cpu_als_sweeps(Tcpu, Fc, lc, 1)
+        t1 = time.perf_counter()
+        if oracle.cpu_als_sweeps(Tcpu, Fc, lc, 2) is not None:
+            cpu_sweep_ms = 1e3 * (time.perf_counter() - t1) / 2
+            cpu = {"value": cpu_sweep_ms * out["random"]["sweeps_p50"], "unit": "ms to target (p50)",
+                   "cores": os.cpu_count() or 1, "kind": "port", "ms_per_sweep": cpu_sweep_ms,
+                   "sample": "2 sweeps of the GEMM-form normal-equation ALS (compiled C++/OpenMP, all host threads) "
+                             "on one 256^3 rank-32 tensor, times the median sweeps random init needs"}
+    except Exception as exc:
+        cpu = {"error": str(exc)}
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
     line = {
-        "metric": "sweeps_to_99pct_of_best_fit", "value": out["learned"]["sweeps_p50"], "unit": "sweeps",
+        "metric": "sweeps_to_99pct_of_best_fit", "value": out["learned"]["sweeps_mean"], "unit": "sweeps (mean)",
         "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "mlp bf16/f32-accumulate; als bf16x3 mttkrp, f64 solve", "data": "synthetic",
-        "config": {"workload": "warm_start_256cube_rank32_sketch32", "train": args.c5_train, "eval": args.c5_eval,
-                   "mlp": [3 * S * R, 512, 512, S * R]},
+        "dtype": "mlp bf16/f32-accumulate (tcgen05); core als f32 mttkrp, f64 solve; als bf16x3 mttkrp, f64 solve",
+        "data": "synthetic",
+        "config": {"workload": "warm_start_256cube_rank32_sketch32", "train": n_train, "eval": args.c5_eval,
+                   "mlp": [6 * S * R, 512, 512, S * R], "teacher": f"core ALS FitCheck({teacher_tol}, {teacher_sweeps})"},
         "c5": out, "fallbacks": fallbacks,
         "gain_vs_random_p50": out["random"]["sweeps_p50"] / max(out["learned"]["sweeps_p50"], 1e-9),
         "gain_vs_random_mean": out["random"]["sweeps_mean"] / max(out["learned"]["sweeps_mean"], 1e-9),
         "gain_vs_proposal_mean": out["proposal"]["sweeps_mean"] / max(out["learned"]["sweeps_mean"], 1e-9),
-        "train": {"data_s": t_data, "train_s": t_train, "loss_first": float(np.mean(losses[:10])),
-                  "loss_last": float(np.mean(losses[-10:])), "samples": int(X.shape[0]) - nv,
-                  "validation_mse": val_mse, "validation_mse_of_zero_correction": val_mse0,
-                  "calibrated_step": scale},
+        "gain_vs_one_core_sweep_mean": out["one_core_sweep"]["sweeps_mean"] / max(out["learned"]["sweeps_mean"], 1e-9),
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                     "frac": achieved / peak_tf, "traffic": None,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "kernel": "k_gemm_tc (the network's eight GEMMs per training step, batch 256; device time "
+                               "of all training launches, so the small epilogue and Adam kernels count against it)"},
+        "e2e": {"value": float(np.median(e2e_ms)) if e2e_ms else None, "unit": "ms per tensor (p50, learned start)",
+                "h2d_bytes_per_step": 4 * int(np.prod(dims)), "d2h_bytes_per_step": 8 * (sum(dims) + 1) * R},
+        "cpu_baseline": cpu,
+        "train": {"data_s": t_data, "core_als_s": t_core, "train_s": t_train, "train_device_ms": train_ms,
+                  "steps": net.fit_steps, "loss_first": float(np.mean(losses[:10])),
+                  "loss_last": float(np.mean(losses[-10:])), "samples": int(Xf.shape[0]) - nv,
+                  "step_scale": step_scale, "validation_mse": val_mse,
+                  "validation_mse_of_zero_correction": val_mse0,
+                  "validation_mse_of_scaled_step": val_mse_step, "scaled_step_factor": a_ls,
+                  "calibrated_step": scale,
+                  "teacher_sweeps_p50": float(np.median(teacher_used)) if teacher_used else None},
     }
     print(json.dumps(line), flush=True)
 

@@ -325,6 +325,9 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
                        const double* ref_norms);
 int cpals_batch_destroy(cpals_batch* b);
 int cpals_batch_set_tensors(cpals_batch* b, const float* host_concat);
+/* New reference norms (count entries, each finite and > 0), e.g. with a new set of tensors of
+ * the same shapes; the FitCheck of the next set_factors / optimize uses them. */
+int cpals_batch_set_norms(cpals_batch* b, const double* ref_norms);
 /* Initial factors (resets every tensor's FitCheck state). */
 int cpals_batch_set_factors(cpals_batch* b, const double* host_concat);
 int cpals_batch_get_factors(cpals_batch* b, double* host_concat);
@@ -369,6 +372,9 @@ int cpals_mlp_gradients(cpals_mlp* m, const float* host_x, const float* host_t, 
                         double* loss_out);
 int cpals_mlp_set_dataset(cpals_mlp* m, const float* host_x, const float* host_t, int64_t n);
 int cpals_mlp_train(cpals_mlp* m, const int* host_idx, int steps, int batch, float lr, double* losses);
+/* Device time of the last cpals_mlp_train call (ms, CUDA events on the network's stream around
+ * its launches) and the tensor-core flops of one training step of B rows. */
+int cpals_mlp_train_stats(cpals_mlp* m, int B, double* ms, double* flops_per_step);
 
 #ifdef __cplusplus
 }

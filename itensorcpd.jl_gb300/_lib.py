@@ -102,6 +102,7 @@ SIGNATURES = {
     "cpals_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int64, _I64P, _I64P, _DP]),
     "cpals_batch_destroy": (C.c_int, [_P]),
     "cpals_batch_set_tensors": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "cpals_batch_set_norms": (C.c_int, [_P, _DP]),
     "cpals_batch_set_factors": (C.c_int, [_P, _DP]),
     "cpals_batch_get_factors": (C.c_int, [_P, _DP]),
     "cpals_batch_set_threads": (C.c_int, [_P, C.c_int]),
@@ -119,6 +120,7 @@ SIGNATURES = {
     "cpals_mlp_gradients": (C.c_int, [_P, _FP, _FP, C.c_int, _FP, _DP]),
     "cpals_mlp_set_dataset": (C.c_int, [_P, _FP, _FP, C.c_int64]),
     "cpals_mlp_train": (C.c_int, [_P, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_float, _DP]),
+    "cpals_mlp_train_stats": (C.c_int, [_P, C.c_int, _DP, _DP]),
 }
 
 _lib = None

@@ -67,6 +67,13 @@ class BatchEngine:
                 "cpals_batch_set_tensors")
         self._tensors_keep = buf
 
+    def set_norms(self, ref_norms):
+        """New reference norms, one per tensor (with new tensors of the same shapes)."""
+        nrm = np.ascontiguousarray(np.asarray(ref_norms, dtype=np.float64))
+        if nrm.size != self.count:
+            raise ValueError("one norm per tensor")
+        L.check(self.lib.cpals_batch_set_norms(self.h, L.dptr(nrm)), "cpals_batch_set_norms")
+
     def pack_factors(self, factors, lams):
         buf = np.empty(self._ftotal, dtype=np.float64)
         for t, (F, lam) in enumerate(zip(factors, lams)):

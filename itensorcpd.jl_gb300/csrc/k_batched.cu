@@ -792,6 +792,18 @@ int cpals_batch_set_tensors(cpals_batch* b, const float* host_concat) {
   return CPALS_OK;
 }
 
+int cpals_batch_set_norms(cpals_batch* b, const double* ref_norms) {
+  if (!b || !ref_norms) return CPALS_E_ARG;
+  for (int64_t t = 0; t < b->count; ++t)
+    if (!(ref_norms[t] > 0.0) || !std::isfinite(ref_norms[t])) return CPALS_E_ARG;
+  DeviceGuard guard(b->device);
+  for (int64_t t = 0; t < b->count; ++t) b->items[t].ref_norm = ref_norms[t];
+  CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(BatchItem) * b->count, cudaMemcpyHostToDevice,
+                                 b->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));  // the host array is the copy's source
+  return CPALS_OK;
+}
+
 int cpals_batch_set_factors(cpals_batch* b, const double* host_concat) {
   if (!b || !host_concat) return CPALS_E_ARG;
   DeviceGuard guard(b->device);

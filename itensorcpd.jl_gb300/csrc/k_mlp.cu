@@ -4,10 +4,12 @@
 //   h1 = relu(x W1^T + b1),  h2 = relu(h1 W2^T + b2),  y = h2 W3^T + b3
 //   loss = mean((y - t)^2)
 //
-// FP32 master weights and Adam moments; BF16 copies of the weights feed the GEMMs, and the
-// activations are stored in BF16 (the GEMM inputs of the next layer and of the backward
-// pass).  One GEMM kernel covers every product of the forward and backward passes through
-// element strides: C[M][N] (+)= sum_k A(m, k) B(k, n), A and B in BF16, FP32 accumulation.
+// FP32 master weights and Adam moments.  Every product of the forward and backward passes
+// runs on the tensor cores (k_gemm_tc.cu: tcgen05.mma.kind::f16, BF16 operands, FP32
+// accumulation in TMEM), over split-K slices that the epilogue kernel sums in a fixed order
+// while it adds the bias, applies the activation or the ReLU mask and writes the BF16
+// panels the next GEMMs read: activations and gradients both as they are and transposed
+// (the weight gradients reduce over the batch), weights as W and W^T.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -15,76 +17,14 @@
 #include <vector>
 
 #include "cpals_internal.cuh"
+#include "gemm_tc.cuh"
 
 namespace cpals {
 namespace {
 
-constexpr int GM = 64, GN = 64, GK = 32;  // block tile
-constexpr int GTHREADS = 256;             // 16 x 16 threads, 4 x 4 outputs each
-
-// C[m][n] = alpha * sum_k A[m*sam + k*sak] * B[k*sbk + n*sbn] (+ beta * C), row-major C (ldc)
-__global__ void __launch_bounds__(GTHREADS) k_gemm_bf16(const __nv_bfloat16* __restrict__ A, int64_t sam,
-                                                        int64_t sak, const __nv_bfloat16* __restrict__ B, int64_t sbk,
-                                                        int64_t sbn, float* __restrict__ C, int64_t ldc, int M, int N,
-                                                        int K, float beta) {
-  __shared__ float As[GK][GM + 4];
-  __shared__ float Bs[GK][GN + 4];
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int m0 = blockIdx.y * GM, n0 = blockIdx.x * GN;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += GK) {
-    for (int e = threadIdx.x; e < GK * GM; e += GTHREADS) {
-      const int kk = e / GM, mm = e % GM;
-      const int m = m0 + mm, k = k0 + kk;
-      As[kk][mm] = (m < M && k < K) ? __bfloat162float(A[(int64_t)m * sam + (int64_t)k * sak]) : 0.f;
-    }
-    for (int e = threadIdx.x; e < GK * GN; e += GTHREADS) {
-      const int kk = e / GN, nn = e % GN;
-      const int n = n0 + nn, k = k0 + kk;
-      Bs[kk][nn] = (n < N && k < K) ? __bfloat162float(B[(int64_t)k * sbk + (int64_t)n * sbn]) : 0.f;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int kk = 0; kk < GK; ++kk) {
-      float a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
-      if (m < M && n < N) {
-        float* c = &C[(int64_t)m * ldc + n];
-        *c = (beta != 0.f ? beta * *c : 0.f) + acc[i][j];
-      }
-    }
-}
-
-// Y (FP32 [B][N]) += bias; optional ReLU; BF16 copy for the next GEMM.
-__global__ void k_bias_act(float* __restrict__ Y, const float* __restrict__ bias, int B, int N, int relu,
-                           __nv_bfloat16* __restrict__ Yb) {
-  const int64_t n = (int64_t)B * N;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    float v = Y[e] + bias[e % N];
-    if (relu) v = fmaxf(v, 0.f);
-    Y[e] = v;
-    if (Yb) Yb[e] = __float2bfloat16_rn(v);
-  }
-}
-
 // dY = 2 (Y - T) / (B N) (mean squared error), loss partial sums per block
 __global__ void k_mse_grad(const float* __restrict__ Y, const float* __restrict__ T, int64_t n, float scale,
-                           __nv_bfloat16* __restrict__ dYb, float* __restrict__ dY, double* __restrict__ loss) {
+                           float* __restrict__ dY, double* __restrict__ loss) {
   __shared__ double red[32];
   double s = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
@@ -92,7 +32,6 @@ __global__ void k_mse_grad(const float* __restrict__ Y, const float* __restrict_
     s += (double)d * d;
     const float g = 2.f * d * scale;
     dY[e] = g;
-    dYb[e] = __float2bfloat16_rn(g);
   }
   for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
@@ -101,16 +40,6 @@ __global__ void k_mse_grad(const float* __restrict__ Y, const float* __restrict_
     double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
     for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
     if (threadIdx.x == 0) loss[blockIdx.x] = t;
-  }
-}
-
-// dH (FP32 [B][N], the product dY W) *= (H > 0); BF16 copy
-__global__ void k_relu_back(float* __restrict__ dH, const __nv_bfloat16* __restrict__ H, int64_t n,
-                            __nv_bfloat16* __restrict__ dHb) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const float g = (__bfloat162float(H[e]) > 0.f) ? dH[e] : 0.f;
-    dH[e] = g;
-    dHb[e] = __float2bfloat16_rn(g);
   }
 }
 
@@ -123,10 +52,9 @@ __global__ void k_bias_grad(const float* __restrict__ dY, int B, int N, float* _
   }
 }
 
-// Adam (Kingma and Ba 2015) on the FP32 master parameters; BF16 copy of the weights
+// Adam (Kingma and Ba 2015) on the FP32 master parameters
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
-                       float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps, float c1, float c2,
-                       __nv_bfloat16* __restrict__ pb) {
+                       float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const float gg = g[e];
     const float a = b1 * m1[e] + (1.f - b1) * gg;
@@ -135,24 +63,16 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     m2[e] = b;
     const float v = p[e] - lr * (a / c1) / (sqrtf(b / c2) + eps);
     p[e] = v;
-    if (pb) pb[e] = __float2bfloat16_rn(v);
   }
 }
 
-__global__ void k_to_bf16(const float* __restrict__ x, int64_t n, __nv_bfloat16* __restrict__ y) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    y[e] = __float2bfloat16_rn(x[e]);
-}
-
-// gather rows idx[b] of a device dataset (FP32 [N][W]) into X (FP32 and BF16 [B][W])
+// gather rows idx[b] of a device dataset (FP32 [N][W]) into X (FP32 [B][W])
 __global__ void k_gather_rows(const float* __restrict__ D, int W, const int* __restrict__ idx, int B,
-                              float* __restrict__ X, __nv_bfloat16* __restrict__ Xb) {
+                              float* __restrict__ X) {
   const int64_t n = (int64_t)B * W;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(e / W), w = (int)(e % W);
-    const float v = D[(int64_t)idx[b] * W + w];
-    if (X) X[e] = v;
-    if (Xb) Xb[e] = __float2bfloat16_rn(v);
+    X[e] = D[(int64_t)idx[b] * W + w];
   }
 }
 
@@ -165,6 +85,7 @@ using namespace cpals;
 
 struct cpals_mlp {
   int device = 0;
+  int sms = 1;
   int w[4] = {};  // in, h1, h2, out
   int64_t np = 0;
   int64_t off[6] = {};  // W1 b1 W2 b2 W3 b3 offsets into the parameter vector
@@ -172,113 +93,155 @@ struct cpals_mlp {
   float* g = nullptr;   // gradients
   float* m1 = nullptr;
   float* m2 = nullptr;
-  __nv_bfloat16* pb = nullptr;  // BF16 copy (weights used by the GEMMs)
+  // weight panels: W_l as [out][in] (forward) and W_l^T (backward; layers 2 and 3)
+  __nv_bfloat16 *W1p = nullptr, *W2p = nullptr, *W2t = nullptr, *W3p = nullptr, *W3t = nullptr;
   int bcap = 0;
   float *x = nullptr, *t = nullptr, *h1 = nullptr, *h2 = nullptr, *y = nullptr, *dy = nullptr, *dh2 = nullptr,
         *dh1 = nullptr;
-  __nv_bfloat16 *xb = nullptr, *h1b = nullptr, *h2b = nullptr, *dyb = nullptr, *dh2b = nullptr, *dh1b = nullptr;
-  double* loss = nullptr;
+  // activation / gradient panels: p = as stored ([batch][features]), t = transposed
+  __nv_bfloat16 *Xp = nullptr, *Xt = nullptr, *H1p = nullptr, *H1t = nullptr, *H2p = nullptr, *H2t = nullptr,
+                *DYp = nullptr, *DYt = nullptr, *DH2p = nullptr, *DH2t = nullptr, *DH1t = nullptr;
+  float* part = nullptr;  // split-K partial sums
+  double* loss = nullptr;  // per-block loss partials
+  int* err = nullptr;      // the GEMM's error word (2 ints)
   int* idx = nullptr;
+  int64_t idx_cap = 0;
   float* dx = nullptr;  // device dataset inputs [N][in]
   float* dt = nullptr;  // device dataset targets [N][out]
   int64_t dn = 0;
   int64_t step = 0;
+  double train_ms = 0.0;  // device time of the last cpals_mlp_train call (its launches only)
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t st = nullptr;
 };
 
 namespace {
 
-void gemm(cpals_mlp* m, const __nv_bfloat16* A, int64_t sam, int64_t sak, const __nv_bfloat16* B, int64_t sbk,
-          int64_t sbn, float* C, int64_t ldc, int M, int N, int K) {
-  dim3 grid((N + GN - 1) / GN, (M + GM - 1) / GM);
-  k_gemm_bf16<<<grid, GTHREADS, 0, m->st>>>(A, sam, sak, B, sbk, sbn, C, ldc, M, N, K, 0.f);
+// C = A B^T on the tensor cores (A: M x K panel, B: N x K panel), then the epilogue
+cudaError_t gemm(cpals_mlp* m, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const float* bias,
+                 int mode, const float* mask, float* out32, __nv_bfloat16* prm, __nv_bfloat16* ptr) {
+  const int sp = gemm_tc_splits(M, N, K, m->sms);
+  cudaError_t e = gemm_tc_launch(A, B, M, N, K, sp, m->part, m->err, m->st);
+  if (e != cudaSuccess) return e;
+  return gemm_tc_epilogue(m->part, sp, M, N, bias, mode, mask, out32, prm, ptr, m->st);
+}
+
+// pack a row-major FP32 matrix [M][N] into its panels
+cudaError_t pack(cpals_mlp* m, const float* src, int M, int N, __nv_bfloat16* prm, __nv_bfloat16* ptr) {
+  return gemm_tc_epilogue(src, 1, M, N, nullptr, 0, nullptr, nullptr, prm, ptr, m->st);
+}
+
+// split-K partial floats the 8 products of a batch of B need
+int64_t part_floats(const cpals_mlp* m, int B) {
+  const int in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
+  const int shapes[8][3] = {{B, a, in}, {B, b, a}, {B, o, b}, {o, b, B}, {B, b, o}, {b, a, B}, {B, a, b}, {a, in, B}};
+  int64_t need = 0;
+  for (const auto& sh : shapes)
+    need = std::max(need, (int64_t)gemm_tc_splits(sh[0], sh[1], sh[2], m->sms) * sh[0] * sh[1]);
+  return need;
+}
+
+template <typename T>
+bool alloc0(T** q, int64_t elems) {
+  *q = nullptr;
+  if (cudaMalloc(q, sizeof(T) * (size_t)std::max<int64_t>(elems, 1)) != cudaSuccess) return false;
+  return cudaMemset(*q, 0, sizeof(T) * (size_t)std::max<int64_t>(elems, 1)) == cudaSuccess;
+}
+
+void free_batch(cpals_mlp* m) {
+  for (void* q : {(void*)m->x, (void*)m->t, (void*)m->h1, (void*)m->h2, (void*)m->y, (void*)m->dy, (void*)m->dh2,
+                  (void*)m->dh1, (void*)m->Xp, (void*)m->Xt, (void*)m->H1p, (void*)m->H1t, (void*)m->H2p,
+                  (void*)m->H2t, (void*)m->DYp, (void*)m->DYt, (void*)m->DH2p, (void*)m->DH2t, (void*)m->DH1t,
+                  (void*)m->part, (void*)m->loss})
+    cudaFree(q);
+  m->x = m->t = m->h1 = m->h2 = m->y = m->dy = m->dh2 = m->dh1 = m->part = nullptr;
+  m->Xp = m->Xt = m->H1p = m->H1t = m->H2p = m->H2t = m->DYp = m->DYt = m->DH2p = m->DH2t = m->DH1t = nullptr;
+  m->loss = nullptr;
+  m->bcap = 0;
 }
 
 int ensure_batch(cpals_mlp* m, int B) {
   if (B <= m->bcap) return CPALS_OK;
-  cudaFree(m->x);
-  cudaFree(m->t);
-  cudaFree(m->h1);
-  cudaFree(m->h2);
-  cudaFree(m->y);
-  cudaFree(m->dy);
-  cudaFree(m->dh2);
-  cudaFree(m->dh1);
-  cudaFree(m->xb);
-  cudaFree(m->h1b);
-  cudaFree(m->h2b);
-  cudaFree(m->dyb);
-  cudaFree(m->dh2b);
-  cudaFree(m->dh1b);
-  cudaFree(m->loss);
-  cudaFree(m->idx);
+  free_batch(m);
   const int64_t in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
-  bool ok = cudaMalloc(&m->x, 4 * B * in) == cudaSuccess && cudaMalloc(&m->t, 4 * B * o) == cudaSuccess &&
-            cudaMalloc(&m->h1, 4 * B * a) == cudaSuccess && cudaMalloc(&m->h2, 4 * B * b) == cudaSuccess &&
-            cudaMalloc(&m->y, 4 * B * o) == cudaSuccess && cudaMalloc(&m->dy, 4 * B * o) == cudaSuccess &&
-            cudaMalloc(&m->dh2, 4 * B * b) == cudaSuccess && cudaMalloc(&m->dh1, 4 * B * a) == cudaSuccess &&
-            cudaMalloc(&m->xb, 2 * B * in) == cudaSuccess && cudaMalloc(&m->h1b, 2 * B * a) == cudaSuccess &&
-            cudaMalloc(&m->h2b, 2 * B * b) == cudaSuccess && cudaMalloc(&m->dyb, 2 * B * o) == cudaSuccess &&
-            cudaMalloc(&m->dh2b, 2 * B * b) == cudaSuccess && cudaMalloc(&m->dh1b, 2 * B * a) == cudaSuccess &&
-            cudaMalloc(&m->loss, sizeof(double) * 4096) == cudaSuccess &&
-            cudaMalloc(&m->idx, sizeof(int) * B) == cudaSuccess;
-  if (!ok) return CPALS_E_CUDA;
+  bool ok = alloc0(&m->x, B * in) && alloc0(&m->t, B * o) && alloc0(&m->h1, B * a) && alloc0(&m->h2, B * b) &&
+            alloc0(&m->y, B * o) && alloc0(&m->dy, B * o) && alloc0(&m->dh2, B * b) && alloc0(&m->dh1, B * a) &&
+            alloc0(&m->Xp, panel_elems(B, in)) && alloc0(&m->Xt, panel_elems(in, B)) &&
+            alloc0(&m->H1p, panel_elems(B, a)) && alloc0(&m->H1t, panel_elems(a, B)) &&
+            alloc0(&m->H2p, panel_elems(B, b)) && alloc0(&m->H2t, panel_elems(b, B)) &&
+            alloc0(&m->DYp, panel_elems(B, o)) && alloc0(&m->DYt, panel_elems(o, B)) &&
+            alloc0(&m->DH2p, panel_elems(B, b)) && alloc0(&m->DH2t, panel_elems(b, B)) &&
+            alloc0(&m->DH1t, panel_elems(a, B)) && alloc0(&m->part, part_floats(m, B)) &&
+            alloc0(&m->loss, 4096);
+  if (!ok) {
+    free_batch(m);
+    return CPALS_E_CUDA;
+  }
   m->bcap = B;
   return CPALS_OK;
 }
 
-// forward pass on m->xb (BF16 [B][in]); y, h1, h2 (FP32) and BF16 copies
-void forward(cpals_mlp* m, int B) {
+// the BF16 weight panels from the FP32 master parameters
+cudaError_t refresh_weights(cpals_mlp* m) {
   const int in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
-  const __nv_bfloat16* W1 = m->pb + m->off[0];
-  const __nv_bfloat16* W2 = m->pb + m->off[2];
-  const __nv_bfloat16* W3 = m->pb + m->off[4];
-  // h1[b][j] = sum_k x[b][k] W1[j][k]
-  gemm(m, m->xb, in, 1, W1, 1, in, m->h1, a, B, a, in);
-  k_bias_act<<<grid1((int64_t)B * a), 256, 0, m->st>>>(m->h1, m->p + m->off[1], B, a, 1, m->h1b);
-  gemm(m, m->h1b, a, 1, W2, 1, a, m->h2, b, B, b, a);
-  k_bias_act<<<grid1((int64_t)B * b), 256, 0, m->st>>>(m->h2, m->p + m->off[3], B, b, 1, m->h2b);
-  gemm(m, m->h2b, b, 1, W3, 1, b, m->y, o, B, o, b);
-  k_bias_act<<<grid1((int64_t)B * o), 256, 0, m->st>>>(m->y, m->p + m->off[5], B, o, 0, nullptr);
+  cudaError_t e = pack(m, m->p + m->off[0], a, in, m->W1p, nullptr);
+  if (e == cudaSuccess) e = pack(m, m->p + m->off[2], b, a, m->W2p, m->W2t);
+  if (e == cudaSuccess) e = pack(m, m->p + m->off[4], o, b, m->W3p, m->W3t);
+  return e;
 }
 
-// backward pass (targets in m->t), gradients into m->g; returns the block loss partials count
-int backward(cpals_mlp* m, int B) {
+// forward pass on the input panels (from m->x); y, h1, h2 (FP32) and their panels
+cudaError_t forward(cpals_mlp* m, int B) {
   const int in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
-  const __nv_bfloat16* W2 = m->pb + m->off[2];
-  const __nv_bfloat16* W3 = m->pb + m->off[4];
+  cudaError_t e = pack(m, m->x, B, in, m->Xp, m->Xt);
+  if (e == cudaSuccess) e = gemm(m, m->Xp, m->W1p, B, a, in, m->p + m->off[1], 1, nullptr, m->h1, m->H1p, m->H1t);
+  if (e == cudaSuccess) e = gemm(m, m->H1p, m->W2p, B, b, a, m->p + m->off[3], 1, nullptr, m->h2, m->H2p, m->H2t);
+  if (e == cudaSuccess) e = gemm(m, m->H2p, m->W3p, B, o, b, m->p + m->off[5], 0, nullptr, m->y, nullptr, nullptr);
+  return e;
+}
+
+// backward pass (targets in m->t), gradients into m->g, loss partials of this step into
+// m->loss[slot * lb ..]; returns the number of loss partials (lb)
+int backward(cpals_mlp* m, int B, int slot, cudaError_t* err) {
+  const int in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
   const int64_t ny = (int64_t)B * o;
-  const int lb = grid1(ny);
-  k_mse_grad<<<lb, 256, 0, m->st>>>(m->y, m->t, ny, 1.f / (float)ny, m->dyb, m->dy, m->loss);
-  // dW3[i][j] = sum_b dy[b][i] h2[b][j];  db3 = sum_b dy
-  gemm(m, m->dyb, 1, o, m->h2b, b, 1, m->g + m->off[4], b, o, b, B);
+  const int lb = std::min(grid1(ny), 64);
+  k_mse_grad<<<lb, 256, 0, m->st>>>(m->y, m->t, ny, 1.f / (float)ny, m->dy, m->loss + (int64_t)slot * lb);
+  cudaError_t e = pack(m, m->dy, B, o, m->DYp, m->DYt);
+  // dW3 = dy^T h2, db3 = sum_b dy
+  if (e == cudaSuccess) e = gemm(m, m->DYt, m->H2t, o, b, B, nullptr, 0, nullptr, m->g + m->off[4], nullptr, nullptr);
   k_bias_grad<<<(o + 255) / 256, 256, 0, m->st>>>(m->dy, B, o, m->g + m->off[5]);
-  // dh2[b][j] = sum_i dy[b][i] W3[i][j], masked
-  gemm(m, m->dyb, o, 1, W3, b, 1, m->dh2, b, B, b, o);
-  k_relu_back<<<grid1((int64_t)B * b), 256, 0, m->st>>>(m->dh2, m->h2b, (int64_t)B * b, m->dh2b);
-  gemm(m, m->dh2b, 1, b, m->h1b, a, 1, m->g + m->off[2], a, b, a, B);
+  // dh2 = (dy W3) masked by h2 > 0
+  if (e == cudaSuccess) e = gemm(m, m->DYp, m->W3t, B, b, o, nullptr, 2, m->h2, m->dh2, m->DH2p, m->DH2t);
+  if (e == cudaSuccess) e = gemm(m, m->DH2t, m->H1t, b, a, B, nullptr, 0, nullptr, m->g + m->off[2], nullptr, nullptr);
   k_bias_grad<<<(b + 255) / 256, 256, 0, m->st>>>(m->dh2, B, b, m->g + m->off[3]);
-  gemm(m, m->dh2b, b, 1, W2, a, 1, m->dh1, a, B, a, b);
-  k_relu_back<<<grid1((int64_t)B * a), 256, 0, m->st>>>(m->dh1, m->h1b, (int64_t)B * a, m->dh1b);
-  gemm(m, m->dh1b, 1, a, m->xb, in, 1, m->g + m->off[0], in, a, in, B);
+  // dh1 = (dh2 W2) masked by h1 > 0
+  if (e == cudaSuccess) e = gemm(m, m->DH2p, m->W2t, B, a, b, nullptr, 2, m->h1, m->dh1, nullptr, m->DH1t);
+  if (e == cudaSuccess) e = gemm(m, m->DH1t, m->Xt, a, in, B, nullptr, 0, nullptr, m->g + m->off[0], nullptr, nullptr);
   k_bias_grad<<<(a + 255) / 256, 256, 0, m->st>>>(m->dh1, B, a, m->g + m->off[1]);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  *err = e;
   return lb;
 }
 
-double read_loss(cpals_mlp* m, int nblocks) {
-  std::vector<double> h(nblocks);
-  cudaMemcpyAsync(h.data(), m->loss, sizeof(double) * nblocks, cudaMemcpyDeviceToHost, m->st);
-  cudaStreamSynchronize(m->st);
-  double s = 0.0;
-  for (double v : h) s += v;
-  return s;
-}
-
-void adam(cpals_mlp* m, float lr) {
+cudaError_t adam(cpals_mlp* m, float lr) {
   m->step += 1;
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.f - powf(b1, (float)m->step), c2 = 1.f - powf(b2, (float)m->step);
-  k_adam<<<grid1(m->np), 256, 0, m->st>>>(m->p, m->g, m->m1, m->m2, m->np, lr, b1, b2, 1e-8f, c1, c2, m->pb);
+  k_adam<<<grid1(m->np), 256, 0, m->st>>>(m->p, m->g, m->m1, m->m2, m->np, lr, b1, b2, 1e-8f, c1, c2);
+  return refresh_weights(m);
+}
+
+// synchronise; CPALS_E_DEVICE (and the word cleared) if a GEMM's bounded wait expired
+int finish(cpals_mlp* m) {
+  CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));
+  int h = 0;
+  CPALS_CUDA_TRY(cudaMemcpy(&h, m->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    CPALS_CUDA_TRY(cudaMemset(m->err, 0, 2 * sizeof(int)));
+    return CPALS_E_DEVICE;
+  }
+  return CPALS_OK;
 }
 
 }  // namespace
@@ -295,6 +258,8 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
   DeviceGuard guard(device);
   cpals_mlp* m = new cpals_mlp();
   m->device = device;
+  cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
+  m->sms = std::max(m->sms, 1);
   for (int i = 0; i < 4; ++i) m->w[i] = widths[i];
   int64_t o = 0;
   for (int l = 0; l < 3; ++l) {
@@ -304,19 +269,17 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
     o += m->w[l + 1];
   }
   m->np = o;
+  const int64_t in = m->w[0], a = m->w[1], b = m->w[2], y = m->w[3];
   bool ok = cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) == cudaSuccess &&
-            cudaMalloc(&m->p, 4 * o) == cudaSuccess && cudaMalloc(&m->g, 4 * o) == cudaSuccess &&
-            cudaMalloc(&m->m1, 4 * o) == cudaSuccess && cudaMalloc(&m->m2, 4 * o) == cudaSuccess &&
-            cudaMalloc(&m->pb, 2 * o) == cudaSuccess;
+            cudaEventCreate(&m->ev0) == cudaSuccess && cudaEventCreate(&m->ev1) == cudaSuccess && alloc0(&m->p, o) &&
+            alloc0(&m->g, o) && alloc0(&m->m1, o) && alloc0(&m->m2, o) && alloc0(&m->err, 2) &&
+            alloc0(&m->W1p, panel_elems(a, in)) && alloc0(&m->W2p, panel_elems(b, a)) &&
+            alloc0(&m->W2t, panel_elems(a, b)) && alloc0(&m->W3p, panel_elems(y, b)) &&
+            alloc0(&m->W3t, panel_elems(b, y));
   if (!ok) {
     cpals_mlp_destroy(m);
     return CPALS_E_CUDA;
   }
-  cudaMemset(m->p, 0, 4 * o);
-  cudaMemset(m->g, 0, 4 * o);
-  cudaMemset(m->m1, 0, 4 * o);
-  cudaMemset(m->m2, 0, 4 * o);
-  cudaMemset(m->pb, 0, 2 * o);
   *out = m;
   return CPALS_OK;
 }
@@ -324,11 +287,12 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
 int cpals_mlp_destroy(cpals_mlp* m) {
   if (!m) return CPALS_OK;
   DeviceGuard guard(m->device);
-  for (void* q : {(void*)m->p, (void*)m->g, (void*)m->m1, (void*)m->m2, (void*)m->pb, (void*)m->x, (void*)m->t,
-                  (void*)m->h1, (void*)m->h2, (void*)m->y, (void*)m->dy, (void*)m->dh2, (void*)m->dh1,
-                  (void*)m->xb, (void*)m->h1b, (void*)m->h2b, (void*)m->dyb, (void*)m->dh2b, (void*)m->dh1b,
-                  (void*)m->loss, (void*)m->idx, (void*)m->dx, (void*)m->dt})
+  free_batch(m);
+  for (void* q : {(void*)m->p, (void*)m->g, (void*)m->m1, (void*)m->m2, (void*)m->err, (void*)m->W1p, (void*)m->W2p,
+                  (void*)m->W2t, (void*)m->W3p, (void*)m->W3t, (void*)m->idx, (void*)m->dx, (void*)m->dt})
     cudaFree(q);
+  if (m->ev0) cudaEventDestroy(m->ev0);
+  if (m->ev1) cudaEventDestroy(m->ev1);
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
   return CPALS_OK;
@@ -343,10 +307,9 @@ int cpals_mlp_set_params(cpals_mlp* m, const float* host_params) {
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->p, host_params, 4 * m->np, cudaMemcpyHostToDevice, m->st));
   CPALS_CUDA_TRY(cudaMemsetAsync(m->m1, 0, 4 * m->np, m->st));
   CPALS_CUDA_TRY(cudaMemsetAsync(m->m2, 0, 4 * m->np, m->st));
-  k_to_bf16<<<grid1(m->np), 256, 0, m->st>>>(m->p, m->np, m->pb);
+  CPALS_CUDA_TRY(refresh_weights(m));
   m->step = 0;
-  CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));
-  return CPALS_OK;
+  return finish(m);
 }
 
 int cpals_mlp_get_params(cpals_mlp* m, float* host_params) {
@@ -363,11 +326,9 @@ int cpals_mlp_forward(cpals_mlp* m, const float* host_x, int B, float* host_y) {
   DeviceGuard guard(m->device);
   if (ensure_batch(m, B) != CPALS_OK) return CPALS_E_CUDA;
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->x, host_x, 4LL * B * m->w[0], cudaMemcpyHostToDevice, m->st));
-  k_to_bf16<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->x, (int64_t)B * m->w[0], m->xb);
-  forward(m, B);
+  CPALS_CUDA_TRY(forward(m, B));
   CPALS_CUDA_TRY(cudaMemcpyAsync(host_y, m->y, 4LL * B * m->w[3], cudaMemcpyDeviceToHost, m->st));
-  CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));
-  return CPALS_OK;
+  return finish(m);
 }
 
 // Loss and gradients (FP32, same layout as the parameters) of one host batch, no update.
@@ -378,13 +339,18 @@ int cpals_mlp_gradients(cpals_mlp* m, const float* host_x, const float* host_t, 
   if (ensure_batch(m, B) != CPALS_OK) return CPALS_E_CUDA;
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->x, host_x, 4LL * B * m->w[0], cudaMemcpyHostToDevice, m->st));
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->t, host_t, 4LL * B * m->w[3], cudaMemcpyHostToDevice, m->st));
-  k_to_bf16<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->x, (int64_t)B * m->w[0], m->xb);
-  forward(m, B);
-  const int lb = backward(m, B);
-  const double l = read_loss(m, lb);
-  if (loss_out) *loss_out = l / ((double)B * m->w[3]);
+  CPALS_CUDA_TRY(forward(m, B));
+  cudaError_t e = cudaSuccess;
+  const int lb = backward(m, B, 0, &e);
+  CPALS_CUDA_TRY(e);
+  std::vector<double> h(lb);
+  CPALS_CUDA_TRY(cudaMemcpyAsync(h.data(), m->loss, sizeof(double) * lb, cudaMemcpyDeviceToHost, m->st));
   CPALS_CUDA_TRY(cudaMemcpyAsync(host_grads, m->g, 4 * m->np, cudaMemcpyDeviceToHost, m->st));
-  CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));
+  const int rc = finish(m);
+  if (rc != CPALS_OK) return rc;
+  double l = 0.0;
+  for (double v : h) l += v;
+  if (loss_out) *loss_out = l / ((double)B * m->w[3]);
   return CPALS_OK;
 }
 
@@ -404,23 +370,66 @@ int cpals_mlp_set_dataset(cpals_mlp* m, const float* host_x, const float* host_t
 }
 
 // `steps` Adam steps on batches of B rows of the device dataset; batch s uses rows
-// idx[s*B .. s*B+B-1].  losses (may be null) receives each step's mean loss.
+// idx[s*B .. s*B+B-1].  losses (may be null) receives each step's mean loss.  The indices
+// go to the device once; the losses come back once per 64 steps.
 int cpals_mlp_train(cpals_mlp* m, const int* host_idx, int steps, int B, float lr, double* losses) {
   if (!m || !host_idx || steps < 1 || B < 1 || !m->dx) return CPALS_E_ARG;
   DeviceGuard guard(m->device);
   if (ensure_batch(m, B) != CPALS_OK) return CPALS_E_CUDA;
-  for (int64_t i = 0; i < (int64_t)steps * B; ++i)
+  const int64_t nidx = (int64_t)steps * B;
+  for (int64_t i = 0; i < nidx; ++i)
     if (host_idx[i] < 0 || host_idx[i] >= m->dn) return CPALS_E_ARG;
-  for (int s = 0; s < steps; ++s) {
-    CPALS_CUDA_TRY(cudaMemcpyAsync(m->idx, host_idx + (int64_t)s * B, sizeof(int) * B, cudaMemcpyHostToDevice, m->st));
-    k_gather_rows<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->dx, m->w[0], m->idx, B, nullptr, m->xb);
-    k_gather_rows<<<grid1((int64_t)B * m->w[3]), 256, 0, m->st>>>(m->dt, m->w[3], m->idx, B, m->t, nullptr);
-    forward(m, B);
-    const int lb = backward(m, B);
-    adam(m, lr);
-    if (losses) losses[s] = read_loss(m, lb) / ((double)B * m->w[3]);
+  if (nidx > m->idx_cap) {
+    cudaFree(m->idx);
+    m->idx = nullptr;
+    m->idx_cap = 0;
+    if (cudaMalloc(&m->idx, sizeof(int) * nidx) != cudaSuccess) return CPALS_E_CUDA;
+    m->idx_cap = nidx;
   }
-  CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));
+  CPALS_CUDA_TRY(cudaMemcpyAsync(m->idx, host_idx, sizeof(int) * nidx, cudaMemcpyHostToDevice, m->st));
+  constexpr int kSlots = 64;  // 64 steps x at most 64 partials fill the 4096 loss words
+  std::vector<double> h;
+  m->train_ms = 0.0;
+  for (int s0 = 0; s0 < steps; s0 += kSlots) {
+    const int ns = std::min(kSlots, steps - s0);
+    int lb = 1;
+    CPALS_CUDA_TRY(cudaEventRecord(m->ev0, m->st));
+    for (int j = 0; j < ns; ++j) {
+      const int* ix = m->idx + (int64_t)(s0 + j) * B;
+      k_gather_rows<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->dx, m->w[0], ix, B, m->x);
+      k_gather_rows<<<grid1((int64_t)B * m->w[3]), 256, 0, m->st>>>(m->dt, m->w[3], ix, B, m->t);
+      CPALS_CUDA_TRY(forward(m, B));
+      cudaError_t e = cudaSuccess;
+      lb = backward(m, B, j, &e);
+      CPALS_CUDA_TRY(e);
+      CPALS_CUDA_TRY(adam(m, lr));
+    }
+    CPALS_CUDA_TRY(cudaEventRecord(m->ev1, m->st));
+    h.assign((size_t)ns * lb, 0.0);
+    CPALS_CUDA_TRY(cudaMemcpyAsync(h.data(), m->loss, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, m->st));
+    const int rc = finish(m);
+    if (rc != CPALS_OK) return rc;
+    float ms = 0.f;
+    CPALS_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+    m->train_ms += ms;
+    if (losses)
+      for (int j = 0; j < ns; ++j) {
+        double l = 0.0;
+        for (int q = 0; q < lb; ++q) l += h[(size_t)j * lb + q];
+        losses[s0 + j] = l / ((double)B * m->w[3]);
+      }
+  }
+  return CPALS_OK;
+}
+
+// Device time (CUDA events on the network's stream) of the last cpals_mlp_train call, in ms,
+// and the tensor-core flops of one training step of B rows (the eight GEMMs).
+int cpals_mlp_train_stats(cpals_mlp* m, int B, double* ms, double* flops_per_step) {
+  if (!m || B < 1) return CPALS_E_ARG;
+  const double in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
+  if (ms) *ms = m->train_ms;
+  // forward: x W1^T, h1 W2^T, h2 W3^T; backward: three weight gradients, two input gradients
+  if (flops_per_step) *flops_per_step = 2.0 * B * (2.0 * in * a + 3.0 * a * b + 3.0 * b * o);
   return CPALS_OK;
 }
 

@@ -10,10 +10,16 @@
    Abel 1993) of the core: two random mode-3 contractions M1, M2 of G; the eigenvectors of
    M1 M2^+ and of M1^T M2^{+T} give the mode-1 and mode-2 coefficients, least squares the
    third.  It is exact for a noise-free core of rank R <= S with independent factors.
-4. Refinement.  A 3-layer MLP (BF16, FP32 accumulation, trained on the device by libcpals'
-   own forward / backward / Adam kernels) maps the proposal of the three modes to a
-   correction of each mode's coefficients; the start is F_n = Q_n (C_n + dC_n), columns
-   normalised: it lies inside the sketched column range.
+4. Teacher.  The batched solver (cpals_batch_*) runs ALS on the cores of many training
+   tensors at once, from their proposals: one sweep gives the step D = P1 - P, convergence
+   gives the core's own CP coefficients P*.  Sweeps on an S^3 core cost a fraction of a
+   sweep on the full tensor, and the column order of P is kept.
+5. Network.  A 3-layer MLP (BF16, FP32 accumulation, every product on the tensor cores,
+   trained on the device by libcpals' own forward / backward / Adam kernels) maps the
+   proposal and its one-sweep step of the three modes to the correction P* - P of each
+   mode; the learned start is F_n = Q_n (P_n + s dP_n), columns normalised: it lies inside
+   the sketched column range.  It costs one core sweep and one forward pass instead of the
+   teacher's many sweeps.
 
 Random-init ALS stays the fallback, and ALS decides when to stop: the warm start changes only
 the starting point, ALS still runs to its convergence check, and a degenerate start (non-finite values
@@ -43,6 +49,7 @@ class WarmStartMLP:
         self.h = h
         self.n_params = int(self.lib.cpals_mlp_num_params(h))
         self.scale = 1.0  # step applied to the predicted correction (see calibrate)
+        self.step_scale = 1.0  # unit of the one-sweep steps and corrections in the network's input and output
         self.min_scale = 0.05
         self.set_params(self.init_params(np.random.default_rng(seed)) if params is None else params)
 
@@ -109,6 +116,12 @@ class WarmStartMLP:
             self.scale = 0.0  # the correction does not generalise: the proposal is used as is
         return self.scale
 
+    def train_stats(self, batch):
+        """Device ms of the last training call's launches and the tensor-core flops of one step."""
+        ms, fl = C.c_double(), C.c_double()
+        L.check(self.lib.cpals_mlp_train_stats(self.h, int(batch), C.byref(ms), C.byref(fl)), "cpals_mlp_train_stats")
+        return ms.value, fl.value
+
     def fit(self, X, T, epochs=30, batch=256, lr=1e-3, seed=0):
         """Adam on (X, T) held on the device; returns the per-step losses."""
         X = np.ascontiguousarray(np.asarray(X, dtype=np.float32))
@@ -119,12 +132,15 @@ class WarmStartMLP:
         batch = min(batch, n)
         steps = n // batch
         losses = []
+        self.fit_ms, self.fit_steps = 0.0, 0
         for _ in range(epochs):
             idx = rng.permutation(n)[: steps * batch].astype(np.int32)
             out = np.empty(steps)
             L.check(self.lib.cpals_mlp_train(self.h, idx.ctypes.data_as(C.POINTER(C.c_int)), steps, batch,
                                              float(lr), L.dptr(out)), "cpals_mlp_train")
             losses.extend(out.tolist())
+            self.fit_ms += self.train_stats(batch)[0]
+            self.fit_steps += steps
         return np.asarray(losses)
 
 
@@ -156,14 +172,45 @@ def sketch_bases(Ys):
     return Qs, Zs
 
 
-def features(Cs):
-    """Network input of each mode: its own coefficients, then the other modes' in mode order."""
-    N = len(Cs)
+def features(props, steps, step_scale=1.0):
+    """Network input of each mode n of each tensor: [P_n, D_n / step_scale] of its own mode,
+    then of the other modes in mode order (P the proposal's coefficients, D the one-sweep
+    step), as rows of FP32."""
     rows = []
-    for n in range(N):
-        parts = [np.asarray(Cs[n]).ravel()] + [np.asarray(Cs[m]).ravel() for m in range(N) if m != n]
-        rows.append(np.concatenate(parts))
+    for P, D in zip(props, steps):
+        N = len(P)
+        for n in range(N):
+            parts = []
+            for m in [n] + [m for m in range(N) if m != n]:
+                parts += [np.asarray(P[m]).ravel(), np.asarray(D[m]).ravel() / step_scale]
+            rows.append(np.concatenate(parts))
     return np.asarray(rows, dtype=np.float32)
+
+
+def targets(props, solved, step_scale=1.0):
+    """Training targets: the correction P*_n - P_n of every mode (in units of step_scale)."""
+    return np.asarray([((np.asarray(C) - np.asarray(P)) / step_scale).ravel()
+                       for Ps, Cs in zip(props, solved) for P, C in zip(Ps, Cs)], dtype=np.float32)
+
+
+def core_als(be, cores, starts, max_iter, tol=0.0):
+    """ALS on S^3 cores with the batched solver `be` (a BatchEngine sized for these cores),
+    from coefficient starts with unit columns.  Returns the coefficients (unit columns, each
+    column signed like its start) and the sweeps each core ran."""
+    R = starts[0][0].shape[1]
+    be.set_norms([max(float(np.linalg.norm(G)), 1e-300) for G in cores])
+    be.set_tensors([np.asarray(G, dtype=np.float32) for G in cores])
+    be.set_factors(starts, [np.ones(R)] * len(cores))
+    sweeps, _, _, _ = be.optimize(tol=tol, max_iter=max_iter)
+    out = []
+    for (F, _), P in zip(be.get_factors(), starts):
+        C = []
+        for Fn, Pn in zip(F, P):
+            sg = np.sign(np.sum(Fn * Pn, axis=0))
+            sg[sg == 0] = 1.0
+            C.append(Fn * sg[None, :])
+        out.append(C)
+    return out, sweeps
 
 
 def core(core_engine, Qs):
@@ -207,38 +254,33 @@ def jennrich(G, R, rng):
     return [A, B, C]
 
 
-def targets(Qs, factors, proposal):
-    """Correction targets: the ALS factors in the sketch bases, C_n = Q_n^T F_n (unit columns),
-    matched to the proposal's components (Hungarian assignment on the summed |cosine| of the
-    three modes) and signed like them, minus the proposal."""
-    from scipy.optimize import linear_sum_assignment
-
-    Cs = []
-    for Q, F in zip(Qs, factors):
-        Cn = Q.T @ np.asarray(F)
-        Cs.append(Cn / np.maximum(np.linalg.norm(Cn, axis=0), 1e-300))
-    score = sum(np.abs(P.T @ Cn) for P, Cn in zip(proposal, Cs))
-    _, col = linear_sum_assignment(-score)
-    out = []
-    for P, Cn in zip(proposal, Cs):
-        Cm = Cn[:, col]
-        sg = np.sign(np.sum(P * Cm, axis=0))
-        sg[sg == 0] = 1.0
-        out.append((Cm * sg[None, :] - P).ravel())
-    return np.asarray(out, dtype=np.float32)
-
-
 def proposal_factors(Qs, proposal):
     """The start without the network: F_n = Q_n C_n from the proposal."""
     return _lift(Qs, proposal)
 
 
-def warm_factors(mlp, Qs, proposal):
-    """The learned start: F_n = Q_n (C_n + s dC_n), dC_n from the network, s its calibrated
-    step; None if degenerate."""
-    S, R = proposal[0].shape
-    D = mlp.forward(features(proposal)) * mlp.scale
-    return _lift(Qs, [P + D[n].astype(np.float64).reshape(S, R) for n, P in enumerate(proposal)])
+def learned_coefficients(mlp, props, steps):
+    """P + s dP for each tensor: the network's correction in step units, times its calibrated
+    step s."""
+    D = mlp.forward(features(props, steps, mlp.step_scale)) * (mlp.scale * mlp.step_scale)
+    out, k = [], 0
+    for P in props:
+        C = []
+        for Pn in P:
+            C.append(Pn + D[k].astype(np.float64).reshape(Pn.shape))
+            k += 1
+        out.append(C)
+    return out
+
+
+def warm_factors(mlp, Qs, proposal, step):
+    """The learned start of one tensor: F_n = Q_n (P_n + s dP_n); None if degenerate."""
+    return _lift(Qs, learned_coefficients(mlp, [proposal], [step])[0])
+
+
+def lift(Qs, Cs):
+    """F_n = Q_n C_n with unit columns; None if degenerate."""
+    return _lift(Qs, Cs)
 
 
 def _lift(Qs, Cs):

@@ -66,6 +66,8 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.cpals_mode_update(None, 0, None) == -1
     assert lib.cpals_tensor_norm(None, None, None) == -1
     assert lib.cpals_check_converge(None, None, None, None) == -1
+    assert lib.cpals_batch_set_norms(None, None) == -1
+    assert lib.cpals_mlp_forward(None, None, 1, None) == -1
 
 
 def test_create_rejects_more_than_2_40_elements_without_overflow(lib):

@@ -548,7 +548,8 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // is the composition of the single-index sweeps over P; after every block A = -V^{-1}.  The
 // indices are swept in blocks of 32 in their natural order (V is symmetric positive definite
 // whenever this path is taken; any pivot order is sound because the solve refines X):
-//   (a) warp 0 sweeps D in shared memory, one index at a time, rows split over the lanes;
+//   (a) warp 0 sweeps D in registers (lane i holds row i), one index at a time; the pivot
+//       row reaches the lanes by shuffles, and per-lane selects replace a branch on lane == k;
 //   (b) all warps form B = A_{.P} D^{-1} and keep A_{.P} (both transposed, 32 x R);
 //   (c) all warps apply the rank-32 update to the rest of A in 4 x 4 register tiles and write
 //       the swept blocks back.

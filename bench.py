@@ -189,6 +189,29 @@ def pinned_like(shape):
         return np.empty(shape, dtype=np.float32, order="F"), None
 
 
+def h2d_probe(keep, device):
+    """The host link as the e2e leg sees it: whether the host tensor is pinned, and the GB/s of
+    one copy of it to the device (CUDA events on torch's stream)."""
+    try:
+        import torch
+
+        if keep is None:
+            return {"host_pinned": False}
+        dst = torch.empty_like(keep, device=f"cuda:{device}")
+        dst.copy_(keep, non_blocking=True)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        dst.copy_(keep, non_blocking=True)
+        b.record()
+        b.synchronize()
+        ms = a.elapsed_time(b)
+        del dst
+        return {"host_pinned": bool(keep.is_pinned()), "h2d_copy_gbs": keep.numel() * 4 / (ms * 1e-3) / 1e9}
+    except Exception as exc:
+        return {"h2d_probe_error": str(exc)}
+
+
 def mttkrp_alg_bytes(dims, R, mode, esize=4):
     n = int(np.prod(dims))
     return n * esize + sum(d * R * 4 for m, d in enumerate(dims) if m != mode) + dims[mode] * R * 4
@@ -942,6 +965,7 @@ def main():
     e2e_ms = max_over_ranks(eng.timer_stop())
     e2e_value = replica_value(world, args.steps, SWEEPS, e2e_ms)
     fac_bytes = sum(d * RANK * 8 for d in DIMS) + RANK * 8
+    h2d = h2d_probe(keep, device)
 
     # ---- sweep time under each convergence check (tolerance 0, so none stops early)
     checks = {}
@@ -1036,7 +1060,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind},
         "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(T_host.nbytes + fac_bytes),
-                "d2h_bytes_per_step": int(fac_bytes)},
+                "d2h_bytes_per_step": int(fac_bytes), **h2d},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,

@@ -114,8 +114,19 @@ cudaError_t cpals::set_smem_limit_once(const void* kernel, int bytes) {
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(mu);
   if (done.count({dev, kernel})) return cudaSuccess;
-  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess) done.insert({dev, kernel});
+  // the opt-in limit covers static and dynamic shared memory together
+  cudaFuncAttributes fa{};
+  int optin = 0;
+  e = cudaFuncGetAttributes(&fa, kernel);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) {
+    bytes = std::min(bytes, optin - (int)fa.sharedSizeBytes);
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+  if (e == cudaSuccess)
+    done.insert({dev, kernel});
+  else
+    (void)cudaGetLastError();  // leave no error behind for the next launch check
   return e;
 }
 

@@ -593,11 +593,19 @@ int batch_launch(cpals_batch* b) {
 // Thread count of class c: sets the kernel's shared-memory limit and the resident CTAs per SM.
 int class_config(BatchClass& c, int nt) {
   const void* fn = sweep_fn(nt);
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
+  // the opt-in maximum less the kernel's static shared memory
+  if (set_smem_limit_once(fn, 227 * 1024) != cudaSuccess) return CPALS_E_CUDA;
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+    (void)cudaGetLastError();
     return CPALS_E_CUDA;
+  }
+  if (c.L.total > (size_t)fa.maxDynamicSharedSizeBytes) return CPALS_E_UNSUPPORTED;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, c.L.total) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, c.L.total) != cudaSuccess || per_sm < 1) {
+    (void)cudaGetLastError();
     return CPALS_E_UNSUPPORTED;
+  }
   c.nt = nt;
   c.ctas_per_sm = per_sm;
   return CPALS_OK;

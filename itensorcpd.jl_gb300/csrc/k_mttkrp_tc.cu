@@ -47,12 +47,11 @@ namespace {
 
 constexpr int kChunk = 64;     // K values per stage (one 128-byte swizzle row of BF16)
 constexpr int kBlockM = 128;   // rows per CTA (one UMMA M)
-// Drain warps: one per TMEM lane quarter, two (each taking half of the columns) when the N
-// block is 64 wide, four when it is 128 wide: more warps per quarter cut the per-chunk drain
-// latency and the accumulator registers of the wide blocks.  Warps 0 and 1 produce and issue
-// the MMAs.
+// Drain warps: one per TMEM lane quarter, or two (each taking half of the columns) when
+// the N block is a multiple of 64 wide, which halves the per-chunk drain latency and the
+// accumulator registers of the wide blocks.  Warps 0 and 1 produce and issue the MMAs.
 template <int NB>
-__host__ __device__ constexpr int tc_drain_warps() { return NB == 128 ? 16 : (NB % 64 == 0) ? 8 : 4; }
+__host__ __device__ constexpr int tc_drain_warps() { return (NB % 64 == 0) ? 8 : 4; }
 template <int NB>
 __host__ __device__ constexpr int tc_threads() { return 64 + 32 * tc_drain_warps<NB>(); }
 constexpr size_t kSmemLimit = 227 * 1024;
@@ -272,9 +271,9 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
       tc_fence_after();
       const float* orow = reinterpret_cast<const float*>(outer_rows(s)) + cb;
       const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
-      // 32 columns per TMEM load, or 16 with two or four drain warps per quarter (their
-      // register budget is smaller: 320 or 576 threads)
-      constexpr int W = (tc_drain_warps<NB>() >= 8) ? 16 : 32;
+      // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
+      // budget is smaller: 320 threads)
+      constexpr int W = (tc_drain_warps<NB>() == 8) ? 16 : 32;
 #pragma unroll
       for (int c0 = 0; c0 < NH; c0 += W) {
         uint32_t vh[W], vl[W];
@@ -286,50 +285,26 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
           tmem_ld16_nowait(base + (uint32_t)c0, vh);
           tmem_ld16_nowait(base + (uint32_t)(NB + c0), vl);
         }
-        if constexpr (tc_drain_warps<NB>() <= 8) {
-          // s(r), the outer rows' product in mode order, formed while the TMEM loads land
-          float sc[W];
+        float sc[W];
 #pragma unroll
-          for (int j = 0; j < W; ++j) sc[j] = 1.0f;
-          for (int jo = 0; jo < p.n_outer; ++jo) {
-#pragma unroll
-            for (int j = 0; j < W; j += 4) {
-              if (c0 + j < NH) {
-                const float4 o4 = *reinterpret_cast<const float4*>(orow + jo * NB + c0 + j);
-                sc[j] *= o4.x;
-                sc[j + 1] *= o4.y;
-                sc[j + 2] *= o4.z;
-                sc[j + 3] *= o4.w;
-              }
-            }
-          }
-          tmem_wait_ld();
-#pragma unroll
-          for (int j = 0; j < W; ++j)
-            if (c0 + j < NH)
-              acc[c0 + j] = fmaf(sc[j], __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
-        } else {
-          tmem_wait_ld();
-          // s(r): the outer rows' product, in mode order, four columns at a time (few live
-          // registers beside the loaded accumulators)
+        for (int j = 0; j < W; ++j) sc[j] = 1.0f;
+        for (int jo = 0; jo < p.n_outer; ++jo) {
 #pragma unroll
           for (int j = 0; j < W; j += 4) {
             if (c0 + j < NH) {
-              float s0 = 1.0f, s1 = 1.0f, s2 = 1.0f, s3 = 1.0f;
-              for (int jo = 0; jo < p.n_outer; ++jo) {
-                const float4 o4 = *reinterpret_cast<const float4*>(orow + jo * NB + c0 + j);
-                s0 *= o4.x;
-                s1 *= o4.y;
-                s2 *= o4.z;
-                s3 *= o4.w;
-              }
-              acc[c0 + j] = fmaf(s0, __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
-              acc[c0 + j + 1] = fmaf(s1, __uint_as_float(vh[j + 1]) + __uint_as_float(vl[j + 1]), acc[c0 + j + 1]);
-              acc[c0 + j + 2] = fmaf(s2, __uint_as_float(vh[j + 2]) + __uint_as_float(vl[j + 2]), acc[c0 + j + 2]);
-              acc[c0 + j + 3] = fmaf(s3, __uint_as_float(vh[j + 3]) + __uint_as_float(vl[j + 3]), acc[c0 + j + 3]);
+              const float4 o4 = *reinterpret_cast<const float4*>(orow + jo * NB + c0 + j);
+              sc[j] *= o4.x;
+              sc[j + 1] *= o4.y;
+              sc[j + 2] *= o4.z;
+              sc[j + 3] *= o4.w;
             }
           }
         }
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          if (c0 + j < NH)
+            acc[c0 + j] = fmaf(sc[j], __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
       }
       tc_fence_before();
       __syncwarp();

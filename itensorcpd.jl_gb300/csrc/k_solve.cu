@@ -616,35 +616,44 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
   const int ntile = Rp / 4;
   for (int p0 = 0; p0 < R; p0 += kBlk32) {
     const int pb = min(kBlk32, R - p0);
-    // (a) sweep of the diagonal block D = A_PP by warp 0: lane i holds row i in registers;
-    // the pivot row reaches every lane by shuffles, and a dynamic column is picked out by an
-    // unrolled select (no dynamically indexed registers)
+    // (a) sweep of the diagonal block D = A_PP by warp 0: lane i holds row i in registers.
+    // Per pivot k, lane k publishes its row in shared memory; every lane reads it back (eight
+    // broadcast 16-byte loads) and takes D(i, k) as D(k, i), the sweep keeping the block
+    // symmetric.  Column k is set by an unrolled select (no dynamically indexed registers).
     if (warp == 0) {
+      float* prow = misc + 32;  // the pivot row (16-byte aligned)
       float r[kBlk32];
 #pragma unroll
       for (int c = 0; c < kBlk32; ++c) r[c] = (lane < pb && c < pb) ? A[(size_t)(p0 + lane) * ld + p0 + c] : 0.f;
       const float thr = misc[0];
       bool bad = false;
       for (int k = 0; k < pb; ++k) {
-        // D(i, k): one nonzero among 32 selected terms, summed as a depth-5 tree (exact)
-        float t[kBlk32];
+        const bool me = (lane == k);
+        if (me) {
 #pragma unroll
-        for (int c = 0; c < kBlk32; ++c) t[c] = (c == k) ? r[c] : 0.f;
+          for (int v = 0; v < kBlk32 / 4; ++v)
+            reinterpret_cast<float4*>(prow)[v] = make_float4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]);
+        }
+        __syncwarp();
+        float rk[kBlk32];
 #pragma unroll
-        for (int w = kBlk32 / 2; w > 0; w >>= 1)
-#pragma unroll
-          for (int c = 0; c < w; ++c) t[c] += t[c + w];
-        const float dik = t[0];
-        const float d = __shfl_sync(0xffffffffu, dik, k);
+        for (int v = 0; v < kBlk32 / 4; ++v) {
+          const float4 x = reinterpret_cast<const float4*>(prow)[v];
+          rk[4 * v] = x.x;
+          rk[4 * v + 1] = x.y;
+          rk[4 * v + 2] = x.z;
+          rk[4 * v + 3] = x.w;
+        }
+        const float dik = prow[lane];
+        const float d = prow[k];
+        __syncwarp();  // the row is read before the next pivot overwrites it
         bad = bad || !(d > thr) || !(d < INFINITY);
-        const float rd = 1.0f / d;
+        const float rd = __frcp_rn(d);
         const float f = dik * rd;
-        const bool me = (lane == k);  // row k itself: per-lane selects, no divergent branch
         const float pk = me ? -rd : f;
 #pragma unroll
         for (int c = 0; c < kBlk32; ++c) {
-          const float rkc = __shfl_sync(0xffffffffu, r[c], k);  // D(k, c)
-          const float v = me ? rkc * rd : fmaf(-f, rkc, r[c]);
+          const float v = me ? rk[c] * rd : fmaf(-f, rk[c], r[c]);
           r[c] = (c == k) ? pk : v;
         }
       }

@@ -46,6 +46,12 @@ struct BatchItem {
   double ref_norm;
 };
 
+struct BatchRun {  // the FitCheck parameters of the current optimize call (read by the sweep kernel)
+  double tol;
+  int max_iter;
+  int pad;
+};
+
 struct BatchCheck {  // fit_check.jl:5-20, per tensor
   int iter, counter, done, sweeps;
   int total_iter, rank_deficient, nan, pad;
@@ -426,10 +432,12 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_batch_sweep(const BatchItem* __restrict__ items, const int* __restrict__ order,
                                                     int count, const float* __restrict__ T, double* __restrict__ F,
                                                     double* __restrict__ G, BatchCheck* __restrict__ chk,
-                                                    unsigned* __restrict__ queue, SmemLayout L, double tol,
-                                                    int max_iter) {
+                                                    unsigned* __restrict__ queue, SmemLayout L,
+                                                    const BatchRun* __restrict__ run) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ int s_t;
+  const double tol = run->tol;
+  const int max_iter = run->max_iter;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_t = (int)atomicAdd(queue, 1u);
@@ -517,6 +525,8 @@ struct cpals_batch {
   unsigned* d_queue = nullptr;
   int* d_active = nullptr;
   int* h_active = nullptr;
+  BatchRun* d_run = nullptr;  // tol and max_iter, outside the graph so that changing them keeps it
+  BatchRun* h_run = nullptr;
   cudaStream_t st = nullptr;
   cudaGraphExec_t graph = nullptr;
   int nt = 256;         // threads per CTA (autotuned)
@@ -550,15 +560,15 @@ int class_launch(cpals_batch* b, const BatchClass& c, int q, cudaStream_t st) {
   switch (c.nt) {
     case 128:
       k_batch_sweep<128><<<grid, 128, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
-                                                          b->d_queue + q, c.L, b->tol, b->max_iter);
+                                                          b->d_queue + q, c.L, b->d_run);
       break;
     case 256:
       k_batch_sweep<256><<<grid, 256, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
-                                                          b->d_queue + q, c.L, b->tol, b->max_iter);
+                                                          b->d_queue + q, c.L, b->d_run);
       break;
     case 512:
       k_batch_sweep<512><<<grid, 512, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
-                                                          b->d_queue + q, c.L, b->tol, b->max_iter);
+                                                          b->d_queue + q, c.L, b->d_run);
       break;
     default:
       return CPALS_E_ARG;
@@ -749,7 +759,9 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
             cudaMalloc(&b->d_queue, sizeof(unsigned) * kMaxBatchClasses) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
             cudaMalloc(&b->d_active, sizeof(int)) == cudaSuccess &&
-            cudaMallocHost(&b->h_active, sizeof(int)) == cudaSuccess;
+            cudaMallocHost(&b->h_active, sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&b->d_run, sizeof(BatchRun)) == cudaSuccess &&
+            cudaMallocHost(&b->h_run, sizeof(BatchRun)) == cudaSuccess;
   for (BatchClass& c : b->split)
     ok = ok && cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming) == cudaSuccess;
@@ -758,6 +770,8 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
     return CPALS_E_CUDA;
   }
   cudaMemcpy(b->d_items, b->items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice);
+  *b->h_run = BatchRun{b->tol, b->max_iter, 0};  // what the autotuner's sweeps use
+  cudaMemcpy(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_order, b->order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
   cudaMemset(b->d_queue, 0, sizeof(unsigned) * kMaxBatchClasses);
   cudaMemset(b->d_chk, 0, sizeof(BatchCheck) * count);
@@ -783,6 +797,8 @@ int cpals_batch_destroy(cpals_batch* b) {
   cudaFree(b->d_queue);
   cudaFree(b->d_active);
   if (b->h_active) cudaFreeHost(b->h_active);
+  cudaFree(b->d_run);
+  if (b->h_run) cudaFreeHost(b->h_run);
   for (BatchClass& c : b->split) {
     if (c.st) cudaStreamDestroy(c.st);
     if (c.done) cudaEventDestroy(c.done);
@@ -842,14 +858,10 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
                          int* flags_out, int64_t* launches_out) {
   if (!b || max_iter < 1 || !(tol >= 0.0)) return CPALS_E_ARG;
   DeviceGuard guard(b->device);
-  if (b->tol != tol || b->max_iter != max_iter) {
-    b->tol = tol;
-    b->max_iter = max_iter;
-    if (b->graph) {
-      cudaGraphExecDestroy(b->graph);
-      b->graph = nullptr;
-    }
-  }
+  b->tol = tol;
+  b->max_iter = max_iter;
+  *b->h_run = BatchRun{tol, max_iter, 0};
+  CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice, b->st));
   if (!b->graph) {
     int rc = build_graph(b);
     if (rc != CPALS_OK) return rc;

@@ -66,6 +66,9 @@ struct TcModePlan {
   // own ring (obytes per stage, at orow_off).  ctl_off: barriers and flags.
   int bres;
   uint32_t bres_off, orow_off, obytes, ctl_off;
+  // Chunks per accumulation group: consecutive factor blocks of one outer index accumulate in
+  // the same TMEM buffer before one drain (1, or 2 for 128-wide N blocks).
+  int grp;
   int64_t outer_dims[kMaxOrder];
   int64_t outer_stride[kMaxOrder];  // element stride of each outer mode in the tensor
   int outer_modes[kMaxOrder];
@@ -205,7 +208,8 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer: per chunk, fresh accumulators in buffer b = it % kBuf.
+    // ---------------- MMA issuer: per accumulation group g (p.grp chunks of one outer index),
+    // fresh accumulators in buffer b = g % kBuf.
     // B = [Bh; Bl] stacked (2 NB rows): one N = 2 NB product gives Th Bh and Th Bl
     // together, a second N = NB product adds Tl Bh onto the cross terms.
     if (lane == 0) {
@@ -215,13 +219,16 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         *abort_flag = 1;
       }
       int64_t fbm = (c_begin % p.nfb);  // the chunk's factor block, kept without a division per chunk
+      int g = 0;          // accumulation group
+      bool first = true;  // first chunk of group g
       for (int it = 0; it < nloc && !*abort_flag; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
-        const int b = it % kBuf;
-        const uint32_t uph = (uint32_t)((it / kBuf) & 1);
+        const int b = g % kBuf;
+        const uint32_t uph = (uint32_t)((g / kBuf) & 1);
+        const bool last = (it + 1 == nloc) || ((fbm + 1) % p.grp == 0) || (fbm + 1 == p.nfb);
         if (!mbar_wait(smem_u32(&full_a[s]), ph, abort_flag) ||
-            !mbar_wait(smem_u32(&acc_empty[b]), uph ^ 1u, abort_flag)) {
+            (first && !mbar_wait(smem_u32(&acc_empty[b]), uph ^ 1u, abort_flag))) {
           atomicCAS(err, 0, 2);
           *abort_flag = 1;
           break;
@@ -234,10 +241,14 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         for (int kk = 0; kk < kChunk / 16; ++kk) {
           const uint32_t off = kk * 32;
           const uint64_t dah = sw128_desc(ah + off), dal = sw128_desc(al + off), dbh = sw128_desc(bh + off);
-          umma_bf16(acc_h, dah, dbh, idesc_w, kk > 0 ? 1u : 0u);  // [Th Bh | Th Bl]
-          umma_bf16(acc_l, dal, dbh, idesc_n, 1u);                // += Tl Bh
+          umma_bf16(acc_h, dah, dbh, idesc_w, (first && kk == 0) ? 0u : 1u);  // [Th Bh | Th Bl]
+          umma_bf16(acc_l, dal, dbh, idesc_n, 1u);                           // += Tl Bh
         }
-        umma_commit(smem_u32(&acc_full[b]));
+        if (last) {
+          umma_commit(smem_u32(&acc_full[b]));
+          ++g;
+        }
+        first = last;
       }
       umma_commit(smem_u32(done_bar));
     }
@@ -253,10 +264,13 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
 #pragma unroll
     for (int j = 0; j < NH; ++j) acc[j] = 0.0f;
     bool ok = true;
-    for (int it = 0; it < nloc && ok; ++it) {
+    int64_t fbm = (c_begin % p.nfb);
+    int g = 0, it0 = 0;  // accumulation group and its first chunk
+    for (int it = 0; it < nloc && ok; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
+      if (!((it + 1 == nloc) || ((fbm + 1) % p.grp == 0) || (fbm + 1 == p.nfb))) continue;  // not a group's last chunk
       const int s = it % S;
-      const int b = it % kBuf;
-      const uint32_t uph = (uint32_t)((it / kBuf) & 1);
+      const int b = g % kBuf;
+      const uint32_t uph = (uint32_t)((g / kBuf) & 1);
       int got = 0;
       if (lane == 0) got = mbar_wait(smem_u32(&acc_full[b]), uph, abort_flag) ? 1 : 0;
       got = __shfl_sync(0xffffffffu, got, 0);
@@ -269,6 +283,10 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         break;
       }
       tc_fence_after();
+      // the group's earlier stages are free: their MMAs have completed, and the outer rows
+      // (one outer index per group) are read from the last chunk's stage
+      if (lane == 0)
+        for (int j = it0; j < it; ++j) mbar_arrive(smem_u32(&empty[j % S]));
       const float* orow = reinterpret_cast<const float*>(outer_rows(s)) + cb;
       const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
       // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
@@ -312,6 +330,8 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         mbar_arrive(smem_u32(&acc_empty[b]));
         mbar_arrive(smem_u32(&empty[s]));
       }
+      ++g;
+      it0 = it + 1;
     }
     if (nloc > 0 && ok) {
       int got = 0;
@@ -488,6 +508,7 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     p.rpad = (int)s->rpad;
     p.tmem_cols = tcols;
     p.nfb = (p.If + kChunk - 1) / kChunk;
+    p.grp = (nb == 128) ? 2 : 1;
     int64_t outer = 1;
     for (int m = 0; m < order; ++m) {
       if (m == n || m == p.fmode) continue;

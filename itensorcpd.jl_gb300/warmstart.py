@@ -50,6 +50,7 @@ class WarmStartMLP:
         self.n_params = int(self.lib.cpals_mlp_num_params(h))
         self.scale = 1.0  # step applied to the predicted correction (see calibrate)
         self.step_scale = 1.0  # unit of the one-sweep steps and corrections in the network's input and output
+        self.step_gain = 0.0  # least-squares gain of the one-sweep step (see fit_step_gain)
         self.min_scale = 0.05
         self.set_params(self.init_params(np.random.default_rng(seed)) if params is None else params)
 
@@ -232,19 +233,34 @@ def core(core_engine, Qs):
 
 
 def jennrich(G, R, rng):
-    """CP proposal of the core by simultaneous diagonalisation; unit columns (real parts of
-    the eigenvectors), components ordered by decreasing |eigenvalue|."""
+    """CP proposal of the core by simultaneous diagonalisation; unit columns, components
+    ordered by decreasing |eigenvalue|.  A complex-conjugate pair of eigenvalues among the R
+    kept gives the real and imaginary parts of its eigenvector as two columns (the real
+    invariant subspace of the pair), so no two columns repeat."""
     S = G.shape[0]
     x, y = rng.standard_normal(S), rng.standard_normal(S)
     M1 = np.tensordot(G, x, axes=([2], [0]))
     M2 = np.tensordot(G, y, axes=([2], [0]))
     ev, V = np.linalg.eig(M1 @ np.linalg.pinv(M2))
-    order = np.argsort(-np.abs(ev))[:R]
-    A = np.real(V[:, order])
+    order = list(np.argsort(-np.abs(ev))[:R])
     ev2, V2 = np.linalg.eig(M1.T @ np.linalg.pinv(M2.T))
+    A = np.empty((S, R))
     B = np.empty((S, R))
-    for k, e in enumerate(ev[order]):
-        B[:, k] = np.real(V2[:, np.argmin(np.abs(ev2 - e))])
+    done = set()
+    for k, j in enumerate(order):
+        if k in done:
+            continue
+        e = ev[j]
+        vb = V2[:, np.argmin(np.abs(ev2 - e))]
+        A[:, k], B[:, k] = np.real(V[:, j]), np.real(vb)
+        done.add(k)
+        if abs(e.imag) > 1e-12 * max(abs(e), 1e-300):
+            # the conjugate partner, if kept: the imaginary parts
+            part = [q for q in range(k + 1, R) if q not in done and abs(ev[order[q]] - np.conj(e)) <= 1e-9 * abs(e)]
+            if part:
+                q = part[0]
+                A[:, q], B[:, q] = np.imag(V[:, j]), np.imag(vb)
+                done.add(q)
     A = A / np.maximum(np.linalg.norm(A, axis=0), 1e-300)
     B = B / np.maximum(np.linalg.norm(B, axis=0), 1e-300)
     K = (B[:, None, :] * A[None, :, :]).reshape(S * S, R)  # column r = B(:, r) (x) A(:, r)
@@ -252,17 +268,30 @@ def jennrich(G, R, rng):
     C = np.linalg.lstsq(K, G2.T, rcond=None)[0].T
     C = C / np.maximum(np.linalg.norm(C, axis=0), 1e-300)
     return [A, B, C]
-
-
 def proposal_factors(Qs, proposal):
     """The start without the network: F_n = Q_n C_n from the proposal."""
     return _lift(Qs, proposal)
 
 
+def fit_step_gain(X, Y, SR):
+    """Least-squares gain a of the one-sweep step (the second S*R block of each feature row)
+    as a predictor of the target rows: the linear part of the correction, which the network
+    then refines."""
+    D = X[:, SR:2 * SR].astype(np.float64)
+    return float(np.sum(D * Y) / max(np.sum(D * D), 1e-300))
+
+
+def residual_targets(X, Y, SR, gain):
+    """What the network learns: the target less the gain times the step."""
+    return (Y - gain * X[:, SR:2 * SR]).astype(np.float32)
+
+
 def learned_coefficients(mlp, props, steps):
-    """P + s dP for each tensor: the network's correction in step units, times its calibrated
-    step s."""
-    D = mlp.forward(features(props, steps, mlp.step_scale)) * (mlp.scale * mlp.step_scale)
+    """P + a D + s dP for each tensor: the step's least-squares gain a (mlp.step_gain) plus the
+    network's correction of what is left, times its calibrated step s."""
+    X = features(props, steps, mlp.step_scale)
+    SR = props[0][0].size
+    D = (mlp.step_gain * X[:, SR:2 * SR] + mlp.forward(X) * mlp.scale) * mlp.step_scale
     out, k = [], 0
     for P in props:
         C = []

@@ -741,22 +741,36 @@ def run_c5(args, pkg, device):
         res = {k: {"sweeps": [], "ms": []} for k in keys}
         fallbacks = 0
         e2e_ms = []
+        # the held-out tensors' starts are made the batched way: sketch, core and proposal per
+        # tensor, then one batched core-ALS call over every held-out core (one sweep for the
+        # network's input, FitCheck(1e-8, 300) for the teacher) and one forward pass; the batched
+        # calls' time is shared out evenly
+        ne = args.c5_eval
+        ev = [prepare(eng, core_eng, 2_000_000 + s) for s in range(ne)]
+        be_ev = pkg.BatchEngine([(S, S, S)] * ne, [R] * ne, [1.0] * ne, device=device)
+        t1 = time.perf_counter()
+        P1e, _ = ws.core_als(be_ev, [e[2] for e in ev], [e[3] for e in ev], 1)
+        ms_p1 = 1e3 * (time.perf_counter() - t1) / ne
+        t1 = time.perf_counter()
+        Cle = ws.learned_coefficients(net, [e[3] for e in ev],
+                                      [[a - b for a, b in zip(p1, e[3])] for p1, e in zip(P1e, ev)])
+        ms_net = 1e3 * (time.perf_counter() - t1) / ne
+        t1 = time.perf_counter()
+        Pte, teach_ev = ws.core_als(be_ev, [e[2] for e in ev], [e[3] for e in ev], teacher_sweeps, tol=teacher_tol)
+        ms_teacher = 1e3 * (time.perf_counter() - t1) / ne
+        be_ev.close()
         be1 = pkg.BatchEngine([(S, S, S)], [R], [1.0], device=device)
-        for s in range(args.c5_eval):
-            nrm, Qs, G, prop, ms_prop = prepare(eng, core_eng, 2_000_000 + s)
-            t1 = time.perf_counter()
-            (p1,), _ = ws.core_als(be1, [G], [prop], 1)
-            ms_p1 = 1e3 * (time.perf_counter() - t1)
-            t1 = time.perf_counter()
-            Cl = ws.learned_coefficients(net, [prop], [[a - b for a, b in zip(p1, prop)]])[0]
-            ms_net = 1e3 * (time.perf_counter() - t1)
-            t1 = time.perf_counter()
-            (pst,), _ = ws.core_als(be1, [G], [prop], teacher_sweeps, tol=teacher_tol)
-            ms_teacher = 1e3 * (time.perf_counter() - t1)
+        for s in range(ne):
+            nrm, Qs, G, prop, ms_prop = ev[s]
+            rng = np.random.default_rng(2_000_000 + s)  # the tensor again (the generator is seeded)
+            ws.synth_device(dims, R, float(rng.uniform(0, 0.8)), float(rng.uniform(10, 40)), rng, buf.data_ptr(),
+                            device=device)
+            eng.set_tensor_device(buf.data_ptr(), keepalive=buf)
             fb = pkg.random_factors(dims, R, np.random.default_rng(s))[0]
-            cand = {"proposal": (ws.lift(Qs, prop), ms_prop), "one_core_sweep": (ws.lift(Qs, p1), ms_prop + ms_p1),
-                    "learned": (ws.lift(Qs, Cl), ms_prop + ms_p1 + ms_net),
-                    "core_als": (ws.lift(Qs, pst), ms_prop + ms_teacher)}
+            cand = {"proposal": (ws.lift(Qs, prop), ms_prop),
+                    "one_core_sweep": (ws.lift(Qs, P1e[s]), ms_prop + ms_p1),
+                    "learned": (ws.lift(Qs, Cle[s]), ms_prop + ms_p1 + ms_net),
+                    "core_als": (ws.lift(Qs, Pte[s]), ms_prop + ms_teacher)}
             starts = {"random": (pkg.random_factors(dims, R, np.random.default_rng(3_000_000 + s))[0], 0.0)}
             for k, (F0, extra) in cand.items():
                 fallbacks += int(F0 is None and k == "learned")
@@ -774,8 +788,9 @@ def run_c5(args, pkg, device):
                 per = ms[k][0] / len(trajs[k])
                 res[k]["ms"].append(ms[k][1] + per * (n if n is not None else 101))
             if s < 32:
-                # end to end through the public API for the learned start: the tensor from pinned
-                # host memory, the start, ALS to the target's sweep count, the factors back
+                # end to end through the public API for the learned start, one tensor at a time:
+                # the tensor from pinned host memory, the start, ALS to the target's sweep count,
+                # the factors back
                 host = buf.cpu().pin_memory()
                 n_l = res["learned"]["sweeps"][-1]
                 torch.cuda.synchronize()
@@ -848,6 +863,10 @@ def run_c5(args, pkg, device):
                   "validation_mse_of_scaled_step": val_mse_step, "scaled_step_factor": a_ls,
                   "calibrated_step": scale,
                   "teacher_sweeps_p50": float(np.median(teacher_used)) if teacher_used else None},
+        "start_ms_per_tensor": {"sketch_core_proposal_p50": float(np.median([e[4] for e in ev])),
+                                "one_core_sweep_batched": ms_p1, "network_forward_batched": ms_net,
+                                "teacher_batched": ms_teacher,
+                                "teacher_sweeps_p50": float(np.median(teach_ev))},
     }
     print(json.dumps(line), flush=True)
 

@@ -219,14 +219,15 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         *abort_flag = 1;
       }
       int64_t fbm = (c_begin % p.nfb);  // the chunk's factor block, kept without a division per chunk
-      int g = 0;          // accumulation group
-      bool first = true;  // first chunk of group g
+      int g = 0;     // accumulation group
+      int gpos = 0;  // position of the chunk in its group
       for (int it = 0; it < nloc && !*abort_flag; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
         const int b = g % kBuf;
         const uint32_t uph = (uint32_t)((g / kBuf) & 1);
-        const bool last = (it + 1 == nloc) || ((fbm + 1) % p.grp == 0) || (fbm + 1 == p.nfb);
+        const bool first = gpos == 0;
+        const bool last = (it + 1 == nloc) || (gpos + 1 == p.grp) || (fbm + 1 == p.nfb);
         if (!mbar_wait(smem_u32(&full_a[s]), ph, abort_flag) ||
             (first && !mbar_wait(smem_u32(&acc_empty[b]), uph ^ 1u, abort_flag))) {
           atomicCAS(err, 0, 2);
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
           umma_commit(smem_u32(&acc_full[b]));
           ++g;
         }
-        first = last;
+        gpos = last ? 0 : gpos + 1;
       }
       umma_commit(smem_u32(done_bar));
     }
@@ -267,7 +268,8 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
     int64_t fbm = (c_begin % p.nfb);
     int g = 0, it0 = 0;  // accumulation group and its first chunk
     for (int it = 0; it < nloc && ok; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
-      if (!((it + 1 == nloc) || ((fbm + 1) % p.grp == 0) || (fbm + 1 == p.nfb))) continue;  // not a group's last chunk
+      // the issuer's grouping: p.grp chunks, cut where the outer index changes
+      if (!((it + 1 == nloc) || (it + 1 - it0 == p.grp) || (fbm + 1 == p.nfb))) continue;
       const int s = it % S;
       const int b = g % kBuf;
       const uint32_t uph = (uint32_t)((g / kBuf) & 1);

@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--c4-count", type=int, default=4096, help="c4: tensors in the batch")
     ap.add_argument("--c5-train", type=int, default=20000, help="c5: training decompositions")
     ap.add_argument("--c5-eval", type=int, default=512, help="c5: held-out tensors")
+    ap.add_argument("--c5-input-sweeps", type=int, default=1,
+                    help="c5: core ALS sweeps whose step D = P_k - P the network reads beside the proposal")
     ap.add_argument("--workload", choices=["c2", "c3", "c4", "c5", "qrcp"], default="c2",
                     help="c2: 512^3 rank 64 (the headline line); c3: 128^4 rank 128, dimension tree, "
                          "plain and randomized paths; c4: 4096 small decompositions, batched; qrcp: the "
@@ -702,7 +704,7 @@ def run_c5(args, pkg, device):
                     be_chunk.close()
                 be_chunk = pkg.BatchEngine([(S, S, S)] * nc, [R] * nc, [1.0] * nc, device=device)
             t1 = time.perf_counter()
-            P1, _ = ws.core_als(be_chunk, Gs, props, 1)
+            P1, _ = ws.core_als(be_chunk, Gs, props, args.c5_input_sweeps)
             Ps, sw = ws.core_als(be_chunk, Gs, props, teacher_sweeps, tol=teacher_tol)
             t_core += time.perf_counter() - t1
             teacher_used.extend(int(x) for x in sw)
@@ -749,7 +751,7 @@ def run_c5(args, pkg, device):
         ev = [prepare(eng, core_eng, 2_000_000 + s) for s in range(ne)]
         be_ev = pkg.BatchEngine([(S, S, S)] * ne, [R] * ne, [1.0] * ne, device=device)
         t1 = time.perf_counter()
-        P1e, _ = ws.core_als(be_ev, [e[2] for e in ev], [e[3] for e in ev], 1)
+        P1e, _ = ws.core_als(be_ev, [e[2] for e in ev], [e[3] for e in ev], args.c5_input_sweeps)
         ms_p1 = 1e3 * (time.perf_counter() - t1) / ne
         t1 = time.perf_counter()
         Cle = ws.learned_coefficients(net, [e[3] for e in ev],
@@ -801,7 +803,7 @@ def run_c5(args, pkg, device):
                 Qs2, _ = ws.sketch_bases(ws.sketch(eng, omegas))
                 G2 = ws.core(core_eng, Qs2)
                 prop2 = ws.jennrich(G2, R, np.random.default_rng(2_000_000 + s + 7))
-                (q1,), _ = ws.core_als(be1, [G2], [prop2], 1)
+                (q1,), _ = ws.core_als(be1, [G2], [prop2], args.c5_input_sweeps)
                 F2 = ws.lift(Qs2, ws.learned_coefficients(net, [prop2], [[a - b for a, b in zip(q1, prop2)]])[0])
                 eng.set_factors(F2 if F2 is not None else fb, np.ones(R))
                 eng.optimize(pkg.api._to_device_check(pkg.NoCheck(min(n_l, 100))))
@@ -841,6 +843,7 @@ def run_c5(args, pkg, device):
         "dtype": "mlp bf16/f32-accumulate (tcgen05); core als f32 mttkrp, f64 solve; als bf16x3 mttkrp, f64 solve",
         "data": "synthetic",
         "config": {"workload": "warm_start_256cube_rank32_sketch32", "train": n_train, "eval": args.c5_eval,
+                   "input_core_sweeps": args.c5_input_sweeps,
                    "mlp": [6 * S * R, 512, 512, S * R], "teacher": f"core ALS FitCheck({teacher_tol}, {teacher_sweeps})"},
         "c5": out, "fallbacks": fallbacks,
         "gain_vs_random_p50": out["random"]["sweeps_p50"] / max(out["learned"]["sweeps_p50"], 1e-9),

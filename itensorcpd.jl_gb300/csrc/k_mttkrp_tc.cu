@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
   const int64_t c_begin = (int64_t)split * p.chunks_per_split;
   const int64_t c_end = min(p.nchunks, c_begin + p.chunks_per_split);
   const int nloc = (c_end > c_begin) ? (int)(c_end - c_begin) : 0;
+  const int nfb = (int)p.nfb;  // factor blocks of the fastest reduction mode (a few)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -218,16 +219,16 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         atomicCAS(err, 0, 2);
         *abort_flag = 1;
       }
-      int64_t fbm = (c_begin % p.nfb);  // the chunk's factor block, kept without a division per chunk
+      int fbm = (int)(c_begin % p.nfb);  // the chunk's factor block, kept without a division per chunk
       int g = 0;     // accumulation group
       int gpos = 0;  // position of the chunk in its group
-      for (int it = 0; it < nloc && !*abort_flag; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
+      for (int it = 0; it < nloc && !*abort_flag; ++it, fbm = (fbm + 1 == nfb) ? 0 : fbm + 1) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
         const int b = g % kBuf;
         const uint32_t uph = (uint32_t)((g / kBuf) & 1);
         const bool first = gpos == 0;
-        const bool last = (it + 1 == nloc) || (gpos + 1 == p.grp) || (fbm + 1 == p.nfb);
+        const bool last = (it + 1 == nloc) || (gpos + 1 == p.grp) || (fbm + 1 == nfb);
         if (!mbar_wait(smem_u32(&full_a[s]), ph, abort_flag) ||
             (first && !mbar_wait(smem_u32(&acc_empty[b]), uph ^ 1u, abort_flag))) {
           atomicCAS(err, 0, 2);
@@ -261,15 +262,16 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
     const int q = warp & 3;  // this warp's TMEM lane quarter
     const int cb = ((warp - 2) >> 2) * NH;  // first column of this warp
     const int64_t row = (int64_t)mblk * kBlockM + q * 32 + lane;
+    float* sw = reinterpret_cast<float*>(ctl + 256) + (warp - 2) * NH;  // this warp's scale slice
     float acc[NH];
 #pragma unroll
     for (int j = 0; j < NH; ++j) acc[j] = 0.0f;
     bool ok = true;
-    int64_t fbm = (c_begin % p.nfb);
+    int fbm = (int)(c_begin % p.nfb);
     int g = 0, it0 = 0;  // accumulation group and its first chunk
-    for (int it = 0; it < nloc && ok; ++it, fbm = (fbm + 1 == p.nfb) ? 0 : fbm + 1) {
+    for (int it = 0; it < nloc && ok; ++it, fbm = (fbm + 1 == nfb) ? 0 : fbm + 1) {
       // the issuer's grouping: p.grp chunks, cut where the outer index changes
-      if (!((it + 1 == nloc) || (it + 1 - it0 == p.grp) || (fbm + 1 == p.nfb))) continue;
+      if (!((it + 1 == nloc) || (it + 1 - it0 == p.grp) || (fbm + 1 == nfb))) continue;
       const int s = it % S;
       const int b = g % kBuf;
       const uint32_t uph = (uint32_t)((g / kBuf) & 1);
@@ -285,11 +287,20 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         break;
       }
       tc_fence_after();
-      // the group's earlier stages are free: their MMAs have completed, and the outer rows
-      // (one outer index per group) are read from the last chunk's stage
-      if (lane == 0)
-        for (int j = it0; j < it; ++j) mbar_arrive(smem_u32(&empty[j % S]));
-      const float* orow = reinterpret_cast<const float*>(outer_rows(s)) + cb;
+      // s(r), the product of the outer factor rows in mode order (one outer index per group),
+      // for this warp's columns into its own shared slice, two columns per lane; then every
+      // stage of the group is free: its MMAs have completed and its outer rows are read
+      {
+        const float* orow = reinterpret_cast<const float*>(outer_rows(s)) + cb;
+        for (int j = lane; j < NH; j += 32) {
+          float v = 1.0f;
+          for (int jo = 0; jo < p.n_outer; ++jo) v *= orow[jo * NB + j];
+          sw[j] = v;
+        }
+        __syncwarp();
+        if (lane == 0)
+          for (int j = it0; j <= it; ++j) mbar_arrive(smem_u32(&empty[j % S]));
+      }
       const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
       // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
       // budget is smaller: 320 threads)
@@ -305,33 +316,21 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
           tmem_ld16_nowait(base + (uint32_t)c0, vh);
           tmem_ld16_nowait(base + (uint32_t)(NB + c0), vl);
         }
-        float sc[W];
-#pragma unroll
-        for (int j = 0; j < W; ++j) sc[j] = 1.0f;
-        for (int jo = 0; jo < p.n_outer; ++jo) {
-#pragma unroll
-          for (int j = 0; j < W; j += 4) {
-            if (c0 + j < NH) {
-              const float4 o4 = *reinterpret_cast<const float4*>(orow + jo * NB + c0 + j);
-              sc[j] *= o4.x;
-              sc[j + 1] *= o4.y;
-              sc[j + 2] *= o4.z;
-              sc[j + 3] *= o4.w;
-            }
-          }
-        }
         tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < W; ++j)
-          if (c0 + j < NH)
-            acc[c0 + j] = fmaf(sc[j], __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
+        for (int j = 0; j < W; j += 4) {
+          if (c0 + j < NH) {
+            const float4 v4 = *reinterpret_cast<const float4*>(sw + c0 + j);  // broadcast read
+            acc[c0 + j] = fmaf(v4.x, __uint_as_float(vh[j]) + __uint_as_float(vl[j]), acc[c0 + j]);
+            acc[c0 + j + 1] = fmaf(v4.y, __uint_as_float(vh[j + 1]) + __uint_as_float(vl[j + 1]), acc[c0 + j + 1]);
+            acc[c0 + j + 2] = fmaf(v4.z, __uint_as_float(vh[j + 2]) + __uint_as_float(vl[j + 2]), acc[c0 + j + 2]);
+            acc[c0 + j + 3] = fmaf(v4.w, __uint_as_float(vh[j + 3]) + __uint_as_float(vl[j + 3]), acc[c0 + j + 3]);
+          }
+        }
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) {
-        mbar_arrive(smem_u32(&acc_empty[b]));
-        mbar_arrive(smem_u32(&empty[s]));
-      }
+      if (lane == 0) mbar_arrive(smem_u32(&acc_empty[b]));
       ++g;
       it0 = it + 1;
     }
@@ -531,7 +530,7 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     // stages the unfolding bytes in flight drop, and the kernel is bound by them (at 512^3
     // R = 64, resident tiles with three stages took 120 us a launch against 110 us with four
     // stages of A + B).  Otherwise each stage is A hi | A lo | B hi | B lo | outer rows.
-    const size_t ctl_bytes = 1024 + 256;  // alignment slack + barriers and flags
+    const size_t ctl_bytes = 1024 + 256 + 16 * (size_t)nb;  // alignment slack, barriers and flags, drain scales
     const size_t a2 = (size_t)2 * kBlockM * kChunk * 2;
     const size_t b2 = (size_t)2 * nb * kChunk * 2;
     const size_t ob = (size_t)round_up((int64_t)p.n_outer * nb * 4, 16);

@@ -548,14 +548,16 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // is the composition of the single-index sweeps over P; after every block A = -V^{-1}.  The
 // indices are swept in blocks of 32 in their natural order (V is symmetric positive definite
 // whenever this path is taken; any pivot order is sound because the solve refines X):
-//   (a) warp 0 sweeps D in registers (lane i holds row i), one index at a time; the pivot
-//       row reaches the lanes by shuffles, and per-lane selects replace a branch on lane == k;
+//   (a) warps 0-3 sweep D in registers (lane i holds row i, eight columns per warp), one
+//       index at a time; the pivot row reaches the lanes through shared memory, one named
+//       barrier per index, and per-lane selects replace a branch on lane == k;
 //   (b) all warps form B = A_{.P} D^{-1} and keep A_{.P} (both transposed, 32 x R);
 //   (c) all warps apply the rank-32 update to the rest of A in 4 x 4 register tiles and write
 //       the swept blocks back.
 // That is three barriers per block (twelve at R = 128) instead of two per index.
 constexpr int FT32 = 512;
 constexpr int kBlk32 = 32;
+constexpr int kSweepWarps = 4;  // warps sweeping the diagonal block (eight columns each)
 // The refinement's FP32 operands, written by the FP32 sweep into the workspace after the
 // FP64 factorisation's area: [W | V_hi | V_lo], each R^2 floats padded to a multiple of four
 // (16-byte aligned, so the solve stages them with 16-byte asynchronous copies).  V = V_hi +
@@ -567,7 +569,7 @@ __host__ __device__ inline size_t ops32_offset_doubles(int R) {
 __host__ __device__ inline int ld32(int R) { return ((R + 3) & ~3) + 4; }  // row stride of A, B^T, C^T
 __host__ __device__ inline size_t factorize32_smem_bytes(int R) {
   const int ld = ld32(R);
-  return sizeof(float) * ((size_t)R * ld + 2 * (size_t)kBlk32 * ld + (size_t)kBlk32 * 33 + 64);
+  return sizeof(float) * ((size_t)R * ld + 2 * (size_t)kBlk32 * ld + (size_t)kBlk32 * 33 + 96);
 }
 // V = Hadamard product of the other modes' Grams (FP64, in mode order, as the FP64 sweep
 // forms it), written as the FP32 pair V_hi + V_lo into the refinement operands.  One
@@ -594,7 +596,7 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
   float* Bt = A + (size_t)R * ld;            // 32 x ld: B^T, row p = column p of B = A_{.P} D^{-1}
   float* Ct = Bt + (size_t)kBlk32 * ld;      // 32 x ld: A_{.P}^T before the block
   float* Dm = Ct + (size_t)kBlk32 * ld;      // 32 x 33: the diagonal block, swept in place
-  float* misc = Dm + kBlk32 * 33;            // [0]: pivot threshold, [1]: failure flag
+  float* misc = Dm + kBlk32 * 33;            // [0]: pivot threshold, [1]: failure flag, [32, 96): pivot rows
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
   const float* __restrict__ Vh = ops + rr4(R);  // V_hi from k_form_v32
   const int Rp = (R + 3) & ~3;
@@ -616,29 +618,35 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
   const int ntile = Rp / 4;
   for (int p0 = 0; p0 < R; p0 += kBlk32) {
     const int pb = min(kBlk32, R - p0);
-    // (a) sweep of the diagonal block D = A_PP by warp 0: lane i holds row i in registers.
-    // Per pivot k, lane k publishes its row in shared memory; every lane reads it back (eight
-    // broadcast 16-byte loads) and takes D(i, k) as D(k, i), the sweep keeping the block
-    // symmetric.  Column k is set by an unrolled select (no dynamically indexed registers).
-    if (warp == 0) {
-      float* prow = misc + 32;  // the pivot row (16-byte aligned)
-      float r[kBlk32];
+    // (a) sweep of the diagonal block D = A_PP by warps 0-3: lane i of warp w holds row i,
+    // columns 8w .. 8w+7, in registers.  Per pivot k, lane k of each warp publishes its
+    // eight entries of row k in shared memory (two buffers, alternating), one named barrier
+    // over the four warps, then every lane reads row k back (broadcast loads) and takes
+    // D(i, k) as D(k, i), the sweep keeping the block symmetric.  Column k is set by an
+    // unrolled select (no dynamically indexed registers).
+    if (warp < kSweepWarps) {
+      constexpr int CW = kBlk32 / kSweepWarps;  // columns per warp
+      const int c0 = warp * CW;
+      float r[CW];
 #pragma unroll
-      for (int c = 0; c < kBlk32; ++c) r[c] = (lane < pb && c < pb) ? A[(size_t)(p0 + lane) * ld + p0 + c] : 0.f;
+      for (int c = 0; c < CW; ++c)
+        r[c] = (lane < pb && c0 + c < pb) ? A[(size_t)(p0 + lane) * ld + p0 + c0 + c] : 0.f;
       const float thr = misc[0];
       bool bad = false;
       for (int k = 0; k < pb; ++k) {
+        float* prow = misc + 32 * (1 + (k & 1));  // 16-byte aligned, two buffers
         const bool me = (lane == k);
         if (me) {
 #pragma unroll
-          for (int v = 0; v < kBlk32 / 4; ++v)
-            reinterpret_cast<float4*>(prow)[v] = make_float4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]);
+          for (int v = 0; v < CW / 4; ++v)
+            reinterpret_cast<float4*>(prow + c0)[v] = make_float4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]);
         }
         __syncwarp();
-        float rk[kBlk32];
+        asm volatile("barrier.sync 1, %0;" ::"n"(kSweepWarps * 32) : "memory");
+        float rk[CW];
 #pragma unroll
-        for (int v = 0; v < kBlk32 / 4; ++v) {
-          const float4 x = reinterpret_cast<const float4*>(prow)[v];
+        for (int v = 0; v < CW / 4; ++v) {
+          const float4 x = reinterpret_cast<const float4*>(prow + c0)[v];
           rk[4 * v] = x.x;
           rk[4 * v + 1] = x.y;
           rk[4 * v + 2] = x.z;
@@ -646,22 +654,21 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
         }
         const float dik = prow[lane];
         const float d = prow[k];
-        __syncwarp();  // the row is read before the next pivot overwrites it
         bad = bad || !(d > thr) || !(d < INFINITY);
         const float rd = __frcp_rn(d);
         const float f = dik * rd;
         const float pk = me ? -rd : f;
 #pragma unroll
-        for (int c = 0; c < kBlk32; ++c) {
+        for (int c = 0; c < CW; ++c) {
           const float v = me ? rk[c] * rd : fmaf(-f, rk[c], r[c]);
-          r[c] = (c == k) ? pk : v;
+          r[c] = (c0 + c == k) ? pk : v;
         }
       }
       if (lane < pb) {
 #pragma unroll
-        for (int c = 0; c < kBlk32; ++c) Dm[lane * 33 + c] = r[c];
+        for (int c = 0; c < CW; ++c) Dm[lane * 33 + c0 + c] = r[c];
       }
-      if (lane == 0 && bad) misc[1] = 1.f;
+      if (warp == 0 && lane == 0 && bad) misc[1] = 1.f;
     }
     __syncthreads();
     if (misc[1] != 0.f) break;

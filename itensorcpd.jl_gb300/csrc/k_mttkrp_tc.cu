@@ -315,12 +315,15 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
       const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
       // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
       // budget is smaller: 320 threads)
-      constexpr int W = (tc_drain_warps<NB>() == 8) ? 16 : 32;
+      constexpr int W = (NB == 128) ? 8 : (tc_drain_warps<NB>() == 8) ? 16 : 32;
 #pragma unroll
       for (int c0 = 0; c0 < NH; c0 += W) {
         uint32_t vh[W], vl[W];
         const bool full = (W == 32) && (c0 + 32 <= NH);
-        if (full) {
+        if constexpr (W == 8) {
+          tmem_ld8_nowait(base + (uint32_t)c0, vh);
+          tmem_ld8_nowait(base + (uint32_t)(NB + c0), vl);
+        } else if (full) {
           tmem_ld32_nowait(base + (uint32_t)c0, vh);
           tmem_ld32_nowait(base + (uint32_t)(NB + c0), vl);
         } else {

@@ -552,8 +552,8 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 //       index at a time; the pivot row reaches the lanes through shared memory, one named
 //       barrier per index, and per-lane selects replace a branch on lane == k;
 //   (b) all warps form B = A_{.P} D^{-1} and keep A_{.P} (both transposed, 32 x R);
-//   (c) all warps apply the rank-32 update to the rest of A in 4 x 4 register tiles and write
-//       the swept blocks back.
+//   (c) all warps apply the rank-32 update to the upper half of the rest of A in 4 x 4
+//       register tiles, each written with its mirror, and write the swept blocks back.
 // That is three barriers per block (twelve at R = 128) instead of two per index.
 constexpr int FT32 = 512;
 constexpr int kBlk32 = 32;
@@ -680,74 +680,100 @@ __global__ void __launch_bounds__(FT32) k_factorize32(int R, float* __restrict__
       for (int pp = 0; pp < kBlk32; ++pp) dcol[pp] = (lane < pb && pp < pb) ? -Dm[pp * 33 + lane] : 0.f;
       for (int i = warp; i < R; i += nt >> 5) {
         const float4* ai = reinterpret_cast<const float4*>(A + (size_t)i * ld + p0);
-        float b = 0.f;
+        float b4[4] = {0.f, 0.f, 0.f, 0.f};  // four independent partial sums: a short dependent chain
 #pragma unroll
         for (int v = 0; v < kBlk32 / 4; ++v) {
           const float4 x = ai[v];
-          b = fmaf(x.x, dcol[4 * v], b);
-          b = fmaf(x.y, dcol[4 * v + 1], b);
-          b = fmaf(x.z, dcol[4 * v + 2], b);
-          b = fmaf(x.w, dcol[4 * v + 3], b);
+          b4[0] = fmaf(x.x, dcol[4 * v], b4[0]);
+          b4[1] = fmaf(x.y, dcol[4 * v + 1], b4[1]);
+          b4[2] = fmaf(x.z, dcol[4 * v + 2], b4[2]);
+          b4[3] = fmaf(x.w, dcol[4 * v + 3], b4[3]);
         }
-        Bt[(size_t)lane * ld + i] = b;
+        Bt[(size_t)lane * ld + i] = (b4[0] + b4[1]) + (b4[2] + b4[3]);
         Ct[(size_t)lane * ld + i] = (lane < pb) ? A[(size_t)i * ld + p0 + lane] : 0.f;
       }
     }
     __syncthreads();
-    // (c) the rank-pb update of the rest, and the swept blocks written back, in 4 x 4 tiles
-    // (tiles never straddle the block: it starts at a multiple of 32)
-    for (int t = tid; t < ntile * ntile; t += nt) {
-      const int ti = t / ntile, tj = t - ti * ntile;
-      const int i0 = 4 * ti, j0 = 4 * tj;
-      const bool inI = (i0 >= p0 && i0 < p0 + pb), inJ = (j0 >= p0 && j0 < p0 + pb);
-      float v[4][4];
-      if (inI && inJ) {
+    // (c) the rank-pb update of the rest and the swept blocks written back, in 4 x 4 tiles
+    // (tiles never straddle the block: it starts at a multiple of 32).  The matrix stays
+    // symmetric, so only tiles (ti <= tj) outside the block's tile range P are computed, each
+    // written with its mirror; the P row strip (the swept block and A_Pj = B_j^T) is written
+    // with its mirror too.  Work items: the rank-pb update tiles first, then the strip's
+    // copies, so that no thread takes two update tiles at R = 128.
+    {
+      const int tp0 = p0 / 4, npt = (pb + 3) / 4;
+      const int m = ntile - npt;                    // tiles outside P, in each direction
+      const int nexp = m * (m + 1) / 2, ncopy = npt * ntile;
+      for (int u = tid; u < nexp + ncopy; u += nt) {
+        float v[4][4];
+        int i0, j0;
+        bool mirror;
+        if (u < nexp) {  // A_ij - sum_p B(i, p) C(j, p), ti <= tj, both outside P
+          int a = 0, rem = u, len = m;
+          while (rem >= len) {
+            rem -= len;
+            ++a;
+            --len;
+          }
+          const int bb = a + rem;
+          const int ti = a < tp0 ? a : a + npt, tj = bb < tp0 ? bb : bb + npt;
+          i0 = 4 * ti;
+          j0 = 4 * tj;
+          mirror = ti != tj;
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+          for (int r4 = 0; r4 < 4; ++r4) {
+            const float4 x = *reinterpret_cast<const float4*>(A + (size_t)(i0 + r4) * ld + j0);
+            v[r4][0] = x.x;
+            v[r4][1] = x.y;
+            v[r4][2] = x.z;
+            v[r4][3] = x.w;
+          }
+          for (int pp = 0; pp < pb; ++pp) {
+            const float4 bi = *reinterpret_cast<const float4*>(Bt + (size_t)pp * ld + i0);
+            const float4 cj = *reinterpret_cast<const float4*>(Ct + (size_t)pp * ld + j0);
+            const float bv[4] = {bi.x, bi.y, bi.z, bi.w}, cv[4] = {cj.x, cj.y, cj.z, cj.w};
 #pragma unroll
-          for (int b = 0; b < 4; ++b)
-            v[a][b] = (i0 + a < p0 + pb && j0 + b < p0 + pb) ? Dm[(i0 + a - p0) * 33 + (j0 + b - p0)] : 0.f;
-      } else if (inI) {  // A_Pj = B_j^T
+            for (int r4 = 0; r4 < 4; ++r4)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const float4 x = *reinterpret_cast<const float4*>(Bt + (size_t)(i0 + a - p0) * ld + j0);
-          v[a][0] = x.x;
-          v[a][1] = x.y;
-          v[a][2] = x.z;
-          v[a][3] = x.w;
+              for (int c4 = 0; c4 < 4; ++c4) v[r4][c4] = fmaf(-bv[r4], cv[c4], v[r4][c4]);
+          }
+        } else {  // the P row strip: tile (tp0 + e / ntile, e % ntile)
+          const int e = u - nexp;
+          const int ti = tp0 + e / ntile, tj = e - (e / ntile) * ntile;
+          i0 = 4 * ti;
+          j0 = 4 * tj;
+          const bool inJ = (j0 >= p0 && j0 < p0 + pb);
+          mirror = !inJ;
+          if (inJ) {  // the swept block: -D^{-1}
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4)
+#pragma unroll
+              for (int c4 = 0; c4 < 4; ++c4)
+                v[r4][c4] = (i0 + r4 < p0 + pb && j0 + c4 < p0 + pb) ? Dm[(i0 + r4 - p0) * 33 + (j0 + c4 - p0)] : 0.f;
+          } else {  // A_Pj = B_j^T (its mirror A_jP = B_j)
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4) {
+              const float4 x = *reinterpret_cast<const float4*>(Bt + (size_t)(i0 + r4 - p0) * ld + j0);
+              v[r4][0] = x.x;
+              v[r4][1] = x.y;
+              v[r4][2] = x.z;
+              v[r4][3] = x.w;
+            }
+          }
         }
-      } else if (inJ) {  // A_iP = B_i
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const float4 x = *reinterpret_cast<const float4*>(Bt + (size_t)(j0 + b - p0) * ld + i0);
-          v[0][b] = x.x;
-          v[1][b] = x.y;
-          v[2][b] = x.z;
-          v[3][b] = x.w;
-        }
-      } else {  // A_ij - sum_p B(i, p) C(j, p)
+        for (int r4 = 0; r4 < 4; ++r4)
+          if (i0 + r4 < R)
+            *reinterpret_cast<float4*>(A + (size_t)(i0 + r4) * ld + j0) =
+                make_float4(v[r4][0], v[r4][1], v[r4][2], v[r4][3]);
+        if (mirror) {
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const float4 x = *reinterpret_cast<const float4*>(A + (size_t)(i0 + a) * ld + j0);
-          v[a][0] = x.x;
-          v[a][1] = x.y;
-          v[a][2] = x.z;
-          v[a][3] = x.w;
-        }
-        for (int pp = 0; pp < pb; ++pp) {
-          const float4 bi = *reinterpret_cast<const float4*>(Bt + (size_t)pp * ld + i0);
-          const float4 cj = *reinterpret_cast<const float4*>(Ct + (size_t)pp * ld + j0);
-          const float bv[4] = {bi.x, bi.y, bi.z, bi.w}, cv[4] = {cj.x, cj.y, cj.z, cj.w};
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) v[a][b] = fmaf(-bv[a], cv[b], v[a][b]);
+          for (int c4 = 0; c4 < 4; ++c4)
+            if (j0 + c4 < R)
+              *reinterpret_cast<float4*>(A + (size_t)(j0 + c4) * ld + i0) =
+                  make_float4(v[0][c4], v[1][c4], v[2][c4], v[3][c4]);
         }
       }
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-        if (i0 + a < R) *reinterpret_cast<float4*>(A + (size_t)(i0 + a) * ld + j0) =
-            make_float4(v[a][0], v[a][1], v[a][2], v[a][3]);
     }
     __syncthreads();
   }

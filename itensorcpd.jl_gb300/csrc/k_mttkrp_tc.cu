@@ -55,9 +55,6 @@ __host__ __device__ constexpr int tc_drain_warps() { return (NB % 64 == 0) ? 8 :
 template <int NB>
 __host__ __device__ constexpr int tc_threads() { return 64 + 32 * tc_drain_warps<NB>(); }
 constexpr size_t kSmemLimit = 227 * 1024;
-// Outer-row slots when the factor-block tiles are resident: the rows get their own ring,
-// released by the drain, so that an unfolding stage is released by the MMA commit alone.
-constexpr int kOrowSlots = 8;
 
 struct TcModePlan {
   int mode, fmode, n_outer, m_blocks, n_blocks, splits, stages, nb, tmem_cols, rpad;
@@ -120,15 +117,13 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
   uint64_t* bres_bar = done_bar + 1;                     // resident B tiles landed
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bres_bar + 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bres_bar + 2);
-  uint64_t* orow_empty = reinterpret_cast<uint64_t*>(ctl + 168);  // [kOrowSlots] outer rows read (resident mode)
   // where stage s keeps its unfolding tile, the B tile of chunk fb, and its outer rows
   auto stage_a = [&](int s) { return smem + (size_t)s * stage_bytes; };
   auto b_tile = [&](int s, int64_t fb) {
     return bres ? smem + p.bres_off + (size_t)fb * (2 * b_bytes) : stage_a(s) + 2 * a_bytes;
   };
-  // outer rows of chunk it (in stage s): its own slot in resident mode, else in the stage
-  auto outer_rows = [&](int s, int it) {
-    return bres ? smem + p.orow_off + (size_t)(it % kOrowSlots) * p.obytes : stage_a(s) + 2 * a_bytes + 2 * b_bytes;
+  auto outer_rows = [&](int s) {
+    return bres ? smem + p.orow_off + (size_t)s * p.obytes : stage_a(s) + 2 * a_bytes + 2 * b_bytes;
   };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -144,10 +139,8 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(smem_u32(&full_a[s]), 1);
-      // resident mode: the MMA commit frees a stage; otherwise the drain (B tile and outer rows)
-      mbar_init(smem_u32(&empty[s]), bres ? 1 : tc_drain_warps<NB>());
+      mbar_init(smem_u32(&empty[s]), tc_drain_warps<NB>());
     }
-    for (int j = 0; j < kOrowSlots; ++j) mbar_init(smem_u32(&orow_empty[j]), tc_drain_warps<NB>());
     for (int b = 0; b < kBuf; ++b) {
       mbar_init(smem_u32(&acc_full[b]), 1);
       mbar_init(smem_u32(&acc_empty[b]), tc_drain_warps<NB>());
@@ -184,9 +177,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
       for (int it = 0; it < nloc; ++it) {
         const int s = it % S;
         const uint32_t ph = (uint32_t)((it / S) & 1);
-        if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag) ||
-            (bres && !mbar_wait(smem_u32(&orow_empty[it % kOrowSlots]), (uint32_t)(((it / kOrowSlots) & 1) ^ 1),
-                                abort_flag))) {
+        if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag)) {
           atomicCAS(err, 0, 1);
           *abort_flag = 1;
           break;
@@ -201,7 +192,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         if (!bres)
           bulk_load(smem_u32(st + 2 * a_bytes), btiles + ((size_t)fb * p.n_blocks + nblk) * (2 * b_bytes),
                     2 * b_bytes, bar);
-        uint8_t* orow = outer_rows(s, it);
+        uint8_t* orow = outer_rows(s);
         for (int j = 0; j < p.n_outer; ++j) {
           const int64_t id = o % p.outer_dims[j];
           o /= p.outer_dims[j];
@@ -255,7 +246,6 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
           umma_bf16(acc_h, dah, dbh, idesc_w, (first && kk == 0) ? 0u : 1u);  // [Th Bh | Th Bl]
           umma_bf16(acc_l, dal, dbh, idesc_n, 1u);                           // += Tl Bh
         }
-        if (bres) umma_commit(smem_u32(&empty[s]));  // the stage is free once these MMAs have read it
         if (last) {
           umma_commit(smem_u32(&acc_full[b]));
           ++g;
@@ -301,7 +291,7 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
       // for this warp's columns into its own shared slice, two columns per lane; then every
       // stage of the group is free: its MMAs have completed and its outer rows are read
       {
-        const float* orow = reinterpret_cast<const float*>(outer_rows(s, it)) + cb;
+        const float* orow = reinterpret_cast<const float*>(outer_rows(s)) + cb;
         for (int j = lane; j < NH; j += 32) {
           float v = 1.0f;
           for (int jo = 0; jo < p.n_outer; ++jo) v *= orow[jo * NB + j];
@@ -309,21 +299,17 @@ __global__ void __launch_bounds__(tc_threads<NBT>(), 1)
         }
         __syncwarp();
         if (lane == 0)
-          for (int j = it0; j <= it; ++j)
-            mbar_arrive(smem_u32(bres ? &orow_empty[j % kOrowSlots] : &empty[j % S]));
+          for (int j = it0; j <= it; ++j) mbar_arrive(smem_u32(&empty[j % S]));
       }
       const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kAcc * NB + cb);
       // 32 columns per TMEM load, or 16 with two drain warps per quarter (their register
       // budget is smaller: 320 threads)
-      constexpr int W = (NB == 128) ? 8 : (tc_drain_warps<NB>() == 8) ? 16 : 32;
+      constexpr int W = (tc_drain_warps<NB>() == 8) ? 16 : 32;
 #pragma unroll
       for (int c0 = 0; c0 < NH; c0 += W) {
         uint32_t vh[W], vl[W];
         const bool full = (W == 32) && (c0 + 32 <= NH);
-        if constexpr (W == 8) {
-          tmem_ld8_nowait(base + (uint32_t)c0, vh);
-          tmem_ld8_nowait(base + (uint32_t)(NB + c0), vl);
-        } else if (full) {
+        if (full) {
           tmem_ld32_nowait(base + (uint32_t)c0, vh);
           tmem_ld32_nowait(base + (uint32_t)(NB + c0), vl);
         } else {
@@ -549,8 +535,7 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     const size_t b2 = (size_t)2 * nb * kChunk * 2;
     const size_t ob = (size_t)round_up((int64_t)p.n_outer * nb * 4, 16);
     const size_t bres_bytes = (size_t)p.nfb * b2;
-    const size_t orow_bytes = (size_t)kOrowSlots * ob;
-    const size_t room = (kSmemLimit > ctl_bytes + bres_bytes + orow_bytes) ? kSmemLimit - ctl_bytes - bres_bytes - orow_bytes : 0;
+    const size_t room = (kSmemLimit > ctl_bytes + bres_bytes + 4 * ob) ? kSmemLimit - ctl_bytes - bres_bytes - 4 * ob : 0;
     const int res_stages = (int)std::min<size_t>(4, room / a2);
     if (res_stages >= 4) {
       p.bres = 1;
@@ -559,7 +544,7 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
       p.bres_off = (uint32_t)(p.stages * a2);
       p.orow_off = p.bres_off + (uint32_t)bres_bytes;
       p.obytes = (uint32_t)ob;
-      p.ctl_off = p.orow_off + (uint32_t)orow_bytes;
+      p.ctl_off = p.orow_off + (uint32_t)(p.stages * ob);
     } else {
       const size_t sb = a2 + b2 + (size_t)p.n_outer * nb * 4;
       p.bres = 0;

@@ -874,11 +874,18 @@ __device__ __forceinline__ void solve_rows_body(const PT* __restrict__ part, int
           sacc = tt;
         }
       }
-      for (; sp < S; ++sp) {
-        const float p = part[(int64_t)sp * sstride + base + e];
-        const float tt = sacc + p;
-        cacc += (fabsf(sacc) >= fabsf(p)) ? ((sacc - tt) + p) : ((p - tt) + sacc);
-        sacc = tt;
+      if (sp < S) {  // the last (< 16) splits, their loads in flight together
+        float v[16];
+#pragma unroll
+        for (int t = 0; t < 16; ++t) v[t] = (sp + t < S) ? part[(int64_t)(sp + t) * sstride + base + e] : 0.0f;
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          if (sp + t < S) {
+            const float tt = sacc + v[t];
+            cacc += (fabsf(sacc) >= fabsf(v[t])) ? ((sacc - tt) + v[t]) : ((v[t] - tt) + sacc);
+            sacc = tt;
+          }
+        }
       }
       Ms[e] = (double)sacc + (double)cacc;
     } else {
@@ -1629,7 +1636,14 @@ __global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
     const int e = eb + lane;
     double acc = 0.0;
     if (e < e1)
-      for (int b = sl; b < nblk; b += 8) acc += __ldcg(&a.gpart[(size_t)b * T + e]);
+      for (int b0 = sl; b0 < nblk; b0 += 64) {  // eight loads in flight, added in block order
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = (b0 + 8 * q < nblk) ? __ldcg(&a.gpart[(size_t)(b0 + 8 * q) * T + e]) : 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (b0 + 8 * q < nblk) acc += v[q];
+      }
     red[sl][lane] = acc;
     __syncthreads();
     if (sl == 0 && e < e1) {

@@ -1060,19 +1060,6 @@ __global__ void __launch_bounds__(SOLVE_T) k_solve_gemm(const PT* __restrict__ p
 }
 
 // ---------------- gram + finalize ----------------
-// Warp-level sum as a tree (deterministic), then across the warps of the block.
-__device__ double block_tree_sum(double v, double* sv) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  __syncthreads();
-  if (lane == 0) sv[w] = v;
-  __syncthreads();
-  double t = (lane < nw) ? sv[lane] : 0.0;
-  for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-  __syncthreads();
-  return t;
-}
-
 // Block-wide helpers for the exact fixed-point sums: the largest int, and the sum of the
 // threads' 128-bit values (every thread gets both).
 __device__ int block_max_int(int v, int* si) {  // si: 32 ints
@@ -1215,7 +1202,6 @@ struct FinalizeArgs {
 __device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam);
 
 __device__ void finalize_body(const double* __restrict__ Graw, int R, const FinalizeArgs& fa, bool coherent) {
-  __shared__ double sv[32];
   __shared__ double s_lam[CPALS_MAX_RANK_SOLVE];
   __shared__ double s_inv[CPALS_MAX_RANK_SOLVE];
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -1261,16 +1247,35 @@ __device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam) {
   __shared__ long long sl[64];
   // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28): the rows' exact
   // fixed-point sums, aligned to the largest row base (+8: room for 2^36 rows) and added
+  // (each thread's first kKeep rows are read once, their loads in flight together, and kept
+  // for the sum; any further rows are read twice)
+  constexpr int kKeep = 4;
   const long long* ir = fa.inner_rows_fx;
+  long long klo[kKeep], khi[kKeep];
+  int kb[kKeep];
+#pragma unroll
+  for (int j = 0; j < kKeep; ++j) {
+    const int64_t i = tid + (int64_t)j * nt;
+    const bool in = i < fa.In;
+    klo[j] = in ? __ldcg(&ir[3 * i]) : 0;
+    khi[j] = in ? __ldcg(&ir[3 * i + 1]) : 0;
+    kb[j] = in ? (int)__ldcg(&ir[3 * i + 2]) : INT_MIN;
+  }
   int bmax = INT_MIN;
-  for (int64_t i = tid; i < fa.In; i += nt) bmax = max(bmax, (int)__ldcg(&ir[3 * i + 2]));
+#pragma unroll
+  for (int j = 0; j < kKeep; ++j) bmax = max(bmax, kb[j]);
+  for (int64_t i = tid + (int64_t)kKeep * nt; i < fa.In; i += nt) bmax = max(bmax, (int)__ldcg(&ir[3 * i + 2]));
   bmax = block_max_int(bmax, si);
   const int ib = (bmax == kFxBad) ? kFxBad : bmax + 8;
   __int128 qi = 0;
-  if (ib != kFxBad)
-    for (int64_t i = tid; i < fa.In; i += nt)
+  if (ib != kFxBad) {
+#pragma unroll
+    for (int j = 0; j < kKeep; ++j)
+      if (tid + (int64_t)j * nt < fa.In) qi += fx_align(fx_join((unsigned long long)klo[j], khi[j]), kb[j], ib);
+    for (int64_t i = tid + (int64_t)kKeep * nt; i < fa.In; i += nt)
       qi += fx_align(fx_join((unsigned long long)__ldcg(&ir[3 * i]), __ldcg(&ir[3 * i + 1])), (int)__ldcg(&ir[3 * i + 2]),
                      ib);
+  }
   const __int128 inner = block_sum_fx(qi, sl);
   // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11): with the per-tile
   // (per-block) shares of the fused path, their exact sums; otherwise each term formed here
@@ -1278,14 +1283,28 @@ __device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam) {
   __int128 qf = 0;
   if (fa.fpart) {
     const long long* fp = reinterpret_cast<const long long*>(fa.fpart);
+#pragma unroll
+    for (int j = 0; j < kKeep; ++j) {
+      const int t = tid + j * nt;
+      const bool in = t < fa.ntiles;
+      klo[j] = in ? __ldcg(&fp[3 * t]) : 0;
+      khi[j] = in ? __ldcg(&fp[3 * t + 1]) : 0;
+      kb[j] = in ? (int)__ldcg(&fp[3 * t + 2]) : INT_MIN;
+    }
     int m = INT_MIN;
-    for (int t = tid; t < fa.ntiles; t += nt) m = max(m, (int)__ldcg(&fp[3 * t + 2]));
+#pragma unroll
+    for (int j = 0; j < kKeep; ++j) m = max(m, kb[j]);
+    for (int t = tid + kKeep * nt; t < fa.ntiles; t += nt) m = max(m, (int)__ldcg(&fp[3 * t + 2]));
     m = block_max_int(m, si);
     fb = (m == kFxBad) ? kFxBad : m + 8;
-    if (fb != kFxBad)
-      for (int t = tid; t < fa.ntiles; t += nt)
+    if (fb != kFxBad) {
+#pragma unroll
+      for (int j = 0; j < kKeep; ++j)
+        if (tid + j * nt < fa.ntiles) qf += fx_align(fx_join((unsigned long long)klo[j], khi[j]), kb[j], fb);
+      for (int t = tid + kKeep * nt; t < fa.ntiles; t += nt)
         qf += fx_align(fx_join((unsigned long long)__ldcg(&fp[3 * t]), __ldcg(&fp[3 * t + 1])),
                        (int)__ldcg(&fp[3 * t + 2]), fb);
+    }
   } else {
     auto term = [&](int e) {
       double h = fa.gs.G[0][e];
@@ -1674,13 +1693,26 @@ __global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
         if (m != a.fa.mode) v *= a.fa.gs.G[m][(size_t)r * R + c];
       return v;
     };
+    // the terms formed once (their loads in flight together), kept in registers for the
+    // largest-exponent pass and the sum; blocks with more than 8 x 32 entries form the rest twice
+    constexpr int kKeep = 8;
+    double keep[kKeep];
+#pragma unroll
+    for (int j = 0; j < kKeep; ++j) keep[j] = (e0 + lane + 32 * j < e1) ? share(e0 + lane + 32 * j) : 0.0;
     int em = 1;
-    for (int e = e0 + lane; e < e1; e += 32) em = max(em, fx_exp(share(e)));
+#pragma unroll
+    for (int j = 0; j < kKeep; ++j)
+      if (e0 + lane + 32 * j < e1) em = max(em, fx_exp(keep[j]));
+    for (int e = e0 + lane + 32 * kKeep; e < e1; e += 32) em = max(em, fx_exp(share(e)));
     em = __reduce_max_sync(0xffffffffu, em);
     const int base = (em == 0x7ff) ? kFxBad : em - kFxHead;
     __int128 q = 0;
-    if (base != kFxBad)
-      for (int e = e0 + lane; e < e1; e += 32) q += fx_term(share(e), base);
+    if (base != kFxBad) {
+#pragma unroll
+      for (int j = 0; j < kKeep; ++j)
+        if (e0 + lane + 32 * j < e1) q += fx_term(keep[j], base);
+      for (int e = e0 + lane + 32 * kKeep; e < e1; e += 32) q += fx_term(share(e), base);
+    }
     q = fx_warp_sum(q);
     if (lane == 0) {
       long long* fp = reinterpret_cast<long long*>(a.fa.fpart);

@@ -22,6 +22,9 @@ inline int64_t panel_elems(int64_t rows, int64_t K) {
   return ((rows + kPanelRows - 1) / kPanelRows) * kPanelRows * ((K + kPanelK - 1) / kPanelK) * kPanelK;
 }
 
+// Sets the GEMM kernel's shared-memory limit on the current device (before any stream capture).
+cudaError_t gemm_tc_prepare();
+
 // Split-K slices the GEMM of an M x N output over K uses on `sms` SMs (partials are
 // float [splits][M][N]).
 int gemm_tc_splits(int M, int N, int K, int sms);

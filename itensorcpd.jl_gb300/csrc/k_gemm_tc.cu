@@ -188,6 +188,10 @@ __global__ void k_gemm_epilogue(const float* __restrict__ part, int splits, int 
 
 }  // namespace
 
+cudaError_t gemm_tc_prepare() {
+  return set_smem_limit_once(reinterpret_cast<const void*>(k_gemm_tc), (int)kGemmSmem);
+}
+
 int gemm_tc_splits(int M, int N, int K, int sms) {
   const int MT = (M + kPanelRows - 1) / kPanelRows, NT = (N + kPanelRows - 1) / kPanelRows;
   const int KT = (K + kPanelK - 1) / kPanelK;

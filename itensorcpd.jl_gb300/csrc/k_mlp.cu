@@ -52,9 +52,34 @@ __global__ void k_bias_grad(const float* __restrict__ dY, int B, int N, float* _
   }
 }
 
-// Adam (Kingma and Ba 2015) on the FP32 master parameters
-__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
-                       float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+// The training step's position, on the device so that one captured step serves every step:
+// k = step within the current cpals_mlp_train call (index offset and loss slot), t = Adam's
+// step count before this step.
+struct MlpStep {
+  long long k;
+  long long t;
+};
+
+constexpr int kLossSlots = 64;  // steps whose loss partials are kept before a read-back
+
+// gather rows idx[k * B + b] of a device dataset (FP32 [N][W]) into X (FP32 [B][W])
+__global__ void k_gather_step(const float* __restrict__ D, int W, const int* __restrict__ idx, int B,
+                              float* __restrict__ X, const MlpStep* __restrict__ st) {
+  const int* ix = idx + st->k * B;
+  const int64_t n = (int64_t)B * W;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e / W), w = (int)(e % W);
+    X[e] = D[(int64_t)ix[b] * W + w];
+  }
+}
+
+// Adam (Kingma and Ba 2015) on the FP32 master parameters, with the bias corrections of step
+// t + 1 formed on the device
+__global__ void k_adam_step(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                            float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps,
+                            const MlpStep* __restrict__ st) {
+  const float t = (float)(st->t + 1);
+  const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const float gg = g[e];
     const float a = b1 * m1[e] + (1.f - b1) * gg;
@@ -66,13 +91,29 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   }
 }
 
-// gather rows idx[b] of a device dataset (FP32 [N][W]) into X (FP32 [B][W])
-__global__ void k_gather_rows(const float* __restrict__ D, int W, const int* __restrict__ idx, int B,
-                              float* __restrict__ X) {
-  const int64_t n = (int64_t)B * W;
+__global__ void k_step_end(MlpStep* st) {
+  st->k += 1;
+  st->t += 1;
+}
+
+// the loss partials of step k go to slot k % kLossSlots
+__global__ void k_mse_grad_step(const float* __restrict__ Y, const float* __restrict__ T, int64_t n, float scale,
+                                float* __restrict__ dY, double* __restrict__ loss, int lb, const MlpStep* __restrict__ st) {
+  __shared__ double red[32];
+  double s = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(e / W), w = (int)(e % W);
-    X[e] = D[(int64_t)idx[b] * W + w];
+    const float d = Y[e] - T[e];
+    s += (double)d * d;
+    const float g = 2.f * d * scale;
+    dY[e] = g;
+  }
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (threadIdx.x == 0) loss[(st->k % kLossSlots) * lb + blockIdx.x] = t;
   }
 }
 
@@ -111,6 +152,12 @@ struct cpals_mlp {
   int64_t dn = 0;
   int64_t step = 0;
   double train_ms = 0.0;  // device time of the last cpals_mlp_train call (its launches only)
+  MlpStep* dstep = nullptr;             // the device step state
+  cudaGraphExec_t step_graph = nullptr;  // one captured training step
+  int graph_B = 0;
+  float graph_lr = 0.f;
+  const int* graph_idx = nullptr;
+  const float* graph_dx = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t st = nullptr;
 };
@@ -160,8 +207,11 @@ void free_batch(cpals_mlp* m) {
   m->bcap = 0;
 }
 
+void drop_step_graph(cpals_mlp* m);
+
 int ensure_batch(cpals_mlp* m, int B) {
   if (B <= m->bcap) return CPALS_OK;
+  drop_step_graph(m);  // it holds the old buffers
   free_batch(m);
   const int64_t in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
   bool ok = alloc0(&m->x, B * in) && alloc0(&m->t, B * o) && alloc0(&m->h1, B * a) && alloc0(&m->h2, B * b) &&
@@ -202,11 +252,14 @@ cudaError_t forward(cpals_mlp* m, int B) {
 
 // backward pass (targets in m->t), gradients into m->g, loss partials of this step into
 // m->loss[slot * lb ..]; returns the number of loss partials (lb)
-int backward(cpals_mlp* m, int B, int slot, cudaError_t* err) {
+int backward(cpals_mlp* m, int B, int slot, cudaError_t* err, const MlpStep* dstep = nullptr) {
   const int in = m->w[0], a = m->w[1], b = m->w[2], o = m->w[3];
   const int64_t ny = (int64_t)B * o;
   const int lb = std::min(grid1(ny), 64);
-  k_mse_grad<<<lb, 256, 0, m->st>>>(m->y, m->t, ny, 1.f / (float)ny, m->dy, m->loss + (int64_t)slot * lb);
+  if (dstep)
+    k_mse_grad_step<<<lb, 256, 0, m->st>>>(m->y, m->t, ny, 1.f / (float)ny, m->dy, m->loss, lb, dstep);
+  else
+    k_mse_grad<<<lb, 256, 0, m->st>>>(m->y, m->t, ny, 1.f / (float)ny, m->dy, m->loss + (int64_t)slot * lb);
   cudaError_t e = pack(m, m->dy, B, o, m->DYp, m->DYt);
   // dW3 = dy^T h2, db3 = sum_b dy
   if (e == cudaSuccess) e = gemm(m, m->DYt, m->H2t, o, b, B, nullptr, 0, nullptr, m->g + m->off[4], nullptr, nullptr);
@@ -224,12 +277,47 @@ int backward(cpals_mlp* m, int B, int slot, cudaError_t* err) {
   return lb;
 }
 
-cudaError_t adam(cpals_mlp* m, float lr) {
-  m->step += 1;
-  const float b1 = 0.9f, b2 = 0.999f;
-  const float c1 = 1.f - powf(b1, (float)m->step), c2 = 1.f - powf(b2, (float)m->step);
-  k_adam<<<grid1(m->np), 256, 0, m->st>>>(m->p, m->g, m->m1, m->m2, m->np, lr, b1, b2, 1e-8f, c1, c2);
-  return refresh_weights(m);
+// one training step on the device state: the batch's rows, forward, backward, Adam, the
+// weight panels, the state advanced; the same launches every step, so it is captured once
+cudaError_t train_step(cpals_mlp* m, int B, float lr) {
+  k_gather_step<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->dx, m->w[0], m->idx, B, m->x, m->dstep);
+  k_gather_step<<<grid1((int64_t)B * m->w[3]), 256, 0, m->st>>>(m->dt, m->w[3], m->idx, B, m->t, m->dstep);
+  cudaError_t e = forward(m, B);
+  if (e != cudaSuccess) return e;
+  (void)backward(m, B, 0, &e, m->dstep);
+  if (e != cudaSuccess) return e;
+  k_adam_step<<<grid1(m->np), 256, 0, m->st>>>(m->p, m->g, m->m1, m->m2, m->np, lr, 0.9f, 0.999f, 1e-8f, m->dstep);
+  e = refresh_weights(m);
+  if (e != cudaSuccess) return e;
+  k_step_end<<<1, 1, 0, m->st>>>(m->dstep);
+  return cudaGetLastError();
+}
+
+void drop_step_graph(cpals_mlp* m) {
+  if (m->step_graph) cudaGraphExecDestroy(m->step_graph);
+  m->step_graph = nullptr;
+}
+
+// captures train_step for (B, lr) and the current buffers; on failure the steps run eagerly
+void build_step_graph(cpals_mlp* m, int B, float lr) {
+  drop_step_graph(m);
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return;
+  }
+  const cudaError_t e = train_step(m, B, lr);
+  const cudaError_t ec = cudaStreamEndCapture(m->st, &g);
+  if (e == cudaSuccess && ec == cudaSuccess && g && cudaGraphInstantiate(&m->step_graph, g, 0) == cudaSuccess) {
+    m->graph_B = B;
+    m->graph_lr = lr;
+    m->graph_idx = m->idx;
+    m->graph_dx = m->dx;
+  } else {
+    m->step_graph = nullptr;
+    (void)cudaGetLastError();
+  }
+  if (g) cudaGraphDestroy(g);
 }
 
 // synchronise; CPALS_E_DEVICE (and the word cleared) if a GEMM's bounded wait expired
@@ -275,7 +363,7 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
             alloc0(&m->g, o) && alloc0(&m->m1, o) && alloc0(&m->m2, o) && alloc0(&m->err, 2) &&
             alloc0(&m->W1p, panel_elems(a, in)) && alloc0(&m->W2p, panel_elems(b, a)) &&
             alloc0(&m->W2t, panel_elems(a, b)) && alloc0(&m->W3p, panel_elems(y, b)) &&
-            alloc0(&m->W3t, panel_elems(b, y));
+            alloc0(&m->W3t, panel_elems(b, y)) && alloc0(&m->dstep, 1) && gemm_tc_prepare() == cudaSuccess;
   if (!ok) {
     cpals_mlp_destroy(m);
     return CPALS_E_CUDA;
@@ -287,8 +375,9 @@ int cpals_mlp_create(cpals_mlp** out, int device, const int* widths) {
 int cpals_mlp_destroy(cpals_mlp* m) {
   if (!m) return CPALS_OK;
   DeviceGuard guard(m->device);
+  drop_step_graph(m);
   free_batch(m);
-  for (void* q : {(void*)m->p, (void*)m->g, (void*)m->m1, (void*)m->m2, (void*)m->err, (void*)m->W1p, (void*)m->W2p,
+  for (void* q : {(void*)m->dstep, (void*)m->p, (void*)m->g, (void*)m->m1, (void*)m->m2, (void*)m->err, (void*)m->W1p, (void*)m->W2p,
                   (void*)m->W2t, (void*)m->W3p, (void*)m->W3t, (void*)m->idx, (void*)m->dx, (void*)m->dt})
     cudaFree(q);
   if (m->ev0) cudaEventDestroy(m->ev0);
@@ -387,22 +476,22 @@ int cpals_mlp_train(cpals_mlp* m, const int* host_idx, int steps, int B, float l
     m->idx_cap = nidx;
   }
   CPALS_CUDA_TRY(cudaMemcpyAsync(m->idx, host_idx, sizeof(int) * nidx, cudaMemcpyHostToDevice, m->st));
-  constexpr int kSlots = 64;  // 64 steps x at most 64 partials fill the 4096 loss words
+  const MlpStep h0{0, (long long)m->step};
+  CPALS_CUDA_TRY(cudaMemcpyAsync(m->dstep, &h0, sizeof(MlpStep), cudaMemcpyHostToDevice, m->st));
+  CPALS_CUDA_TRY(cudaStreamSynchronize(m->st));  // h0 is a stack value
+  if (!m->step_graph || m->graph_B != B || m->graph_lr != lr || m->graph_idx != m->idx || m->graph_dx != m->dx)
+    build_step_graph(m, B, lr);
+  const int lb = std::min(grid1((int64_t)B * m->w[3]), 64);
   std::vector<double> h;
   m->train_ms = 0.0;
-  for (int s0 = 0; s0 < steps; s0 += kSlots) {
-    const int ns = std::min(kSlots, steps - s0);
-    int lb = 1;
+  for (int s0 = 0; s0 < steps; s0 += kLossSlots) {
+    const int ns = std::min(kLossSlots, steps - s0);
     CPALS_CUDA_TRY(cudaEventRecord(m->ev0, m->st));
     for (int j = 0; j < ns; ++j) {
-      const int* ix = m->idx + (int64_t)(s0 + j) * B;
-      k_gather_rows<<<grid1((int64_t)B * m->w[0]), 256, 0, m->st>>>(m->dx, m->w[0], ix, B, m->x);
-      k_gather_rows<<<grid1((int64_t)B * m->w[3]), 256, 0, m->st>>>(m->dt, m->w[3], ix, B, m->t);
-      CPALS_CUDA_TRY(forward(m, B));
-      cudaError_t e = cudaSuccess;
-      lb = backward(m, B, j, &e);
-      CPALS_CUDA_TRY(e);
-      CPALS_CUDA_TRY(adam(m, lr));
+      if (m->step_graph)
+        CPALS_CUDA_TRY(cudaGraphLaunch(m->step_graph, m->st));
+      else
+        CPALS_CUDA_TRY(train_step(m, B, lr));
     }
     CPALS_CUDA_TRY(cudaEventRecord(m->ev1, m->st));
     h.assign((size_t)ns * lb, 0.0);
@@ -413,12 +502,13 @@ int cpals_mlp_train(cpals_mlp* m, const int* host_idx, int steps, int B, float l
     CPALS_CUDA_TRY(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
     m->train_ms += ms;
     if (losses)
-      for (int j = 0; j < ns; ++j) {
+      for (int j = 0; j < ns; ++j) {  // step s0 + j wrote slot j (s0 is a multiple of the slot count)
         double l = 0.0;
         for (int q = 0; q < lb; ++q) l += h[(size_t)j * lb + q];
         losses[s0 + j] = l / ((double)B * m->w[3]);
       }
   }
+  m->step += steps;
   return CPALS_OK;
 }
 

@@ -1247,35 +1247,16 @@ __device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam) {
   __shared__ long long sl[64];
   // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28): the rows' exact
   // fixed-point sums, aligned to the largest row base (+8: room for 2^36 rows) and added
-  // (each thread's first kKeep rows are read once, their loads in flight together, and kept
-  // for the sum; any further rows are read twice)
-  constexpr int kKeep = 4;
   const long long* ir = fa.inner_rows_fx;
-  long long klo[kKeep], khi[kKeep];
-  int kb[kKeep];
-#pragma unroll
-  for (int j = 0; j < kKeep; ++j) {
-    const int64_t i = tid + (int64_t)j * nt;
-    const bool in = i < fa.In;
-    klo[j] = in ? __ldcg(&ir[3 * i]) : 0;
-    khi[j] = in ? __ldcg(&ir[3 * i + 1]) : 0;
-    kb[j] = in ? (int)__ldcg(&ir[3 * i + 2]) : INT_MIN;
-  }
   int bmax = INT_MIN;
-#pragma unroll
-  for (int j = 0; j < kKeep; ++j) bmax = max(bmax, kb[j]);
-  for (int64_t i = tid + (int64_t)kKeep * nt; i < fa.In; i += nt) bmax = max(bmax, (int)__ldcg(&ir[3 * i + 2]));
+  for (int64_t i = tid; i < fa.In; i += nt) bmax = max(bmax, (int)__ldcg(&ir[3 * i + 2]));
   bmax = block_max_int(bmax, si);
   const int ib = (bmax == kFxBad) ? kFxBad : bmax + 8;
   __int128 qi = 0;
-  if (ib != kFxBad) {
-#pragma unroll
-    for (int j = 0; j < kKeep; ++j)
-      if (tid + (int64_t)j * nt < fa.In) qi += fx_align(fx_join((unsigned long long)klo[j], khi[j]), kb[j], ib);
-    for (int64_t i = tid + (int64_t)kKeep * nt; i < fa.In; i += nt)
+  if (ib != kFxBad)
+    for (int64_t i = tid; i < fa.In; i += nt)
       qi += fx_align(fx_join((unsigned long long)__ldcg(&ir[3 * i]), __ldcg(&ir[3 * i + 1])), (int)__ldcg(&ir[3 * i + 2]),
                      ib);
-  }
   const __int128 inner = block_sum_fx(qi, sl);
   // ||X||^2 = lambda^T (G_1 o ... o G_N) lambda  (converge_checks.jl:5-11): with the per-tile
   // (per-block) shares of the fused path, their exact sums; otherwise each term formed here
@@ -1283,28 +1264,14 @@ __device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam) {
   __int128 qf = 0;
   if (fa.fpart) {
     const long long* fp = reinterpret_cast<const long long*>(fa.fpart);
-#pragma unroll
-    for (int j = 0; j < kKeep; ++j) {
-      const int t = tid + j * nt;
-      const bool in = t < fa.ntiles;
-      klo[j] = in ? __ldcg(&fp[3 * t]) : 0;
-      khi[j] = in ? __ldcg(&fp[3 * t + 1]) : 0;
-      kb[j] = in ? (int)__ldcg(&fp[3 * t + 2]) : INT_MIN;
-    }
     int m = INT_MIN;
-#pragma unroll
-    for (int j = 0; j < kKeep; ++j) m = max(m, kb[j]);
-    for (int t = tid + kKeep * nt; t < fa.ntiles; t += nt) m = max(m, (int)__ldcg(&fp[3 * t + 2]));
+    for (int t = tid; t < fa.ntiles; t += nt) m = max(m, (int)__ldcg(&fp[3 * t + 2]));
     m = block_max_int(m, si);
     fb = (m == kFxBad) ? kFxBad : m + 8;
-    if (fb != kFxBad) {
-#pragma unroll
-      for (int j = 0; j < kKeep; ++j)
-        if (tid + j * nt < fa.ntiles) qf += fx_align(fx_join((unsigned long long)klo[j], khi[j]), kb[j], fb);
-      for (int t = tid + kKeep * nt; t < fa.ntiles; t += nt)
+    if (fb != kFxBad)
+      for (int t = tid; t < fa.ntiles; t += nt)
         qf += fx_align(fx_join((unsigned long long)__ldcg(&fp[3 * t]), __ldcg(&fp[3 * t + 1])),
                        (int)__ldcg(&fp[3 * t + 2]), fb);
-    }
   } else {
     auto term = [&](int e) {
       double h = fa.gs.G[0][e];
@@ -1693,26 +1660,13 @@ __global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
         if (m != a.fa.mode) v *= a.fa.gs.G[m][(size_t)r * R + c];
       return v;
     };
-    // the terms formed once (their loads in flight together), kept in registers for the
-    // largest-exponent pass and the sum; blocks with more than 8 x 32 entries form the rest twice
-    constexpr int kKeep = 8;
-    double keep[kKeep];
-#pragma unroll
-    for (int j = 0; j < kKeep; ++j) keep[j] = (e0 + lane + 32 * j < e1) ? share(e0 + lane + 32 * j) : 0.0;
     int em = 1;
-#pragma unroll
-    for (int j = 0; j < kKeep; ++j)
-      if (e0 + lane + 32 * j < e1) em = max(em, fx_exp(keep[j]));
-    for (int e = e0 + lane + 32 * kKeep; e < e1; e += 32) em = max(em, fx_exp(share(e)));
+    for (int e = e0 + lane; e < e1; e += 32) em = max(em, fx_exp(share(e)));
     em = __reduce_max_sync(0xffffffffu, em);
     const int base = (em == 0x7ff) ? kFxBad : em - kFxHead;
     __int128 q = 0;
-    if (base != kFxBad) {
-#pragma unroll
-      for (int j = 0; j < kKeep; ++j)
-        if (e0 + lane + 32 * j < e1) q += fx_term(keep[j], base);
-      for (int e = e0 + lane + 32 * kKeep; e < e1; e += 32) q += fx_term(share(e), base);
-    }
+    if (base != kFxBad)
+      for (int e = e0 + lane; e < e1; e += 32) q += fx_term(share(e), base);
     q = fx_warp_sum(q);
     if (lane == 0) {
       long long* fp = reinterpret_cast<long long*>(a.fa.fpart);

@@ -119,7 +119,7 @@ __device__ __forceinline__ long long bkey(double v) {
 }
 
 // One ALS sweep of tensor `it` by the whole CTA.
-__device__ __forceinline__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T, double* __restrict__ Fg,
+__device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T, double* __restrict__ Fg,
                                 double* __restrict__ Gg, BatchCheck* __restrict__ chk, const SmemLayout& L,
                                 unsigned char* sm, double tol, int max_iter) {
   __shared__ double red[32];
@@ -182,90 +182,58 @@ __device__ __forceinline__ void batch_sweep_one(const BatchItem& it, const float
         cp_async_wait_0();
       }
       __syncthreads();
-      // Each thread takes Q output rows 32 apart (lane l: rows l, l+32, .. of a 32Q-row group)
-      // and four consecutive rank columns: per reduction step Q scalar slice loads
-      // (consecutive across the warp, one wavefront each) and one broadcast 16-byte factor
-      // load feed 4Q FMAs.  Q is 4, 2 or 1, the largest that still gives every thread an
-      // item.  Each output's chain runs over the reduction index in order.
+      // Each thread takes one row of the output and four consecutive rank columns: one
+      // scalar slice load and one 16-byte factor load feed four FMAs.
       const int R4 = (R + 3) >> 2;
-      const int Iout = (n == 0) ? I0 : I1;
-      const int Q = (Iout * R4 >= 4 * nt) ? 4 : (Iout * R4 >= 2 * nt) ? 2 : 1;
       if (n == 0) {
         // M0[i][r] += F2[k][r] * sum_j S[i,j] F1[j][r]
-        const int G0 = (I0 + 32 * Q - 1) / (32 * Q);
-        for (int e = tid; e < 32 * G0 * R4; e += nt) {
-          const int l = e & 31, g = (e >> 5) % G0, r0 = ((e >> 5) / G0) * 4;
-          const int ib = g * 32 * Q + l;
-          float4 a[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) a[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int e = tid; e < I0 * R4; e += nt) {
+          const int i = e % I0, r0 = (e / I0) * 4;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int j = 0; j < I1; ++j) {
+            const float sv = Sk[i + ldS * j];
             const float4 f = *reinterpret_cast<const float4*>(&Fa[j * Rm + r0]);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const int i = ib + 32 * q;
-              const float sv = (q < Q && i < I0) ? Sk[i + ldS * j] : 0.f;
-              a[q].x = fmaf(sv, f.x, a[q].x);
-              a[q].y = fmaf(sv, f.y, a[q].y);
-              a[q].z = fmaf(sv, f.z, a[q].z);
-              a[q].w = fmaf(sv, f.w, a[q].w);
-            }
+            a.x = fmaf(sv, f.x, a.x);
+            a.y = fmaf(sv, f.y, a.y);
+            a.z = fmaf(sv, f.z, a.z);
+            a.w = fmaf(sv, f.w, a.w);
           }
           const float4 f2 = *reinterpret_cast<const float4*>(&F2[k * Rm + r0]);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int i = ib + 32 * q;
-            if (q < Q && i < I0) {
-              double* Mi = M + i * lm + r0;
-              Mi[0] += (double)(a[q].x * f2.x);
-              if (r0 + 1 < R) Mi[1] += (double)(a[q].y * f2.y);
-              if (r0 + 2 < R) Mi[2] += (double)(a[q].z * f2.z);
-              if (r0 + 3 < R) Mi[3] += (double)(a[q].w * f2.w);
-            }
-          }
+          double* Mi = M + i * lm + r0;
+          Mi[0] += (double)(a.x * f2.x);
+          if (r0 + 1 < R) Mi[1] += (double)(a.y * f2.y);
+          if (r0 + 2 < R) Mi[2] += (double)(a.z * f2.z);
+          if (r0 + 3 < R) Mi[3] += (double)(a.w * f2.w);
         }
       } else {
         // y[j][r] = sum_i S[i,j] F0[i][r]; mode 1: M1[j][r] += F2[k][r] y[j][r];
         // mode 2: M2[k][r] = sum_j F1[j][r] y[j][r] (X holds the per-j terms)
         const float* F1 = F32 + (size_t)1 * L.Imax * Rm;
-        const int G1 = (I1 + 32 * Q - 1) / (32 * Q);
-        for (int e = tid; e < 32 * G1 * R4; e += nt) {
-          const int l = e & 31, g = (e >> 5) % G1, r0 = ((e >> 5) / G1) * 4;
-          const int jb = g * 32 * Q + l;
-          float4 a[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) a[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int e = tid; e < I1 * R4; e += nt) {
+          const int j = e % I1, r0 = (e / I1) * 4;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int i = 0; i < I0; ++i) {
+            const float sv = Sk[i + ldS * j];
             const float4 f = *reinterpret_cast<const float4*>(&Fa[i * Rm + r0]);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const int j = jb + 32 * q;
-              const float sv = (q < Q && j < I1) ? Sk[i + ldS * j] : 0.f;
-              a[q].x = fmaf(sv, f.x, a[q].x);
-              a[q].y = fmaf(sv, f.y, a[q].y);
-              a[q].z = fmaf(sv, f.z, a[q].z);
-              a[q].w = fmaf(sv, f.w, a[q].w);
-            }
+            a.x = fmaf(sv, f.x, a.x);
+            a.y = fmaf(sv, f.y, a.y);
+            a.z = fmaf(sv, f.z, a.z);
+            a.w = fmaf(sv, f.w, a.w);
           }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int j = jb + 32 * q;
-            if (q >= Q || j >= I1) continue;
-            const float4 gg = *reinterpret_cast<const float4*>(n == 1 ? &F2[k * Rm + r0] : &F1[j * Rm + r0]);
-            double* out = (n == 1) ? M + j * lm + r0 : X + j * lm + r0;
-            const double v0 = (double)(a[q].x * gg.x), v1 = (double)(a[q].y * gg.y), v2 = (double)(a[q].z * gg.z),
-                         v3 = (double)(a[q].w * gg.w);
-            if (n == 1) {
-              out[0] += v0;
-              if (r0 + 1 < R) out[1] += v1;
-              if (r0 + 2 < R) out[2] += v2;
-              if (r0 + 3 < R) out[3] += v3;
-            } else {
-              out[0] = v0;
-              if (r0 + 1 < R) out[1] = v1;
-              if (r0 + 2 < R) out[2] = v2;
-              if (r0 + 3 < R) out[3] = v3;
-            }
+          const float4 g = *reinterpret_cast<const float4*>(n == 1 ? &F2[k * Rm + r0] : &F1[j * Rm + r0]);
+          double* out = (n == 1) ? M + j * lm + r0 : X + j * lm + r0;
+          const double v0 = (double)(a.x * g.x), v1 = (double)(a.y * g.y), v2 = (double)(a.z * g.z),
+                       v3 = (double)(a.w * g.w);
+          if (n == 1) {
+            out[0] += v0;
+            if (r0 + 1 < R) out[1] += v1;
+            if (r0 + 2 < R) out[2] += v2;
+            if (r0 + 3 < R) out[3] += v3;
+          } else {
+            out[0] = v0;
+            if (r0 + 1 < R) out[1] = v1;
+            if (r0 + 2 < R) out[2] = v2;
+            if (r0 + 3 < R) out[3] = v3;
           }
         }
         if (n == 2) {
@@ -461,7 +429,7 @@ __device__ __forceinline__ void batch_sweep_one(const BatchItem& it, const float
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_batch_sweep(const BatchItem* __restrict__ items, const int* __restrict__ order,
+__global__ void __launch_bounds__(NT) k_batch_sweep(const BatchItem* __restrict__ items, const int* __restrict__ order,
                                                     int count, const float* __restrict__ T, double* __restrict__ F,
                                                     double* __restrict__ G, BatchCheck* __restrict__ chk,
                                                     unsigned* __restrict__ queue, SmemLayout L,

@@ -17,21 +17,24 @@
 // stored in the order the CTAs consume them.  A stage is one contiguous 32 KB bulk copy
 // and every CTA streams one contiguous region (4 bytes per element, the FP32 size).
 //
-// CTA (6 or 10 warps).  Warp 0 is the producer: per stage it issues three kinds of
-// cp.async.bulk copies into a 2-4 stage mbarrier ring -- the 32 KB unfolding tile (hi, lo),
-// the prebuilt BF16 hi/lo factor-block tile of F_f[k0:k0+64, n0:n0+NB] (written by
-// k_build_btiles, or by the normalisation kernel when the factor is updated in a sweep) and
-// the FP32 rows of the outer factors.  Warp 1 issues tcgen05.mma.kind::f16 (M = 128, K = 16,
-// four steps per chunk): one N = 2 NB product Th [Bh | Bl] and one N = NB product Tl Bh.
-// The tensor core's FP32 accumulation rounds toward zero, which over long chains shrinks
-// the result (about 0.5 ulp per accumulation), so each chunk accumulates into fresh TMEM
-// accumulators (2 or 4 buffers), and the drain warps (4, or 8 when NB is a multiple of 64:
-// one or two per TMEM lane quarter) read them with tcgen05.ld, scale them by the product
-// of the outer rows and accumulate in FP32 registers with round-to-nearest adds.  A stage
-// is released when every drain warp has read its outer rows.  The reduction range is split
-// across CTAs; each writes FP32 partials part[split][I_n][R], reduced by the solve kernel.
-// Every wait is bounded: on expiry the kernel records an error code, drains its own copies
-// in flight (bounded), frees TMEM and returns.
+// CTA (6 or 10 warps).  Warp 0 is the producer: per stage it issues cp.async.bulk copies
+// into a 2-4 stage mbarrier ring -- the 32 KB unfolding tile (hi, lo), the FP32 rows of the
+// outer factors and, unless every factor-block tile of the CTA's N block is resident in
+// shared memory (loaded once, when four stages still fit beside them), the prebuilt BF16
+// hi/lo factor-block tile of F_f[k0:k0+64, n0:n0+NB] (written by k_build_btiles, or by the
+// normalisation when the factor is updated in a sweep).  Warp 1 issues
+// tcgen05.mma.kind::f16 (M = 128, K = 16, four steps per chunk): one N = 2 NB product
+// Th [Bh | Bl] and one N = NB product Tl Bh.  The tensor core's FP32 accumulation rounds
+// toward zero, which over long chains shrinks the result (about 0.5 ulp per accumulation),
+// so accumulation groups stay short: each group of chunks (one chunk, or two consecutive
+// factor blocks of one outer index when NB = 128) accumulates into fresh TMEM accumulators
+// (2 or 4 buffers).  The drain warps (4, or 8 when NB is a multiple of 64: one or two per
+// TMEM lane quarter) form the group's outer-row scale s(r) into their own shared slice,
+// release the group's stages, read the accumulators with tcgen05.ld and accumulate
+// s(r) (hi + cross terms) in FP32 registers with round-to-nearest adds.  The reduction
+// range is split across CTAs; each writes FP32 partials part[split][I_n][R], reduced by the
+// solve.  Every wait is bounded: on expiry the kernel records an error code, drains its own
+// copies in flight (bounded), frees TMEM and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>

@@ -29,8 +29,6 @@
 #include <numeric>
 #include <vector>
 
-#include <cuda_bf16.h>
-
 #include "cpals_internal.cuh"
 
 namespace cpals {
@@ -115,66 +113,12 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// x ~ hi + lo, both BF16 (round to nearest): the split-BF16 operands of the tensor-core products
-__device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-  const float2 hf = __bfloat1622float2(h);
-  const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
-  hi = *reinterpret_cast<const uint32_t*>(&h);
-  lo = *reinterpret_cast<const uint32_t*>(&l);
-}
-
-// D (16 x 8, FP32) += A (16 x 16, BF16, row) B (16 x 8, BF16, col): one warp
-__device__ __forceinline__ void mma_bf16_16816(float* d, const uint32_t* a, const uint32_t* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// One slice of the batched MTTKRP on the tensor cores: Y (Iout x R) = A (Iout x K) Fk (K x R),
-// A(m, q) = S[m + ldS q] (mode 0: rows i, reduction j) or S[q + ldS m] (modes 1, 2: rows j,
-// reduction i), Fk = the FP32 factor rows (ld Rm).  Each warp takes 16 x 8 output tiles; per
-// 16-wide reduction step it loads and splits its A and B elements into BF16 hi / lo and
-// issues the three products Ah Bh + Ah Bl + Al Bh (m16n8k16, FP32 accumulation over the
-// slice).  out(m, r, y) is called for every output of the warp's tiles.
-template <typename Out>
-__device__ __forceinline__ void slice_mma(bool trans, int Iout, int K, int R, int Rm, int ldS, const float* S,
-                                          const float* Fk, int warp, int nwarps, int lane, Out out) {
-  const int g = lane >> 2, t = lane & 3;
-  const int mt = (Iout + 15) >> 4, ntl = (R + 7) >> 3;
-  for (int tile = warp; tile < mt * ntl; tile += nwarps) {
-    const int m0 = (tile % mt) * 16, n0 = (tile / mt) * 8;
-    float d[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int q0 = 0; q0 < K; q0 += 16) {
-      auto av = [&](int m, int q) -> float {
-        if (m >= Iout || q >= K) return 0.f;
-        return trans ? S[q + ldS * m] : S[m + ldS * q];
-      };
-      auto bv = [&](int q, int n) -> float { return (q < K && n < R) ? Fk[q * Rm + n] : 0.f; };
-      uint32_t ah[4], al[4], bh[2], bl[2];
-      split_bf16x2(av(m0 + g, q0 + 2 * t), av(m0 + g, q0 + 2 * t + 1), ah[0], al[0]);
-      split_bf16x2(av(m0 + g + 8, q0 + 2 * t), av(m0 + g + 8, q0 + 2 * t + 1), ah[1], al[1]);
-      split_bf16x2(av(m0 + g, q0 + 2 * t + 8), av(m0 + g, q0 + 2 * t + 9), ah[2], al[2]);
-      split_bf16x2(av(m0 + g + 8, q0 + 2 * t + 8), av(m0 + g + 8, q0 + 2 * t + 9), ah[3], al[3]);
-      split_bf16x2(bv(q0 + 2 * t, n0 + g), bv(q0 + 2 * t + 1, n0 + g), bh[0], bl[0]);
-      split_bf16x2(bv(q0 + 2 * t + 8, n0 + g), bv(q0 + 2 * t + 9, n0 + g), bh[1], bl[1]);
-      mma_bf16_16816(d, ah, bh);
-      mma_bf16_16816(d, ah, bl);
-      mma_bf16_16816(d, al, bh);
-    }
-    // d0, d1: row m0 + g, columns n0 + 2t, +1; d2, d3: row m0 + g + 8
-    const int ra = m0 + g, rb = m0 + g + 8, c0 = n0 + 2 * t;
-    if (ra < Iout) {
-      if (c0 < R) out(ra, c0, d[0]);
-      if (c0 + 1 < R) out(ra, c0 + 1, d[1]);
-    }
-    if (rb < Iout) {
-      if (c0 < R) out(rb, c0, d[2]);
-      if (c0 + 1 < R) out(rb, c0 + 1, d[3]);
-    }
-  }
+// s + c += v, a compensated (Neumaier) FP32 sum: the MTTKRP's sums across slices stay off the
+// FP64 pipe (2 operations per clock per SM on this part), at FP32-product accuracy
+__device__ __forceinline__ void acc2(float2& a, float v) {
+  const float t = a.x + v;
+  a.y += (fabsf(a.x) >= fabsf(v)) ? ((a.x - t) + v) : ((v - t) + a.x);
+  a.x = t;
 }
 
 __device__ __forceinline__ long long bkey(double v) {
@@ -223,7 +167,10 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   for (int n = 0; n < 3; ++n) {
     const int In = it.I[n];
     // ---- MTTKRP, slice by slice over the last mode: each slice S = T[:, :, k]
-    for (int e = tid; e < In * R; e += nt) M[(e / R) * lm + e % R] = 0.0;
+    // M accumulates as FP32 pairs (same bytes, float2 per entry) until the slices are done
+    float2* Mc = reinterpret_cast<float2*>(M);
+    float* X32 = reinterpret_cast<float*>(X);
+    for (int e = tid; e < In * R; e += nt) Mc[(e / R) * lm + e % R] = make_float2(0.f, 0.f);
     const float* Fa = F32 + (size_t)(n == 0 ? 1 : 0) * L.Imax * Rm;  // the other in-slice mode
     const float* F2 = F32 + (size_t)2 * L.Imax * Rm;
     // Slices are double-buffered: slice k+1 is copied (cp.async, 4 bytes per element) while
@@ -246,40 +193,76 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
         cp_async_wait_0();
       }
       __syncthreads();
-      // The slice's product on the tensor cores (split-BF16, three products, FP32 over the
-      // slice), scaled and added in FP64 as before.
+      // Each thread takes one row of the output and four consecutive rank columns: one
+      // scalar slice load and one 16-byte factor load feed four FMAs.
+      const int R4 = (R + 3) >> 2;
       if (n == 0) {
         // M0[i][r] += F2[k][r] * sum_j S[i,j] F1[j][r]
-        slice_mma(false, I0, I1, R, Rm, ldS, Sk, Fa, warp, nt >> 5, lane, [&](int i, int r, float y) {
-          M[i * lm + r] += (double)(y * F2[k * Rm + r]);
-        });
+        for (int e = tid; e < I0 * R4; e += nt) {
+          const int i = e % I0, r0 = (e / I0) * 4;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int j = 0; j < I1; ++j) {
+            const float sv = Sk[i + ldS * j];
+            const float4 f = *reinterpret_cast<const float4*>(&Fa[j * Rm + r0]);
+            a.x = fmaf(sv, f.x, a.x);
+            a.y = fmaf(sv, f.y, a.y);
+            a.z = fmaf(sv, f.z, a.z);
+            a.w = fmaf(sv, f.w, a.w);
+          }
+          const float4 f2 = *reinterpret_cast<const float4*>(&F2[k * Rm + r0]);
+          float2* Mi = Mc + i * lm + r0;
+          acc2(Mi[0], a.x * f2.x);
+          if (r0 + 1 < R) acc2(Mi[1], a.y * f2.y);
+          if (r0 + 2 < R) acc2(Mi[2], a.z * f2.z);
+          if (r0 + 3 < R) acc2(Mi[3], a.w * f2.w);
+        }
       } else {
         // y[j][r] = sum_i S[i,j] F0[i][r]; mode 1: M1[j][r] += F2[k][r] y[j][r];
         // mode 2: M2[k][r] = sum_j F1[j][r] y[j][r] (X holds the per-j terms)
         const float* F1 = F32 + (size_t)1 * L.Imax * Rm;
-        if (n == 1)
-          slice_mma(true, I1, I0, R, Rm, ldS, Sk, Fa, warp, nt >> 5, lane, [&](int j, int r, float y) {
-            M[j * lm + r] += (double)(y * F2[k * Rm + r]);
-          });
-        else
-          slice_mma(true, I1, I0, R, Rm, ldS, Sk, Fa, warp, nt >> 5, lane, [&](int j, int r, float y) {
-            X[j * lm + r] = (double)(y * F1[j * Rm + r]);
-          });
+        for (int e = tid; e < I1 * R4; e += nt) {
+          const int j = e % I1, r0 = (e / I1) * 4;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int i = 0; i < I0; ++i) {
+            const float sv = Sk[i + ldS * j];
+            const float4 f = *reinterpret_cast<const float4*>(&Fa[i * Rm + r0]);
+            a.x = fmaf(sv, f.x, a.x);
+            a.y = fmaf(sv, f.y, a.y);
+            a.z = fmaf(sv, f.z, a.z);
+            a.w = fmaf(sv, f.w, a.w);
+          }
+          const float4 g = *reinterpret_cast<const float4*>(n == 1 ? &F2[k * Rm + r0] : &F1[j * Rm + r0]);
+          const float v0 = a.x * g.x, v1 = a.y * g.y, v2 = a.z * g.z, v3 = a.w * g.w;
+          if (n == 1) {
+            float2* out = Mc + j * lm + r0;
+            acc2(out[0], v0);
+            if (r0 + 1 < R) acc2(out[1], v1);
+            if (r0 + 2 < R) acc2(out[2], v2);
+            if (r0 + 3 < R) acc2(out[3], v3);
+          } else {
+            float* out = X32 + j * lm + r0;
+            out[0] = v0;
+            if (r0 + 1 < R) out[1] = v1;
+            if (r0 + 2 < R) out[2] = v2;
+            if (r0 + 3 < R) out[3] = v3;
+          }
+        }
         if (n == 2) {
           __syncthreads();
           for (int r = tid; r < R; r += nt) {
-            double s0 = 0.0, s1 = 0.0;
-            int j = 0;
-            for (; j + 1 < I1; j += 2) {
-              s0 += X[j * lm + r];
-              s1 += X[(j + 1) * lm + r];
-            }
-            if (j < I1) s0 += X[j * lm + r];
-            M[k * lm + r] = s0 + s1;
+            float2 a2 = make_float2(0.f, 0.f);
+            for (int j = 0; j < I1; ++j) acc2(a2, X32[j * lm + r]);
+            Mc[k * lm + r] = a2;
           }
         }
       }
       __syncthreads();  // slice k's buffer is refilled at iteration k+1
+    }
+    __syncthreads();
+    for (int e = tid; e < In * R; e += nt) {  // the pairs to FP64, in place
+      const int idx = (e / R) * lm + e % R;
+      const float2 a2 = Mc[idx];
+      M[idx] = (double)a2.x + (double)a2.y;
     }
     __syncthreads();
     // ---- V = G_a .* G_b (mode order), upper triangle into A

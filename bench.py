@@ -623,7 +623,7 @@ def run_c4(args, pkg, device):
     line = {
         "metric": "batched_cp_als_solves_per_s", "value": count / total_s, "unit": "solves/s", "n_gpus": 1,
         "steps": max(1, args.steps), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 mttkrp (f32 slices, f64 across slices), f64 solve/gram/fit", "data": "synthetic",
+        "dtype": "f32 mttkrp (f32 slices, compensated f32 pairs across slices), f64 sweep, compensated f32 X = M W, f64 gram/fit", "data": "synthetic",
         "config": {"workload": f"batched_{count}_order3_dims16-96_rank4-32_fitcheck1e-5_200", "count": count,
                    "elements": elems, "tensor_bytes": 4 * elems},
         "ms_per_batch": total_s * 1e3,

@@ -5,9 +5,9 @@
 // one full ALS sweep of that tensor in shared memory, with the reference's steps
 // (src/optimizers/als_optimizers/optimize.jl:15-32) for every mode n:
 //   M_n = T_(n) (F_b (.) F_a)          FP32 products, FP32 accumulation over one tensor
-//                                      slice, FP64 across slices
+//                                      slice, compensated FP32 pairs across slices
 //   V = G_a .* G_b                     FP64 (MttkrpAlgorithm.jl:18-31)
-//   X = M_n V^{-1}                     pivoted symmetric sweep of V (tol 1e-6) + FP64 product
+//   X = M_n V^{-1}                     pivoted symmetric sweep of V (tol 1e-6) + compensated FP32 product
 //   lambda, F_n = X / lambda, G_n      FP64 (row_norm.jl, standard/tensor.jl:46-49)
 // and after the last mode the fit and the tensor's own FitCheck (fit_check.jl:24-66).
 // Converged tensors are skipped by later launches.  The sweep is a CUDA graph (queue reset
@@ -16,7 +16,7 @@
 // Shared memory per CTA (Imax = largest mode size, Rmax = largest rank of the batch):
 //   slice   Imax^2 floats             one I0 x I1 slice of T
 //   F32     3 Imax Rmax floats        the factors in FP32 (MTTKRP operands)
-//   M       Imax Rmax doubles         MTTKRP result
+//   M       Imax Rmax float pairs     MTTKRP result (hi + lo)
 //   X       Imax Rmax doubles         solve result
 //   A       Rmax (Rmax|1) doubles     V, swept in place into -V^{-1}
 //   G       3 Rmax^2 doubles          Grams
@@ -259,12 +259,6 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
       __syncthreads();  // slice k's buffer is refilled at iteration k+1
     }
     __syncthreads();
-    for (int e = tid; e < In * R; e += nt) {  // the pairs to FP64, in place
-      const int idx = (e / R) * lm + e % R;
-      const float2 a2 = Mc[idx];
-      M[idx] = (double)a2.x + (double)a2.y;
-    }
-    __syncthreads();
     // ---- V = G_a .* G_b (mode order), upper triangle into A
     const double* Ga = G + (size_t)(n == 0 ? 1 : 0) * R * R;
     const double* Gb = G + (size_t)(n == 2 ? 1 : 2) * R * R;
@@ -334,35 +328,50 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
     // fallback, ldiv_solve.jl:20-21, returns its least-squares solution instead)
     if (rank < R && tid == 0) chk->rank_deficient += 1;
     __syncthreads();
-    // ---- X = M W (FP64): W(l, c) = -A(min, max) for swept l, c; 0 otherwise
+    // ---- X = M W: W(l, c) = -A(min, max) for swept l, c; 0 otherwise.  M is the MTTKRP's
+    // FP32 pair m = mh + ml and W is split the same way (into the space of G_n, which is
+    // rewritten at the end of the mode); each product is a compensated FP32 dot product
+    // (Dot2: the mh wh terms split exactly by one FMA and summed with TwoSum, the cross
+    // terms added in FP32), as accurate as FP64 to ~2^-48 and off the FP64 pipe.
+    float2* Wp = reinterpret_cast<float2*>(G + (size_t)n * R * R);
+    for (int e = tid; e < R * R; e += nt) {
+      const int l = e / R, c = e - l * R;
+      const bool sw = vec[3 * Rm + c] != 0.0 && vec[3 * Rm + l] != 0.0;
+      const double w = sw ? -((l <= c) ? A[l * ld + c] : A[c * ld + l]) : 0.0;
+      const float wh = (float)w;
+      Wp[e] = make_float2(wh, (float)(w - (double)wh));
+    }
+    __syncthreads();
     for (int e = tid; e < In * R; e += nt) {
       const int i = e / R, c = e - i * R;
-      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-      const bool cs = vec[3 * Rm + c] != 0.0;
+      const float2* mrow = Mc + i * lm;
+      float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+      // the _rn intrinsics keep the compiler from contracting the error-free steps into FMAs
+      auto term = [&](const float2 m, const float2 w, float& sa, float& ca) {
+        const float pr = __fmul_rn(m.x, w.x);
+        const float pe = fmaf(m.x, w.x, -pr);
+        const float t = __fadd_rn(sa, pr);
+        const float z = __fsub_rn(t, sa);
+        const float er = __fadd_rn(__fsub_rn(sa, __fsub_rn(t, z)), __fsub_rn(pr, z));
+        sa = t;
+        ca += (pe + er) + fmaf(m.x, w.y, m.y * w.x);
+      };
       int l = 0;
-      for (; l + 4 <= R; l += 4) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int ll = l + q;
-          const double w = (cs && vec[3 * Rm + ll] != 0.0) ? -((ll <= c) ? A[ll * ld + c] : A[c * ld + ll]) : 0.0;
-          const double mv = M[i * lm + ll];
-          if (q == 0) s0 = fma(mv, w, s0);
-          else if (q == 1) s1 = fma(mv, w, s1);
-          else if (q == 2) s2 = fma(mv, w, s2);
-          else s3 = fma(mv, w, s3);
-        }
+      for (; l + 2 <= R; l += 2) {
+        term(mrow[l], Wp[l * R + c], s0, c0);
+        term(mrow[l + 1], Wp[(l + 1) * R + c], s1, c1);
       }
-      for (; l < R; ++l) {
-        const double w = (cs && vec[3 * Rm + l] != 0.0) ? -((l <= c) ? A[l * ld + c] : A[c * ld + l]) : 0.0;
-        s0 = fma(M[i * lm + l], w, s0);
-      }
-      X[i * lm + c] = (s0 + s1) + (s2 + s3);
+      if (l < R) term(mrow[l], Wp[l * R + c], s0, c0);
+      X[i * lm + c] = ((double)s0 + (double)s1) + ((double)c0 + (double)c1);
     }
     __syncthreads();
     // ---- <T, X> on the last mode (fit_check.jl:28)
     if (n == 2) {
       double p = 0.0;
-      for (int e = tid; e < In * R; e += nt) p += M[(e / R) * lm + e % R] * X[(e / R) * lm + e % R];
+      for (int e = tid; e < In * R; e += nt) {
+        const float2 m = Mc[(e / R) * lm + e % R];
+        p += ((double)m.x + (double)m.y) * X[(e / R) * lm + e % R];
+      }
       inner = block_sum_d(p, red);
     }
     // ---- lambda = column norms, F_n = X / lambda (row_norm.jl:4-24)

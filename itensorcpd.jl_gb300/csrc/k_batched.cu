@@ -38,7 +38,8 @@ namespace {
 constexpr double kBatchTol = 1e-6;  // cholesky_epsilon (src/ITensorCPD.jl:2)
 
 struct BatchItem {
-  int64_t toff;  // tensor offset (elements)
+  int64_t toff;     // tensor offset (elements) in the natural layout, as uploaded
+  int64_t loff[3];  // offsets of the MTTKRP's per-mode layouts (floats, 16-byte aligned)
   int64_t foff;  // factor offset (doubles): F0, F1, F2 (I_m x R column-major), lambda [R]
   int64_t goff;  // Gram offset (doubles): G0, G1, G2 (R x R each)
   int I[3];
@@ -60,13 +61,53 @@ struct BatchCheck {  // fit_check.jl:5-20, per tensor
 
 struct SmemLayout {
   int Imax, Rmax, ld, lm;  // lm: odd leading dimension (doubles) of M and X
-  size_t slice, f32, M, X, A, G, vec, total;
-  size_t slice_bytes;      // one of the two slice buffers
+  size_t ring, ring_bytes, f32, M, X, A, G, vec, total;
 };
 
 __host__ __device__ inline size_t al16(size_t b) { return (b + 15) & ~size_t(15); }
 
-__host__ __device__ inline SmemLayout smem_layout(int Imax, int Rmax) {
+// The MTTKRP's slab ring holds at least two steps of P slabs; P is chosen so that two steps
+// take at most this many bytes (two 96 x 96 FP32 slabs), or P = 1.
+constexpr int kRingBytes = 2 * 96 * 96 * 4;
+
+// FP32 elements of one slab of a mode layout (In x Ia), padded to 16 bytes.
+__host__ __device__ inline int64_t slab_floats(int In, int Ia) { return (((int64_t)In * Ia + 3) / 4) * 4; }
+
+// Rank columns per MTTKRP thread: 8 unless that pads the rank further than groups of 4 do.
+__host__ __device__ inline int rank_width(int R) { return ((R + 7) / 8) * 8 == ((R + 3) / 4) * 4 ? 8 : 4; }
+
+// Slab partitions of one mode's MTTKRP (In outputs, Rg rank groups, Ia x Ib slab extents): as
+// many as keep the items at 512 or fewer and two steps of P slabs within kRingBytes.  A
+// function of the tensor's shape alone, so that the sums and their order do not depend on the
+// thread count or the schedule.
+__host__ __device__ inline int mttkrp_parts(int In, int Rg, int Ia, int Ib) {
+  int P = 512 / (In * Rg);
+  const int pr = (int)(kRingBytes / (2 * 4 * slab_floats(In, Ia)));
+  P = P < pr ? P : pr;
+  return P < 1 ? 1 : (P > Ib ? Ib : P);
+}
+
+// Shared memory a tensor's MTTKRP needs beyond the sweep's arrays: the slab ring (two steps of
+// P slabs, the largest over the modes) and the partial pairs of the partitions p >= 1.
+struct MttkrpNeed {
+  size_t ring = 0, part = 0;
+};
+inline MttkrpNeed mttkrp_need(const int I[3], int R) {
+  MttkrpNeed m;
+  const int W = rank_width(R), Rg = (R + W - 1) / W;
+  for (int n = 0; n < 3; ++n) {
+    const int ma = (n == 0) ? 1 : 0, mb = (n == 2) ? 1 : 2;
+    const int P = mttkrp_parts(I[n], Rg, I[ma], I[mb]);
+    m.ring = std::max(m.ring, (size_t)2 * P * slab_floats(I[n], I[ma]) * 4);
+    m.part = std::max(m.part, (size_t)(P - 1) * I[n] * Rg * W * 8);
+  }
+  return m;
+}
+
+// Imax, Rmax: the largest extent and rank of the tensors that use the layout; need: the
+// largest of their MTTKRP needs.  The partial pairs share the space of X, which is free
+// during the MTTKRP.
+inline SmemLayout smem_layout(int Imax, int Rmax, MttkrpNeed need) {
   SmemLayout L{};
   L.Imax = Imax;
   L.Rmax = (Rmax + 3) & ~3;  // FP32 factor rows of 16-byte multiples (float4 loads)
@@ -74,15 +115,15 @@ __host__ __device__ inline SmemLayout smem_layout(int Imax, int Rmax) {
   L.ld = Rmax | 1;
   L.lm = Rmax + 1;  // Rmax is a multiple of 4: odd, so row walks of M and X are conflict-free
   size_t o = 0;
-  L.slice = o;
-  L.slice_bytes = al16((size_t)Imax * (Imax | 1) * 4);
-  o += 2 * L.slice_bytes;  // double-buffered: slice k+1 loads while slice k is used
+  L.ring = o;
+  L.ring_bytes = need.ring;
+  o += al16(L.ring_bytes);
   L.f32 = o;
   o += al16((size_t)3 * Imax * Rmax * 4);
   L.M = o;
   o += al16((size_t)Imax * L.lm * 8);
   L.X = o;
-  o += al16((size_t)Imax * L.lm * 8);
+  o += al16(std::max((size_t)Imax * L.lm * 8, need.part));
   L.A = o;
   o += al16((size_t)Rmax * L.ld * 8);
   L.G = o;
@@ -105,20 +146,142 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
   return t;
 }
 
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 // s + c += v, a compensated (Neumaier) FP32 sum: the MTTKRP's sums across slices stay off the
 // FP64 pipe (2 operations per clock per SM on this part), at FP32-product accuracy
 __device__ __forceinline__ void acc2(float2& a, float v) {
   const float t = a.x + v;
   a.y += (fabsf(a.x) >= fabsf(v)) ? ((a.x - t) + v) : ((v - t) + a.x);
   a.x = t;
+}
+
+// s += v for two compensated pairs: TwoSum of the leading parts, the rest added in FP32
+__device__ __forceinline__ void merge2(float2& s, const float2 v) {
+  const float t = s.x + v.x;
+  const float z = t - s.x;
+  const float e = (s.x - (t - z)) + (v.x - z);
+  s.x = t;
+  s.y = (s.y + v.y) + e;
+}
+
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_dyn(int n) {
+  // wait_group takes an immediate: the ring depths that occur
+  if (n <= 0) cp_async_wait<0>();
+  else if (n == 1) cp_async_wait<1>();
+  else if (n == 2) cp_async_wait<2>();
+  else if (n == 3) cp_async_wait<3>();
+  else if (n == 4) cp_async_wait<4>();
+  else if (n == 5) cp_async_wait<5>();
+  else cp_async_wait<6>();
+}
+
+// One mode's MTTKRP, M[o][r] = sum_b Fb[b][r] sum_a S_b[o + In a] Fa[a][r], with S_b slab b of the
+// mode's own layout of T (this mode's index o fastest, a and b the other two; slabs `slab`
+// floats apart, 16-byte aligned).
+// Thread item (o, rank group, slab partition p): the W rank columns of output row o over the
+// slabs b = p, p + P, ...; the slab's sum over a in FP32, the sum across slabs as compensated
+// FP32 pairs in registers.  The slabs stream through a shared-memory ring in steps of P (slab
+// s P + p for partition p), 16-byte cp.async copies by all threads, up to NS - 1 steps ahead;
+// one block barrier per step.  S reads are consecutive across the warp's o, Fa rows broadcast.
+// Partition 0 writes M; the others write partial pairs merged into M in the order of p.
+template <int W>
+__device__ __forceinline__ void mttkrp_mode(const float* __restrict__ Tn, int In, int Ia, int Ib, int R, int P,
+                                            const float* Fa, const float* Fb, int Rm, float2* Mc, int lm,
+                                            float2* part, float* ring, size_t ring_bytes) {
+  const int Rg = (R + W - 1) / W;
+  const int items = In * Rg * P;
+  const int slab = (int)slab_floats(In, Ia);
+  const int stepf = P * slab;
+  const int steps = (Ib + P - 1) / P;
+  const int NS = (int)(ring_bytes / ((size_t)stepf * 4)) < 7 ? (int)(ring_bytes / ((size_t)stepf * 4)) : 7;
+  auto copy_step = [&](int s) {
+    if (s < steps) {
+      const int nb = (s + 1) * P <= Ib ? P : Ib - s * P;
+      const int n16 = nb * slab / 4;
+      const float* src = Tn + (int64_t)s * stepf;
+      float* dst = ring + (s % NS) * stepf;
+      for (int c = threadIdx.x; c < n16; c += blockDim.x) cp_async16(dst + 4 * c, src + 4 * c);
+    }
+    cp_async_commit();  // empty groups keep the count uniform
+  };
+  for (int e0 = 0; e0 < items; e0 += blockDim.x) {
+    const int e = e0 + threadIdx.x;
+    const bool active = e < items;
+    const int o = e % In, q = e / In, rg = q % Rg, p = q / Rg;
+    const int r0 = rg * W;
+    float2 acc[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) acc[w] = make_float2(0.f, 0.f);
+    __syncthreads();  // the ring's previous contents are consumed
+    for (int s = 0; s < NS - 1; ++s) copy_step(s);
+    for (int s = 0; s < steps; ++s) {
+      cp_async_wait_dyn(NS - 2);  // this thread's copies of step s have landed
+      __syncthreads();            // everyone's have; step s - 1's slot is free
+      copy_step(s + NS - 1);
+      const int b = s * P + p;
+      if (active && b < Ib) {
+        const float* S = ring + (s % NS) * stepf + p * slab + o;
+        float t[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) t[w] = 0.f;
+#pragma unroll 4
+        for (int a = 0; a < Ia; ++a) {
+          const float sv = S[a * In];
+          const float* fr = Fa + a * Rm + r0;
+          const float4 f0 = *reinterpret_cast<const float4*>(fr);
+          t[0] = fmaf(sv, f0.x, t[0]);
+          t[1] = fmaf(sv, f0.y, t[1]);
+          t[2] = fmaf(sv, f0.z, t[2]);
+          t[3] = fmaf(sv, f0.w, t[3]);
+          if constexpr (W == 8) {
+            const float4 f1 = *reinterpret_cast<const float4*>(fr + 4);
+            t[4] = fmaf(sv, f1.x, t[4]);
+            t[5] = fmaf(sv, f1.y, t[5]);
+            t[6] = fmaf(sv, f1.z, t[6]);
+            t[7] = fmaf(sv, f1.w, t[7]);
+          }
+        }
+        const float* gr = Fb + b * Rm + r0;
+#pragma unroll
+        for (int w = 0; w < W; w += 4) {
+          const float4 g = *reinterpret_cast<const float4*>(gr + w);
+          acc2(acc[w], t[w] * g.x);
+          acc2(acc[w + 1], t[w + 1] * g.y);
+          acc2(acc[w + 2], t[w + 2] * g.z);
+          acc2(acc[w + 3], t[w + 3] * g.w);
+        }
+      }
+    }
+    cp_async_wait<0>();  // no copy is left in flight (the trailing groups are empty)
+    if (active) {
+      if (p == 0) {
+        float2* d = Mc + o * lm + r0;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+          if (r0 + w < R) d[w] = acc[w];
+      } else {
+        float2* d = part + ((size_t)((p - 1) * Rg + rg) * In + o) * W;
+#pragma unroll
+        for (int w = 0; w < W; ++w) d[w] = acc[w];
+      }
+    }
+  }
+  if (P > 1) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < In * R; e += blockDim.x) {
+      const int o = e / R, r = e - o * R, rg = r / W, w = r - rg * W;
+      float2 sm2 = Mc[o * lm + r];
+      for (int p = 1; p < P; ++p) merge2(sm2, part[((size_t)((p - 1) * Rg + rg) * In + o) * W + w]);
+      Mc[o * lm + r] = sm2;
+    }
+  }
 }
 
 __device__ __forceinline__ long long bkey(double v) {
@@ -137,7 +300,6 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   const int R = it.R, I0 = it.I[0], I1 = it.I[1], I2 = it.I[2];
   const int Rm = L.Rmax;
   const int lm = L.lm;
-  float* S = reinterpret_cast<float*>(sm + L.slice);
   float* F32 = reinterpret_cast<float*>(sm + L.f32);  // F32 + m*Imax*Rm: [I_m][R] row-major (ld Rm)
   double* M = reinterpret_cast<double*>(sm + L.M);     // [I_n][Rm]
   double* X = reinterpret_cast<double*>(sm + L.X);     // [I_n][Rm]
@@ -148,8 +310,6 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   double* a_row = vec + Rm;   // pivot row
   double* t_row = vec + 2 * Rm;
   const int ld = L.ld;
-  const float* Tt = T + it.toff;
-  const int ldS = I0 | 1;
   double* F0g = Fg + it.foff;
   const int64_t fo[3] = {0, (int64_t)I0 * R, (int64_t)(I0 + I1) * R};
   double* lamg = Fg + it.foff + (int64_t)(I0 + I1 + I2) * R;
@@ -166,97 +326,23 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   double inner = 0.0;
   for (int n = 0; n < 3; ++n) {
     const int In = it.I[n];
-    // ---- MTTKRP, slice by slice over the last mode: each slice S = T[:, :, k]
-    // M accumulates as FP32 pairs (same bytes, float2 per entry) until the slices are done
+    // ---- MTTKRP from the mode's own layout of T (this mode's index fastest): mode 0 over
+    // (a, b) = (j, k), mode 1 over (i, k), mode 2 over (i, j); M as compensated FP32 pairs
+    // (same bytes as the FP64 array, float2 per entry)
     float2* Mc = reinterpret_cast<float2*>(M);
-    float* X32 = reinterpret_cast<float*>(X);
-    for (int e = tid; e < In * R; e += nt) Mc[(e / R) * lm + e % R] = make_float2(0.f, 0.f);
-    const float* Fa = F32 + (size_t)(n == 0 ? 1 : 0) * L.Imax * Rm;  // the other in-slice mode
-    const float* F2 = F32 + (size_t)2 * L.Imax * Rm;
-    // Slices are double-buffered: slice k+1 is copied (cp.async, 4 bytes per element) while
-    // slice k is used.  S[i + ldS j] has an odd leading dimension, so column walks are free
-    // of bank conflicts.
-    auto load_slice = [&](int k, float* dst) {
-      const float* Tk = Tt + (int64_t)k * I0 * I1;
-      for (int e = tid; e < I0 * I1; e += nt) cp_async4(dst + (e % I0) + ldS * (e / I0), Tk + e);
-      cp_async_commit();
-    };
-    float* Sbuf[2] = {S, S + L.slice_bytes / 4};
-    __syncthreads();  // the previous mode's reads of both buffers are done
-    load_slice(0, Sbuf[0]);
-    for (int k = 0; k < I2; ++k) {
-      const float* Sk = Sbuf[k & 1];
-      if (k + 1 < I2) {
-        load_slice(k + 1, Sbuf[(k + 1) & 1]);
-        cp_async_wait_1();
-      } else {
-        cp_async_wait_0();
-      }
-      __syncthreads();
-      // Each thread takes one row of the output and four consecutive rank columns: one
-      // scalar slice load and one 16-byte factor load feed four FMAs.
-      const int R4 = (R + 3) >> 2;
-      if (n == 0) {
-        // M0[i][r] += F2[k][r] * sum_j S[i,j] F1[j][r]
-        for (int e = tid; e < I0 * R4; e += nt) {
-          const int i = e % I0, r0 = (e / I0) * 4;
-          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int j = 0; j < I1; ++j) {
-            const float sv = Sk[i + ldS * j];
-            const float4 f = *reinterpret_cast<const float4*>(&Fa[j * Rm + r0]);
-            a.x = fmaf(sv, f.x, a.x);
-            a.y = fmaf(sv, f.y, a.y);
-            a.z = fmaf(sv, f.z, a.z);
-            a.w = fmaf(sv, f.w, a.w);
-          }
-          const float4 f2 = *reinterpret_cast<const float4*>(&F2[k * Rm + r0]);
-          float2* Mi = Mc + i * lm + r0;
-          acc2(Mi[0], a.x * f2.x);
-          if (r0 + 1 < R) acc2(Mi[1], a.y * f2.y);
-          if (r0 + 2 < R) acc2(Mi[2], a.z * f2.z);
-          if (r0 + 3 < R) acc2(Mi[3], a.w * f2.w);
-        }
-      } else {
-        // y[j][r] = sum_i S[i,j] F0[i][r]; mode 1: M1[j][r] += F2[k][r] y[j][r];
-        // mode 2: M2[k][r] = sum_j F1[j][r] y[j][r] (X holds the per-j terms)
-        const float* F1 = F32 + (size_t)1 * L.Imax * Rm;
-        for (int e = tid; e < I1 * R4; e += nt) {
-          const int j = e % I1, r0 = (e / I1) * 4;
-          float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int i = 0; i < I0; ++i) {
-            const float sv = Sk[i + ldS * j];
-            const float4 f = *reinterpret_cast<const float4*>(&Fa[i * Rm + r0]);
-            a.x = fmaf(sv, f.x, a.x);
-            a.y = fmaf(sv, f.y, a.y);
-            a.z = fmaf(sv, f.z, a.z);
-            a.w = fmaf(sv, f.w, a.w);
-          }
-          const float4 g = *reinterpret_cast<const float4*>(n == 1 ? &F2[k * Rm + r0] : &F1[j * Rm + r0]);
-          const float v0 = a.x * g.x, v1 = a.y * g.y, v2 = a.z * g.z, v3 = a.w * g.w;
-          if (n == 1) {
-            float2* out = Mc + j * lm + r0;
-            acc2(out[0], v0);
-            if (r0 + 1 < R) acc2(out[1], v1);
-            if (r0 + 2 < R) acc2(out[2], v2);
-            if (r0 + 3 < R) acc2(out[3], v3);
-          } else {
-            float* out = X32 + j * lm + r0;
-            out[0] = v0;
-            if (r0 + 1 < R) out[1] = v1;
-            if (r0 + 2 < R) out[2] = v2;
-            if (r0 + 3 < R) out[3] = v3;
-          }
-        }
-        if (n == 2) {
-          __syncthreads();
-          for (int r = tid; r < R; r += nt) {
-            float2 a2 = make_float2(0.f, 0.f);
-            for (int j = 0; j < I1; ++j) acc2(a2, X32[j * lm + r]);
-            Mc[k * lm + r] = a2;
-          }
-        }
-      }
-      __syncthreads();  // slice k's buffer is refilled at iteration k+1
+    {
+      const int ma = (n == 0) ? 1 : 0, mb = (n == 2) ? 1 : 2;
+      const float* Tn = T + it.loff[n];
+      const float* Fa = F32 + (size_t)ma * L.Imax * Rm;
+      const float* Fb = F32 + (size_t)mb * L.Imax * Rm;
+      float2* part = reinterpret_cast<float2*>(X);
+      float* ring = reinterpret_cast<float*>(sm + L.ring);
+      const int W = rank_width(R);
+      const int P = mttkrp_parts(In, (R + W - 1) / W, it.I[ma], it.I[mb]);
+      if (W == 8)
+        mttkrp_mode<8>(Tn, In, it.I[ma], it.I[mb], R, P, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes);
+      else
+        mttkrp_mode<4>(Tn, In, it.I[ma], it.I[mb], R, P, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes);
     }
     __syncthreads();
     // ---- V = G_a .* G_b (mode order), upper triangle into A
@@ -484,6 +570,46 @@ __global__ void k_batch_reset(unsigned* queue, int nqueue, const BatchCheck* chk
   if (threadIdx.x == 0) *active = s;
 }
 
+// dst[y + dx x] = src[x + sy y] for x < X, y < Y, through a 32 x 33 tile (256 threads).
+__device__ void transpose_plane(const float* __restrict__ src, float* __restrict__ dst, int X, int Y, int64_t sy,
+                                int64_t dx, float (*tile)[33]) {
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int y0 = 0; y0 < Y; y0 += 32)
+    for (int x0 = 0; x0 < X; x0 += 32) {
+      for (int yy = ty; yy < 32; yy += 8) {
+        const int x = x0 + tx, y = y0 + yy;
+        if (x < X && y < Y) tile[yy][tx] = src[x + sy * y];
+      }
+      __syncthreads();
+      for (int xx = ty; xx < 32; xx += 8) {
+        const int x = x0 + xx, y = y0 + tx;
+        if (x < X && y < Y) dst[y + dx * x] = tile[tx][xx];
+      }
+      __syncthreads();
+    }
+}
+
+// The MTTKRP's per-mode layouts of every tensor, from the natural one (T[i + I0 j + I0 I1 k]):
+// mode n's layout holds element (o, a, b) at loff[n] + b slab + o + In a, with o mode n's index
+// and (a, b) = (j, k), (i, k), (i, j) for n = 0, 1, 2; slabs are padded to 16 bytes so that the
+// sweep streams them with 16-byte copies.  256 threads per block.
+__global__ void k_batch_layouts(const BatchItem* __restrict__ items, int count, const float* __restrict__ T,
+                                float* __restrict__ Lay) {
+  __shared__ float tile[32][33];
+  for (int id = blockIdx.x; id < count; id += gridDim.x) {
+    const BatchItem it = items[id];
+    const int I0 = it.I[0], I1 = it.I[1], I2 = it.I[2];
+    const float* src = T + it.toff;
+    const int64_t s0 = slab_floats(I0, I1), s1 = slab_floats(I1, I0), s2 = slab_floats(I2, I0);
+    const int64_t plane = (int64_t)I0 * I1;
+    for (int k = 0; k < I2; ++k)
+      for (int e = threadIdx.x; e < plane; e += blockDim.x) Lay[it.loff[0] + k * s0 + e] = src[plane * k + e];
+    for (int k = 0; k < I2; ++k) transpose_plane(src + plane * k, Lay + it.loff[1] + k * s1, I0, I1, I0, I1, tile);
+    for (int j = 0; j < I1; ++j)
+      transpose_plane(src + (int64_t)I0 * j, Lay + it.loff[2] + j * s2, I0, I2, plane, I2, tile);
+  }
+}
+
 // Grams of the initial factors, and lambda / checks reset.
 __global__ void k_batch_init(const BatchItem* __restrict__ items, int count, double* __restrict__ F,
                              double* __restrict__ G, BatchCheck* __restrict__ chk) {
@@ -521,6 +647,7 @@ using namespace cpals;
 struct BatchClass {
   int begin = 0, end = 0;
   int Imax = 0, Rmax = 0;
+  MttkrpNeed need;
   SmemLayout L{};
   int nt = 256;
   int ctas_per_sm = 1;
@@ -534,12 +661,14 @@ struct cpals_batch {
   int device = 0;
   int64_t count = 0;
   int Imax = 0, Rmax = 0;
+  MttkrpNeed need;  // the largest MTTKRP needs of the batch
   std::vector<BatchItem> items;
   std::vector<int> order;
-  int64_t tot_T = 0, tot_F = 0, tot_G = 0;
+  int64_t tot_T = 0, tot_L = 0, tot_F = 0, tot_G = 0;
   BatchItem* d_items = nullptr;
   int* d_order = nullptr;
-  float* d_T = nullptr;
+  float* d_T = nullptr;  // the tensors as uploaded
+  float* d_L = nullptr;  // the MTTKRP's per-mode layouts
   double* d_F = nullptr;
   double* d_G = nullptr;
   BatchCheck* d_chk = nullptr;
@@ -580,15 +709,15 @@ int class_launch(cpals_batch* b, const BatchClass& c, int q, cudaStream_t st) {
   const int* order = b->d_order + c.begin;
   switch (c.nt) {
     case 128:
-      k_batch_sweep<128><<<grid, 128, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
+      k_batch_sweep<128><<<grid, 128, c.L.total, st>>>(b->d_items, order, n, b->d_L, b->d_F, b->d_G, b->d_chk,
                                                           b->d_queue + q, c.L, b->d_run);
       break;
     case 256:
-      k_batch_sweep<256><<<grid, 256, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
+      k_batch_sweep<256><<<grid, 256, c.L.total, st>>>(b->d_items, order, n, b->d_L, b->d_F, b->d_G, b->d_chk,
                                                           b->d_queue + q, c.L, b->d_run);
       break;
     case 512:
-      k_batch_sweep<512><<<grid, 512, c.L.total, st>>>(b->d_items, order, n, b->d_T, b->d_F, b->d_G, b->d_chk,
+      k_batch_sweep<512><<<grid, 512, c.L.total, st>>>(b->d_items, order, n, b->d_L, b->d_F, b->d_G, b->d_chk,
                                                           b->d_queue + q, c.L, b->d_run);
       break;
     default:
@@ -724,12 +853,21 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
     it.foff = b->tot_F;
     it.goff = b->tot_G;
     b->tot_T += (int64_t)it.I[0] * it.I[1] * it.I[2];
+    it.loff[0] = b->tot_L;
+    b->tot_L += it.I[2] * slab_floats(it.I[0], it.I[1]);
+    it.loff[1] = b->tot_L;
+    b->tot_L += it.I[2] * slab_floats(it.I[1], it.I[0]);
+    it.loff[2] = b->tot_L;
+    b->tot_L += it.I[1] * slab_floats(it.I[2], it.I[0]);
     b->tot_F += (int64_t)(it.I[0] + it.I[1] + it.I[2] + 1) * it.R;
     b->tot_G += (int64_t)3 * it.R * it.R;
     b->Imax = std::max({b->Imax, it.I[0], it.I[1], it.I[2]});
     b->Rmax = std::max(b->Rmax, it.R);
+    const MttkrpNeed m = mttkrp_need(it.I, it.R);
+    b->need.ring = std::max(b->need.ring, m.ring);
+    b->need.part = std::max(b->need.part, m.part);
   }
-  b->L = smem_layout(b->Imax, b->Rmax);
+  b->L = smem_layout(b->Imax, b->Rmax, b->need);
   if (b->L.total > 227 * 1024) {
     delete b;
     return CPALS_E_UNSUPPORTED;
@@ -750,7 +888,7 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
     std::vector<int> cps(count);
     for (int64_t t = 0; t < count; ++t) {
       const BatchItem& it = b->items[t];
-      const size_t tot = smem_layout(std::max({it.I[0], it.I[1], it.I[2]}), b->Rmax).total;
+      const size_t tot = smem_layout(std::max({it.I[0], it.I[1], it.I[2]}), b->Rmax, mttkrp_need(it.I, it.R)).total;
       cps[t] = (int)std::max<size_t>(1, std::min<size_t>(kMaxBatchClasses, (227 * 1024) / tot));
     }
     for (int k = 1; k <= kMaxBatchClasses; ++k) {
@@ -761,10 +899,13 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
           b->order_split.push_back(t);
           c.Imax = std::max({c.Imax, b->items[t].I[0], b->items[t].I[1], b->items[t].I[2]});
           c.Rmax = std::max(c.Rmax, b->items[t].R);
+          const MttkrpNeed m = mttkrp_need(b->items[t].I, b->items[t].R);
+          c.need.ring = std::max(c.need.ring, m.ring);
+          c.need.part = std::max(c.need.part, m.part);
         }
       c.end = (int)b->order_split.size();
       if (c.end > c.begin) {
-        c.L = smem_layout(c.Imax, c.Rmax);
+        c.L = smem_layout(c.Imax, c.Rmax, c.need);
         b->split.push_back(c);
       }
     }
@@ -774,6 +915,8 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
             cudaMalloc(&b->d_items, sizeof(BatchItem) * count) == cudaSuccess &&
             cudaMalloc(&b->d_order, sizeof(int) * count) == cudaSuccess &&
             cudaMalloc(&b->d_T, sizeof(float) * b->tot_T) == cudaSuccess &&
+            cudaMalloc(&b->d_L, sizeof(float) * b->tot_L) == cudaSuccess &&
+            cudaMemset(b->d_L, 0, sizeof(float) * b->tot_L) == cudaSuccess &&  // slab padding
             cudaMalloc(&b->d_F, sizeof(double) * b->tot_F) == cudaSuccess &&
             cudaMalloc(&b->d_G, sizeof(double) * b->tot_G) == cudaSuccess &&
             cudaMalloc(&b->d_chk, sizeof(BatchCheck) * count) == cudaSuccess &&
@@ -812,6 +955,7 @@ int cpals_batch_destroy(cpals_batch* b) {
   cudaFree(b->d_items);
   cudaFree(b->d_order);
   cudaFree(b->d_T);
+  cudaFree(b->d_L);
   cudaFree(b->d_F);
   cudaFree(b->d_G);
   cudaFree(b->d_chk);
@@ -834,6 +978,10 @@ int cpals_batch_set_tensors(cpals_batch* b, const float* host_concat) {
   if (!b || !host_concat) return CPALS_E_ARG;
   DeviceGuard guard(b->device);
   CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_T, host_concat, sizeof(float) * b->tot_T, cudaMemcpyHostToDevice, b->st));
+  const int blocks = (int)std::min<int64_t>(b->count, 8192);
+  k_batch_layouts<<<blocks, 256, 0, b->st>>>(b->d_items, (int)b->count, b->d_T, b->d_L);
+  CPALS_CUDA_TRY(cudaGetLastError());
+  b->launches += 1;
   return CPALS_OK;
 }
 

@@ -94,10 +94,13 @@ def test_batched_autotune_and_thread_counts(built, oracle):
 
 
 def test_batched_split_schedule_matches_one_class(built, oracle):
-    # extents 16..96: the tensors' own layouts allow 1 to 4 CTAs per SM, so the autotuner has
-    # a split schedule to try; whichever it keeps, every tensor is solved once, as one class
-    # solves it (only the fit's block sums depend on the warp count)
-    dims, ranks, Ts, Fs, lams = make_batch(oracle, 40, seed=7, dmin=16, dmax=96, rmin=4, rmax=16)
+    # small (12..20) and large (60..96) extents: the small tensors' own layouts allow more CTAs
+    # per SM than the large ones', so the autotuner has a split schedule to try; whichever it
+    # keeps, every tensor is solved once, as one class solves it (only the fit's block sums
+    # depend on the warp count)
+    small = make_batch(oracle, 20, seed=7, dmin=12, dmax=20, rmin=2, rmax=6)
+    large = make_batch(oracle, 20, seed=8, dmin=60, dmax=96, rmin=4, rmax=16)
+    dims, ranks, Ts, Fs, lams = (a + b for a, b in zip(small, large))
     norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
     with built.BatchEngine(dims, ranks, norms) as be:
         be.set_tensors(Ts)

@@ -76,15 +76,39 @@ __host__ __device__ inline int64_t slab_floats(int In, int Ia) { return (((int64
 // Rank columns per MTTKRP thread: 8 unless that pads the rank further than groups of 4 do.
 __host__ __device__ inline int rank_width(int R) { return ((R + 7) / 8) * 8 == ((R + 3) / 4) * 4 ? 8 : 4; }
 
-// Slab partitions of one mode's MTTKRP (In outputs, Rg rank groups, Ia x Ib slab extents): as
-// many as keep the items at 512 or fewer and two steps of P slabs within kRingBytes.  A
-// function of the tensor's shape alone, so that the sums and their order do not depend on the
-// thread count or the schedule.
-__host__ __device__ inline int mttkrp_parts(int In, int Rg, int Ia, int Ib) {
-  int P = 512 / (In * Rg);
+// Slab partitions of one mode's MTTKRP (Ig output groups, Rg rank groups, In x Ia slabs, Ib of
+// them): as many as keep the items at 480 or fewer (one round on the MTTKRP's 15 warps of a
+// 512-thread CTA) and two steps of P slabs within kRingBytes.
+__host__ __device__ inline int mttkrp_parts(int Ig, int Rg, int In, int Ia, int Ib) {
+  int P = 480 / (Ig * Rg);
   const int pr = (int)(kRingBytes / (2 * 4 * slab_floats(In, Ia)));
   P = P < pr ? P : pr;
   return P < 1 ? 1 : (P > Ib ? Ib : P);
+}
+
+// How one mode's MTTKRP is split: W rank columns and Q output rows (o and o + ceil(In/Q)) per
+// thread item, P slab partitions.  Two rows per item when that keeps as many items (the slab
+// partitions double instead): half the steps, the Fa loads shared by two rows.  A function of
+// the tensor's shape alone, so that the sums and their order do not depend on the thread count
+// or the schedule.
+struct MttkrpPlan {
+  int W, Q, P, Rg, Ig;
+};
+__host__ __device__ inline MttkrpPlan mttkrp_plan(int In, int Ia, int Ib, int R) {
+  MttkrpPlan m;
+  m.W = rank_width(R);
+  m.Rg = (R + m.W - 1) / m.W;
+  const int P1 = mttkrp_parts(In, m.Rg, In, Ia, Ib);
+  const int Ih = (In + 1) / 2;
+  int P2 = mttkrp_parts(Ih, m.Rg, In, Ia, Ib);
+  const int pp = 1 + 4096 / (In * m.Rg * m.W);  // partial pairs of p >= 1 within 32 KB
+  P2 = P2 < pp ? P2 : pp;
+  if (In >= 2 && Ih * m.Rg * P2 >= In * m.Rg * P1) {
+    m.Q = 2, m.P = P2, m.Ig = Ih;
+  } else {
+    m.Q = 1, m.P = P1, m.Ig = In;
+  }
+  return m;
 }
 
 // Shared memory a tensor's MTTKRP needs beyond the sweep's arrays: the slab ring (two steps of
@@ -94,12 +118,11 @@ struct MttkrpNeed {
 };
 inline MttkrpNeed mttkrp_need(const int I[3], int R) {
   MttkrpNeed m;
-  const int W = rank_width(R), Rg = (R + W - 1) / W;
   for (int n = 0; n < 3; ++n) {
     const int ma = (n == 0) ? 1 : 0, mb = (n == 2) ? 1 : 2;
-    const int P = mttkrp_parts(I[n], Rg, I[ma], I[mb]);
-    m.ring = std::max(m.ring, (size_t)2 * P * slab_floats(I[n], I[ma]) * 4);
-    m.part = std::max(m.part, (size_t)(P - 1) * I[n] * Rg * W * 8);
+    const MttkrpPlan pl = mttkrp_plan(I[n], I[ma], I[mb], R);
+    m.ring = std::max(m.ring, (size_t)2 * pl.P * slab_floats(I[n], I[ma]) * 4);
+    m.part = std::max(m.part, (size_t)(pl.P - 1) * I[n] * pl.Rg * pl.W * 8);
   }
   return m;
 }
@@ -189,14 +212,21 @@ __device__ __forceinline__ void cp_async_wait_dyn(int n) {
 // slabs b = p, p + P, ...; the slab's sum over a in FP32, the sum across slabs as compensated
 // FP32 pairs in registers.  The slabs stream through a shared-memory ring in steps of P (slab
 // s P + p for partition p), 16-byte cp.async copies by all threads, up to NS - 1 steps ahead;
-// one block barrier per step.  S reads are consecutive across the warp's o, Fa rows broadcast.
+// one barrier per step.  S reads are consecutive across the warp's o, Fa rows broadcast.
 // Partition 0 writes M; the others write partial pairs merged into M in the order of p.
-template <int W>
-__device__ __forceinline__ void mttkrp_mode(const float* __restrict__ Tn, int In, int Ia, int Ib, int R, int P,
-                                            const float* Fa, const float* Fb, int Rm, float2* Mc, int lm,
-                                            float2* part, float* ring, size_t ring_bytes) {
-  const int Rg = (R + W - 1) / W;
-  const int items = In * Rg * P;
+__device__ __forceinline__ void bar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// Run by threads [0, nthr) of the block (named barrier 1); the block's last warp runs the
+// pivoted sweep meanwhile.
+template <int W, int Q>
+__device__ __forceinline__ void mttkrp_mode(const float* __restrict__ Tn, int In, int Ia, int Ib, int R,
+                                            const MttkrpPlan pl, const float* Fa, const float* Fb, int Rm,
+                                            float2* Mc, int lm, float2* part, float* ring, size_t ring_bytes,
+                                            int tid, int nthr) {
+  const int Rg = pl.Rg, P = pl.P, Ig = pl.Ig;
+  const int items = Ig * Rg * P;
   const int slab = (int)slab_floats(In, Ia);
   const int stepf = P * slab;
   const int steps = (Ib + P - 1) / P;
@@ -207,75 +237,96 @@ __device__ __forceinline__ void mttkrp_mode(const float* __restrict__ Tn, int In
       const int n16 = nb * slab / 4;
       const float* src = Tn + (int64_t)s * stepf;
       float* dst = ring + (s % NS) * stepf;
-      for (int c = threadIdx.x; c < n16; c += blockDim.x) cp_async16(dst + 4 * c, src + 4 * c);
+      for (int c = tid; c < n16; c += nthr) cp_async16(dst + 4 * c, src + 4 * c);
     }
     cp_async_commit();  // empty groups keep the count uniform
   };
-  for (int e0 = 0; e0 < items; e0 += blockDim.x) {
-    const int e = e0 + threadIdx.x;
+  for (int e0 = 0; e0 < items; e0 += nthr) {
+    const int e = e0 + tid;
     const bool active = e < items;
-    const int o = e % In, q = e / In, rg = q % Rg, p = q / Rg;
+    const int og = e % Ig, q = e / Ig, rg = q % Rg, p = q / Rg;
     const int r0 = rg * W;
-    float2 acc[W];
+    int orow[Q];
+    bool ok[Q];
 #pragma unroll
-    for (int w = 0; w < W; ++w) acc[w] = make_float2(0.f, 0.f);
-    __syncthreads();  // the ring's previous contents are consumed
+    for (int h = 0; h < Q; ++h) {
+      const int o = og + h * Ig;
+      ok[h] = o < In;
+      orow[h] = ok[h] ? o : og;  // a row past the extent repeats row og; its sums are dropped
+    }
+    float2 acc[Q][W];
+#pragma unroll
+    for (int h = 0; h < Q; ++h)
+#pragma unroll
+      for (int w = 0; w < W; ++w) acc[h][w] = make_float2(0.f, 0.f);
+    bar_sync(1, nthr);  // the ring's previous contents are consumed
     for (int s = 0; s < NS - 1; ++s) copy_step(s);
     for (int s = 0; s < steps; ++s) {
       cp_async_wait_dyn(NS - 2);  // this thread's copies of step s have landed
-      __syncthreads();            // everyone's have; step s - 1's slot is free
+      bar_sync(1, nthr);          // everyone's have; step s - 1's slot is free
       copy_step(s + NS - 1);
       const int b = s * P + p;
       if (active && b < Ib) {
-        const float* S = ring + (s % NS) * stepf + p * slab + o;
-        float t[W];
+        const float* S = ring + (s % NS) * stepf + p * slab;
+        float t[Q][W];
 #pragma unroll
-        for (int w = 0; w < W; ++w) t[w] = 0.f;
+        for (int h = 0; h < Q; ++h)
+#pragma unroll
+          for (int w = 0; w < W; ++w) t[h][w] = 0.f;
 #pragma unroll 4
         for (int a = 0; a < Ia; ++a) {
-          const float sv = S[a * In];
+          float sv[Q];
+#pragma unroll
+          for (int h = 0; h < Q; ++h) sv[h] = S[orow[h] + a * In];
           const float* fr = Fa + a * Rm + r0;
-          const float4 f0 = *reinterpret_cast<const float4*>(fr);
-          t[0] = fmaf(sv, f0.x, t[0]);
-          t[1] = fmaf(sv, f0.y, t[1]);
-          t[2] = fmaf(sv, f0.z, t[2]);
-          t[3] = fmaf(sv, f0.w, t[3]);
-          if constexpr (W == 8) {
-            const float4 f1 = *reinterpret_cast<const float4*>(fr + 4);
-            t[4] = fmaf(sv, f1.x, t[4]);
-            t[5] = fmaf(sv, f1.y, t[5]);
-            t[6] = fmaf(sv, f1.z, t[6]);
-            t[7] = fmaf(sv, f1.w, t[7]);
+#pragma unroll
+          for (int w4 = 0; w4 < W; w4 += 4) {
+            const float4 f = *reinterpret_cast<const float4*>(fr + w4);
+#pragma unroll
+            for (int h = 0; h < Q; ++h) {
+              t[h][w4] = fmaf(sv[h], f.x, t[h][w4]);
+              t[h][w4 + 1] = fmaf(sv[h], f.y, t[h][w4 + 1]);
+              t[h][w4 + 2] = fmaf(sv[h], f.z, t[h][w4 + 2]);
+              t[h][w4 + 3] = fmaf(sv[h], f.w, t[h][w4 + 3]);
+            }
           }
         }
         const float* gr = Fb + b * Rm + r0;
 #pragma unroll
-        for (int w = 0; w < W; w += 4) {
-          const float4 g = *reinterpret_cast<const float4*>(gr + w);
-          acc2(acc[w], t[w] * g.x);
-          acc2(acc[w + 1], t[w + 1] * g.y);
-          acc2(acc[w + 2], t[w + 2] * g.z);
-          acc2(acc[w + 3], t[w + 3] * g.w);
+        for (int w4 = 0; w4 < W; w4 += 4) {
+          const float4 g = *reinterpret_cast<const float4*>(gr + w4);
+#pragma unroll
+          for (int h = 0; h < Q; ++h) {
+            acc2(acc[h][w4], t[h][w4] * g.x);
+            acc2(acc[h][w4 + 1], t[h][w4 + 1] * g.y);
+            acc2(acc[h][w4 + 2], t[h][w4 + 2] * g.z);
+            acc2(acc[h][w4 + 3], t[h][w4 + 3] * g.w);
+          }
         }
       }
     }
     cp_async_wait<0>();  // no copy is left in flight (the trailing groups are empty)
     if (active) {
-      if (p == 0) {
-        float2* d = Mc + o * lm + r0;
 #pragma unroll
-        for (int w = 0; w < W; ++w)
-          if (r0 + w < R) d[w] = acc[w];
-      } else {
-        float2* d = part + ((size_t)((p - 1) * Rg + rg) * In + o) * W;
+      for (int h = 0; h < Q; ++h) {
+        if (!ok[h]) continue;
+        const int o = orow[h];
+        if (p == 0) {
+          float2* d = Mc + o * lm + r0;
 #pragma unroll
-        for (int w = 0; w < W; ++w) d[w] = acc[w];
+          for (int w = 0; w < W; ++w)
+            if (r0 + w < R) d[w] = acc[h][w];
+        } else {
+          float2* d = part + ((size_t)((p - 1) * Rg + rg) * In + o) * W;
+#pragma unroll
+          for (int w = 0; w < W; ++w) d[w] = acc[h][w];
+        }
       }
     }
   }
   if (P > 1) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < In * R; e += blockDim.x) {
+    bar_sync(1, nthr);
+    for (int e = tid; e < In * R; e += nthr) {
       const int o = e / R, r = e - o * R, rg = r / W, w = r - rg * W;
       float2 sm2 = Mc[o * lm + r];
       for (int p = 1; p < P; ++p) merge2(sm2, part[((size_t)((p - 1) * Rg + rg) * In + o) * W + w]);
@@ -294,9 +345,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
                                 double* __restrict__ Gg, BatchCheck* __restrict__ chk, const SmemLayout& L,
                                 unsigned char* sm, double tol, int max_iter) {
   __shared__ double red[32];
-  __shared__ int s_p, s_stop;
-  __shared__ double s_pinv;
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   const int R = it.R, I0 = it.I[0], I1 = it.I[1], I2 = it.I[2];
   const int Rm = L.Rmax;
   const int lm = L.lm;
@@ -326,39 +375,41 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   double inner = 0.0;
   for (int n = 0; n < 3; ++n) {
     const int In = it.I[n];
-    // ---- MTTKRP from the mode's own layout of T (this mode's index fastest): mode 0 over
-    // (a, b) = (j, k), mode 1 over (i, k), mode 2 over (i, j); M as compensated FP32 pairs
-    // (same bytes as the FP64 array, float2 per entry)
+    // ---- MTTKRP (warps 0 .. nw-2) and, concurrently, V and its pivoted sweep (the last
+    // warp): V = G_a .* G_b needs only the other modes' Grams.
     float2* Mc = reinterpret_cast<float2*>(M);
-    {
+    if (warp < nwarps - 1) {
+      // MTTKRP from the mode's own layout of T (this mode's index fastest): mode 0 over
+      // (a, b) = (j, k), mode 1 over (i, k), mode 2 over (i, j); M as compensated FP32 pairs
+      // (same bytes as the FP64 array, float2 per entry)
       const int ma = (n == 0) ? 1 : 0, mb = (n == 2) ? 1 : 2;
       const float* Tn = T + it.loff[n];
       const float* Fa = F32 + (size_t)ma * L.Imax * Rm;
       const float* Fb = F32 + (size_t)mb * L.Imax * Rm;
       float2* part = reinterpret_cast<float2*>(X);
       float* ring = reinterpret_cast<float*>(sm + L.ring);
-      const int W = rank_width(R);
-      const int P = mttkrp_parts(In, (R + W - 1) / W, it.I[ma], it.I[mb]);
-      if (W == 8)
-        mttkrp_mode<8>(Tn, In, it.I[ma], it.I[mb], R, P, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes);
+      const MttkrpPlan pl = mttkrp_plan(In, it.I[ma], it.I[mb], R);
+      if (pl.W == 8 && pl.Q == 2)
+        mttkrp_mode<8, 2>(Tn, In, it.I[ma], it.I[mb], R, pl, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes, tid, nt - 32);
+      else if (pl.W == 8)
+        mttkrp_mode<8, 1>(Tn, In, it.I[ma], it.I[mb], R, pl, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes, tid, nt - 32);
+      else if (pl.Q == 2)
+        mttkrp_mode<4, 2>(Tn, In, it.I[ma], it.I[mb], R, pl, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes, tid, nt - 32);
       else
-        mttkrp_mode<4>(Tn, In, it.I[ma], it.I[mb], R, P, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes);
-    }
-    __syncthreads();
-    // ---- V = G_a .* G_b (mode order), upper triangle into A
-    const double* Ga = G + (size_t)(n == 0 ? 1 : 0) * R * R;
-    const double* Gb = G + (size_t)(n == 2 ? 1 : 2) * R * R;
-    for (int e = tid; e < R * R; e += nt) {
-      const int r = e / R, c = e - r * R;
-      if (c >= r) A[r * ld + c] = (1.0 * Ga[e]) * Gb[e];
-    }
-    __syncthreads();
-    // ---- pivoted symmetric sweep (same pivot rule and tolerance as dpstrf)
-    for (int i = tid; i < R; i += nt) vec[3 * Rm + i] = 0.0;  // swept flags
-    __syncthreads();
-    int rank = R;
-    for (int j = 0; j < R; ++j) {
-      if (warp == 0) {
+        mttkrp_mode<4, 1>(Tn, In, it.I[ma], it.I[mb], R, pl, Fa, Fb, Rm, Mc, lm, part, ring, L.ring_bytes, tid, nt - 32);
+    } else {
+      // V = G_a .* G_b (mode order), upper triangle into A
+      const double* Ga = G + (size_t)(n == 0 ? 1 : 0) * R * R;
+      const double* Gb = G + (size_t)(n == 2 ? 1 : 2) * R * R;
+      for (int e = lane; e < R * R; e += 32) {
+        const int r = e / R, c = e - r * R;
+        if (c >= r) A[r * ld + c] = (1.0 * Ga[e]) * Gb[e];
+      }
+      // pivoted symmetric sweep (same pivot rule and tolerance as dpstrf), by this warp alone
+      for (int i = lane; i < R; i += 32) vec[3 * Rm + i] = 0.0;  // swept flags
+      __syncwarp();
+      int rank = R;
+      for (int j = 0; j < R; ++j) {
         long long bk = LLONG_MIN;
         int bi = R;
         for (int i = lane; i < R; i += 32) {
@@ -374,45 +425,37 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
         const int mhi = __reduce_max_sync(0xffffffffu, khi);
         const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
         const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
-        const int p = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
-        if (lane == 0) {
-          const int stop = (mk == LLONG_MAX) || !(mk > bkey(kBatchTol)) || p >= R;
-          s_stop = stop;
-          s_p = p;
-          if (!stop) s_pinv = 1.0 / __longlong_as_double(mk);
+        const int k = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+        if ((mk == LLONG_MAX) || !(mk > bkey(kBatchTol)) || k >= R) {  // warp-uniform
+          rank = j;
+          break;
+        }
+        const double dk = 1.0 / __longlong_as_double(mk);
+        for (int i = lane; i < R; i += 32) {
+          const double av = (i <= k) ? A[i * ld + k] : A[k * ld + i];
+          a_row[i] = av;
+          t_row[i] = av * dk;
         }
         __syncwarp();
+        for (int c = lane; c < R; c += 32) {
+          const double tc = t_row[c];
+          for (int i = 0; i <= c; ++i) {
+            double v;
+            if (i == k && c == k) v = -dk;
+            else if (i == k) v = tc;
+            else if (c == k) v = t_row[i];
+            else v = fma(-a_row[i], tc, A[i * ld + c]);
+            A[i * ld + c] = v;
+          }
+        }
+        if (lane == 0) vec[3 * Rm + k] = 1.0;
+        __syncwarp();
       }
-      __syncthreads();
-      if (s_stop) {
-        rank = j;
-        break;
-      }
-      const int k = s_p;
-      const double dk = s_pinv;
-      for (int i = tid; i < R; i += nt) {
-        const double av = (i <= k) ? A[i * ld + k] : A[k * ld + i];
-        a_row[i] = av;
-        t_row[i] = av * dk;
-      }
-      __syncthreads();
-      for (int e = tid; e < R * R; e += nt) {
-        const int i = e / R, c = e - i * R;
-        if (c < i) continue;
-        double v;
-        if (i == k && c == k) v = -dk;
-        else if (i == k) v = t_row[c];
-        else if (c == k) v = t_row[i];
-        else v = fma(-a_row[i], t_row[c], A[i * ld + c]);
-        A[i * ld + c] = v;
-      }
-      if (tid == 0) vec[3 * Rm + k] = 1.0;
-      __syncthreads();
+      // W = -A on the swept indices.  A rank-deficient V (a pivot <= 1e-6) keeps the basic
+      // solution: the unswept components of X are zero (the reference's pivoted-QR
+      // fallback, ldiv_solve.jl:20-21, returns its least-squares solution instead)
+      if (rank < R && lane == 0) chk->rank_deficient += 1;
     }
-    // W = -A on the swept indices.  A rank-deficient V (a pivot <= 1e-6) keeps the basic
-    // solution: the unswept components of X are zero (the reference's pivoted-QR
-    // fallback, ldiv_solve.jl:20-21, returns its least-squares solution instead)
-    if (rank < R && tid == 0) chk->rank_deficient += 1;
     __syncthreads();
     // ---- X = M W: W(l, c) = -A(min, max) for swept l, c; 0 otherwise.  M is the MTTKRP's
     // FP32 pair m = mh + ml and W is split the same way (into the space of G_n, which is

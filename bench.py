@@ -60,6 +60,9 @@ def parse():
                          "QR-pivoted solvers' pivot factorizations of the 512^3 tensor's unfoldings")
     ap.add_argument("--profile-mttkrp", action="store_true",
                     help="only set up the workload and run one MTTKRP per mode (a small case for ncu)")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="c4: only one batched sweep launch over 152 tensors 56x56x56 at rank 18, "
+                         "512 threads per CTA (a small case for ncu)")
     return ap.parse_args()
 
 
@@ -548,6 +551,18 @@ def run_c4(args, pkg, device):
     from itensorcpd_gb300.synthetic import lowrank_plus_noise
 
     rng = np.random.default_rng(SEED + 4)
+    if args.profile_batched:
+        d, R, n = (56, 56, 56), 18, 152
+        T, _, _ = lowrank_plus_noise(d, R, 0.3, 30.0, rng)
+        F, lam = pkg.random_factors(d, R, rng)
+        nrm = float(np.linalg.norm(T.astype(np.float64)))
+        with pkg.BatchEngine([d] * n, [R] * n, [nrm] * n, device=device) as be:
+            be.set_tensors([T] * n)
+            be.set_threads(512)
+            be.set_factors([F] * n, [lam] * n)
+            be.optimize(tol=0.0, max_iter=1)
+        print(json.dumps({"profile_batched": "ok", "sweep_launches": 1}))
+        return
     count = args.c4_count
     dims, ranks, Ts, Fs, lams, norms = [], [], [], [], [], []
     for t in range(count):

@@ -360,7 +360,7 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   double* t_row = vec + 2 * Rm;
   const int ld = L.ld;
   double* F0g = Fg + it.foff;
-  const int64_t fo[3] = {0, (int64_t)I0 * R, (int64_t)(I0 + I1) * R};
+  const int64_t fo1 = (int64_t)I0 * R, fo2 = (int64_t)(I0 + I1) * R;
   double* lamg = Fg + it.foff + (int64_t)(I0 + I1 + I2) * R;
   // factors (FP32 copies, zero beyond column R) and Grams into shared memory
   for (int e = tid; e < 3 * L.Imax * Rm; e += nt) F32[e] = 0.f;
@@ -368,13 +368,14 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
   for (int m = 0; m < 3; ++m)
     for (int e = tid; e < it.I[m] * R; e += nt) {
       const int i = e % it.I[m], r = e / it.I[m];
-      F32[(size_t)m * L.Imax * Rm + (size_t)i * Rm + r] = (float)F0g[fo[m] + e];
+      F32[(size_t)m * L.Imax * Rm + (size_t)i * Rm + r] = (float)F0g[(m == 0 ? 0 : m == 1 ? fo1 : fo2) + e];
     }
   for (int e = tid; e < 3 * R * R; e += nt) G[e] = Gg[it.goff + e];
   __syncthreads();
   double inner = 0.0;
   for (int n = 0; n < 3; ++n) {
     const int In = it.I[n];
+    const int64_t fon = n == 0 ? 0 : n == 1 ? fo1 : fo2;
     // ---- MTTKRP (warps 0 .. nw-2) and, concurrently, V and its pivoted sweep (the last
     // warp): V = G_a .* G_b needs only the other modes' Grams.
     float2* Mc = reinterpret_cast<float2*>(M);
@@ -508,16 +509,22 @@ __device__ void batch_sweep_one(const BatchItem& it, const float* __restrict__ T
       double s = 0.0;
       for (int i = lane; i < In; i += 32) s = fma(X[i * lm + r], X[i * lm + r], s);
       for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-      if (lane == 0) lam[r] = sqrt(s);
+      if (lane == 0) {
+        const double l = sqrt(s);
+        lam[r] = l;
+        // one FP64 reciprocal per column (the FP64 divide is a long software sequence on this
+        // part's FP64 pipe); a column left at zero by a rank-deficient solve (basic solution)
+        // stays zero
+        t_row[r] = (l > 0.0) ? 1.0 / l : 0.0;
+      }
     }
     __syncthreads();
     float* Fn32 = F32 + (size_t)n * L.Imax * Rm;
     for (int e = tid; e < In * R; e += nt) {
       const int i = e / R, r = e - i * R;
-      // a column left at zero by a rank-deficient solve (basic solution) stays zero
-      const double f = (lam[r] > 0.0) ? X[i * lm + r] / lam[r] : 0.0;
+      const double f = X[i * lm + r] * t_row[r];
       X[i * lm + r] = f;
-      F0g[fo[n] + i + (int64_t)In * r] = f;
+      F0g[fon + i + (int64_t)In * r] = f;
       Fn32[i * Rm + r] = (float)f;
     }
     __syncthreads();

@@ -588,12 +588,14 @@ def run_c4(args, pkg, device):
         nt, tune_ms = be.autotune(Fs, lams, sweeps=2)
         sched, split_ms = be.schedule()
         runs = []
-        for _ in range(max(1, args.steps)):
-            be.set_factors(Fs, lams)
-            t1 = time.perf_counter()
-            sweeps, fits, flags, launches = be.optimize(tol=1e-5, max_iter=200)
-            runs.append(time.perf_counter() - t1)
+        with ClockSampler(device) as clk:
+            for _ in range(max(1, args.steps)):
+                be.set_factors(Fs, lams)
+                t1 = time.perf_counter()
+                sweeps, fits, flags, launches = be.optimize(tol=1e-5, max_iter=200)
+                runs.append(time.perf_counter() - t1)
         total_s = float(np.median(runs))
+        clocks = clk.summary()
         # end to end through the public API: tensors in, initial factors in, solve, factors out
         e2e_runs = []
         for _ in range(max(1, args.steps)):
@@ -611,6 +613,13 @@ def run_c4(args, pkg, device):
                           for sw, d, R in zip(sweeps, dims, ranks)))
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / total_s / 1e9
+    # the MTTKRP's FP32 FMAs (three modes, unpadded rank) against the SIMT FP32 rate at the
+    # sampled SM clock: the per-tensor MTTKRP runs on the FP32 pipe, not from HBM
+    import torch
+
+    mttkrp_flop = float(sum(int(sw) * 2 * 3 * int(np.prod(d)) * R for sw, d, R in zip(sweeps, dims, ranks)))
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    fp32_peak = sms * 128 * 2 * (clocks["sm_mhz"] or 2070.0) * 1e6 / 1e12
     # baselines on a bounded subset (the first 64 tensors): a host loop of the single-tensor
     # GPU engine (decompose per tensor, src/decompose.jl:1-30, FitCheck(1e-5, 200)), and the
     # CPU oracle (KRP-free normal-equation ALS, the reference default) on the first 16
@@ -648,6 +657,11 @@ def run_c4(args, pkg, device):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_kind,
                      "kernel": "k_batch_sweep (whole job: every sweep streams each tensor 3 times)"},
+        "fp32_mttkrp": {"achieved": mttkrp_flop / total_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": mttkrp_flop / total_s / 1e12 / fp32_peak,
+                        "what": "the MTTKRP's FP32 multiply-adds (3 modes x I0 I1 I2 R per sweep) over the whole "
+                                "job's time, against 128 FP32 FMA per clock per SM at the sampled SM clock"},
+        "clocks": clocks,
         "e2e": {"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(4 * elems + fac_bytes),
                 "d2h_bytes_per_step": int(fac_bytes)},
         "cpu_baseline": {"value": csub / cpu_s, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port",

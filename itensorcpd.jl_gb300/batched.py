@@ -105,6 +105,23 @@ class BatchEngine:
         L.check(self.lib.cpals_batch_get_factors(self.h, L.dptr(buf)), "cpals_batch_get_factors")
         return self.unpack_factors(buf)
 
+    def set_factors_concat(self, buf):
+        """The factors already packed (pack_factors' layout: per tensor F_0, F_1, F_2
+        column-major, then lambda) in one FP64 host buffer."""
+        if buf.dtype != np.float64 or not buf.flags.c_contiguous or buf.size != self._ftotal:
+            raise TypeError("expected one contiguous float64 buffer of the packed factors' size")
+        L.check(self.lib.cpals_batch_set_factors(self.h, L.dptr(buf)), "cpals_batch_set_factors")
+        self._factors_keep = buf
+
+    def get_factors_concat(self, out=None):
+        """The factors into one FP64 host buffer in pack_factors' layout (unpack_factors splits it)."""
+        if out is None:
+            out = np.empty(self._ftotal, dtype=np.float64)
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != self._ftotal:
+            raise TypeError("expected one contiguous float64 buffer of the packed factors' size")
+        L.check(self.lib.cpals_batch_get_factors(self.h, L.dptr(out)), "cpals_batch_get_factors")
+        return out
+
     def set_threads(self, threads):
         L.check(self.lib.cpals_batch_set_threads(self.h, int(threads)), "cpals_batch_set_threads")
 

@@ -67,8 +67,8 @@ struct SmemLayout {
 __host__ __device__ inline size_t al16(size_t b) { return (b + 15) & ~size_t(15); }
 
 // The MTTKRP's slab ring holds at least two steps of P slabs; P is chosen so that two steps
-// take at most this many bytes (two 96 x 96 FP32 slabs), or P = 1.
-constexpr int kRingBytes = 2 * 96 * 96 * 4;
+// take at most this many bytes, or P = 1 (two 96 x 96 FP32 slabs take 72 KB).
+constexpr int kRingBytes = 96 * 1024;
 
 // FP32 elements of one slab of a mode layout (In x Ia), padded to 16 bytes.
 __host__ __device__ inline int64_t slab_floats(int In, int Ia) { return (((int64_t)In * Ia + 3) / 4) * 4; }

@@ -139,3 +139,25 @@ def test_batched_rejects_bad_input(built):
         built.BatchEngine([(4, 5, 6)], [0], [1.0])
     with pytest.raises(Exception):
         built.BatchEngine([(4, 5, 6)], [3], [0.0])
+
+
+def test_batched_flat_buffers_match_lists(built, oracle):
+    # the flat-buffer calls (one packed FP64 host buffer each way) solve exactly as the lists do
+    dims, ranks, Ts, Fs, lams = make_batch(oracle, 12, seed=11)
+    norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    with built.BatchEngine(dims, ranks, norms) as be:
+        be.set_tensors(Ts)
+        be.set_factors(Fs, lams)
+        _, fits_l, _, _ = be.optimize(tol=0.0, max_iter=3)
+        out_l = be.get_factors()
+        buf = be.pack_factors(Fs, lams)
+        be.set_factors_concat(buf)
+        _, fits_c, _, _ = be.optimize(tol=0.0, max_iter=3)
+        flat = be.get_factors_concat()
+        with pytest.raises(TypeError):
+            be.set_factors_concat(buf[:-1])
+    assert np.array_equal(fits_l, fits_c)
+    for (Fa, la), (Fb, lb) in zip(out_l, be.unpack_factors(flat)):
+        assert np.array_equal(la, lb)
+        for a, b in zip(Fa, Fb):
+            assert np.array_equal(a, b)

@@ -273,7 +273,7 @@ __device__ __forceinline__ void mttkrp_mode(const float* __restrict__ Tn, int In
         for (int h = 0; h < Q; ++h)
 #pragma unroll
           for (int w = 0; w < W; ++w) t[h][w] = 0.f;
-#pragma unroll 4
+#pragma unroll 8
         for (int a = 0; a < Ia; ++a) {
           float sv[Q];
 #pragma unroll

@@ -1090,43 +1090,6 @@ __device__ __int128 block_sum_fx(__int128 q, long long* sl) {  // sl: 64 words
   __syncthreads();
   return t;
 }
-// Two of each at once (one set of block barriers instead of two).
-__device__ void block_max_int2(int& v1, int& v2, int* si) {  // si: 64 ints
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v1 = __reduce_max_sync(0xffffffffu, v1);
-  v2 = __reduce_max_sync(0xffffffffu, v2);
-  __syncthreads();
-  if (lane == 0) {
-    si[w] = v1;
-    si[32 + w] = v2;
-  }
-  __syncthreads();
-  v1 = __reduce_max_sync(0xffffffffu, (lane < nw) ? si[lane] : INT_MIN);
-  v2 = __reduce_max_sync(0xffffffffu, (lane < nw) ? si[32 + lane] : INT_MIN);
-  __syncthreads();
-}
-__device__ void block_sum_fx2(__int128& q1, __int128& q2, long long* sl) {  // sl: 128 words
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  q1 = fx_warp_sum(q1);
-  q2 = fx_warp_sum(q2);
-  __syncthreads();
-  if (lane == 0) {
-    sl[2 * w] = (long long)(unsigned long long)q1;
-    sl[2 * w + 1] = (long long)(q1 >> 64);
-    sl[64 + 2 * w] = (long long)(unsigned long long)q2;
-    sl[64 + 2 * w + 1] = (long long)(q2 >> 64);
-  }
-  __syncthreads();
-  __int128 t1 = 0, t2 = 0;
-  if (lane < nw) {
-    t1 = (__int128)(((unsigned __int128)(unsigned long long)sl[2 * lane + 1] << 64) | (unsigned long long)sl[2 * lane]);
-    t2 = (__int128)(((unsigned __int128)(unsigned long long)sl[64 + 2 * lane + 1] << 64) |
-                    (unsigned long long)sl[64 + 2 * lane]);
-  }
-  q1 = fx_warp_sum(t1);
-  q2 = fx_warp_sum(t2);
-  __syncthreads();
-}
 __device__ __forceinline__ __int128 fx_join(unsigned long long lo, long long hi) {
   return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
 }
@@ -1280,59 +1243,11 @@ __device__ void finalize_body(const double* __restrict__ Graw, int R, const Fina
 __device__ void finalize_fit(int R, const FinalizeArgs& fa, const double* lam) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int n = R * R;
-  __shared__ int si[64];
-  __shared__ long long sl[128];
-  const long long* ir = fa.inner_rows_fx;
-  if (fa.fpart && fa.In <= 4 * (int64_t)nt && fa.ntiles <= nt) {
-    // The fused tail's case, as below with every load issued up front (one round trip
-    // instead of four; the same sums)
-    unsigned long long rlo[4];
-    long long rhi[4];
-    int rbs[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int64_t i = tid + (int64_t)q * nt;
-      rbs[q] = INT_MIN;
-      if (i < fa.In) {
-        rlo[q] = (unsigned long long)__ldcg(&ir[3 * i]);
-        rhi[q] = __ldcg(&ir[3 * i + 1]);
-        rbs[q] = (int)__ldcg(&ir[3 * i + 2]);
-      }
-    }
-    const long long* fp = reinterpret_cast<const long long*>(fa.fpart);
-    unsigned long long tlo = 0;
-    long long thi = 0;
-    int tbs = INT_MIN;
-    if (tid < fa.ntiles) {
-      tlo = (unsigned long long)__ldcg(&fp[3 * tid]);
-      thi = __ldcg(&fp[3 * tid + 1]);
-      tbs = (int)__ldcg(&fp[3 * tid + 2]);
-    }
-    int bmax = max(max(rbs[0], rbs[1]), max(rbs[2], rbs[3])), m = tbs;
-    block_max_int2(bmax, m, si);
-    const int ib = (bmax == kFxBad) ? kFxBad : bmax + 8;
-    const int fb = (m == kFxBad) ? kFxBad : m + 8;
-    __int128 qi = 0, qf = 0;
-    if (ib != kFxBad)
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (rbs[q] != INT_MIN) qi += fx_align(fx_join(rlo[q], rhi[q]), rbs[q], ib);
-    if (fb != kFxBad && tid < fa.ntiles) qf = fx_align(fx_join(tlo, thi), tbs, fb);
-    block_sum_fx2(qi, qf, sl);
-    if (tid != 0) return;
-    DevCheck& k = *fa.chk;
-    k.inner_lo = (unsigned long long)qi;
-    k.inner_hi = (long long)(qi >> 64);
-    k.inner_base = ib;
-    k.fsq_lo = (unsigned long long)qf;
-    k.fsq_hi = (long long)(qf >> 64);
-    k.fsq_base = fb;
-    k.terms_ready = 1;
-    if (fa.run_check) check_update(k, fa.traj, fa.traj_cap);
-    return;
-  }
+  __shared__ int si[32];
+  __shared__ long long sl[64];
   // <T, X> = sum(M_N .* F_N .* lambda) = sum(M_N .* X_N)  (fit_check.jl:28): the rows' exact
   // fixed-point sums, aligned to the largest row base (+8: room for 2^36 rows) and added
+  const long long* ir = fa.inner_rows_fx;
   int bmax = INT_MIN;
   for (int64_t i = tid; i < fa.In; i += nt) bmax = max(bmax, (int)__ldcg(&ir[3 * i + 2]));
   bmax = block_max_int(bmax, si);
@@ -1703,29 +1618,16 @@ __global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
       c = r + (t - (R - p));
     }
   };
-  // On the last mode the block's share of ||X||^2 = sum over its entries of Graw .* prod_{m !=
-  // mode} G_m (off-diagonal entries twice), exact in fixed point below; the terms are formed
-  // as the entries are summed (up to 128 entries here; more take the reloading path)
-  constexpr int kShareMax = 128;
-  __shared__ double s_share[kShareMax];
-  const bool share_here = a.fa.last && e1 - e0 <= kShareMax;
   for (int eb = e0; eb < e1; eb += 32) {
     const int e = eb + lane;
     double acc = 0.0;
-    double gv[kMaxOrder];  // the other modes' Gram entries (1 elsewhere), loaded beside the partials
-    int r = 0, c = 0;
-    if (sl == 0 && e < e1) entry(e, r, c);
-    const bool gload = share_here && sl == 0 && e < e1;
-#pragma unroll
-    for (int m = 0; m < kMaxOrder; ++m)
-      gv[m] = (gload && m < a.fa.order && m != a.fa.mode) ? a.fa.gs.G[m][(size_t)r * R + c] : 1.0;
     if (e < e1)
-      for (int b0 = sl; b0 < nblk; b0 += 192) {  // 24 loads in flight, added in block order
-        double v[24];
+      for (int b0 = sl; b0 < nblk; b0 += 64) {  // eight loads in flight, added in block order
+        double v[8];
 #pragma unroll
-        for (int q = 0; q < 24; ++q) v[q] = (b0 + 8 * q < nblk) ? __ldcg(&a.gpart[(size_t)(b0 + 8 * q) * T + e]) : 0.0;
+        for (int q = 0; q < 8; ++q) v[q] = (b0 + 8 * q < nblk) ? __ldcg(&a.gpart[(size_t)(b0 + 8 * q) * T + e]) : 0.0;
 #pragma unroll
-        for (int q = 0; q < 24; ++q)
+        for (int q = 0; q < 8; ++q)
           if (b0 + 8 * q < nblk) acc += v[q];
       }
     red[sl][lane] = acc;
@@ -1733,6 +1635,8 @@ __global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
     if (sl == 0 && e < e1) {
       double sum = 0.0;
       for (int q = 0; q < 8; ++q) sum += red[q][lane];
+      int r, c;
+      entry(e, r, c);
       a.Graw[(size_t)r * R + c] = sum;
       a.Graw[(size_t)c * R + r] = sum;
       if (r == c) {
@@ -1740,25 +1644,21 @@ __global__ void __launch_bounds__(SOLVE_T) k_mode_tail(TailArgs a) {
         a.fa.lam[r] = sum * ri;
         a.fa.lam_inv[r] = ri;
       }
-      if (share_here) {
-        double g = 1.0;  // prod G_m in mode order (the factors of 1 are exact)
-#pragma unroll
-        for (int m = 0; m < kMaxOrder; ++m) g *= gv[m];
-        s_share[e - e0] = ((r == c) ? sum : 2.0 * sum) * g;
-      }
     }
     __syncthreads();
   }
   if (a.fa.last && sl == 0) {
+    // this block's share of ||X||^2 = sum over its entries of Graw .* prod_{m != mode} G_m
+    // (off-diagonal entries twice), exact in fixed point; each lane reads back the entries
+    // it wrote above
     auto share = [&](int e) {
-      if (share_here) return s_share[e - e0];
       int r, c;
       entry(e, r, c);
-      double g = 1.0;  // the same product as above: Graw (twice off the diagonal) times prod G_m
+      double v = a.Graw[(size_t)r * R + c];
+      v = (r == c) ? v : 2.0 * v;
       for (int m = 0; m < a.fa.order; ++m)
-        if (m != a.fa.mode) g *= a.fa.gs.G[m][(size_t)r * R + c];
-      const double v = a.Graw[(size_t)r * R + c];
-      return ((r == c) ? v : 2.0 * v) * g;
+        if (m != a.fa.mode) v *= a.fa.gs.G[m][(size_t)r * R + c];
+      return v;
     };
     int em = 1;
     for (int e = e0 + lane; e < e1; e += 32) em = max(em, fx_exp(share(e)));

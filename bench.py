@@ -60,6 +60,9 @@ def parse():
                          "QR-pivoted solvers' pivot factorizations of the 512^3 tensor's unfoldings")
     ap.add_argument("--profile-mttkrp", action="store_true",
                     help="only set up the workload and run one MTTKRP per mode (a small case for ncu)")
+    ap.add_argument("--lowmem", action="store_true",
+                    help="c2: the engine's low-memory mode (one shared tile-stream buffer, each mode's "
+                         "stream built just before its MTTKRP)")
     ap.add_argument("--profile-batched", action="store_true",
                     help="c4: only one batched sweep launch over 152 tensors 56x56x56 at rank 18, "
                          "512 threads per CTA (a small case for ncu)")
@@ -972,7 +975,7 @@ def main():
         c.ref_norm = ref_norm
         return c
 
-    eng = pkg.Engine(DIMS, RANK, dtype=np.float32, precision="bf16x3", device=device)
+    eng = pkg.Engine(DIMS, RANK, dtype=np.float32, precision="bf16x3", device=device, lowmem=args.lowmem)
     eng.set_tensor(T_host)
 
     def step():
@@ -1114,6 +1117,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "dims": list(DIMS), "rank": RANK, "congruence": CONGRUENCE,
                    "snr_db": SNR_DB, "sweeps_per_step": SWEEPS, "parallelism": f"replicas x{world}",
+                   "tile_streams": "one shared buffer, built per mode" if args.lowmem else "one per mode",
                    "l2": "inputs larger than L2 (BF16 planes 1.07 GB, FP32 tensor 537 MB)"},
         "final_fit": final_fit,
         "mttkrp": {"avg_launch_us": mt_avg_s * 1e6, "launches_timed": mt_n, "hbm_gbs": achieved,

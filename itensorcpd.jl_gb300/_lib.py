@@ -22,6 +22,7 @@ MTTKRP_FP64 = 0
 MTTKRP_BF16X3 = 1
 FLAG_NO_GRAPH = 1
 FLAG_DIMTREE = 2
+FLAG_LOWMEM = 4
 CHECK_NONE = 0
 CHECK_FIT = 1
 CHECK_DIFF = 2

@@ -171,6 +171,10 @@ cudaError_t enqueue_mttkrp(cpals_ctx* c, int n, const DevCheck* chk) {
   if (c->mmode == CPALS_MTTKRP_FP64)
     return launch_mttkrp_f64(c->dT, c->tdtype, factor_set(c), c->geom[n], c->R, c->splits[n], c->cps[n],
                              static_cast<double*>(c->part), chk, c->st);
+  // CPALS_FLAG_LOWMEM: mode n's tile stream is built into the shared buffer first
+  const int k = tc_prepare_mode(c->tc, n, c->st);
+  if (k < 0) return cudaErrorInvalidValue;
+  c->launches += k;
   return tc_launch_mttkrp(c->tc, n, static_cast<float*>(c->part), chk, c->st);
 }
 
@@ -547,6 +551,9 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   if (rank < 1 || rank > CPALS_MAX_RANK_SOLVE) return CPALS_E_ARG;
   if (tensor_dtype != CPALS_DTYPE_F64 && tensor_dtype != CPALS_DTYPE_F32) return CPALS_E_ARG;
   if (mttkrp_mode != CPALS_MTTKRP_FP64 && mttkrp_mode != CPALS_MTTKRP_BF16X3) return CPALS_E_ARG;
+  // the shared tile buffer belongs to the plain split-BF16 engine's tile streams
+  if ((flags & CPALS_FLAG_LOWMEM) && (mttkrp_mode != CPALS_MTTKRP_BF16X3 || (flags & CPALS_FLAG_DIMTREE)))
+    return CPALS_E_ARG;
   int64_t numel = 1, maxI = 0;
   for (int m = 0; m < order; ++m) {
     if (dims[m] < 1 || dims[m] > (int64_t(1) << 31)) return CPALS_E_ARG;
@@ -601,7 +608,7 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
       return rc;
     }
   } else if (mttkrp_mode == CPALS_MTTKRP_BF16X3) {
-    rc = tc_create(&c->tc, order, dims, R, tensor_dtype, c->num_sms);
+    rc = tc_create(&c->tc, order, dims, R, tensor_dtype, c->num_sms, ~0u, (flags & CPALS_FLAG_LOWMEM) != 0);
     if (rc != CPALS_OK) {
       cpals_destroy(c);
       return rc;

@@ -7,12 +7,18 @@ namespace cpals {
 struct TcState;
 
 // Plan the tensor-core MTTKRP for the modes of an order-`order` tensor set in `mode_mask`
-// (bit n = mode n); only those modes get a tile stream.
+// (bit n = mode n); only those modes get a tile stream.  `shared`: one buffer, the size of the
+// largest stream, holds the stream of the mode being computed (built by tc_prepare_mode).
 int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms,
-              unsigned mode_mask = ~0u);
+              unsigned mode_mask = ~0u, bool shared = false);
 void tc_destroy(TcState* s);
-// Split the (FP32 or FP64) tensor into BF16 hi/lo planes in the two layouts the kernel streams.
+// Split the (FP32 or FP64) tensor into BF16 hi/lo planes in the layouts the kernel streams
+// (with a shared buffer: only remember T, which must stay at its address).
 int tc_set_tensor(TcState* s, const void* T, cudaStream_t st);
+// With a shared buffer: build mode n's stream from the remembered tensor (stream-ordered before
+// the MTTKRP that reads it); otherwise nothing.  Returns the launches enqueued (0 or 1), or a
+// negative CPALS_E_* code.
+int tc_prepare_mode(TcState* s, int n, cudaStream_t st);
 // Split-K slices of mode n (partials are float [splits][I_n][R]).
 int tc_splits(const TcState* s, int n);
 // Device error word of the tensor-core kernel (0 = ok; non-zero = a bounded wait expired).

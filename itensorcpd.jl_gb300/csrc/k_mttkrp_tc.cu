@@ -463,12 +463,17 @@ struct TcState {
   const float* F32r[kMaxOrder] = {};
   int* err = nullptr;  // [2]: error code, spare (never set: bounded drain flag)
   size_t smem_bytes[kMaxOrder] = {};
+  bool shared = false;          // one buffer for every mode's stream, built per MTTKRP
+  uint8_t* shared_buf = nullptr;
+  const void* T = nullptr;      // the tensor the shared buffer's streams are built from
 };
 
-int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms, unsigned mode_mask) {
+int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdtype, int num_sms, unsigned mode_mask,
+              bool shared) {
   *out = nullptr;
   if (R > 512) return CPALS_E_UNSUPPORTED;
   TcState* s = new TcState();
+  s->shared = shared;
   s->order = order;
   s->tdtype = tdtype;
   s->num_sms = num_sms;
@@ -561,10 +566,20 @@ int tc_create(TcState** out, int order, const int64_t* dims, int64_t R, int tdty
     }
     s->smem_bytes[n] = ctl_bytes + p.ctl_off;
     s->tile_bytes[n] = (size_t)p.m_blocks * p.nchunks * (2 * kBlockM * kChunk * 2);
-    if (cudaMalloc(&s->tiles[n], s->tile_bytes[n]) != cudaSuccess) {
+    if (!shared && cudaMalloc(&s->tiles[n], s->tile_bytes[n]) != cudaSuccess) {
       tc_destroy(s);
       return CPALS_E_CUDA;
     }
+  }
+  if (shared) {
+    size_t mx = 0;
+    for (int n = 0; n < order; ++n) mx = std::max(mx, s->tile_bytes[n]);
+    if (mx == 0 || cudaMalloc(&s->shared_buf, mx) != cudaSuccess) {
+      tc_destroy(s);
+      return mx == 0 ? CPALS_E_ARG : CPALS_E_CUDA;
+    }
+    for (int n = 0; n < order; ++n)
+      if (s->tile_bytes[n]) s->tiles[n] = s->shared_buf;
   }
   for (int f = 0; f < 2; ++f) {
     bool used = false;  // is f the fastest reduction mode of a planned mode?
@@ -616,26 +631,42 @@ cudaError_t tc_update_factor(TcState* s, int m, const double* F, const DevCheck*
 
 void tc_destroy(TcState* s) {
   if (!s) return;
-  for (int m = 0; m < kMaxOrder; ++m) cudaFree(s->tiles[m]);
+  if (s->shared)
+    cudaFree(s->shared_buf);
+  else
+    for (int m = 0; m < kMaxOrder; ++m) cudaFree(s->tiles[m]);
   cudaFree(s->btiles[0]);
   cudaFree(s->btiles[1]);
   cudaFree(s->err);
   delete s;
 }
 
+static int build_mode(TcState* s, int n, const void* T, cudaStream_t st) {
+  const TcModePlan& p = s->plan[n];
+  if (!p.m_blocks) return 0;  // mode not planned
+  const int64_t ntiles = (int64_t)p.m_blocks * p.nchunks;
+  if (ntiles >= (int64_t(1) << 31)) return CPALS_E_UNSUPPORTED;
+  if (s->tdtype == CPALS_DTYPE_F64)
+    k_build_tiles<double><<<(unsigned)ntiles, 256, 0, st>>>(static_cast<const double*>(T), p, s->tiles[n]);
+  else
+    k_build_tiles<float><<<(unsigned)ntiles, 256, 0, st>>>(static_cast<const float*>(T), p, s->tiles[n]);
+  return cudaGetLastError() == cudaSuccess ? 1 : CPALS_E_CUDA;
+}
+
 int tc_set_tensor(TcState* s, const void* T, cudaStream_t st) {
+  s->T = T;
+  if (s->shared) return CPALS_OK;  // built per MTTKRP
   for (int n = 0; n < s->order; ++n) {
-    const TcModePlan& p = s->plan[n];
-    if (!p.m_blocks) continue;  // mode not planned
-    const int64_t ntiles = (int64_t)p.m_blocks * p.nchunks;
-    if (ntiles >= (int64_t(1) << 31)) return CPALS_E_UNSUPPORTED;
-    if (s->tdtype == CPALS_DTYPE_F64)
-      k_build_tiles<double><<<(unsigned)ntiles, 256, 0, st>>>(static_cast<const double*>(T), p, s->tiles[n]);
-    else
-      k_build_tiles<float><<<(unsigned)ntiles, 256, 0, st>>>(static_cast<const float*>(T), p, s->tiles[n]);
-    if (cudaGetLastError() != cudaSuccess) return CPALS_E_CUDA;
+    const int rc = build_mode(s, n, T, st);
+    if (rc < 0) return rc;
   }
   return CPALS_OK;
+}
+
+int tc_prepare_mode(TcState* s, int n, cudaStream_t st) {
+  if (!s->shared) return 0;
+  if (!s->T) return CPALS_E_STATE;
+  return build_mode(s, n, s->T, st);
 }
 
 int tc_splits(const TcState* s, int n) { return s->plan[n].splits; }

@@ -56,6 +56,8 @@ def test_create_rejects_bad_arguments_before_touching_a_device(lib):
     bad = (ctypes.c_int64 * 3)(4, 0, 6)
     assert lib.cpals_create(ctypes.byref(h), 0, 3, bad, 4, 0, 0, 0) == -1  # zero extent
     assert lib.cpals_create(None, 0, 3, dims, 4, 0, 0, 0) == -1
+    assert lib.cpals_create(ctypes.byref(h), 0, 3, dims, 4, 0, 0, 4) == -1  # low-memory tiles on FP64
+    assert lib.cpals_create(ctypes.byref(h), 0, 3, dims, 4, 0, 1, 4 | 2) == -1  # ... or on the dimension tree
     assert lib.cpals_destroy(None) == 0
 
 

@@ -216,3 +216,35 @@ def test_bf16x3_rank_deficient_normal_equations(built, oracle):
     fits = _tracking(built, T, F, lam, R, 3)
     assert np.all(np.isfinite(fits["bf16x3"])) and np.all(np.isfinite(fits["fp64"]))
     assert np.max(np.abs(fits["fp64"] - fits["bf16x3"])) < 1e-3
+
+
+def test_lowmem_engine_matches_the_per_mode_streams(built, oracle):
+    # CPALS_FLAG_LOWMEM builds each mode's tile stream into one shared buffer right before its
+    # MTTKRP: the same tiles and the same kernel, so the MTTKRPs and a whole graph-replayed
+    # FitCheck run equal the engine with one stream per mode bit for bit
+    rng = np.random.default_rng(8)
+    T, _, _ = oracle.lowrank_plus_noise((72, 60, 50), 8, 0.4, 25.0, rng)
+    F, lam = det_factors(T.shape, 8, seed=9)
+    out = {}
+    for low in (False, True):
+        chk = built.FitCheck(1e-7, 20, float(np.linalg.norm(T.astype(np.float64))))
+        with built.Engine(T.shape, 8, dtype=np.float32, precision="bf16x3", lowmem=low) as eng:
+            eng.set_tensor(T)
+            eng.set_factors(F, lam)
+            ms = [eng.mttkrp(n) for n in (2, 0, 1)]  # out of order: each call builds its own stream
+            fits = eng.optimize(built.api._to_device_check(chk))
+            Fo, lo = eng.get_factors()
+        out[low] = (ms, fits, Fo, lo)
+    for a, b in zip(out[False][0], out[True][0]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(out[False][1], out[True][1])
+    for a, b in zip(out[False][2], out[True][2]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(out[False][3], out[True][3])
+
+
+def test_lowmem_needs_the_plain_split_bf16_engine(built):
+    with pytest.raises(Exception):
+        built.Engine((8, 9, 10), 4, dtype=np.float32, precision="fp64", lowmem=True)
+    with pytest.raises(Exception):
+        built.Engine((8, 9, 10, 11), 4, dtype=np.float32, precision="bf16x3", dimtree=True, lowmem=True)

@@ -1118,7 +1118,7 @@ def main():
         "config": {"workload": WORKLOAD, "dims": list(DIMS), "rank": RANK, "congruence": CONGRUENCE,
                    "snr_db": SNR_DB, "sweeps_per_step": SWEEPS, "parallelism": f"replicas x{world}",
                    "tile_streams": "one shared buffer, built per mode" if args.lowmem else "one per mode",
-                   "l2": "inputs larger than L2 (BF16 planes 1.07 GB, FP32 tensor 537 MB)"},
+                   "l2": "inputs larger than L2 (each MTTKRP streams a 537 MB BF16 hi/lo tile stream; FP32 tensor 537 MB)"},
         "final_fit": final_fit,
         "mttkrp": {"avg_launch_us": mt_avg_s * 1e6, "launches_timed": mt_n, "hbm_gbs": achieved,
                    "tflops": flops / mt_avg_s / 1e12, "effective_tflops_3_products": 3 * flops / mt_avg_s / 1e12},

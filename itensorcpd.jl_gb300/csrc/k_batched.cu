@@ -50,7 +50,7 @@ struct BatchItem {
 struct BatchRun {  // the FitCheck parameters of the current optimize call (read by the sweep kernel)
   double tol;
   int max_iter;
-  int pad;
+  int sweeps_per_pull;  // sweeps a CTA runs on a tensor it pulls (stopping at its check); < 2: one
 };
 
 struct BatchCheck {  // fit_check.jl:5-20, per tensor
@@ -595,6 +595,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_batch_sweep(const BatchItem* _
   __shared__ int s_t;
   const double tol = run->tol;
   const int max_iter = run->max_iter;
+  const int spp = run->sweeps_per_pull > 1 ? run->sweeps_per_pull : 1;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_t = (int)atomicAdd(queue, 1u);
@@ -603,7 +604,12 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_batch_sweep(const BatchItem* _
     if (t >= count) break;
     const int id = order[t];
     if (chk[id].done) continue;
-    batch_sweep_one(items[id], T, F, G, &chk[id], L, sm, tol, max_iter);
+    // one sweep, or up to spp: each tensor's sweeps and check are its own, so running several
+    // back to back in one CTA gives the same results as one launch per sweep
+    for (int s = 0; s < spp; ++s) {
+      batch_sweep_one(items[id], T, F, G, &chk[id], L, sm, tol, max_iter);  // ends with a block barrier
+      if (*reinterpret_cast<volatile const int*>(&chk[id].done)) break;
+    }
   }
 }
 
@@ -984,7 +990,7 @@ int cpals_batch_create(cpals_batch** out, int device, int64_t count, const int64
     return CPALS_E_CUDA;
   }
   cudaMemcpy(b->d_items, b->items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice);
-  *b->h_run = BatchRun{b->tol, b->max_iter, 0};  // what the autotuner's sweeps use
+  *b->h_run = BatchRun{b->tol, b->max_iter, 1};  // what the autotuner's sweeps use
   cudaMemcpy(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_order, b->order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
   cudaMemset(b->d_queue, 0, sizeof(unsigned) * kMaxBatchClasses);
@@ -1079,23 +1085,35 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
   DeviceGuard guard(b->device);
   b->tol = tol;
   b->max_iter = max_iter;
-  *b->h_run = BatchRun{tol, max_iter, 0};
+  *b->h_run = BatchRun{tol, max_iter, 1};
   CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice, b->st));
   if (!b->graph) {
     int rc = build_graph(b);
     if (rc != CPALS_OK) return rc;
   }
+  // One launch per sweep while most tensors are active; once fewer than 60% are, the rest run
+  // to their own stop in one launch (a CTA sweeps the tensor it pulls until its check stops it):
+  // launch after launch with few active tensors would each last as long as its slowest tensor's
+  // sweep with most SMs idle.  The results are the same either way.
   int launched = 0, batch = 4;
   const int64_t l0 = b->launches;
   while (launched < max_iter) {
-    const int n = std::min(batch, max_iter - launched);
+    const bool tail = launched > 0 && *b->h_active < (int)(0.6 * (double)b->count);
+    if (tail) b->h_run->sweeps_per_pull = max_iter - launched;  // the previous copy completed at the sync
+    if (tail) CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice, b->st));
+    const int n = tail ? 1 : std::min(batch, max_iter - launched);
     for (int k = 0; k < n; ++k) CPALS_CUDA_TRY(cudaGraphLaunch(b->graph, b->st));
     b->launches += (int64_t)(b->cls.size() + 1) * n;
-    launched += n;
+    launched = tail ? max_iter : launched + n;
     CPALS_CUDA_TRY(cudaMemcpyAsync(b->h_active, b->d_active, sizeof(int), cudaMemcpyDeviceToHost, b->st));
     CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
     if (*b->h_active == 0) break;
     batch = std::min(batch * 2, 32);
+  }
+  if (b->h_run->sweeps_per_pull != 1) {  // one sweep per pull again (the autotuner's launches)
+    b->h_run->sweeps_per_pull = 1;
+    CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice, b->st));
+    CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
   }
   std::vector<BatchCheck> h(b->count);
   CPALS_CUDA_TRY(cudaMemcpy(h.data(), b->d_chk, sizeof(BatchCheck) * b->count, cudaMemcpyDeviceToHost));

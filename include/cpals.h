@@ -336,6 +336,10 @@ int cpals_batch_set_factors(cpals_batch* b, const double* host_concat);
 int cpals_batch_get_factors(cpals_batch* b, double* host_concat);
 /* Threads per CTA: 128, 256 or 512. */
 int cpals_batch_set_threads(cpals_batch* b, int threads);
+/* Sweeps per tensor in one launch of cpals_batch_optimize: 0 (the default) runs every tensor to
+ * its own stop in a single launch; k >= 1 launches k sweeps at a time (the host polls the
+ * active count between launches).  The results are the same either way. */
+int cpals_batch_set_sweeps_per_launch(cpals_batch* b, int k);
 /* Sweeps until every tensor's FitCheck(tol, max_iter) has stopped.  Per tensor: sweeps run,
  * final fit, flags (1 NaN fit, 2 rank-deficient normal equations met, 4 stopped). */
 int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_out, double* fits_out, int* flags_out,

@@ -107,6 +107,7 @@ SIGNATURES = {
     "cpals_batch_set_factors": (C.c_int, [_P, _DP]),
     "cpals_batch_get_factors": (C.c_int, [_P, _DP]),
     "cpals_batch_set_threads": (C.c_int, [_P, C.c_int]),
+    "cpals_batch_set_sweeps_per_launch": (C.c_int, [_P, C.c_int]),
     "cpals_batch_optimize": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(C.c_int), _DP, C.POINTER(C.c_int),
                                        _I64P]),
     "cpals_batch_autotune": (C.c_int, [_P, _DP, C.c_int, C.POINTER(C.c_int), _DP]),

@@ -125,6 +125,11 @@ class BatchEngine:
     def set_threads(self, threads):
         L.check(self.lib.cpals_batch_set_threads(self.h, int(threads)), "cpals_batch_set_threads")
 
+    def set_sweeps_per_launch(self, k):
+        """0 (default): optimize runs every tensor to its own stop in one launch; k >= 1: k
+        sweeps per launch, the active count polled between launches.  Same results."""
+        L.check(self.lib.cpals_batch_set_sweeps_per_launch(self.h, int(k)), "cpals_batch_set_sweeps_per_launch")
+
     def autotune(self, factors, lams, sweeps=2):
         buf = self.pack_factors(factors, lams)
         nt = C.c_int()

@@ -739,6 +739,7 @@ struct cpals_batch {
   int ctas_per_sm = 1;  // resident CTAs per SM (from the occupancy calculator)
   double tol = 1e-5;
   int max_iter = 200;
+  int sweeps_per_launch = 0;  // 0: every tensor to its own stop in one launch
   int num_sms = 0;
   SmemLayout L{};
   int64_t launches = 0;
@@ -1073,6 +1074,12 @@ int cpals_batch_get_factors(cpals_batch* b, double* host_concat) {
   return CPALS_OK;
 }
 
+int cpals_batch_set_sweeps_per_launch(cpals_batch* b, int k) {
+  if (!b || k < 0) return CPALS_E_ARG;
+  b->sweeps_per_launch = k;
+  return CPALS_OK;
+}
+
 int cpals_batch_set_threads(cpals_batch* b, int threads) {
   if (!b || (threads != 128 && threads != 256 && threads != 512)) return CPALS_E_ARG;
   DeviceGuard guard(b->device);
@@ -1085,26 +1092,25 @@ int cpals_batch_optimize(cpals_batch* b, double tol, int max_iter, int* sweeps_o
   DeviceGuard guard(b->device);
   b->tol = tol;
   b->max_iter = max_iter;
-  *b->h_run = BatchRun{tol, max_iter, 1};
+  // By default one launch runs every tensor to its own stop: a CTA sweeps the tensor it pulls
+  // until that tensor's check stops it.  Each tensor's sweeps and check are its own, so this
+  // gives the results of one launch per sweep; launches of one sweep each would last as long
+  // as the slowest active tensor's sweep, with most SMs idle once most tensors have stopped.
+  // With sweeps_per_launch = k >= 1, k sweeps per launch and the active count polled between.
+  const int spl = b->sweeps_per_launch > 0 ? std::min(b->sweeps_per_launch, max_iter) : max_iter;
+  *b->h_run = BatchRun{tol, max_iter, spl};
   CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice, b->st));
   if (!b->graph) {
     int rc = build_graph(b);
     if (rc != CPALS_OK) return rc;
   }
-  // One launch per sweep while most tensors are active; once fewer than 60% are, the rest run
-  // to their own stop in one launch (a CTA sweeps the tensor it pulls until its check stops it):
-  // launch after launch with few active tensors would each last as long as its slowest tensor's
-  // sweep with most SMs idle.  The results are the same either way.
-  int launched = 0, batch = 4;
+  int launched = 0, batch = (spl == max_iter) ? 1 : 4;
   const int64_t l0 = b->launches;
   while (launched < max_iter) {
-    const bool tail = launched > 0 && *b->h_active < (int)(0.6 * (double)b->count);
-    if (tail) b->h_run->sweeps_per_pull = max_iter - launched;  // the previous copy completed at the sync
-    if (tail) CPALS_CUDA_TRY(cudaMemcpyAsync(b->d_run, b->h_run, sizeof(BatchRun), cudaMemcpyHostToDevice, b->st));
-    const int n = tail ? 1 : std::min(batch, max_iter - launched);
+    const int n = std::min(batch, (max_iter - launched + spl - 1) / spl);
     for (int k = 0; k < n; ++k) CPALS_CUDA_TRY(cudaGraphLaunch(b->graph, b->st));
     b->launches += (int64_t)(b->cls.size() + 1) * n;
-    launched = tail ? max_iter : launched + n;
+    launched += n * spl;
     CPALS_CUDA_TRY(cudaMemcpyAsync(b->h_active, b->d_active, sizeof(int), cudaMemcpyDeviceToHost, b->st));
     CPALS_CUDA_TRY(cudaStreamSynchronize(b->st));
     if (*b->h_active == 0) break;

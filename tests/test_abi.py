@@ -69,6 +69,7 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.cpals_tensor_norm(None, None, None) == -1
     assert lib.cpals_check_converge(None, None, None, None) == -1
     assert lib.cpals_batch_set_norms(None, None) == -1
+    assert lib.cpals_batch_set_sweeps_per_launch(None, 0) == -1
     assert lib.cpals_mlp_forward(None, None, 1, None) == -1
 
 

@@ -163,13 +163,13 @@ def test_batched_flat_buffers_match_lists(built, oracle):
             assert np.array_equal(a, b)
 
 
-def test_batched_tail_runs_match_one_launch_per_sweep(built, oracle):
-    # Half the batch is exactly rank R and starts at its own factors (it stops within a few
-    # sweeps at tol 1e-3: near fit 1 the FP32-product fit terms jitter by ~1e-4, so a tighter
-    # tol would not stop it), so after the first poll fewer than 60% of the tensors are active
-    # and the rest finish inside one launch, each CTA sweeping its tensor to its own stop.  Each
-    # slow tensor alone (a batch of one: one launch per sweep throughout) gives the same sweeps,
-    # fits and factors, bit for bit (same thread count).
+def test_batched_one_launch_matches_one_launch_per_sweep(built, oracle):
+    # By default one launch runs every tensor to its own stop (a CTA sweeps the tensor it pulls
+    # until its check stops it); set_sweeps_per_launch(1) launches one sweep at a time and
+    # polls.  Each tensor's sweeps and check are its own, so sweeps, fits, flags and factors
+    # agree bit for bit.  Half the batch is exactly rank R and starts at its own factors (it
+    # stops within a few sweeps at tol 1e-3: near fit 1 the FP32-product fit terms jitter by
+    # ~1e-4, so a tighter tol would not stop it); the other half runs on.
     rng = np.random.default_rng(13)
     dims, ranks, Ts, Fs, lams = [], [], [], [], []
     for t in range(12):
@@ -188,25 +188,25 @@ def test_batched_tail_runs_match_one_launch_per_sweep(built, oracle):
         Fs.append(F)
         lams.append(lam)
     norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    res = {}
     with built.BatchEngine(dims, ranks, norms) as be:
         be.set_tensors(Ts)
         be.set_threads(256)
-        be.set_factors(Fs, lams)
-        sw, fits, flags, _ = be.optimize(tol=1e-3, max_iter=80)
-        out = be.get_factors()
-    print("sweeps:", sw)
-    assert np.sum(sw <= 4) >= 5  # over 40% stopped by the first poll (after four sweeps) ...
-    assert np.sum(sw > 6) >= 3   # ... and the rest ran on past it, in the tail launch
-    for t in range(12):
-        if sw[t] <= 4:
-            continue
-        with built.BatchEngine([dims[t]], [ranks[t]], [norms[t]]) as one:
-            one.set_tensors([Ts[t]])
-            one.set_threads(256)
-            one.set_factors([Fs[t]], [lams[t]])
-            sw1, fits1, flags1, _ = one.optimize(tol=1e-3, max_iter=80)
-            (F1, l1), = one.get_factors()
-        assert sw1[0] == sw[t] and fits1[0] == fits[t] and flags1[0] == flags[t], t
-        assert np.array_equal(l1, out[t][1])
-        for a, b in zip(F1, out[t][0]):
-            assert np.array_equal(a, b)
+        for k in (0, 1, 3):
+            be.set_sweeps_per_launch(k)
+            be.set_factors(Fs, lams)
+            sw, fits, flags, launches = be.optimize(tol=1e-3, max_iter=80)
+            res[k] = (sw, fits, flags, launches, be.get_factors())
+        with pytest.raises(Exception):
+            be.set_sweeps_per_launch(-1)
+    sw = res[0][0]
+    print("sweeps:", sw, "launches:", res[0][3], res[1][3], res[3][3])
+    assert np.sum(sw <= 4) >= 5 and np.sum(sw > 6) >= 3
+    assert res[0][3] < res[3][3] < res[1][3]
+    for k in (1, 3):
+        assert np.array_equal(res[k][0], sw) and np.array_equal(res[k][1], res[0][1])
+        assert np.array_equal(res[k][2], res[0][2])
+        for (Fa, la), (Fb, lb) in zip(res[k][4], res[0][4]):
+            assert np.array_equal(la, lb)
+            for x, y in zip(Fa, Fb):
+                assert np.array_equal(x, y)

@@ -50,6 +50,9 @@ extern "C" {
 /* ---- create flags ---- */
 #define CPALS_FLAG_NO_GRAPH 1 /* launch sweeps kernel by kernel instead of replaying a CUDA graph */
 #define CPALS_FLAG_DIMTREE 2  /* dimension-tree MTTKRP (order >= 3): two passes over T per sweep */
+#define CPALS_FLAG_FUSED_TAIL 8 /* per-mode tail (solve, Gram, lambda, normalisation, fit) as one cooperative
+                                  launch instead of three kernels; measured slower on GB300 (2341 against 2374
+                                  sweeps/s at 512^3 R=64, 1222 against 1249 at 128^4 R=128) */
 #define CPALS_FLAG_LOWMEM 4   /* split-BF16 engine: one tile stream buffer, each mode's stream built from T
                                  just before its MTTKRP (2x the tensor's bytes on the device instead of
                                  (N + 1)x; about 0.43 ms per GB of tensor per mode more) */

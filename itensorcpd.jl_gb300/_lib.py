@@ -23,6 +23,7 @@ MTTKRP_BF16X3 = 1
 FLAG_NO_GRAPH = 1
 FLAG_DIMTREE = 2
 FLAG_LOWMEM = 4
+FLAG_FUSED_TAIL = 8
 CHECK_NONE = 0
 CHECK_FIT = 1
 CHECK_DIFF = 2

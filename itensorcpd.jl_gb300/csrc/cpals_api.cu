@@ -684,10 +684,12 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   CK(dmalloc(&c->tail_err, 1));
   CPALS_CUDA_TRY(cudaMemset(c->gbar, 0, sizeof(GridBar)));
   CPALS_CUDA_TRY(cudaMemset(c->tail_err, 0, sizeof(int)));
-  {
+  if (flags & CPALS_FLAG_FUSED_TAIL) {  // opt-in: the three kernels measured faster
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
     c->fused_tail = coop != 0;
+  } else {
+    c->fused_tail = false;
   }
   CK(dmalloc(&c->chk, 1));
   CPALS_CUDA_TRY(cudaMemset(c->chk, 0, sizeof(DevCheck)));

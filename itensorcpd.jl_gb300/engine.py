@@ -41,10 +41,12 @@ class Engine:
     (tcgen05 split-BF16 MTTKRP with FP32 accumulation; FP64 Gram / solve / fit).
     ``lowmem`` (``"bf16x3"`` without ``dimtree``): one tile-stream buffer, each mode's stream
     built just before its MTTKRP, so the device holds twice the tensor instead of N + 1 times.
+    ``fused_tail``: each mode's tail as one cooperative launch instead of three kernels (the
+    three kernels measured faster; the results are the same to rounding).
     """
 
     def __init__(self, dims, rank, dtype=np.float64, precision="fp64", device=0, graph=True, dimtree=False,
-                 lowmem=False):
+                 lowmem=False, fused_tail=False):
         self.lib = L.load()
         self.dims = tuple(int(d) for d in dims)
         self.order = len(self.dims)
@@ -54,7 +56,8 @@ class Engine:
             raise TypeError(f"tensor element type must be float64 or float32, got {self.dtype}")
         self.precision = precision
         mm = {"fp64": L.MTTKRP_FP64, "bf16x3": L.MTTKRP_BF16X3}[precision]
-        flags = (0 if graph else L.FLAG_NO_GRAPH) | (L.FLAG_DIMTREE if dimtree else 0) | (L.FLAG_LOWMEM if lowmem else 0)
+        flags = ((0 if graph else L.FLAG_NO_GRAPH) | (L.FLAG_DIMTREE if dimtree else 0) | (L.FLAG_LOWMEM if lowmem else 0)
+                 | (L.FLAG_FUSED_TAIL if fused_tail else 0))
         d = np.asarray(self.dims, dtype=np.int64)
         h = C.c_void_p()
         tdt = L.DTYPE_F64 if self.dtype == np.float64 else L.DTYPE_F32

@@ -130,18 +130,26 @@ def test_mode_update_after_a_converged_optimize_still_updates(built):
         assert not np.array_equal(before[0], after[0])
 
 
-def test_a_sweep_runs_one_fused_tail_per_mode(built):
-    # per mode: the factorisation, the MTTKRP and one cooperative launch for the solve, the
-    # Gram, lambda and the normalisation (the fit included on the last mode)
+@pytest.mark.parametrize("fused,per_mode", [(True, 3), (False, 5)])
+def test_a_sweep_launches_per_mode(built, fused, per_mode):
+    # per mode: the factorisation, the MTTKRP, then either one cooperative launch for the
+    # solve, the Gram, lambda and the normalisation (the fit included on the last mode), or
+    # (the default) the solve, the Gram reduction with its finalize and the normalisation;
+    # both give the same fits to rounding
     from itensorcpd_gb300 import _lib as L
 
     dims, R = (40, 30, 20), 6
     T = np.asfortranarray(det_normal(8, dims))
     F0, lam0 = det_factors(dims, R, seed=8)
-    with built.Engine(dims, R) as e:
+    with built.Engine(dims, R, fused_tail=fused) as e:
         e.set_tensor(T)
         e.set_factors(F0, lam0)
         c = fitcheck(L, float(np.linalg.norm(T)), 3)
         l0 = e.launch_count()
-        e.optimize(c)
-        assert e.launch_count() - l0 == 3 * 3 * len(dims)
+        fits = e.optimize(c)
+        assert e.launch_count() - l0 == 3 * per_mode * len(dims)
+    with built.Engine(dims, R, fused_tail=not fused) as e:
+        e.set_tensor(T)
+        e.set_factors(F0, lam0)
+        other = e.optimize(fitcheck(L, float(np.linalg.norm(T)), 3))
+    assert np.max(np.abs(np.asarray(fits) - np.asarray(other))) < 1e-12

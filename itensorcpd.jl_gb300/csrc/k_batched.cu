@@ -1,23 +1,25 @@
 // Batched CP-ALS: thousands of small independent order-3 decompositions of uneven shape
-// and rank, one persistent kernel launch per ALS sweep.
+// and rank in one persistent kernel.
 //
 // Each CTA pulls tensor indices from a device work queue (largest tensors first) and runs
-// one full ALS sweep of that tensor in shared memory, with the reference's steps
+// ALS sweeps of that tensor in shared memory -- by default until the tensor's own check
+// stops it, or one (k) sweep(s) per launch -- with the reference's steps
 // (src/optimizers/als_optimizers/optimize.jl:15-32) for every mode n:
-//   M_n = T_(n) (F_b (.) F_a)          FP32 products, FP32 accumulation over one tensor
-//                                      slice, compensated FP32 pairs across slices
-//   V = G_a .* G_b                     FP64 (MttkrpAlgorithm.jl:18-31)
-//   X = M_n V^{-1}                     pivoted symmetric sweep of V (tol 1e-6) + compensated FP32 product
+//   M_n = T_(n) (F_b (.) F_a)          from the mode's own layout of T (slabs streamed through a
+//                                      shared-memory ring): FP32 products, FP32 sums within a
+//                                      slab, compensated FP32 pairs across slabs
+//   V = G_a .* G_b                     FP64 (MttkrpAlgorithm.jl:18-31), and its pivoted
+//                                      symmetric sweep (tol 1e-6) on one warp beside the MTTKRP
+//   X = M_n V^{-1}                     compensated FP32 (Dot2) product
 //   lambda, F_n = X / lambda, G_n      FP64 (row_norm.jl, standard/tensor.jl:46-49)
 // and after the last mode the fit and the tensor's own FitCheck (fit_check.jl:24-66).
-// Converged tensors are skipped by later launches.  The sweep is a CUDA graph (queue reset
-// + kernel); the host replays it in batches and polls the count of active tensors.
+// Converged tensors are skipped.  The launch is a CUDA graph (queue reset + kernel).
 //
-// Shared memory per CTA (Imax = largest mode size, Rmax = largest rank of the batch):
-//   slice   Imax^2 floats             one I0 x I1 slice of T
+// Shared memory per CTA (Imax = largest mode size, Rmax = largest rank of its tensors):
+//   ring    two or more steps of slabs (the MTTKRP's tensor stream)
 //   F32     3 Imax Rmax floats        the factors in FP32 (MTTKRP operands)
 //   M       Imax Rmax float pairs     MTTKRP result (hi + lo)
-//   X       Imax Rmax doubles         solve result
+//   X       Imax Rmax doubles         solve result (during the MTTKRP: partial pairs)
 //   A       Rmax (Rmax|1) doubles     V, swept in place into -V^{-1}
 //   G       3 Rmax^2 doubles          Grams
 //   vecs    6 Rmax doubles
@@ -169,7 +171,7 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
   return t;
 }
 
-// s + c += v, a compensated (Neumaier) FP32 sum: the MTTKRP's sums across slices stay off the
+// s + c += v, a compensated (Neumaier) FP32 sum: the MTTKRP's sums across slabs stay off the
 // FP64 pipe (2 operations per clock per SM on this part), at FP32-product accuracy
 __device__ __forceinline__ void acc2(float2& a, float v) {
   const float t = a.x + v;

@@ -2,7 +2,7 @@
 
 Each tensor of a batch of uneven shapes and ranks must follow the oracle's FP64 ALS from
 the same initial factors.  The batched MTTKRP multiplies FP32 tensor entries by FP32 factor
-copies with FP32 accumulation inside a slice (compensated FP32 pairs across slices), so per-sweep fits agree
+copies with FP32 accumulation inside a slab (compensated FP32 pairs across slabs), so per-sweep fits agree
 to ~1e-6 rather than FP64 rounding: the test bounds the final fit after a fixed number of
 sweeps by 2e-5, and FitCheck stopping sweeps by +-3 of the oracle's.
 """

@@ -210,3 +210,46 @@ def test_batched_one_launch_matches_one_launch_per_sweep(built, oracle):
             assert np.array_equal(la, lb)
             for x, y in zip(Fa, Fb):
                 assert np.array_equal(x, y)
+
+
+def test_batched_tiny_extents_follow_the_oracle(built, oracle):
+    # extents 1 to 4 and ranks 1 to 3: one-row slabs, more slab partitions than rows, rank
+    # groups wider than the rank
+    rng = np.random.default_rng(21)
+    dims, ranks, Ts, Fs, lams = [], [], [], [], []
+    for t in range(16):
+        d = tuple(int(x) for x in rng.integers(1, 5, size=3))
+        R = int(rng.integers(1, 4))
+        T = np.asfortranarray(rng.standard_normal(d)).astype(np.float32)
+        F, lam = det_factors(d, R, seed=500 + t)
+        dims.append(d)
+        ranks.append(R)
+        Ts.append(T)
+        Fs.append(F)
+        lams.append(lam)
+    norms = [float(np.linalg.norm(T.astype(np.float64))) for T in Ts]
+    with built.BatchEngine(dims, ranks, norms) as be:
+        be.set_tensors(Ts)
+        be.set_factors(Fs, lams)
+        sweeps, fits, flags, _ = be.optimize(tol=0.0, max_iter=5)
+    assert np.all(sweeps == 5) and not np.any(flags & 1) and np.all(np.isfinite(fits))
+    compared = 0
+    for t in range(len(Ts)):
+        chk = oracle.FitCheck(0.0, 5, norms[t])
+        oracle.als_optimize(Ts[t].astype(np.float64), Fs[t], lams[t], check=chk)
+        if flags[t] & 2:  # a rank-deficient V keeps the basic solution (the oracle's QR differs)
+            continue
+        if chk.trajectory[-1] > 0.999:
+            # an (almost) exactly rank-R tensor: near fit 1 the FP32-product fit terms cancel
+            # and the batch's fit carries ~1e-4 of jitter
+            assert abs(fits[t] - chk.trajectory[-1]) < 1e-3, (t, dims[t], ranks[t], fits[t])
+            continue
+        assert abs(fits[t] - chk.trajectory[-1]) < 2e-5, (t, dims[t], ranks[t], fits[t], chk.trajectory[-1])
+        compared += 1
+    assert compared >= 4
+
+
+def test_batched_refuses_a_tensor_beyond_shared_memory(built):
+    # a 160^3 tensor's per-CTA layout (slab ring, FP32 factors, M, X) exceeds 227 KB
+    with pytest.raises(Exception):
+        built.BatchEngine([(160, 160, 160)], [8], [1.0])

@@ -71,7 +71,8 @@ struct cpals_ctx {
   int64_t* dpiv = nullptr;
   int64_t piv_cap = 0;
   double* Scol = nullptr;
-  double* Srow = nullptr;
+  float2* Spair = nullptr;  // the samples' S as FP32 pairs (the compensated sampled products)
+  float2* Tpair = nullptr;  // T_s as FP32 pairs, for FP64 tensors
   void* Ts = nullptr;
   double* Spart = nullptr;
   size_t spart_cap = 0;
@@ -389,16 +390,19 @@ int ensure_sample_buffers(cpals_ctx* c, int64_t nsamps) {
   if (nsamps <= c->samp_cap) return CPALS_OK;
   cudaFree(c->dpiv);
   cudaFree(c->Scol);
-  cudaFree(c->Srow);
+  cudaFree(c->Spair);
+  cudaFree(c->Tpair);
   cudaFree(c->Ts);
   c->dpiv = nullptr;
-  c->Scol = c->Srow = nullptr;
+  c->Scol = nullptr;
+  c->Spair = c->Tpair = nullptr;
   c->Ts = nullptr;
   c->samp_cap = 0;
   const size_t esz = c->tdtype == CPALS_DTYPE_F64 ? 8 : 4;
   if (dmalloc(&c->dpiv, (size_t)nsamps * (c->order - 1)) || dmalloc(&c->Scol, (size_t)nsamps * c->R) ||
-      dmalloc(&c->Srow, (size_t)nsamps * c->R))
+      dmalloc(&c->Spair, (size_t)nsamps * c->R))
     return CPALS_E_CUDA;
+  if (c->tdtype == CPALS_DTYPE_F64 && dmalloc(&c->Tpair, (size_t)c->maxI * nsamps)) return CPALS_E_CUDA;
   char* ts = nullptr;
   if (dmalloc(&ts, (size_t)c->maxI * nsamps * esz)) return CPALS_E_CUDA;
   c->Ts = ts;
@@ -522,7 +526,8 @@ int cpals_destroy(cpals_ctx* c) {
   cudaFree(c->traj);
   cudaFree(c->dpiv);
   cudaFree(c->Scol);
-  cudaFree(c->Srow);
+  cudaFree(c->Spair);
+  cudaFree(c->Tpair);
   cudaFree(c->Ts);
   cudaFree(c->Spart);
   cudaFree(c->derr);
@@ -1756,19 +1761,10 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
                                        c->st));
   CPALS_CUDA_TRY(launch_fibers(c->dT, c->tdtype, c->order, mode, c->dims, c->dpiv, nsamps, c->Ts, c->derr, c->st));
   if (prof) CPALS_CUDA_TRY(cudaEventRecord(ev[2], c->st));
-  CPALS_CUDA_TRY(launch_colmajor_to_rowmajor(c->Scol, nsamps, R, c->Srow, c->st));
-  // A = S^T S (the Gram partial buffer holds up to max(gS2) splits)
-  const int s2 = std::min(gram_splits(nsamps, R, c->num_sms), *std::max_element(c->gS2, c->gS2 + c->order));
-  CPALS_CUDA_TRY(launch_gram(c->Srow, nsamps, R, s2, c->gpart, c->gcnt, c->Graw, nullptr, c->st));
-  GramSet one{};
-  one.G[0] = c->Graw;
-  CPALS_CUDA_TRY(launch_factorize(one, 1, -1, R, c->work, c->U, c->piv, c->W, c->info, nullptr, c->st));
-  // B = T_s S : an order-2 FP64 MTTKRP of T_s (In x nsamps) with the factor S
-  const int64_t d2[2] = {In, nsamps};
-  const ModeGeom g2 = make_geom(2, d2, 0, 32);
-  int64_t cps = 0;
-  const int sp = mttkrp_f64_splits(g2, R, c->num_sms, &cps);
-  const size_t need = (size_t)sp * In * R;
+  // A = S^T S and the split-K partials of B = T_s S, both as compensated FP32 (Dot2) products
+  // summed into FP64 (FP64 runs some 60 times slower than FP32 on this part)
+  const int sp = sampled_splits(nsamps);
+  const size_t need = (size_t)sp * std::max<int64_t>(In, R) * R;
   if (need > c->spart_cap) {
     cudaFree(c->Spart);
     c->Spart = nullptr;
@@ -1776,11 +1772,13 @@ int cpals_sampled_update(cpals_ctx* c, int mode, const int64_t* pivots, int64_t 
     if (dmalloc(&c->Spart, need) != CPALS_OK) return CPALS_E_CUDA;
     c->spart_cap = need;
   }
-  FactorSet fs2{};
-  fs2.F[0] = nullptr;
-  fs2.F[1] = c->Srow;
-  CPALS_CUDA_TRY(launch_mttkrp_f64(c->Ts, c->tdtype, fs2, g2, R, sp, cps, c->Spart, nullptr, c->st));
-  CPALS_CUDA_TRY(launch_solve_rows(c->Spart, 0, sp, In, R, c->work, c->U, c->piv, c->W, c->info, c->X, nullptr,
+  CPALS_CUDA_TRY(launch_sampled_gram(c->Scol, nsamps, R, c->Spair, c->Spart, c->Graw, c->st));
+  GramSet one{};
+  one.G[0] = c->Graw;
+  CPALS_CUDA_TRY(launch_factorize(one, 1, -1, R, c->work, c->U, c->piv, c->W, c->info, nullptr, c->st));
+  int sp_rhs = 0;
+  CPALS_CUDA_TRY(launch_sampled_rhs(c->Ts, c->tdtype, In, nsamps, R, c->Spair, c->Tpair, c->Spart, &sp_rhs, c->st));
+  CPALS_CUDA_TRY(launch_solve_rows(c->Spart, 0, sp_rhs, In, R, c->work, c->U, c->piv, c->W, c->info, c->X, nullptr,
                                    nullptr, c->st));
   // row_norm, Gram refresh, FP32 copy
   CPALS_CUDA_TRY(launch_gram(c->X, In, R, c->gS2[mode], c->gpart, c->gcnt, c->Graw, nullptr, c->st));

@@ -280,6 +280,15 @@ cudaError_t launch_pivot_hadamard(const FactorSet& fs, int order, int mode, cons
 cudaError_t launch_fibers(const void* T, int tdtype, int order, int mode, const int64_t* dims, const int64_t* piv,
                           int64_t nsamps, void* out, int* err, cudaStream_t st);
 cudaError_t launch_colmajor_to_rowmajor(const double* src, int64_t rows, int R, double* dst, cudaStream_t st);
+// The sampled system's products as compensated FP32 (Dot2) sums: G = S^T S from the column-major
+// nsamps x R S (split into pairs Spair), and the split-K partials part[splits][In][R] of T_s S
+// (T_s column-major In x nsamps, FP32 or FP64; Tpair: In x nsamps pairs for FP64 T_s).  part:
+// sampled_splits(nsamps) x max(R, In) x R doubles.
+int sampled_splits(int64_t nsamps);
+cudaError_t launch_sampled_gram(const double* Scol, int64_t nsamps, int R, float2* Spair, double* part, double* G,
+                                cudaStream_t st);
+cudaError_t launch_sampled_rhs(const void* Ts, int tdtype, int64_t In, int64_t nsamps, int R, const float2* Spair,
+                               float2* Tpair, double* part, int* splits_out, cudaStream_t st);
 cudaError_t launch_leverage_rows(const double* F, int64_t In, int R, const double* work, const double* U,
                                  const int* piv, const SolveInfo* info, double scale, double* probs, cudaStream_t st);
 

@@ -70,6 +70,111 @@ __global__ void k_fibers(const TT* __restrict__ T, int order, int mode, Dims dm,
 }
 
 // row-major copy of a column-major nsamps x R matrix (for the Gram / MTTKRP of the sampled solve)
+// ---------------- the sampled system's products in compensated FP32 (Dot2)
+// This part issues FP64 some 60 times slower than FP32, so S^T S and T_s S (2 x 16384 x 128^2
+// multiply-adds per mode update at 128^4 R = 128, 16384 samples) run as Dot2 products (Ogita,
+// Rump & Oishi 2005): each FP64 operand is split once into an FP32 pair hi + lo (exact to
+// 2^-48), each term's leading product split exactly by one FMA and added with TwoSum, the
+// cross terms in FP32; a sum stays a pair until it is written as one FP64 partial.
+
+// x = hi + lo (FP32 pairs) of an FP64 array
+__global__ void k_split_pairs(const double* __restrict__ x, int64_t n, float2* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[e];
+    const float h = (float)v;
+    out[e] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+__device__ __forceinline__ float2 pair_of(float v) { return make_float2(v, 0.f); }
+__device__ __forceinline__ float2 pair_of(float2 v) { return v; }
+
+// s + c += a b for pairs a, b (the _rn intrinsics keep the compiler from contracting the
+// error-free steps into FMAs)
+__device__ __forceinline__ void dot2_acc(float& s, float& c, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = fmaf(ah, bh, -p);
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  s = t;
+  c += (e + r) + fmaf(ah, bl, al * bh);
+}
+
+// part[y][m][n] = sum over k in split y of A(k, m) B(k, n), A(k, m) = A[k lak + m lam] and
+// B(k, n) = B[k lbk + n lbn] (FP32 pairs, or FP32 values with a zero lo); 32 x 32 output tiles
+// (blockIdx.x), splits of kchunk (blockIdx.y); with `upper` only tiles on or above the
+// diagonal.  256 threads, each 2 x 2 outputs; 32-deep K steps staged in shared memory.
+template <typename TA>
+__global__ void __launch_bounds__(256) k_dot2_atb(const TA* __restrict__ A, int64_t lak, int64_t lam,
+                                                   const float2* __restrict__ B, int64_t lbk, int64_t lbn, int64_t K,
+                                                   int M, int N, int64_t kchunk, int upper, double* __restrict__ part) {
+  __shared__ float Ah[32][33], Al[32][33], Bh[32][33], Bl[32][33];  // [k][m], [k][n]
+  const int tiles_n = (N + 31) / 32;
+  const int mb = blockIdx.x / tiles_n, nb = blockIdx.x % tiles_n;
+  if (upper && mb > nb) return;  // uniform over the block
+  const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+  const int64_t k1 = (K < k0 + kchunk) ? K : k0 + kchunk;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float s[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, c[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  for (int64_t kk = k0; kk < k1; kk += 32) {
+    for (int e = threadIdx.x; e < 1024; e += 256) {
+      // the index that is contiguous in memory runs across consecutive threads
+      int kl, ml;
+      if (lak == 1) {
+        kl = e & 31, ml = e >> 5;
+      } else {
+        ml = e & 31, kl = e >> 5;
+      }
+      const int64_t k = kk + kl;
+      const int m = mb * 32 + ml;
+      const float2 a = (k < k1 && m < M) ? pair_of(A[k * lak + (int64_t)m * lam]) : make_float2(0.f, 0.f);
+      Ah[kl][ml] = a.x;
+      Al[kl][ml] = a.y;
+      int kb, nl;
+      if (lbk == 1) {
+        kb = e & 31, nl = e >> 5;
+      } else {
+        nl = e & 31, kb = e >> 5;
+      }
+      const int64_t kq = kk + kb;
+      const int n = nb * 32 + nl;
+      const float2 b = (kq < k1 && n < N) ? B[kq * lbk + (int64_t)n * lbn] : make_float2(0.f, 0.f);
+      Bh[kb][nl] = b.x;
+      Bl[kb][nl] = b.y;
+    }
+    __syncthreads();
+    const int kn = (k1 - kk < 32) ? (int)(k1 - kk) : 32;
+    for (int kl = 0; kl < kn; ++kl) {
+      const float a0h = Ah[kl][2 * ty], a0l = Al[kl][2 * ty], a1h = Ah[kl][2 * ty + 1], a1l = Al[kl][2 * ty + 1];
+      const float b0h = Bh[kl][2 * tx], b0l = Bl[kl][2 * tx], b1h = Bh[kl][2 * tx + 1], b1l = Bl[kl][2 * tx + 1];
+      dot2_acc(s[0][0], c[0][0], a0h, a0l, b0h, b0l);
+      dot2_acc(s[0][1], c[0][1], a0h, a0l, b1h, b1l);
+      dot2_acc(s[1][0], c[1][0], a1h, a1l, b0h, b0l);
+      dot2_acc(s[1][1], c[1][1], a1h, a1l, b1h, b1l);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int m = mb * 32 + 2 * ty + i, n = nb * 32 + 2 * tx + j;
+      if (m < M && n < N) part[((size_t)blockIdx.y * M + m) * N + n] = (double)s[i][j] + (double)c[i][j];
+    }
+}
+
+// G = the splits' partials summed in split order, the upper triangle mirrored
+__global__ void k_reduce_gram_splits(const double* __restrict__ part, int splits, int R, double* __restrict__ G) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < R * R; e += gridDim.x * blockDim.x) {
+    const int a = e / R, b = e - a * R;
+    const int src = (a <= b) ? a * R + b : b * R + a;
+    double v = 0.0;
+    for (int y = 0; y < splits; ++y) v += part[(size_t)y * R * R + src];
+    G[e] = v;
+  }
+}
+
 __global__ void k_colmajor_to_rowmajor(const double* __restrict__ src, int64_t rows, int R, double* __restrict__ dst) {
   const int64_t n = rows * R;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
@@ -155,6 +260,45 @@ cudaError_t launch_colmajor_to_rowmajor(const double* src, int64_t rows, int R, 
   const int64_t n = rows * R;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, 8192);
   k_colmajor_to_rowmajor<<<blocks, 256, 0, st>>>(src, rows, R, dst);
+  return cudaGetLastError();
+}
+
+// Splits of the sampled products' K range (the samples): about 512 samples each, at least one.
+int sampled_splits(int64_t nsamps) { return (int)std::max<int64_t>(1, std::min<int64_t>(64, (nsamps + 511) / 512)); }
+
+cudaError_t launch_sampled_gram(const double* Scol, int64_t nsamps, int R, float2* Spair, double* part, double* G,
+                                cudaStream_t st) {
+  const int64_t n = nsamps * R;
+  k_split_pairs<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(Scol, n, Spair);
+  const int sp = sampled_splits(nsamps);
+  const int64_t kchunk = (nsamps + sp - 1) / sp;
+  const int tiles = ((R + 31) / 32) * ((R + 31) / 32);
+  // S^T S: A = B = S, S(s, r) at s + nsamps r (column-major)
+  k_dot2_atb<float2><<<dim3((unsigned)tiles, (unsigned)sp), 256, 0, st>>>(Spair, 1, nsamps, Spair, 1, nsamps, nsamps, R,
+                                                                          R, kchunk, 1, part);
+  k_reduce_gram_splits<<<(R * R + 255) / 256, 256, 0, st>>>(part, sp, R, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sampled_rhs(const void* Ts, int tdtype, int64_t In, int64_t nsamps, int R, const float2* Spair,
+                               float2* Tpair, double* part, int* splits_out, cudaStream_t st) {
+  const int sp = sampled_splits(nsamps);
+  const int64_t kchunk = (nsamps + sp - 1) / sp;
+  const int tiles = (int)(((In + 31) / 32) * ((R + 31) / 32));
+  if (In > INT_MAX) return cudaErrorInvalidValue;
+  // T_s S: A = T_s (i, s) at i + In s, B = S
+  if (tdtype == CPALS_DTYPE_F64) {
+    const int64_t n = In * nsamps;
+    k_split_pairs<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(static_cast<const double*>(Ts), n,
+                                                                                  Tpair);
+    k_dot2_atb<float2><<<dim3((unsigned)tiles, (unsigned)sp), 256, 0, st>>>(Tpair, In, 1, Spair, 1, nsamps, nsamps,
+                                                                            (int)In, R, kchunk, 0, part);
+  } else {
+    k_dot2_atb<float><<<dim3((unsigned)tiles, (unsigned)sp), 256, 0, st>>>(static_cast<const float*>(Ts), In, 1, Spair,
+                                                                           1, nsamps, nsamps, (int)In, R, kchunk, 0,
+                                                                           part);
+  }
+  *splits_out = sp;
   return cudaGetLastError();
 }
 

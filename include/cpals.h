@@ -272,6 +272,10 @@ int cpals_profile_read(cpals_ctx* ctx, double* mttkrp_ms, int64_t* launches);
 int cpals_profile_read_sampled(cpals_ctx* ctx, double* update_ms, double* gather_ms, int64_t* updates);
 /* Kernel launches enqueued by this handle so far (every libcpals kernel). */
 int cpals_launch_count(cpals_ctx* ctx, int64_t* launches);
+/* Smallest rank whose FP64 factorisation (pivoted Cholesky / sweep of the normal equations)
+ * runs over a cluster of CTAs instead of one CTA; both give bit-identical results.  Process
+ * wide; a value above 256 keeps every factorisation on one CTA.  Returns the previous value. */
+int cpals_set_cluster_sweep_min_rank(int min_rank);
 
 /* ---- MTTKRP without any allocation (no counterpart in the reference) ---- */
 

@@ -92,6 +92,7 @@ SIGNATURES = {
     "cpals_set_profiling": (C.c_int, [_P, C.c_int]),
     "cpals_profile_read": (C.c_int, [_P, _DP, _I64P]),
     "cpals_launch_count": (C.c_int, [_P, _I64P]),
+    "cpals_set_cluster_sweep_min_rank": (C.c_int, [C.c_int]),
     "cpals_mttkrp_fp64_noalloc": (C.c_int, [C.c_int, _I64P, C.c_int64, C.c_int, C.c_int, _P, C.POINTER(_DP), _DP,
                                             _P]),
     "cpals_mode_update": (C.c_int, [_P, C.c_int, _DP]),

@@ -254,7 +254,7 @@ int enqueue_mode(cpals_ctx* c, int n, int run_check) {
     CPALS_CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_main[n], 0));
     const int mixed = (c->mmode == CPALS_MTTKRP_BF16X3 && R <= 128) ? 1 : 0;
     CPALS_CUDA_TRY(launch_factorize(gs, N, n, R, c->work, c->U, c->piv, c->W, c->info, c->chk, c->side, mixed));
-    c->launches += 2 * mixed;  // V for the FP32 sweep, the FP32 sweep
+    c->launches += factorize_launches(R, mixed) - 1;  // the FP32 sweep and its V, or the cluster sweep
     CPALS_CUDA_TRY(cudaEventRecord(c->ev_side[n], c->side));
     const bool prof = c->profiling && c->prof_used + 2 <= (int64_t)c->prof_ev.size();
     if (prof) CPALS_CUDA_TRY(cudaEventRecord(c->prof_ev[c->prof_used], c->st));
@@ -1693,6 +1693,8 @@ int cpals_profile_read(cpals_ctx* c, double* mttkrp_ms, int64_t* launches) {
   *launches = c->prof_used / 2;
   return CPALS_OK;
 }
+
+int cpals_set_cluster_sweep_min_rank(int min_rank) { return set_cluster_sweep_min_rank(min_rank); }
 
 int cpals_launch_count(cpals_ctx* c, int64_t* launches) {
   if (!c || !launches) return CPALS_E_ARG;

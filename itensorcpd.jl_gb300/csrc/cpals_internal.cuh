@@ -162,6 +162,7 @@ struct SolveInfo {
   int qr_rank;   // numerical rank found by the QR path
   int refine;    // 1: the FP32 sweep's inverse W and V = V_hi + V_lo (FP32) are in the
                  // workspace; the solve refines X once with the residual M - X V
+  int swept;     // 1: the cluster sweep factorised V at full rank (W, U, dinv, piv written)
 };
 
 // ---- launchers (defined in the kernel translation units) ----
@@ -179,6 +180,11 @@ cudaError_t launch_mttkrp_f64(const void* T, int tdtype, const FactorSet& fs, co
 cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, double* work, double* U, int* piv,
                              double* W, SolveInfo* info, DevCheck* chk, cudaStream_t st, int mixed = 0);
 size_t factorize_work_doubles(int R);
+// kernels one launch_factorize issues; the cluster size of the FP64 sweep at rank R (0: one
+// CTA); the smallest rank given to the cluster sweep (process-wide, returns the previous)
+int factorize_launches(int R, int mixed);
+int cluster_sweep_size(int R);
+int set_cluster_sweep_min_rank(int r);
 
 // Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and
 // (optionally) per-row sums of M .* X for the fit, exact in fixed point (three words per row).  `work` is the factorize workspace.

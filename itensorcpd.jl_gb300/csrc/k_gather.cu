@@ -184,41 +184,54 @@ __global__ void k_colmajor_to_rowmajor(const double* __restrict__ src, int64_t r
   }
 }
 
-// leverage scores: warp per row, forward substitution with the pivoted Cholesky factor of F^T F
-template <int RQ>
+// leverage scores: warp per row, forward substitution with the pivoted Cholesky factor of F^T F.
+// With STAGED, U and dinv are first copied into shared memory (R <= 128) and the warps of a
+// grid of at most one block per SM stride over the rows: the substitution's R dependent
+// steps then wait on shared-memory loads instead of L2 round trips.
+template <int RQ, bool STAGED>
 __global__ void k_leverage_rows(const double* __restrict__ F, int64_t In, int R, const double* __restrict__ U,
                                 const double* __restrict__ dinv, const int* __restrict__ piv,
                                 const SolveInfo* __restrict__ info, double scale, double* __restrict__ probs) {
+  extern __shared__ double lsm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  const int64_t row = (int64_t)blockIdx.x * wpb + warp;
-  if (row >= In) return;
   const int rank = info->rank;
-  double t[RQ];
-#pragma unroll
-  for (int q = 0; q < RQ; ++q) {
-    const int j = lane + 32 * q;
-    t[q] = (j < rank) ? F[row * R + piv[j]] : 0.0;
+  const double* Us = U;
+  const double* ds = dinv;
+  if (STAGED) {
+    for (int e = threadIdx.x; e < rank * R; e += blockDim.x) lsm[e] = U[e];
+    for (int e = threadIdx.x; e < rank; e += blockDim.x) lsm[R * R + e] = dinv[e];
+    __syncthreads();
+    Us = lsm;
+    ds = lsm + R * R;
   }
-  for (int k = 0; k < rank; ++k) {
-    const int qk = k >> 5, owner = k & 31;
-    double tk = 0.0;
-#pragma unroll
-    for (int q = 0; q < RQ; ++q)
-      if (q == qk) tk = t[q];
-    const double c = __shfl_sync(0xffffffffu, tk * dinv[k], owner);
-    const double* Uk = U + (size_t)k * R;
+  for (int64_t row = (int64_t)blockIdx.x * wpb + warp; row < In; row += (int64_t)gridDim.x * wpb) {
+    double t[RQ];
 #pragma unroll
     for (int q = 0; q < RQ; ++q) {
       const int j = lane + 32 * q;
-      if (j == k) t[q] = c;
-      else if (j > k && j < rank) t[q] = fma(-c, Uk[j], t[q]);
+      t[q] = (j < rank) ? F[row * R + piv[j]] : 0.0;
     }
-  }
-  double s = 0.0;
+    for (int k = 0; k < rank; ++k) {
+      const int qk = k >> 5, owner = k & 31;
+      double tk = 0.0;
 #pragma unroll
-  for (int q = 0; q < RQ; ++q) s = fma(t[q], t[q], s);
-  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-  if (lane == 0) probs[row] = s * scale;
+      for (int q = 0; q < RQ; ++q)
+        if (q == qk) tk = t[q];
+      const double c = __shfl_sync(0xffffffffu, tk * ds[k], owner);
+      const double* Uk = Us + (size_t)k * R;
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        const int j = lane + 32 * q;
+        if (j == k) t[q] = c;
+        else if (j > k && j < rank) t[q] = fma(-c, Uk[j], t[q]);
+      }
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) s = fma(t[q], t[q], s);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) probs[row] = s * scale;
+  }
 }
 
 Dims make_dims(int order, const int64_t* dims) {
@@ -305,17 +318,34 @@ cudaError_t launch_sampled_rhs(const void* Ts, int tdtype, int64_t In, int64_t n
 cudaError_t launch_leverage_rows(const double* F, int64_t In, int R, const double* work, const double* U,
                                  const int* piv, const SolveInfo* info, double scale, double* probs, cudaStream_t st) {
   const double* dinv = work + (size_t)R * R;
+  const int rq = (R + 31) / 32;
+  if (R <= 128) {
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int wpb = 8;
+    const size_t smem = sizeof(double) * ((size_t)R * R + R);
+    dim3 grid((unsigned)std::min<int64_t>((In + wpb - 1) / wpb, nsm));
+#define CPALS_LEV_STAGED(Q)                                                                           \
+  if (rq <= Q) {                                                                                      \
+    e = set_smem_limit_once((const void*)k_leverage_rows<Q, true>, (int)(sizeof(double) * (128 * 128 + 128))); \
+    if (e != cudaSuccess) return e;                                                                   \
+    k_leverage_rows<Q, true><<<grid, 32 * wpb, smem, st>>>(F, In, R, U, dinv, piv, info, scale, probs); \
+    return cudaGetLastError();                                                                        \
+  }
+    CPALS_LEV_STAGED(1)
+    CPALS_LEV_STAGED(2)
+    CPALS_LEV_STAGED(4)
+#undef CPALS_LEV_STAGED
+  }
   const int wpb = 4;
   dim3 grid((unsigned)((In + wpb - 1) / wpb));
-  const int rq = (R + 31) / 32;
-#define CPALS_LEV_CASE(Q)                                                                          \
-  if (rq <= Q) {                                                                                   \
-    k_leverage_rows<Q><<<grid, 32 * wpb, 0, st>>>(F, In, R, U, dinv, piv, info, scale, probs); \
-    return cudaGetLastError();                                                                     \
+#define CPALS_LEV_CASE(Q)                                                                                \
+  if (rq <= Q) {                                                                                         \
+    k_leverage_rows<Q, false><<<grid, 32 * wpb, 0, st>>>(F, In, R, U, dinv, piv, info, scale, probs); \
+    return cudaGetLastError();                                                                           \
   }
-  CPALS_LEV_CASE(1)
-  CPALS_LEV_CASE(2)
-  CPALS_LEV_CASE(4)
   CPALS_LEV_CASE(8)
   CPALS_LEV_CASE(16)
 #undef CPALS_LEV_CASE

@@ -20,8 +20,11 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
+#include <map>
+#include <mutex>
 
 #include "cpals_internal.cuh"
 
@@ -299,9 +302,10 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
                                                   double* __restrict__ U, double* __restrict__ dinv,
                                                   int* __restrict__ piv, double* __restrict__ W,
                                                   double* __restrict__ qwork, SolveInfo* info, DevCheck* chk,
-                                                  int mixed) {
+                                                  int mixed, int clustered) {
   if (done_flag(chk)) return;
-  if (mixed && info->refine) return;  // the FP32 sweep produced W
+  if (mixed && info->refine) return;     // the FP32 sweep produced W
+  if (clustered && info->swept) return;  // the cluster sweep produced W and U at full rank
   if (threadIdx.x == 0) info->refine = 0;
   extern __shared__ double smA[];
   // an odd leading dimension in shared memory keeps column accesses free of bank conflicts
@@ -499,28 +503,33 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
     info->fallback = (rank < R) ? 1 : 0;
     info->qr_rank = rank;
   }
+  // U in pivoted order, rows 0..rank-1 (the leverage scores use its leading rank x rank
+  // block): U(j,j) = sqrt(d_j), U(j,c) = Uo(j, piv(c)) / sqrt(d_j) for c > j
+  for (int jj = tid; jj < R; jj += blockDim.x) {
+    const double ri = (jj < rank) ? rsqrt(s_dp[jj]) : 0.0;
+    s_a[jj] = ri;
+    dinv[jj] = ri;
+    piv[jj] = s_piv[jj];
+  }
+  __syncthreads();
+  {
+    double* UT = U + (size_t)R * R;
+    for (int e = tid; e < R * R; e += blockDim.x) {
+      const int r = e / R, c = e - r * R;
+      double u = 0.0;
+      if (r < rank && c < rank) {
+        if (c == r) u = s_dp[r] * s_a[r];
+        else if (c > r) u = Uo[(size_t)r * R + s_piv[c]] * s_a[r];
+      }
+      U[e] = u;
+      UT[(size_t)c * R + r] = u;
+    }
+  }
   if (rank == R) {
     // W = -A (symmetric; also W^T)
     for (int e = tid; e < R * R; e += blockDim.x) {
       const int r = e / R, c = e - r * R;
       W[e] = -((r <= c) ? A[r * ld + c] : A[c * ld + r]);
-    }
-    // U in pivoted order: U(j,j) = sqrt(d_j), U(j,c) = Uo(j, piv(c)) / sqrt(d_j) for c > j
-    for (int jj = tid; jj < R; jj += blockDim.x) {
-      const double ri = rsqrt(s_dp[jj]);
-      s_a[jj] = ri;
-      dinv[jj] = ri;
-      piv[jj] = s_piv[jj];
-    }
-    __syncthreads();
-    double* UT = U + (size_t)R * R;
-    for (int e = tid; e < R * R; e += blockDim.x) {
-      const int r = e / R, c = e - r * R;
-      double u = 0.0;
-      if (c == r) u = s_dp[r] * s_a[r];
-      else if (c > r) u = Uo[(size_t)r * R + s_piv[c]] * s_a[r];
-      U[e] = u;
-      UT[(size_t)c * R + r] = u;
     }
   } else {
     if (tid == 0 && chk) atomicAdd(reinterpret_cast<unsigned long long*>(&chk->fallbacks), 1ull);
@@ -532,6 +541,225 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
     double* cn = qwork + 4 * (size_t)R * R + 2 * R;
     __syncthreads();
     qr_fallback(gs, order, skip, R, B, Z, Y, tau, perm, W, info, sv, si, cn);
+  }
+}
+
+// ---------------- FP64 pivoted sweep over a thread-block cluster ----------------
+// The same sweep as k_factorize, with the rows of V dealt round-robin to the C CTAs of one
+// cluster (row i lives in CTA i % C), so that the O(R^3) FP64 FMAs of a factorisation run
+// on C SMs instead of one.  Every operation on every entry is the one k_factorize performs
+// (entry (i, c) takes fma(-a_min(i,c), t_max(i,c), A) and both triangles are stored, so
+// they stay bitwise symmetric), and the pivot search applies the same keys and tie rule:
+// W, U, dinv, piv and the rank come out bit-identical.  One step:
+//   (a) every warp finds the pivot from the cluster-wide table of diagonal keys (each CTA
+//       holds a copy);
+//   (b) the pivot row is read from its owner's shared memory (the matrix is
+//       double-buffered by step parity, so the owner's next update goes to the other
+//       buffer) and kept as the step's row of U, while one thread forms the pivot's
+//       reciprocal (a division is a chain of dependent FP64 operations: it hides under
+//       the remote loads); then the row is scaled;
+//   (c) each CTA updates its rows into the other buffer, several independent entries per
+//       thread, and writes its diagonal keys into every CTA's table for the next step (one
+//       remote store per thread);
+//   (d) one cluster barrier (release / acquire) publishes the rows and the table.
+// On GB300 a step costs about a microsecond: the remote loads of (b), the FP64 FMAs of (c)
+// at 2 per clock per SM, and the barrier.
+// A rank-deficient V (the stopping rule fires before R pivots) leaves info->swept = 0, and
+// the single-CTA k_factorize launched after it redoes the factorisation with its QR
+// fallback; at full rank k_factorize returns at once.
+constexpr int CLT = 256;        // threads per CTA of the cluster sweep
+constexpr int kClMaxRank = 256; // one pivot-row entry per thread in step (b)
+constexpr int kClMinRank = 64;  // below it the single CTA's steps are shorter than a cluster barrier round
+constexpr int kClUnroll = 4;    // independent entries in flight per thread in step (c)
+
+__device__ __forceinline__ unsigned cl_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// address of the same shared-memory location in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned cl_map(const void* p, unsigned rank) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  unsigned out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(a), "r"(rank));
+  return out;
+}
+__device__ __forceinline__ double cl_ld_f64(unsigned addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void cl_st_s64(unsigned addr, long long v) {
+  asm volatile("st.shared::cluster.s64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+// all threads of all CTAs of the cluster; shared-memory writes before it are visible after it
+__device__ __forceinline__ void cl_sync() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__host__ __device__ inline int cl_rows(int R, int C) { return (R + C - 1) / C; }
+__host__ __device__ inline size_t cl_smem_bytes(int R, int C) {
+  const size_t nloc = (size_t)cl_rows(R, C);
+  // A[2][nloc][R], Uo[nloc][R], s_ri[nloc], s_dkey[nloc], keys[2][R], s_a, s_t, s_dp [R], s_dk,
+  // s_piv, s_swept [R]
+  return sizeof(double) * (3 * nloc * R + 2 * nloc + 2 * (size_t)R + 3 * (size_t)R + 1) + sizeof(int) * 2 * (size_t)R;
+}
+
+__global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order, int skip, int R, int C,
+                                                          double* __restrict__ U, double* __restrict__ dinv,
+                                                          int* __restrict__ piv, double* __restrict__ W,
+                                                          SolveInfo* info, const DevCheck* chk) {
+  if (done_flag(chk)) return;  // the same flag for every CTA: the cluster leaves together
+  extern __shared__ __align__(16) double clsm[];
+  const int nloc = cl_rows(R, C);
+  const int nent = nloc * R;
+  const int me = (int)cl_ctarank();
+  const int tid = threadIdx.x, lane = tid & 31;
+  double* A0 = clsm;                       // [2][nloc][R]: row li holds V row me + C li
+  double* Uo = A0 + 2 * (size_t)nent;      // [nloc][R]: pivot rows of steps me + C lr
+  double* s_ri = Uo + (size_t)nent;        // [nloc]
+  long long* s_dkey = reinterpret_cast<long long*>(s_ri + nloc);  // [nloc]: this step's diagonal keys
+  long long* keys = s_dkey + nloc;                                  // [2][R]
+  double* s_a = reinterpret_cast<double*>(keys + 2 * R);
+  double* s_t = s_a + R;
+  double* s_dp = s_t + R;
+  double* s_dk = s_dp + R;
+  int* s_piv = reinterpret_cast<int*>(s_dk + 1);
+  int* s_swept = s_piv + R;
+
+  for (int t = tid; t < R; t += CLT) s_swept[t] = 0;
+  cl_sync();  // every CTA of the cluster is running before the first remote store
+  // V = ones .* G_a .* G_b ... in mode order, each entry from the upper triangle of the Grams
+  for (int e = tid; e < nent; e += CLT) {
+    const int li = e / R, c = e - li * R, i = me + C * li;
+    if (i >= R) continue;
+    const int lo = min(i, c), hi = max(i, c);
+    double v = 1.0;
+    for (int m = 0; m < order; ++m)
+      if (m != skip) v *= gs.G[m][(size_t)lo * R + hi];
+    A0[e] = v;
+    if (c == i)
+      for (int q = 0; q < C; ++q) cl_st_s64(cl_map(&keys[i], (unsigned)q), pivot_key(v));
+  }
+  cl_sync();
+
+  // the thread that divides: one not needed for the row fetch when there is one
+  const int div_tid = (R < CLT) ? R : 0;
+  int rank = R;
+  for (int j = 0; j < R; ++j) {
+    const int cur = j & 1;
+    const double* __restrict__ Ac = A0 + (size_t)cur * nent;
+    double* __restrict__ An = A0 + (size_t)(cur ^ 1) * nent;
+    const long long* kc = keys + cur * R;
+    // (a) pivot: largest key, first index on ties (k_factorize's pick_pivot), in every warp
+    long long bk = LLONG_MIN;
+    int bi = R;
+    for (int i = lane; i < R; i += 32) {
+      const long long key = kc[i];
+      if (bi == R || key > bk) {
+        bk = key;
+        bi = i;
+      }
+    }
+    const int khi = (int)(bk >> 32);
+    const int mhi = __reduce_max_sync(0xffffffffu, khi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
+    const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
+    const int k = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+    if (key_is_nan(mk) || !(mk > pivot_key(kCholTol))) {  // the same decision in every warp of the cluster
+      rank = j;
+      break;
+    }
+    const double pv = __longlong_as_double(mk);
+    // (b) the pivot row from its owner, before this step's update; its reciprocal beside it
+    double a = 0.0;
+    if (tid < R) {
+      a = cl_ld_f64(cl_map(Ac + (size_t)(k / C) * R + tid, (unsigned)(k % C)));
+      s_a[tid] = a;
+      if (j % C == me) Uo[(size_t)(j / C) * R + tid] = (s_swept[tid] || tid == k) ? 0.0 : a;
+      if (tid == k) s_swept[tid] = 1;
+    }
+    if (tid == div_tid) {
+      *s_dk = 1.0 / pv;
+      s_piv[j] = k;
+      s_dp[j] = pv;
+    }
+    __syncthreads();
+    const double dk = *s_dk;
+    if (tid < R) s_t[tid] = a * dk;
+    __syncthreads();
+    // (c) this CTA's rows, into the other buffer
+    long long* kn = keys + (cur ^ 1) * R;
+    for (int e0 = tid; e0 < nent; e0 += kClUnroll * CLT) {
+      double nv[kClUnroll];
+      int ev[kClUnroll];
+#pragma unroll
+      for (int u = 0; u < kClUnroll; ++u) {
+        const int e = e0 + u * CLT;
+        ev[u] = -1;
+        nv[u] = 0.0;
+        if (e < nent) {
+          const int li = e / R, c = e - li * R, i = me + C * li;
+          if (i < R) {
+            ev[u] = e;
+            if (i == k) {
+              nv[u] = (c == k) ? -dk : s_t[c];
+            } else if (c == k) {
+              nv[u] = s_t[i];
+            } else {
+              const int lo = min(i, c), hi = max(i, c);
+              nv[u] = fma(-s_a[lo], s_t[hi], Ac[e]);
+            }
+            if (c == i) s_dkey[li] = s_swept[i] ? LLONG_MIN : pivot_key(nv[u]);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kClUnroll; ++u)
+        if (ev[u] >= 0) An[ev[u]] = nv[u];
+    }
+    __syncthreads();
+    for (int t = tid; t < nloc * C; t += CLT) {
+      const int li = t / C, q = t - li * C, i = me + C * li;
+      if (i < R) cl_st_s64(cl_map(&kn[i], (unsigned)q), s_dkey[li]);
+    }
+    // (d)
+    cl_sync();
+  }
+
+  if (rank == R) {
+    const double* Af = A0 + (size_t)(R & 1) * nent;
+    for (int lr = tid; lr < nloc; lr += CLT) {
+      const int r = me + C * lr;
+      if (r < R) s_ri[lr] = rsqrt(s_dp[r]);
+    }
+    __syncthreads();
+    double* UT = U + (size_t)R * R;
+    for (int e = tid; e < nent; e += CLT) {
+      const int li = e / R, c = e - li * R, i = me + C * li;
+      if (i >= R) continue;
+      W[(size_t)i * R + c] = -Af[e];  // W = -A = V^{-1}
+      // row i of U (pivoted order): U(i,i) = sqrt(d_i), U(i,c) = Uo(i, piv(c)) / sqrt(d_i) for c > i
+      const double ri = s_ri[li];
+      double u = 0.0;
+      if (c == i) u = s_dp[i] * ri;
+      else if (c > i) u = Uo[(size_t)li * R + s_piv[c]] * ri;
+      U[(size_t)i * R + c] = u;
+      UT[(size_t)c * R + i] = u;
+      if (c == 0) {
+        dinv[i] = ri;
+        piv[i] = s_piv[i];
+      }
+    }
+    if (me == 0 && tid == 0) {
+      info->rank = R;
+      info->fallback = 0;
+      info->qr_rank = R;
+      info->refine = 0;
+      info->swept = 1;
+    }
+  } else if (me == 0 && tid == 0) {
+    info->swept = 0;
   }
 }
 
@@ -1903,8 +2131,80 @@ cudaError_t launch_factorize(const GramSet& gs, int order, int skip, int R, doub
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  k_factorize<<<1, FT, smem, st>>>(gs, order, skip, R, Aglob, U, dinv, piv, W, qwork, info, chk, mixed);
+  const int C = mixed ? 0 : cluster_sweep_size(R);
+  if (C > 0) {
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)C);
+    cfg.blockDim = dim3(CLT);
+    cfg.dynamicSmemBytes = cl_smem_bytes(R, C);
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_factorize_cluster, gs, order, skip, R, C, U, dinv, piv, W, info,
+                                       (const DevCheck*)chk);
+    if (e != cudaSuccess) return e;
+  }
+  k_factorize<<<1, FT, smem, st>>>(gs, order, skip, R, Aglob, U, dinv, piv, W, qwork, info, chk, mixed, C > 0);
   return cudaGetLastError();
+}
+
+int factorize_launches(int R, int mixed) {
+  if (mixed && R <= 128) return 3;
+  return cluster_sweep_size(R) > 0 ? 2 : 1;
+}
+
+namespace {
+std::atomic<int> g_cl_min_rank{kClMinRank};
+}
+
+int set_cluster_sweep_min_rank(int r) { return g_cl_min_rank.exchange(r); }
+
+// Cluster size of the FP64 sweep for rank R on the current device: 16 CTAs where the device
+// can place such a cluster with the sweep's shared memory, else 8, else 0 (single CTA).
+int cluster_sweep_size(int R) {
+  if (R < g_cl_min_rank.load() || R > kClMaxRank) return 0;
+  static std::mutex mu;
+  static std::map<int, int> sizes;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = sizes.find(dev);
+  if (it != sizes.end()) return it->second;
+  int best = 0;
+  const size_t smem = cl_smem_bytes(kClMaxRank, 8);
+  if (cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    for (int C : {16, 8}) {
+      cudaLaunchConfig_t cfg{};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)C;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)C);
+      cfg.blockDim = dim3(CLT);
+      cfg.dynamicSmemBytes = cl_smem_bytes(kClMaxRank, C);
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, k_factorize_cluster, &cfg) == cudaSuccess && n > 0) {
+        best = C;
+        break;
+      }
+    }
+  }
+  (void)cudaGetLastError();  // leave no error behind for the next launch check
+  sizes[dev] = best;
+  return best;
 }
 
 static int solve_rows_per_block(int R) { return R >= 256 ? 1 : 256 / R; }

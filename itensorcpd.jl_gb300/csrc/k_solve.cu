@@ -545,32 +545,31 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 }
 
 // ---------------- FP64 pivoted sweep over a thread-block cluster ----------------
-// The same sweep as k_factorize, with the rows of V dealt round-robin to the C CTAs of one
-// cluster (row i lives in CTA i % C), so that the O(R^3) FP64 FMAs of a factorisation run
-// on C SMs instead of one.  Every operation on every entry is the one k_factorize performs
-// (entry (i, c) takes fma(-a_min(i,c), t_max(i,c), A) and both triangles are stored, so
-// they stay bitwise symmetric), and the pivot search applies the same keys and tie rule:
-// W, U, dinv, piv and the rank come out bit-identical.  One step:
-//   (a) every warp finds the pivot from the cluster-wide table of diagonal keys (each CTA
-//       holds a copy);
-//   (b) the pivot row is read from its owner's shared memory (the matrix is
-//       double-buffered by step parity, so the owner's next update goes to the other
-//       buffer) and kept as the step's row of U, while one thread forms the pivot's
-//       reciprocal (a division is a chain of dependent FP64 operations: it hides under
-//       the remote loads); then the row is scaled;
-//   (c) each CTA updates its rows into the other buffer, several independent entries per
-//       thread, and writes its diagonal keys into every CTA's table for the next step (one
-//       remote store per thread);
+// The same sweep as k_factorize, with the rows of V dealt to the C CTAs of one cluster, so
+// that the O(R^3) FP64 FMAs of a factorisation run on C SMs instead of one.  Like
+// k_factorize, only the upper triangle (c >= i) is stored and updated, each entry by the
+// operation k_factorize applies to it, and the pivot search uses the same keys and tie
+// rule: W, U, dinv, piv and the rank come out bit-identical.  Row i belongs to block
+// b = i / C at position i % C, and goes to CTA i % C for even b, C - 1 - i % C for odd b,
+// so that the upper-triangle rows (R - i entries) even out over the CTAs.  One step:
+//   (a) warp 0 finds the pivot in the cluster-wide table of diagonal keys (each CTA holds
+//       a copy);
+//   (b) each thread reads one entry of the pivot row, A(min(t,k), max(t,k)), from the
+//       shared memory of the CTA holding it (the matrix is double-buffered by step
+//       parity, so that CTA's next update goes to the other buffer); the row is kept as
+//       the step's row of U, while one thread forms the pivot's reciprocal (a division is
+//       a chain of dependent FP64 operations: it hides under the remote loads); then the
+//       row is scaled;
+//   (c) each CTA updates its diagonal entries and writes their keys into every CTA's
+//       table for the next step, then updates the rest of its upper-triangle entries into
+//       the other buffer;
 //   (d) one cluster barrier (release / acquire) publishes the rows and the table.
-// On GB300 a step costs about a microsecond: the remote loads of (b), the FP64 FMAs of (c)
-// at 2 per clock per SM, and the barrier.
 // A rank-deficient V (the stopping rule fires before R pivots) leaves info->swept = 0, and
 // the single-CTA k_factorize launched after it redoes the factorisation with its QR
 // fallback; at full rank k_factorize returns at once.
-constexpr int CLT = 256;        // threads per CTA of the cluster sweep
+constexpr int CLT = 512;        // threads per CTA of the cluster sweep
 constexpr int kClMaxRank = 256; // one pivot-row entry per thread in step (b)
 constexpr int kClMinRank = 64;  // below it the single CTA's steps are shorter than a cluster barrier round
-constexpr int kClUnroll = 4;    // independent entries in flight per thread in step (c)
 
 __device__ __forceinline__ unsigned cl_ctarank() {
   unsigned r;
@@ -596,13 +595,26 @@ __device__ __forceinline__ void cl_st_s64(unsigned addr, long long v) {
 __device__ __forceinline__ void cl_sync() {
   asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
+// owner CTA and local row of row i
+__host__ __device__ inline int cl_owner(int i, int C) {
+  const int b = i / C, p = i - b * C;
+  return (b & 1) ? C - 1 - p : p;
+}
+__host__ __device__ inline int cl_row(int li, int me, int C) { return li * C + ((li & 1) ? C - 1 - me : me); }
+
+// -x by flipping the sign bit: the same bits as FP64 negation, without an FP64 instruction
+// (on this part one warp's FP64 instruction holds the SM's FP64 pipe for about 19 cycles)
+__device__ __forceinline__ double neg_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
 
 __host__ __device__ inline int cl_rows(int R, int C) { return (R + C - 1) / C; }
 __host__ __device__ inline size_t cl_smem_bytes(int R, int C) {
   const size_t nloc = (size_t)cl_rows(R, C);
-  // A[2][nloc][R], Uo[nloc][R], s_ri[nloc], s_dkey[nloc], keys[2][R], s_a, s_t, s_dp [R], s_dk,
-  // s_piv, s_swept [R]
-  return sizeof(double) * (3 * nloc * R + 2 * nloc + 2 * (size_t)R + 3 * (size_t)R + 1) + sizeof(int) * 2 * (size_t)R;
+  // A[2][nloc][R], Uo[nloc][R], s_ri[nloc], keys[2][R], s_na, s_t, s_dp [R], s_dk, s_pv |
+  // emap[nloc R], s_piv, s_swept [R], s_k, s_stop
+  return sizeof(double) * (3 * nloc * R + nloc + 2 * (size_t)R + 3 * (size_t)R + 2) +
+         sizeof(int) * (nloc * R + 2 * (size_t)R + 2);
 }
 
 __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order, int skip, int R, int C,
@@ -615,31 +627,50 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
   const int nent = nloc * R;
   const int me = (int)cl_ctarank();
   const int tid = threadIdx.x, lane = tid & 31;
-  double* A0 = clsm;                       // [2][nloc][R]: row li holds V row me + C li
+  double* A0 = clsm;                       // [2][nloc][R]: row li holds V row cl_row(li), c >= that row
   double* Uo = A0 + 2 * (size_t)nent;      // [nloc][R]: pivot rows of steps me + C lr
   double* s_ri = Uo + (size_t)nent;        // [nloc]
-  long long* s_dkey = reinterpret_cast<long long*>(s_ri + nloc);  // [nloc]: this step's diagonal keys
-  long long* keys = s_dkey + nloc;                                  // [2][R]
-  double* s_a = reinterpret_cast<double*>(keys + 2 * R);
-  double* s_t = s_a + R;
+  long long* keys = reinterpret_cast<long long*>(s_ri + nloc);  // [2][R]
+  double* s_na = reinterpret_cast<double*>(keys + 2 * R);  // the pivot row, negated
+  double* s_t = s_na + R;
   double* s_dp = s_t + R;
   double* s_dk = s_dp + R;
-  int* s_piv = reinterpret_cast<int*>(s_dk + 1);
+  double* s_pv = s_dk + 1;
+  int* emap = reinterpret_cast<int*>(s_pv + 1);  // upper-triangle entries of the local rows: li << 16 | c
+  int* s_piv = emap + nent;
   int* s_swept = s_piv + R;
+  int* s_k = s_swept + R;
+  int* s_stop = s_k + 1;
 
+  // the local strictly-upper entries, row by row (row li has R - 1 - cl_row(li) of them); the
+  // diagonal entry of local row li is lane li of warp 0's
+  int nup = 0;
+  for (int li = 0; li < nloc; ++li) {
+    const int i = cl_row(li, me, C);
+    if (i >= R) continue;
+    for (int c = i + 1 + tid; c < R; c += CLT) emap[nup + c - i - 1] = (li << 16) | c;
+    nup += R - 1 - i;
+  }
   for (int t = tid; t < R; t += CLT) s_swept[t] = 0;
   cl_sync();  // every CTA of the cluster is running before the first remote store
-  // V = ones .* G_a .* G_b ... in mode order, each entry from the upper triangle of the Grams
-  for (int e = tid; e < nent; e += CLT) {
-    const int li = e / R, c = e - li * R, i = me + C * li;
-    if (i >= R) continue;
-    const int lo = min(i, c), hi = max(i, c);
+  // V = ones .* G_a .* G_b ... in mode order (upper triangle, as k_factorize forms it)
+  auto form_v = [&](int i, int c) {
     double v = 1.0;
-    for (int m = 0; m < order; ++m)
-      if (m != skip) v *= gs.G[m][(size_t)lo * R + hi];
-    A0[e] = v;
-    if (c == i)
+    for (int q = 0; q < order; ++q)
+      if (q != skip) v *= gs.G[q][(size_t)i * R + c];
+    return v;
+  };
+  for (int f = tid; f < nup; f += CLT) {
+    const int m = emap[f], li = m >> 16, c = m & 0xffff;
+    A0[li * R + c] = form_v(cl_row(li, me, C), c);
+  }
+  if (tid < nloc) {
+    const int i = cl_row(tid, me, C);
+    if (i < R) {
+      const double v = form_v(i, i);
+      A0[tid * R + i] = v;
       for (int q = 0; q < C; ++q) cl_st_s64(cl_map(&keys[i], (unsigned)q), pivot_key(v));
+    }
   }
   cl_sync();
 
@@ -650,32 +681,46 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
     const int cur = j & 1;
     const double* __restrict__ Ac = A0 + (size_t)cur * nent;
     double* __restrict__ An = A0 + (size_t)(cur ^ 1) * nent;
-    const long long* kc = keys + cur * R;
-    // (a) pivot: largest key, first index on ties (k_factorize's pick_pivot), in every warp
-    long long bk = LLONG_MIN;
-    int bi = R;
-    for (int i = lane; i < R; i += 32) {
-      const long long key = kc[i];
-      if (bi == R || key > bk) {
-        bk = key;
-        bi = i;
+    // (a) pivot: largest key, first index on ties (k_factorize's pick_pivot)
+    if (tid < 32) {
+      const long long* kc = keys + cur * R;
+      long long kv[kClMaxRank / 32];
+#pragma unroll
+      for (int q = 0; q < kClMaxRank / 32; ++q) kv[q] = (lane + 32 * q < R) ? kc[lane + 32 * q] : LLONG_MIN;
+      long long bk = LLONG_MIN;
+      int bi = R;
+#pragma unroll
+      for (int q = 0; q < kClMaxRank / 32; ++q) {
+        const int i = lane + 32 * q;
+        if (i < R && (bi == R || kv[q] > bk)) {
+          bk = kv[q];
+          bi = i;
+        }
+      }
+      const int khi = (int)(bk >> 32);
+      const int mhi = __reduce_max_sync(0xffffffffu, khi);
+      const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
+      const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
+      const int k = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
+      if (lane == 0) {
+        *s_k = k;
+        *s_pv = __longlong_as_double(mk);
+        *s_stop = key_is_nan(mk) || !(mk > pivot_key(kCholTol));
       }
     }
-    const int khi = (int)(bk >> 32);
-    const int mhi = __reduce_max_sync(0xffffffffu, khi);
-    const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
-    const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
-    const int k = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
-    if (key_is_nan(mk) || !(mk > pivot_key(kCholTol))) {  // the same decision in every warp of the cluster
+    __syncthreads();
+    if (*s_stop) {  // the same decision in every CTA of the cluster
       rank = j;
       break;
     }
-    const double pv = __longlong_as_double(mk);
-    // (b) the pivot row from its owner, before this step's update; its reciprocal beside it
+    const int k = *s_k;
+    const double pv = *s_pv;
+    // (b) the pivot row, before this step's update; its reciprocal beside it
     double a = 0.0;
     if (tid < R) {
-      a = cl_ld_f64(cl_map(Ac + (size_t)(k / C) * R + tid, (unsigned)(k % C)));
-      s_a[tid] = a;
+      const int lo = min(tid, k), hi = max(tid, k);
+      a = cl_ld_f64(cl_map(Ac + (size_t)(lo / C) * R + hi, (unsigned)cl_owner(lo, C)));
+      s_na[tid] = neg_bits(a);
       if (j % C == me) Uo[(size_t)(j / C) * R + tid] = (s_swept[tid] || tid == k) ? 0.0 : a;
       if (tid == k) s_swept[tid] = 1;
     }
@@ -688,40 +733,29 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
     const double dk = *s_dk;
     if (tid < R) s_t[tid] = a * dk;
     __syncthreads();
-    // (c) this CTA's rows, into the other buffer
-    long long* kn = keys + (cur ^ 1) * R;
-    for (int e0 = tid; e0 < nent; e0 += kClUnroll * CLT) {
-      double nv[kClUnroll];
-      int ev[kClUnroll];
-#pragma unroll
-      for (int u = 0; u < kClUnroll; ++u) {
-        const int e = e0 + u * CLT;
-        ev[u] = -1;
-        nv[u] = 0.0;
-        if (e < nent) {
-          const int li = e / R, c = e - li * R, i = me + C * li;
-          if (i < R) {
-            ev[u] = e;
-            if (i == k) {
-              nv[u] = (c == k) ? -dk : s_t[c];
-            } else if (c == k) {
-              nv[u] = s_t[i];
-            } else {
-              const int lo = min(i, c), hi = max(i, c);
-              nv[u] = fma(-s_a[lo], s_t[hi], Ac[e]);
-            }
-            if (c == i) s_dkey[li] = s_swept[i] ? LLONG_MIN : pivot_key(nv[u]);
-          }
-        }
+    // (c) this CTA's upper-triangle entries, into the other buffer (k_factorize's update).
+    // One warp's FP64 instruction holds its scheduler's FP64 pipe for ~64 cycles whatever
+    // its active lanes, so every entry takes the same single FMA, with the special rows
+    // and columns selected after it: no divergent FP64 code.  The diagonal comes first
+    // (warp 0), so that its keys travel to the other CTAs while the rest is updated.
+    if (tid < nloc) {
+      const int i = cl_row(tid, me, C);
+      if (i < R) {
+        const int e = tid * R + i;
+        const double f = fma(s_na[i], s_t[i], Ac[e]);
+        const double v = (i == k) ? neg_bits(dk) : f;
+        An[e] = v;
+        const long long key = s_swept[i] ? LLONG_MIN : pivot_key(v);
+        long long* kn = keys + (cur ^ 1) * R;
+        for (int q = 0; q < C; ++q) cl_st_s64(cl_map(&kn[i], (unsigned)q), key);
       }
-#pragma unroll
-      for (int u = 0; u < kClUnroll; ++u)
-        if (ev[u] >= 0) An[ev[u]] = nv[u];
     }
-    __syncthreads();
-    for (int t = tid; t < nloc * C; t += CLT) {
-      const int li = t / C, q = t - li * C, i = me + C * li;
-      if (i < R) cl_st_s64(cl_map(&kn[i], (unsigned)q), s_dkey[li]);
+    for (int f0 = tid; f0 < nup; f0 += CLT) {
+      const int m = emap[f0], li = m >> 16, c = m & 0xffff, i = cl_row(li, me, C);
+      const int e = li * R + c;
+      const double tc = s_t[c], ti = s_t[i];
+      const double f = fma(s_na[i], tc, Ac[e]);
+      An[e] = (i == k) ? tc : ((c == k) ? ti : f);  // row and column k take A(i,k) / d
     }
     // (d)
     cl_sync();
@@ -734,21 +768,31 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
       if (r < R) s_ri[lr] = rsqrt(s_dp[r]);
     }
     __syncthreads();
+    // W = -A = V^{-1}, both triangles
+    for (int f = tid; f < nup; f += CLT) {
+      const int m = emap[f], li = m >> 16, c = m & 0xffff, i = cl_row(li, me, C);
+      const double w = -Af[li * R + c];
+      W[(size_t)i * R + c] = w;
+      W[(size_t)c * R + i] = w;
+    }
+    if (tid < nloc) {
+      const int i = cl_row(tid, me, C);
+      if (i < R) W[(size_t)i * R + i] = -Af[tid * R + i];
+    }
+    // rows me + C lr of U (pivoted order): U(r,r) = sqrt(d_r), U(r,c) = Uo(r, piv(c)) / sqrt(d_r) for c > r
     double* UT = U + (size_t)R * R;
     for (int e = tid; e < nent; e += CLT) {
-      const int li = e / R, c = e - li * R, i = me + C * li;
-      if (i >= R) continue;
-      W[(size_t)i * R + c] = -Af[e];  // W = -A = V^{-1}
-      // row i of U (pivoted order): U(i,i) = sqrt(d_i), U(i,c) = Uo(i, piv(c)) / sqrt(d_i) for c > i
-      const double ri = s_ri[li];
+      const int lr = e / R, c = e - lr * R, r = me + C * lr;
+      if (r >= R) continue;
+      const double ri = s_ri[lr];
       double u = 0.0;
-      if (c == i) u = s_dp[i] * ri;
-      else if (c > i) u = Uo[(size_t)li * R + s_piv[c]] * ri;
-      U[(size_t)i * R + c] = u;
-      UT[(size_t)c * R + i] = u;
+      if (c == r) u = s_dp[r] * ri;
+      else if (c > r) u = Uo[(size_t)lr * R + s_piv[c]] * ri;
+      U[(size_t)r * R + c] = u;
+      UT[(size_t)c * R + r] = u;
       if (c == 0) {
-        dinv[i] = ri;
-        piv[i] = s_piv[i];
+        dinv[r] = ri;
+        piv[r] = s_piv[r];
       }
     }
     if (me == 0 && tid == 0) {
@@ -2178,12 +2222,15 @@ int cluster_sweep_size(int R) {
   std::lock_guard<std::mutex> lock(mu);
   auto it = sizes.find(dev);
   if (it != sizes.end()) return it->second;
-  int best = 0;
-  const size_t smem = cl_smem_bytes(kClMaxRank, 8);
-  if (cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-          cudaSuccess &&
+  int best = 0, optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
       cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
     for (int C : {16, 8}) {
+      const size_t smem = cl_smem_bytes(kClMaxRank, C);
+      if (smem > (size_t)optin ||
+          cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+              cudaSuccess)
+        continue;
       cudaLaunchConfig_t cfg{};
       cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeClusterDimension;
@@ -2192,7 +2239,7 @@ int cluster_sweep_size(int R) {
       at[0].val.clusterDim.z = 1;
       cfg.gridDim = dim3((unsigned)C);
       cfg.blockDim = dim3(CLT);
-      cfg.dynamicSmemBytes = cl_smem_bytes(kClMaxRank, C);
+      cfg.dynamicSmemBytes = smem;
       cfg.attrs = at;
       cfg.numAttrs = 1;
       int n = 0;

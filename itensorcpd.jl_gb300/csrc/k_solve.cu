@@ -552,17 +552,17 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // rule: W, U, dinv, piv and the rank come out bit-identical.  Row i belongs to block
 // b = i / C at position i % C, and goes to CTA i % C for even b, C - 1 - i % C for odd b,
 // so that the upper-triangle rows (R - i entries) even out over the CTAs.  One step:
-//   (a) warp 0 finds the pivot in the cluster-wide table of diagonal keys (each CTA holds
-//       a copy);
+//   (a) every warp finds the pivot among the C CTAs' candidates (each CTA's largest
+//       diagonal key and its index, in a table every CTA holds a copy of);
 //   (b) each thread reads one entry of the pivot row, A(min(t,k), max(t,k)), from the
 //       shared memory of the CTA holding it (the matrix is double-buffered by step
 //       parity, so that CTA's next update goes to the other buffer); the row is kept as
 //       the step's row of U, while one thread forms the pivot's reciprocal (a division is
 //       a chain of dependent FP64 operations: it hides under the remote loads); then the
 //       row is scaled;
-//   (c) each CTA updates its diagonal entries and writes their keys into every CTA's
-//       table for the next step, then updates the rest of its upper-triangle entries into
-//       the other buffer;
+//   (c) warp 0 updates the CTA's diagonal entries and writes the CTA's candidate for the
+//       next pivot into every CTA's table, then all threads update the rest of the
+//       CTA's upper-triangle entries into the other buffer;
 //   (d) one cluster barrier (release / acquire) publishes the rows and the table.
 // A rank-deficient V (the stopping rule fires before R pivots) leaves info->swept = 0, and
 // the single-CTA k_factorize launched after it redoes the factorisation with its QR
@@ -595,6 +595,26 @@ __device__ __forceinline__ void cl_st_s64(unsigned addr, long long v) {
 __device__ __forceinline__ void cl_sync() {
   asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
+// largest key over the warp, smallest index among the lanes holding it (LAPACK MAXLOC on the
+// keys); idx = INT_MAX marks a lane with no candidate
+__device__ __forceinline__ void warp_argmax_key(long long key, int idx, long long& mk, int& k) {
+  const int khi = (int)(key >> 32);
+  const int mhi = __reduce_max_sync(0xffffffffu, khi);
+  const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(key & 0xffffffffll) : 0u);
+  mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
+  k = (int)__reduce_min_sync(0xffffffffu, (unsigned)((idx != INT_MAX && key == mk) ? idx : INT_MAX));
+}
+// warp 0: this CTA's best {key, index} into slot `me` of the candidate table in every CTA
+__device__ __forceinline__ void cl_st_pair(unsigned addr, long long a, long long b) {
+  asm volatile("st.shared::cluster.v2.s64 [%0], {%1, %2};" ::"r"(addr), "l"(a), "l"(b) : "memory");
+}
+__device__ __forceinline__ void push_candidate(long long key, int idx, long long* table, int me, int C) {
+  long long mk;
+  int k;
+  warp_argmax_key(key, idx, mk, k);
+  const int lane = threadIdx.x & 31;
+  if (lane < C) cl_st_pair(cl_map(table + 2 * me, (unsigned)lane), mk, (long long)k);
+}
 // owner CTA and local row of row i
 __host__ __device__ inline int cl_owner(int i, int C) {
   const int b = i / C, p = i - b * C;
@@ -611,10 +631,10 @@ __device__ __forceinline__ double neg_bits(double x) {
 __host__ __device__ inline int cl_rows(int R, int C) { return (R + C - 1) / C; }
 __host__ __device__ inline size_t cl_smem_bytes(int R, int C) {
   const size_t nloc = (size_t)cl_rows(R, C);
-  // A[2][nloc][R], Uo[nloc][R], s_ri[nloc], keys[2][R], s_na, s_t, s_dp [R], s_dk, s_pv |
-  // emap[nloc R], s_piv, s_swept [R], s_k, s_stop
-  return sizeof(double) * (3 * nloc * R + nloc + 2 * (size_t)R + 3 * (size_t)R + 2) +
-         sizeof(int) * (nloc * R + 2 * (size_t)R + 2);
+  // A[2][nloc][R], Uo[nloc][R], s_ri[nloc], (pad), cand[2][C][2] (16-byte aligned), s_na, s_t,
+  // s_dp [R], s_dk | emap[nloc R], s_piv, s_swept [R]
+  return sizeof(double) * (3 * nloc * R + nloc + 1 + 4 * (size_t)C + 3 * (size_t)R + 1) +
+         sizeof(int) * (nloc * R + 2 * (size_t)R);
 }
 
 __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order, int skip, int R, int C,
@@ -630,17 +650,14 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
   double* A0 = clsm;                       // [2][nloc][R]: row li holds V row cl_row(li), c >= that row
   double* Uo = A0 + 2 * (size_t)nent;      // [nloc][R]: pivot rows of steps me + C lr
   double* s_ri = Uo + (size_t)nent;        // [nloc]
-  long long* keys = reinterpret_cast<long long*>(s_ri + nloc);  // [2][R]
-  double* s_na = reinterpret_cast<double*>(keys + 2 * R);  // the pivot row, negated
+  long long* cand = reinterpret_cast<long long*>(clsm + ((3 * (size_t)nent + nloc + 1) & ~(size_t)1));  // [2][C][2]
+  double* s_na = reinterpret_cast<double*>(cand + 4 * C);        // the pivot row, negated
   double* s_t = s_na + R;
   double* s_dp = s_t + R;
   double* s_dk = s_dp + R;
-  double* s_pv = s_dk + 1;
-  int* emap = reinterpret_cast<int*>(s_pv + 1);  // upper-triangle entries of the local rows: li << 16 | c
+  int* emap = reinterpret_cast<int*>(s_dk + 1);  // strictly-upper entries of the local rows: li << 16 | c
   int* s_piv = emap + nent;
   int* s_swept = s_piv + R;
-  int* s_k = s_swept + R;
-  int* s_stop = s_k + 1;
 
   // the local strictly-upper entries, row by row (row li has R - 1 - cl_row(li) of them); the
   // diagonal entry of local row li is lane li of warp 0's
@@ -664,13 +681,17 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
     const int m = emap[f], li = m >> 16, c = m & 0xffff;
     A0[li * R + c] = form_v(cl_row(li, me, C), c);
   }
-  if (tid < nloc) {
-    const int i = cl_row(tid, me, C);
-    if (i < R) {
+  if (tid < 32) {
+    long long key = LLONG_MIN;
+    int idx = INT_MAX;
+    const int i = cl_row(lane, me, C);
+    if (lane < nloc && i < R) {
       const double v = form_v(i, i);
-      A0[tid * R + i] = v;
-      for (int q = 0; q < C; ++q) cl_st_s64(cl_map(&keys[i], (unsigned)q), pivot_key(v));
+      A0[lane * R + i] = v;
+      key = pivot_key(v);
+      idx = i;
     }
+    push_candidate(key, idx, cand, me, C);
   }
   cl_sync();
 
@@ -681,40 +702,20 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
     const int cur = j & 1;
     const double* __restrict__ Ac = A0 + (size_t)cur * nent;
     double* __restrict__ An = A0 + (size_t)(cur ^ 1) * nent;
-    // (a) pivot: largest key, first index on ties (k_factorize's pick_pivot)
-    if (tid < 32) {
-      const long long* kc = keys + cur * R;
-      long long kv[kClMaxRank / 32];
-#pragma unroll
-      for (int q = 0; q < kClMaxRank / 32; ++q) kv[q] = (lane + 32 * q < R) ? kc[lane + 32 * q] : LLONG_MIN;
-      long long bk = LLONG_MIN;
-      int bi = R;
-#pragma unroll
-      for (int q = 0; q < kClMaxRank / 32; ++q) {
-        const int i = lane + 32 * q;
-        if (i < R && (bi == R || kv[q] > bk)) {
-          bk = kv[q];
-          bi = i;
-        }
-      }
-      const int khi = (int)(bk >> 32);
-      const int mhi = __reduce_max_sync(0xffffffffu, khi);
-      const unsigned mlo = __reduce_max_sync(0xffffffffu, khi == mhi ? (unsigned)(bk & 0xffffffffll) : 0u);
-      const long long mk = (long long)(((unsigned long long)(unsigned)mhi << 32) | mlo);
-      const int k = __reduce_min_sync(0xffffffffu, (bi < R && bk == mk) ? bi : INT_MAX);
-      if (lane == 0) {
-        *s_k = k;
-        *s_pv = __longlong_as_double(mk);
-        *s_stop = key_is_nan(mk) || !(mk > pivot_key(kCholTol));
-      }
+    // (a) pivot: largest key, first index on ties (k_factorize's pick_pivot), in every warp
+    long long mk;
+    int k;
+    {
+      const long long* cc = cand + cur * 2 * C;
+      const long long key = (lane < C) ? cc[2 * lane] : LLONG_MIN;
+      const int idx = (lane < C) ? (int)cc[2 * lane + 1] : INT_MAX;
+      warp_argmax_key(key, idx, mk, k);
     }
-    __syncthreads();
-    if (*s_stop) {  // the same decision in every CTA of the cluster
+    if (key_is_nan(mk) || !(mk > pivot_key(kCholTol))) {  // the same decision everywhere in the cluster
       rank = j;
       break;
     }
-    const int k = *s_k;
-    const double pv = *s_pv;
+    const double pv = __longlong_as_double(mk);
     // (b) the pivot row, before this step's update; its reciprocal beside it
     double a = 0.0;
     if (tid < R) {
@@ -737,18 +738,23 @@ __global__ void __launch_bounds__(CLT) k_factorize_cluster(GramSet gs, int order
     // One warp's FP64 instruction holds its scheduler's FP64 pipe for ~64 cycles whatever
     // its active lanes, so every entry takes the same single FMA, with the special rows
     // and columns selected after it: no divergent FP64 code.  The diagonal comes first
-    // (warp 0), so that its keys travel to the other CTAs while the rest is updated.
-    if (tid < nloc) {
-      const int i = cl_row(tid, me, C);
-      if (i < R) {
-        const int e = tid * R + i;
+    // (warp 0), so that the CTA's candidate travels to the other CTAs while the rest is
+    // updated.
+    if (tid < 32) {
+      long long key = LLONG_MIN;
+      int idx = INT_MAX;
+      const int i = cl_row(lane, me, C);
+      if (lane < nloc && i < R) {
+        const int e = lane * R + i;
         const double f = fma(s_na[i], s_t[i], Ac[e]);
         const double v = (i == k) ? neg_bits(dk) : f;
         An[e] = v;
-        const long long key = s_swept[i] ? LLONG_MIN : pivot_key(v);
-        long long* kn = keys + (cur ^ 1) * R;
-        for (int q = 0; q < C; ++q) cl_st_s64(cl_map(&kn[i], (unsigned)q), key);
+        if (!s_swept[i]) {
+          key = pivot_key(v);
+          idx = i;
+        }
       }
+      push_candidate(key, idx, cand + (cur ^ 1) * 2 * C, me, C);
     }
     for (int f0 = tid; f0 < nup; f0 += CLT) {
       const int m = emap[f0], li = m >> 16, c = m & 0xffff, i = cl_row(li, me, C);

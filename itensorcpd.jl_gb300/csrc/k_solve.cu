@@ -14,9 +14,9 @@
 //                FitCheck / NoCheck update (fit_check.jl:24-66, no_check.jl:11-19).
 //   normalize  : F_n = X ./ lambda, plus the FP32 column-major copy the tensor-core
 //                MTTKRP reads.
-// FP64 runs at 2 FMA/clk/SM on GB300, so every O(I_n R^2) piece is spread over many
-// CTAs; only the O(R^3) factorisation is a single CTA, and it runs on a side stream
-// concurrently with the MTTKRP of the same mode.
+// FP64 runs at under 2 FMA/clk/SM on GB300, so every O(I_n R^2) piece is spread over many
+// CTAs; the O(R^3) factorisation is a single CTA below rank 64 and a 16-CTA cluster from 64
+// to 256, and it runs on a side stream concurrently with the MTTKRP of the same mode.
 #include <cuda_bf16.h>
 
 #include <algorithm>

@@ -101,65 +101,90 @@ __device__ __forceinline__ void dot2_acc(float& s, float& c, float ah, float al,
   c += (e + r) + fmaf(ah, bl, al * bh);
 }
 
-// part[y][m][n] = sum over k in split y of A(k, m) B(k, n), A(k, m) = A[k lak + m lam] and
-// B(k, n) = B[k lbk + n lbn] (FP32 pairs, or FP32 values with a zero lo); 32 x 32 output tiles
-// (blockIdx.x), splits of kchunk (blockIdx.y); with `upper` only tiles on or above the
-// diagonal.  256 threads, each 2 x 2 outputs; 32-deep K steps staged in shared memory.
+// S (column-major nsamps x R, S(s, r) at s + nsamps r) as FP32 pairs in sample-major order,
+// P[s R + r], through 32 x 32 tiles in shared memory (both sides coalesced)
+__global__ void k_split_pairs_t(const double* __restrict__ S, int64_t nsamps, int R, float2* __restrict__ P) {
+  __shared__ double tile[32][33];
+  const int64_t s0 = (int64_t)blockIdx.x * 32;
+  const int r0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 rows per pass
+  for (int q = ty; q < 32; q += 8) {
+    const int64_t sv = s0 + tx;
+    const int r = r0 + q;
+    tile[q][tx] = (sv < nsamps && r < R) ? S[sv + nsamps * r] : 0.0;
+  }
+  __syncthreads();
+  for (int q = ty; q < 32; q += 8) {
+    const int64_t sv = s0 + q;
+    const int r = r0 + tx;
+    if (sv < nsamps && r < R) {
+      const double v = tile[tx][q];
+      const float h = (float)v;
+      P[sv * R + r] = make_float2(h, (float)(v - (double)h));
+    }
+  }
+}
+
+__device__ __forceinline__ float2 ld_pair(const float* p) { return make_float2(*p, 0.f); }
+__device__ __forceinline__ float2 ld_pair(const float2* p) { return *p; }
+
+// part[y][m][n] = sum over k in split y of A(k, m) B(k, n), A(k, m) = A[k lak + m] and
+// B(k, n) = B[k lbk + n] (FP32 pairs, or FP32 values with a zero lo; m and n contiguous);
+// 32 x 32 output tiles (blockIdx.x), splits of kchunk (blockIdx.y); with `upper` only tiles on
+// or above the diagonal.  64 threads, each a 4 x 4 block of outputs (16 independent Dot2
+// chains, the shared-memory operands read as 16-byte vectors); 32-deep K steps.  Every output
+// takes its terms in k order within its split, one sum per split.
 template <typename TA>
-__global__ void __launch_bounds__(256) k_dot2_atb(const TA* __restrict__ A, int64_t lak, int64_t lam,
-                                                   const float2* __restrict__ B, int64_t lbk, int64_t lbn, int64_t K,
-                                                   int M, int N, int64_t kchunk, int upper, double* __restrict__ part) {
-  __shared__ float Ah[32][33], Al[32][33], Bh[32][33], Bl[32][33];  // [k][m], [k][n]
+__global__ void __launch_bounds__(64) k_dot2_atb(const TA* __restrict__ A, int64_t lak, const float2* __restrict__ B,
+                                                  int64_t lbk, int64_t K, int M, int N, int64_t kchunk, int upper,
+                                                  double* __restrict__ part) {
+  __shared__ __align__(16) float Ah[32][36], Al[32][36], Bh[32][36], Bl[32][36];  // [k][m], [k][n]
   const int tiles_n = (N + 31) / 32;
   const int mb = blockIdx.x / tiles_n, nb = blockIdx.x % tiles_n;
   if (upper && mb > nb) return;  // uniform over the block
   const int64_t k0 = (int64_t)blockIdx.y * kchunk;
   const int64_t k1 = (K < k0 + kchunk) ? K : k0 + kchunk;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  float s[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, c[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
+  float s[4][4], c[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s[i][j] = c[i][j] = 0.f;
   for (int64_t kk = k0; kk < k1; kk += 32) {
-    for (int e = threadIdx.x; e < 1024; e += 256) {
-      // the index that is contiguous in memory runs across consecutive threads
-      int kl, ml;
-      if (lak == 1) {
-        kl = e & 31, ml = e >> 5;
-      } else {
-        ml = e & 31, kl = e >> 5;
-      }
+    // 32 x 32 of each operand: consecutive threads on consecutive m (n)
+#pragma unroll 4
+    for (int e = tid; e < 1024; e += 64) {
+      const int ml = e & 31, kl = e >> 5;
       const int64_t k = kk + kl;
-      const int m = mb * 32 + ml;
-      const float2 a = (k < k1 && m < M) ? pair_of(A[k * lak + (int64_t)m * lam]) : make_float2(0.f, 0.f);
+      const int m = mb * 32 + ml, n = nb * 32 + ml;
+      const float2 a = (k < k1 && m < M) ? ld_pair(A + k * lak + m) : make_float2(0.f, 0.f);
+      const float2 b = (k < k1 && n < N) ? B[k * lbk + n] : make_float2(0.f, 0.f);
       Ah[kl][ml] = a.x;
       Al[kl][ml] = a.y;
-      int kb, nl;
-      if (lbk == 1) {
-        kb = e & 31, nl = e >> 5;
-      } else {
-        nl = e & 31, kb = e >> 5;
-      }
-      const int64_t kq = kk + kb;
-      const int n = nb * 32 + nl;
-      const float2 b = (kq < k1 && n < N) ? B[kq * lbk + (int64_t)n * lbn] : make_float2(0.f, 0.f);
-      Bh[kb][nl] = b.x;
-      Bl[kb][nl] = b.y;
+      Bh[kl][ml] = b.x;
+      Bl[kl][ml] = b.y;
     }
     __syncthreads();
     const int kn = (k1 - kk < 32) ? (int)(k1 - kk) : 32;
     for (int kl = 0; kl < kn; ++kl) {
-      const float a0h = Ah[kl][2 * ty], a0l = Al[kl][2 * ty], a1h = Ah[kl][2 * ty + 1], a1l = Al[kl][2 * ty + 1];
-      const float b0h = Bh[kl][2 * tx], b0l = Bl[kl][2 * tx], b1h = Bh[kl][2 * tx + 1], b1l = Bl[kl][2 * tx + 1];
-      dot2_acc(s[0][0], c[0][0], a0h, a0l, b0h, b0l);
-      dot2_acc(s[0][1], c[0][1], a0h, a0l, b1h, b1l);
-      dot2_acc(s[1][0], c[1][0], a1h, a1l, b0h, b0l);
-      dot2_acc(s[1][1], c[1][1], a1h, a1l, b1h, b1l);
+      const float4 ah = *reinterpret_cast<const float4*>(&Ah[kl][4 * ty]);
+      const float4 al = *reinterpret_cast<const float4*>(&Al[kl][4 * ty]);
+      const float4 bh = *reinterpret_cast<const float4*>(&Bh[kl][4 * tx]);
+      const float4 bl = *reinterpret_cast<const float4*>(&Bl[kl][4 * tx]);
+      const float avh[4] = {ah.x, ah.y, ah.z, ah.w}, avl[4] = {al.x, al.y, al.z, al.w};
+      const float bvh[4] = {bh.x, bh.y, bh.z, bh.w}, bvl[4] = {bl.x, bl.y, bl.z, bl.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dot2_acc(s[i][j], c[i][j], avh[i], avl[i], bvh[j], bvl[j]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int m = mb * 32 + 2 * ty + i, n = nb * 32 + 2 * tx + j;
+    for (int j = 0; j < 4; ++j) {
+      const int m = mb * 32 + 4 * ty + i, n = nb * 32 + 4 * tx + j;
       if (m < M && n < N) part[((size_t)blockIdx.y * M + m) * N + n] = (double)s[i][j] + (double)c[i][j];
     }
 }
@@ -276,19 +301,21 @@ cudaError_t launch_colmajor_to_rowmajor(const double* src, int64_t rows, int R, 
   return cudaGetLastError();
 }
 
-// Splits of the sampled products' K range (the samples): about 512 samples each, at least one.
-int sampled_splits(int64_t nsamps) { return (int)std::max<int64_t>(1, std::min<int64_t>(64, (nsamps + 511) / 512)); }
+// Splits of the sampled products' K range (the samples): about 128 samples each, at least one,
+// so that the 64-thread tiles of k_dot2_atb keep ~16 warps on each SM at R = 128.
+int sampled_splits(int64_t nsamps) { return (int)std::max<int64_t>(1, std::min<int64_t>(256, (nsamps + 127) / 128)); }
 
 cudaError_t launch_sampled_gram(const double* Scol, int64_t nsamps, int R, float2* Spair, double* part, double* G,
                                 cudaStream_t st) {
-  const int64_t n = nsamps * R;
-  k_split_pairs<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(Scol, n, Spair);
+  if (nsamps > (int64_t)INT_MAX * 32) return cudaErrorInvalidValue;
+  k_split_pairs_t<<<dim3((unsigned)((nsamps + 31) / 32), (unsigned)((R + 31) / 32)), 256, 0, st>>>(Scol, nsamps, R,
+                                                                                                  Spair);
   const int sp = sampled_splits(nsamps);
   const int64_t kchunk = (nsamps + sp - 1) / sp;
   const int tiles = ((R + 31) / 32) * ((R + 31) / 32);
-  // S^T S: A = B = S, S(s, r) at s + nsamps r (column-major)
-  k_dot2_atb<float2><<<dim3((unsigned)tiles, (unsigned)sp), 256, 0, st>>>(Spair, 1, nsamps, Spair, 1, nsamps, nsamps, R,
-                                                                          R, kchunk, 1, part);
+  // S^T S: A = B = S, S(s, r) at s R + r (the sample-major pairs)
+  k_dot2_atb<float2><<<dim3((unsigned)tiles, (unsigned)sp), 64, 0, st>>>(Spair, R, Spair, R, nsamps, R, R, kchunk, 1,
+                                                                         part);
   k_reduce_gram_splits<<<(R * R + 255) / 256, 256, 0, st>>>(part, sp, R, G);
   return cudaGetLastError();
 }
@@ -299,17 +326,16 @@ cudaError_t launch_sampled_rhs(const void* Ts, int tdtype, int64_t In, int64_t n
   const int64_t kchunk = (nsamps + sp - 1) / sp;
   const int tiles = (int)(((In + 31) / 32) * ((R + 31) / 32));
   if (In > INT_MAX) return cudaErrorInvalidValue;
-  // T_s S: A = T_s (i, s) at i + In s, B = S
+  // T_s S: A = T_s (i, s) at i + In s, B = S (sample-major pairs)
   if (tdtype == CPALS_DTYPE_F64) {
     const int64_t n = In * nsamps;
     k_split_pairs<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(static_cast<const double*>(Ts), n,
                                                                                   Tpair);
-    k_dot2_atb<float2><<<dim3((unsigned)tiles, (unsigned)sp), 256, 0, st>>>(Tpair, In, 1, Spair, 1, nsamps, nsamps,
-                                                                            (int)In, R, kchunk, 0, part);
+    k_dot2_atb<float2><<<dim3((unsigned)tiles, (unsigned)sp), 64, 0, st>>>(Tpair, In, Spair, R, nsamps, (int)In, R,
+                                                                           kchunk, 0, part);
   } else {
-    k_dot2_atb<float><<<dim3((unsigned)tiles, (unsigned)sp), 256, 0, st>>>(static_cast<const float*>(Ts), In, 1, Spair,
-                                                                           1, nsamps, nsamps, (int)In, R, kchunk, 0,
-                                                                           part);
+    k_dot2_atb<float><<<dim3((unsigned)tiles, (unsigned)sp), 64, 0, st>>>(static_cast<const float*>(Ts), In, Spair, R,
+                                                                          nsamps, (int)In, R, kchunk, 0, part);
   }
   *splits_out = sp;
   return cudaGetLastError();

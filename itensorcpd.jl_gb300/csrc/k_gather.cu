@@ -246,6 +246,10 @@ __global__ void k_leverage_rows(const double* __restrict__ F, int64_t In, int R,
       const double* Uk = Us + (size_t)k * R;
 #pragma unroll
       for (int q = 0; q < RQ; ++q) {
+        // blocks of 32 below the pivot's hold no j > k: a warp-uniform skip, so that no FP64
+        // instruction issues for them (a warp's FP64 instruction holds its scheduler's FP64
+        // pipe for ~64 cycles whatever its active lanes)
+        if (q < qk) continue;
         const int j = lane + 32 * q;
         if (j == k) t[q] = c;
         else if (j > k && j < rank) t[q] = fma(-c, Uk[j], t[q]);
@@ -350,7 +354,7 @@ cudaError_t launch_leverage_rows(const double* F, int64_t In, int R, const doubl
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    const int wpb = 8;
+    const int wpb = 4;  // one row per scheduler: the substitution's FP64 chain owns its pipe
     const size_t smem = sizeof(double) * ((size_t)R * R + R);
     dim3 grid((unsigned)std::min<int64_t>((In + wpb - 1) / wpb, nsm));
 #define CPALS_LEV_STAGED(Q)                                                                           \

@@ -67,7 +67,7 @@ def same(a, b):
 
 
 # R = 240 on 16 CTAs puts all fifteen diagonal entries of a CTA's rows in one thread
-@pytest.mark.parametrize("dims,R", [((80, 70, 66), 64), ((130, 120, 9), 100), ((140, 131, 130), 128),
+@pytest.mark.parametrize("dims,R", [((60, 50, 45), 40), ((80, 70, 66), 64), ((130, 120, 9), 100), ((140, 131, 130), 128),
                                     ((210, 205, 8, 3), 200), ((250, 245, 6, 4), 240), ((260, 257, 7, 5), 256)])
 def test_cluster_sweep_is_bit_identical(built, dims, R):
     with cluster_min_rank(1):

@@ -15,7 +15,7 @@
 //   normalize  : F_n = X ./ lambda, plus the FP32 column-major copy the tensor-core
 //                MTTKRP reads.
 // FP64 runs at under 2 FMA/clk/SM on GB300, so every O(I_n R^2) piece is spread over many
-// CTAs; the O(R^3) factorisation is a single CTA below rank 64 and a 16-CTA cluster from 64
+// CTAs; the O(R^3) factorisation is a single CTA below rank 40 and a 16-CTA cluster from 40
 // to 256, and it runs on a side stream concurrently with the MTTKRP of the same mode.
 #include <cuda_bf16.h>
 
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(FT) k_factorize(GramSet gs, int order, int ski
 // fallback; at full rank k_factorize returns at once.
 constexpr int CLT = 512;        // threads per CTA of the cluster sweep
 constexpr int kClMaxRank = 256; // one pivot-row entry per thread in step (b)
-constexpr int kClMinRank = 64;  // below it the single CTA's steps are shorter than a cluster barrier round
+constexpr int kClMinRank = 40;  // below it the single CTA's steps are shorter than a cluster round trip
 
 __device__ __forceinline__ unsigned cl_ctarank() {
   unsigned r;

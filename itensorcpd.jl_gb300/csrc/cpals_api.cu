@@ -580,6 +580,12 @@ int cpals_create(cpals_ctx** out, int device, int order, const int64_t* dims, in
   c->maxI = maxI;
   for (int m = 0; m < order; ++m) c->dims[m] = dims[m];
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  {
+    // the cluster sweep's device query (function attributes, occupancy) runs here, never
+    // inside the capture of a sweep graph
+    DeviceGuard g(device);
+    (void)cluster_sweep_device_size();
+  }
   int rc = CPALS_OK;
 #define CK(x)                \
   do {                       \

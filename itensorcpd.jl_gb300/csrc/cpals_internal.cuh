@@ -184,6 +184,7 @@ size_t factorize_work_doubles(int R);
 // CTA); the smallest rank given to the cluster sweep (process-wide, returns the previous)
 int factorize_launches(int R, int mixed);
 int cluster_sweep_size(int R);
+int cluster_sweep_device_size();  // the current device's cluster size, whatever the rank
 int set_cluster_sweep_min_rank(int r);
 
 // Reduce the MTTKRP partials, solve X = M V^{-1} one warp per row, write X and

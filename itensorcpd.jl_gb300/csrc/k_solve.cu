@@ -2218,6 +2218,10 @@ int set_cluster_sweep_min_rank(int r) { return g_cl_min_rank.exchange(r); }
 // can place such a cluster with the sweep's shared memory, else 8, else 0 (single CTA).
 int cluster_sweep_size(int R) {
   if (R < g_cl_min_rank.load() || R > kClMaxRank) return 0;
+  return cluster_sweep_device_size();
+}
+
+int cluster_sweep_device_size() {
   static std::mutex mu;
   static std::map<int, int> sizes;
   int dev = 0;

@@ -2215,7 +2215,8 @@ std::atomic<int> g_cl_min_rank{kClMinRank};
 int set_cluster_sweep_min_rank(int r) { return g_cl_min_rank.exchange(r); }
 
 // Cluster size of the FP64 sweep for rank R on the current device: 16 CTAs where the device
-// can place such a cluster with the sweep's shared memory, else 8, else 0 (single CTA).
+// can place such a cluster with the sweep's shared memory (a non-portable size, which GB300
+// supports), else 0 (single CTA).
 int cluster_sweep_size(int R) {
   if (R < g_cl_min_rank.load() || R > kClMaxRank) return 0;
   return cluster_sweep_device_size();
@@ -2235,7 +2236,7 @@ int cluster_sweep_device_size() {
   int best = 0, optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
       cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
-    for (int C : {16, 8}) {
+    for (int C : {16}) {
       const size_t smem = cl_smem_bytes(kClMaxRank, C);
       if (smem > (size_t)optin ||
           cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=

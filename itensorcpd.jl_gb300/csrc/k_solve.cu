@@ -588,9 +588,6 @@ __device__ __forceinline__ double cl_ld_f64(unsigned addr) {
   asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
   return v;
 }
-__device__ __forceinline__ void cl_st_s64(unsigned addr, long long v) {
-  asm volatile("st.shared::cluster.s64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
-}
 // all threads of all CTAs of the cluster; shared-memory writes before it are visible after it
 __device__ __forceinline__ void cl_sync() {
   asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
@@ -2236,12 +2233,11 @@ int cluster_sweep_device_size() {
   int best = 0, optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
       cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
-    for (int C : {16}) {
-      const size_t smem = cl_smem_bytes(kClMaxRank, C);
-      if (smem > (size_t)optin ||
-          cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-              cudaSuccess)
-        continue;
+    const int C = 16;
+    const size_t smem = cl_smem_bytes(kClMaxRank, C);
+    if (smem <= (size_t)optin &&
+        cudaFuncSetAttribute(k_factorize_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+            cudaSuccess) {
       cudaLaunchConfig_t cfg{};
       cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeClusterDimension;
@@ -2254,10 +2250,7 @@ int cluster_sweep_device_size() {
       cfg.attrs = at;
       cfg.numAttrs = 1;
       int n = 0;
-      if (cudaOccupancyMaxActiveClusters(&n, k_factorize_cluster, &cfg) == cudaSuccess && n > 0) {
-        best = C;
-        break;
-      }
+      if (cudaOccupancyMaxActiveClusters(&n, k_factorize_cluster, &cfg) == cudaSuccess && n > 0) best = C;
     }
   }
   (void)cudaGetLastError();  // leave no error behind for the next launch check

@@ -159,6 +159,14 @@ def test_leverage_scores(oracle):
     assert np.allclose(p, np.sum(Q * Q, axis=1) / 7)
 
 
+def test_leverage_scores_wide_factor(oracle):
+    # I < R: the thin QR's Q is square and orthogonal, every row scores 1 / I (the device takes
+    # them from the leading rank x rank block of the pivoted Cholesky factor, rank = I)
+    F, _ = det_factors((40, 90, 80), 70, seed=5)
+    p = oracle.leverage_score_probabilities(F[0])
+    assert np.allclose(p, 1.0 / 40, rtol=0, atol=1e-14)
+
+
 def test_golden_fixtures_reproduce(oracle, golden_dir):
     small = json.loads((golden_dir / "als_small.json").read_text())
     T = np.asfortranarray(det_normal(small["tensor_seed"], small["dims"]))
